@@ -1,0 +1,395 @@
+"""Benchmark of the MSBG hot path on GB300.
+
+Workload (default): the 4096^3 surface reconstruction -- 1,024 seeded ellipsoid
+clusters x 32,000 points, base block 32^3, three resolution levels by distance
+to the points (level 0 within 8 voxels, level 1 within 16), FP16 storage with
+FP32 arithmetic, 8-color in-place mean-curvature-flow sweeps (laplTyp 4).
+
+* ``value``: voxel-updates/s of one step = applyChannelPdeFast with 50 MCF
+  iterations over every level-0 voxel, field resident in HBM.  The field
+  (~9.4 GB) is far larger than L2, so no flush is needed between steps.
+* ``e2e``: the same metric through the public entry point msbg_gpu_surface_job
+  with host buffers: pinned host points in, layout + splat + finalize + 50
+  sweeps on the device, the level-0 payload back to pinned host memory.
+* ``roofline``: the sweep kernel's algorithmic bytes (read + write of every
+  updated voxel, 2 x 2 B) per launch over its average launch time, against the
+  measured HBM copy bandwidth in MEASURED_PEAKS.json.
+* ``cpu_baseline``: the CPU restatement (oracle/msbg_oracle.c, OpenMP) on a
+  bounded sample of the same workload.
+
+``--impl reference`` times the reference's CPU implementation of the path on
+the host cores instead: the reference library built from its sources where it
+compiles (x86-64), else the CPU restatement of it (aarch64 hosts).
+Multi-GPU: the path does not shard here ("replicas only"); N ranks each run the
+full workload and ``value`` is the sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import platform
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from msbg_gb300 import gpu as G  # noqa: E402
+from msbg_gb300 import workloads as W  # noqa: E402
+
+OPT8 = 1 << 29
+MCF8 = -(4 + OPT8)
+
+
+# ------------------------------------------------------------------------------------
+# helpers
+# ------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int = 0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.gpu)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> tuple[dict, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.isfile(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class Dist:
+    """torch.distributed only for barrier / max over ranks when WORLD_SIZE > 1."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.dist = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            torch.cuda.set_device(self.local)
+            dist.init_process_group("gloo")
+            self.dist = dist
+            self.torch = torch
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.dist:
+            return v
+        t = self.torch.tensor([v], dtype=self.torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------------------------
+# CPU baseline: the oracle on a bounded sample of the workload
+# ------------------------------------------------------------------------------------
+def cpu_sample(spec: dict, pts: np.ndarray, target_sec: float = 10.0, max_blocks: int = 0):
+    """MCF sweeps of the CPU restatement on a crop of the level-0 blocks.
+
+    Returns (updates/s, sample description, threads).  The crop is the first
+    ``n`` level-0 blocks in bid order (a contiguous slab of the volume) with the
+    rest of the grid empty; sweeps run with the same 8-color schedule and FP16
+    storage as the GPU."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import port as P  # test/bench infrastructure only: the timed CPU baseline
+    res, bsx = spec["res"], spec["bsx"]
+    storage = {"f16": P.F16, "f32": P.F32}[spec["storage"]]
+    g = P.grid(res, res, res, bsx, storage)
+    nb = g.nbx * g.nby * g.nbz
+    cnt, valid, nv = P.mark_blocks(g, pts, 0.0)
+    lv = np.zeros(nb, np.int32)
+    if "fine_band" in spec:
+        rb = np.array([spec["fine_band"], spec["mid_band"]], np.float32)
+        P.lib().orc_band_levels(C.byref(g), P._p(pts), len(pts), P._p(valid), P._p(rb), 2, 3, P._p(lv))
+    else:
+        cnt, valid, nv = P.mark_blocks(g, pts, 4.0)
+        lv = np.where(cnt > 0, 0, 2).astype(np.int32)
+    lv, _ = P.regularize(lv, g.nbx, g.nby, g.nbz, 3)
+    act = np.nonzero(lv == 0)[0]
+    n_take = max_blocks or min(len(act), 2048)
+    keep = np.full(nb, 2, np.int32)
+    keep[act[:n_take]] = 0
+    slot = np.empty(nb, np.int32)
+    bids = np.empty(nb, np.int32)
+    n_act = P.lib().orc_build_slots(P._p(keep), nb, P._p(slot), P._p(bids))
+    bids = bids[:n_act].copy()
+    vox = n_act * bsx ** 3
+    rng = np.random.Generator(np.random.PCG64(7))
+    field = rng.random(vox).astype(np.float32)
+    payload = field.astype(np.float16).view(np.uint16) if storage == P.F16 else field
+    # one iteration first to size the sample to ~target_sec
+    t0 = time.perf_counter()
+    P.pde(g, slot, bids, payload, MCF8, 1, 2, 0.1)
+    t2 = time.perf_counter() - t0
+    per_iter = t2 / 2
+    n_iter = max(2, int(target_sec / max(per_iter, 1e-6)) // 2 * 2)
+    t0 = time.perf_counter()
+    P.pde(g, slot, bids, payload, MCF8, 1, n_iter, 0.1)
+    dt = time.perf_counter() - t0
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    desc = (f"{n_iter} MCF 8-color iterations of the CPU restatement over {n_act} level-0 "
+            f"blocks ({vox / 1e6:.1f} M voxels, {spec['storage']}) cropped from the workload")
+    return vox * n_iter / dt, desc, threads
+
+
+# ------------------------------------------------------------------------------------
+# reference arm
+# ------------------------------------------------------------------------------------
+def run_reference(args, spec, dist: Dist):
+    if dist.rank != 0:
+        return
+    pts = W.make_points(spec, 2 if spec is W.SURFACE_4096 else 1)
+    arch = platform.machine()
+    ref_driver = os.path.join(ROOT, "oracle", "_ref", "msbg_ref_driver")
+    kind = "port"
+    vals = []
+    desc = ""
+    threads = os.cpu_count() or 1
+    if arch in ("x86_64", "AMD64") and os.path.isfile(ref_driver):
+        # the reference library itself on a cropped sample (its MCF sweep timing)
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_io as O
+        kind = "reference"
+        res = 1024 if spec["res"] > 1024 else spec["res"]
+        sub = pts[(pts < res - 1).all(axis=1)]
+        for _ in range(args.warmup + args.steps):
+            job = O.SurfaceJob(res, res, res, spec["bsx"], sub, chan=O.CHAN_U16, n_iter=4, dt=0.1,
+                               n_threads=threads)
+            r = O.run_reference_surface(job)
+            vals.append(r.n_active * spec["bsx"] ** 3 * 4 / r.times["pde"])
+        vals = vals[args.warmup:]
+        desc = (f"reference applyChannelPdeFast<uint16> MCF, 4 iterations over the level-0 blocks of "
+                f"the workload's points inside a {res}^3 crop")
+    else:
+        for i in range(args.warmup + args.steps):
+            v, desc, threads = cpu_sample(spec, pts, target_sec=8.0)
+            vals.append(v)
+        vals = vals[args.warmup:]
+        desc = "reference CPU path unavailable on this host (x86 SIMD); " + desc
+    value = float(np.median(vals))
+    line = {
+        "impl": "reference", "metric": "voxel-updates/s (MCF sweeps)", "value": value,
+        "unit": "voxel-updates/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": spec["name"]},
+        "cpu_baseline": {"value": value, "unit": "voxel-updates/s", "cores": threads, "kind": kind,
+                         "sample": desc},
+        "e2e": {"value": value, "unit": "voxel-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------------
+# GB300 arm
+# ------------------------------------------------------------------------------------
+def run_gpu(args, spec, dist: Dist):
+    storage = {"f16": G.F16, "f32": G.F32}[spec["storage"]]
+    elem = 2 if storage == G.F16 else 4
+    variant = G.SWEEP_FAST if args.variant == "fast" else G.SWEEP_EXACT
+    n_iter = spec["n_iter"]
+    pts = W.make_points(spec, 2 if spec is W.SURFACE_4096 else 1)
+    bands = (spec["fine_band"], spec["mid_band"]) if "fine_band" in spec else None
+    res, bsx = spec["res"], spec["bsx"]
+
+    g = G.MultiresSparseGrid(res, res, res, bsx, spec["n_levels"], storage)
+    d = g.to_device(pts)
+    n = len(pts)
+    if bands:
+        g.levels_from_bands(d, n, bands)
+    else:
+        g.mark_points(d, n, 4.0)
+        g.levels_from_marks()
+    g.regularizeRefinementMap()
+    g.setRefinementMap(1.0)
+    g.splat(d, n, 2.0, 2.0)
+    g.splat_finalize(2.0, 2.0)
+    g.synchronize()
+    info = g.info()
+    n_act = info.nActive
+    vox = n_act * bsx ** 3
+    updates_per_step = vox * (n_iter + (n_iter & 1))
+
+    for _ in range(args.warmup):
+        g.applyChannelPdeFast(0, MCF8, 1, n_iter, spec["dt"], 0.0, variant)
+    g.synchronize()
+    dist.barrier()
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    l0 = g.launch_count()
+    g.event_record(0)
+    for _ in range(args.steps):
+        g.applyChannelPdeFast(0, MCF8, 1, n_iter, spec["dt"], 0.0, variant)
+    g.event_record(1)
+    g.synchronize()
+    ms = g.event_elapsed_ms(0, 1)
+    launches = g.launch_count() - l0
+    clk = clocks.stop()
+    dist.barrier()
+    ms_max = dist.max(ms)
+    value = updates_per_step * args.steps * dist.world / (ms_max / 1e3)
+
+    # roofline of the sweep kernel: every launch of the timed region is a color pass
+    peaks, peak_kind = measured_peaks()
+    bytes_per_update = 2 * elem
+    per_launch_bytes = updates_per_step * bytes_per_update / (launches / args.steps)
+    per_launch_s = (ms / 1e3) / launches
+    achieved = per_launch_bytes / per_launch_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": args.traffic_per_launch,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"}
+
+    # e2e through the host-buffer entry point
+    e2e = None
+    if not args.no_e2e:
+        hp = C.c_void_p()
+        G.load_library().msbg_gpu_host_alloc(C.byref(hp), pts.nbytes)
+        hpts = np.ctypeslib.as_array(C.cast(hp, C.POINTER(C.c_float)), shape=(pts.size,))
+        hpts[:] = pts.ravel()
+        out_bytes = vox * elem
+        ho = C.c_void_p()
+        G.load_library().msbg_gpu_host_alloc(C.byref(ho), out_bytes)
+        times = []
+        e2e_steps = max(1, min(args.steps, 3))
+        b = np.asarray(bands, np.float32) if bands else None
+        n_act_out = C.c_int64()
+        for i in range(1 + e2e_steps):
+            dist.barrier()
+            t0 = time.perf_counter()
+            rc = g.L.msbg_gpu_surface_job(g.h, hp, n, 2.0, 2.0, G._ptr(b), 0 if b is None else len(b),
+                                          MCF8, n_iter, spec["dt"], variant, ho, out_bytes,
+                                          C.byref(n_act_out))
+            dt_s = time.perf_counter() - t0
+            g._check(rc)
+            if i > 0:
+                times.append(dt_s)
+        t_e2e = dist.max(float(np.median(times)))
+        e2e = {"value": updates_per_step * dist.world / t_e2e, "unit": "voxel-updates/s",
+               "h2d_bytes_per_step": int(pts.nbytes), "d2h_bytes_per_step": int(out_bytes),
+               "seconds_per_step": t_e2e}
+        G.load_library().msbg_gpu_host_free(hp)
+        G.load_library().msbg_gpu_host_free(ho)
+
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        v, desc, threads = cpu_sample(spec, pts, target_sec=args.cpu_seconds)
+        cpu = {"value": v, "unit": "voxel-updates/s", "cores": threads, "kind": "port",
+               "sample": desc}
+
+    d.free()
+    g.close()
+    if dist.rank != 0:
+        return
+    line = {
+        "metric": "voxel-updates/s (MCF sweeps)", "value": value, "unit": "voxel-updates/s",
+        "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f16 storage / f32 math" if storage == G.F16 else "f32",
+        "data": "synthetic",
+        "config": {"workload": spec["name"], "points": int(n), "level0_blocks": int(n_act),
+                   "blocks_per_level": [int(x) for x in info.blocksPerLevel[:3]],
+                   "voxel_updates_per_step": int(updates_per_step), "mcf_iterations": n_iter,
+                   "sweep_variant": args.variant, "l2": "inputs larger than L2 (no flush)",
+                   "parallelism": f"replicas x{dist.world}"},
+        "gpu_launches": int(launches),
+        "roofline": roofline,
+        "clocks": clk,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="surface4096", choices=["surface4096", "surface512"])
+    ap.add_argument("--variant", default="fast", choices=["fast", "exact"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--traffic-per-launch", type=float, default=None,
+                    help="DRAM bytes per sweep launch from an ncu capture (reported as roofline.traffic)")
+    args = ap.parse_args()
+    spec = W.SURFACE_4096 if args.workload == "surface4096" else W.SURFACE_512
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, spec, dist)
+        else:
+            run_gpu(args, spec, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

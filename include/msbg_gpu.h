@@ -1,0 +1,197 @@
+/*
+ * msbg_gpu.h -- C ABI of the GB300 (sm_103a) implementation of the MSBG
+ * (Multiresolution Sparse Block Grids, tum-pbs/MSBG) data-parallel hot path.
+ *
+ * The reference exposes this path as C++ methods of MSBG::MultiresSparseGrid
+ * and SBG::SparseGrid<T> (src/msbg.h, src/sbg.h).  Each entry point below
+ * names the reference interface it replaces.  All functions:
+ *   - return 0 (MSBG_GPU_OK) or a negative MSBG_GPU_ERR_* code; the last error
+ *     message of a context is available from msbg_gpu_last_error();
+ *   - launch on the context's stream (msbg_gpu_set_stream) and are
+ *     asynchronous unless stated otherwise; pointers named d* are device
+ *     pointers, h* host pointers;
+ *   - take plain C types only.
+ * A context is not thread-safe (like the reference, whose per-thread scratch is
+ * indexed by TBB thread id, src/halo.cpp:72-92); use one context per host thread.
+ *
+ * Data layout on the device:
+ *   block id     bid = bx + by*nbx + bz*nbx*nby          (src/sbg.h:1744-1749)
+ *   voxel index  vid = x + y*bs + z*bs*bs inside a block (src/sbg.h:1816-1820)
+ *   slot[bid]    payload index of a level-0 ("value") block, or -1 for the
+ *                shared constant empty block              (src/sbg.h:2042-2047)
+ *   payload      one slab per channel: [nActive][bs^3] elements of the
+ *                channel's storage type, slots in ascending bid order.
+ */
+#ifndef MSBG_GPU_H
+#define MSBG_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MSBG_GPU_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------------- */
+enum {
+  MSBG_GPU_OK = 0,
+  MSBG_GPU_ERR_ARG = -1,         /* invalid argument (size, pointer, option)     */
+  MSBG_GPU_ERR_CUDA = -2,        /* a CUDA runtime call failed                  */
+  MSBG_GPU_ERR_NOMEM = -3,       /* device or pinned host allocation failed     */
+  MSBG_GPU_ERR_STATE = -4,       /* call out of order (e.g. no layout yet)      */
+  MSBG_GPU_ERR_CAPACITY = -5,    /* block pool exhausted                        */
+  MSBG_GPU_ERR_NONFINITE = -6,   /* a reduction met NaN/Inf (src/msbg.cpp:4635) */
+  MSBG_GPU_ERR_DIVERGED = -7,    /* solver residual non-finite or increasing    */
+  MSBG_GPU_ERR_UNSUPPORTED = -8  /* option the GPU path does not implement      */
+};
+
+/* ---- storage types of a channel ------------------------------------------ */
+enum {
+  MSBG_GPU_F32 = 0, /* float                                                   */
+  MSBG_GPU_U16 = 1, /* uint16 density, v/65535 (src/sbg.h:225-351)              */
+  MSBG_GPU_F16 = 2, /* IEEE half, FP32 arithmetic                              */
+  MSBG_GPU_F64 = 3  /* double (the FP64 check path)                            */
+};
+
+/* ---- applyChannelPdeFast laplTyp values (src/msbg.h:132-141) -------------- */
+#define MSBG_GPU_OPT_8_COLOR_SCHEME (1 << 29)
+#define MSBG_GPU_PDE_MEAN_CURVATURE 4
+
+/* ---- block flags (same bits as src/msbg.h:561-573) ------------------------ */
+#define MSBG_GPU_BLK_DOM_BORDER (1 << 1)
+#define MSBG_GPU_BLK_COARSE_FINE (1 << 2)
+#define MSBG_GPU_BLK_FINE_COARSE (1 << 3)
+#define MSBG_GPU_BLK_EXISTS (1 << 12)
+#define MSBG_GPU_BLK_UNIFORM_EMPTY (1 << 13)
+
+/* ---- sweep kernel variants ------------------------------------------------- */
+enum {
+  MSBG_GPU_SWEEP_EXACT = 0, /* reference expression order, every float op
+                               individually rounded: bit-identical to the CPU
+                               restatement                                       */
+  MSBG_GPU_SWEEP_FAST = 1   /* same PDE, re-associated with fused multiply-adds;
+                               agrees within rel-L2 1e-5                          */
+};
+
+typedef struct msbg_gpu_ctx msbg_gpu_ctx;
+
+typedef struct {
+  int32_t sx, sy, sz;       /* finest-level voxels                          */
+  int32_t bsx;              /* finest-level block edge                      */
+  int32_t nbx, nby, nbz;    /* blocks per axis                              */
+  int32_t nLevels;          /* resolution levels                            */
+  int64_t nBlocks;          /* nbx*nby*nbz                                  */
+  int64_t nActive;          /* level-0 (value) blocks after the last layout */
+  int64_t capacityBlocks;   /* block-pool capacity (value blocks)           */
+  int64_t blocksPerLevel[8];
+  int32_t colorCount[8];    /* value blocks per 8-color class               */
+  int64_t nActParticles;    /* points that passed the domain checks         */
+  int64_t nAborted;         /* particles abandoned at a non-value block     */
+} msbg_gpu_info;
+
+/* ---- lifecycle --------------------------------------------------------------
+ * Replaces MultiresSparseGrid::create / destroy (src/msbg.h:834-852).
+ * Creates the block index for an sx*sy*sz grid with base block bsx (a power of
+ * two, 8..32, dividing each side) and nLevels resolution levels (block size
+ * halves per level, src/msbg.cpp:808-811).  Channel 0 (the density channel of
+ * the demo, CH_UINT16_1 / CH_FLOAT_1) is created with storage `storage`.
+ * capacityBlocks bounds the value blocks of the block pool (0 = all blocks). */
+int msbg_gpu_create(msbg_gpu_ctx **ctx, int sx, int sy, int sz, int bsx, int nLevels,
+                    int storage, int64_t capacityBlocks);
+int msbg_gpu_destroy(msbg_gpu_ctx *ctx);
+const char *msbg_gpu_last_error(const msbg_gpu_ctx *ctx);
+int msbg_gpu_set_stream(msbg_gpu_ctx *ctx, void *cudaStream);
+int msbg_gpu_get_info(msbg_gpu_ctx *ctx, msbg_gpu_info *info); /* synchronizes */
+int msbg_gpu_synchronize(msbg_gpu_ctx *ctx);
+
+/* Creates another payload channel over the same block layout (reference:
+ * MultiresSparseGrid channels by id, src/msbg.h:274-343, src/msbgaux.cpp:26-96). */
+int msbg_gpu_channel_create(msbg_gpu_ctx *ctx, int chan, int storage);
+
+/* ---- layout ----------------------------------------------------------------
+ * Active-block marking of the demo (src/msbg_demo.cpp:339-397): every block of
+ * each in-domain point's rScan box is marked; dPts is float xyz[n] on the device. */
+int msbg_gpu_mark_points(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rScan);
+/* Level map from the marks: marked -> 0, else nLevels-1 (src/msbg_demo.cpp:413-425). */
+int msbg_gpu_levels_from_marks(msbg_gpu_ctx *ctx);
+/* Distance-band level map: level l for blocks in the rBand[l] box of a point,
+ * nLevels-1 elsewhere (nBands <= nLevels-1). */
+int msbg_gpu_levels_from_bands(msbg_gpu_ctx *ctx, const float *dPts, int64_t n,
+                               const float *hBands, int nBands);
+/* Caller-supplied level map, int32 per block, host memory. */
+int msbg_gpu_set_levels(msbg_gpu_ctx *ctx, const int32_t *hLevels);
+/* regularizeRefinementMap (src/msbg.h:897-901, src/msbg.cpp:1202-1423). */
+int msbg_gpu_regularize_refinement_map(msbg_gpu_ctx *ctx);
+/* setRefinementMap for levelMg 0 (src/msbg.h:903-908, src/msbg.cpp:1428-2165) plus
+ * the demo's allocation loop (src/msbg_demo.cpp:455-511): BlockInfo flags,
+ * value blocks for level 0 in ascending bid order, 8-color lists, every
+ * channel's payload filled with fillValue. */
+int msbg_gpu_set_refinement_map(msbg_gpu_ctx *ctx, double fillValue);
+/* Read back the layout (synchronize): levels int8[nBlocks], flags uint16[nBlocks],
+ * active block ids int32[nActive], slots int32[nBlocks]. */
+int msbg_gpu_get_levels(msbg_gpu_ctx *ctx, int8_t *hLevels);
+int msbg_gpu_get_flags(msbg_gpu_ctx *ctx, uint16_t *hFlags);
+int msbg_gpu_get_active_blocks(msbg_gpu_ctx *ctx, int32_t *hBids, int64_t cap, int64_t *n);
+int msbg_gpu_get_slots(msbg_gpu_ctx *ctx, int32_t *hSlots);
+
+/* ---- channel data ------------------------------------------------------------
+ * Payload of all value blocks, [nActive][bs^3] of the channel's storage type
+ * (SparseGrid::getBlockDataPtr for every block of the active list). */
+int msbg_gpu_upload_payload(msbg_gpu_ctx *ctx, int chan, const void *hData);
+int msbg_gpu_download_payload(msbg_gpu_ctx *ctx, int chan, void *hData);
+/* Device pointer of a channel's payload slab (valid until the next layout). */
+int msbg_gpu_payload_ptr(msbg_gpu_ctx *ctx, int chan, void **dPtr);
+int msbg_gpu_fill(msbg_gpu_ctx *ctx, int chan, double value);
+
+/* ---- splat --------------------------------------------------------------------
+ * Splat of min(distSq/distSqMax) into channel 0 (src/msbg_demo.cpp:527-636):
+ * a particle is abandoned at its first (z,y,x scan order) in-sphere voxel that
+ * lies in a non-value block, as the demo does.  Min is order-independent, so
+ * one launch replaces the demo's 8 color passes.  Then the distance-to-density
+ * finalize (src/msbg_demo.cpp:655-680). */
+int msbg_gpu_splat(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rParticle,
+                   float nbDist);
+int msbg_gpu_splat_finalize(msbg_gpu_ctx *ctx, float rParticle, float nbDist);
+
+/* ---- stencil sweeps -------------------------------------------------------------
+ * applyChannelPdeFast<T> (src/msbg.h:2150-2172, src/msbg4.cpp:60-957) over all
+ * value blocks of channel `chan`: laplTyp < 0 updates in place with 8 colors
+ * (with MSBG_GPU_OPT_8_COLOR_SCHEME) or red-black, laplTyp > 0 ping-pongs with a
+ * temporary slab.  Kernels 4 (mean curvature), 17 (Jacobi diffusion),
+ * 15/14 (Perona-Malik, anisAlpha > 0), 3 (simple diffusion), 1 (Laplacian).
+ * numIter is rounded up to even, as the reference does.  Halo: OPT_BC_NEUMANN. */
+int msbg_gpu_apply_channel_pde_fast(msbg_gpu_ctx *ctx, int chan, int laplTyp, int doConstrZeroOne,
+                                    int numIter, float timeStep, float anisDiffAlpha,
+                                    int variant);
+
+/* ---- whole surface job with host buffers (end-to-end entry point) --------------
+ * Upload n points (host, float xyz), build the layout (marks with rScan =
+ * rParticle + nbDist, or distance bands when nBands > 0), splat, finalize,
+ * numIter sweeps of laplTyp, and download channel 0's payload into hOut
+ * (capacity hOutCap bytes).  *nActiveOut receives the value-block count. */
+int msbg_gpu_surface_job(msbg_gpu_ctx *ctx, const float *hPts, int64_t n, float rParticle,
+                         float nbDist, const float *hBands, int nBands, int laplTyp, int numIter,
+                         float timeStep, int variant, void *hOut, size_t hOutCap,
+                         int64_t *nActiveOut);
+
+/* ---- timing and accounting -------------------------------------------------------
+ * CUDA events on the context's stream (slot 0..15); elapsed in milliseconds. */
+int msbg_gpu_event_record(msbg_gpu_ctx *ctx, int slot);
+int msbg_gpu_event_elapsed(msbg_gpu_ctx *ctx, int slotA, int slotB, float *ms);
+/* Kernels this context has launched since creation. */
+int64_t msbg_gpu_launch_count(const msbg_gpu_ctx *ctx);
+/* Pinned host memory for staging (cudaMallocHost / cudaFreeHost). */
+int msbg_gpu_host_alloc(void **hPtr, size_t bytes);
+int msbg_gpu_host_free(void *hPtr);
+/* Device memory helpers for callers without a CUDA runtime of their own. */
+int msbg_gpu_device_alloc(void **dPtr, size_t bytes);
+int msbg_gpu_device_free(void *dPtr);
+int msbg_gpu_copy_h2d(msbg_gpu_ctx *ctx, void *dDst, const void *hSrc, size_t bytes);
+int msbg_gpu_copy_d2h(msbg_gpu_ctx *ctx, void *hDst, const void *dSrc, size_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MSBG_GPU_H */

@@ -1,0 +1,343 @@
+"""Python host side of the msbg_gpu C ABI (include/msbg_gpu.h), through ctypes.
+
+``MultiresSparseGrid`` mirrors the method names and argument meaning of the
+reference's MSBG::MultiresSparseGrid for the hot path (src/msbg.h:828-3797):
+``create``, ``regularizeRefinementMap``, ``setRefinementMap``,
+``applyChannelPdeFast`` ... so that tests and tools read like code written
+against the reference.  Every call goes to the CUDA library; there is no CPU
+fallback: loading fails loudly when ``libmsbg_gpu.so`` is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libmsbg_gpu.so")
+
+OK = 0
+ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_CAPACITY, ERR_NONFINITE, ERR_DIVERGED, ERR_UNSUPPORTED = \
+    -1, -2, -3, -4, -5, -6, -7, -8
+
+F32, U16, F16, F64 = 0, 1, 2, 3
+NP_STORAGE = {F32: np.float32, U16: np.uint16, F16: np.float16, F64: np.float64}
+
+OPT_8_COLOR_SCHEME = 1 << 29
+PDE_MEAN_CURVATURE = 4
+LAPL_MCF_8COLOR = -(PDE_MEAN_CURVATURE + OPT_8_COLOR_SCHEME)
+SWEEP_EXACT, SWEEP_FAST = 0, 1
+
+BLK_DOM_BORDER, BLK_COARSE_FINE, BLK_FINE_COARSE = 1 << 1, 1 << 2, 1 << 3
+BLK_EXISTS, BLK_UNIFORM_EMPTY = 1 << 12, 1 << 13
+
+# Every function the header declares, with its ctypes signature.
+P, I, I64, F, D, SZ = C.c_void_p, C.c_int, C.c_int64, C.c_float, C.c_double, C.c_size_t
+SIGNATURES = {
+    "msbg_gpu_create": (I, [C.POINTER(P), I, I, I, I, I, I, I64]),
+    "msbg_gpu_destroy": (I, [P]),
+    "msbg_gpu_last_error": (C.c_char_p, [P]),
+    "msbg_gpu_set_stream": (I, [P, P]),
+    "msbg_gpu_get_info": (I, [P, P]),
+    "msbg_gpu_synchronize": (I, [P]),
+    "msbg_gpu_channel_create": (I, [P, I, I]),
+    "msbg_gpu_mark_points": (I, [P, P, I64, F]),
+    "msbg_gpu_levels_from_marks": (I, [P]),
+    "msbg_gpu_levels_from_bands": (I, [P, P, I64, P, I]),
+    "msbg_gpu_set_levels": (I, [P, P]),
+    "msbg_gpu_regularize_refinement_map": (I, [P]),
+    "msbg_gpu_set_refinement_map": (I, [P, D]),
+    "msbg_gpu_get_levels": (I, [P, P]),
+    "msbg_gpu_get_flags": (I, [P, P]),
+    "msbg_gpu_get_active_blocks": (I, [P, P, I64, C.POINTER(I64)]),
+    "msbg_gpu_get_slots": (I, [P, P]),
+    "msbg_gpu_upload_payload": (I, [P, I, P]),
+    "msbg_gpu_download_payload": (I, [P, I, P]),
+    "msbg_gpu_payload_ptr": (I, [P, I, C.POINTER(P)]),
+    "msbg_gpu_fill": (I, [P, I, D]),
+    "msbg_gpu_splat": (I, [P, P, I64, F, F]),
+    "msbg_gpu_splat_finalize": (I, [P, F, F]),
+    "msbg_gpu_apply_channel_pde_fast": (I, [P, I, I, I, I, F, F, I]),
+    "msbg_gpu_surface_job": (I, [P, P, I64, F, F, P, I, I, I, F, I, P, SZ, C.POINTER(I64)]),
+    "msbg_gpu_event_record": (I, [P, I]),
+    "msbg_gpu_event_elapsed": (I, [P, I, I, C.POINTER(F)]),
+    "msbg_gpu_launch_count": (I64, [P]),
+    "msbg_gpu_host_alloc": (I, [C.POINTER(P), SZ]),
+    "msbg_gpu_host_free": (I, [P]),
+    "msbg_gpu_device_alloc": (I, [C.POINTER(P), SZ]),
+    "msbg_gpu_device_free": (I, [P]),
+    "msbg_gpu_copy_h2d": (I, [P, P, P, SZ]),
+    "msbg_gpu_copy_d2h": (I, [P, P, P, SZ]),
+}
+
+_lib = None
+
+
+class Info(C.Structure):
+    _fields_ = [("sx", C.c_int32), ("sy", C.c_int32), ("sz", C.c_int32), ("bsx", C.c_int32),
+                ("nbx", C.c_int32), ("nby", C.c_int32), ("nbz", C.c_int32), ("nLevels", C.c_int32),
+                ("nBlocks", C.c_int64), ("nActive", C.c_int64), ("capacityBlocks", C.c_int64),
+                ("blocksPerLevel", C.c_int64 * 8), ("colorCount", C.c_int32 * 8),
+                ("nActParticles", C.c_int64), ("nAborted", C.c_int64)]
+
+
+class MsbgGpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"msbg_gpu error {code}: {msg}")
+        self.code = code
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Load libmsbg_gpu.so and bind every ABI function (raises if it is missing)."""
+    global _lib
+    if _lib is not None and path == LIB_PATH:
+        return _lib
+    if not os.path.isfile(path):
+        raise OSError(f"{path} not found: run `python -m msbg_gb300.build` (the GPU path has no fallback)")
+    L = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path == LIB_PATH:
+        _lib = L
+    return L
+
+
+def _ptr(a) -> C.c_void_p | None:
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data_as(C.c_void_p)
+    return C.c_void_p(int(a))
+
+
+@dataclass
+class DeviceBuffer:
+    """Raw device allocation owned by Python (freed on close/GC)."""
+    ptr: int
+    nbytes: int
+
+    def free(self):
+        if self.ptr:
+            load_library().msbg_gpu_device_free(C.c_void_p(self.ptr))
+            self.ptr = 0
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class MultiresSparseGrid:
+    """GPU MultiresSparseGrid over one context of the C ABI."""
+
+    def __init__(self, sx: int, sy: int, sz: int, bsx: int, n_levels: int = 3, storage: int = F32,
+                 capacity_blocks: int = 0):
+        self.L = load_library()
+        h = C.c_void_p()
+        rc = self.L.msbg_gpu_create(C.byref(h), sx, sy, sz, bsx, n_levels, storage, capacity_blocks)
+        if rc != OK:
+            raise MsbgGpuError(rc, "msbg_gpu_create failed")
+        self.h = h
+        self.sx, self.sy, self.sz, self.bsx, self.n_levels = sx, sy, sz, bsx, n_levels
+        self.nbx, self.nby, self.nbz = sx // bsx, sy // bsx, sz // bsx
+        self.n_blocks = self.nbx * self.nby * self.nbz
+        self.storage = {0: storage}
+
+    # reference: MultiresSparseGrid::create (src/msbg.h:834-852)
+    @classmethod
+    def create(cls, name: str, sx: int, sy: int, sz: int, blockSize0: int, nLevels: int = 3,
+               storage: int = F32, capacity_blocks: int = 0) -> "MultiresSparseGrid":
+        return cls(sx, sy, sz, blockSize0, nLevels, storage, capacity_blocks)
+
+    def _check(self, rc: int):
+        if rc != OK:
+            raise MsbgGpuError(rc, self.L.msbg_gpu_last_error(self.h).decode(errors="replace"))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.msbg_gpu_destroy(self.h)
+            self.h = None
+
+    destroy = close
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- info ---------------------------------------------------------------------
+    def info(self) -> Info:
+        inf = Info()
+        self._check(self.L.msbg_gpu_get_info(self.h, C.byref(inf)))
+        return inf
+
+    def nBlocks(self) -> int:
+        return self.n_blocks
+
+    def set_stream(self, stream_handle: int):
+        self._check(self.L.msbg_gpu_set_stream(self.h, C.c_void_p(stream_handle)))
+
+    def synchronize(self):
+        self._check(self.L.msbg_gpu_synchronize(self.h))
+
+    def launch_count(self) -> int:
+        return int(self.L.msbg_gpu_launch_count(self.h))
+
+    # ---- device memory --------------------------------------------------------------
+    def to_device(self, a: np.ndarray) -> DeviceBuffer:
+        a = np.ascontiguousarray(a)
+        p = C.c_void_p()
+        if self.L.msbg_gpu_device_alloc(C.byref(p), max(a.nbytes, 1)) != OK:
+            raise MsbgGpuError(ERR_NOMEM, "device alloc")
+        buf = DeviceBuffer(p.value, a.nbytes)
+        if a.nbytes:
+            self._check(self.L.msbg_gpu_copy_h2d(self.h, C.c_void_p(buf.ptr), _ptr(a), a.nbytes))
+        self.synchronize()
+        return buf
+
+    # ---- layout -----------------------------------------------------------------------
+    def channel_create(self, chan: int, storage: int):
+        self._check(self.L.msbg_gpu_channel_create(self.h, chan, storage))
+        self.storage[chan] = storage
+
+    def mark_points(self, d_pts: DeviceBuffer, n: int, r_scan: float):
+        self._check(self.L.msbg_gpu_mark_points(self.h, C.c_void_p(d_pts.ptr), n, r_scan))
+
+    def levels_from_marks(self):
+        self._check(self.L.msbg_gpu_levels_from_marks(self.h))
+
+    def levels_from_bands(self, d_pts: DeviceBuffer, n: int, bands):
+        b = np.ascontiguousarray(bands, np.float32)
+        self._check(self.L.msbg_gpu_levels_from_bands(self.h, C.c_void_p(d_pts.ptr), n, _ptr(b), len(b)))
+
+    def set_levels(self, levels: np.ndarray):
+        lv = np.ascontiguousarray(levels, np.int32)
+        self._check(self.L.msbg_gpu_set_levels(self.h, _ptr(lv)))
+
+    # reference: regularizeRefinementMap (src/msbg.h:897-901)
+    def regularizeRefinementMap(self):
+        self._check(self.L.msbg_gpu_regularize_refinement_map(self.h))
+
+    # reference: setRefinementMap (src/msbg.h:903-908) + the demo's allocation loop
+    def setRefinementMap(self, fill_value: float = 1.0):
+        self._check(self.L.msbg_gpu_set_refinement_map(self.h, fill_value))
+
+    def levels(self) -> np.ndarray:
+        out = np.empty(self.n_blocks, np.int8)
+        self._check(self.L.msbg_gpu_get_levels(self.h, _ptr(out)))
+        return out
+
+    def flags(self) -> np.ndarray:
+        out = np.empty(self.n_blocks, np.uint16)
+        self._check(self.L.msbg_gpu_get_flags(self.h, _ptr(out)))
+        return out
+
+    def active_blocks(self) -> np.ndarray:
+        n = C.c_int64()
+        self._check(self.L.msbg_gpu_get_active_blocks(self.h, None, 0, C.byref(n)))
+        out = np.empty(n.value, np.int32)
+        self._check(self.L.msbg_gpu_get_active_blocks(self.h, _ptr(out), n.value, C.byref(n)))
+        return out
+
+    def slots(self) -> np.ndarray:
+        out = np.empty(self.n_blocks, np.int32)
+        self._check(self.L.msbg_gpu_get_slots(self.h, _ptr(out)))
+        return out
+
+    # ---- data ---------------------------------------------------------------------------
+    def payload(self, chan: int = 0) -> np.ndarray:
+        n = self.info().nActive
+        out = np.empty((n, self.bsx ** 3), NP_STORAGE[self.storage[chan]])
+        self._check(self.L.msbg_gpu_download_payload(self.h, chan, _ptr(out)))
+        return out
+
+    def upload_payload(self, data: np.ndarray, chan: int = 0):
+        a = np.ascontiguousarray(data, NP_STORAGE[self.storage[chan]])
+        self._check(self.L.msbg_gpu_upload_payload(self.h, chan, _ptr(a)))
+        self.synchronize()
+
+    def payload_ptr(self, chan: int = 0) -> int:
+        p = C.c_void_p()
+        self._check(self.L.msbg_gpu_payload_ptr(self.h, chan, C.byref(p)))
+        return p.value or 0
+
+    def fill(self, value: float, chan: int = 0):
+        self._check(self.L.msbg_gpu_fill(self.h, chan, value))
+
+    def splat(self, d_pts: DeviceBuffer, n: int, r_particle: float = 2.0, nb_dist: float = 2.0):
+        self._check(self.L.msbg_gpu_splat(self.h, C.c_void_p(d_pts.ptr), n, r_particle, nb_dist))
+
+    def splat_finalize(self, r_particle: float = 2.0, nb_dist: float = 2.0):
+        self._check(self.L.msbg_gpu_splat_finalize(self.h, r_particle, nb_dist))
+
+    # reference: applyChannelPdeFast<T> (src/msbg.h:2150-2172); the reference's
+    # (chPhi, laplTyp, doConstrZeroOne, numIter, timeStep, anisDiffAlpha) subset
+    def applyChannelPdeFast(self, chPhi: int, laplTyp: int, doConstrZeroOne: int, numIter: int,
+                            timeStep: float, anisDiffAlpha: float = 0.0, variant: int = SWEEP_EXACT):
+        self._check(self.L.msbg_gpu_apply_channel_pde_fast(self.h, chPhi, laplTyp, doConstrZeroOne,
+                                                           numIter, timeStep, anisDiffAlpha, variant))
+
+    def surface_job(self, pts: np.ndarray, r_particle=2.0, nb_dist=2.0, bands=None,
+                    laplTyp=LAPL_MCF_8COLOR, numIter=20, timeStep=0.1, variant=SWEEP_EXACT,
+                    out: np.ndarray | None = None):
+        """Whole pipeline from host points to the host payload (the e2e entry point)."""
+        pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 3)
+        b = None if bands is None else np.ascontiguousarray(bands, np.float32)
+        n_act = C.c_int64()
+        cap = 0 if out is None else out.nbytes
+        self._check(self.L.msbg_gpu_surface_job(
+            self.h, _ptr(pts), len(pts), r_particle, nb_dist, _ptr(b), 0 if b is None else len(b),
+            laplTyp, numIter, timeStep, variant, _ptr(out), cap, C.byref(n_act)))
+        return n_act.value
+
+    # ---- timing -------------------------------------------------------------------------
+    def event_record(self, slot: int):
+        self._check(self.L.msbg_gpu_event_record(self.h, slot))
+
+    def event_elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_float()
+        self._check(self.L.msbg_gpu_event_elapsed(self.h, a, b, C.byref(ms)))
+        return ms.value
+
+
+def surface_pipeline(pts: np.ndarray, res, bsx: int, storage: int = F32, n_iter: int = 20,
+                     lapl_typ: int = LAPL_MCF_8COLOR, dt: float = 0.1, r_particle: float = 2.0,
+                     nb_dist: float = 2.0, n_levels: int = 3, bands=None, variant: int = SWEEP_EXACT,
+                     keep_after_finalize: bool = True):
+    """Step-by-step GPU pipeline (same stages as the reference demo); returns a dict."""
+    sx, sy, sz = (res, res, res) if np.isscalar(res) else res
+    pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 3)
+    g = MultiresSparseGrid(sx, sy, sz, bsx, n_levels, storage)
+    try:
+        d = g.to_device(pts)
+        if bands is None:
+            g.mark_points(d, len(pts), r_particle + nb_dist)
+            g.levels_from_marks()
+        else:
+            g.levels_from_bands(d, len(pts), bands)
+        g.regularizeRefinementMap()
+        g.setRefinementMap(1.0)
+        g.splat(d, len(pts), r_particle, nb_dist)
+        g.splat_finalize(r_particle, nb_dist)
+        after_final = g.payload(0) if keep_after_finalize else None
+        if n_iter > 0:
+            g.applyChannelPdeFast(0, lapl_typ, 1, n_iter, dt, 0.0, variant)
+        out = dict(levels=g.levels(), flags=g.flags(), active_bids=g.active_blocks(),
+                   after_finalize=after_final, after_pde=g.payload(0), info=g.info(),
+                   launches=g.launch_count())
+        d.free()
+        return out
+    finally:
+        g.close()

@@ -1,0 +1,652 @@
+/*
+ * CPU restatement of the MSBG hot path -- test infrastructure only (the checker
+ * for the GPU library, never linked into it).  See msbg_oracle.h for the data
+ * layout.  Built with -ffp-contract=off so float expressions round exactly as
+ * written; the GPU library's parity kernels use the same expression order with
+ * explicitly rounded operations, so FP32 results compare bit for bit.
+ *
+ * Parity of this restatement with the reference itself is pinned by the tests,
+ * which run the reference library compiled from its own sources (oracle/_ref)
+ * on the same seeded inputs.
+ */
+#include "msbg_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* conversions                                                               */
+/* ------------------------------------------------------------------------ */
+
+/* IEEE binary16 round-to-nearest-even conversion (bit manipulation). */
+uint16_t orc_f32_to_f16(float f) {
+  uint32_t x;
+  memcpy(&x, &f, 4);
+  uint32_t sign = (x >> 16) & 0x8000u;
+  uint32_t absx = x & 0x7fffffffu;
+  if (absx >= 0x7f800000u) { /* inf or nan */
+    return (uint16_t)(sign | 0x7c00u | (absx > 0x7f800000u ? 0x200u : 0u));
+  }
+  if (absx >= 0x477ff000u) return (uint16_t)(sign | 0x7c00u); /* rounds to inf */
+  if (absx < 0x38800000u) {                                   /* subnormal or zero */
+    if (absx < 0x33000000u) return (uint16_t)sign;             /* < 2^-25: rounds to 0 */
+    uint32_t e = absx >> 23;
+    uint32_t m = (absx & 0x7fffffu) | 0x800000u;
+    uint32_t shift = 126u - e; /* 14..24 */
+    uint32_t q = m >> shift;
+    uint32_t rem = m & ((1u << shift) - 1u);
+    uint32_t half = 1u << (shift - 1u);
+    if (rem > half || (rem == half && (q & 1u))) q++;
+    return (uint16_t)(sign | q);
+  }
+  uint32_t e = (absx >> 23) - 112u;
+  uint32_t m = absx & 0x7fffffu;
+  uint32_t q = (e << 10) | (m >> 13);
+  uint32_t rem = m & 0x1fffu;
+  if (rem > 0x1000u || (rem == 0x1000u && (q & 1u))) q++;
+  return (uint16_t)(sign | q);
+}
+
+float orc_f16_to_f32(uint16_t h) {
+  uint32_t sign = ((uint32_t)h & 0x8000u) << 16;
+  uint32_t e = ((uint32_t)h >> 10) & 0x1fu;
+  uint32_t m = (uint32_t)h & 0x3ffu;
+  uint32_t x;
+  if (e == 0) {
+    if (m == 0) {
+      x = sign;
+    } else { /* subnormal */
+      float v = (float)m * (1.0f / 16777216.0f);
+      memcpy(&x, &v, 4);
+      x |= sign;
+    }
+  } else if (e == 31) {
+    x = sign | 0x7f800000u | (m << 13);
+  } else {
+    x = sign | ((e + 112u) << 23) | (m << 13);
+  }
+  float f;
+  memcpy(&f, &x, 4);
+  return f;
+}
+
+/* uint16 density: load v*(1/65535) (src/sbg.h:225-247); stores either
+ * round-half-even (the SIMD sweep store, src/sbg.h:343-351) or round-half-away
+ * (the scalar store used by splat/finalize, src/sbg.h:271-296). */
+static const float kU16ToF = 1.0f / 65535.0f;
+static inline uint16_t u16_rne(float f) { return (uint16_t)nearbyintf(f * 65535.0f); }
+static inline uint16_t u16_rha(float f) { return (uint16_t)roundf(f * 65535.0f); }
+
+static inline double load_val(const orc_grid *g, const void *p, int64_t i) {
+  switch (g->storage) {
+    case ORC_F32: return ((const float *)p)[i];
+    case ORC_U16: return (float)((const uint16_t *)p)[i] * kU16ToF;
+    case ORC_F16: return orc_f16_to_f32(((const uint16_t *)p)[i]);
+    default: return ((const double *)p)[i];
+  }
+}
+
+static inline size_t elem_bytes(int storage) {
+  return storage == ORC_F32 ? 4 : storage == ORC_F64 ? 8 : 2;
+}
+
+void orc_grid_init(orc_grid *g, int sx, int sy, int sz, int bsx, int storage) {
+  g->sx = sx; g->sy = sy; g->sz = sz; g->bsx = bsx;
+  g->nbx = sx / bsx; g->nby = sy / bsx; g->nbz = sz / bsx;
+  g->storage = storage;
+  g->emptyValue = 0.0;
+}
+
+static inline int ilog2(int v) { int l = 0; while ((1 << l) < v) l++; return l; }
+static inline int imin(int a, int b) { return a < b ? a : b; }
+static inline int imax(int a, int b) { return a > b ? a : b; }
+
+/* Domain limits of MultiresSparseGrid::isInDomainRange: (0,s) shrunk by 0.005 and
+ * snapped to the 24-bit particle quantisation grid (src/sbg.cpp:262-316,
+ * src/msbgcell.h:74, src/msbgcell.h:138). */
+static float quant24(float x) {
+  double scale = ((1 << 24) - 1) * (1.0 / 32768.0);
+  return (float)((int32_t)floor(scale * x + 0.5) / scale);
+}
+
+static inline int point_valid(const orc_grid *g, float px, float py, float pz, float *dmin,
+                              float *dmax) {
+  if (px < dmin[0] || px > dmax[0] || py < dmin[1] || py > dmax[1] || pz < dmin[2] ||
+      pz > dmax[2])
+    return 0;
+  int ix = (int)px, iy = (int)py, iz = (int)pz;
+  return ix >= 0 && ix < g->sx && iy >= 0 && iy < g->sy && iz >= 0 && iz < g->sz;
+}
+
+static void domain_limits(const orc_grid *g, float *dmin, float *dmax) {
+  const float beps = 0.005f;
+  dmin[0] = quant24(0.0f + beps); dmax[0] = quant24((float)g->sx - beps);
+  dmin[1] = quant24(0.0f + beps); dmax[1] = quant24((float)g->sy - beps);
+  dmin[2] = quant24(0.0f + beps); dmax[2] = quant24((float)g->sz - beps);
+}
+
+/* ------------------------------------------------------------------------ */
+/* marking / bucketing / levels                                              */
+/* ------------------------------------------------------------------------ */
+
+int64_t orc_mark_blocks(const orc_grid *g, const float *pts, int64_t n, float rScan,
+                        int32_t *blockCount, uint8_t *valid) {
+  float dmin[3], dmax[3];
+  domain_limits(g, dmin, dmax);
+  const float scale = 1.0f / (float)g->bsx, rs = rScan / (float)g->bsx;
+  const int nbx = g->nbx, nby = g->nby, nbz = g->nbz;
+  int64_t nValid = 0;
+#pragma omp parallel for schedule(static) reduction(+ : nValid)
+  for (int64_t i = 0; i < n; i++) {
+    const float px = pts[3 * i], py = pts[3 * i + 1], pz = pts[3 * i + 2];
+    if (!point_valid(g, px, py, pz, dmin, dmax)) { valid[i] = 0; continue; }
+    valid[i] = 1;
+    nValid++;
+    const float bx = px * scale, by = py * scale, bz = pz * scale;
+    const int x1 = imax((int)(bx - rs), 0), x2 = imin((int)(bx + rs), nbx - 1);
+    const int y1 = imax((int)(by - rs), 0), y2 = imin((int)(by + rs), nby - 1);
+    const int z1 = imax((int)(bz - rs), 0), z2 = imin((int)(bz + rs), nbz - 1);
+    for (int k = z1; k <= z2; k++)
+      for (int j = y1; j <= y2; j++)
+        for (int l = x1; l <= x2; l++) {
+#pragma omp atomic
+          blockCount[(int64_t)k * nbx * nby + (int64_t)j * nbx + l]++;
+        }
+  }
+  return nValid;
+}
+
+static inline int64_t own_block(const orc_grid *g, const float *p) {
+  const int s = ilog2(g->bsx);
+  const int ix = (int)p[0], iy = (int)p[1], iz = (int)p[2];
+  return (int64_t)(iz >> s) * g->nbx * g->nby + (int64_t)(iy >> s) * g->nbx + (ix >> s);
+}
+
+void orc_bucket_points(const orc_grid *g, const float *pts, int64_t n, const uint8_t *valid,
+                       int64_t *bucketStart, int64_t *bucketIdx) {
+  const int64_t nB = (int64_t)g->nbx * g->nby * g->nbz;
+  memset(bucketStart, 0, sizeof(int64_t) * (size_t)(nB + 1));
+  for (int64_t i = 0; i < n; i++)
+    if (valid[i]) bucketStart[own_block(g, pts + 3 * i) + 1]++;
+  for (int64_t b = 0; b < nB; b++) bucketStart[b + 1] += bucketStart[b];
+  int64_t *fill = (int64_t *)malloc(sizeof(int64_t) * (size_t)nB);
+  memcpy(fill, bucketStart, sizeof(int64_t) * (size_t)nB);
+  for (int64_t i = 0; i < n; i++)
+    if (valid[i]) bucketIdx[fill[own_block(g, pts + 3 * i)]++] = i;
+  free(fill);
+}
+
+void orc_band_levels(const orc_grid *g, const float *pts, int64_t n, const uint8_t *valid,
+                     const float *rBand, int nBands, int nLevels, int32_t *levels) {
+  const int64_t nB = (int64_t)g->nbx * g->nby * g->nbz;
+  for (int64_t b = 0; b < nB; b++) levels[b] = nLevels - 1;
+  const float scale = 1.0f / (float)g->bsx;
+  for (int l = nBands - 1; l >= 0; l--) {
+    const float rs = rBand[l] / (float)g->bsx;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+      if (!valid[i]) continue;
+      const float bx = pts[3 * i] * scale, by = pts[3 * i + 1] * scale, bz = pts[3 * i + 2] * scale;
+      const int x1 = imax((int)(bx - rs), 0), x2 = imin((int)(bx + rs), g->nbx - 1);
+      const int y1 = imax((int)(by - rs), 0), y2 = imin((int)(by + rs), g->nby - 1);
+      const int z1 = imax((int)(bz - rs), 0), z2 = imin((int)(bz + rs), g->nbz - 1);
+      for (int k = z1; k <= z2; k++)
+        for (int j = y1; j <= y2; j++)
+          for (int m = x1; m <= x2; m++) {
+            int32_t *lv = &levels[(int64_t)k * g->nbx * g->nby + (int64_t)j * g->nbx + m];
+            if (*lv > l) {
+#pragma omp atomic write
+              *lv = l;
+            }
+          }
+    }
+  }
+}
+
+void orc_regularize(const int32_t *levelsIn, int32_t *levelsOut, int nbx, int nby, int nbz,
+                    int nLevels, int64_t *perLevel) {
+  const int64_t nB = (int64_t)nbx * nby * nbz;
+  int32_t *src = (int32_t *)malloc(sizeof(int32_t) * (size_t)nB);
+  int32_t *dst = (int32_t *)malloc(sizeof(int32_t) * (size_t)nB);
+  memcpy(src, levelsIn, sizeof(int32_t) * (size_t)nB);
+  memcpy(dst, levelsIn, sizeof(int32_t) * (size_t)nB);
+  for (int ll = 1; ll <= nLevels - 2; ll++) {
+#pragma omp parallel for schedule(static)
+    for (int64_t bid = 0; bid < nB; bid++) {
+      const int bz = (int)(bid / ((int64_t)nbx * nby));
+      const int rem = (int)(bid % ((int64_t)nbx * nby));
+      const int by = rem / nbx, bx = rem % nbx;
+      int level = src[bid];
+      if (level >= ll) {
+        int finest = nLevels - 1;
+        for (int dz = -1; dz <= 1; dz++)
+          for (int dy = -1; dy <= 1; dy++)
+            for (int dx = -1; dx <= 1; dx++) {
+              if (!dx && !dy && !dz) continue;
+              const int x = bx + dx, y = by + dy, z = bz + dz;
+              if (x < 0 || y < 0 || z < 0 || x >= nbx || y >= nby || z >= nbz) continue;
+              const int l2 = src[(int64_t)z * nbx * nby + (int64_t)y * nbx + x];
+              if (l2 < finest) finest = l2;
+            }
+        if (finest == ll - 1) level = ll;
+      }
+      dst[bid] = level;
+    }
+    memcpy(src, dst, sizeof(int32_t) * (size_t)nB);
+  }
+  if (perLevel) {
+    for (int l = 0; l < 8; l++) perLevel[l] = 0;
+    for (int64_t b = 0; b < nB; b++)
+      if (dst[b] >= 0 && dst[b] < 8) perLevel[dst[b]]++;
+  }
+  memcpy(levelsOut, dst, sizeof(int32_t) * (size_t)nB);
+  free(src);
+  free(dst);
+}
+
+void orc_block_flags(const int32_t *levels, const uint16_t *existsFlags, uint16_t *flags,
+                     int nbx, int nby, int nbz) {
+  const int64_t nB = (int64_t)nbx * nby * nbz;
+#pragma omp parallel for schedule(static)
+  for (int64_t bid = 0; bid < nB; bid++) {
+    const int bz = (int)(bid / ((int64_t)nbx * nby));
+    const int rem = (int)(bid % ((int64_t)nbx * nby));
+    const int by = rem / nbx, bx = rem % nbx;
+    uint16_t f = existsFlags ? (uint16_t)(existsFlags[bid] & ORC_BLK_EXISTS) : 0;
+    if (bx == 0 || bx == nbx - 1 || by == 0 || by == nby - 1 || bz == 0 || bz == nbz - 1)
+      f |= ORC_BLK_DOM_BORDER;
+    const int level = levels[bid];
+    int lmax = 0, lmin = 1 << 20;
+    for (int dz = -1; dz <= 1; dz++)
+      for (int dy = -1; dy <= 1; dy++)
+        for (int dx = -1; dx <= 1; dx++) {
+          if (!dx && !dy && !dz) continue;
+          const int x = bx + dx, y = by + dy, z = bz + dz;
+          if (x < 0 || y < 0 || z < 0 || x >= nbx || y >= nby || z >= nbz) continue;
+          const int l2 = levels[(int64_t)z * nbx * nby + (int64_t)y * nbx + x];
+          lmax = imax(lmax, l2);
+          lmin = imin(lmin, l2);
+        }
+    if (lmax > level) f |= ORC_BLK_FINE_COARSE;
+    if (lmin < level) f |= ORC_BLK_COARSE_FINE;
+    if (!(f & ORC_BLK_EXISTS) && !(f & (ORC_BLK_FINE_COARSE | ORC_BLK_COARSE_FINE)))
+      f |= ORC_BLK_UNIFORM_EMPTY;
+    flags[bid] = f;
+  }
+}
+
+int32_t orc_build_slots(const int32_t *levels, int nBlocks, int32_t *slot, int32_t *activeBids) {
+  int32_t n = 0;
+  for (int b = 0; b < nBlocks; b++) {
+    if (levels[b] == 0) {
+      slot[b] = n;
+      activeBids[n++] = b;
+    } else {
+      slot[b] = -1;
+    }
+  }
+  return n;
+}
+
+void orc_fill(const orc_grid *g, void *payload, int64_t nActive, double v) {
+  const int64_t nv = (int64_t)nActive * g->bsx * g->bsx * g->bsx;
+  for (int64_t i = 0; i < nv; i++) {
+    switch (g->storage) {
+      case ORC_F32: ((float *)payload)[i] = (float)v; break;
+      case ORC_U16: ((uint16_t *)payload)[i] = u16_rha((float)v); break;
+      case ORC_F16: ((uint16_t *)payload)[i] = orc_f32_to_f16((float)v); break;
+      default: ((double *)payload)[i] = v; break;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* splat / finalize                                                          */
+/* ------------------------------------------------------------------------ */
+
+static inline int block_color8(int bx, int by, int bz) {
+  return (bx & 1) + ((by & 1) << 1) + ((bz & 1) << 2); /* src/msbg.h:642-646 */
+}
+
+/* min-store of q = distSq/distSqMax into the voxel, in the slab's storage type. */
+static inline void splat_store(const orc_grid *g, void *payload, int64_t i, float q) {
+  switch (g->storage) {
+    case ORC_F32: {
+      float *p = (float *)payload + i;
+      if (q < *p) *p = q;
+      break;
+    }
+    case ORC_U16: {
+      uint16_t *p = (uint16_t *)payload + i, v = u16_rha(q);
+      if (v < *p) *p = v;
+      break;
+    }
+    case ORC_F16: {
+      uint16_t *p = (uint16_t *)payload + i, v = orc_f32_to_f16(q);
+      if (v < *p) *p = v; /* non-negative halves order like their bit patterns */
+      break;
+    }
+    default: {
+      double *p = (double *)payload + i;
+      if ((double)q < *p) *p = q;
+      break;
+    }
+  }
+}
+
+int64_t orc_splat(const orc_grid *g, const float *pts, const int64_t *bucketStart,
+                  const int64_t *bucketIdx, const int32_t *slot, const int32_t *activeBids,
+                  int32_t nActive, void *payload, float rParticle, float nbDist) {
+  const float rScan = rParticle + nbDist;
+  const float distSqMax = rScan * rScan, distSqMaxInv = 1.0f / distSqMax;
+  const int bs = g->bsx, s = ilog2(bs), s2 = 2 * s, mask = bs - 1;
+  const int nx = g->nbx, nxy = g->nbx * g->nby;
+  const int64_t nv = (int64_t)bs * bs * bs;
+  int64_t nAborted = 0;
+  int32_t *lists[8];
+  int32_t cnt[8] = {0};
+  for (int c = 0; c < 8; c++) lists[c] = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nActive + 1));
+  for (int32_t t = 0; t < nActive; t++) {
+    const int bid = activeBids[t];
+    const int bz = bid / nxy, by = (bid % nxy) / nx, bx = bid % nx;
+    const int c = block_color8(bx, by, bz);
+    lists[c][cnt[c]++] = bid;
+  }
+  for (int c = 0; c < 8; c++) {
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : nAborted)
+    for (int32_t t = 0; t < cnt[c]; t++) {
+      const int bid = lists[c][t];
+      for (int64_t q = bucketStart[bid]; q < bucketStart[bid + 1]; q++) {
+        const float *p = pts + 3 * bucketIdx[q];
+        const int ix1 = imax((int)ceilf(p[0] - rScan - 0.5f), 0);
+        const int iy1 = imax((int)ceilf(p[1] - rScan - 0.5f), 0);
+        const int iz1 = imax((int)ceilf(p[2] - rScan - 0.5f), 0);
+        const int ix2 = imin((int)floorf(p[0] + rScan - 0.5f), g->sx - 1);
+        const int iy2 = imin((int)floorf(p[1] + rScan - 0.5f), g->sy - 1);
+        const int iz2 = imin((int)floorf(p[2] + rScan - 0.5f), g->sz - 1);
+        const float x0 = p[0] - 0.5f, y0 = p[1] - 0.5f, z0 = p[2] - 0.5f;
+        for (int iz = iz1; iz <= iz2; iz++) {
+          const float dz = (float)iz - z0;
+          const int ibz = (iz >> s) * nxy, ivz = (iz & mask) << s2;
+          for (int iy = iy1; iy <= iy2; iy++) {
+            const float dy = (float)iy - y0;
+            const float dzy = dz * dz + dy * dy;
+            const int ibzy = ibz + (iy >> s) * nx, ivzy = ivz + ((iy & mask) << s);
+            for (int ix = ix1; ix <= ix2; ix++) {
+              const float dx = (float)ix - x0;
+              const float d2 = dzy + dx * dx;
+              if (d2 > distSqMax) continue;
+              const int sl = slot[ibzy + (ix >> s)];
+              if (sl < 0) { nAborted++; goto next_particle; }
+              splat_store(g, payload, (int64_t)sl * nv + ivzy + (ix & mask), d2 * distSqMaxInv);
+            }
+          }
+        }
+      next_particle:;
+      }
+    }
+  }
+  for (int c = 0; c < 8; c++) free(lists[c]);
+  return nAborted;
+}
+
+/* MT_LINSTEPF, src/mtool.h:400-408.  The reference is built with -ffast-math,
+ * under which the division by the constant (b - a) becomes a multiplication by
+ * its rounded reciprocal; that is the rounding reproduced here. */
+static inline float linstepf(float a, float b, float x) {
+  if (x < a) return 0.0f;
+  if (x >= b) return 1.0f;
+  const float inv = 1.0f / (b - a);
+  return (x - a) * inv;
+}
+
+void orc_finalize(const orc_grid *g, void *payload, int64_t nActive, float rParticle,
+                  float nbDist) {
+  const float rScan = rParticle + nbDist, distSqMax = rScan * rScan;
+  const int64_t n = nActive * (int64_t)g->bsx * g->bsx * g->bsx;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; i++) {
+    float d = (float)load_val(g, payload, i);
+    float f = 0.0f;
+    if (d < 0.999f) {
+      d *= distSqMax;
+      const float dist = sqrtf(d) - rParticle;
+      f = 1.0f - linstepf(-rParticle, rParticle + nbDist, dist);
+    }
+    switch (g->storage) {
+      case ORC_F32: ((float *)payload)[i] = f; break;
+      case ORC_U16: ((uint16_t *)payload)[i] = u16_rha(f); break;
+      case ORC_F16: ((uint16_t *)payload)[i] = orc_f32_to_f16(f); break;
+      default: ((double *)payload)[i] = f; break;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* halo fill + stencil sweeps                                                */
+/* ------------------------------------------------------------------------ */
+
+/* Halo of h voxels around block bid, as fillHaloBlock_ with OPT_BC_NEUMANN
+ * (src/halo.cpp:266-479, src/halo.h:266-355): in-domain voxels read their block
+ * (a constant empty block reads emptyValue); out-of-domain voxels take the value
+ * of the nearest voxel of the block itself. */
+#define DEFINE_HALO(REAL, NAME)                                                           \
+  static void NAME(const orc_grid *g, const int32_t *slot, const void *payload, int bid, \
+                   int h, REAL *halo) {                                                   \
+    const int bs = g->bsx, hs = bs + 2 * h, s = ilog2(bs);                                \
+    const int nx = g->nbx, nxy = g->nbx * g->nby;                                         \
+    const int bz = bid / nxy, by = (bid % nxy) / nx, bx = bid % nx;                       \
+    const int x0 = bx * bs, y0 = by * bs, z0 = bz * bs;                                   \
+    const int64_t nv = (int64_t)bs * bs * bs;                                             \
+    const int64_t own = (int64_t)slot[bid] * nv;                                          \
+    for (int hz = 0; hz < hs; hz++)                                                       \
+      for (int hy = 0; hy < hs; hy++)                                                     \
+        for (int hx = 0; hx < hs; hx++) {                                                 \
+          int x = x0 + hx - h, y = y0 + hy - h, z = z0 + hz - h;                          \
+          double v;                                                                       \
+          if (x >= 0 && x < g->sx && y >= 0 && y < g->sy && z >= 0 && z < g->sz) {        \
+            const int sl = slot[(z >> s) * nxy + (y >> s) * nx + (x >> s)];               \
+            const int vid = ((z & (bs - 1)) << (2 * s)) + ((y & (bs - 1)) << s) +          \
+                            (x & (bs - 1));                                               \
+            v = sl < 0 ? g->emptyValue : load_val(g, payload, (int64_t)sl * nv + vid);     \
+          } else {                                                                        \
+            x = imin(imax(x, x0), x0 + bs - 1);                                           \
+            y = imin(imax(y, y0), y0 + bs - 1);                                           \
+            z = imin(imax(z, z0), z0 + bs - 1);                                           \
+            const int vid = ((z - z0) * bs + (y - y0)) * bs + (x - x0);                   \
+            v = load_val(g, payload, own + vid);                                          \
+          }                                                                               \
+          halo[((int64_t)hz * hs + hy) * hs + hx] = (REAL)v;                              \
+        }                                                                                 \
+  }
+
+DEFINE_HALO(float, halo_f)
+DEFINE_HALO(double, halo_d)
+
+typedef struct {
+  int laplTyp, constr01;
+  float dt, anisAlpha;
+} pde_params;
+
+/* Per-voxel update of applyChannelPdeFast (src/msbg4.cpp:559-825), written once
+ * for float and once for double math.  F(dx,dy,dz) reads the halo. */
+#define DEFINE_UPDATE(REAL, NAME, SQRT, EXP)                                              \
+  static inline REAL NAME(const REAL *ph, int hs, const pde_params *pp, int iIter) {      \
+    const int hs2 = hs * hs;                                                              \
+    const REAL dt = (REAL)pp->dt;                                                         \
+    REAL phi = ph[0];                                                                     \
+    REAL out = phi;                                                                       \
+    (void)iIter;                                                                          \
+    if (pp->laplTyp == 4) {                                                               \
+      const REAL f0 = ph[0], f1 = ph[-1], f2 = ph[1], f3 = ph[-hs], f4 = ph[hs],          \
+                 f5 = ph[-hs2], f6 = ph[hs2];                                             \
+      const REAL fx = (REAL)0.5 * (f2 - f1), fy = (REAL)0.5 * (f4 - f3),                  \
+                 fz = (REAL)0.5 * (f6 - f5);                                              \
+      const REAL fxx = f1 + f2 - 2 * f0, fyy = f3 + f4 - 2 * f0, fzz = f5 + f6 - 2 * f0;  \
+      const REAL fy_r = (ph[1 + hs] - ph[1 - hs]) * (REAL)0.5;                            \
+      const REAL fy_l = (ph[-1 + hs] - ph[-1 - hs]) * (REAL)0.5;                          \
+      const REAL fz_r = (ph[1 + hs2] - ph[1 - hs2]) * (REAL)0.5;                          \
+      const REAL fz_l = (ph[-1 + hs2] - ph[-1 - hs2]) * (REAL)0.5;                        \
+      const REAL fz_u = (ph[hs + hs2] - ph[hs - hs2]) * (REAL)0.5;                        \
+      const REAL fz_d = (ph[-hs + hs2] - ph[-hs - hs2]) * (REAL)0.5;                      \
+      const REAL fyx = (fy_r - fy_l) * (REAL)0.5, fzx = (fz_r - fz_l) * (REAL)0.5,        \
+                 fzy = (fz_u - fz_d) * (REAL)0.5;                                         \
+      REAL H = (fy * fy + fz * fz) * fxx + (fx * fx + fz * fz) * fyy +                    \
+               (fx * fx + fy * fy) * fzz -                                                \
+               (REAL)2 * (fx * fy * fyx + fx * fz * fzx + fy * fz * fzy);                 \
+      const REAL g2 = fx * fx + fy * fy + fz * fz;                                        \
+      H = g2 > (REAL)1e-7f ? H / g2 : (REAL)0;                                            \
+      REAL D = dt * H;                                                                    \
+      D = D < (REAL)-0.1f ? (REAL)-0.1f : D;                                              \
+      D = D > (REAL)0.1f ? (REAL)0.1f : D;                                                \
+      out = phi + D;                                                                      \
+    } else if (pp->laplTyp == 17) {                                                       \
+      const REAL s6 = ph[-1] + ph[1] + ph[-hs] + ph[hs] + ph[-hs2] + ph[hs2];             \
+      out = (phi + dt * s6) / ((REAL)1 + dt * (REAL)6);                                   \
+    } else if (pp->laplTyp == 3) {                                                        \
+      const REAL S = ((REAL)1 / (REAL)6) *                                                \
+                     (ph[-1] + ph[1] + ph[-hs] + ph[hs] + ph[-hs2] + ph[hs2]);            \
+      out = phi + dt * (S - phi);                                                         \
+    } else if (pp->laplTyp == 1) {                                                        \
+      const REAL F1 = ph[-1], F2 = ph[1], F3 = ph[-hs], F4 = ph[hs], F5 = ph[-hs2],       \
+                 F6 = ph[hs2];                                                            \
+      const REAL L = F1 + F2 + F3 + F4 + F5 + F6 - (REAL)6 * phi;                         \
+      const REAL GX = (REAL)0.5 * (F2 - F1), GY = (REAL)0.5 * (F4 - F3),                  \
+                 GZ = (REAL)0.5 * (F6 - F5);                                              \
+      const REAL G = SQRT(GX * GX + GY * GY + GZ * GZ);                                   \
+      out = phi + dt * L * G;                                                             \
+    } else if (pp->laplTyp == 14 || pp->laplTyp == 15) {                                  \
+      const REAL a = (REAL)pp->anisAlpha;                                                 \
+      const REAL fn[6] = {ph[-1], ph[1], ph[-hs], ph[hs], ph[-hs2], ph[hs2]};             \
+      REAL sum = 0, wsum = 0, dsum = 0;                                                   \
+      for (int k = 0; k < 6; k++) {                                                       \
+        const REAL gk = fn[k] - phi;                                                      \
+        const REAL ag = gk < 0 ? -gk : gk;                                                \
+        REAL Gk;                                                                          \
+        if (a < 0) {                                                                      \
+          const REAL t = ag * ((REAL)1 / -a);                                             \
+          Gk = EXP(-(t * t));                                                             \
+        } else {                                                                          \
+          const REAL t = ag / a;                                                          \
+          Gk = (REAL)1 / ((REAL)1 + t * t);                                               \
+        }                                                                                 \
+        sum += Gk * fn[k];                                                                \
+        wsum += Gk;                                                                       \
+        dsum += Gk * gk;                                                                  \
+      }                                                                                   \
+      if (pp->laplTyp == 15)                                                              \
+        out = (phi + dt * sum) / ((REAL)1 + dt * wsum);                                   \
+      else                                                                                \
+        out = phi + dt * dsum;                                                            \
+    }                                                                                     \
+    if (pp->constr01) {                                                                   \
+      out = out > (REAL)0 ? out : (REAL)0;                                                \
+      out = out < (REAL)1 ? out : (REAL)1;                                                \
+    }                                                                                     \
+    return out;                                                                           \
+  }
+
+DEFINE_UPDATE(float, update_f, sqrtf, expf)
+DEFINE_UPDATE(double, update_d, sqrt, exp)
+
+static inline void store_val(const orc_grid *g, void *p, int64_t i, double v) {
+  switch (g->storage) {
+    case ORC_F32: ((float *)p)[i] = (float)v; break;
+    case ORC_U16: ((uint16_t *)p)[i] = u16_rne((float)v); break; /* round_to_int: RNE */
+    case ORC_F16: ((uint16_t *)p)[i] = orc_f32_to_f16((float)v); break;
+    default: ((double *)p)[i] = v; break;
+  }
+}
+
+/* One block: halo from src, update into dst (dst may equal src for colored
+ * schedules; the halo is a private copy so the block reads only old values). */
+static void sweep_block(const orc_grid *g, const int32_t *slot, const void *src, void *dst,
+                        int bid, const pde_params *pp, int iIter, void *haloBuf) {
+  const int bs = g->bsx, h = 1, hs = bs + 2 * h;
+  const int64_t nv = (int64_t)bs * bs * bs, base = (int64_t)slot[bid] * nv;
+  if (g->storage == ORC_F64) {
+    double *halo = (double *)haloBuf;
+    halo_d(g, slot, src, bid, h, halo);
+    for (int z = 0; z < bs; z++)
+      for (int y = 0; y < bs; y++)
+        for (int x = 0; x < bs; x++) {
+          const double *ph = halo + ((int64_t)(z + h) * hs + (y + h)) * hs + (x + h);
+          store_val(g, dst, base + ((int64_t)z * bs + y) * bs + x, update_d(ph, hs, pp, iIter));
+        }
+  } else {
+    float *halo = (float *)haloBuf;
+    halo_f(g, slot, src, bid, h, halo);
+    for (int z = 0; z < bs; z++)
+      for (int y = 0; y < bs; y++)
+        for (int x = 0; x < bs; x++) {
+          const float *ph = halo + ((int64_t)(z + h) * hs + (y + h)) * hs + (x + h);
+          store_val(g, dst, base + ((int64_t)z * bs + y) * bs + x, update_f(ph, hs, pp, iIter));
+        }
+  }
+}
+
+int orc_pde(const orc_grid *g, const int32_t *slot, const int32_t *activeBids, int32_t nActive,
+            void *payload, void *payloadTmp, int laplTyp, int constr01, int numIter, float dt,
+            float anisAlpha) {
+  int color8 = 0, redBlack = 0;
+  if (laplTyp < 0) { /* src/msbg4.cpp:100-114 */
+    laplTyp = -laplTyp;
+    if (laplTyp & (1 << 29)) {
+      laplTyp &= ~(1 << 29);
+      color8 = 1;
+    } else {
+      redBlack = 1;
+    }
+  }
+  if (!(laplTyp == 4 || laplTyp == 17 || laplTyp == 3 || laplTyp == 1 || laplTyp == 14 ||
+        laplTyp == 15))
+    return -1;
+  if (!color8 && !redBlack && !payloadTmp) return -2;
+  const int nIter0 = numIter;
+  int nIter = numIter;
+  if (nIter % 2 == 1) nIter++; /* src/msbg4.cpp:150-152 */
+  pde_params pp = {laplTyp, constr01, dt, anisAlpha};
+  const int bs = g->bsx, hs = bs + 2;
+  const int nx = g->nbx, nxy = g->nbx * g->nby;
+  const int64_t nv = (int64_t)bs * bs * bs;
+  const size_t eb = elem_bytes(g->storage);
+  const size_t haloBytes = (size_t)hs * hs * hs * (g->storage == ORC_F64 ? 8 : 4);
+  const int nPass = color8 ? 8 : redBlack ? 2 : 1;
+
+  /* ping-pong: slot layout identical in both slabs */
+  void *bufs[2] = {payload, payloadTmp};
+  int cur = 0;
+  for (int it = 0; it < nIter; it++) {
+    void *src = color8 || redBlack ? payload : bufs[cur];
+    void *dst = color8 || redBlack ? payload : bufs[cur ^ 1];
+    const int copyOnly = !(color8 || redBlack) && it == nIter - 1 && (nIter0 % 2) == 1;
+    for (int pass = 0; pass < nPass; pass++) {
+#pragma omp parallel
+      {
+        void *halo = malloc(haloBytes);
+#pragma omp for schedule(dynamic, 4)
+        for (int32_t t = 0; t < nActive; t++) {
+          const int bid = activeBids[t];
+          const int bz = bid / nxy, by = (bid % nxy) / nx, bx = bid % nx;
+          if (redBlack && ((bx + by + bz) & 1) == pass) continue; /* src/msbg4.cpp:447-454 */
+          if (color8 && block_color8(bx, by, bz) != pass) continue;
+          if (copyOnly) {
+            memcpy((char *)dst + (size_t)slot[bid] * nv * eb,
+                   (const char *)src + (size_t)slot[bid] * nv * eb, (size_t)nv * eb);
+            continue;
+          }
+          sweep_block(g, slot, src, dst, bid, &pp, it, halo);
+        }
+        free(halo);
+      }
+    }
+    cur ^= 1;
+  }
+  /* ping-pong ends with the result in bufs[cur]; nIter is even so cur == 0 */
+  return 0;
+}

@@ -1,0 +1,107 @@
+/*
+ * CPU restatement of the MSBG hot path (test infrastructure only).
+ *
+ * This is the checker the GPU library is compared against: plain C (+OpenMP),
+ * portable to x86-64 and aarch64, and itself pinned against the reference
+ * library built from its own sources (oracle/_ref, x86 only) by the tests.
+ * Nothing in the GPU product links or calls it.
+ *
+ * Data layout (the same one the GPU library uses, so results compare directly):
+ *   block id     bid = bx + by*nbx + bz*nbx*nby            (src/sbg.h:1744-1749)
+ *   voxel index  vid = x + y*bs + z*bs*bs inside a block   (src/sbg.h:1816-1820)
+ *   slot[bid]    >= 0: index of the block's payload in a dense slab of
+ *                [nActive][bs^3] values; -1: the shared constant "empty" block
+ *                whose every voxel reads emptyValue (src/sbg.h:2042-2047).
+ */
+#ifndef MSBG_ORACLE_H
+#define MSBG_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Storage types of a payload slab. */
+enum { ORC_F32 = 0, ORC_U16 = 1, ORC_F16 = 2, ORC_F64 = 3 };
+
+/* Block flags, same bit values as src/msbg.h:561-573. */
+enum {
+  ORC_BLK_DOM_BORDER = 1 << 1,
+  ORC_BLK_COARSE_FINE = 1 << 2,
+  ORC_BLK_FINE_COARSE = 1 << 3,
+  ORC_BLK_EXISTS = 1 << 12,
+  ORC_BLK_UNIFORM_EMPTY = 1 << 13
+};
+
+typedef struct {
+  int32_t sx, sy, sz;   /* voxels at the finest level */
+  int32_t bsx;          /* block edge (power of two)  */
+  int32_t nbx, nby, nbz;
+  int32_t storage;      /* ORC_* */
+  double emptyValue;    /* value of every voxel of a constant empty block */
+} orc_grid;
+
+void orc_grid_init(orc_grid *g, int sx, int sy, int sz, int bsx, int storage);
+
+/* ---- active-block marking and per-block particle buckets ------------------
+ * src/msbg_demo.cpp:339-397.  valid[i]=1 for points that pass the domain tests;
+ * blockCount[bid] += 1 for every block of the point's rScan box.  Points are then
+ * bucketed by the block that contains them: bucketStart[nBlocks+1] (prefix sums)
+ * and bucketIdx[nValid] (point indices).  Returns the number of valid points. */
+int64_t orc_mark_blocks(const orc_grid *g, const float *pts, int64_t n, float rScan,
+                        int32_t *blockCount, uint8_t *valid);
+void orc_bucket_points(const orc_grid *g, const float *pts, int64_t n, const uint8_t *valid,
+                       int64_t *bucketStart, int64_t *bucketIdx);
+
+/* Multi-band level assignment: level 0 for blocks in the rBand[0] box of any
+ * point, level l for the rBand[l] box, nLevels-1 elsewhere (nBands <= nLevels-1). */
+void orc_band_levels(const orc_grid *g, const float *pts, int64_t n, const uint8_t *valid,
+                     const float *rBand, int nBands, int nLevels, int32_t *levels);
+
+/* ---- refinement map --------------------------------------------------------
+ * regularizeRefinementMap (src/msbg.cpp:1202-1423): at most one level jump
+ * between 26-neighbours.  levelsOut may alias levelsIn.  perLevel[8] counts. */
+void orc_regularize(const int32_t *levelsIn, int32_t *levelsOut, int nbx, int nby, int nbz,
+                    int nLevels, int64_t *perLevel);
+/* BlockInfo flags of setRefinementMap (src/msbg.cpp:1632-1720) for levelMg 0;
+ * existsFlags may be NULL (no BLK_EXISTS). */
+void orc_block_flags(const int32_t *levels, const uint16_t *existsFlags, uint16_t *flags,
+                     int nbx, int nby, int nbz);
+
+/* Level-0 blocks get slots in ascending bid order (src/msbg_demo.cpp:455-511).
+ * Returns nActive; activeBids[nActive]. */
+int32_t orc_build_slots(const int32_t *levels, int nBlocks, int32_t *slot, int32_t *activeBids);
+
+/* Fill every active payload voxel with v. */
+void orc_fill(const orc_grid *g, void *payload, int64_t nActive, double v);
+
+/* ---- splat and finalize ----------------------------------------------------
+ * 8-color splat of min(distSq/distSqMax) (src/msbg_demo.cpp:527-636) and the
+ * distance-to-density finalize (src/msbg_demo.cpp:655-680).  A particle is
+ * abandoned at its first in-sphere voxel that lies in a non-value block. */
+int64_t orc_splat(const orc_grid *g, const float *pts, const int64_t *bucketStart,
+                  const int64_t *bucketIdx, const int32_t *slot, const int32_t *activeBids,
+                  int32_t nActive, void *payload, float rParticle, float nbDist);
+void orc_finalize(const orc_grid *g, void *payload, int64_t nActive, float rParticle,
+                  float nbDist);
+
+/* ---- stencil sweeps: applyChannelPdeFast (src/msbg4.cpp:60-957) -----------
+ * laplTyp as the reference takes it: negative = in-place colored schedule (with
+ * OPT_8_COLOR_SCHEME = 1<<29: 8 colors, else red-black), positive = ping-pong.
+ * Kernels: 4 MCF, 17 Jacobi diffusion, 15 Perona-Malik Jacobi, 14 Perona-Malik,
+ * 3 simple diffusion, 1 Laplacian smoothing.  numIter is rounded up to even as
+ * the reference does.  Math runs in float, or in double when storage==ORC_F64.
+ * payloadTmp is needed for the ping-pong schedule only. */
+int orc_pde(const orc_grid *g, const int32_t *slot, const int32_t *activeBids, int32_t nActive,
+            void *payload, void *payloadTmp, int laplTyp, int constr01, int numIter, float dt,
+            float anisAlpha);
+
+/* ---- conversions (exposed for tests) ---- */
+uint16_t orc_f32_to_f16(float f);
+float orc_f16_to_f32(uint16_t h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,150 @@
+"""Job/result files for the CPU oracles (test infrastructure only).
+
+Two oracles share one binary layout (``oracle_common.h``):
+
+* ``_ref/msbg_ref_driver`` - the MSBG reference library compiled from its own
+  sources (x86-64 only; built by ``make -C oracle ref``);
+* ``_build/libmsbg_oracle.so`` - the project's C restatement (any arch; built by
+  ``make -C oracle port``), reached through ctypes in ``oracle/port.py``.
+
+Only tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use
+this module.
+"""
+from __future__ import annotations
+
+import os
+import struct
+import subprocess
+import tempfile
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DRIVER = os.path.join(HERE, "_ref", "msbg_ref_driver")
+
+JOB_MAGIC = b"MSBGJOB2"
+OUT_MAGIC = b"MSBGOUT2"
+CHAN_F32, CHAN_U16 = 0, 1
+JOB_SURFACE, JOB_LEVELS = 1, 2
+
+# OracleJobHeader: magic[8], 11 x int32, 4 x float, int32, 2 x int64
+_JOB_FMT = "<8s11i4fi2q"
+# OracleOutHeader: magic[8], int32 nBlocks, int32 nActive, int64 nActParticles,
+# int64[8], 6 x double, int32 elemBytes, int32 nThreadsUsed
+_OUT_FMT = "<8s2iq8q6d2i"
+
+PDE_MEAN_CURVATURE = 4
+OPT_8_COLOR_SCHEME = 1 << 29
+LAPL_MCF_8COLOR = -(PDE_MEAN_CURVATURE + OPT_8_COLOR_SCHEME)
+
+
+@dataclass
+class SurfaceJob:
+    sx: int
+    sy: int
+    sz: int
+    bsx: int
+    points: np.ndarray
+    chan: int = CHAN_F32
+    n_iter: int = 20
+    lapl_typ: int = LAPL_MCF_8COLOR
+    constr01: int = 1
+    dt: float = 0.1
+    r_particle: float = 2.0
+    nb_dist: float = 2.0
+    n_levels: int = 3
+    n_threads: int = 0
+    levels: np.ndarray | None = None  # optional caller-supplied level map
+    anis_alpha: float = 0.0
+
+
+@dataclass
+class OracleResult:
+    n_blocks: int
+    n_active: int
+    n_act_particles: int
+    blocks_per_level: np.ndarray
+    times: dict
+    levels: np.ndarray          # int8 [nBlocks]
+    flags: np.ndarray           # uint16 [nBlocks]
+    active_bids: np.ndarray     # int32 [nActive]
+    after_finalize: np.ndarray  # [nActive, bsx^3]
+    after_pde: np.ndarray       # [nActive, bsx^3]
+    threads: int
+
+
+def write_surface_job(path: str, job: SurfaceJob) -> None:
+    pts = np.ascontiguousarray(job.points, dtype=np.float32).reshape(-1, 3)
+    lv = None if job.levels is None else np.ascontiguousarray(job.levels, np.int32).ravel()
+    hdr = struct.pack(_JOB_FMT, JOB_MAGIC, JOB_SURFACE, job.sx, job.sy, job.sz, job.bsx,
+                      job.n_levels, job.chan, job.n_iter, job.lapl_typ, job.constr01,
+                      job.n_threads, job.dt, job.r_particle, job.nb_dist, job.anis_alpha, 0,
+                      pts.shape[0], 0 if lv is None else lv.size)
+    with open(path, "wb") as f:
+        f.write(hdr)
+        f.write(pts.tobytes())
+        if lv is not None:
+            f.write(lv.tobytes())
+
+
+def write_levels_job(path: str, sx: int, sy: int, sz: int, bsx: int, n_levels: int,
+                     levels: np.ndarray, n_threads: int = 0) -> None:
+    lv = np.ascontiguousarray(levels, dtype=np.int32).ravel()
+    hdr = struct.pack(_JOB_FMT, JOB_MAGIC, JOB_LEVELS, sx, sy, sz, bsx, n_levels, 0, 0, 0, 0,
+                      n_threads, 0.0, 0.0, 0.0, 0.0, 0, 0, lv.size)
+    with open(path, "wb") as f:
+        f.write(hdr)
+        f.write(lv.tobytes())
+
+
+def read_result(path: str, bsx: int, surface: bool = True) -> OracleResult:
+    with open(path, "rb") as f:
+        buf = f.read()
+    hsz = struct.calcsize(_OUT_FMT)
+    h = struct.unpack(_OUT_FMT, buf[:hsz])
+    if h[0] != OUT_MAGIC:
+        raise ValueError("bad oracle output")
+    n_blocks, n_active, n_act = h[1], h[2], h[3]
+    per_level = np.array(h[4:12], dtype=np.int64)
+    tnames = ["mark", "levels", "alloc", "splat", "final", "pde"]
+    times = dict(zip(tnames, h[12:18]))
+    elem, threads = h[18], h[19]
+    off = hsz
+    levels = np.frombuffer(buf, np.int8, n_blocks, off); off += n_blocks
+    flags = np.frombuffer(buf, np.uint16, n_blocks, off); off += 2 * n_blocks
+    if not surface:
+        z = np.zeros((0, bsx ** 3), np.float32)
+        return OracleResult(n_blocks, 0, 0, per_level, times, levels.copy(), flags.copy(),
+                            np.zeros(0, np.int32), z, z, threads)
+    bids = np.frombuffer(buf, np.int32, n_active, off); off += 4 * n_active
+    dt = np.float32 if elem == 4 else np.uint16
+    nv = bsx ** 3
+    a = np.frombuffer(buf, dt, n_active * nv, off).reshape(n_active, nv); off += elem * n_active * nv
+    b = np.frombuffer(buf, dt, n_active * nv, off).reshape(n_active, nv)
+    return OracleResult(n_blocks, n_active, n_act, per_level, times, levels.copy(), flags.copy(),
+                        bids.copy(), a.copy(), b.copy(), threads)
+
+
+def ref_available() -> bool:
+    return os.path.isfile(REF_DRIVER) and os.access(REF_DRIVER, os.X_OK)
+
+
+def run_reference_surface(job: SurfaceJob, timeout: float = 600) -> OracleResult:
+    """Run the compiled reference library on a surface job."""
+    with tempfile.TemporaryDirectory() as td:
+        jp, op = os.path.join(td, "job.bin"), os.path.join(td, "out.bin")
+        write_surface_job(jp, job)
+        subprocess.run([REF_DRIVER, jp, op], check=True, cwd=td, timeout=timeout,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        return read_result(op, job.bsx, surface=True)
+
+
+def run_reference_levels(sx, sy, sz, bsx, n_levels, levels, timeout: float = 600) -> OracleResult:
+    """Run the reference regularizeRefinementMap + setRefinementMap on a level map."""
+    with tempfile.TemporaryDirectory() as td:
+        jp, op = os.path.join(td, "job.bin"), os.path.join(td, "out.bin")
+        write_levels_job(jp, sx, sy, sz, bsx, n_levels, levels)
+        subprocess.run([REF_DRIVER, jp, op], check=True, cwd=td, timeout=timeout,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        return read_result(op, bsx, surface=False)

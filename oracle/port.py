@@ -1,0 +1,200 @@
+"""ctypes front end of the project's C restatement (oracle/msbg_oracle.c).
+
+Test infrastructure only: the checker that GPU results are compared with, and
+the timed CPU baseline.  ``surface_pipeline`` runs the same stages, in the same
+order, as the reference demo (src/msbg_demo.cpp:228-727) and returns the same
+fields as ``oracle_io.run_reference_surface``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libmsbg_oracle.so")
+
+F32, U16, F16, F64 = 0, 1, 2, 3
+BLK_DOM_BORDER, BLK_COARSE_FINE, BLK_FINE_COARSE = 1 << 1, 1 << 2, 1 << 3
+BLK_EXISTS, BLK_UNIFORM_EMPTY = 1 << 12, 1 << 13
+NP_STORAGE = {F32: np.float32, U16: np.uint16, F16: np.uint16, F64: np.float64}
+
+_lib = None
+
+
+class Grid(C.Structure):
+    _fields_ = [("sx", C.c_int32), ("sy", C.c_int32), ("sz", C.c_int32), ("bsx", C.c_int32),
+                ("nbx", C.c_int32), ("nby", C.c_int32), ("nbz", C.c_int32),
+                ("storage", C.c_int32), ("emptyValue", C.c_double)]
+
+
+def build() -> None:
+    subprocess.run(["make", "-C", HERE, "port"], check=True, stdout=subprocess.DEVNULL)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.isfile(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        P = C.c_void_p
+        L.orc_grid_init.argtypes = [C.POINTER(Grid), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.orc_mark_blocks.argtypes = [C.POINTER(Grid), P, C.c_int64, C.c_float, P, P]
+        L.orc_mark_blocks.restype = C.c_int64
+        L.orc_bucket_points.argtypes = [C.POINTER(Grid), P, C.c_int64, P, P, P]
+        L.orc_band_levels.argtypes = [C.POINTER(Grid), P, C.c_int64, P, P, C.c_int, C.c_int, P]
+        L.orc_regularize.argtypes = [P, P, C.c_int, C.c_int, C.c_int, C.c_int, P]
+        L.orc_block_flags.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int]
+        L.orc_build_slots.argtypes = [P, C.c_int, P, P]
+        L.orc_build_slots.restype = C.c_int32
+        L.orc_fill.argtypes = [C.POINTER(Grid), P, C.c_int64, C.c_double]
+        L.orc_splat.argtypes = [C.POINTER(Grid), P, P, P, P, P, C.c_int32, P, C.c_float, C.c_float]
+        L.orc_splat.restype = C.c_int64
+        L.orc_finalize.argtypes = [C.POINTER(Grid), P, C.c_int64, C.c_float, C.c_float]
+        L.orc_pde.argtypes = [C.POINTER(Grid), P, P, C.c_int32, P, P, C.c_int, C.c_int, C.c_int,
+                              C.c_float, C.c_float]
+        L.orc_pde.restype = C.c_int
+        L.orc_f32_to_f16.argtypes = [C.c_float]
+        L.orc_f32_to_f16.restype = C.c_uint16
+        L.orc_f16_to_f32.argtypes = [C.c_uint16]
+        L.orc_f16_to_f32.restype = C.c_float
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def grid(sx, sy, sz, bsx, storage) -> Grid:
+    g = Grid()
+    lib().orc_grid_init(C.byref(g), sx, sy, sz, bsx, storage)
+    return g
+
+
+@dataclass
+class PortResult:
+    n_blocks: int
+    n_active: int
+    n_act_particles: int
+    n_aborted: int
+    blocks_per_level: np.ndarray
+    levels: np.ndarray
+    flags: np.ndarray
+    active_bids: np.ndarray
+    slot: np.ndarray
+    after_finalize: np.ndarray
+    after_pde: np.ndarray
+    times: dict
+
+
+def mark_blocks(g: Grid, pts: np.ndarray, r_scan: float):
+    n_blocks = g.nbx * g.nby * g.nbz
+    cnt = np.zeros(n_blocks, np.int32)
+    valid = np.zeros(len(pts), np.uint8)
+    n_valid = lib().orc_mark_blocks(C.byref(g), _p(pts), len(pts), r_scan, _p(cnt), _p(valid))
+    return cnt, valid, n_valid
+
+
+def regularize(levels: np.ndarray, nbx, nby, nbz, n_levels):
+    lv = np.ascontiguousarray(levels, np.int32).copy()
+    per = np.zeros(8, np.int64)
+    lib().orc_regularize(_p(lv), _p(lv), nbx, nby, nbz, n_levels, _p(per))
+    return lv, per
+
+
+def block_flags(levels: np.ndarray, nbx, nby, nbz, exists: np.ndarray | None = None):
+    lv = np.ascontiguousarray(levels, np.int32)
+    fl = np.zeros(lv.size, np.uint16)
+    ex = None if exists is None else np.ascontiguousarray(exists, np.uint16)
+    lib().orc_block_flags(_p(lv), None if ex is None else _p(ex), _p(fl), nbx, nby, nbz)
+    return fl
+
+
+def pde(g: Grid, slot, active_bids, payload: np.ndarray, lapl_typ: int, constr01: int,
+        n_iter: int, dt: float, anis_alpha: float = 0.0, tmp: np.ndarray | None = None):
+    if lapl_typ > 0 and tmp is None:
+        tmp = np.empty_like(payload)
+    rc = lib().orc_pde(C.byref(g), _p(slot), _p(active_bids), len(active_bids), _p(payload),
+                       None if tmp is None else _p(tmp), lapl_typ, constr01, n_iter, dt,
+                       anis_alpha)
+    if rc != 0:
+        raise ValueError(f"orc_pde rc={rc}")
+    return payload
+
+
+def surface_pipeline(pts: np.ndarray, res, bsx: int, storage: int = F32, n_iter: int = 20,
+                     lapl_typ: int = -(4 + (1 << 29)), constr01: int = 1, dt: float = 0.1,
+                     r_particle: float = 2.0, nb_dist: float = 2.0, n_levels: int = 3,
+                     bands=None, levels_in: np.ndarray | None = None,
+                     anis_alpha: float = 0.0) -> PortResult:
+    """Mark -> levels -> regularize -> slots -> fill(1) -> splat -> finalize -> sweeps.
+
+    ``bands`` (optional, e.g. (8, 16)) selects the distance-band level map of the
+    multi-level workload instead of the demo's single band of width rScan.
+    """
+    sx, sy, sz = (res, res, res) if np.isscalar(res) else res
+    pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 3)
+    g = grid(sx, sy, sz, bsx, storage)
+    n_blocks = g.nbx * g.nby * g.nbz
+    times = {}
+    t0 = time.perf_counter()
+    cnt, valid, n_valid = mark_blocks(g, pts, r_particle + nb_dist)
+    times["mark"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    if levels_in is not None:
+        levels = np.ascontiguousarray(levels_in, np.int32).copy()
+    elif bands is None:
+        levels = np.where(cnt > 0, 0, n_levels - 1).astype(np.int32)
+    else:
+        levels = np.zeros(n_blocks, np.int32)
+        rb = np.asarray(bands, np.float32)
+        lib().orc_band_levels(C.byref(g), _p(pts), len(pts), _p(valid), _p(rb), len(rb),
+                              n_levels, _p(levels))
+    levels, per = regularize(levels, g.nbx, g.nby, g.nbz, n_levels)
+    # setRefinementMap sees no BLK_EXISTS; the demo's allocation loop then sets it
+    # on every level-0 block (src/msbg_demo.cpp:477-491).
+    flags = block_flags(levels, g.nbx, g.nby, g.nbz)
+    flags[levels == 0] |= BLK_EXISTS
+    times["levels"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    slot = np.empty(n_blocks, np.int32)
+    bids = np.empty(n_blocks, np.int32)
+    n_active = lib().orc_build_slots(_p(levels), n_blocks, _p(slot), _p(bids))
+    bids = bids[:n_active].copy()
+    nv = bsx ** 3
+    payload = np.empty(n_active * nv, NP_STORAGE[storage])
+    lib().orc_fill(C.byref(g), _p(payload), n_active, 1.0)
+    bstart = np.empty(n_blocks + 1, np.int64)
+    bidx = np.empty(max(int(n_valid), 1), np.int64)
+    lib().orc_bucket_points(C.byref(g), _p(pts), len(pts), _p(valid), _p(bstart), _p(bidx))
+    times["alloc"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    n_abort = lib().orc_splat(C.byref(g), _p(pts), _p(bstart), _p(bidx), _p(slot), _p(bids),
+                              n_active, _p(payload), r_particle, nb_dist)
+    times["splat"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    lib().orc_finalize(C.byref(g), _p(payload), n_active, r_particle, nb_dist)
+    times["final"] = time.perf_counter() - t0
+    after_final = payload.copy()
+    t0 = time.perf_counter()
+    if n_iter > 0:
+        pde(g, slot, bids, payload, lapl_typ, constr01, n_iter, dt, anis_alpha)
+    times["pde"] = time.perf_counter() - t0
+    return PortResult(n_blocks, n_active, int(n_valid), int(n_abort), per, levels.astype(np.int8),
+                      flags, bids, slot, after_final.reshape(n_active, nv),
+                      payload.reshape(n_active, nv), times)
+
+
+def to_float(storage: int, a: np.ndarray) -> np.ndarray:
+    """Payload values as float64 (uint16 densities scaled by 1/65535)."""
+    if storage == U16:
+        return a.astype(np.float64) / 65535.0
+    if storage == F16:
+        return a.view(np.float16).astype(np.float64)
+    return a.astype(np.float64)

@@ -1,0 +1,343 @@
+/*
+ * Oracle driver linked against the MSBG reference library (compiled from the
+ * reference's own sources by oracle/Makefile).  Test infrastructure only.
+ *
+ * Usage:  msbg_ref_driver <job.bin> <out.bin>
+ *
+ * The demo's marking / splat / finalize loops live in the application, not in
+ * the library (src/msbg_demo.cpp:326-680), so this driver restates them with the
+ * library's own types and index helpers, keeping every step of their
+ * arithmetic and their control flow (including the "abort this particle on a
+ * non-value block" rule at src/msbg_demo.cpp:613-618).  Everything else is the
+ * library itself: MultiresSparseGrid::create, regularizeRefinementMap,
+ * setRefinementMap, SparseGrid block management and applyChannelPdeFast<T>.
+ *
+ * Differences from the demo, both forced by the workload definition:
+ *  - points come from the job file (already in voxel coordinates) instead of
+ *    the bunny instancing of src/msbg_demo.cpp:349-356;
+ *  - an FP32 channel (CH_FLOAT_1) stores floats directly, because the demo's
+ *    renderDensFromFloat_<float> scales by FLT_MAX (src/sbg.h:302-314).
+ */
+#include <omp.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <chrono>
+#include <cmath>
+#include <vector>
+
+#include "msbg.h"
+#include "oracle_common.h"
+
+extern int nMaxThreads;
+
+namespace {
+
+using MSBG::MultiresSparseGrid;
+using SBG::SparseGrid;
+
+double nowSec() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+// Storage conversions that mirror src/sbg.h:236-296 for uint16 and are the identity for
+// float (the FP32 harness stores values directly).
+template <typename T> struct Quant;
+template <> struct Quant<float> {
+  static float fromFloat(float f) { return f; }
+  static float toFloat(float v) { return v; }
+  static float one() { return 1.0f; }
+  static float zero() { return 0.0f; }
+};
+template <> struct Quant<uint16_t> {
+  static uint16_t fromFloat(float f) { return SBG::renderDensFromFloat_<uint16_t>(f); }
+  static float toFloat(uint16_t v) { return SBG::renderDensToFloat_<uint16_t>(v); }
+  static uint16_t one() { return fromFloat(1.0f); }
+  static uint16_t zero() { return fromFloat(0.0f); }
+};
+
+struct Particle {
+  float x, y, z;
+  uint32_t next;  // 0 = end of list; particle i is stored at slot i+1
+};
+
+template <typename T>
+int runSurfaceJob(const OracleJobHeader &job, const float *pts, const int32_t *levelsIn, FILE *fout) {
+  OracleOutHeader out;
+  memset(&out, 0, sizeof(out));
+  memcpy(out.magic, ORACLE_OUT_MAGIC, 8);
+
+  const int chan = (sizeof(T) == 4) ? MSBG::CH_FLOAT_1 : MSBG::CH_UINT16_1;
+  MultiresSparseGrid *msbg = MultiresSparseGrid::create(
+      "TEST", job.sx, job.sy, job.sz, job.bsx, -1, 0, -1,
+      MSBG::OPT_SINGLE_LEVEL | MSBG::OPT_SINGLE_CHANNEL_FLOAT);
+  if (!msbg) return 2;
+  SparseGrid<T> *sg0 = MSBG::getChannel<T>(msbg, chan, 0);
+  if (!sg0) return 3;
+
+  const int nBlocks = msbg->nBlocks();
+  const float rParticle = job.rParticle, nbDist = job.nbDist;
+  const float rScan = rParticle + nbDist;
+
+  std::vector<long> blockActive(nBlocks, 0);
+  std::vector<uint32_t> listHead(nBlocks, 0);
+  std::vector<Particle> parts((size_t)job.nPoints + 1);
+  int64_t nAct = 0;
+
+  // ---- active-block marking + per-block particle lists (demo 339-397) ----
+  double t0 = nowSec();
+  {
+    const int bxMax = sg0->nbx() - 1, byMax = sg0->nby() - 1, bzMax = sg0->nbz() - 1;
+    const float scale2Blk = 1.0f / (float)sg0->bsx();
+    const float rScanBsx = rScan / (float)sg0->bsx();
+    const int nxBlk = sg0->nbx(), nxyBlk = sg0->nbxy();
+    const int bsxLog2 = sg0->bsxLog2();
+#pragma omp parallel for schedule(static) reduction(+ : nAct)
+    for (int64_t i = 0; i < job.nPoints; i++) {
+      const float px = pts[3 * i], py = pts[3 * i + 1], pz = pts[3 * i + 2];
+      Vec4f pos(px, py, pz, 0.f);
+      if (!msbg->isInDomainRange(pos)) continue;
+      const int ix = (int)px, iy = (int)py, iz = (int)pz;
+      if (!sg0->inRange(Vec4i(ix, iy, iz, 0))) continue;
+      Particle &p = parts[i + 1];
+      p.x = px; p.y = py; p.z = pz;
+      const float bx = px * scale2Blk, by = py * scale2Blk, bz = pz * scale2Blk;
+      const int bx1 = std::max((int)(bx - rScanBsx), 0), bx2 = std::min((int)(bx + rScanBsx), bxMax);
+      const int by1 = std::max((int)(by - rScanBsx), 0), by2 = std::min((int)(by + rScanBsx), byMax);
+      const int bz1 = std::max((int)(bz - rScanBsx), 0), bz2 = std::min((int)(bz + rScanBsx), bzMax);
+      for (int k = bz1; k <= bz2; k++)
+        for (int j = by1; j <= by2; j++)
+          for (int l = bx1; l <= bx2; l++) {
+            const int bid = sg0->getBlockIndex(l, j, k);
+            __atomic_fetch_add(&blockActive[bid], 1, __ATOMIC_RELAXED);
+          }
+      const int bidOwn = (iz >> bsxLog2) * nxyBlk + (iy >> bsxLog2) * nxBlk + (ix >> bsxLog2);
+      p.next = __atomic_exchange_n(&listHead[bidOwn], (uint32_t)(i + 1), __ATOMIC_RELAXED);
+      nAct++;
+    }
+  }
+  out.tMarkSec = nowSec() - t0;
+  out.nActParticles = nAct;
+
+  // ---- level map + regularize + setRefinementMap (demo 413-436) ----
+  t0 = nowSec();
+  std::vector<int> levels(nBlocks);
+  for (int b = 0; b < nBlocks; b++) levels[b] = blockActive[b] ? 0 : msbg->getNumLevels() - 1;
+  if (job.nBlocksIn == nBlocks && levelsIn) {
+    // caller-supplied level map (used to provoke the splat's abort rule)
+    for (int b = 0; b < nBlocks; b++) levels[b] = levelsIn[b];
+  }
+  msbg->regularizeRefinementMap(levels.data());
+  msbg->setRefinementMap(levels.data(), NULL, -1, NULL, false);
+  out.tLevelsSec = nowSec() - t0;
+
+  // ---- allocate level-0 blocks, value 1.0; others become the const empty block (demo 455-511) ----
+  t0 = nowSec();
+  std::vector<int> activeBlocks;
+  sg0->reset();
+  sg0->prepareDataAccess();
+  sg0->setEmptyValue(Quant<T>::zero());
+  sg0->setFullValue(Quant<T>::one());
+  for (int bid = 0; bid < nBlocks; bid++) {
+    MSBG::BlockInfo *bi = msbg->getBlockInfo(bid);
+    bi->flags &= ~MSBG::BLK_EXISTS;
+    if (bi->level > 0) {
+      sg0->setEmptyBlock(bid);
+      continue;
+    }
+    activeBlocks.push_back(bid);
+    bi->flags |= MSBG::BLK_EXISTS;
+    T *data = sg0->getBlockDataPtr(bid, 1, 0);
+    for (int v = 0; v < sg0->nVoxelsInBlock(); v++) data[v] = Quant<T>::one();
+  }
+  out.tAllocSec = nowSec() - t0;
+  out.nActive = (int)activeBlocks.size();
+
+  // ---- 8-color splat of min(distSq/distSqMax) (demo 527-636) ----
+  t0 = nowSec();
+  {
+    const float distSqMax = rScan * rScan, distSqMaxInv = 1.0f / distSqMax;
+    std::vector<int> perColor[8];
+    for (int bid : activeBlocks) {
+      int bx, by, bz;
+      sg0->getBlockCoordsById(bid, bx, by, bz);
+      perColor[MSBG::getBlockColor8(bx, by, bz)].push_back(bid);
+    }
+    const int bsxLog2 = sg0->bsxLog2(), bsx2Log2 = sg0->bsx2Log2(), bsxMask = sg0->bsx() - 1;
+    const int nx = sg0->nbx(), nxy = sg0->nbxy();
+    const int xMax = job.sx - 1, yMax = job.sy - 1, zMax = job.sz - 1;
+    for (int c = 0; c < 8; c++) {
+      const std::vector<int> &lst = perColor[c];
+#pragma omp parallel for schedule(dynamic, 1)
+      for (size_t t = 0; t < lst.size(); t++) {
+        const int bid = lst[t];
+        for (uint32_t ixp = listHead[bid]; ixp; ixp = parts[ixp].next) {
+          const Particle &p = parts[ixp];
+          const int ix1 = std::max((int)std::ceil(p.x - rScan - 0.5f), 0);
+          const int iy1 = std::max((int)std::ceil(p.y - rScan - 0.5f), 0);
+          const int iz1 = std::max((int)std::ceil(p.z - rScan - 0.5f), 0);
+          const int ix2 = std::min((int)std::floor(p.x + rScan - 0.5f), xMax);
+          const int iy2 = std::min((int)std::floor(p.y + rScan - 0.5f), yMax);
+          const int iz2 = std::min((int)std::floor(p.z + rScan - 0.5f), zMax);
+          const float x0 = p.x - 0.5f, y0 = p.y - 0.5f, z0 = p.z - 0.5f;
+          bool aborted = false;
+          for (int iz = iz1; iz <= iz2 && !aborted; iz++) {
+            const float dz = iz - z0;
+            const int ibz = (iz >> bsxLog2) * nxy, ivz = (iz & bsxMask) << bsx2Log2;
+            for (int iy = iy1; iy <= iy2 && !aborted; iy++) {
+              const float dy = iy - y0;
+              const float dzy = dz * dz + dy * dy;
+              const int ibzy = ibz + (iy >> bsxLog2) * nx, ivzy = ivz + ((iy & bsxMask) << bsxLog2);
+              for (int ix = ix1; ix <= ix2; ix++) {
+                const float dx = ix - x0;
+                const float d2 = dzy + dx * dx;
+                if (d2 > distSqMax) continue;
+                SBG::Block<T> *blk = sg0->getBlock(ibzy + (ix >> bsxLog2));
+                if (!sg0->isValueBlock(blk)) { aborted = true; break; }
+                const int iv = ivzy + (ix & bsxMask);
+                const T val = Quant<T>::fromFloat(d2 * distSqMaxInv);
+                if (val < blk->_data[iv]) blk->_data[iv] = val;
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  out.tSplatSec = nowSec() - t0;
+
+  // ---- finalize: distance -> density with iso 0.5 (demo 655-680) ----
+  t0 = nowSec();
+  {
+    const float distSqMax = rScan * rScan;
+#pragma omp parallel for schedule(static)
+    for (size_t t = 0; t < activeBlocks.size(); t++) {
+      T *data = sg0->getBlockDataPtr(activeBlocks[t]);
+      for (int v = 0; v < sg0->nVoxelsInBlock(); v++) {
+        float d = Quant<T>::toFloat(data[v]);
+        T q = Quant<T>::fromFloat(0.0f);
+        if (d < 0.999f) {
+          d *= distSqMax;
+          const float dist = sqrtf(d) - rParticle;
+          const float f = 1.0f - MT_LINSTEPF(-rParticle, rParticle + nbDist, dist);
+          q = Quant<T>::fromFloat(f);
+        }
+        data[v] = q;
+      }
+    }
+  }
+  out.tFinalSec = nowSec() - t0;
+
+  const size_t nv = (size_t)sg0->nVoxelsInBlock();
+  std::vector<T> afterFinal(activeBlocks.size() * nv);
+  for (size_t t = 0; t < activeBlocks.size(); t++)
+    memcpy(&afterFinal[t * nv], sg0->getBlockDataPtr(activeBlocks[t]), nv * sizeof(T));
+
+  // ---- the library's sweep (demo 716-727) ----
+  t0 = nowSec();
+  if (job.nIter > 0) {
+    // Colored schedules update in place; the plain ping-pong schedule needs a
+    // temporary channel of the same type.
+    const int chTmp = job.laplTyp < 0 ? (int)MSBG::CH_NULL
+                                      : (sizeof(T) == 4 ? (int)MSBG::CH_FLOAT_2 : (int)MSBG::CH_UINT16_2);
+    msbg->applyChannelPdeFast<T>(chan, chTmp, MSBG::CH_NULL, &activeBlocks, job.laplTyp,
+                                 job.constr01, 0, 0, 0, job.nIter, 1.0f, job.dt, 0, NULL, 0, 0, 0,
+                                 0, job.anisAlpha, 0, 0, 0);
+  }
+  out.tPdeSec = nowSec() - t0;
+
+  std::vector<int8_t> lev8(nBlocks);
+  std::vector<uint16_t> flags(nBlocks);
+  for (int b = 0; b < nBlocks; b++) {
+    lev8[b] = (int8_t)msbg->getBlockInfo(b)->level;
+    flags[b] = msbg->getBlockInfo(b)->flags;
+    if (lev8[b] >= 0 && lev8[b] < 8) out.nBlocksPerLevel[lev8[b]]++;
+  }
+  out.nBlocks = nBlocks;
+  out.elemBytes = (int)sizeof(T);
+  out.nThreadsUsed = omp_get_max_threads();
+
+  fwrite(&out, sizeof(out), 1, fout);
+  fwrite(lev8.data(), 1, nBlocks, fout);
+  fwrite(flags.data(), 2, nBlocks, fout);
+  fwrite(activeBlocks.data(), 4, activeBlocks.size(), fout);
+  fwrite(afterFinal.data(), sizeof(T), afterFinal.size(), fout);
+  for (size_t t = 0; t < activeBlocks.size(); t++)
+    fwrite(sg0->getBlockDataPtr(activeBlocks[t]), sizeof(T), nv, fout);
+
+  MultiresSparseGrid::destroy(msbg);
+  return 0;
+}
+
+// Multi-level layout: regularizeRefinementMap then setRefinementMap on the full
+// (non-single-level) grid; dumps the per-block level and BlockInfo flags.
+int runLevelsJob(const OracleJobHeader &job, const int32_t *levelsIn, FILE *fout) {
+  OracleOutHeader out;
+  memset(&out, 0, sizeof(out));
+  memcpy(out.magic, ORACLE_OUT_MAGIC, 8);
+  MultiresSparseGrid *msbg = MultiresSparseGrid::create(
+      "TEST", job.sx, job.sy, job.sz, job.bsx, -1, 0, -1, 0, NULL, NULL, job.nLevels);
+  if (!msbg) return 2;
+  const int nBlocks = msbg->nBlocks();
+  if ((int64_t)nBlocks != job.nBlocksIn) return 4;
+  std::vector<int> levels(levelsIn, levelsIn + nBlocks);
+  double t0 = nowSec();
+  msbg->regularizeRefinementMap(levels.data());
+  msbg->setRefinementMap(levels.data(), NULL, 0, NULL, false, false);
+  out.tLevelsSec = nowSec() - t0;
+  std::vector<int8_t> lev8(nBlocks);
+  std::vector<uint16_t> flags(nBlocks);
+  for (int b = 0; b < nBlocks; b++) {
+    lev8[b] = (int8_t)levels[b];
+    flags[b] = msbg->getBlockInfo(b, 0)->flags;
+    if (levels[b] >= 0 && levels[b] < 8) out.nBlocksPerLevel[levels[b]]++;
+  }
+  out.nBlocks = nBlocks;
+  out.nThreadsUsed = omp_get_max_threads();
+  fwrite(&out, sizeof(out), 1, fout);
+  fwrite(lev8.data(), 1, nBlocks, fout);
+  fwrite(flags.data(), 2, nBlocks, fout);
+  MultiresSparseGrid::destroy(msbg);
+  return 0;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+  if (argc != 3) {
+    fprintf(stderr, "usage: %s job.bin out.bin\n", argv[0]);
+    return 1;
+  }
+  FILE *fin = fopen(argv[1], "rb");
+  if (!fin) return 1;
+  OracleJobHeader job;
+  if (fread(&job, sizeof(job), 1, fin) != 1 || memcmp(job.magic, ORACLE_JOB_MAGIC, 8) != 0) {
+    fprintf(stderr, "bad job file\n");
+    return 1;
+  }
+  std::vector<float> pts((size_t)job.nPoints * 3);
+  std::vector<int32_t> lv((size_t)job.nBlocksIn);
+  if (job.nPoints && fread(pts.data(), 4, pts.size(), fin) != pts.size()) return 1;
+  if (job.nBlocksIn && fread(lv.data(), 4, lv.size(), fin) != lv.size()) return 1;
+  fclose(fin);
+
+  if (job.nThreads > 0) {
+    omp_set_num_threads(job.nThreads);
+  }
+  ThrInit();
+  nMaxThreads = omp_get_max_threads();
+
+  FILE *fout = fopen(argv[2], "wb");
+  if (!fout) return 1;
+  int rc;
+  if (job.jobType == ORACLE_JOB_LEVELS)
+    rc = runLevelsJob(job, lv.data(), fout);
+  else if (job.chanType == ORACLE_CHAN_U16)
+    rc = runSurfaceJob<uint16_t>(job, pts.data(), job.nBlocksIn ? lv.data() : nullptr, fout);
+  else
+    rc = runSurfaceJob<float>(job, pts.data(), job.nBlocksIn ? lv.data() : nullptr, fout);
+  fclose(fout);
+  return rc;
+}

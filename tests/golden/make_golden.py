@@ -1,0 +1,107 @@
+"""Regenerates the golden fixtures of tests/golden/ from the MSBG reference itself.
+
+The reference library is compiled from its own sources by ``make -C oracle ref``
+(x86-64 only) and driven by oracle/_ref/msbg_ref_driver, which runs the demo's
+marking/splat/finalize loops and the library's regularizeRefinementMap,
+setRefinementMap and applyChannelPdeFast<T> (see oracle/ref_driver.cpp).
+This script needs the reference sources, so it runs in the build container,
+never on the GPU host; the .npz files it writes are committed.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle_io as O  # noqa: E402
+
+OPT8 = 1 << 29
+RES, BSX = 64, 16
+
+
+def golden_points() -> np.ndarray:
+    """Two seeded spheres (radii 9 and 12 voxels) in a 64^3 grid, 1500 points each."""
+    rng = np.random.Generator(np.random.PCG64(20261203 + 900))
+    out = []
+    for c, r in (((22.3, 25.1, 30.7), 9.0), ((40.2, 37.9, 33.4), 12.0)):
+        d = rng.standard_normal((1500, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        out.append(np.asarray(c) + r * d + rng.normal(0, 0.1, (1500, 3)))
+    return np.concatenate(out).astype(np.float32)
+
+
+# (name, storage, laplTyp, numIter, dt, anisAlpha)
+SWEEP_CASES = [
+    ("mcf8_f32", O.CHAN_F32, -(4 + OPT8), 4, 0.1, 0.0),
+    ("mcf8_u16_odd", O.CHAN_U16, -(4 + OPT8), 5, 0.1, 0.0),
+    ("jacobi_rb_f32", O.CHAN_F32, -17, 3, 0.1, 0.0),
+    ("jacobi_pp_f32_odd", O.CHAN_F32, 17, 3, 0.1, 0.0),
+    ("diff_pp_f32", O.CHAN_F32, 3, 2, 0.2, 0.0),
+    ("lapl8_f32", O.CHAN_F32, -(1 + OPT8), 2, 0.1, 0.0),
+    ("pmj8_f32", O.CHAN_F32, -(15 + OPT8), 2, 0.1, 0.2),
+]
+
+
+def main() -> None:
+    if not O.ref_available():
+        raise SystemExit("oracle/_ref/msbg_ref_driver missing: run `make -C oracle ref` first")
+    pts = golden_points()
+    out = {"points": pts, "res": np.int32(RES), "bsx": np.int32(BSX)}
+    for name, chan, lt, it, dt, al in SWEEP_CASES:
+        r = O.run_reference_surface(O.SurfaceJob(RES, RES, RES, BSX, pts, chan=chan, n_iter=it,
+                                                 lapl_typ=lt, dt=dt, anis_alpha=al))
+        if "levels" not in out:
+            out["levels"] = r.levels
+            out["flags"] = r.flags
+            out["active_bids"] = r.active_bids
+            out["n_act_particles"] = np.int64(r.n_act_particles)
+        else:
+            assert np.array_equal(out["levels"], r.levels)
+        if chan == O.CHAN_F32 and "final_f32" not in out:
+            out["final_f32"] = r.after_finalize
+        if chan == O.CHAN_U16 and "final_u16" not in out:
+            out["final_u16"] = r.after_finalize
+        out[f"pde_{name}"] = r.after_pde
+        out[f"meta_{name}"] = np.array([chan, lt, it, dt, al], np.float64)
+
+    # abort rule: a fifth of the active blocks forced to level 1
+    nb = (RES // BSX) ** 3
+    lv = out["levels"].astype(np.int32).copy()
+    rng = np.random.Generator(np.random.PCG64(20261203 + 901))
+    act = np.nonzero(lv == 0)[0]
+    lv[rng.choice(act, max(1, len(act) // 5), replace=False)] = 1
+    r = O.run_reference_surface(O.SurfaceJob(RES, RES, RES, BSX, pts, chan=O.CHAN_F32, n_iter=2,
+                                             dt=0.1, levels=lv))
+    out["abort_levels_in"] = lv
+    out["abort_levels"] = r.levels
+    out["abort_active_bids"] = r.active_bids
+    out["abort_final_f32"] = r.after_finalize
+    out["abort_pde_f32"] = r.after_pde
+    assert nb == lv.size
+
+    # multi-level refinement maps (regularize + BlockInfo flags), 8^3 blocks
+    for nl in (3, 4):
+        rng = np.random.Generator(np.random.PCG64(20261203 + 910 + nl))
+        u = rng.random(8 ** 3)
+        lv = np.where(u < 0.04, 0, np.where(u < 0.10, 1, nl - 1)).astype(np.int32)
+        r = O.run_reference_levels(8 * BSX, 8 * BSX, 8 * BSX, BSX, nl, lv)
+        out[f"lvl{nl}_in"] = lv
+        out[f"lvl{nl}_out"] = r.levels
+        out[f"lvl{nl}_flags"] = r.flags
+        out[f"lvl{nl}_per_level"] = r.blocks_per_level
+
+    path = os.path.join(HERE, "reference_small.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
+
+
+if __name__ == "__main__":
+    main()

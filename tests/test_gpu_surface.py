@@ -1,0 +1,223 @@
+"""GPU parity: the sm_103a library, called through its C ABI, against the CPU
+oracles on identical seeded inputs.
+
+* Against the reference's golden vectors (tests/golden): integer outputs bit for
+  bit, fields within relative L2 1e-5.
+* Against the CPU restatement: integer outputs bit for bit; FP32 / uint16 /
+  FP16 / FP64 fields of the EXACT sweep variant bit for bit (same expression
+  order, every operation rounded once); the FAST variant within rel-L2 1e-5.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from msbg_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-5
+OPT8 = 1 << 29
+MCF8 = -(4 + OPT8)
+GOLDEN_NAMES = ["mcf8_f32", "mcf8_u16_odd", "jacobi_rb_f32", "jacobi_pp_f32_odd", "diff_pp_f32",
+                "lapl8_f32", "pmj8_f32"]
+
+
+def _gpu_pipeline(gpulib, pts, res, bsx, storage, n_iter, lapl_typ, dt, alpha=0.0, variant=0,
+                  levels_in=None, bands=None, n_levels=3):
+    G = gpulib
+    sx, sy, sz = (res, res, res) if np.isscalar(res) else res
+    g = G.MultiresSparseGrid(sx, sy, sz, bsx, n_levels, storage)
+    try:
+        d = g.to_device(np.ascontiguousarray(pts, np.float32))
+        n = len(pts)
+        if bands is not None:
+            g.levels_from_bands(d, n, bands)
+        else:
+            g.mark_points(d, n, 4.0)
+            g.levels_from_marks()
+        if levels_in is not None:
+            g.set_levels(levels_in)
+        g.regularizeRefinementMap()
+        g.setRefinementMap(1.0)
+        g.splat(d, n, 2.0, 2.0)
+        g.splat_finalize(2.0, 2.0)
+        fin = g.payload(0)
+        if n_iter:
+            g.applyChannelPdeFast(0, lapl_typ, 1, n_iter, dt, alpha, variant)
+        out = dict(levels=g.levels(), flags=g.flags(), bids=g.active_blocks(), final=fin,
+                   pde=g.payload(0), info=g.info(), launches=g.launch_count())
+        d.free()
+        return out
+    finally:
+        g.close()
+
+
+def _as_bits(a):
+    a = np.asarray(a)
+    return a.view(np.uint16) if a.dtype == np.float16 else a
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_gpu_matches_reference_golden_and_port(gpulib, port, golden, name):
+    chan, lt, it, dt, al = golden[f"meta_{name}"]
+    storage = gpulib.F32 if int(chan) == 0 else gpulib.U16
+    res, bsx = int(golden["res"]), int(golden["bsx"])
+    r = _gpu_pipeline(gpulib, golden["points"], res, bsx, storage, int(it), int(lt), float(dt), float(al))
+    assert np.array_equal(r["levels"], golden["levels"])
+    assert np.array_equal(r["flags"], golden["flags"])
+    assert np.array_equal(r["bids"], golden["active_bids"])
+    assert r["info"].nActParticles == int(golden["n_act_particles"])
+    want = golden[f"pde_{name}"]
+    to_f = (lambda a: a) if storage == gpulib.F32 else (lambda a: port.to_float(port.U16, a))
+    assert rel_l2(to_f(r["pde"]), to_f(want)) <= REL_TOL
+    # bit-exact against the CPU restatement
+    p = port.surface_pipeline(golden["points"], res, bsx, storage=storage, n_iter=int(it),
+                              lapl_typ=int(lt), dt=float(dt), anis_alpha=float(al))
+    assert np.array_equal(r["final"], p.after_finalize)
+    assert np.array_equal(r["pde"], p.after_pde)
+    assert r["launches"] > 0
+
+
+def test_gpu_abort_rule(gpulib, port, golden):
+    res, bsx = int(golden["res"]), int(golden["bsx"])
+    r = _gpu_pipeline(gpulib, golden["points"], res, bsx, gpulib.F32, 2, MCF8, 0.1,
+                      levels_in=golden["abort_levels_in"])
+    assert np.array_equal(r["levels"], golden["abort_levels"])
+    assert np.array_equal(r["bids"], golden["abort_active_bids"])
+    assert rel_l2(r["final"], golden["abort_final_f32"]) <= REL_TOL
+    assert rel_l2(r["pde"], golden["abort_pde_f32"]) <= REL_TOL
+    p = port.surface_pipeline(golden["points"], res, bsx, storage=port.F32, n_iter=2, dt=0.1,
+                              levels_in=golden["abort_levels_in"])
+    assert r["info"].nAborted == p.n_aborted > 0
+    assert np.array_equal(r["final"], p.after_finalize)
+    assert np.array_equal(r["pde"], p.after_pde)
+
+
+@pytest.mark.parametrize("nl", [3, 4])
+def test_gpu_refinement_map_golden(gpulib, golden, nl):
+    g = gpulib.MultiresSparseGrid(128, 128, 128, 16, nl, gpulib.F32)
+    try:
+        g.set_levels(golden[f"lvl{nl}_in"])
+        g.regularizeRefinementMap()
+        g.setRefinementMap(0.0)
+        assert np.array_equal(g.levels(), golden[f"lvl{nl}_out"])
+        fl = g.flags()
+        # the demo's allocation loop adds BLK_EXISTS to level-0 blocks afterwards
+        assert np.array_equal(fl & ~np.uint16(gpulib.BLK_EXISTS), golden[f"lvl{nl}_flags"])
+        assert np.array_equal((fl & gpulib.BLK_EXISTS) != 0, golden[f"lvl{nl}_out"] == 0)
+        per = np.array(g.info().blocksPerLevel[:])
+        assert np.array_equal(per, golden[f"lvl{nl}_per_level"])
+    finally:
+        g.close()
+
+
+@pytest.mark.parametrize("storage", ["F32", "U16", "F16", "F64"])
+@pytest.mark.parametrize("bsx", [16, 32])
+def test_gpu_vs_port_seeded(gpulib, port, storage, bsx):
+    res = 256
+    pts = W.sphere_cloud(res, 12, 6000, seed=W.workload_seed(1, 50 + bsx))
+    st = getattr(gpulib, storage)
+    r = _gpu_pipeline(gpulib, pts, res, bsx, st, 4, MCF8, 0.1)
+    p = port.surface_pipeline(pts, res, bsx, storage=getattr(port, storage), n_iter=4, dt=0.1)
+    assert np.array_equal(r["levels"], p.levels)
+    assert np.array_equal(r["flags"], p.flags)
+    assert np.array_equal(r["bids"], p.active_bids)
+    assert np.array_equal(_as_bits(r["final"]), _as_bits(p.after_finalize))
+    assert np.array_equal(_as_bits(r["pde"]), _as_bits(p.after_pde))
+
+
+def test_gpu_fast_variant_within_tolerance(gpulib, port):
+    res = 256
+    pts = W.sphere_cloud(res, 12, 6000, seed=W.workload_seed(1, 77))
+    r = _gpu_pipeline(gpulib, pts, res, 16, gpulib.F32, 20, MCF8, 0.1, variant=gpulib.SWEEP_FAST)
+    p = port.surface_pipeline(pts, res, 16, storage=port.F32, n_iter=20, dt=0.1)
+    assert np.array_equal(r["bids"], p.active_bids)
+    err = rel_l2(r["pde"], p.after_pde)
+    assert err <= REL_TOL, err
+    moved = rel_l2(p.after_pde, p.after_finalize)
+    assert moved > 100 * REL_TOL  # the sweeps really changed the field
+
+
+def test_gpu_band_levels_vs_port(gpulib, port):
+    res = 512
+    pts = W.ellipsoid_cloud(res, 20, 3000, seed=W.workload_seed(2, 5), axis_range=(0.02, 0.08))
+    r = _gpu_pipeline(gpulib, pts, res, 32, gpulib.F16, 2, MCF8, 0.1, bands=(8.0, 16.0))
+    p = port.surface_pipeline(pts, res, 32, storage=port.F16, n_iter=2, dt=0.1, bands=(8.0, 16.0))
+    assert np.array_equal(r["levels"], p.levels)
+    assert set(np.unique(r["levels"])) == {0, 1, 2}
+    assert np.array_equal(r["bids"], p.active_bids)
+    assert np.array_equal(_as_bits(r["pde"]), _as_bits(p.after_pde))
+
+
+def test_gpu_empty_and_out_of_domain_points(gpulib):
+    pts = np.array([[-5.0, 3.0, 3.0], [70.0, 1.0, 1.0], [0.001, 30.0, 30.0]], np.float32)
+    r = _gpu_pipeline(gpulib, pts, 64, 16, gpulib.F32, 2, MCF8, 0.1)
+    assert r["info"].nActParticles == 0
+    assert len(r["bids"]) == 0
+    r = _gpu_pipeline(gpulib, np.zeros((0, 3), np.float32), 64, 16, gpulib.F32, 2, MCF8, 0.1)
+    assert len(r["bids"]) == 0
+
+
+def test_gpu_domain_boundary_neumann(gpulib, port):
+    # a sphere that crosses the domain faces: marks clamp to the grid, the halo
+    # falls back to the Neumann clamp outside the domain
+    rng = np.random.Generator(np.random.PCG64(99))
+    d = rng.standard_normal((4000, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    pts = (np.array([3.0, 60.0, 32.0]) + 10.0 * d).astype(np.float32)
+    r = _gpu_pipeline(gpulib, pts, 64, 16, gpulib.F32, 4, MCF8, 0.1)
+    p = port.surface_pipeline(pts, 64, 16, storage=port.F32, n_iter=4, dt=0.1)
+    assert r["info"].nActParticles == p.n_act_particles < len(pts)
+    assert np.array_equal(r["bids"], p.active_bids)
+    assert np.array_equal(r["pde"], p.after_pde)
+
+
+def test_gpu_surface_job_entry_point(gpulib):
+    res = 128
+    pts = W.sphere_cloud(res, 6, 3000, seed=W.workload_seed(1, 11))
+    step = _gpu_pipeline(gpulib, pts, res, 16, gpulib.F32, 6, MCF8, 0.1)
+    g = gpulib.MultiresSparseGrid(res, res, res, 16, 3, gpulib.F32)
+    try:
+        out = np.empty((res // 16) ** 3 * 16 ** 3, np.float32)
+        n = g.surface_job(pts, numIter=6, timeStep=0.1, out=out)
+        assert n == len(step["bids"])
+        assert np.array_equal(out[: n * 4096].reshape(n, 4096), step["pde"])
+    finally:
+        g.close()
+
+
+def test_gpu_error_codes(gpulib):
+    G = gpulib
+    with pytest.raises(G.MsbgGpuError) as e:
+        G.MultiresSparseGrid(100, 64, 64, 16)
+    with pytest.raises(G.MsbgGpuError) as e:
+        G.MultiresSparseGrid(64, 64, 64, 12)
+    g = G.MultiresSparseGrid(64, 64, 64, 16, 3, G.F32, capacity_blocks=2)
+    try:
+        with pytest.raises(G.MsbgGpuError) as e:
+            g.applyChannelPdeFast(0, MCF8, 1, 2, 0.1)
+        assert e.value.code == G.ERR_STATE
+        pts = W.sphere_cloud(64, 2, 2000, seed=5, radius_range=(0.15, 0.2))
+        d = g.to_device(pts)
+        g.mark_points(d, len(pts), 4.0)
+        g.levels_from_marks()
+        with pytest.raises(G.MsbgGpuError) as e:
+            g.setRefinementMap(1.0)
+        assert e.value.code == G.ERR_CAPACITY
+        d.free()
+    finally:
+        g.close()
+    g = G.MultiresSparseGrid(64, 64, 64, 16, 3, G.F32)
+    try:
+        g.set_levels(np.zeros(64, np.int32))
+        g.setRefinementMap(0.5)
+        with pytest.raises(G.MsbgGpuError) as e:
+            g.applyChannelPdeFast(0, -(2 + OPT8), 1, 2, 0.1)
+        assert e.value.code == G.ERR_UNSUPPORTED
+        with pytest.raises(G.MsbgGpuError) as e:
+            g.set_levels(np.full(64, 7, np.int32))
+        assert e.value.code == G.ERR_ARG
+    finally:
+        g.close()
