@@ -120,6 +120,7 @@ __global__ void __launch_bounds__(256) kSplat(const float *__restrict__ pts, int
     if (d2 > g.distSqMax) continue;
     const int64_t b = (int64_t)(iz >> s) * nxy + (int64_t)(iy >> s) * g.nbx + (ix >> s);
     const int sl = slot[b];
+    if (sl < 0) continue;  // unreachable: an earlier in-sphere voxel would have set abortAt
     const int vid = ((iz & mask) << (2 * s)) + ((iy & mask) << s) + (ix & mask);
     const float q = __fmul_rn(d2, g.distSqMaxInv);
     atomicMin((int *)(dst + (int64_t)sl * vpb + vid), __float_as_int(q));
