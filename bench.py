@@ -204,7 +204,7 @@ def cpu_sample(spec: dict, pts: np.ndarray, target_sec: float = 10.0, max_blocks
 def run_reference(args, spec, dist: Dist):
     if dist.rank != 0:
         return
-    pts = W.make_points(spec, 2 if spec is W.SURFACE_4096 else 1)
+    pts = W.make_points(spec, 1 if spec is W.SURFACE_512 else 2)
     arch = platform.machine()
     ref_driver = os.path.join(ROOT, "oracle", "_ref", "msbg_ref_driver")
     kind = "port"
@@ -254,7 +254,7 @@ def run_gpu(args, spec, dist: Dist):
     elem = 2 if storage == G.F16 else 4
     variant = G.SWEEP_FAST if args.variant == "fast" else G.SWEEP_EXACT
     n_iter = spec["n_iter"]
-    pts = W.make_points(spec, 2 if spec is W.SURFACE_4096 else 1)
+    pts = W.make_points(spec, 1 if spec is W.SURFACE_512 else 2)
     bands = (spec["fine_band"], spec["mid_band"]) if "fine_band" in spec else None
     res, bsx = spec["res"], spec["bsx"]
 
@@ -372,7 +372,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="surface4096", choices=["surface4096", "surface512"])
+    ap.add_argument("--workload", default="surface4096",
+                    choices=["surface4096", "surface4096-crop", "surface512"])
     ap.add_argument("--variant", default="fast", choices=["fast", "exact"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -380,7 +381,8 @@ def main():
     ap.add_argument("--traffic-per-launch", type=float, default=None,
                     help="DRAM bytes per sweep launch from an ncu capture (reported as roofline.traffic)")
     args = ap.parse_args()
-    spec = W.SURFACE_4096 if args.workload == "surface4096" else W.SURFACE_512
+    spec = {"surface4096": W.SURFACE_4096, "surface4096-crop": W.SURFACE_4096_CROP,
+            "surface512": W.SURFACE_512}[args.workload]
     dist = Dist()
     try:
         if args.impl == "reference":

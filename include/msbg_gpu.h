@@ -44,7 +44,8 @@ enum {
   MSBG_GPU_ERR_CAPACITY = -5,    /* block pool exhausted                        */
   MSBG_GPU_ERR_NONFINITE = -6,   /* a reduction met NaN/Inf (src/msbg.cpp:4635) */
   MSBG_GPU_ERR_DIVERGED = -7,    /* solver residual non-finite or increasing    */
-  MSBG_GPU_ERR_UNSUPPORTED = -8  /* option the GPU path does not implement      */
+  MSBG_GPU_ERR_UNSUPPORTED = -8, /* option the GPU path does not implement      */
+  MSBG_GPU_ERR_TIMEOUT = -9      /* a bounded device-side wait gave up          */
 };
 
 /* ---- storage types of a channel ------------------------------------------ */

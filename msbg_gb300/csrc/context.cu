@@ -373,11 +373,13 @@ extern "C" int msbg_gpu_create(msbg_gpu_ctx **out, int sx, int sy, int sz, int b
   ALLOC(ctx->dColorBids, nB * 4);
   ALLOC(ctx->dScanPartial, (size_t)nPart * 8);
   ALLOC(ctx->dCounters, 16 * 8);
+  ALLOC(ctx->dStatus, 16);
 #undef ALLOC
   if (e == cudaSuccess) e = cudaMallocHost((void **)&ctx->hCounters, 16 * 8);
   for (int i = 0; i < kMaxEvents && e == cudaSuccess; i++) e = cudaEventCreate(&ctx->ev[i]);
   if (e == cudaSuccess) e = cudaMemset(ctx->dMark, 0, nB * 4);
   if (e == cudaSuccess) e = cudaMemset(ctx->dCounters, 0, 16 * 8);
+  if (e == cudaSuccess) e = cudaMemset(ctx->dStatus, 0, 16);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e != cudaSuccess) {
     msbg_gpu_destroy(ctx);
@@ -394,9 +396,12 @@ extern "C" int msbg_gpu_destroy(msbg_gpu_ctx *ctx) {
   cudaStreamSynchronize(ctx->stream);
   cudaFree(ctx->dMark); cudaFree(ctx->dLevels); cudaFree(ctx->dLevelsTmp); cudaFree(ctx->dFlags);
   cudaFree(ctx->dSlot); cudaFree(ctx->dActive); cudaFree(ctx->dColorBids);
-  cudaFree(ctx->dScanPartial); cudaFree(ctx->dCounters);
+  cudaFree(ctx->dScanPartial); cudaFree(ctx->dCounters); cudaFree(ctx->dStatus);
   if (ctx->hCounters) cudaFreeHost(ctx->hCounters);
-  for (auto &c : ctx->ch) if (c.d) cudaFree(c.d);
+  for (auto &c : ctx->ch) {
+    if (c.d) cudaFree(c.d);
+    if (c.cache) cudaFree(c.cache);
+  }
   if (ctx->dTmpSlab) cudaFree(ctx->dTmpSlab);
   if (ctx->dPts) cudaFree(ctx->dPts);
   for (auto &ev : ctx->ev) if (ev) cudaEventDestroy(ev);

@@ -20,6 +20,8 @@ struct Channel {
   int storage = MSBG_GPU_F32;
   void *d = nullptr;      // [capacity][bs^3]
   size_t capBlocks = 0;   // blocks the slab can hold
+  void *cache = nullptr;  // x-face + corner-column cache of the colored sweeps
+  size_t cacheBytes = 0;
 };
 
 }  // namespace msbg
@@ -46,6 +48,7 @@ struct msbg_gpu_ctx {
   int64_t *dScanPartial = nullptr; // scan scratch
   int64_t *dCounters = nullptr;  // [8]: 0 nActParticles, 1 nAborted, 2 nActive, 3.. color counts
   int64_t *hCounters = nullptr;  // pinned mirror
+  int *dStatus = nullptr;        // device-side error bits (bounded waits that gave up)
   bool layoutValid = false;
   int64_t nActive = 0;
   int32_t colorStart[9] = {};

@@ -65,9 +65,14 @@ __global__ void __launch_bounds__(256) kSplat(const float *__restrict__ pts, int
   if (px < g.domMin[0] || px > g.domMax[0] || py < g.domMin[1] || py > g.domMax[1] ||
       pz < g.domMin[2] || pz > g.domMax[2])
     return;
+  const int s = g.log2bs, mask = (1 << s) - 1;
+  const int64_t nxy = (int64_t)g.nbx * g.nby;
   {
     const int ix = (int)px, iy = (int)py, iz = (int)pz;
     if (ix < 0 || ix >= g.sx || iy < 0 || iy >= g.sy || iz < 0 || iz >= g.sz) return;
+    // the demo walks the particle lists of value blocks only
+    // (src/msbg_demo.cpp:541-566): a particle owned by a non-value block is never splatted
+    if (slot[(int64_t)(iz >> s) * nxy + (int64_t)(iy >> s) * g.nbx + (ix >> s)] < 0) return;
   }
   const float r = g.rScan;
   const int ix1 = max((int)ceilf(__fsub_rn(__fsub_rn(px, r), 0.5f)), 0);
@@ -79,8 +84,6 @@ __global__ void __launch_bounds__(256) kSplat(const float *__restrict__ pts, int
   const int nx = ix2 - ix1 + 1, ny = iy2 - iy1 + 1, nz = iz2 - iz1 + 1;
   if (nx <= 0 || ny <= 0 || nz <= 0) return;
   const float x0 = __fsub_rn(px, 0.5f), y0 = __fsub_rn(py, 0.5f), z0 = __fsub_rn(pz, 0.5f);
-  const int s = g.log2bs, mask = (1 << s) - 1;
-  const int64_t nxy = (int64_t)g.nbx * g.nby;
   const int64_t vpb = (int64_t)1 << (3 * s);
 
   // blocks touched by the box (<= 2 per axis)

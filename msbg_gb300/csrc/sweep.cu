@@ -7,148 +7,26 @@
 // reads blocks of other colors (same-color blocks are never 26-neighbours), and
 // its own voxels are read before they are written.
 //
-// Kernel: one CTA per block of the pass.  The CTA marches through the block in
+// The in-place schedules of FP32/FP16/uint16 channels run the streaming kernel
+// of sweep_color.cu; this file's gather kernel serves the ping-pong schedule and
+// FP64 channels.
+//
+// Gather kernel: one CTA per block of the pass.  The CTA marches through the block in
 // z with a ring of three halo'd planes ((bs+2)^2 values each, compute type) in
 // shared memory: plane z+1 is gathered (own block, neighbour blocks, the
 // constant empty value for non-value blocks, Neumann clamp outside the domain),
 // then plane z is computed from planes z-1..z+1 and stored in place.  A plane of
 // the own block is always in shared memory before the store that overwrites it.
 #include "internal.cuh"
+#include "sweep_common.cuh"
 
 namespace msbg {
-
-enum { K_MCF = 4, K_JACOBI = 17, K_PM_JACOBI = 15, K_PM = 14, K_DIFF = 3, K_LAPL = 1 };
 
 struct SweepGeom {
   int sx, sy, sz, nbx, nby;
   double emptyValue;
-  int kind, constr01;
-  float dt, anisAlpha;
+  SweepParams p;
 };
-
-// Correctly rounded scalar ops; no contraction, so results follow the written
-// expression order exactly (the reference's and the CPU restatement's).
-template <typename R> struct Op;
-template <> struct Op<float> {
-  static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
-  static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
-  static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
-  static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
-  static __device__ __forceinline__ float sqrt_(float a) { return __fsqrt_rn(a); }
-};
-template <> struct Op<double> {
-  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
-  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
-  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
-  static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
-  static __device__ __forceinline__ double sqrt_(double a) { return __dsqrt_rn(a); }
-};
-
-// Mean curvature flow update, laplTyp 4 (src/msbg4.cpp:559-637), in the
-// reference's expression order.  P(dx,dy,dz) reads the halo'd planes.
-template <typename R, typename P>
-__device__ __forceinline__ R mcfExact(const P &F, R dt) {
-  using O = Op<R>;
-  const R h = (R)0.5, two = (R)2;
-  const R f0 = F(0, 0, 0), f1 = F(-1, 0, 0), f2 = F(1, 0, 0), f3 = F(0, -1, 0), f4 = F(0, 1, 0),
-          f5 = F(0, 0, -1), f6 = F(0, 0, 1);
-  const R fx = O::mul(h, O::sub(f2, f1)), fy = O::mul(h, O::sub(f4, f3)), fz = O::mul(h, O::sub(f6, f5));
-  const R f02 = O::mul(two, f0);
-  const R fxx = O::sub(O::add(f1, f2), f02), fyy = O::sub(O::add(f3, f4), f02),
-          fzz = O::sub(O::add(f5, f6), f02);
-  const R fy_r = O::mul(O::sub(F(1, 1, 0), F(1, -1, 0)), h);
-  const R fy_l = O::mul(O::sub(F(-1, 1, 0), F(-1, -1, 0)), h);
-  const R fz_r = O::mul(O::sub(F(1, 0, 1), F(1, 0, -1)), h);
-  const R fz_l = O::mul(O::sub(F(-1, 0, 1), F(-1, 0, -1)), h);
-  const R fz_u = O::mul(O::sub(F(0, 1, 1), F(0, 1, -1)), h);
-  const R fz_d = O::mul(O::sub(F(0, -1, 1), F(0, -1, -1)), h);
-  const R fyx = O::mul(O::sub(fy_r, fy_l), h), fzx = O::mul(O::sub(fz_r, fz_l), h),
-          fzy = O::mul(O::sub(fz_u, fz_d), h);
-  const R xx = O::mul(fx, fx), yy = O::mul(fy, fy), zz = O::mul(fz, fz);
-  R H = O::add(O::add(O::mul(O::add(yy, zz), fxx), O::mul(O::add(xx, zz), fyy)), O::mul(O::add(xx, yy), fzz));
-  const R cross = O::add(O::add(O::mul(O::mul(fx, fy), fyx), O::mul(O::mul(fx, fz), fzx)),
-                         O::mul(O::mul(fy, fz), fzy));
-  H = O::sub(H, O::mul(two, cross));
-  const R g2 = O::add(O::add(xx, yy), zz);
-  H = g2 > (R)1e-7f ? O::div(H, g2) : (R)0;
-  R D = O::mul(dt, H);
-  D = D < (R)-0.1f ? (R)-0.1f : D;
-  D = D > (R)0.1f ? (R)0.1f : D;
-  return O::add(f0, D);
-}
-
-// Same PDE, re-associated for fused multiply-adds (float only).  Uses unscaled
-// central differences g = 2*f_x and G = 4*f_xy:
-//   H |grad|^2 = |g|^2 lap/4 - (gx^2 fxx + gy^2 fyy + gz^2 fzz)/4 - (gx gy Gyx + ...)/8
-// with |grad|^2 = |g|^2/4.
-template <typename P>
-__device__ __forceinline__ float mcfFast(const P &F, float dt) {
-  const float f0 = F(0, 0, 0), f1 = F(-1, 0, 0), f2 = F(1, 0, 0), f3 = F(0, -1, 0), f4 = F(0, 1, 0),
-              f5 = F(0, 0, -1), f6 = F(0, 0, 1);
-  const float gx = f2 - f1, gy = f4 - f3, gz = f6 - f5;
-  const float fxx = fmaf(-2.0f, f0, f1 + f2), fyy = fmaf(-2.0f, f0, f3 + f4),
-              fzz = fmaf(-2.0f, f0, f5 + f6);
-  const float Gyx = (F(1, 1, 0) - F(1, -1, 0)) - (F(-1, 1, 0) - F(-1, -1, 0));
-  const float Gzx = (F(1, 0, 1) - F(1, 0, -1)) - (F(-1, 0, 1) - F(-1, 0, -1));
-  const float Gzy = (F(0, 1, 1) - F(0, 1, -1)) - (F(0, -1, 1) - F(0, -1, -1));
-  const float xx = gx * gx, yy = gy * gy, zz = gz * gz;
-  const float g2 = xx + yy + zz;  // 4 |grad f|^2
-  const float lap = fxx + fyy + fzz;
-  const float s = fmaf(xx, fxx, fmaf(yy, fyy, zz * fzz));
-  const float n1 = fmaf(g2, lap, -s);                         // 4 * (first part)
-  const float n2 = fmaf(gx, fmaf(gy, Gyx, gz * Gzx), gy * gz * Gzy);  // 16 * cross
-  // H = (n1/4 - n2/8) / (g2/4) = (n1 - n2/2) / g2
-  const float Hn = fmaf(-0.5f, n2, n1);
-  float H = g2 > 4e-7f ? __fdividef(Hn, g2) : 0.0f;
-  float D = fminf(fmaxf(dt * H, -0.1f), 0.1f);
-  return f0 + D;
-}
-
-// 7-point kernels (src/msbg4.cpp:681-805).
-template <typename R, typename P>
-__device__ __forceinline__ R stencil7(const P &F, const SweepGeom &g) {
-  using O = Op<R>;
-  const R dt = (R)g.dt;
-  const R phi = F(0, 0, 0);
-  const R F1 = F(-1, 0, 0), F2 = F(1, 0, 0), F3 = F(0, -1, 0), F4 = F(0, 1, 0), F5 = F(0, 0, -1),
-          F6 = F(0, 0, 1);
-  switch (g.kind) {
-    case K_JACOBI: {
-      const R s6 = O::add(O::add(O::add(O::add(O::add(F1, F2), F3), F4), F5), F6);
-      return O::div(O::add(phi, O::mul(dt, s6)), O::add((R)1, O::mul(dt, (R)6)));
-    }
-    case K_DIFF: {
-      const R s6 = O::add(O::add(O::add(O::add(O::add(F1, F2), F3), F4), F5), F6);
-      const R S = O::mul((R)1 / (R)6, s6);
-      return O::add(phi, O::mul(dt, O::sub(S, phi)));
-    }
-    case K_LAPL: {
-      const R s6 = O::add(O::add(O::add(O::add(O::add(F1, F2), F3), F4), F5), F6);
-      const R L = O::sub(s6, O::mul((R)6, phi));
-      const R GX = O::mul((R)0.5, O::sub(F2, F1)), GY = O::mul((R)0.5, O::sub(F4, F3)),
-              GZ = O::mul((R)0.5, O::sub(F6, F5));
-      const R G = O::sqrt_(O::add(O::add(O::mul(GX, GX), O::mul(GY, GY)), O::mul(GZ, GZ)));
-      return O::add(phi, O::mul(O::mul(dt, L), G));
-    }
-    default: {  // K_PM_JACOBI / K_PM, anisAlpha > 0 (src/msbg4.cpp:738-790)
-      const R a = (R)g.anisAlpha;
-      const R fn[6] = {F1, F2, F3, F4, F5, F6};
-      R sum = 0, wsum = 0, dsum = 0;
-#pragma unroll
-      for (int k = 0; k < 6; k++) {
-        const R gk = O::sub(fn[k], phi);
-        const R ag = gk < (R)0 ? -gk : gk;
-        const R t = O::div(ag, a);
-        const R Gk = O::div((R)1, O::add((R)1, O::mul(t, t)));
-        sum = O::add(sum, O::mul(Gk, fn[k]));
-        wsum = O::add(wsum, Gk);
-        dsum = O::add(dsum, O::mul(Gk, gk));
-      }
-      if (g.kind == K_PM_JACOBI) return O::div(O::add(phi, O::mul(dt, sum)), O::add((R)1, O::mul(dt, wsum)));
-      return O::add(phi, O::mul(dt, dsum));
-    }
-  }
-}
 
 template <typename T, typename R>
 __device__ __forceinline__ R loadAs(const T *p) {
@@ -214,14 +92,8 @@ __global__ void __launch_bounds__(256) kSweep(const int32_t *__restrict__ bids, 
         const R *pl = dz < 0 ? pm : dz > 0 ? pp : pc;
         return pl[c + dy * HS + dx];
       };
-      R out;
-      if (g.kind == K_MCF) {
-        if constexpr (EXACT || sizeof(R) == 8) out = mcfExact<R>(F, (R)g.dt);
-        else out = mcfFast(F, g.dt);
-      } else {
-        out = stencil7<R>(F, g);
-      }
-      if (g.constr01) {
+      R out = g.p.kind == K_MCF ? mcfExact<R>(F, (R)g.p.dt) : stencil7<R>(F, g.p);
+      if (g.p.constr01) {
         out = out > (R)0 ? out : (R)0;
         out = out < (R)1 ? out : (R)1;
       }
@@ -292,15 +164,31 @@ int pdeRun(msbg_gpu_ctx *ctx, int chan, int laplTyp, int constr01, int numIter, 
   SweepGeom g;
   g.sx = ctx->sx; g.sy = ctx->sy; g.sz = ctx->sz; g.nbx = ctx->nbx; g.nby = ctx->nby;
   g.emptyValue = 0.0;
-  g.kind = kind;
-  g.constr01 = constr01 ? 1 : 0;
-  g.dt = dt;
-  g.anisAlpha = anisAlpha;
+  g.p.kind = kind;
+  g.p.constr01 = constr01 ? 1 : 0;
+  g.p.dt = dt;
+  g.p.anisAlpha = anisAlpha;
   const int nIter0 = numIter;
   int nIter = numIter;
   if (nIter % 2 == 1) nIter++;  // src/msbg4.cpp:150-152
   const int32_t *cb = ctx->dColorBids;
   const int *cs = ctx->colorStart;
+  if ((color8 || redBlack) && c.storage != MSBG_GPU_F64) {
+    // streaming kernel with the x-face cache (sweep_color.cu)
+    const int rc = colorSweepRun(ctx, c, exact, color8, nIter, g.p);
+    if (rc < 0) return rc;
+    if (rc == 0) {
+      // the streaming kernel's bounded shared-memory waits report through dStatus
+      int st = 0;
+      MSBG_CUDA(ctx, cudaMemcpyAsync(&st, ctx->dStatus, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      if (st) {
+        MSBG_CUDA(ctx, cudaMemsetAsync(ctx->dStatus, 0, sizeof(int), ctx->stream));
+        return fail(ctx, MSBG_GPU_ERR_TIMEOUT, "a sweep CTA gave up waiting for its tile (status %d)", st);
+      }
+      return MSBG_GPU_OK;
+    }
+  }
   if (color8 || redBlack) {
     // red-black pass 0 processes parity-1 blocks, pass 1 parity-0 (src/msbg4.cpp:447-454);
     // parity = popcount(color) & 1

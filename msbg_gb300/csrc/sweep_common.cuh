@@ -1,0 +1,182 @@
+// Per-voxel arithmetic of applyChannelPdeFast (src/msbg4.cpp:559-825), shared by
+// the gather kernel (sweep.cu) and the streaming colored kernel (sweep_color.cu).
+#pragma once
+
+#include "internal.cuh"
+
+namespace msbg {
+
+enum { K_MCF = 4, K_JACOBI = 17, K_PM_JACOBI = 15, K_PM = 14, K_DIFF = 3, K_LAPL = 1 };
+
+struct SweepParams {
+  int kind, constr01;
+  float dt, anisAlpha;
+};
+
+// Correctly rounded scalar ops; no contraction, so results follow the written
+// expression order exactly (the reference's and the CPU restatement's).
+template <typename R> struct Op;
+template <> struct Op<float> {
+  static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+  static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+  static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+  static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+  static __device__ __forceinline__ float sqrt_(float a) { return __fsqrt_rn(a); }
+};
+template <> struct Op<double> {
+  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+  static __device__ __forceinline__ double sqrt_(double a) { return __dsqrt_rn(a); }
+};
+
+// Mean curvature flow update, laplTyp 4 (src/msbg4.cpp:559-637), in the
+// reference's expression order.  F(dx,dy,dz) reads the neighbourhood.
+template <typename R, typename P>
+__device__ __forceinline__ R mcfExact(const P &F, R dt) {
+  using O = Op<R>;
+  const R h = (R)0.5, two = (R)2;
+  const R f0 = F(0, 0, 0), f1 = F(-1, 0, 0), f2 = F(1, 0, 0), f3 = F(0, -1, 0), f4 = F(0, 1, 0),
+          f5 = F(0, 0, -1), f6 = F(0, 0, 1);
+  const R fx = O::mul(h, O::sub(f2, f1)), fy = O::mul(h, O::sub(f4, f3)), fz = O::mul(h, O::sub(f6, f5));
+  const R f02 = O::mul(two, f0);
+  const R fxx = O::sub(O::add(f1, f2), f02), fyy = O::sub(O::add(f3, f4), f02),
+          fzz = O::sub(O::add(f5, f6), f02);
+  const R fy_r = O::mul(O::sub(F(1, 1, 0), F(1, -1, 0)), h);
+  const R fy_l = O::mul(O::sub(F(-1, 1, 0), F(-1, -1, 0)), h);
+  const R fz_r = O::mul(O::sub(F(1, 0, 1), F(1, 0, -1)), h);
+  const R fz_l = O::mul(O::sub(F(-1, 0, 1), F(-1, 0, -1)), h);
+  const R fz_u = O::mul(O::sub(F(0, 1, 1), F(0, 1, -1)), h);
+  const R fz_d = O::mul(O::sub(F(0, -1, 1), F(0, -1, -1)), h);
+  const R fyx = O::mul(O::sub(fy_r, fy_l), h), fzx = O::mul(O::sub(fz_r, fz_l), h),
+          fzy = O::mul(O::sub(fz_u, fz_d), h);
+  const R xx = O::mul(fx, fx), yy = O::mul(fy, fy), zz = O::mul(fz, fz);
+  R H = O::add(O::add(O::mul(O::add(yy, zz), fxx), O::mul(O::add(xx, zz), fyy)), O::mul(O::add(xx, yy), fzz));
+  const R cross = O::add(O::add(O::mul(O::mul(fx, fy), fyx), O::mul(O::mul(fx, fz), fzx)),
+                         O::mul(O::mul(fy, fz), fzy));
+  H = O::sub(H, O::mul(two, cross));
+  const R g2 = O::add(O::add(xx, yy), zz);
+  H = g2 > (R)1e-7f ? O::div(H, g2) : (R)0;
+  R D = O::mul(dt, H);
+  D = D < (R)-0.1f ? (R)-0.1f : D;
+  D = D > (R)0.1f ? (R)0.1f : D;
+  return O::add(f0, D);
+}
+
+// 7-point kernels (src/msbg4.cpp:681-805), reference expression order.
+template <typename R, typename P>
+__device__ __forceinline__ R stencil7(const P &F, const SweepParams &g) {
+  using O = Op<R>;
+  const R dt = (R)g.dt;
+  const R phi = F(0, 0, 0);
+  const R F1 = F(-1, 0, 0), F2 = F(1, 0, 0), F3 = F(0, -1, 0), F4 = F(0, 1, 0), F5 = F(0, 0, -1),
+          F6 = F(0, 0, 1);
+  switch (g.kind) {
+    case K_JACOBI: {
+      const R s6 = O::add(O::add(O::add(O::add(O::add(F1, F2), F3), F4), F5), F6);
+      return O::div(O::add(phi, O::mul(dt, s6)), O::add((R)1, O::mul(dt, (R)6)));
+    }
+    case K_DIFF: {
+      const R s6 = O::add(O::add(O::add(O::add(O::add(F1, F2), F3), F4), F5), F6);
+      const R S = O::mul((R)1 / (R)6, s6);
+      return O::add(phi, O::mul(dt, O::sub(S, phi)));
+    }
+    case K_LAPL: {
+      const R s6 = O::add(O::add(O::add(O::add(O::add(F1, F2), F3), F4), F5), F6);
+      const R L = O::sub(s6, O::mul((R)6, phi));
+      const R GX = O::mul((R)0.5, O::sub(F2, F1)), GY = O::mul((R)0.5, O::sub(F4, F3)),
+              GZ = O::mul((R)0.5, O::sub(F6, F5));
+      const R G = O::sqrt_(O::add(O::add(O::mul(GX, GX), O::mul(GY, GY)), O::mul(GZ, GZ)));
+      return O::add(phi, O::mul(O::mul(dt, L), G));
+    }
+    default: {  // K_PM_JACOBI / K_PM, anisAlpha > 0 (src/msbg4.cpp:738-790)
+      const R a = (R)g.anisAlpha;
+      const R fn[6] = {F1, F2, F3, F4, F5, F6};
+      R sum = 0, wsum = 0, dsum = 0;
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        const R gk = O::sub(fn[k], phi);
+        const R ag = gk < (R)0 ? -gk : gk;
+        const R t = O::div(ag, a);
+        const R Gk = O::div((R)1, O::add((R)1, O::mul(t, t)));
+        sum = O::add(sum, O::mul(Gk, fn[k]));
+        wsum = O::add(wsum, Gk);
+        dsum = O::add(dsum, O::mul(Gk, gk));
+      }
+      if (g.kind == K_PM_JACOBI) return O::div(O::add(phi, O::mul(dt, sum)), O::add((R)1, O::mul(dt, wsum)));
+      return O::add(phi, O::mul(dt, dsum));
+    }
+  }
+}
+
+// Fast MCF of four x-consecutive voxels from a register window W[r][c]
+// (r: y-1..y+1, c: x-1..x+4 of planes z-1 / z / z+1).  Re-associated with fused
+// multiply-adds and shared central differences:
+//   D_y(c) = P0(c,y+1) - P0(c,y-1), D_z(c) = Pp(c,y) - Pm(c,y)
+//   gx = P0(c+1) - P0(c-1),  gy = D_y(c), gz = D_z(c)            (= 2 f_x ...)
+//   Gyx = D_y(c+1) - D_y(c-1), Gzx = D_z(c+1) - D_z(c-1),
+//   Gzy = (Pp(c,y+1) - Pm(c,y+1)) - (Pp(c,y-1) - Pm(c,y-1))        (= 4 f_xy ...)
+//   H = [ (gy^2+gz^2) fxx + (gx^2+gz^2) fyy + (gx^2+gy^2) fzz
+//         - (gx gy Gyx + gx gz Gzx + gy gz Gzy) / 2 ] / |g|^2
+// which is the reference's H with |grad f|^2 = |g|^2 / 4 (threshold 4e-7).
+__device__ __forceinline__ void mcfFastStrip(const float Pm[3][6], const float P0[3][6],
+                                             const float Pp[3][6], float dt, bool clamp01,
+                                             float out[4]) {
+  float Dy[6], Dz[6];
+#pragma unroll
+  for (int c = 0; c < 6; c++) {
+    Dy[c] = P0[2][c] - P0[0][c];
+    Dz[c] = Pp[1][c] - Pm[1][c];
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int c = i + 1;
+    const float f0 = P0[1][c];
+    const float gx = P0[1][c + 1] - P0[1][c - 1], gy = Dy[c], gz = Dz[c];
+    const float fxx = fmaf(-2.0f, f0, P0[1][c - 1] + P0[1][c + 1]);
+    const float fyy = fmaf(-2.0f, f0, P0[0][c] + P0[2][c]);
+    const float fzz = fmaf(-2.0f, f0, Pm[1][c] + Pp[1][c]);
+    const float Gyx = Dy[c + 1] - Dy[c - 1];
+    const float Gzx = Dz[c + 1] - Dz[c - 1];
+    const float Gzy = (Pp[2][c] - Pm[2][c]) - (Pp[0][c] - Pm[0][c]);
+    const float xx = gx * gx, yy = gy * gy, zz = gz * gz;
+    const float A = yy + zz, B = xx + zz, Cc = xx + yy;
+    const float g2 = A + xx;
+    const float n1 = fmaf(A, fxx, fmaf(B, fyy, Cc * fzz));
+    const float n2 = fmaf(gx, fmaf(gy, Gyx, gz * Gzx), gy * gz * Gzy);
+    const float Hn = fmaf(-0.5f, n2, n1);
+    const float r = g2 > 4e-7f ? __fdividef(dt, g2) : 0.0f;
+    const float D = fminf(fmaxf(Hn * r, -0.1f), 0.1f);
+    out[i] = clamp01 ? __saturatef(f0 + D) : f0 + D;
+  }
+}
+
+// Four voxels of a strip, any kernel, from the register window.
+template <bool EXACT>
+__device__ __forceinline__ void computeStrip(const float Pm[3][6], const float P0[3][6],
+                                             const float Pp[3][6], const SweepParams &p,
+                                             float out[4]) {
+  if (!EXACT && p.kind == K_MCF) {
+    mcfFastStrip(Pm, P0, Pp, p.dt, p.constr01 != 0, out);
+    return;
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int c = i + 1;
+    auto F = [&](int dx, int dy, int dz) -> float {
+      const float(*W)[6] = dz < 0 ? Pm : dz > 0 ? Pp : P0;
+      return W[1 + dy][c + dx];
+    };
+    float v = p.kind == K_MCF ? mcfExact<float>(F, p.dt) : stencil7<float>(F, p);
+    if (p.constr01) {
+      v = v > 0.0f ? v : 0.0f;
+      v = v < 1.0f ? v : 1.0f;
+    }
+    out[i] = v;
+  }
+}
+
+int colorSweepRun(msbg_gpu_ctx *ctx, Channel &c, bool exact, bool color8, int nIter, const SweepParams &p);
+
+}  // namespace msbg

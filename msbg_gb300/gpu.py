@@ -19,8 +19,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "lib", "libmsbg_gpu.so")
 
 OK = 0
-ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_CAPACITY, ERR_NONFINITE, ERR_DIVERGED, ERR_UNSUPPORTED = \
-    -1, -2, -3, -4, -5, -6, -7, -8
+ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_CAPACITY, ERR_NONFINITE, ERR_DIVERGED, ERR_UNSUPPORTED, ERR_TIMEOUT = \
+    -1, -2, -3, -4, -5, -6, -7, -8, -9
 
 F32, U16, F16, F64 = 0, 1, 2, 3
 NP_STORAGE = {F32: np.float32, U16: np.uint16, F16: np.float16, F64: np.float64}

@@ -85,6 +85,11 @@ SURFACE_4096 = dict(name="surface-4096^3-bs32-3lvl-fp16", res=4096, bsx=32, n_le
                     dt=0.1, storage="f16", fine_band=8.0, mid_band=16.0)
 
 
+# A crop of the 4096^3 workload (first 96 of its 1,024 clusters, same seed), a
+# few GB on the device: the case kernels are profiled on.
+SURFACE_4096_CROP = dict(SURFACE_4096, name="surface-4096^3-bs32-3lvl-fp16-crop96", n_objects=96)
+
+
 def make_points(spec: dict, workload: int, index: int = 0) -> np.ndarray:
     seed = workload_seed(workload, index)
     if spec["kind"] == "sphere":
