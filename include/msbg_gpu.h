@@ -177,6 +177,26 @@ int msbg_gpu_surface_job(msbg_gpu_ctx *ctx, const float *hPts, int64_t n, float 
                          float timeStep, int variant, void *hOut, size_t hOutCap,
                          int64_t *nActiveOut);
 
+/* ---- value-block slots without allocating ----------------------------------------
+ * This entry point has no counterpart in the reference.  It computes what
+ * msbg_gpu_set_refinement_map's block-pool step computes -- slot[bid] = rank of bid
+ * among the blocks whose level is 0 (ascending bid), -1 for all others,
+ * activeBids[rank] = bid, *dCount = number of level-0 blocks -- for callers that
+ * must not allocate device memory: a runtime that owns all device memory, a
+ * memory budget fixed before the solve, code that may not call cudaMalloc or
+ * cudaFree.  It needs no context and allocates nothing; all five pointers are the
+ * caller's device buffers (dSlot: nBlocks entries, dActiveBids: nBlocks entries,
+ * dCount: one int64), launched on cudaStream.
+ * Its scan scratch is a fixed array inside the library (32 KiB on every device
+ * that loads it, kept until the process exits), so nBlocks is limited to
+ * MSBG_GPU_NOALLOC_MAX_BLOCKS; larger maps return MSBG_GPU_ERR_CAPACITY.
+ * The first call on a device looks the array's address up: make that call
+ * before any stream capture.  All calls share the array, so calls whose kernels
+ * may overlap on the GPU (unordered streams) race; order them on one stream. */
+#define MSBG_GPU_NOALLOC_MAX_BLOCKS ((int64_t)1 << 24)
+int msbg_gpu_assign_slots_noalloc(const int32_t *dLevels, int64_t nBlocks, int32_t *dSlot,
+                                  int32_t *dActiveBids, int64_t *dCount, void *cudaStream);
+
 /* ---- timing and accounting -------------------------------------------------------
  * CUDA events on the context's stream (slot 0..15); elapsed in milliseconds. */
 int msbg_gpu_event_record(msbg_gpu_ctx *ctx, int slot);

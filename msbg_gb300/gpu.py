@@ -70,6 +70,7 @@ SIGNATURES = {
     "msbg_gpu_device_free": (I, [P]),
     "msbg_gpu_copy_h2d": (I, [P, P, P, SZ]),
     "msbg_gpu_copy_d2h": (I, [P, P, P, SZ]),
+    "msbg_gpu_assign_slots_noalloc": (I, [P, I64, P, P, P, P]),
 }
 
 _lib = None
