@@ -177,6 +177,45 @@ int msbg_gpu_surface_job(msbg_gpu_ctx *ctx, const float *hPts, int64_t n, float 
                          float timeStep, int variant, void *hOut, size_t hOutCap,
                          int64_t *nActiveOut);
 
+/* ---- sparse Poisson solve -------------------------------------------------------------
+ * Operator on the value-block cells (src/msbg3.cpp:1281-1296):
+ *   (A x)_i = d_i x_i - sum_f c_f x_nb(f),   x = 0 outside the value blocks (Dirichlet)
+ * Coefficients are FP32 channels of the current layout: the lower-face coefficient of
+ * every cell in x, y, z and the diagonal d (which includes faces towards inactive
+ * cells).  The upper face of a cell is the lower face of the cell above.  Setting the
+ * coefficients (re)builds the multigrid hierarchy: block edge halving down to one cell
+ * per block, then 2x2x2 aggregation of the block grid (the dense coarse levels of
+ * src/msbg.cpp:854-998), coarse operators P^T A P / 2 with piecewise-constant transfers. */
+int msbg_gpu_poisson_set_coefficients(msbg_gpu_ctx *ctx, int chanCx, int chanCy, int chanCz,
+                                      int chanDiag);
+/* Seeded coefficients uniform in [0.5, 2] per face (hash of the face position and
+ * seed); copies them into the given FP32 channels when they are >= 0. */
+int msbg_gpu_poisson_procedural_coefficients(msbg_gpu_ctx *ctx, uint32_t seed, int chanCx,
+                                             int chanCy, int chanCz, int chanDiag);
+/* multiplyLaplacianMatrixOpt (src/msbg.h:3167-3176): Y = A X, or Y = B - A X. */
+int msbg_gpu_multiply_laplacian(msbg_gpu_ctx *ctx, int chanX, int chanB, int chanDstY,
+                                int calcResidual);
+/* relax (src/msbg.h:3269-3277): nIter red-black Gauss-Seidel sweeps of A X = B on the
+ * finest level (red first, or black first when reverseOrder). */
+int msbg_gpu_relax(msbg_gpu_ctx *ctx, int chanX, int chanB, int nIter, int reverseOrder);
+/* One multigrid V-cycle X = M^{-1} B from X = 0 (the CG preconditioner). */
+int msbg_gpu_vcycle(msbg_gpu_ctx *ctx, int chanX, int chanB);
+/* dotProdChannel (src/msbg.h:3331-3341): FP64-accumulated sum; MSBG_GPU_ERR_NONFINITE
+ * when the sum is not finite (src/msbg.cpp:4635-4642).  Synchronizes. */
+int msbg_gpu_dot(msbg_gpu_ctx *ctx, int chanA, int chanB, double *out);
+/* AXPBYChannel (src/msbg.h:3356-3362): Y = a X + b Y. */
+int msbg_gpu_axpby(msbg_gpu_ctx *ctx, double a, int chanX, double b, int chanY);
+/* AXPBYChannelCombined (src/msbg.h:3364-3368): X += a P; P = Q + b P. */
+int msbg_gpu_axpby_combined(msbg_gpu_ctx *ctx, double a, double b, int chanQ, int chanX,
+                            int chanP);
+/* Multigrid-preconditioned CG: solves A X = B from the given X until the FP64-checked
+ * relative residual ||B - A X|| / ||B|| <= tol or maxIter iterations.  Returns
+ * MSBG_GPU_ERR_DIVERGED when the residual becomes non-finite or keeps growing. */
+int msbg_gpu_mgpcg_solve(msbg_gpu_ctx *ctx, int chanX, int chanB, double tol, int maxIter,
+                         int *itersOut, double *relResOut);
+/* Multigrid levels of the current hierarchy and their cell counts. */
+int msbg_gpu_mg_info(msbg_gpu_ctx *ctx, int *nLevels, int64_t *cellsPerLevel, int cap);
+
 /* ---- value-block slots without allocating ----------------------------------------
  * This entry point has no counterpart in the reference.  It computes what
  * msbg_gpu_set_refinement_map's block-pool step computes -- slot[bid] = rank of bid

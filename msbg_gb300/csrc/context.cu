@@ -15,6 +15,7 @@
 #include <cmath>
 
 #include "internal.cuh"
+#include "poisson.cuh"
 
 namespace msbg {
 
@@ -404,6 +405,7 @@ extern "C" int msbg_gpu_destroy(msbg_gpu_ctx *ctx) {
   }
   if (ctx->dTmpSlab) cudaFree(ctx->dTmpSlab);
   if (ctx->dPts) cudaFree(ctx->dPts);
+  msbg::poissonFree(ctx->poisson);
   for (auto &ev : ctx->ev) if (ev) cudaEventDestroy(ev);
   delete ctx;
   return MSBG_GPU_OK;
@@ -561,6 +563,7 @@ extern "C" int msbg_gpu_set_refinement_map(msbg_gpu_ctx *ctx, double fillValue) 
   }
   ctx->colorStart[8] = base;
   ctx->nActive = nAct;
+  ctx->layoutStamp++;
   // block pool: (re)size every channel slab to the value-block count
   for (auto &c : ctx->ch) {
     if (!c.exists) continue;

@@ -12,6 +12,7 @@
 
 namespace msbg {
 
+struct PoissonState;
 constexpr int kMaxChannels = 64;
 constexpr int kMaxEvents = 16;
 
@@ -65,6 +66,8 @@ struct msbg_gpu_ctx {
 
   int64_t nActParticles = 0, nAborted = 0;
   int64_t launches = 0;
+  int64_t layoutStamp = 0;                 // bumped by every set_refinement_map
+  msbg::PoissonState *poisson = nullptr;   // solver hierarchy of the current layout
   std::string err;
 };
 

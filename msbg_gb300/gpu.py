@@ -71,6 +71,16 @@ SIGNATURES = {
     "msbg_gpu_copy_h2d": (I, [P, P, P, SZ]),
     "msbg_gpu_copy_d2h": (I, [P, P, P, SZ]),
     "msbg_gpu_assign_slots_noalloc": (I, [P, I64, P, P, P, P]),
+    "msbg_gpu_poisson_set_coefficients": (I, [P, I, I, I, I]),
+    "msbg_gpu_poisson_procedural_coefficients": (I, [P, C.c_uint32, I, I, I, I]),
+    "msbg_gpu_multiply_laplacian": (I, [P, I, I, I, I]),
+    "msbg_gpu_relax": (I, [P, I, I, I, I]),
+    "msbg_gpu_vcycle": (I, [P, I, I]),
+    "msbg_gpu_dot": (I, [P, I, I, C.POINTER(D)]),
+    "msbg_gpu_axpby": (I, [P, D, I, D, I]),
+    "msbg_gpu_axpby_combined": (I, [P, D, D, I, I, I]),
+    "msbg_gpu_mgpcg_solve": (I, [P, I, I, D, I, C.POINTER(I), C.POINTER(D)]),
+    "msbg_gpu_mg_info": (I, [P, C.POINTER(I), P, I]),
 }
 
 _lib = None
@@ -302,6 +312,44 @@ class MultiresSparseGrid:
             self.h, _ptr(pts), len(pts), r_particle, nb_dist, _ptr(b), 0 if b is None else len(b),
             laplTyp, numIter, timeStep, variant, _ptr(out), cap, C.byref(n_act)))
         return n_act.value
+
+    # ---- Poisson solve (src/msbg3.cpp, src/msbg.cpp:4524-4872) --------------------------
+    def poisson_set_coefficients(self, cx: int, cy: int, cz: int, diag: int):
+        self._check(self.L.msbg_gpu_poisson_set_coefficients(self.h, cx, cy, cz, diag))
+
+    def poisson_procedural_coefficients(self, seed: int, cx=-1, cy=-1, cz=-1, diag=-1):
+        self._check(self.L.msbg_gpu_poisson_procedural_coefficients(self.h, seed, cx, cy, cz, diag))
+
+    def multiplyLaplacianMatrix(self, chanX: int, chanB: int, chanDstY: int, calcResidual: bool = False):
+        self._check(self.L.msbg_gpu_multiply_laplacian(self.h, chanX, chanB, chanDstY, int(calcResidual)))
+
+    def relax(self, chanX: int, chanB: int, nIter: int, reverseOrder: bool = False):
+        self._check(self.L.msbg_gpu_relax(self.h, chanX, chanB, nIter, int(reverseOrder)))
+
+    def vcycle(self, chanX: int, chanB: int):
+        self._check(self.L.msbg_gpu_vcycle(self.h, chanX, chanB))
+
+    def dotProdChannel(self, a: int, b: int) -> float:
+        out = C.c_double()
+        self._check(self.L.msbg_gpu_dot(self.h, a, b, C.byref(out)))
+        return out.value
+
+    def AXPBYChannel(self, a: float, chanX: int, b: float, chanY: int):
+        self._check(self.L.msbg_gpu_axpby(self.h, a, chanX, b, chanY))
+
+    def AXPBYChannelCombined(self, a: float, b: float, chanQ: int, chanX: int, chanP: int):
+        self._check(self.L.msbg_gpu_axpby_combined(self.h, a, b, chanQ, chanX, chanP))
+
+    def mgpcg_solve(self, chanX: int, chanB: int, tol: float = 1e-6, max_iter: int = 200):
+        it, rel = C.c_int(), C.c_double()
+        self._check(self.L.msbg_gpu_mgpcg_solve(self.h, chanX, chanB, tol, max_iter, C.byref(it), C.byref(rel)))
+        return it.value, rel.value
+
+    def mg_info(self):
+        n = C.c_int()
+        cells = np.zeros(32, np.int64)
+        self._check(self.L.msbg_gpu_mg_info(self.h, C.byref(n), _ptr(cells), 32))
+        return cells[: n.value].copy()
 
     # ---- timing -------------------------------------------------------------------------
     def event_record(self, slot: int):

@@ -650,3 +650,280 @@ int orc_pde(const orc_grid *g, const int32_t *slot, const int32_t *activeBids, i
   /* ping-pong ends with the result in bufs[cur]; nIter is even so cur == 0 */
   return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* sparse Poisson solve (FP64)                                               */
+/* ------------------------------------------------------------------------ */
+
+static inline uint32_t hash32(uint32_t x) {
+  x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+  return x;
+}
+
+float orc_face_coeff(uint32_t seed, int axis, int gx, int gy, int gz) {
+  uint32_t h = hash32(seed ^ hash32((uint32_t)axis + 0x9e3779b9U * 3u));
+  h = hash32(h ^ (uint32_t)gx);
+  h = hash32(h ^ (uint32_t)gy * 0x85ebca6bU);
+  h = hash32(h ^ (uint32_t)gz * 0xc2b2ae35U);
+  return 0.5f + 1.5f * (float)(h >> 8) * (1.0f / 16777216.0f);
+}
+
+typedef struct {
+  int nx, ny, nz;
+  uint8_t *act;
+  double *cx, *cy, *cz, *d, *x, *b, *r;
+  int64_t nAct;
+} plev;
+
+#define PIDX(L, x, y, z) (((int64_t)(z) * (L)->ny + (y)) * (L)->nx + (x))
+
+static inline int pin(const plev *L, int x, int y, int z) {
+  return x >= 0 && y >= 0 && z >= 0 && x < L->nx && y < L->ny && z < L->nz && L->act[PIDX(L, x, y, z)];
+}
+
+static void papply(const plev *L, const double *x, const double *b, double *y, int residual) {
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int z = 0; z < L->nz; z++)
+    for (int yy = 0; yy < L->ny; yy++)
+      for (int xx = 0; xx < L->nx; xx++) {
+        const int64_t i = PIDX(L, xx, yy, z);
+        if (!L->act[i]) { y[i] = 0; continue; }
+        double s = L->d[i] * x[i];
+        if (pin(L, xx - 1, yy, z)) s -= L->cx[i] * x[i - 1];
+        if (pin(L, xx + 1, yy, z)) s -= L->cx[i + 1] * x[i + 1];
+        if (pin(L, xx, yy - 1, z)) s -= L->cy[i] * x[i - L->nx];
+        if (pin(L, xx, yy + 1, z)) s -= L->cy[i + L->nx] * x[i + L->nx];
+        const int64_t sl = (int64_t)L->nx * L->ny;
+        if (pin(L, xx, yy, z - 1)) s -= L->cz[i] * x[i - sl];
+        if (pin(L, xx, yy, z + 1)) s -= L->cz[i + sl] * x[i + sl];
+        y[i] = residual ? b[i] - s : s;
+      }
+}
+
+static void prbgs(const plev *L, double *x, const double *b, int nSweeps, int redFirst) {
+  const int64_t sl = (int64_t)L->nx * L->ny;
+  for (int sw = 0; sw < nSweeps; sw++)
+    for (int k = 0; k < 2; k++) {
+      const int color = redFirst ? k : 1 - k;
+#pragma omp parallel for collapse(2) schedule(static)
+      for (int z = 0; z < L->nz; z++)
+        for (int yy = 0; yy < L->ny; yy++)
+          for (int xx = 0; xx < L->nx; xx++) {
+            if (((xx + yy + z) & 1) != color) continue;
+            const int64_t i = PIDX(L, xx, yy, z);
+            if (!L->act[i]) continue;
+            double s = b[i];
+            if (pin(L, xx - 1, yy, z)) s += L->cx[i] * x[i - 1];
+            if (pin(L, xx + 1, yy, z)) s += L->cx[i + 1] * x[i + 1];
+            if (pin(L, xx, yy - 1, z)) s += L->cy[i] * x[i - L->nx];
+            if (pin(L, xx, yy + 1, z)) s += L->cy[i + L->nx] * x[i + L->nx];
+            if (pin(L, xx, yy, z - 1)) s += L->cz[i] * x[i - sl];
+            if (pin(L, xx, yy, z + 1)) s += L->cz[i + sl] * x[i + sl];
+            x[i] = s / L->d[i];
+          }
+    }
+}
+
+static plev *pcoarsen(const plev *F) {
+  plev *C = (plev *)calloc(1, sizeof(plev));
+  C->nx = (F->nx + 1) / 2; C->ny = (F->ny + 1) / 2; C->nz = (F->nz + 1) / 2;
+  const int64_t n = (int64_t)C->nx * C->ny * C->nz;
+  C->act = (uint8_t *)calloc((size_t)n, 1);
+  double **arr[7] = {&C->cx, &C->cy, &C->cz, &C->d, &C->x, &C->b, &C->r};
+  for (int k = 0; k < 7; k++) *arr[k] = (double *)calloc((size_t)n, sizeof(double));
+  for (int z = 0; z < C->nz; z++)
+    for (int y = 0; y < C->ny; y++)
+      for (int x = 0; x < C->nx; x++) {
+        const int64_t c = PIDX(C, x, y, z);
+        double dsum = 0, lx = 0, ly = 0, lz = 0;
+        int any = 0;
+        for (int k = 0; k < 8; k++) {
+          const int ix = k & 1, iy = (k >> 1) & 1, iz = k >> 2;
+          const int fx = 2 * x + ix, fy = 2 * y + iy, fz = 2 * z + iz;
+          if (!pin(F, fx, fy, fz)) continue;
+          any = 1;
+          const int64_t f = PIDX(F, fx, fy, fz);
+          dsum += F->d[f];
+          if (ix == 0) { if (pin(F, fx - 1, fy, fz)) lx += F->cx[f]; }
+          else if (pin(F, fx - 1, fy, fz)) dsum -= 2.0 * F->cx[f];
+          if (iy == 0) { if (pin(F, fx, fy - 1, fz)) ly += F->cy[f]; }
+          else if (pin(F, fx, fy - 1, fz)) dsum -= 2.0 * F->cy[f];
+          if (iz == 0) { if (pin(F, fx, fy, fz - 1)) lz += F->cz[f]; }
+          else if (pin(F, fx, fy, fz - 1)) dsum -= 2.0 * F->cz[f];
+        }
+        C->act[c] = (uint8_t)any;
+        if (any) {
+          C->nAct++;
+          C->cx[c] = 0.5 * lx; C->cy[c] = 0.5 * ly; C->cz[c] = 0.5 * lz; C->d[c] = 0.5 * dsum;
+        }
+      }
+  return C;
+}
+
+static void pfree(plev *L, int ownsCoeffs) {
+  if (!L) return;
+  free(L->act);
+  if (ownsCoeffs) { free(L->cx); free(L->cy); free(L->cz); free(L->d); }
+  free(L->x); free(L->b); free(L->r);
+  free(L);
+}
+
+typedef struct {
+  plev *lv[40];
+  int n;
+  int pre, post, coarsestIter;
+} phier;
+
+static void pbuild(phier *H, const orc_level0 *L0, int log2bs0, int64_t coarsestCells) {
+  plev *F = (plev *)calloc(1, sizeof(plev));
+  F->nx = L0->nx; F->ny = L0->ny; F->nz = L0->nz;
+  const int64_t n = (int64_t)F->nx * F->ny * F->nz;
+  F->act = (uint8_t *)malloc((size_t)n);
+  memcpy(F->act, L0->act, (size_t)n);
+  F->cx = (double *)L0->cx; F->cy = (double *)L0->cy; F->cz = (double *)L0->cz; F->d = (double *)L0->d;
+  F->x = (double *)calloc((size_t)n, 8); F->b = (double *)calloc((size_t)n, 8); F->r = (double *)calloc((size_t)n, 8);
+  for (int64_t i = 0; i < n; i++) F->nAct += F->act[i];
+  H->lv[0] = F;
+  H->n = 1;
+  for (int l = 0; l < log2bs0; l++) {
+    plev *c = pcoarsen(H->lv[H->n - 1]);
+    H->lv[H->n] = c;
+    H->n++;
+  }
+  while (H->n < 40) {
+    const plev *f = H->lv[H->n - 1];
+    if (f->nAct <= coarsestCells || (f->nx <= 2 && f->ny <= 2 && f->nz <= 2)) break;
+    H->lv[H->n] = pcoarsen(f);
+    H->n++;
+  }
+}
+
+static void phfree(phier *H) {
+  for (int l = 0; l < H->n; l++) pfree(H->lv[l], l > 0);
+}
+
+static void pvcycle(phier *H, int l, double *x, const double *b, double *r) {
+  plev *L = H->lv[l];
+  const int64_t n = (int64_t)L->nx * L->ny * L->nz;
+  memset(x, 0, (size_t)n * 8);
+  if (l == H->n - 1) {
+    prbgs(L, x, b, H->coarsestIter, 1);
+    return;
+  }
+  prbgs(L, x, b, H->pre, 1);
+  papply(L, x, b, r, 1);
+  plev *C = H->lv[l + 1];
+  for (int z = 0; z < C->nz; z++)
+    for (int y = 0; y < C->ny; y++)
+      for (int xx = 0; xx < C->nx; xx++) {
+        const int64_t c = PIDX(C, xx, y, z);
+        double s = 0;
+        for (int k = 0; k < 8; k++) {
+          const int fx = 2 * xx + (k & 1), fy = 2 * y + ((k >> 1) & 1), fz = 2 * z + (k >> 2);
+          if (pin(L, fx, fy, fz)) s += r[PIDX(L, fx, fy, fz)];
+        }
+        C->b[c] = C->act[c] ? s : 0;
+      }
+  pvcycle(H, l + 1, C->x, C->b, C->r);
+  for (int z = 0; z < L->nz; z++)
+    for (int y = 0; y < L->ny; y++)
+      for (int xx = 0; xx < L->nx; xx++) {
+        const int64_t i = PIDX(L, xx, y, z);
+        if (L->act[i]) x[i] += C->x[PIDX(C, xx >> 1, y >> 1, z >> 1)];
+      }
+  prbgs(L, x, b, H->post, 0);
+}
+
+static plev view0(const orc_level0 *L0) {
+  plev v;
+  memset(&v, 0, sizeof(v));
+  v.nx = L0->nx; v.ny = L0->ny; v.nz = L0->nz;
+  v.act = (uint8_t *)L0->act;
+  v.cx = (double *)L0->cx; v.cy = (double *)L0->cy; v.cz = (double *)L0->cz; v.d = (double *)L0->d;
+  return v;
+}
+
+void orc_poisson_apply(const orc_level0 *L0, const double *x, const double *b, double *y, int residual) {
+  plev v = view0(L0);
+  papply(&v, x, b, y, residual);
+}
+
+void orc_poisson_rbgs(const orc_level0 *L0, double *x, const double *b, int nSweeps, int redFirst) {
+  plev v = view0(L0);
+  prbgs(&v, x, b, nSweeps, redFirst);
+}
+
+int orc_poisson_vcycle(const orc_level0 *L0, int log2bs0, const double *b, double *x, int preSweeps,
+                       int postSweeps, int coarsestIter, int64_t coarsestCells) {
+  phier H;
+  memset(&H, 0, sizeof(H));
+  H.pre = preSweeps; H.post = postSweeps; H.coarsestIter = coarsestIter;
+  pbuild(&H, L0, log2bs0, coarsestCells);
+  pvcycle(&H, 0, x, b, H.lv[0]->r);
+  const int n = H.n;
+  phfree(&H);
+  return n;
+}
+
+static double pdot(const double *a, const double *b, int64_t n) {
+  double s = 0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+  for (int64_t i = 0; i < n; i++) s += a[i] * b[i];
+  return s;
+}
+
+int orc_poisson_mgpcg(const orc_level0 *L0, int log2bs0, const double *b, double *x, double tol,
+                      int maxIter, int *iters, double *relres) {
+  phier H;
+  memset(&H, 0, sizeof(H));
+  H.pre = 2; H.post = 2; H.coarsestIter = 200;
+  pbuild(&H, L0, log2bs0, 512);
+  plev *L = H.lv[0];
+  const int64_t n = (int64_t)L->nx * L->ny * L->nz;
+  double *r = (double *)calloc((size_t)n, 8), *z = (double *)calloc((size_t)n, 8),
+         *p = (double *)calloc((size_t)n, 8), *q = (double *)calloc((size_t)n, 8);
+  papply(L, x, b, r, 1);
+  const double bn = sqrt(pdot(b, b, n));
+  double rel = bn > 0 ? sqrt(pdot(r, r, n)) / bn : 0;
+  int it = 0;
+  if (bn > 0 && rel > tol) {
+    pvcycle(&H, 0, z, r, L->r);
+    memcpy(p, z, (size_t)n * 8);
+    double rz = pdot(r, z, n);
+    for (it = 1; it <= maxIter; it++) {
+      papply(L, p, NULL, q, 0);
+      const double alpha = rz / pdot(p, q, n);
+      for (int64_t i = 0; i < n; i++) { x[i] += alpha * p[i]; r[i] -= alpha * q[i]; }
+      rel = sqrt(pdot(r, r, n)) / bn;
+      if (rel <= tol) break;
+      pvcycle(&H, 0, z, r, L->r);
+      const double rz2 = pdot(r, z, n);
+      const double beta = rz2 / rz;
+      rz = rz2;
+      for (int64_t i = 0; i < n; i++) p[i] = z[i] + beta * p[i];
+    }
+    if (it > maxIter) it = maxIter;
+  }
+  free(r); free(z); free(p); free(q);
+  phfree(&H);
+  if (iters) *iters = it;
+  if (relres) *relres = rel;
+  return 0;
+}
+
+void orc_poisson_coeffs_dense(uint32_t seed, int nx, int ny, int nz, const uint8_t *act, double *cx,
+                              double *cy, double *cz, double *d) {
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int z = 0; z < nz; z++)
+    for (int y = 0; y < ny; y++)
+      for (int x = 0; x < nx; x++) {
+        const int64_t i = ((int64_t)z * ny + y) * nx + x;
+        if (!act[i]) { cx[i] = cy[i] = cz[i] = d[i] = 0; continue; }
+        const float lx = orc_face_coeff(seed, 0, x, y, z), ly = orc_face_coeff(seed, 1, x, y, z),
+                    lz = orc_face_coeff(seed, 2, x, y, z);
+        const float ux = orc_face_coeff(seed, 0, x + 1, y, z), uy = orc_face_coeff(seed, 1, x, y + 1, z),
+                    uz = orc_face_coeff(seed, 2, x, y, z + 1);
+        cx[i] = lx; cy[i] = ly; cz[i] = lz;
+        d[i] = (float)(((lx + ux) + (ly + uy)) + (lz + uz));
+      }
+}

@@ -101,7 +101,36 @@ int orc_pde(const orc_grid *g, const int32_t *slot, const int32_t *activeBids, i
 uint16_t orc_f32_to_f16(float f);
 float orc_f16_to_f32(uint16_t h);
 
+/* ---- sparse Poisson solve (FP64 restatement) ---------------------------------
+ * Same operator, hierarchy, transfers, smoother and CG as the GPU solver, on dense
+ * per-level arrays with an activity mask (x = 0 outside, Dirichlet):
+ *   (A x)_i = d_i x_i - sum_f c_f x_nb(f)            (src/msbg3.cpp:1281-1296)
+ * cx/cy/cz hold each cell's lower-face coefficient, d the diagonal.  Level l+1 has
+ * ceil(n/2) cells per axis; a coarse cell is active when any child is; coarse
+ * operator = P^T A P / 2 with piecewise-constant P; red-black Gauss-Seidel
+ * smoothing (pre: red first, post: black first); coarsest level: coarsestIter RB
+ * sweeps from zero.  Levels: log2(bs0) halvings, then more while the coarse level
+ * has more than coarsestCells active cells and a side longer than 2. */
+typedef struct {
+  int nx, ny, nz;
+  const uint8_t *act;  /* [nz][ny][nx] */
+  const double *cx, *cy, *cz, *d;
+} orc_level0;
+
+/* Seeded face coefficients of level 0 in [0.5,2] (identical bits to the GPU). */
+float orc_face_coeff(uint32_t seed, int axis, int gx, int gy, int gz);
+void orc_poisson_apply(const orc_level0 *L, const double *x, const double *b, double *y, int residual);
+void orc_poisson_rbgs(const orc_level0 *L, double *x, const double *b, int nSweeps, int redFirst);
+int orc_poisson_vcycle(const orc_level0 *L, int log2bs0, const double *b, double *x, int preSweeps,
+                       int postSweeps, int coarsestIter, int64_t coarsestCells);
+int orc_poisson_mgpcg(const orc_level0 *L, int log2bs0, const double *b, double *x, double tol,
+                      int maxIter, int *iters, double *relres);
+/* The GPU's seeded coefficients (float values) on a dense grid: lower faces + diagonal. */
+void orc_poisson_coeffs_dense(uint32_t seed, int nx, int ny, int nz, const uint8_t *act, double *cx,
+                              double *cy, double *cz, double *d);
+
 #ifdef __cplusplus
 }
 #endif
 #endif
+

@@ -59,6 +59,15 @@ def lib():
         L.orc_pde.argtypes = [C.POINTER(Grid), P, P, C.c_int32, P, P, C.c_int, C.c_int, C.c_int,
                               C.c_float, C.c_float]
         L.orc_pde.restype = C.c_int
+        L.orc_face_coeff.argtypes = [C.c_uint32, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.orc_face_coeff.restype = C.c_float
+        L.orc_poisson_apply.argtypes = [P, P, P, P, C.c_int]
+        L.orc_poisson_rbgs.argtypes = [P, P, P, C.c_int, C.c_int]
+        L.orc_poisson_vcycle.argtypes = [P, C.c_int, P, P, C.c_int, C.c_int, C.c_int, C.c_int64]
+        L.orc_poisson_vcycle.restype = C.c_int
+        L.orc_poisson_mgpcg.argtypes = [P, C.c_int, P, P, C.c_double, C.c_int, C.POINTER(C.c_int),
+                                        C.POINTER(C.c_double)]
+        L.orc_poisson_coeffs_dense.argtypes = [C.c_uint32, C.c_int, C.c_int, C.c_int, P, P, P, P, P]
         L.orc_f32_to_f16.argtypes = [C.c_float]
         L.orc_f32_to_f16.restype = C.c_uint16
         L.orc_f16_to_f32.argtypes = [C.c_uint16]
@@ -198,3 +207,84 @@ def to_float(storage: int, a: np.ndarray) -> np.ndarray:
     if storage == F16:
         return a.view(np.float16).astype(np.float64)
     return a.astype(np.float64)
+
+
+# ---- sparse Poisson (FP64 restatement) ------------------------------------------------
+class Level0(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("act", C.c_void_p),
+                ("cx", C.c_void_p), ("cy", C.c_void_p), ("cz", C.c_void_p), ("d", C.c_void_p)]
+
+
+def payload_to_dense(payload: np.ndarray, bids: np.ndarray, nb, bs: int, dtype=np.float64):
+    """[nActive][bs^3] payload -> dense (nz*bs, ny*bs, nx*bs) array (zeros elsewhere)."""
+    nbx, nby, nbz = nb
+    out = np.zeros((nbz * bs, nby * bs, nbx * bs), dtype)
+    pay = np.asarray(payload).reshape(len(bids), bs, bs, bs)
+    bx, by, bz = bids % nbx, (bids // nbx) % nby, bids // (nbx * nby)
+    for k in range(len(bids)):
+        out[bz[k] * bs:(bz[k] + 1) * bs, by[k] * bs:(by[k] + 1) * bs, bx[k] * bs:(bx[k] + 1) * bs] = pay[k]
+    return out
+
+
+def dense_to_payload(dense: np.ndarray, bids: np.ndarray, nb, bs: int, dtype=np.float32):
+    nbx, nby, nbz = nb
+    out = np.empty((len(bids), bs, bs, bs), dtype)
+    bx, by, bz = bids % nbx, (bids // nbx) % nby, bids // (nbx * nby)
+    for k in range(len(bids)):
+        out[k] = dense[bz[k] * bs:(bz[k] + 1) * bs, by[k] * bs:(by[k] + 1) * bs, bx[k] * bs:(bx[k] + 1) * bs]
+    return out.reshape(len(bids), bs ** 3)
+
+
+def active_mask(bids: np.ndarray, nb, bs: int) -> np.ndarray:
+    return payload_to_dense(np.ones((len(bids), bs ** 3), np.uint8), bids, nb, bs, np.uint8)
+
+
+class PoissonProblem:
+    """Dense FP64 restatement of one Poisson problem on a value-block layout."""
+
+    def __init__(self, bids: np.ndarray, nb, bs: int, seed: int):
+        self.bids, self.nb, self.bs, self.seed = np.asarray(bids, np.int64), nb, bs, seed
+        self.act = np.ascontiguousarray(active_mask(self.bids, nb, bs))
+        nz, ny, nx = self.act.shape
+        self.cx, self.cy, self.cz, self.d = (np.zeros(self.act.shape) for _ in range(4))
+        lib().orc_poisson_coeffs_dense(seed, nx, ny, nz, _p(self.act), _p(self.cx), _p(self.cy),
+                                       _p(self.cz), _p(self.d))
+        self.L = Level0(nx, ny, nz, self.act.ctypes.data, self.cx.ctypes.data, self.cy.ctypes.data,
+                        self.cz.ctypes.data, self.d.ctypes.data)
+        self.log2bs = int(round(np.log2(bs)))
+
+    def dense(self, payload):
+        return np.ascontiguousarray(payload_to_dense(payload, self.bids, self.nb, self.bs))
+
+    def payload(self, dense):
+        return dense_to_payload(dense, self.bids, self.nb, self.bs)
+
+    def apply(self, x, b=None):
+        y = np.zeros_like(self.d)
+        bb = np.zeros_like(self.d) if b is None else np.ascontiguousarray(b, np.float64)
+        lib().orc_poisson_apply(C.byref(self.L), _p(np.ascontiguousarray(x, np.float64)), _p(bb), _p(y),
+                                0 if b is None else 1)
+        return y
+
+    def rbgs(self, x, b, n, red_first=True):
+        x = np.ascontiguousarray(x, np.float64).copy()
+        lib().orc_poisson_rbgs(C.byref(self.L), _p(x), _p(np.ascontiguousarray(b, np.float64)), n,
+                               int(red_first))
+        return x
+
+    def vcycle(self, b):
+        x = np.zeros_like(self.d)
+        nlev = lib().orc_poisson_vcycle(C.byref(self.L), self.log2bs, _p(np.ascontiguousarray(b, np.float64)),
+                                        _p(x), 2, 2, 200, 512)
+        return x, nlev
+
+    def solve(self, b, tol=1e-6, max_iter=200, x0=None):
+        x = np.zeros_like(self.d) if x0 is None else np.ascontiguousarray(x0, np.float64).copy()
+        it, rel = C.c_int(), C.c_double()
+        lib().orc_poisson_mgpcg(C.byref(self.L), self.log2bs, _p(np.ascontiguousarray(b, np.float64)),
+                                _p(x), tol, max_iter, C.byref(it), C.byref(rel))
+        return x, it.value, rel.value
+
+    def rel_residual(self, x, b):
+        r = self.apply(x, b)
+        return float(np.linalg.norm(r) / np.linalg.norm(b))

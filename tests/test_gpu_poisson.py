@@ -1,0 +1,132 @@
+"""GPU sparse Poisson pieces against the FP64 CPU restatement (oracle/msbg_oracle.c).
+
+The reference release has no Poisson driver and no test for these kernels, so
+parity is against the restatement of its formulas (src/msbg3.cpp:1281-1296,
+src/msbg.cpp:4524-4872): operator, smoother, V-cycle and dot/AXPBY within
+FP32 tolerances; the full MG-PCG solve reaches the FP64-checked tolerance and
+matches the FP64 solution.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from msbg_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+CH_X, CH_B, CH_Y, CH_CX, CH_CY, CH_CZ, CH_D, CH_Q = range(1, 9)
+
+
+def _layout(G, P, res=128, bs=16, n_spheres=6, seed_idx=1):
+    pts = W.sphere_cloud(res, n_spheres, 3000, seed=W.workload_seed(3, seed_idx))
+    g = G.MultiresSparseGrid(res, res, res, bs, 3, G.F32)
+    d = g.to_device(pts)
+    g.mark_points(d, len(pts), 4.0)
+    g.levels_from_marks()
+    g.regularizeRefinementMap()
+    g.setRefinementMap(0.0)
+    d.free()
+    for ch in (CH_X, CH_B, CH_Y, CH_CX, CH_CY, CH_CZ, CH_D, CH_Q):
+        g.channel_create(ch, G.F32)
+    bids = g.active_blocks().astype(np.int64)
+    prob = P.PoissonProblem(bids, (g.nbx, g.nby, g.nbz), bs, seed=4242)
+    g.poisson_procedural_coefficients(4242, CH_CX, CH_CY, CH_CZ, CH_D)
+    return g, prob
+
+
+def _rand(prob, rng):
+    return np.where(prob.act > 0, rng.standard_normal(prob.act.shape), 0.0)
+
+
+@pytest.fixture(scope="module")
+def setup(gpulib, port):
+    g, prob = _layout(gpulib, port)
+    yield gpulib, port, g, prob
+    g.close()
+
+
+def test_coefficients_bit_identical(setup):
+    G, P, g, prob = setup
+    for ch, ref in ((CH_CX, prob.cx), (CH_CY, prob.cy), (CH_CZ, prob.cz), (CH_D, prob.d)):
+        got = prob.dense(g.payload(ch))
+        assert np.array_equal(got.astype(np.float32), ref.astype(np.float32))
+
+
+def test_multiply_and_residual(setup):
+    G, P, g, prob = setup
+    rng = np.random.default_rng(1)
+    x, b = _rand(prob, rng).astype(np.float32), _rand(prob, rng).astype(np.float32)
+    g.upload_payload(prob.payload(x), CH_X)
+    g.upload_payload(prob.payload(b), CH_B)
+    g.multiplyLaplacianMatrix(CH_X, CH_B, CH_Y, calcResidual=False)
+    assert rel_l2(prob.dense(g.payload(CH_Y)), prob.apply(x)) < 1e-6
+    g.multiplyLaplacianMatrix(CH_X, CH_B, CH_Y, calcResidual=True)
+    assert rel_l2(prob.dense(g.payload(CH_Y)), prob.apply(x, b)) < 1e-6
+
+
+@pytest.mark.parametrize("reverse", [False, True])
+def test_relax_red_black(setup, reverse):
+    G, P, g, prob = setup
+    rng = np.random.default_rng(2)
+    x, b = _rand(prob, rng).astype(np.float32), _rand(prob, rng).astype(np.float32)
+    g.upload_payload(prob.payload(x), CH_X)
+    g.upload_payload(prob.payload(b), CH_B)
+    g.relax(CH_X, CH_B, 2, reverseOrder=reverse)
+    want = prob.rbgs(x, b, 2, red_first=not reverse)
+    assert rel_l2(prob.dense(g.payload(CH_X)), want) < 1e-5
+
+
+def test_vcycle_matches_fp64(setup):
+    G, P, g, prob = setup
+    rng = np.random.default_rng(3)
+    b = _rand(prob, rng).astype(np.float32)
+    g.upload_payload(prob.payload(b), CH_B)
+    g.vcycle(CH_X, CH_B)
+    want, nlev = prob.vcycle(b)
+    assert len(g.mg_info()) == nlev
+    assert rel_l2(prob.dense(g.payload(CH_X)), want) < 1e-5
+
+
+def test_dot_and_axpby(setup):
+    G, P, g, prob = setup
+    rng = np.random.default_rng(4)
+    x, y, q = (_rand(prob, rng).astype(np.float32) for _ in range(3))
+    px, py, pq = prob.payload(x), prob.payload(y), prob.payload(q)
+    g.upload_payload(px, CH_X)
+    g.upload_payload(py, CH_Y)
+    g.upload_payload(pq, CH_Q)
+    want = float(np.dot(px.astype(np.float64).ravel(), py.astype(np.float64).ravel()))
+    assert abs(g.dotProdChannel(CH_X, CH_Y) - want) <= 1e-9 * abs(want) + 1e-9
+    g.AXPBYChannel(0.5, CH_X, -2.0, CH_Y)
+    assert rel_l2(g.payload(CH_Y), 0.5 * px.astype(np.float64) - 2.0 * py) < 1e-6
+    g.upload_payload(py, CH_Y)
+    g.AXPBYChannelCombined(0.25, 1.5, CH_Q, CH_X, CH_Y)  # X += aP ; P = Q + bP  with P = CH_Y
+    assert rel_l2(g.payload(CH_X), px.astype(np.float64) + 0.25 * py) < 1e-6
+    assert rel_l2(g.payload(CH_Y), pq.astype(np.float64) + 1.5 * py) < 1e-6
+
+
+def test_dot_nonfinite_is_an_error(setup):
+    G, P, g, prob = setup
+    x = np.zeros((len(prob.bids), prob.bs ** 3), np.float32)
+    x[0, 5] = np.inf
+    g.upload_payload(x, CH_X)
+    with pytest.raises(G.MsbgGpuError) as e:
+        g.dotProdChannel(CH_X, CH_X)
+    assert e.value.code == G.ERR_NONFINITE
+
+
+def test_mgpcg_solve_to_tolerance(setup):
+    G, P, g, prob = setup
+    rng = np.random.default_rng(5)
+    b = _rand(prob, rng).astype(np.float32)
+    g.upload_payload(prob.payload(b), CH_B)
+    g.fill(0.0, CH_X)
+    it, rel = g.mgpcg_solve(CH_X, CH_B, tol=1e-6, max_iter=100)
+    x = prob.dense(g.payload(CH_X))
+    check = prob.rel_residual(x, b)          # FP64 check on the CPU
+    assert rel <= 1e-6 and check <= 1.5e-6, (it, rel, check)
+    xs, it_ref, rel_ref = prob.solve(b.astype(np.float64), 1e-6)
+    assert abs(it - it_ref) <= 2
+    assert rel_l2(x, xs) < 1e-5
