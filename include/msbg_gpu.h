@@ -213,6 +213,14 @@ int msbg_gpu_axpby_combined(msbg_gpu_ctx *ctx, double a, double b, int chanQ, in
  * MSBG_GPU_ERR_DIVERGED when the residual becomes non-finite or keeps growing. */
 int msbg_gpu_mgpcg_solve(msbg_gpu_ctx *ctx, int chanX, int chanB, double tol, int maxIter,
                          int *itersOut, double *relResOut);
+/* Mixed precision: FP32 iterative refinement around an FP16-storage MG-PCG.  Each
+ * outer step forms r = B - A X with the FP32 operator, solves A e = r / rms(r) with
+ * FP16 vectors and FP16 coefficients (FP32 arithmetic, FP64 dots) to innerTol or
+ * maxInner iterations, and adds rms(r) e to X; stops at the FP64-checked relative
+ * residual tol or after maxOuter steps. */
+int msbg_gpu_mgpcg_solve_mixed(msbg_gpu_ctx *ctx, int chanX, int chanB, double tol, int maxOuter,
+                               double innerTol, int maxInner, int *outerOut, int *innerTotalOut,
+                               double *relResOut);
 /* Multigrid levels of the current hierarchy and their cell counts. */
 int msbg_gpu_mg_info(msbg_gpu_ctx *ctx, int *nLevels, int64_t *cellsPerLevel, int cap);
 

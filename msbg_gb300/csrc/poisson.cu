@@ -26,8 +26,14 @@
 // P^T A P / 2 (the rediscretized coefficient of a coarse face is half the sum of
 // its four fine faces), which keeps the V-cycle symmetric for CG.  Smoothing is
 // red-black Gauss-Seidel on cells (parity of x+y+z), pre-smoothing red first and
-// post-smoothing black first; the coarsest level (<= 4096 cells) is relaxed by one
+// post-smoothing black first; the coarsest level (<= 512 cells) is relaxed by one
 // CTA for many sweeps.
+//
+// Precision.  Every kernel is templated on the storage type (FP32, or FP16 for the
+// mixed-precision solve); arithmetic is FP32, dot products and norms FP64.  The
+// mixed solve is FP32 iterative refinement: the outer residual b - A x uses the
+// FP32 operator, each correction comes from an FP16-storage MG-PCG on the scaled
+// residual to a loose inner tolerance.
 #include <math.h>
 #include <string.h>
 
@@ -39,18 +45,33 @@
 namespace msbg {
 
 // ---------------------------------------------------------------------------------
+// storage types: FP32, or FP16 (mixed precision); arithmetic is FP32
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ float ldv(const float *p) { return *p; }
+__device__ __forceinline__ float ldv(const __half *p) { return __half2float(*p); }
+__device__ __forceinline__ void stv(float *p, float v) { *p = v; }
+__device__ __forceinline__ void stv(__half *p, float v) { *p = __float2half_rn(v); }
+
+// ---------------------------------------------------------------------------------
 // cell addressing on a level
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ void cellOf(const LvGeom &g, int64_t c, int &gx, int &gy, int &gz) {
+struct Cell {
+  int gx, gy, gz;  // global cell coordinates on the level
+  int lx, ly, lz;  // inside the block
+};
+
+__device__ __forceinline__ Cell cellOf(const LvGeom &g, int64_t c) {
   const int s = (int)(c >> (3 * g.log2bs));
   const int v = (int)(c & ((1 << (3 * g.log2bs)) - 1));
   const int m = g.bs - 1;
-  const int lx = v & m, ly = (v >> g.log2bs) & m, lz = v >> (2 * g.log2bs);
+  Cell q;
+  q.lx = v & m; q.ly = (v >> g.log2bs) & m; q.lz = v >> (2 * g.log2bs);
   const int bid = g.active[s];
   const int bx = bid % g.nbx, by = (bid / g.nbx) % g.nby, bz = bid / (g.nbx * g.nby);
-  gx = (bx << g.log2bs) + lx;
-  gy = (by << g.log2bs) + ly;
-  gz = (bz << g.log2bs) + lz;
+  q.gx = (bx << g.log2bs) + q.lx;
+  q.gy = (by << g.log2bs) + q.ly;
+  q.gz = (bz << g.log2bs) + q.lz;
+  return q;
 }
 
 // linear index of cell (gx,gy,gz) on the level, or -1 when outside / inactive
@@ -64,156 +85,141 @@ __device__ __forceinline__ int64_t cellIdx(const LvGeom &g, int gx, int gy, int 
   return ((int64_t)s << (3 * g.log2bs)) + ((((gz & m) << g.log2bs) + (gy & m)) << g.log2bs) + (gx & m);
 }
 
-template <typename R>
-__device__ __forceinline__ R nbVal(const LvGeom &g, const float *x, int gx, int gy, int gz) {
-  const int64_t j = cellIdx(g, gx, gy, gz);
-  return j < 0 ? (R)0 : (R)x[j];
+// The six neighbour indices of cell c: inside the block by offset, across a block
+// face through the slot map (-1: outside / inactive).
+struct Nb6 {
+  int64_t xm, xp, ym, yp, zm, zp;
+};
+__device__ __forceinline__ Nb6 neighbours(const LvGeom &g, int64_t c, const Cell &q) {
+  Nb6 n;
+  const int e = g.bs - 1;
+  const int64_t sy = (int64_t)g.bs, sz = (int64_t)g.bs * g.bs;
+  n.xm = q.lx > 0 ? c - 1 : cellIdx(g, q.gx - 1, q.gy, q.gz);
+  n.xp = q.lx < e ? c + 1 : cellIdx(g, q.gx + 1, q.gy, q.gz);
+  n.ym = q.ly > 0 ? c - sy : cellIdx(g, q.gx, q.gy - 1, q.gz);
+  n.yp = q.ly < e ? c + sy : cellIdx(g, q.gx, q.gy + 1, q.gz);
+  n.zm = q.lz > 0 ? c - sz : cellIdx(g, q.gx, q.gy, q.gz - 1);
+  n.zp = q.lz < e ? c + sz : cellIdx(g, q.gx, q.gy, q.gz + 1);
+  return n;
 }
 
-// A x at cell c (coords gx,gy,gz), compute type R
-template <typename R>
-__device__ __forceinline__ R applyAt(const LvGeom &g, const float *__restrict__ x, const float *__restrict__ cx,
-                                     const float *__restrict__ cy, const float *__restrict__ cz,
-                                     const float *__restrict__ d, int64_t c, int gx, int gy, int gz) {
-  R s = (R)d[c] * (R)x[c];
-  {
-    const int64_t j = cellIdx(g, gx - 1, gy, gz);
-    if (j >= 0) s -= (R)cx[c] * (R)x[j];
-    const int64_t k = cellIdx(g, gx + 1, gy, gz);
-    if (k >= 0) s -= (R)cx[k] * (R)x[k];
-  }
-  {
-    const int64_t j = cellIdx(g, gx, gy - 1, gz);
-    if (j >= 0) s -= (R)cy[c] * (R)x[j];
-    const int64_t k = cellIdx(g, gx, gy + 1, gz);
-    if (k >= 0) s -= (R)cy[k] * (R)x[k];
-  }
-  {
-    const int64_t j = cellIdx(g, gx, gy, gz - 1);
-    if (j >= 0) s -= (R)cz[c] * (R)x[j];
-    const int64_t k = cellIdx(g, gx, gy, gz + 1);
-    if (k >= 0) s -= (R)cz[k] * (R)x[k];
-  }
+// (A x)_c in compute type R
+template <typename R, typename V, typename Cf>
+__device__ __forceinline__ R applyAt(const V *__restrict__ x, const Cf *__restrict__ cx, const Cf *__restrict__ cy,
+                                     const Cf *__restrict__ cz, const Cf *__restrict__ d, int64_t c, const Nb6 &n) {
+  R s = (R)ldv(d + c) * (R)ldv(x + c);
+  if (n.xm >= 0) s -= (R)ldv(cx + c) * (R)ldv(x + n.xm);
+  if (n.xp >= 0) s -= (R)ldv(cx + n.xp) * (R)ldv(x + n.xp);
+  if (n.ym >= 0) s -= (R)ldv(cy + c) * (R)ldv(x + n.ym);
+  if (n.yp >= 0) s -= (R)ldv(cy + n.yp) * (R)ldv(x + n.yp);
+  if (n.zm >= 0) s -= (R)ldv(cz + c) * (R)ldv(x + n.zm);
+  if (n.zp >= 0) s -= (R)ldv(cz + n.zp) * (R)ldv(x + n.zp);
   return s;
 }
+
+#define GRID_STRIDE(c, n) \
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < (n); c += (int64_t)gridDim.x * blockDim.x)
 
 // ---------------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------------
-// mode 0: y = A x; mode 1: y = b - A x.  Grid-stride over the level's cells.
-__global__ void kApply(LvGeom g, const float *__restrict__ x, const float *__restrict__ b,
-                       const float *__restrict__ cx, const float *__restrict__ cy,
-                       const float *__restrict__ cz, const float *__restrict__ d, float *__restrict__ y,
-                       int mode) {
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < g.nCell;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    int gx, gy, gz;
-    cellOf(g, c, gx, gy, gz);
-    const float ax = applyAt<float>(g, x, cx, cy, cz, d, c, gx, gy, gz);
-    y[c] = mode ? b[c] - ax : ax;
+// mode 0: y = A x; mode 1: y = b - A x
+template <typename V, typename Cf>
+__global__ void kApply(LvGeom g, const V *__restrict__ x, const V *__restrict__ b, const Cf *__restrict__ cx,
+                       const Cf *__restrict__ cy, const Cf *__restrict__ cz, const Cf *__restrict__ d,
+                       V *__restrict__ y, int mode) {
+  GRID_STRIDE(c, g.nCell) {
+    const Cell q = cellOf(g, c);
+    const float ax = applyAt<float>(x, cx, cy, cz, d, c, neighbours(g, c, q));
+    stv(y + c, mode ? ldv(b + c) - ax : ax);
   }
 }
 
 // Red-black Gauss-Seidel half sweep: cells with (gx+gy+gz)&1 == color get
 // x = (b + sum c x_nb) / d.
-__global__ void kRBGS(LvGeom g, float *__restrict__ x, const float *__restrict__ b,
-                      const float *__restrict__ cx, const float *__restrict__ cy,
-                      const float *__restrict__ cz, const float *__restrict__ d, int color) {
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < g.nCell;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    int gx, gy, gz;
-    cellOf(g, c, gx, gy, gz);
-    if (((gx + gy + gz) & 1) != color) continue;
-    float s = b[c];
-    int64_t j;
-    if ((j = cellIdx(g, gx - 1, gy, gz)) >= 0) s += cx[c] * x[j];
-    if ((j = cellIdx(g, gx + 1, gy, gz)) >= 0) s += cx[j] * x[j];
-    if ((j = cellIdx(g, gx, gy - 1, gz)) >= 0) s += cy[c] * x[j];
-    if ((j = cellIdx(g, gx, gy + 1, gz)) >= 0) s += cy[j] * x[j];
-    if ((j = cellIdx(g, gx, gy, gz - 1)) >= 0) s += cz[c] * x[j];
-    if ((j = cellIdx(g, gx, gy, gz + 1)) >= 0) s += cz[j] * x[j];
-    x[c] = s / d[c];
-  }
+template <typename V, typename Cf>
+__device__ __forceinline__ void rbgsCell(const LvGeom &g, V *__restrict__ x, const V *__restrict__ b,
+                                         const Cf *__restrict__ cx, const Cf *__restrict__ cy,
+                                         const Cf *__restrict__ cz, const Cf *__restrict__ d, int64_t c,
+                                         int color) {
+  const Cell q = cellOf(g, c);
+  if (((q.gx + q.gy + q.gz) & 1) != color) return;
+  const Nb6 n = neighbours(g, c, q);
+  float s = ldv(b + c);
+  if (n.xm >= 0) s += ldv(cx + c) * ldv(x + n.xm);
+  if (n.xp >= 0) s += ldv(cx + n.xp) * ldv(x + n.xp);
+  if (n.ym >= 0) s += ldv(cy + c) * ldv(x + n.ym);
+  if (n.yp >= 0) s += ldv(cy + n.yp) * ldv(x + n.yp);
+  if (n.zm >= 0) s += ldv(cz + c) * ldv(x + n.zm);
+  if (n.zp >= 0) s += ldv(cz + n.zp) * ldv(x + n.zp);
+  stv(x + c, s / ldv(d + c));
 }
 
-// Coarsest level: nIter red-black sweeps by one CTA (cells <= blockDim * k).
-__global__ void kCoarsestGS(LvGeom g, float *__restrict__ x, const float *__restrict__ b,
-                            const float *__restrict__ cx, const float *__restrict__ cy,
-                            const float *__restrict__ cz, const float *__restrict__ d, int nIter) {
-  for (int64_t c = threadIdx.x; c < g.nCell; c += blockDim.x) x[c] = 0.0f;
+template <typename V, typename Cf>
+__global__ void kRBGS(LvGeom g, V *__restrict__ x, const V *__restrict__ b, const Cf *__restrict__ cx,
+                      const Cf *__restrict__ cy, const Cf *__restrict__ cz, const Cf *__restrict__ d, int color) {
+  GRID_STRIDE(c, g.nCell) rbgsCell(g, x, b, cx, cy, cz, d, c, color);
+}
+
+// Coarsest level: nIter red-black sweeps by one CTA from x = 0.
+template <typename V, typename Cf>
+__global__ void kCoarsestGS(LvGeom g, V *__restrict__ x, const V *__restrict__ b, const Cf *__restrict__ cx,
+                            const Cf *__restrict__ cy, const Cf *__restrict__ cz, const Cf *__restrict__ d,
+                            int nIter) {
+  for (int64_t c = threadIdx.x; c < g.nCell; c += blockDim.x) stv(x + c, 0.0f);
   __syncthreads();
-  for (int it = 0; it < nIter; it++) {
+  for (int it = 0; it < nIter; it++)
     for (int color = 0; color < 2; color++) {
-      for (int64_t c = threadIdx.x; c < g.nCell; c += blockDim.x) {
-        int gx, gy, gz;
-        cellOf(g, c, gx, gy, gz);
-        if (((gx + gy + gz) & 1) != color) continue;
-        float s = b[c];
-        int64_t j;
-        if ((j = cellIdx(g, gx - 1, gy, gz)) >= 0) s += cx[c] * x[j];
-        if ((j = cellIdx(g, gx + 1, gy, gz)) >= 0) s += cx[j] * x[j];
-        if ((j = cellIdx(g, gx, gy - 1, gz)) >= 0) s += cy[c] * x[j];
-        if ((j = cellIdx(g, gx, gy + 1, gz)) >= 0) s += cy[j] * x[j];
-        if ((j = cellIdx(g, gx, gy, gz - 1)) >= 0) s += cz[c] * x[j];
-        if ((j = cellIdx(g, gx, gy, gz + 1)) >= 0) s += cz[j] * x[j];
-        x[c] = s / d[c];
-      }
+      for (int64_t c = threadIdx.x; c < g.nCell; c += blockDim.x) rbgsCell(g, x, b, cx, cy, cz, d, c, color);
       __syncthreads();
     }
-  }
 }
 
 // b_C = R r_F (sum of the active children); x_C = 0.
-__global__ void kRestrictSum(LvGeom gf, LvGeom gc, const float *__restrict__ rf, float *__restrict__ bc,
-                             float *__restrict__ xc) {
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < gc.nCell;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    int gx, gy, gz;
-    cellOf(gc, c, gx, gy, gz);
+template <typename V>
+__global__ void kRestrictSum(LvGeom gf, LvGeom gc, const V *__restrict__ rf, V *__restrict__ bc, V *__restrict__ xc) {
+  GRID_STRIDE(c, gc.nCell) {
+    const Cell q = cellOf(gc, c);
     float s = 0.0f;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-      const int64_t j = cellIdx(gf, 2 * gx + (k & 1), 2 * gy + ((k >> 1) & 1), 2 * gz + (k >> 2));
-      if (j >= 0) s += rf[j];
+      const int64_t j = cellIdx(gf, 2 * q.gx + (k & 1), 2 * q.gy + ((k >> 1) & 1), 2 * q.gz + (k >> 2));
+      if (j >= 0) s += ldv(rf + j);
     }
-    bc[c] = s;
-    xc[c] = 0.0f;
+    stv(bc + c, s);
+    stv(xc + c, 0.0f);
   }
 }
 
 // x_F += P x_C (constant injection of the parent's value)
-__global__ void kProlongAdd(LvGeom gf, LvGeom gc, const float *__restrict__ xc, float *__restrict__ xf) {
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < gf.nCell;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    int gx, gy, gz;
-    cellOf(gf, c, gx, gy, gz);
-    const int64_t p = cellIdx(gc, gx >> 1, gy >> 1, gz >> 1);
-    if (p >= 0) xf[c] += xc[p];
+template <typename V>
+__global__ void kProlongAdd(LvGeom gf, LvGeom gc, const V *__restrict__ xc, V *__restrict__ xf) {
+  GRID_STRIDE(c, gf.nCell) {
+    const Cell q = cellOf(gf, c);
+    const int64_t p = cellIdx(gc, q.gx >> 1, q.gy >> 1, q.gz >> 1);
+    if (p >= 0) stv(xf + c, ldv(xf + c) + ldv(xc + p));
   }
 }
 
-// Coarse operator P^T A P / 2 from the fine level's coefficients.
-__global__ void kCoarseCoeffs(LvGeom gf, LvGeom gc, const float *__restrict__ fcx,
-                              const float *__restrict__ fcy, const float *__restrict__ fcz,
-                              const float *__restrict__ fd, float *__restrict__ ccx, float *__restrict__ ccy,
-                              float *__restrict__ ccz, float *__restrict__ cd) {
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < gc.nCell;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    int gx, gy, gz;
-    cellOf(gc, c, gx, gy, gz);
+// Coarse operator P^T A P / 2 from the fine level's coefficients (FP32).
+__global__ void kCoarseCoeffs(LvGeom gf, LvGeom gc, const float *__restrict__ fcx, const float *__restrict__ fcy,
+                              const float *__restrict__ fcz, const float *__restrict__ fd, float *__restrict__ ccx,
+                              float *__restrict__ ccy, float *__restrict__ ccz, float *__restrict__ cd) {
+  GRID_STRIDE(c, gc.nCell) {
+    const Cell q = cellOf(gc, c);
     int64_t ch[8];
 #pragma unroll
     for (int k = 0; k < 8; k++)
-      ch[k] = cellIdx(gf, 2 * gx + (k & 1), 2 * gy + ((k >> 1) & 1), 2 * gz + (k >> 2));
+      ch[k] = cellIdx(gf, 2 * q.gx + (k & 1), 2 * q.gy + ((k >> 1) & 1), 2 * q.gz + (k >> 2));
     double dsum = 0.0, lx = 0.0, ly = 0.0, lz = 0.0;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
       if (ch[k] < 0) continue;
       const int ix = k & 1, iy = (k >> 1) & 1, iz = k >> 2;
-      const int fx = 2 * gx + ix, fy = 2 * gy + iy, fz = 2 * gz + iz;
+      const int fx = 2 * q.gx + ix, fy = 2 * q.gy + iy, fz = 2 * q.gz + iz;
       dsum += fd[ch[k]];
-      // lower faces: external when the child sits on the coarse cell's lower side,
-      // internal otherwise (coupling to the sibling below)
+      // a child's lower face is external on the coarse cell's lower side, internal
+      // (coupling to the sibling below) otherwise
       if (ix == 0) { if (cellIdx(gf, fx - 1, fy, fz) >= 0) lx += fcx[ch[k]]; }
       else if (ch[k - 1] >= 0) dsum -= 2.0 * fcx[ch[k]];
       if (iy == 0) { if (cellIdx(gf, fx, fy - 1, fz) >= 0) ly += fcy[ch[k]]; }
@@ -226,6 +232,10 @@ __global__ void kCoarseCoeffs(LvGeom gf, LvGeom gc, const float *__restrict__ fc
     ccz[c] = (float)(0.5 * lz);
     cd[c] = (float)(0.5 * dsum);
   }
+}
+
+__global__ void kToHalf(const float *__restrict__ a, __half *__restrict__ b, int64_t n) {
+  GRID_STRIDE(i, n) b[i] = __float2half_rn(a[i]);
 }
 
 // ---- reductions ----------------------------------------------------------------------
@@ -247,12 +257,11 @@ __device__ __forceinline__ double blockSum(double v) {
   return v;
 }
 
-// partial[blockIdx] = sum a*b (FP64 accumulation of FP32 products)
-__global__ void kDotPartial(const float *__restrict__ a, const float *__restrict__ b, int64_t n,
-                            double *__restrict__ partial) {
+// partial[blockIdx] = sum a*b (FP64 accumulation)
+template <typename V>
+__global__ void kDotPartial(const V *__restrict__ a, const V *__restrict__ b, int64_t n, double *__restrict__ partial) {
   double s = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    s += (double)a[i] * (double)b[i];
+  GRID_STRIDE(i, n) s += (double)ldv(a + i) * (double)ldv(b + i);
   s = blockSum(s);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
@@ -264,17 +273,15 @@ __global__ void kSumPartials(const double *__restrict__ partial, int n, double *
   if (threadIdx.x == 0) *out = s;
 }
 
-// true residual in FP64: partial[block] = {sum (b - A x)^2, sum b^2}
+// true residual in FP64 (FP32 operator data): partial[block] = {sum (b - A x)^2, sum b^2}
 __global__ void kResidualNorm64(LvGeom g, const float *__restrict__ x, const float *__restrict__ b,
                                 const float *__restrict__ cx, const float *__restrict__ cy,
                                 const float *__restrict__ cz, const float *__restrict__ d,
                                 double *__restrict__ partial) {
   double rr = 0.0, bb = 0.0;
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < g.nCell;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    int gx, gy, gz;
-    cellOf(g, c, gx, gy, gz);
-    const double r = (double)b[c] - applyAt<double>(g, x, cx, cy, cz, d, c, gx, gy, gz);
+  GRID_STRIDE(c, g.nCell) {
+    const Cell q = cellOf(g, c);
+    const double r = (double)b[c] - applyAt<double>(x, cx, cy, cz, d, c, neighbours(g, c, q));
     rr += r * r;
     bb += (double)b[c] * (double)b[c];
   }
@@ -299,27 +306,33 @@ __global__ void kSumPartials2(const double *__restrict__ partial, int n, double 
 
 // CG updates with the scalars read from device memory (no host round trip):
 // alpha = sc[0] / sc[1]; x += alpha p; r -= alpha q
-__global__ void kCgUpdateXR(const double *__restrict__ sc, const float *__restrict__ p, const float *__restrict__ q,
-                            float *__restrict__ x, float *__restrict__ r, int64_t n) {
-  const double alpha = sc[1] != 0.0 ? sc[0] / sc[1] : 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] = (float)((double)x[i] + alpha * (double)p[i]);
-    r[i] = (float)((double)r[i] - alpha * (double)q[i]);
+template <typename V>
+__global__ void kCgUpdateXR(const double *__restrict__ sc, const V *__restrict__ p, const V *__restrict__ q,
+                            V *__restrict__ x, V *__restrict__ r, int64_t n) {
+  const float alpha = sc[1] != 0.0 ? (float)(sc[0] / sc[1]) : 0.0f;
+  GRID_STRIDE(i, n) {
+    stv(x + i, fmaf(alpha, ldv(p + i), ldv(x + i)));
+    stv(r + i, fmaf(-alpha, ldv(q + i), ldv(r + i)));
   }
 }
 // beta = sc[2] / sc[0]; p = z + beta p
-__global__ void kCgUpdateP(const double *__restrict__ sc, const float *__restrict__ z, float *__restrict__ p, int64_t n) {
-  const double beta = sc[0] != 0.0 ? sc[2] / sc[0] : 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = (float)((double)z[i] + beta * (double)p[i]);
+template <typename V>
+__global__ void kCgUpdateP(const double *__restrict__ sc, const V *__restrict__ z, V *__restrict__ p, int64_t n) {
+  const float beta = sc[0] != 0.0 ? (float)(sc[2] / sc[0]) : 0.0f;
+  GRID_STRIDE(i, n) stv(p + i, fmaf(beta, ldv(p + i), ldv(z + i)));
 }
-__global__ void kCopy(const float *__restrict__ a, float *__restrict__ b, int64_t n) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) b[i] = a[i];
+template <typename V>
+__global__ void kCopy(const V *__restrict__ a, V *__restrict__ b, int64_t n) {
+  GRID_STRIDE(i, n) b[i] = a[i];
+}
+template <typename V>
+__global__ void kZero(V *p, int64_t n) {
+  GRID_STRIDE(i, n) stv(p + i, 0.0f);
 }
 // AXPBYChannelCombined: X += aP; P = Q + bP (FP64 arithmetic, src/msbg.cpp:4651-4768)
 __global__ void kAxpbyCombined(double a, double b, const float *__restrict__ q, float *__restrict__ x,
                                float *__restrict__ p, int64_t n) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  GRID_STRIDE(i, n) {
     const double pi = p[i];
     x[i] = (float)((double)x[i] + a * pi);
     p[i] = (float)((double)q[i] + b * pi);
@@ -327,11 +340,20 @@ __global__ void kAxpbyCombined(double a, double b, const float *__restrict__ q, 
 }
 // AXPBYChannel: Y = aX + bY (src/msbg.cpp:4773-4872)
 __global__ void kAxpby(double a, const float *__restrict__ x, double b, float *__restrict__ y, int64_t n) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    y[i] = (float)(a * (double)x[i] + b * (double)y[i]);
+  GRID_STRIDE(i, n) y[i] = (float)(a * (double)x[i] + b * (double)y[i]);
 }
-__global__ void kZero(float *p, int64_t n) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = 0.0f;
+// mixed precision: rh = r / scale (FP16), scale from sc[0] = sum r^2
+__global__ void kScaleToHalf(const float *__restrict__ r, const double *__restrict__ sc, int64_t nCell,
+                             __half *__restrict__ rh, int64_t n) {
+  const double rms = sqrt(sc[0] / (double)(nCell > 0 ? nCell : 1));
+  const float inv = rms > 0.0 ? (float)(1.0 / rms) : 0.0f;
+  GRID_STRIDE(i, n) rh[i] = __float2half_rn(r[i] * inv);
+}
+// x += scale * e
+__global__ void kAddScaledHalf(const __half *__restrict__ e, const double *__restrict__ sc, int64_t nCell,
+                               float *__restrict__ x, int64_t n) {
+  const float rms = (float)sqrt(sc[0] / (double)(nCell > 0 ? nCell : 1));
+  GRID_STRIDE(i, n) x[i] = fmaf(rms, __half2float(e[i]), x[i]);
 }
 
 // Coarse level blocks: parent of every fine active block (block grid halved).
@@ -366,21 +388,19 @@ __device__ __forceinline__ float faceCoeff(uint32_t seed, int axis, int gx, int 
   h = hash32(h ^ (uint32_t)gx);
   h = hash32(h ^ (uint32_t)gy * 0x85ebca6bU);
   h = hash32(h ^ (uint32_t)gz * 0xc2b2ae35U);
-  return 0.5f + 1.5f * (float)(h >> 8) * (1.0f / 16777216.0f);
+  return __fadd_rn(0.5f, __fmul_rn(__fmul_rn(1.5f, (float)(h >> 8)), 1.0f / 16777216.0f));
 }
 // cx, cy, cz (lower faces) and d (all six faces) of level 0 from the seeded field
 __global__ void kProceduralCoeffs(LvGeom g, uint32_t seed, float *__restrict__ cx, float *__restrict__ cy,
                                   float *__restrict__ cz, float *__restrict__ d) {
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < g.nCell;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    int gx, gy, gz;
-    cellOf(g, c, gx, gy, gz);
-    const float lx = faceCoeff(seed, 0, gx, gy, gz), ly = faceCoeff(seed, 1, gx, gy, gz),
-                lz = faceCoeff(seed, 2, gx, gy, gz);
-    const float ux = faceCoeff(seed, 0, gx + 1, gy, gz), uy = faceCoeff(seed, 1, gx, gy + 1, gz),
-                uz = faceCoeff(seed, 2, gx, gy, gz + 1);
+  GRID_STRIDE(c, g.nCell) {
+    const Cell q = cellOf(g, c);
+    const float lx = faceCoeff(seed, 0, q.gx, q.gy, q.gz), ly = faceCoeff(seed, 1, q.gx, q.gy, q.gz),
+                lz = faceCoeff(seed, 2, q.gx, q.gy, q.gz);
+    const float ux = faceCoeff(seed, 0, q.gx + 1, q.gy, q.gz), uy = faceCoeff(seed, 1, q.gx, q.gy + 1, q.gz),
+                uz = faceCoeff(seed, 2, q.gx, q.gy, q.gz + 1);
     cx[c] = lx; cy[c] = ly; cz[c] = lz;
-    d[c] = ((lx + ux) + (ly + uy)) + (lz + uz);
+    d[c] = __fadd_rn(__fadd_rn(__fadd_rn(lx, ux), __fadd_rn(ly, uy)), __fadd_rn(lz, uz));
   }
 }
 
@@ -391,105 +411,38 @@ using namespace msbg;
 // =====================================================================================
 // host side
 // =====================================================================================
-namespace {
+namespace msbg {
 
-unsigned gridCells(int64_t n) {
+static unsigned gridCells(int64_t n) {
   int64_t g = (n + 255) / 256;
   if (g > 152 * 16) g = 152 * 16;
   if (g < 1) g = 1;
   return (unsigned)g;
 }
 
-void freeLevel(MgLevel &L) {
-  for (float **p : {&L.x, &L.b, &L.r, &L.cx, &L.cy, &L.cz, &L.d})
-    if (*p) { cudaFree(*p); *p = nullptr; }
-  if (L.ownsIndex) {
-    if (L.slot) cudaFree(L.slot);
-    if (L.active) cudaFree(L.active);
-  }
-  L.slot = nullptr;
-  L.active = nullptr;
+template <typename T>
+static int allocT(msbg_gpu_ctx *ctx, T **p, int64_t n) {
+  MSBG_CUDA(ctx, cudaMalloc((void **)p, (size_t)(n > 0 ? n : 1) * sizeof(T)));
+  return MSBG_GPU_OK;
 }
-
-}  // namespace
-
-namespace msbg {
 
 void poissonFree(PoissonState *ps) {
   if (!ps) return;
-  for (auto &L : ps->levels) freeLevel(L);
-  for (float **p : {&ps->r, &ps->p, &ps->z, &ps->s})
-    if (*p) cudaFree(*p);
+  for (auto &L : ps->levels) {
+    if (L.ownsIndex) {
+      if (L.slot) cudaFree(L.slot);
+      if (L.active) cudaFree(L.active);
+    }
+  }
+  for (PrecSet *P : {&ps->f32, &ps->f16}) {
+    for (auto *v : {&P->x, &P->b, &P->r, &P->cx, &P->cy, &P->cz, &P->d})
+      for (void *q : *v) if (q) cudaFree(q);
+    for (void *q : {P->vr, P->vp, P->vz, P->vs, P->ve, P->vb}) if (q) cudaFree(q);
+  }
   if (ps->dPartial) cudaFree(ps->dPartial);
   if (ps->dScal) cudaFree(ps->dScal);
   if (ps->hScal) cudaFreeHost(ps->hScal);
   delete ps;
-}
-
-static int allocF(msbg_gpu_ctx *ctx, float **p, int64_t n) {
-  MSBG_CUDA(ctx, cudaMalloc((void **)p, (size_t)(n > 0 ? n : 1) * sizeof(float)));
-  return MSBG_GPU_OK;
-}
-
-// Builds the level hierarchy over the context's current layout.
-static int buildHierarchy(msbg_gpu_ctx *ctx, PoissonState *ps) {
-  int rc;
-  MgLevel L0{};
-  L0.bs = ctx->bsx; L0.log2bs = ctx->log2bs;
-  L0.nbx = ctx->nbx; L0.nby = ctx->nby; L0.nbz = ctx->nbz;
-  L0.nAct = ctx->nActive; L0.nCell = ctx->nActive * ctx->voxPerBlock;
-  L0.slot = ctx->dSlot; L0.active = ctx->dActive; L0.ownsIndex = false;
-  ps->levels.push_back(L0);
-  // block edge halves on the same blocks
-  while (ps->levels.back().bs > 1) {
-    MgLevel f = ps->levels.back(), c{};
-    c = f;
-    c.bs = f.bs / 2; c.log2bs = f.log2bs - 1;
-    c.nCell = c.nAct << (3 * c.log2bs);
-    c.x = c.b = c.r = c.cx = c.cy = c.cz = c.d = nullptr;
-    c.ownsIndex = false;
-    ps->levels.push_back(c);
-  }
-  // then aggregate blocks of the block grid
-  while (true) {
-    const MgLevel &f = ps->levels.back();
-    if (f.nCell <= ps->coarsestCells || (f.nbx <= 2 && f.nby <= 2 && f.nbz <= 2)) break;
-    MgLevel c{};
-    c.bs = 1; c.log2bs = 0;
-    c.nbx = (f.nbx + 1) / 2; c.nby = (f.nby + 1) / 2; c.nbz = (f.nbz + 1) / 2;
-    const int64_t nB = (int64_t)c.nbx * c.nby * c.nbz;
-    MSBG_CUDA(ctx, cudaMalloc(&c.slot, (size_t)nB * 4));
-    MSBG_CUDA(ctx, cudaMalloc(&c.active, (size_t)nB * 4));
-    c.ownsIndex = true;
-    rc = ensureTmpSlab(ctx, (size_t)nB * 12 + 16);
-    if (rc) return rc;
-    int32_t *mark = (int32_t *)ctx->dTmpSlab;
-    int64_t *off = (int64_t *)((char *)ctx->dTmpSlab + (((size_t)nB * 4 + 15) & ~size_t(15)));
-    MSBG_CUDA(ctx, cudaMemsetAsync(mark, 0, (size_t)nB * 4, ctx->stream));
-    MSBG_LAUNCH(ctx, kMarkParents, gridFor(f.nAct, 256), 256, 0, f.active, f.nAct, f.nbx, f.nby, c.nbx, c.nby, mark);
-    rc = exclusiveScanFlags(ctx, mark, nB, off, ctx->dCounters + 5);
-    if (rc) return rc;
-    MSBG_LAUNCH(ctx, kSlotsFromMarks, gridFor(nB, 256), 256, 0, mark, off, nB, c.slot, c.active);
-    int64_t cnt = 0;
-    MSBG_CUDA(ctx, cudaMemcpyAsync(&cnt, ctx->dCounters + 5, 8, cudaMemcpyDeviceToHost, ctx->stream));
-    MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    c.nAct = cnt;
-    c.nCell = cnt;
-    ps->levels.push_back(c);
-  }
-  // storage: levels >= 1 own x, b, r and coefficients; level 0 coefficients too
-  for (size_t l = 0; l < ps->levels.size(); l++) {
-    MgLevel &L = ps->levels[l];
-    for (float **p : {&L.cx, &L.cy, &L.cz, &L.d}) if ((rc = allocF(ctx, p, L.nCell))) return rc;
-    if (l > 0) for (float **p : {&L.x, &L.b, &L.r}) if ((rc = allocF(ctx, p, L.nCell))) return rc;
-  }
-  const int64_t n0 = ps->levels[0].nCell;
-  for (float **p : {&ps->r, &ps->p, &ps->z, &ps->s}) if ((rc = allocF(ctx, p, n0))) return rc;
-  ps->nPartial = 152 * 16;
-  MSBG_CUDA(ctx, cudaMalloc(&ps->dPartial, (size_t)ps->nPartial * 2 * sizeof(double)));
-  MSBG_CUDA(ctx, cudaMalloc(&ps->dScal, 16 * sizeof(double)));
-  MSBG_CUDA(ctx, cudaMallocHost((void **)&ps->hScal, 16 * sizeof(double)));
-  return MSBG_GPU_OK;
 }
 
 LvGeom geomOf(const MgLevel &L) {
@@ -499,61 +452,231 @@ LvGeom geomOf(const MgLevel &L) {
   return g;
 }
 
-// coarse operators of all levels from level 0's coefficients
-static int buildCoarseOps(msbg_gpu_ctx *ctx, PoissonState *ps) {
-  for (size_t l = 1; l < ps->levels.size(); l++) {
-    MgLevel &F = ps->levels[l - 1], &C = ps->levels[l];
-    MSBG_LAUNCH(ctx, kCoarseCoeffs, gridCells(C.nCell), 256, 0, geomOf(F), geomOf(C), F.cx, F.cy, F.cz, F.d,
-                C.cx, C.cy, C.cz, C.d);
+// Level geometry over the context's current layout and the FP32 arrays.
+static int buildHierarchy(msbg_gpu_ctx *ctx, PoissonState *ps) {
+  int rc;
+  MgLevel L0{};
+  L0.bs = ctx->bsx; L0.log2bs = ctx->log2bs;
+  L0.nbx = ctx->nbx; L0.nby = ctx->nby; L0.nbz = ctx->nbz;
+  L0.nAct = ctx->nActive; L0.nCell = ctx->nActive * ctx->voxPerBlock;
+  L0.slot = ctx->dSlot; L0.active = ctx->dActive; L0.ownsIndex = false;
+  ps->levels.push_back(L0);
+  while (ps->levels.back().bs > 1) {  // block edge halves on the same blocks
+    MgLevel c = ps->levels.back();
+    c.bs /= 2; c.log2bs -= 1;
+    c.nCell = c.nAct << (3 * c.log2bs);
+    c.ownsIndex = false;
+    ps->levels.push_back(c);
   }
+  while (true) {  // then 2x2x2 aggregation of the block grid
+    const MgLevel &f = ps->levels.back();
+    if (f.nCell <= ps->coarsestCells || (f.nbx <= 2 && f.nby <= 2 && f.nbz <= 2)) break;
+    MgLevel c{};
+    c.bs = 1; c.log2bs = 0;
+    c.nbx = (f.nbx + 1) / 2; c.nby = (f.nby + 1) / 2; c.nbz = (f.nbz + 1) / 2;
+    const int64_t nB = (int64_t)c.nbx * c.nby * c.nbz;
+    MSBG_CUDA(ctx, cudaMalloc(&c.slot, (size_t)nB * 4));
+    MSBG_CUDA(ctx, cudaMalloc(&c.active, (size_t)nB * 4));
+    c.ownsIndex = true;
+    if ((rc = ensureTmpSlab(ctx, (size_t)nB * 12 + 16))) return rc;
+    int32_t *mark = (int32_t *)ctx->dTmpSlab;
+    int64_t *off = (int64_t *)((char *)ctx->dTmpSlab + (((size_t)nB * 4 + 15) & ~size_t(15)));
+    MSBG_CUDA(ctx, cudaMemsetAsync(mark, 0, (size_t)nB * 4, ctx->stream));
+    MSBG_LAUNCH(ctx, kMarkParents, gridFor(f.nAct, 256), 256, 0, f.active, f.nAct, f.nbx, f.nby, c.nbx, c.nby, mark);
+    if ((rc = exclusiveScanFlags(ctx, mark, nB, off, ctx->dCounters + 5))) return rc;
+    MSBG_LAUNCH(ctx, kSlotsFromMarks, gridFor(nB, 256), 256, 0, mark, off, nB, c.slot, c.active);
+    int64_t cnt = 0;
+    MSBG_CUDA(ctx, cudaMemcpyAsync(&cnt, ctx->dCounters + 5, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    c.nAct = cnt;
+    c.nCell = cnt;
+    ps->levels.push_back(c);
+  }
+  const size_t nL = ps->levels.size();
+  PrecSet &P = ps->f32;
+  for (auto *v : {&P.x, &P.b, &P.r, &P.cx, &P.cy, &P.cz, &P.d}) v->assign(nL, nullptr);
+  for (size_t l = 0; l < nL; l++) {
+    const int64_t n = ps->levels[l].nCell;
+    for (auto *v : {&P.cx, &P.cy, &P.cz, &P.d}) if ((rc = allocT(ctx, (float **)&(*v)[l], n))) return rc;
+    if (l > 0) for (auto *v : {&P.x, &P.b, &P.r}) if ((rc = allocT(ctx, (float **)&(*v)[l], n))) return rc;
+  }
+  const int64_t n0 = ps->levels[0].nCell;
+  for (void **q : {&P.vr, &P.vp, &P.vz, &P.vs}) if ((rc = allocT(ctx, (float **)q, n0))) return rc;
+  ps->nPartial = 152 * 16;
+  MSBG_CUDA(ctx, cudaMalloc(&ps->dPartial, (size_t)ps->nPartial * 2 * sizeof(double)));
+  MSBG_CUDA(ctx, cudaMalloc(&ps->dScal, 32 * sizeof(double)));
+  MSBG_CUDA(ctx, cudaMallocHost((void **)&ps->hScal, 32 * sizeof(double)));
   return MSBG_GPU_OK;
 }
 
-static int smooth(msbg_gpu_ctx *ctx, const MgLevel &L, float *x, const float *b, int nSweeps, bool redFirst) {
+// coarse operators of all levels from level 0's coefficients (FP32); drops FP16 copies
+static int buildCoarseOps(msbg_gpu_ctx *ctx, PoissonState *ps) {
+  PrecSet &P = ps->f32;
+  for (size_t l = 1; l < ps->levels.size(); l++) {
+    const MgLevel &F = ps->levels[l - 1], &C = ps->levels[l];
+    MSBG_LAUNCH(ctx, kCoarseCoeffs, gridCells(C.nCell), 256, 0, geomOf(F), geomOf(C), (float *)P.cx[l - 1],
+                (float *)P.cy[l - 1], (float *)P.cz[l - 1], (float *)P.d[l - 1], (float *)P.cx[l], (float *)P.cy[l],
+                (float *)P.cz[l], (float *)P.d[l]);
+  }
+  ps->f16Valid = false;
+  return MSBG_GPU_OK;
+}
+
+// FP16 copies of every level's coefficients and the FP16 work vectors
+static int ensureHalf(msbg_gpu_ctx *ctx, PoissonState *ps) {
+  if (ps->f16Valid) return MSBG_GPU_OK;
+  int rc;
+  PrecSet &H = ps->f16;
+  const size_t nL = ps->levels.size();
+  if (H.cx.size() != nL) {
+    for (auto *v : {&H.x, &H.b, &H.r, &H.cx, &H.cy, &H.cz, &H.d}) v->assign(nL, nullptr);
+    for (size_t l = 0; l < nL; l++) {
+      const int64_t n = ps->levels[l].nCell;
+      for (auto *v : {&H.cx, &H.cy, &H.cz, &H.d}) if ((rc = allocT(ctx, (__half **)&(*v)[l], n))) return rc;
+      if (l > 0) for (auto *v : {&H.x, &H.b, &H.r}) if ((rc = allocT(ctx, (__half **)&(*v)[l], n))) return rc;
+    }
+    const int64_t n0 = ps->levels[0].nCell;
+    for (void **q : {&H.vr, &H.vp, &H.vz, &H.vs, &H.ve, &H.vb}) if ((rc = allocT(ctx, (__half **)q, n0))) return rc;
+  }
+  for (size_t l = 0; l < nL; l++) {
+    const int64_t n = ps->levels[l].nCell;
+    void *src[4] = {ps->f32.cx[l], ps->f32.cy[l], ps->f32.cz[l], ps->f32.d[l]};
+    void *dst[4] = {H.cx[l], H.cy[l], H.cz[l], H.d[l]};
+    for (int k = 0; k < 4; k++) MSBG_LAUNCH(ctx, kToHalf, gridCells(n), 256, 0, (const float *)src[k], (__half *)dst[k], n);
+  }
+  ps->f16Valid = true;
+  return MSBG_GPU_OK;
+}
+
+template <typename V>
+struct Arr {
+  const PrecSet &P;
+  size_t l;
+  V *x() const { return (V *)P.x[l]; }
+  V *b() const { return (V *)P.b[l]; }
+  V *r() const { return (V *)P.r[l]; }
+  V *cx() const { return (V *)P.cx[l]; }
+  V *cy() const { return (V *)P.cy[l]; }
+  V *cz() const { return (V *)P.cz[l]; }
+  V *d() const { return (V *)P.d[l]; }
+};
+
+template <typename V>
+static int smoothT(msbg_gpu_ctx *ctx, PoissonState *ps, const PrecSet &P, size_t l, V *x, const V *b, int nSweeps,
+                   bool redFirst) {
+  const MgLevel &L = ps->levels[l];
   const LvGeom g = geomOf(L);
+  const Arr<V> a{P, l};
   for (int s = 0; s < nSweeps; s++)
     for (int k = 0; k < 2; k++) {
       const int color = redFirst ? k : 1 - k;
-      MSBG_LAUNCH(ctx, kRBGS, gridCells(L.nCell), 256, 0, g, x, b, L.cx, L.cy, L.cz, L.d, color);
+      MSBG_LAUNCH(ctx, (kRBGS<V, V>), gridCells(L.nCell), 256, 0, g, x, b, a.cx(), a.cy(), a.cz(), a.d(), color);
     }
   return MSBG_GPU_OK;
 }
 
-// One V-cycle: x = M^{-1} b on level l (x starts at zero).
-static int vcycle(msbg_gpu_ctx *ctx, PoissonState *ps, size_t l, float *x, const float *b, float *r) {
-  MgLevel &L = ps->levels[l];
-  const LvGeom g = geomOf(L);
-  int rc;
-  if (l + 1 == ps->levels.size()) {
-    MSBG_LAUNCH(ctx, kCoarsestGS, 1, 1024, 0, g, x, b, L.cx, L.cy, L.cz, L.d, ps->coarsestIter);
-    return MSBG_GPU_OK;
-  }
-  MSBG_LAUNCH(ctx, kZero, gridCells(L.nCell), 256, 0, x, L.nCell);
-  if ((rc = smooth(ctx, L, x, b, ps->preSweeps, true))) return rc;
-  MSBG_LAUNCH(ctx, kApply, gridCells(L.nCell), 256, 0, g, x, b, L.cx, L.cy, L.cz, L.d, r, 1);
-  MgLevel &C = ps->levels[l + 1];
-  MSBG_LAUNCH(ctx, kRestrictSum, gridCells(C.nCell), 256, 0, g, geomOf(C), r, C.b, C.x);
-  if ((rc = vcycle(ctx, ps, l + 1, C.x, C.b, C.r))) return rc;
-  MSBG_LAUNCH(ctx, kProlongAdd, gridCells(L.nCell), 256, 0, g, geomOf(C), C.x, x);
-  return smooth(ctx, L, x, b, ps->postSweeps, false);
+template <typename V>
+static int applyT(msbg_gpu_ctx *ctx, PoissonState *ps, const PrecSet &P, size_t l, const V *x, const V *b, V *y,
+                  int mode) {
+  const MgLevel &L = ps->levels[l];
+  const Arr<V> a{P, l};
+  MSBG_LAUNCH(ctx, (kApply<V, V>), gridCells(L.nCell), 256, 0, geomOf(L), x, b, a.cx(), a.cy(), a.cz(), a.d(), y,
+              mode);
+  return MSBG_GPU_OK;
 }
 
-static int dotDev(msbg_gpu_ctx *ctx, PoissonState *ps, const float *a, const float *b, int64_t n, double *dOut) {
-  MSBG_LAUNCH(ctx, kDotPartial, (unsigned)ps->nPartial, kRedThreads, 0, a, b, n, ps->dPartial);
+// One V-cycle: x = M^{-1} b on level l (x starts at zero).
+template <typename V>
+static int vcycleT(msbg_gpu_ctx *ctx, PoissonState *ps, const PrecSet &P, size_t l, V *x, const V *b, V *r) {
+  const MgLevel &L = ps->levels[l];
+  const LvGeom g = geomOf(L);
+  const Arr<V> a{P, l};
+  int rc;
+  if (l + 1 == ps->levels.size()) {
+    MSBG_LAUNCH(ctx, (kCoarsestGS<V, V>), 1, 1024, 0, g, x, b, a.cx(), a.cy(), a.cz(), a.d(), ps->coarsestIter);
+    return MSBG_GPU_OK;
+  }
+  MSBG_LAUNCH(ctx, (kZero<V>), gridCells(L.nCell), 256, 0, x, L.nCell);
+  if ((rc = smoothT<V>(ctx, ps, P, l, x, b, ps->preSweeps, true))) return rc;
+  if ((rc = applyT<V>(ctx, ps, P, l, x, b, r, 1))) return rc;
+  const MgLevel &C = ps->levels[l + 1];
+  const Arr<V> ac{P, l + 1};
+  MSBG_LAUNCH(ctx, (kRestrictSum<V>), gridCells(C.nCell), 256, 0, g, geomOf(C), (const V *)r, ac.b(), ac.x());
+  if ((rc = vcycleT<V>(ctx, ps, P, l + 1, ac.x(), ac.b(), ac.r()))) return rc;
+  MSBG_LAUNCH(ctx, (kProlongAdd<V>), gridCells(L.nCell), 256, 0, g, geomOf(C), (const V *)ac.x(), x);
+  return smoothT<V>(ctx, ps, P, l, x, b, ps->postSweeps, false);
+}
+
+template <typename V>
+static int dotDev(msbg_gpu_ctx *ctx, PoissonState *ps, const V *a, const V *b, int64_t n, double *dOut) {
+  MSBG_LAUNCH(ctx, (kDotPartial<V>), (unsigned)ps->nPartial, kRedThreads, 0, a, b, n, ps->dPartial);
   MSBG_LAUNCH(ctx, kSumPartials, 1, kRedThreads, 0, ps->dPartial, ps->nPartial, dOut);
   return MSBG_GPU_OK;
 }
 
-static int trueResidual(msbg_gpu_ctx *ctx, PoissonState *ps, const float *x, const float *b, double *rr,
-                        double *bb) {
-  const MgLevel &L = ps->levels[0];
-  MSBG_LAUNCH(ctx, kResidualNorm64, (unsigned)ps->nPartial, kRedThreads, 0, geomOf(L), x, b, L.cx, L.cy, L.cz,
-              L.d, ps->dPartial);
-  MSBG_LAUNCH(ctx, kSumPartials2, 1, kRedThreads, 0, ps->dPartial, ps->nPartial, ps->dScal + 8);
-  MSBG_CUDA(ctx, cudaMemcpyAsync(ps->hScal + 8, ps->dScal + 8, 16, cudaMemcpyDeviceToHost, ctx->stream));
+static int fetchScal(msbg_gpu_ctx *ctx, PoissonState *ps, int i, int n) {
+  MSBG_CUDA(ctx, cudaMemcpyAsync(ps->hScal + i, ps->dScal + i, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream));
   MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return MSBG_GPU_OK;
+}
+
+static int trueResidual(msbg_gpu_ctx *ctx, PoissonState *ps, const float *x, const float *b, double *rr, double *bb) {
+  const MgLevel &L = ps->levels[0];
+  const Arr<float> a{ps->f32, 0};
+  MSBG_LAUNCH(ctx, kResidualNorm64, (unsigned)ps->nPartial, kRedThreads, 0, geomOf(L), x, b, a.cx(), a.cy(), a.cz(),
+              a.d(), ps->dPartial);
+  MSBG_LAUNCH(ctx, kSumPartials2, 1, kRedThreads, 0, ps->dPartial, ps->nPartial, ps->dScal + 8);
+  int rc = fetchScal(ctx, ps, 8, 2);
+  if (rc) return rc;
   *rr = ps->hScal[8];
   *bb = ps->hScal[9];
+  return MSBG_GPU_OK;
+}
+
+// Preconditioned CG on level 0 in storage type V.  r must hold b - A x on entry.
+// Stops when the recurrence residual drops to relTol * r0norm (or maxIter); when
+// checkTrue (FP32 only) the stop is confirmed on the FP64 true residual of (x, b).
+// sc[0] rz, sc[1] pq, sc[2] rz_new, sc[3] rr.
+template <typename V>
+static int pcgT(msbg_gpu_ctx *ctx, PoissonState *ps, const PrecSet &P, V *x, const V *b, V *r, double stopNorm,
+                int maxIter, bool checkTrue, double bnorm, int *itersOut, double *relOut) {
+  const int64_t n = ps->levels[0].nCell;
+  V *p = (V *)P.vp, *z = (V *)P.vz, *s = (V *)P.vs;
+  double *sc = ps->dScal;
+  int rc;
+  if ((rc = vcycleT<V>(ctx, ps, P, 0, z, r, s))) return rc;
+  MSBG_LAUNCH(ctx, (kCopy<V>), gridCells(n), 256, 0, z, p, n);
+  if ((rc = dotDev<V>(ctx, ps, r, z, n, sc + 0))) return rc;
+  double prev = 1e300, rel = 0.0;
+  int growth = 0, it;
+  for (it = 1; it <= maxIter; it++) {
+    if ((rc = applyT<V>(ctx, ps, P, 0, p, nullptr, s, 0))) return rc;
+    if ((rc = dotDev<V>(ctx, ps, p, s, n, sc + 1))) return rc;
+    MSBG_LAUNCH(ctx, (kCgUpdateXR<V>), gridCells(n), 256, 0, sc, p, s, x, r, n);
+    if ((rc = dotDev<V>(ctx, ps, r, r, n, sc + 3))) return rc;
+    if ((rc = fetchScal(ctx, ps, 3, 1))) return rc;
+    const double rn = sqrt(ps->hScal[3]);
+    rel = rn / bnorm;
+    if (!isfinite(rn)) return fail(ctx, MSBG_GPU_ERR_DIVERGED, "residual is not finite at iteration %d", it);
+    growth = rn > prev ? growth + 1 : 0;
+    if (growth >= 8) return fail(ctx, MSBG_GPU_ERR_DIVERGED, "residual grew for 8 iterations (%g)", rel);
+    prev = rn;
+    if (rn <= stopNorm) {
+      if (!checkTrue) break;
+      double rr, bb;
+      if ((rc = trueResidual(ctx, ps, (const float *)x, (const float *)b, &rr, &bb))) return rc;
+      rel = sqrt(rr) / bnorm;
+      if (sqrt(rr) <= stopNorm) break;
+      if ((rc = applyT<V>(ctx, ps, P, 0, x, b, r, 1))) return rc;  // restart from the true residual
+    }
+    if ((rc = vcycleT<V>(ctx, ps, P, 0, z, r, s))) return rc;
+    if ((rc = dotDev<V>(ctx, ps, r, z, n, sc + 2))) return rc;
+    MSBG_LAUNCH(ctx, (kCgUpdateP<V>), gridCells(n), 256, 0, sc, z, p, n);
+    MSBG_CUDA(ctx, cudaMemcpyAsync(sc + 0, sc + 2, 8, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  if (it > maxIter) it = maxIter;
+  *itersOut = it;
+  *relOut = rel;
   return MSBG_GPU_OK;
 }
 
@@ -589,13 +712,13 @@ extern "C" int msbg_gpu_poisson_set_coefficients(msbg_gpu_ctx *ctx, int chanCx, 
   int rc = needLayoutP(ctx);
   if (rc) return rc;
   PoissonState *ps = ctx->poisson;
-  MgLevel &L = ps->levels[0];
+  const int64_t n = ps->levels[0].nCell;
   float *src[4];
   const int ch[4] = {chanCx, chanCy, chanCz, chanDiag};
   for (int k = 0; k < 4; k++) if ((rc = chanF32(ctx, ch[k], &src[k]))) return rc;
-  float *dst[4] = {L.cx, L.cy, L.cz, L.d};
+  void *dst[4] = {ps->f32.cx[0], ps->f32.cy[0], ps->f32.cz[0], ps->f32.d[0]};
   for (int k = 0; k < 4; k++)
-    MSBG_CUDA(ctx, cudaMemcpyAsync(dst[k], src[k], (size_t)L.nCell * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    MSBG_CUDA(ctx, cudaMemcpyAsync(dst[k], src[k], (size_t)n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
   ps->coeffsValid = true;
   return buildCoarseOps(ctx, ps);
 }
@@ -606,11 +729,11 @@ extern "C" int msbg_gpu_poisson_procedural_coefficients(msbg_gpu_ctx *ctx, uint3
   int rc = needLayoutP(ctx);
   if (rc) return rc;
   PoissonState *ps = ctx->poisson;
-  MgLevel &L = ps->levels[0];
-  MSBG_LAUNCH(ctx, kProceduralCoeffs, gridCells(L.nCell), 256, 0, geomOf(L), seed, L.cx, L.cy, L.cz, L.d);
+  const MgLevel &L = ps->levels[0];
+  float *dst[4] = {(float *)ps->f32.cx[0], (float *)ps->f32.cy[0], (float *)ps->f32.cz[0], (float *)ps->f32.d[0]};
+  MSBG_LAUNCH(ctx, kProceduralCoeffs, gridCells(L.nCell), 256, 0, geomOf(L), seed, dst[0], dst[1], dst[2], dst[3]);
   ps->coeffsValid = true;
   const int ch[4] = {chanCx, chanCy, chanCz, chanDiag};
-  float *dst[4] = {L.cx, L.cy, L.cz, L.d};
   for (int k = 0; k < 4; k++) {
     if (ch[k] < 0) continue;
     float *p;
@@ -634,9 +757,7 @@ extern "C" int msbg_gpu_multiply_laplacian(msbg_gpu_ctx *ctx, int chanX, int cha
   float *x, *b = nullptr, *y;
   if ((rc = chanF32(ctx, chanX, &x)) || (rc = chanF32(ctx, chanDstY, &y))) return rc;
   if (calcResidual && (rc = chanF32(ctx, chanB, &b))) return rc;
-  const MgLevel &L = ctx->poisson->levels[0];
-  MSBG_LAUNCH(ctx, kApply, gridCells(L.nCell), 256, 0, geomOf(L), x, b, L.cx, L.cy, L.cz, L.d, y, calcResidual ? 1 : 0);
-  return MSBG_GPU_OK;
+  return applyT<float>(ctx, ctx->poisson, ctx->poisson->f32, 0, x, b, y, calcResidual ? 1 : 0);
 }
 
 extern "C" int msbg_gpu_relax(msbg_gpu_ctx *ctx, int chanX, int chanB, int nIter, int reverseOrder) {
@@ -645,7 +766,7 @@ extern "C" int msbg_gpu_relax(msbg_gpu_ctx *ctx, int chanX, int chanB, int nIter
   if (rc) return rc;
   float *x, *b;
   if ((rc = chanF32(ctx, chanX, &x)) || (rc = chanF32(ctx, chanB, &b))) return rc;
-  return smooth(ctx, ctx->poisson->levels[0], x, b, nIter, !reverseOrder);
+  return smoothT<float>(ctx, ctx->poisson, ctx->poisson->f32, 0, x, b, nIter, !reverseOrder);
 }
 
 extern "C" int msbg_gpu_vcycle(msbg_gpu_ctx *ctx, int chanX, int chanB) {
@@ -654,7 +775,8 @@ extern "C" int msbg_gpu_vcycle(msbg_gpu_ctx *ctx, int chanX, int chanB) {
   if (rc) return rc;
   float *x, *b;
   if ((rc = chanF32(ctx, chanX, &x)) || (rc = chanF32(ctx, chanB, &b))) return rc;
-  return vcycle(ctx, ctx->poisson, 0, x, b, ctx->poisson->s);
+  PoissonState *ps = ctx->poisson;
+  return vcycleT<float>(ctx, ps, ps->f32, 0, x, b, (float *)ps->f32.vs);
 }
 
 extern "C" int msbg_gpu_dot(msbg_gpu_ctx *ctx, int chanA, int chanB, double *out) {
@@ -664,9 +786,8 @@ extern "C" int msbg_gpu_dot(msbg_gpu_ctx *ctx, int chanA, int chanB, double *out
   float *a, *b;
   if ((rc = chanF32(ctx, chanA, &a)) || (rc = chanF32(ctx, chanB, &b))) return rc;
   PoissonState *ps = ctx->poisson;
-  if ((rc = dotDev(ctx, ps, a, b, ps->levels[0].nCell, ps->dScal + 12))) return rc;
-  MSBG_CUDA(ctx, cudaMemcpyAsync(ps->hScal + 12, ps->dScal + 12, 8, cudaMemcpyDeviceToHost, ctx->stream));
-  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if ((rc = dotDev<float>(ctx, ps, a, b, ps->levels[0].nCell, ps->dScal + 12))) return rc;
+  if ((rc = fetchScal(ctx, ps, 12, 1))) return rc;
   *out = ps->hScal[12];
   if (!isfinite(*out)) return fail(ctx, MSBG_GPU_ERR_NONFINITE, "dot product is not finite");  // src/msbg.cpp:4635
   return MSBG_GPU_OK;
@@ -702,51 +823,66 @@ extern "C" int msbg_gpu_mgpcg_solve(msbg_gpu_ctx *ctx, int chanX, int chanB, dou
   float *x, *b;
   if ((rc = chanF32(ctx, chanX, &x)) || (rc = chanF32(ctx, chanB, &b))) return rc;
   PoissonState *ps = ctx->poisson;
-  const MgLevel &L = ps->levels[0];
-  const LvGeom g = geomOf(L);
-  const int64_t n = L.nCell;
-  double *sc = ps->dScal;  // [0] rz, [1] pq, [2] rz_new, [3] rr
-  // r = b - A x; z = M r; p = z; rz = <r,z>
-  MSBG_LAUNCH(ctx, kApply, gridCells(n), 256, 0, g, x, b, L.cx, L.cy, L.cz, L.d, ps->r, 1);
+  float *r = (float *)ps->f32.vr;
+  if ((rc = applyT<float>(ctx, ps, ps->f32, 0, x, b, r, 1))) return rc;
   double rr0, bb;
   if ((rc = trueResidual(ctx, ps, x, b, &rr0, &bb))) return rc;
   const double bnorm = sqrt(bb);
   double rel = bnorm > 0 ? sqrt(rr0) / bnorm : 0.0;
   int it = 0;
   if (bnorm > 0 && rel > tol) {
-    if ((rc = vcycle(ctx, ps, 0, ps->z, ps->r, ps->s))) return rc;
-    MSBG_LAUNCH(ctx, kCopy, gridCells(n), 256, 0, ps->z, ps->p, n);
-    if ((rc = dotDev(ctx, ps, ps->r, ps->z, n, sc + 0))) return rc;
-    double prevRel = rel;
-    int growth = 0;
-    for (it = 1; it <= maxIter; it++) {
-      MSBG_LAUNCH(ctx, kApply, gridCells(n), 256, 0, g, ps->p, nullptr, L.cx, L.cy, L.cz, L.d, ps->s, 0);
-      if ((rc = dotDev(ctx, ps, ps->p, ps->s, n, sc + 1))) return rc;
-      MSBG_LAUNCH(ctx, kCgUpdateXR, gridCells(n), 256, 0, sc, ps->p, ps->s, x, ps->r, n);
-      if ((rc = dotDev(ctx, ps, ps->r, ps->r, n, sc + 3))) return rc;
-      MSBG_CUDA(ctx, cudaMemcpyAsync(ps->hScal + 3, sc + 3, 8, cudaMemcpyDeviceToHost, ctx->stream));
-      MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-      rel = sqrt(ps->hScal[3]) / bnorm;
-      if (!isfinite(rel)) return fail(ctx, MSBG_GPU_ERR_DIVERGED, "residual is not finite at iteration %d", it);
-      growth = rel > prevRel ? growth + 1 : 0;
-      if (growth >= 8) return fail(ctx, MSBG_GPU_ERR_DIVERGED, "residual grew for 8 iterations (%g)", rel);
-      prevRel = rel;
-      if (rel <= tol) {
-        // confirm with the FP64 true residual; continue if the recurrence drifted
-        double rr;
-        if ((rc = trueResidual(ctx, ps, x, b, &rr, &bb))) return rc;
-        rel = sqrt(rr) / bnorm;
-        if (rel <= tol) break;
-        MSBG_LAUNCH(ctx, kApply, gridCells(n), 256, 0, g, x, b, L.cx, L.cy, L.cz, L.d, ps->r, 1);
-      }
-      if ((rc = vcycle(ctx, ps, 0, ps->z, ps->r, ps->s))) return rc;
-      if ((rc = dotDev(ctx, ps, ps->r, ps->z, n, sc + 2))) return rc;
-      MSBG_LAUNCH(ctx, kCgUpdateP, gridCells(n), 256, 0, sc, ps->z, ps->p, n);
-      MSBG_CUDA(ctx, cudaMemcpyAsync(sc + 0, sc + 2, 8, cudaMemcpyDeviceToDevice, ctx->stream));
-    }
-    if (it > maxIter) it = maxIter;
+    if ((rc = pcgT<float>(ctx, ps, ps->f32, x, b, r, tol * bnorm, maxIter, true, bnorm, &it, &rel))) return rc;
   }
   if (itersOut) *itersOut = it;
+  if (relResOut) *relResOut = rel;
+  return MSBG_GPU_OK;
+}
+
+extern "C" int msbg_gpu_mgpcg_solve_mixed(msbg_gpu_ctx *ctx, int chanX, int chanB, double tol, int maxOuter,
+                                          double innerTol, int maxInner, int *outerOut, int *innerTotalOut,
+                                          double *relResOut) {
+  if (!ctx || maxOuter < 0 || maxInner < 1 || !(tol > 0) || !(innerTol > 0 && innerTol < 1))
+    return MSBG_GPU_ERR_ARG;
+  int rc = needCoeffs(ctx);
+  if (rc) return rc;
+  float *x, *b;
+  if ((rc = chanF32(ctx, chanX, &x)) || (rc = chanF32(ctx, chanB, &b))) return rc;
+  PoissonState *ps = ctx->poisson;
+  if ((rc = ensureHalf(ctx, ps))) return rc;
+  const int64_t n = ps->levels[0].nCell;
+  float *r = (float *)ps->f32.vr;
+  __half *rh = (__half *)ps->f16.vb, *rw = (__half *)ps->f16.vr, *e = (__half *)ps->f16.ve;
+  double *sc = ps->dScal;
+  // outer residual in FP32 with the FP32 operator; its norm in FP64
+  double rr, bb;
+  if ((rc = trueResidual(ctx, ps, x, b, &rr, &bb))) return rc;
+  const double bnorm = sqrt(bb);
+  double rel = bnorm > 0 ? sqrt(rr) / bnorm : 0.0;
+  int outer = 0, innerTotal = 0;
+  while (bnorm > 0 && rel > tol && outer < maxOuter) {
+    outer++;
+    if ((rc = applyT<float>(ctx, ps, ps->f32, 0, x, b, r, 1))) return rc;
+    // rh = r / rms(r) in FP16 (keeps the inner problem O(1) in half range)
+    if ((rc = dotDev<float>(ctx, ps, r, r, n, sc + 16))) return rc;
+    MSBG_LAUNCH(ctx, kScaleToHalf, gridCells(n), 256, 0, r, sc + 16, n, rh, n);
+    MSBG_LAUNCH(ctx, (kZero<__half>), gridCells(n), 256, 0, e, n);
+    MSBG_LAUNCH(ctx, (kCopy<__half>), gridCells(n), 256, 0, rh, rw, n);
+    // inner FP16-storage MG-PCG on A e = rh to innerTol (relative to ||rh||)
+    if ((rc = dotDev<__half>(ctx, ps, rh, rh, n, sc + 17))) return rc;
+    if ((rc = fetchScal(ctx, ps, 17, 1))) return rc;
+    const double rhn = sqrt(ps->hScal[17]);
+    int itIn = 0;
+    double relIn = 0.0;
+    if ((rc = pcgT<__half>(ctx, ps, ps->f16, e, rh, rw, innerTol * rhn, maxInner, false, rhn, &itIn, &relIn)))
+      return rc;
+    innerTotal += itIn;
+    MSBG_LAUNCH(ctx, kAddScaledHalf, gridCells(n), 256, 0, e, sc + 16, n, x, n);
+    if ((rc = trueResidual(ctx, ps, x, b, &rr, &bb))) return rc;
+    rel = sqrt(rr) / bnorm;
+    if (!isfinite(rel)) return fail(ctx, MSBG_GPU_ERR_DIVERGED, "outer residual not finite");
+  }
+  if (outerOut) *outerOut = outer;
+  if (innerTotalOut) *innerTotalOut = innerTotal;
   if (relResOut) *relResOut = rel;
   return MSBG_GPU_OK;
 }

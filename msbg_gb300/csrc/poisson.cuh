@@ -15,20 +15,25 @@ struct LvGeom {
   const int32_t *active;  // [nAct] block ids
 };
 
-struct MgLevel {
+struct MgLevel {  // geometry of one level (arrays live in PrecSet)
   int bs = 0, log2bs = 0, nbx = 0, nby = 0, nbz = 0;
   int64_t nAct = 0, nCell = 0;
   int32_t *slot = nullptr, *active = nullptr;
   bool ownsIndex = false;
-  float *x = nullptr, *b = nullptr, *r = nullptr;             // levels >= 1
-  float *cx = nullptr, *cy = nullptr, *cz = nullptr, *d = nullptr;  // lower faces, diagonal
+};
+
+// Arrays of one storage precision: per level x, b, r (levels >= 1) and the
+// coefficients (lower faces cx, cy, cz and diagonal d); level-0 work vectors.
+struct PrecSet {
+  std::vector<void *> x, b, r, cx, cy, cz, d;
+  void *vr = nullptr, *vp = nullptr, *vz = nullptr, *vs = nullptr, *ve = nullptr, *vb = nullptr;
 };
 
 struct PoissonState {
   int64_t layoutStamp = -1;
   std::vector<MgLevel> levels;
-  bool coeffsValid = false;
-  float *r = nullptr, *p = nullptr, *z = nullptr, *s = nullptr;  // CG vectors on level 0
+  bool coeffsValid = false, f16Valid = false;
+  PrecSet f32, f16;
   double *dPartial = nullptr;
   int nPartial = 0;
   double *dScal = nullptr, *hScal = nullptr;

@@ -81,6 +81,7 @@ SIGNATURES = {
     "msbg_gpu_axpby_combined": (I, [P, D, D, I, I, I]),
     "msbg_gpu_mgpcg_solve": (I, [P, I, I, D, I, C.POINTER(I), C.POINTER(D)]),
     "msbg_gpu_mg_info": (I, [P, C.POINTER(I), P, I]),
+    "msbg_gpu_mgpcg_solve_mixed": (I, [P, I, I, D, I, D, I, C.POINTER(I), C.POINTER(I), C.POINTER(D)]),
 }
 
 _lib = None
@@ -344,6 +345,13 @@ class MultiresSparseGrid:
         it, rel = C.c_int(), C.c_double()
         self._check(self.L.msbg_gpu_mgpcg_solve(self.h, chanX, chanB, tol, max_iter, C.byref(it), C.byref(rel)))
         return it.value, rel.value
+
+    def mgpcg_solve_mixed(self, chanX: int, chanB: int, tol: float = 1e-6, max_outer: int = 10,
+                          inner_tol: float = 1e-3, max_inner: int = 60):
+        o, i, rel = C.c_int(), C.c_int(), C.c_double()
+        self._check(self.L.msbg_gpu_mgpcg_solve_mixed(self.h, chanX, chanB, tol, max_outer, inner_tol,
+                                                      max_inner, C.byref(o), C.byref(i), C.byref(rel)))
+        return o.value, i.value, rel.value
 
     def mg_info(self):
         n = C.c_int()

@@ -130,3 +130,37 @@ def test_mgpcg_solve_to_tolerance(setup):
     xs, it_ref, rel_ref = prob.solve(b.astype(np.float64), 1e-6)
     assert abs(it - it_ref) <= 2
     assert rel_l2(x, xs) < 1e-5
+
+
+def test_mixed_precision_solve_to_tolerance(setup):
+    """FP16-storage inner MG-PCG inside FP32 iterative refinement reaches the same
+    FP64-checked tolerance and the same solution as the FP32 solve."""
+    G, P, g, prob = setup
+    rng = np.random.default_rng(6)
+    b = _rand(prob, rng).astype(np.float32)
+    g.upload_payload(prob.payload(b), CH_B)
+    g.fill(0.0, CH_X)
+    outer, inner, rel = g.mgpcg_solve_mixed(CH_X, CH_B, tol=1e-6, max_outer=12, inner_tol=1e-2, max_inner=40)
+    x = prob.dense(g.payload(CH_X))
+    check = prob.rel_residual(x, b)
+    assert rel <= 1e-6 and check <= 1.5e-6, (outer, inner, rel, check)
+    assert 1 <= outer <= 12
+    xs, _, _ = prob.solve(b.astype(np.float64), 1e-6)
+    assert rel_l2(x, xs) < 1e-5
+
+
+def test_mixed_precision_warm_start_and_zero_rhs(setup):
+    G, P, g, prob = setup
+    g.fill(0.0, CH_B)
+    g.fill(0.0, CH_X)
+    outer, inner, rel = g.mgpcg_solve_mixed(CH_X, CH_B, tol=1e-6)
+    assert outer == 0 and inner == 0 and rel == 0.0
+    assert not np.any(g.payload(CH_X))
+    # an exact start needs no outer step
+    rng = np.random.default_rng(7)
+    b = _rand(prob, rng).astype(np.float32)
+    g.upload_payload(prob.payload(b), CH_B)
+    g.fill(0.0, CH_X)
+    g.mgpcg_solve(CH_X, CH_B, tol=5e-7, max_iter=100)
+    outer, inner, rel = g.mgpcg_solve_mixed(CH_X, CH_B, tol=1e-6)
+    assert outer == 0 and inner == 0 and rel <= 1e-6
