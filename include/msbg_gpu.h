@@ -221,6 +221,16 @@ int msbg_gpu_mgpcg_solve(msbg_gpu_ctx *ctx, int chanX, int chanB, double tol, in
 int msbg_gpu_mgpcg_solve_mixed(msbg_gpu_ctx *ctx, int chanX, int chanB, double tol, int maxOuter,
                                double innerTol, int maxInner, int *outerOut, int *innerTotalOut,
                                double *relResOut);
+/* Multigrid parameters (defaults 2, 2, 1, 0): smoothing passes before and
+ * after the coarse correction, in-tile red-black sweeps per pass (levels with
+ * block edge >= 8 smooth 16^3 / 8^3 tiles in two tile colours; smaller levels
+ * do that many pointwise red-black sweeps), and the coarsest level's solver:
+ * 0 = exact (dense inverse from an FP64 Cholesky factor), > 0 = that many
+ * red-black sweeps from zero.  Pre-smoothing orders tile colours 0,1 and cells red first;
+ * post-smoothing uses the reverse (adjoint) order, which keeps the V-cycle a
+ * symmetric preconditioner. */
+int msbg_gpu_poisson_set_params(msbg_gpu_ctx *ctx, int preSweeps, int postSweeps, int tileIters,
+                                int coarsestIter);
 /* Multigrid levels of the current hierarchy and their cell counts. */
 int msbg_gpu_mg_info(msbg_gpu_ctx *ctx, int *nLevels, int64_t *cellsPerLevel, int cap);
 

@@ -68,6 +68,7 @@ struct msbg_gpu_ctx {
   int64_t launches = 0;
   int64_t layoutStamp = 0;                 // bumped by every set_refinement_map
   msbg::PoissonState *poisson = nullptr;   // solver hierarchy of the current layout
+  int mgPre = 2, mgPost = 2, mgTileIters = 1, mgCoarsestIter = 0;  // multigrid parameters
   std::string err;
 };
 

@@ -45,14 +45,6 @@
 namespace msbg {
 
 // ---------------------------------------------------------------------------------
-// storage types: FP32, or FP16 (mixed precision); arithmetic is FP32
-// ---------------------------------------------------------------------------------
-__device__ __forceinline__ float ldv(const float *p) { return *p; }
-__device__ __forceinline__ float ldv(const __half *p) { return __half2float(*p); }
-__device__ __forceinline__ void stv(float *p, float v) { *p = v; }
-__device__ __forceinline__ void stv(__half *p, float v) { *p = __float2half_rn(v); }
-
-// ---------------------------------------------------------------------------------
 // cell addressing on a level
 // ---------------------------------------------------------------------------------
 struct Cell {
@@ -239,24 +231,6 @@ __global__ void kToHalf(const float *__restrict__ a, __half *__restrict__ b, int
 }
 
 // ---- reductions ----------------------------------------------------------------------
-constexpr int kRedThreads = 256;
-
-__device__ __forceinline__ double blockSum(double v) {
-  __shared__ double ws[kRedThreads / 32];
-#pragma unroll
-  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) ws[w] = v;
-  __syncthreads();
-  v = threadIdx.x < kRedThreads / 32 ? ws[threadIdx.x] : 0.0;
-  if (w == 0) {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  }
-  __syncthreads();
-  return v;
-}
-
 // partial[blockIdx] = sum a*b (FP64 accumulation)
 template <typename V>
 __global__ void kDotPartial(const V *__restrict__ a, const V *__restrict__ b, int64_t n, double *__restrict__ partial) {
@@ -305,15 +279,21 @@ __global__ void kSumPartials2(const double *__restrict__ partial, int n, double 
 }
 
 // CG updates with the scalars read from device memory (no host round trip):
-// alpha = sc[0] / sc[1]; x += alpha p; r -= alpha q
+// alpha = sc[0] / sc[1]; x += alpha p; r -= alpha q; partial[block] = sum r^2 (new r)
 template <typename V>
 __global__ void kCgUpdateXR(const double *__restrict__ sc, const V *__restrict__ p, const V *__restrict__ q,
-                            V *__restrict__ x, V *__restrict__ r, int64_t n) {
+                            V *__restrict__ x, V *__restrict__ r, int64_t n, double *__restrict__ partial) {
   const float alpha = sc[1] != 0.0 ? (float)(sc[0] / sc[1]) : 0.0f;
+  double rr = 0.0;
   GRID_STRIDE(i, n) {
     stv(x + i, fmaf(alpha, ldv(p + i), ldv(x + i)));
-    stv(r + i, fmaf(-alpha, ldv(q + i), ldv(r + i)));
+    const float rn = fmaf(-alpha, ldv(q + i), ldv(r + i));
+    stv(r + i, rn);
+    const double rs = ldv(r + i);  // the stored value
+    rr += rs * rs;
   }
+  rr = blockSum(rr);
+  if (threadIdx.x == 0) partial[blockIdx.x] = rr;
 }
 // beta = sc[2] / sc[0]; p = z + beta p
 template <typename V>
@@ -375,6 +355,37 @@ __global__ void kSlotsFromMarks(const int32_t *__restrict__ mark, const int64_t 
   } else {
     slot[i] = -1;
   }
+}
+
+// ---- coarsest level: exact solve with a dense inverse ---------------------------
+// A[c][c] = d_c, A[c][nb] = -c_f (FP64, row-major, n = cells of the level)
+__global__ void kDenseOperator(LvGeom g, const float *__restrict__ cx, const float *__restrict__ cy,
+                               const float *__restrict__ cz, const float *__restrict__ d, double *__restrict__ A,
+                               int64_t n) {
+  GRID_STRIDE(c, g.nCell) {
+    const Cell q = cellOf(g, c);
+    const Nb6 nb = neighbours(g, c, q);
+    double *row = A + c * n;
+    row[c] = d[c];
+    if (nb.xm >= 0) row[nb.xm] = -(double)cx[c];
+    if (nb.xp >= 0) row[nb.xp] = -(double)cx[nb.xp];
+    if (nb.ym >= 0) row[nb.ym] = -(double)cy[c];
+    if (nb.yp >= 0) row[nb.yp] = -(double)cy[nb.yp];
+    if (nb.zm >= 0) row[nb.zm] = -(double)cz[c];
+    if (nb.zp >= 0) row[nb.zp] = -(double)cz[nb.zp];
+  }
+}
+// x = inv b, one warp per row
+template <typename V>
+__global__ void kCoarsestDense(const float *__restrict__ inv, const V *__restrict__ b, V *__restrict__ x, int n) {
+  const int row = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const float *a = inv + (int64_t)row * n;
+  float s = 0.f;
+  for (int j = lane; j < n; j += 32) s = fmaf(a[j], ldv(b + j), s);
+#pragma unroll
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) stv(x + row, s);
 }
 
 // ---- procedural workload fields --------------------------------------------------
@@ -439,6 +450,10 @@ void poissonFree(PoissonState *ps) {
       for (void *q : *v) if (q) cudaFree(q);
     for (void *q : {P->vr, P->vp, P->vz, P->vs, P->ve, P->vb}) if (q) cudaFree(q);
   }
+  if (ps->dCoarseInv) cudaFree(ps->dCoarseInv);
+  if (ps->dNbr) cudaFree(ps->dNbr);
+  if (ps->dBpar) cudaFree(ps->dBpar);
+  if (ps->dParList) cudaFree(ps->dParList);
   if (ps->dPartial) cudaFree(ps->dPartial);
   if (ps->dScal) cudaFree(ps->dScal);
   if (ps->hScal) cudaFreeHost(ps->hScal);
@@ -460,6 +475,7 @@ static int buildHierarchy(msbg_gpu_ctx *ctx, PoissonState *ps) {
   L0.nbx = ctx->nbx; L0.nby = ctx->nby; L0.nbz = ctx->nbz;
   L0.nAct = ctx->nActive; L0.nCell = ctx->nActive * ctx->voxPerBlock;
   L0.slot = ctx->dSlot; L0.active = ctx->dActive; L0.ownsIndex = false;
+  L0.sameSet = true;
   ps->levels.push_back(L0);
   while (ps->levels.back().bs > 1) {  // block edge halves on the same blocks
     MgLevel c = ps->levels.back();
@@ -468,6 +484,9 @@ static int buildHierarchy(msbg_gpu_ctx *ctx, PoissonState *ps) {
     c.ownsIndex = false;
     ps->levels.push_back(c);
   }
+  // smoother tiles: 32x16x8 on bs-32 levels, the block on bs-16 and bs-8 levels,
+  // pointwise red-black below
+  for (auto &L : ps->levels) L.tile = (L.sameSet && L.bs >= 8) ? L.bs : 0;
   while (true) {  // then 2x2x2 aggregation of the block grid
     const MgLevel &f = ps->levels.back();
     if (f.nCell <= ps->coarsestCells || (f.nbx <= 2 && f.nby <= 2 && f.nbz <= 2)) break;
@@ -506,10 +525,77 @@ static int buildHierarchy(msbg_gpu_ctx *ctx, PoissonState *ps) {
   MSBG_CUDA(ctx, cudaMalloc(&ps->dPartial, (size_t)ps->nPartial * 2 * sizeof(double)));
   MSBG_CUDA(ctx, cudaMalloc(&ps->dScal, 32 * sizeof(double)));
   MSBG_CUDA(ctx, cudaMallocHost((void **)&ps->hScal, 32 * sizeof(double)));
+  return blkBuildTables(ctx, ps);
+}
+
+// Inverse of a symmetric positive definite matrix (row-major, n x n) through its
+// Cholesky factor, in FP64; false when a pivot is not positive.
+static bool spdInverse(std::vector<double> &A, int n, std::vector<float> &inv) {
+  std::vector<double> &L = A;  // factor in place (lower triangle)
+  for (int j = 0; j < n; j++) {
+    double s = L[(size_t)j * n + j];
+    for (int k = 0; k < j; k++) s -= L[(size_t)j * n + k] * L[(size_t)j * n + k];
+    if (!(s > 0.0)) return false;
+    const double dj = sqrt(s);
+    L[(size_t)j * n + j] = dj;
+    for (int i = j + 1; i < n; i++) {
+      double t = L[(size_t)i * n + j];
+      for (int k = 0; k < j; k++) t -= L[(size_t)i * n + k] * L[(size_t)j * n + k];
+      L[(size_t)i * n + j] = t / dj;
+    }
+  }
+  inv.assign((size_t)n * n, 0.0f);
+  std::vector<double> y(n);
+  for (int c = 0; c < n; c++) {
+    for (int i = 0; i < n; i++) {  // L y = e_c
+      double t = i == c ? 1.0 : 0.0;
+      for (int k = 0; k < i; k++) t -= L[(size_t)i * n + k] * y[k];
+      y[i] = t / L[(size_t)i * n + i];
+    }
+    for (int i = n - 1; i >= 0; i--) {  // L^T x = y
+      double t = y[i];
+      for (int k = i + 1; k < n; k++) t -= L[(size_t)k * n + i] * y[k];
+      y[i] = t / L[(size_t)i * n + i];
+    }
+    for (int i = 0; i < n; i++) inv[(size_t)i * n + c] = (float)y[i];
+  }
+  return true;
+}
+
+static int buildCoarseInverse(msbg_gpu_ctx *ctx, PoissonState *ps) {
+  const size_t l = ps->levels.size() - 1;
+  const MgLevel &C = ps->levels[l];
+  const int64_t n = C.nCell;
+  ps->coarseInvValid = false;
+  if (n <= 0) return MSBG_GPU_OK;
+  if (n > 4096) return fail(ctx, MSBG_GPU_ERR_CAPACITY, "coarsest level has %lld cells", (long long)n);
+  int rc;
+  if ((rc = ensureTmpSlab(ctx, (size_t)n * n * 8))) return rc;
+  double *dA = (double *)ctx->dTmpSlab;
+  MSBG_CUDA(ctx, cudaMemsetAsync(dA, 0, (size_t)n * n * 8, ctx->stream));
+  const PrecSet &P = ps->f32;
+  MSBG_LAUNCH(ctx, kDenseOperator, gridCells(n), 256, 0, geomOf(C), (const float *)P.cx[l], (const float *)P.cy[l],
+              (const float *)P.cz[l], (const float *)P.d[l], dA, n);
+  std::vector<double> A((size_t)n * n);
+  MSBG_CUDA(ctx, cudaMemcpyAsync(A.data(), dA, (size_t)n * n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  std::vector<float> inv;
+  if (!spdInverse(A, (int)n, inv))
+    return fail(ctx, MSBG_GPU_ERR_DIVERGED, "coarsest operator is not positive definite");
+  if (ps->coarseInvN != n) {
+    if (ps->dCoarseInv) cudaFree(ps->dCoarseInv);
+    ps->dCoarseInv = nullptr;
+    MSBG_CUDA(ctx, cudaMalloc(&ps->dCoarseInv, (size_t)n * n * 4));
+    ps->coarseInvN = n;
+  }
+  MSBG_CUDA(ctx, cudaMemcpyAsync(ps->dCoarseInv, inv.data(), (size_t)n * n * 4, cudaMemcpyHostToDevice, ctx->stream));
+  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ps->coarseInvValid = true;
   return MSBG_GPU_OK;
 }
 
-// coarse operators of all levels from level 0's coefficients (FP32); drops FP16 copies
+// coarse operators of all levels from level 0's coefficients (FP32), the dense
+// inverse of the coarsest one; drops FP16 copies
 static int buildCoarseOps(msbg_gpu_ctx *ctx, PoissonState *ps) {
   PrecSet &P = ps->f32;
   for (size_t l = 1; l < ps->levels.size(); l++) {
@@ -519,7 +605,7 @@ static int buildCoarseOps(msbg_gpu_ctx *ctx, PoissonState *ps) {
                 (float *)P.cz[l], (float *)P.d[l]);
   }
   ps->f16Valid = false;
-  return MSBG_GPU_OK;
+  return buildCoarseInverse(ctx, ps);
 }
 
 // FP16 copies of every level's coefficients and the FP16 work vectors
@@ -561,31 +647,70 @@ struct Arr {
   V *d() const { return (V *)P.d[l]; }
 };
 
+// Smoothing passes on level l.  Tile levels: per pass the two tile colours (0,1;
+// reversed 1,0) with k in-tile red-black sweeps each.  Pointwise levels: k
+// red-black sweeps per pass.  first: kOwnZero for a pre-smoother whose x starts
+// at zero (x is not read), kOwnCorr for a post-smoother that adds the coarse
+// correction xc while it loads; other levels do those steps as separate kernels.
+enum { kFirstNone = 0, kFirstZero = 1, kFirstCorr = 2 };
+
 template <typename V>
-static int smoothT(msbg_gpu_ctx *ctx, PoissonState *ps, const PrecSet &P, size_t l, V *x, const V *b, int nSweeps,
-                   bool redFirst) {
+static int smoothLevel(msbg_gpu_ctx *ctx, PoissonState *ps, const PrecSet &P, size_t l, V *x, const V *b,
+                       int passes, bool reverse, int first, const V *xc) {
   const MgLevel &L = ps->levels[l];
+  const int k = ps->tileIters;
+  int rc;
+  if (L.tile) {
+    if (passes == 0) {
+      if (first == kFirstZero) MSBG_LAUNCH(ctx, (kZero<V>), gridCells(L.nCell), 256, 0, x, L.nCell);
+      if (first == kFirstCorr) {
+        const MgLevel &C = ps->levels[l + 1];
+        MSBG_LAUNCH(ctx, (kProlongAdd<V>), gridCells(L.nCell), 256, 0, geomOf(L), geomOf(C), xc, x);
+      }
+      return MSBG_GPU_OK;
+    }
+    for (int p = 0; p < passes; p++)
+      for (int i = 0; i < 2; i++) {
+        const int tc = reverse ? 1 - i : i;
+        int flags = 0;
+        if (p == 0 && first == kFirstZero) flags = i == 0 ? (kOwnZero | kHaloZero) : kOwnZero;
+        if (p == 0 && first == kFirstCorr) flags = i == 0 ? (kOwnCorr | kHaloCorr) : kOwnCorr;
+        if ((rc = blkSmoothColor<V>(ctx, ps, l, P, x, b, xc, tc, k, reverse ? 1 : 0, flags))) return rc;
+      }
+    return MSBG_GPU_OK;
+  }
   const LvGeom g = geomOf(L);
   const Arr<V> a{P, l};
-  for (int s = 0; s < nSweeps; s++)
-    for (int k = 0; k < 2; k++) {
-      const int color = redFirst ? k : 1 - k;
+  if (first == kFirstZero) MSBG_LAUNCH(ctx, (kZero<V>), gridCells(L.nCell), 256, 0, x, L.nCell);
+  if (first == kFirstCorr) {
+    const MgLevel &C = ps->levels[l + 1];
+    MSBG_LAUNCH(ctx, (kProlongAdd<V>), gridCells(L.nCell), 256, 0, g, geomOf(C), xc, x);
+  }
+  for (int s = 0; s < passes * k; s++)
+    for (int i = 0; i < 2; i++) {
+      const int color = reverse ? 1 - i : i;
       MSBG_LAUNCH(ctx, (kRBGS<V, V>), gridCells(L.nCell), 256, 0, g, x, b, a.cx(), a.cy(), a.cz(), a.d(), color);
     }
   return MSBG_GPU_OK;
 }
 
+// y = A x (mode 0) or y = b - A x (mode 1); dotOut: also sum x.y into *dotOut (device)
 template <typename V>
 static int applyT(msbg_gpu_ctx *ctx, PoissonState *ps, const PrecSet &P, size_t l, const V *x, const V *b, V *y,
-                  int mode) {
+                  int mode, double *dotOut = nullptr) {
   const MgLevel &L = ps->levels[l];
+  if (L.sameSet && L.bs >= 4) return blkApply<V>(ctx, ps, l, P, x, b, y, mode, dotOut, nullptr, nullptr);
   const Arr<V> a{P, l};
   MSBG_LAUNCH(ctx, (kApply<V, V>), gridCells(L.nCell), 256, 0, geomOf(L), x, b, a.cx(), a.cy(), a.cz(), a.d(), y,
               mode);
+  if (dotOut) {
+    MSBG_LAUNCH(ctx, (kDotPartial<V>), (unsigned)ps->nPartial, kRedThreads, 0, x, (const V *)y, L.nCell, ps->dPartial);
+    MSBG_LAUNCH(ctx, kSumPartials, 1, kRedThreads, 0, ps->dPartial, ps->nPartial, dotOut);
+  }
   return MSBG_GPU_OK;
 }
 
-// One V-cycle: x = M^{-1} b on level l (x starts at zero).
+// One V-cycle: x = M^{-1} b on level l (x starts at zero; its old content is ignored).
 template <typename V>
 static int vcycleT(msbg_gpu_ctx *ctx, PoissonState *ps, const PrecSet &P, size_t l, V *x, const V *b, V *r) {
   const MgLevel &L = ps->levels[l];
@@ -593,18 +718,25 @@ static int vcycleT(msbg_gpu_ctx *ctx, PoissonState *ps, const PrecSet &P, size_t
   const Arr<V> a{P, l};
   int rc;
   if (l + 1 == ps->levels.size()) {
-    MSBG_LAUNCH(ctx, (kCoarsestGS<V, V>), 1, 1024, 0, g, x, b, a.cx(), a.cy(), a.cz(), a.d(), ps->coarsestIter);
+    if (ps->coarsestIter > 0) {
+      MSBG_LAUNCH(ctx, (kCoarsestGS<V, V>), 1, 1024, 0, g, x, b, a.cx(), a.cy(), a.cz(), a.d(), ps->coarsestIter);
+    } else {
+      if (!ps->coarseInvValid) return fail(ctx, MSBG_GPU_ERR_STATE, "coarsest inverse missing");
+      MSBG_LAUNCH(ctx, (kCoarsestDense<V>), gridFor(L.nCell * 32, 256), 256, 0, ps->dCoarseInv, b, x, (int)L.nCell);
+    }
     return MSBG_GPU_OK;
   }
-  MSBG_LAUNCH(ctx, (kZero<V>), gridCells(L.nCell), 256, 0, x, L.nCell);
-  if ((rc = smoothT<V>(ctx, ps, P, l, x, b, ps->preSweeps, true))) return rc;
-  if ((rc = applyT<V>(ctx, ps, P, l, x, b, r, 1))) return rc;
+  if ((rc = smoothLevel<V>(ctx, ps, P, l, x, b, ps->preSweeps, false, kFirstZero, nullptr))) return rc;
   const MgLevel &C = ps->levels[l + 1];
   const Arr<V> ac{P, l + 1};
-  MSBG_LAUNCH(ctx, (kRestrictSum<V>), gridCells(C.nCell), 256, 0, g, geomOf(C), (const V *)r, ac.b(), ac.x());
+  if (L.sameSet && L.bs >= 4) {  // residual and restriction in one pass
+    if ((rc = blkApply<V>(ctx, ps, l, P, x, b, nullptr, 1, nullptr, ac.b(), ac.x()))) return rc;
+  } else {
+    if ((rc = applyT<V>(ctx, ps, P, l, x, b, r, 1))) return rc;
+    MSBG_LAUNCH(ctx, (kRestrictSum<V>), gridCells(C.nCell), 256, 0, g, geomOf(C), (const V *)r, ac.b(), ac.x());
+  }
   if ((rc = vcycleT<V>(ctx, ps, P, l + 1, ac.x(), ac.b(), ac.r()))) return rc;
-  MSBG_LAUNCH(ctx, (kProlongAdd<V>), gridCells(L.nCell), 256, 0, g, geomOf(C), (const V *)ac.x(), x);
-  return smoothT<V>(ctx, ps, P, l, x, b, ps->postSweeps, false);
+  return smoothLevel<V>(ctx, ps, P, l, x, b, ps->postSweeps, true, kFirstCorr, (const V *)ac.x());
 }
 
 template <typename V>
@@ -620,14 +752,11 @@ static int fetchScal(msbg_gpu_ctx *ctx, PoissonState *ps, int i, int n) {
   return MSBG_GPU_OK;
 }
 
+// ||b - A x||^2 and ||b||^2 with the residual in double-float arithmetic
 static int trueResidual(msbg_gpu_ctx *ctx, PoissonState *ps, const float *x, const float *b, double *rr, double *bb) {
-  const MgLevel &L = ps->levels[0];
-  const Arr<float> a{ps->f32, 0};
-  MSBG_LAUNCH(ctx, kResidualNorm64, (unsigned)ps->nPartial, kRedThreads, 0, geomOf(L), x, b, a.cx(), a.cy(), a.cz(),
-              a.d(), ps->dPartial);
-  MSBG_LAUNCH(ctx, kSumPartials2, 1, kRedThreads, 0, ps->dPartial, ps->nPartial, ps->dScal + 8);
-  int rc = fetchScal(ctx, ps, 8, 2);
-  if (rc) return rc;
+  int rc;
+  if ((rc = blkApply<float>(ctx, ps, 0, ps->f32, x, b, nullptr, 2, ps->dScal + 8, nullptr, nullptr))) return rc;
+  if ((rc = fetchScal(ctx, ps, 8, 2))) return rc;
   *rr = ps->hScal[8];
   *bb = ps->hScal[9];
   return MSBG_GPU_OK;
@@ -646,14 +775,12 @@ static int pcgT(msbg_gpu_ctx *ctx, PoissonState *ps, const PrecSet &P, V *x, con
   int rc;
   if ((rc = vcycleT<V>(ctx, ps, P, 0, z, r, s))) return rc;
   MSBG_LAUNCH(ctx, (kCopy<V>), gridCells(n), 256, 0, z, p, n);
-  if ((rc = dotDev<V>(ctx, ps, r, z, n, sc + 0))) return rc;
+  if ((rc = blkDot<V>(ctx, ps, r, z, n, sc + 0))) return rc;
   double prev = 1e300, rel = 0.0;
   int growth = 0, it;
   for (it = 1; it <= maxIter; it++) {
-    if ((rc = applyT<V>(ctx, ps, P, 0, p, nullptr, s, 0))) return rc;
-    if ((rc = dotDev<V>(ctx, ps, p, s, n, sc + 1))) return rc;
-    MSBG_LAUNCH(ctx, (kCgUpdateXR<V>), gridCells(n), 256, 0, sc, p, s, x, r, n);
-    if ((rc = dotDev<V>(ctx, ps, r, r, n, sc + 3))) return rc;
+    if ((rc = applyT<V>(ctx, ps, P, 0, p, nullptr, s, 0, sc + 1))) return rc;  // s = A p, sc[1] = p.s
+    if ((rc = blkUpdateXR<V>(ctx, ps, sc, p, s, x, r, n, sc + 3))) return rc;
     if ((rc = fetchScal(ctx, ps, 3, 1))) return rc;
     const double rn = sqrt(ps->hScal[3]);
     rel = rn / bnorm;
@@ -670,13 +797,26 @@ static int pcgT(msbg_gpu_ctx *ctx, PoissonState *ps, const PrecSet &P, V *x, con
       if ((rc = applyT<V>(ctx, ps, P, 0, x, b, r, 1))) return rc;  // restart from the true residual
     }
     if ((rc = vcycleT<V>(ctx, ps, P, 0, z, r, s))) return rc;
-    if ((rc = dotDev<V>(ctx, ps, r, z, n, sc + 2))) return rc;
-    MSBG_LAUNCH(ctx, (kCgUpdateP<V>), gridCells(n), 256, 0, sc, z, p, n);
+    if ((rc = blkDot<V>(ctx, ps, r, z, n, sc + 2))) return rc;
+    if ((rc = blkUpdateP<V>(ctx, ps, sc, z, p, n))) return rc;
     MSBG_CUDA(ctx, cudaMemcpyAsync(sc + 0, sc + 2, 8, cudaMemcpyDeviceToDevice, ctx->stream));
   }
   if (it > maxIter) it = maxIter;
   *itersOut = it;
   *relOut = rel;
+  return MSBG_GPU_OK;
+}
+
+// Device status after smoother launches: a bounded shared-memory wait that gave up
+// sets bit 1 (the launch then wrote nothing).
+static int checkStatus(msbg_gpu_ctx *ctx) {
+  int st = 0;
+  MSBG_CUDA(ctx, cudaMemcpyAsync(&st, ctx->dStatus, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (st) {
+    MSBG_CUDA(ctx, cudaMemsetAsync(ctx->dStatus, 0, sizeof(int), ctx->stream));
+    return fail(ctx, MSBG_GPU_ERR_TIMEOUT, "a smoother tile wait timed out (status %d)", st);
+  }
   return MSBG_GPU_OK;
 }
 
@@ -686,6 +826,8 @@ int poissonEnsure(msbg_gpu_ctx *ctx) {
   PoissonState *ps = new PoissonState();
   ctx->poisson = ps;
   ps->layoutStamp = ctx->layoutStamp;
+  ps->preSweeps = ctx->mgPre; ps->postSweeps = ctx->mgPost;
+  ps->tileIters = ctx->mgTileIters; ps->coarsestIter = ctx->mgCoarsestIter;
   return buildHierarchy(ctx, ps);
 }
 
@@ -766,7 +908,10 @@ extern "C" int msbg_gpu_relax(msbg_gpu_ctx *ctx, int chanX, int chanB, int nIter
   if (rc) return rc;
   float *x, *b;
   if ((rc = chanF32(ctx, chanX, &x)) || (rc = chanF32(ctx, chanB, &b))) return rc;
-  return smoothT<float>(ctx, ctx->poisson, ctx->poisson->f32, 0, x, b, nIter, !reverseOrder);
+  if ((rc = smoothLevel<float>(ctx, ctx->poisson, ctx->poisson->f32, 0, x, b, nIter, reverseOrder != 0, kFirstNone,
+                                nullptr)))
+    return rc;
+  return checkStatus(ctx);
 }
 
 extern "C" int msbg_gpu_vcycle(msbg_gpu_ctx *ctx, int chanX, int chanB) {
@@ -776,7 +921,8 @@ extern "C" int msbg_gpu_vcycle(msbg_gpu_ctx *ctx, int chanX, int chanB) {
   float *x, *b;
   if ((rc = chanF32(ctx, chanX, &x)) || (rc = chanF32(ctx, chanB, &b))) return rc;
   PoissonState *ps = ctx->poisson;
-  return vcycleT<float>(ctx, ps, ps->f32, 0, x, b, (float *)ps->f32.vs);
+  if ((rc = vcycleT<float>(ctx, ps, ps->f32, 0, x, b, (float *)ps->f32.vs))) return rc;
+  return checkStatus(ctx);
 }
 
 extern "C" int msbg_gpu_dot(msbg_gpu_ctx *ctx, int chanA, int chanB, double *out) {
@@ -835,7 +981,7 @@ extern "C" int msbg_gpu_mgpcg_solve(msbg_gpu_ctx *ctx, int chanX, int chanB, dou
   }
   if (itersOut) *itersOut = it;
   if (relResOut) *relResOut = rel;
-  return MSBG_GPU_OK;
+  return checkStatus(ctx);
 }
 
 extern "C" int msbg_gpu_mgpcg_solve_mixed(msbg_gpu_ctx *ctx, int chanX, int chanB, double tol, int maxOuter,
@@ -863,12 +1009,12 @@ extern "C" int msbg_gpu_mgpcg_solve_mixed(msbg_gpu_ctx *ctx, int chanX, int chan
     outer++;
     if ((rc = applyT<float>(ctx, ps, ps->f32, 0, x, b, r, 1))) return rc;
     // rh = r / rms(r) in FP16 (keeps the inner problem O(1) in half range)
-    if ((rc = dotDev<float>(ctx, ps, r, r, n, sc + 16))) return rc;
+    if ((rc = blkDot<float>(ctx, ps, r, r, n, sc + 16))) return rc;
     MSBG_LAUNCH(ctx, kScaleToHalf, gridCells(n), 256, 0, r, sc + 16, n, rh, n);
     MSBG_LAUNCH(ctx, (kZero<__half>), gridCells(n), 256, 0, e, n);
     MSBG_LAUNCH(ctx, (kCopy<__half>), gridCells(n), 256, 0, rh, rw, n);
     // inner FP16-storage MG-PCG on A e = rh to innerTol (relative to ||rh||)
-    if ((rc = dotDev<__half>(ctx, ps, rh, rh, n, sc + 17))) return rc;
+    if ((rc = blkDot<__half>(ctx, ps, rh, rh, n, sc + 17))) return rc;
     if ((rc = fetchScal(ctx, ps, 17, 1))) return rc;
     const double rhn = sqrt(ps->hScal[17]);
     int itIn = 0;
@@ -884,6 +1030,21 @@ extern "C" int msbg_gpu_mgpcg_solve_mixed(msbg_gpu_ctx *ctx, int chanX, int chan
   if (outerOut) *outerOut = outer;
   if (innerTotalOut) *innerTotalOut = innerTotal;
   if (relResOut) *relResOut = rel;
+  return checkStatus(ctx);
+}
+
+extern "C" int msbg_gpu_poisson_set_params(msbg_gpu_ctx *ctx, int preSweeps, int postSweeps, int tileIters,
+                                           int coarsestIter) {
+  if (!ctx || preSweeps < 0 || postSweeps < 0 || preSweeps > 16 || postSweeps > 16 || tileIters < 1 ||
+      tileIters > 16 || coarsestIter < 0 || coarsestIter > 100000)
+    return MSBG_GPU_ERR_ARG;
+  ctx->mgPre = preSweeps; ctx->mgPost = postSweeps;
+  ctx->mgTileIters = tileIters; ctx->mgCoarsestIter = coarsestIter;
+  if (ctx->poisson) {
+    PoissonState *ps = ctx->poisson;
+    ps->preSweeps = preSweeps; ps->postSweeps = postSweeps;
+    ps->tileIters = tileIters; ps->coarsestIter = coarsestIter;
+  }
   return MSBG_GPU_OK;
 }
 

@@ -1,0 +1,837 @@
+// Block-structured Poisson kernels for the multigrid levels that keep level 0's
+// block set (block edge bs = 32, 16, 8, 4 on a bs-32 layout): every cell finds
+// its neighbours by offset inside its block and through a per-block table of the
+// six face-neighbour slots across block faces, so no cell decodes a block id.
+//
+//   kApplyRows    y = A x, or r = b - A x, 4 cells along x per thread; with a
+//                 fused FP64 dot (x . A x, the CG step length) or a fused
+//                 restriction (the 8 children of a coarse cell sit in one
+//                 4-lane group: lanes differ in the y and z parity bits).
+//   kTileSmooth   one tile colour of the smoother: tiles of edge T (16 or 8) of
+//                 one colour ((gx/T + gy/T + gz/T) & 1) are staged in shared
+//                 memory with their one-cell halo by TMA, relaxed k times by
+//                 red-black Gauss-Seidel inside the tile, and written back once.  The
+//                 first pre-smoothing pass of a V-cycle starts from zero without
+//                 reading x; the first post-smoothing pass adds the coarse
+//                 correction (constant prolongation) while it loads.
+//
+// The reference relaxes red-black ordered blocks with block-local in-place
+// iterations (src/msbg3.cpp:2170-2369, _mgSmBlockIter src/msbg.cpp:814-843) and
+// evaluates the operator per block with a halo (src/msbg3.cpp:1281-1296); these
+// kernels keep that structure with tiles as the GPU's unit of shared memory.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_fp16.h>
+
+#include <mutex>
+
+#include "internal.cuh"
+#include "poisson.cuh"
+
+namespace msbg {
+
+__device__ __forceinline__ uint32_t smemAddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbarInit(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbarExpectTx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbarTryWait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smemAddr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Index of the cell at block-local (lx, ly, lz) of slot s, where at most one
+// coordinate may lie one block outside ([-bs, 2bs)); -1 when that block is absent.
+__device__ __forceinline__ int64_t cellAt(const BlkGeom &g, int s, int lx, int ly, int lz) {
+  const int bs = g.bs, L = g.log2bs;
+  int dir = -1;
+  if (lx < 0) { dir = 0; lx += bs; }
+  else if (lx >= bs) { dir = 1; lx -= bs; }
+  else if (ly < 0) { dir = 2; ly += bs; }
+  else if (ly >= bs) { dir = 3; ly -= bs; }
+  else if (lz < 0) { dir = 4; lz += bs; }
+  else if (lz >= bs) { dir = 5; lz -= bs; }
+  if (dir >= 0) {
+    s = g.nbr[(int64_t)s * 6 + dir];
+    if (s < 0) return -1;
+  }
+  return ((int64_t)s << (3 * L)) + ((int64_t)((lz << L) + ly) << L) + lx;
+}
+
+// Index on the coarse level (same blocks, edge bs/2) of the parent of fine cell j.
+__device__ __forceinline__ int64_t parentOf(int64_t j, int L) {
+  const int64_t s = j >> (3 * L);
+  const int v = (int)(j & ((1 << (3 * L)) - 1));
+  const int m = (1 << L) - 1;
+  const int lx = v & m, ly = (v >> L) & m, lz = v >> (2 * L);
+  const int Lc = L - 1;
+  return (s << (3 * Lc)) + ((int64_t)(((lz >> 1) << Lc) + (ly >> 1)) << Lc) + (lx >> 1);
+}
+
+// ---------------------------------------------------------------------------------
+// operator rows
+// ---------------------------------------------------------------------------------
+// Quad q of a block (4 cells along x) -> block-local origin.  Bits of q from the
+// bottom: x quad (log2(bs/4) bits), y parity, z parity, y pair, z pair; so the 8
+// children of a coarse cell pair are the 4 lanes {q, q^xq, q^2xq, q^3xq}.
+template <typename V>
+__global__ void __launch_bounds__(256) kApplyRows(BlkGeom g, const V *__restrict__ x, const V *__restrict__ b,
+                                                  const V *__restrict__ cx, const V *__restrict__ cy,
+                                                  const V *__restrict__ cz, const V *__restrict__ d,
+                                                  V *__restrict__ y, int mode, double *__restrict__ dotPartial,
+                                                  V *__restrict__ bc, V *__restrict__ xc) {
+  const int L = g.log2bs, bs = g.bs;
+  const int xb = L - 2;
+  const int qPerBlockLog = 3 * L - 2;
+  const int64_t nQuad = g.nAct << qPerBlockLog;
+  const int64_t nQuadPad = (nQuad + 31) & ~int64_t(31);
+  const int64_t sy = bs, sz = (int64_t)bs * bs;
+  double dot = 0.0, dot2 = 0.0;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nQuadPad;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const bool act = q < nQuad;
+    const int64_t qq = act ? q : 0;
+    const int s = (int)(qq >> qPerBlockLog);
+    const int qb = (int)(qq & ((int64_t(1) << qPerBlockLog) - 1));
+    const int qx = qb & ((1 << xb) - 1);
+    const int yp = (qb >> xb) & 1, zp = (qb >> (xb + 1)) & 1;
+    const int rest = qb >> (xb + 2);
+    const int yh = rest & ((bs >> 1) - 1), zh = rest >> (L - 1);
+    const int lx = qx << 2, ly = 2 * yh + yp, lz = 2 * zh + zp;
+    const int64_t base = (int64_t)s << (3 * L);
+    const int64_t c = base + ((int64_t)((lz << L) + ly) << L) + lx;
+
+    float xv[4], dv[4], cxv[4], cyv[4], czv[4], ym[4], yq[4], zm[4], zq[4], cyu[4], czu[4];
+    ldRow<4>(x + c, xv);
+    ldRow<4>(d + c, dv);
+    ldRow<4>(cx + c, cxv);
+    ldRow<4>(cy + c, cyv);
+    ldRow<4>(cz + c, czv);
+    float xl = 0.f, xr = 0.f, cxr = 0.f;
+    {
+      const int64_t j = lx > 0 ? c - 1 : cellAt(g, s, lx - 1, ly, lz);
+      if (j >= 0) xl = ldv(x + j);
+      const int64_t k = lx + 4 < bs ? c + 4 : cellAt(g, s, lx + 4, ly, lz);
+      if (k >= 0) { xr = ldv(x + k); cxr = ldv(cx + k); }
+    }
+    {
+      const int64_t j = ly > 0 ? c - sy : cellAt(g, s, lx, ly - 1, lz);
+      if (j >= 0) ldRow<4>(x + j, ym); else ym[0] = ym[1] = ym[2] = ym[3] = 0.f;
+      const int64_t k = ly + 1 < bs ? c + sy : cellAt(g, s, lx, ly + 1, lz);
+      if (k >= 0) { ldRow<4>(x + k, yq); ldRow<4>(cy + k, cyu); }
+      else { yq[0] = yq[1] = yq[2] = yq[3] = 0.f; cyu[0] = cyu[1] = cyu[2] = cyu[3] = 0.f; }
+    }
+    {
+      const int64_t j = lz > 0 ? c - sz : cellAt(g, s, lx, ly, lz - 1);
+      if (j >= 0) ldRow<4>(x + j, zm); else zm[0] = zm[1] = zm[2] = zm[3] = 0.f;
+      const int64_t k = lz + 1 < bs ? c + sz : cellAt(g, s, lx, ly, lz + 1);
+      if (k >= 0) { ldRow<4>(x + k, zq); ldRow<4>(cz + k, czu); }
+      else { zq[0] = zq[1] = zq[2] = zq[3] = 0.f; czu[0] = czu[1] = czu[2] = czu[3] = 0.f; }
+    }
+    float r[4];
+    if (mode == 2) {
+      // r = b - A x in double-float arithmetic: every product split exactly into
+      // a rounded part and its error (fma), the running sum kept exact with
+      // TwoSum and the errors gathered in a second float; then sum r^2, b^2.
+      float bv[4];
+      ldRow<4>(b + c, bv);
+      float rq = 0.f, bq = 0.f;
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const float xm1 = i == 0 ? xl : xv[i - 1];
+        const float xp1 = i == 3 ? xr : xv[i + 1];
+        const float cxp = i == 3 ? cxr : cxv[i + 1];
+        const float fa[7] = {-dv[i], cxv[i], cxp, cyv[i], cyu[i], czv[i], czu[i]};
+        const float fb[7] = {xv[i], xm1, xp1, ym[i], yq[i], zm[i], zq[i]};
+        float S = bv[i], E = 0.f;
+#pragma unroll
+        for (int t = 0; t < 7; t++) {
+          const float h = __fmul_rn(fa[t], fb[t]);
+          const float l = __fmaf_rn(fa[t], fb[t], -h);
+          const float sn = __fadd_rn(S, h);
+          const float bb2 = __fsub_rn(sn, S);
+          const float e = __fadd_rn(__fsub_rn(S, __fsub_rn(sn, bb2)), __fsub_rn(h, bb2));
+          S = sn;
+          E = __fadd_rn(E, __fadd_rn(e, l));
+        }
+        r[i] = __fadd_rn(S, E);
+        rq = fmaf(r[i], r[i], rq);
+        bq = fmaf(bv[i], bv[i], bq);
+      }
+      if (act) {
+        dot += (double)rq;
+        dot2 += (double)bq;
+      }
+      continue;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const float xm1 = i == 0 ? xl : xv[i - 1];
+      const float xp1 = i == 3 ? xr : xv[i + 1];
+      const float cxp = i == 3 ? cxr : cxv[i + 1];
+      float a = dv[i] * xv[i];
+      a -= cxv[i] * xm1;
+      a -= cxp * xp1;
+      a -= cyv[i] * ym[i];
+      a -= cyu[i] * yq[i];
+      a -= czv[i] * zm[i];
+      a -= czu[i] * zq[i];
+      r[i] = a;
+    }
+    if (mode == 1) {
+      float bv[4];
+      ldRow<4>(b + c, bv);
+#pragma unroll
+      for (int i = 0; i < 4; i++) r[i] = bv[i] - r[i];
+    }
+    if (dotPartial && act) {
+      float qd = 0.f;  // four products in FP32, then FP64 accumulation
+#pragma unroll
+      for (int i = 0; i < 4; i++) qd = fmaf(xv[i], r[i], qd);
+      dot += (double)qd;
+    }
+    if (bc) {
+      // sum the 8 children: x pairs in-thread, y and z parities across lanes
+      float p[2] = {r[0] + r[1], r[2] + r[3]};
+#pragma unroll
+      for (int i = 0; i < 2; i++) {
+        p[i] += __shfl_xor_sync(0xffffffffu, p[i], 1 << xb);
+        p[i] += __shfl_xor_sync(0xffffffffu, p[i], 2 << xb);
+      }
+      if (act && yp == 0 && zp == 0) {
+        const int Lc = L - 1;
+        const int64_t ci = ((int64_t)s << (3 * Lc)) + ((int64_t)((zh << Lc) + yh) << Lc) + (lx >> 1);
+        const float zz[2] = {0.f, 0.f};
+        stRow<2>(bc + ci, p);
+        stRow<2>(xc + ci, zz);
+      }
+    } else if (act && y) {
+      stRow<4>(y + c, r);
+    }
+  }
+  if (dotPartial) {
+    dot = blockSum(dot);
+    if (mode == 2) {
+      dot2 = blockSum(dot2);
+      if (threadIdx.x == 0) {
+        dotPartial[2 * blockIdx.x] = dot;
+        dotPartial[2 * blockIdx.x + 1] = dot2;
+      }
+    } else if (threadIdx.x == 0) {
+      dotPartial[blockIdx.x] = dot;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// tile smoother
+// ---------------------------------------------------------------------------------
+// Tiles: 32x16x8 cells on bs-32 levels (full 128-byte block rows, 8 tiles per
+// block), the whole block on bs-16 and bs-8 levels.  Tile colour =
+// (gx/TX + gy/TY + gz/TZ) & 1.  A CTA relaxes NT tiles; thread (tx, ty) of a tile
+// owns the column of cells (tx, ty, 0..TZ-1): its x values with the two z-halo
+// cells, b, 1/d and the z-face coefficients live in registers; the x values of
+// the whole tile live in shared memory ([z][y][x], dense), where the x and y
+// neighbours are read.  Lanes of a warp hold consecutive tx, so every shared
+// access of a warp is to consecutive words.  Both cell colours of a half step are
+// handled without divergence (each thread updates every other cell of its
+// column, starting at its parity).
+//
+// Loading: one thread per tile issues 3-D TMA boxes (cp.async.bulk.tensor) for the
+// tile's x, b, d, cx, cy, cz and for the y and z halo faces of x and the upper
+// y / z faces of cy / cz, all completing on one mbarrier.  A face whose
+// neighbour block is absent is requested at a coordinate outside the tensor and
+// arrives as zeros.  The x halo faces (x = -1, x = TX) and the upper x face of cx
+// start at an x not aligned to 16 bytes, so threads load them with plain loads
+// while the boxes are in flight.
+struct TileMaps {
+  CUtensorMap xM, xY, xZ, b, d, cx, cy, cyY, cz, czZ;
+};
+
+template <int BS> struct TileShape;
+template <> struct TileShape<32> { static constexpr int TX = 32, TY = 16, TZ = 8, NT = 1; };
+template <> struct TileShape<16> { static constexpr int TX = 16, TY = 16, TZ = 16, NT = 1; };
+template <> struct TileShape<8> { static constexpr int TX = 8, TY = 8, TZ = 8, NT = 4; };
+
+__device__ __forceinline__ void tmaLoad3(void *dst, const CUtensorMap *map, int c0, int c1, int c2, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smemAddr(dst)),
+      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smemAddr(bar))
+      : "memory");
+}
+
+// Byte offsets of one tile's buffers (each 128-byte aligned).
+template <typename V, int BS>
+struct TileSmem {
+  using Sh = TileShape<BS>;
+  static constexpr int TX = Sh::TX, TY = Sh::TY, TZ = Sh::TZ;
+  static constexpr int E = (int)sizeof(V);
+  static constexpr int C3 = TX * TY * TZ, CY2 = TX * TZ, CZ2 = TX * TY, CX2 = TY * TZ;
+  static constexpr int al(int b) { return (b + 127) & ~127; }
+  static constexpr int X = 0;                       // main boxes [z][y][x] (V)
+  static constexpr int B = X + al(C3 * E);
+  static constexpr int D = B + al(C3 * E);
+  static constexpr int CX = D + al(C3 * E);
+  static constexpr int CY = CX + al(C3 * E);
+  static constexpr int CZ = CY + al(C3 * E);
+  static constexpr int XYLO = CZ + al(C3 * E);      // x at y = -1, y = TY ([z][x], V)
+  static constexpr int XYHI = XYLO + al(CY2 * E);
+  static constexpr int XZLO = XYHI + al(CY2 * E);   // x at z = -1, z = TZ ([y][x], V)
+  static constexpr int XZHI = XZLO + al(CZ2 * E);
+  static constexpr int CYHI = XZHI + al(CZ2 * E);   // cy at y = TY ([z][x], V)
+  static constexpr int CZHI = CYHI + al(CY2 * E);   // cz at z = TZ ([y][x], V)
+  static constexpr int XXLO = CZHI + al(CZ2 * E);   // x at x = -1, x = TX ([z][y], float)
+  static constexpr int XXHI = XXLO + al(CX2 * 4);
+  static constexpr int CXHI = XXHI + al(CX2 * 4);   // cx at x = TX ([z][y], V)
+  // FP32 working copies (FP16 storage only): x and its y / z faces
+  static constexpr int WX = CXHI + al(CX2 * E);
+  static constexpr int WYLO = WX + (E == 4 ? 0 : al(C3 * 4));
+  static constexpr int WYHI = WYLO + (E == 4 ? 0 : al(CY2 * 4));
+  static constexpr int WZLO = WYHI + (E == 4 ? 0 : al(CY2 * 4));
+  static constexpr int WZHI = WZLO + (E == 4 ? 0 : al(CZ2 * 4));
+  static constexpr int BYTES = WZHI + (E == 4 ? 0 : al(CZ2 * 4));
+};
+template <int BS>
+constexpr int tileThreads() {
+  using Sh = TileShape<BS>;
+  return Sh::NT * Sh::TX * Sh::TY;
+}
+template <typename V, int BS>
+constexpr size_t tileSmemBytes() {
+  return (size_t)TileShape<BS>::NT * TileSmem<V, BS>::BYTES + 128;  // + mbarrier
+}
+
+template <typename V, int BS>
+__global__ void __launch_bounds__(tileThreads<BS>(), 2)
+    kTileSmooth(const __grid_constant__ TileMaps maps, BlkGeom g, V *__restrict__ x, const V *__restrict__ cxg,
+                const V *__restrict__ xc, int tc, int k, int reverse, int flags, int *__restrict__ status) {
+  using S = TileSmem<V, BS>;
+  using Sh = TileShape<BS>;
+  constexpr int TX = Sh::TX, TY = Sh::TY, TZ = Sh::TZ, NT = Sh::NT, TXY = TX * TY;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int tIn = threadIdx.x / TXY, r = threadIdx.x % TXY;
+  const int tx = r % TX, ty = r / TX;
+  unsigned char *tb = smem + tIn * S::BYTES;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + NT * S::BYTES);
+
+  const int L = g.log2bs;
+  const int64_t unit = (int64_t)blockIdx.x * NT + tIn;
+  int s = 0, ox = 0, oy = 0, oz = 0;
+  bool valid;
+  if (BS == 32) {  // 4 tiles of each colour per block: tz = j, ty from the colour
+    valid = unit < g.nAct * 4;
+    if (valid) {
+      s = (int)(unit >> 2);
+      const int j = (int)(unit & 3);
+      const int bxp = g.bpar[s] & 1;
+      oy = ((tc + bxp + j) & 1) * TY;
+      oz = j * TZ;
+    }
+  } else {         // the tile is the block: block parity lists
+    const int64_t nUnits = tc == 0 ? g.nEven : g.nAct - g.nEven;
+    valid = unit < nUnits;
+    if (valid) s = g.parList[tc == 0 ? unit : g.nEven + unit];
+  }
+  const bool ownZero = flags & kOwnZero, haloZero = flags & kHaloZero;
+  const bool ownCorr = flags & kOwnCorr, haloCorr = flags & kHaloCorr;
+  const int zb = s * BS;
+
+  if (threadIdx.x == 0) {
+    mbarInit(bar, NT);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (r == 0) {
+    if (valid) {
+      constexpr uint32_t B3 = S::C3 * S::E, BY = S::CY2 * S::E, BZ = S::CZ2 * S::E;
+      const uint32_t bytes = (ownZero ? 5 : 6) * B3 + (haloZero ? 0 : 2 * (BY + BZ)) + BY + BZ;
+      mbarExpectTx(bar, bytes);
+      if (!ownZero) tmaLoad3(tb + S::X, &maps.xM, ox, oy, zb + oz, bar);
+      tmaLoad3(tb + S::B, &maps.b, ox, oy, zb + oz, bar);
+      tmaLoad3(tb + S::D, &maps.d, ox, oy, zb + oz, bar);
+      tmaLoad3(tb + S::CX, &maps.cx, ox, oy, zb + oz, bar);
+      tmaLoad3(tb + S::CY, &maps.cy, ox, oy, zb + oz, bar);
+      tmaLoad3(tb + S::CZ, &maps.cz, ox, oy, zb + oz, bar);
+      const int32_t *nb = g.nbr + (int64_t)s * 6;
+      // y faces (box TX x 1 x TZ), z faces (box TX x TY x 1); absent -> outside -> zeros
+      int ylo, ylz, yhi, yhz, zlo, zhi;
+      if (oy > 0) { ylo = oy - 1; ylz = zb + oz; }
+      else { const int n = nb[2]; ylo = BS - 1; ylz = n >= 0 ? n * BS + oz : -2 * TZ; }
+      if (oy + TY < BS) { yhi = oy + TY; yhz = zb + oz; }
+      else { const int n = nb[3]; yhi = 0; yhz = n >= 0 ? n * BS + oz : -2 * TZ; }
+      if (oz > 0) zlo = zb + oz - 1;
+      else { const int n = nb[4]; zlo = n >= 0 ? n * BS + BS - 1 : -2; }
+      if (oz + TZ < BS) zhi = zb + oz + TZ;
+      else { const int n = nb[5]; zhi = n >= 0 ? n * BS : -2; }
+      if (!haloZero) {
+        tmaLoad3(tb + S::XYLO, &maps.xY, ox, ylo, ylz, bar);
+        tmaLoad3(tb + S::XYHI, &maps.xY, ox, yhi, yhz, bar);
+        tmaLoad3(tb + S::XZLO, &maps.xZ, ox, oy, zlo, bar);
+        tmaLoad3(tb + S::XZHI, &maps.xZ, ox, oy, zhi, bar);
+      }
+      tmaLoad3(tb + S::CYHI, &maps.cyY, ox, yhi, yhz, bar);
+      tmaLoad3(tb + S::CZHI, &maps.czZ, ox, oy, zhi, bar);
+    } else {
+      mbarExpectTx(bar, 0);
+    }
+  }
+  // plain loads of the x halo faces (x = -1, x = TX) and of cx at x = TX:
+  // face cell (y, z) = (r % TY, r / TY), layout [z][y]
+  float *xxlo = reinterpret_cast<float *>(tb + S::XXLO);
+  float *xxhi = reinterpret_cast<float *>(tb + S::XXHI);
+  V *cxhi = reinterpret_cast<V *>(tb + S::CXHI);
+  if (valid && r < S::CX2) {
+    const int j = r % TY, kk = r / TY;
+    const int64_t lo = cellAt(g, s, ox - 1, oy + j, oz + kk);
+    const int64_t hi = cellAt(g, s, ox + TX, oy + j, oz + kk);
+    float vlo = 0.f, vhi = 0.f;
+    V chi = V(0.f);
+    if (lo >= 0 && !haloZero) vlo = ldv(x + lo) + (haloCorr ? ldv(xc + parentOf(lo, L)) : 0.f);
+    if (hi >= 0) {
+      chi = cxg[hi];
+      if (!haloZero) vhi = ldv(x + hi) + (haloCorr ? ldv(xc + parentOf(hi, L)) : 0.f);
+    }
+    xxlo[r] = vlo;
+    xxhi[r] = vhi;
+    cxhi[r] = chi;
+  }
+  // coarse corrections of this thread's column (one parent per z pair)
+  float corr[TZ / 2];
+  if (valid && ownCorr) {
+    const int Lc = L - 1;
+    const int64_t pb = ((int64_t)s << (3 * Lc)) + ((ox + tx) >> 1) + ((int64_t)((oy + ty) >> 1) << Lc);
+#pragma unroll
+    for (int z = 0; z < TZ / 2; z++) corr[z] = ldv(xc + pb + ((int64_t)((oz >> 1) + z) << (2 * Lc)));
+  } else {
+#pragma unroll
+    for (int z = 0; z < TZ / 2; z++) corr[z] = 0.f;
+  }
+  // halo-face corrections (first post-smoothing launch), computed while the boxes fly:
+  // y-face cell (x, z) = (r % TX, r / TX) for r < TX*TZ; z-face cell (x, y) = (tx, ty)
+  float cy0 = 0.f, cy1 = 0.f, cz0 = 0.f, cz1 = 0.f;
+  if (valid && haloCorr) {
+    if (r < S::CY2) {
+      const int fx = r % TX, fz = r / TX;
+      const int64_t j0 = cellAt(g, s, ox + fx, oy - 1, oz + fz), j1 = cellAt(g, s, ox + fx, oy + TY, oz + fz);
+      if (j0 >= 0) cy0 = ldv(xc + parentOf(j0, L));
+      if (j1 >= 0) cy1 = ldv(xc + parentOf(j1, L));
+    }
+    const int64_t j2 = cellAt(g, s, ox + tx, oy + ty, oz - 1), j3 = cellAt(g, s, ox + tx, oy + ty, oz + TZ);
+    if (j2 >= 0) cz0 = ldv(xc + parentOf(j2, L));
+    if (j3 >= 0) cz1 = ldv(xc + parentOf(j3, L));
+  }
+  // wait for the boxes (bounded): one warp polls the barrier, the others sleep in
+  // __syncthreads, which also publishes the landed data to them; the decision is
+  // CTA-uniform
+  bool ok = true;
+  if (threadIdx.x < 32) {
+    int it = 0;
+    while (!mbarTryWait(bar, 0))
+      if (++it >= (1 << 22)) { ok = false; break; }
+  }
+  ok = __syncthreads_and(ok);
+  if (!ok) {
+    if (threadIdx.x == 0) atomicOr(status, 2);
+    for (int it = 0; it < (1 << 22); it++)
+      if (mbarTryWait(bar, 0)) break;  // no copy may land after exit
+    return;
+  }
+
+  // FP32 working copy of x and of its y / z halo faces
+  float *xs, *wylo, *wyhi, *wzlo, *wzhi;
+  if constexpr (S::E == 4) {
+    xs = reinterpret_cast<float *>(tb + S::X);
+    wylo = reinterpret_cast<float *>(tb + S::XYLO); wyhi = reinterpret_cast<float *>(tb + S::XYHI);
+    wzlo = reinterpret_cast<float *>(tb + S::XZLO); wzhi = reinterpret_cast<float *>(tb + S::XZHI);
+  } else {
+    xs = reinterpret_cast<float *>(tb + S::WX);
+    wylo = reinterpret_cast<float *>(tb + S::WYLO); wyhi = reinterpret_cast<float *>(tb + S::WYHI);
+    wzlo = reinterpret_cast<float *>(tb + S::WZLO); wzhi = reinterpret_cast<float *>(tb + S::WZHI);
+  }
+  const int own = ty * TX + tx;
+  float xr[TZ + 2], bb[TZ], rd[TZ], czr[TZ + 1];
+  {
+    const V *sx = reinterpret_cast<const V *>(tb + S::X), *sb = reinterpret_cast<const V *>(tb + S::B);
+    const V *sd = reinterpret_cast<const V *>(tb + S::D), *scz = reinterpret_cast<const V *>(tb + S::CZ);
+#pragma unroll
+    for (int z = 0; z < TZ; z++) {
+      float v = ownZero ? 0.f : ldv(sx + own + z * TXY);
+      v += corr[z >> 1];
+      xr[z + 1] = v;
+      xs[own + z * TXY] = v;
+      bb[z] = ldv(sb + own + z * TXY);
+      rd[z] = __frcp_rn(ldv(sd + own + z * TXY));
+      czr[z] = ldv(scz + own + z * TXY);
+    }
+    czr[TZ] = ldv(reinterpret_cast<const V *>(tb + S::CZHI) + own);
+  }
+  // halo faces in FP32: zero (first pre-smoothing launch) or + coarse correction
+  {
+    const V *fy0 = reinterpret_cast<const V *>(tb + S::XYLO), *fy1 = reinterpret_cast<const V *>(tb + S::XYHI);
+    const V *fz0 = reinterpret_cast<const V *>(tb + S::XZLO), *fz1 = reinterpret_cast<const V *>(tb + S::XZHI);
+    if (r < S::CY2) {
+      wylo[r] = haloZero ? 0.f : ldv(fy0 + r) + cy0;
+      wyhi[r] = haloZero ? 0.f : ldv(fy1 + r) + cy1;
+    }
+    wzlo[own] = haloZero ? 0.f : ldv(fz0 + own) + cz0;
+    wzhi[own] = haloZero ? 0.f : ldv(fz1 + own) + cz1;
+  }
+  __syncthreads();
+  xr[0] = wzlo[own];
+  xr[TZ + 1] = wzhi[own];
+  // neighbour sources (pointer, stride per z) inside the tile or on a halo face
+  const float *pxm = tx > 0 ? xs + own - 1 : xxlo + ty;
+  const int sxm = tx > 0 ? TXY : TY;
+  const float *pxp = tx < TX - 1 ? xs + own + 1 : xxhi + ty;
+  const int sxp = tx < TX - 1 ? TXY : TY;
+  const float *pym = ty > 0 ? xs + own - TX : wylo + tx;
+  const int sym = ty > 0 ? TXY : TX;
+  const float *pyp = ty < TY - 1 ? xs + own + TX : wyhi + tx;
+  const int syp = ty < TY - 1 ? TXY : TX;
+  const V *cxs = reinterpret_cast<const V *>(tb + S::CX) + own;
+  const V *cys = reinterpret_cast<const V *>(tb + S::CY) + own;
+  const V *pcxu = tx < TX - 1 ? cxs + 1 : cxhi + ty;
+  const int scxu = tx < TX - 1 ? TXY : TY;
+  const V *pcyu = ty < TY - 1 ? cys + TX : reinterpret_cast<const V *>(tb + S::CYHI) + tx;
+  const int scyu = ty < TY - 1 ? TXY : TX;
+  const int colPar = (tx + ty) & 1;
+  for (int it = 0; it < k; it++) {
+    for (int ci = 0; ci < 2; ci++) {
+      const int cc = reverse ? 1 - ci : ci;
+      if (valid) {
+        // cells z = 2m + p of this column have colour cc
+        const bool p = ((cc - colPar) & 1) != 0;
+        const int pz = p ? 1 : 0;
+#pragma unroll
+        for (int m = 0; m < TZ / 2; m++) {
+          const int z = 2 * m + pz;
+          const float zm = p ? xr[2 * m + 1] : xr[2 * m];
+          const float zp = p ? xr[2 * m + 3] : xr[2 * m + 2];
+          const float c0 = p ? czr[2 * m + 1] : czr[2 * m];
+          const float c1 = p ? czr[2 * m + 2] : czr[2 * m + 1];
+          float acc = p ? bb[2 * m + 1] : bb[2 * m];
+          const float rr = p ? rd[2 * m + 1] : rd[2 * m];
+          acc += ldv(cxs + z * TXY) * pxm[z * sxm];
+          acc += ldv(pcxu + z * scxu) * pxp[z * sxp];
+          acc += ldv(cys + z * TXY) * pym[z * sym];
+          acc += ldv(pcyu + z * scyu) * pyp[z * syp];
+          acc += c0 * zm;
+          acc += c1 * zp;
+          const float v = acc * rr;
+          xr[2 * m + 1] = p ? xr[2 * m + 1] : v;
+          xr[2 * m + 2] = p ? v : xr[2 * m + 2];
+          xs[own + z * TXY] = v;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (valid) {
+    const int64_t base = ((int64_t)s << (3 * L)) + ((int64_t)(oy + ty) << L) + ox + tx;
+#pragma unroll
+    for (int z = 0; z < TZ; z++) stv(x + base + ((int64_t)(oz + z) << (2 * L)), xr[z + 1]);
+  }
+}
+
+static __global__ void kSumPartialsBlk(const double *__restrict__ partial, int n, double *__restrict__ out) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[i];
+  s = blockSum(s);
+  if (threadIdx.x == 0) *out = s;
+}
+static __global__ void kSumPartialsBlk2(const double *__restrict__ partial, int n, double *__restrict__ out) {
+  double s0 = 0.0, s1 = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    s0 += partial[2 * i];
+    s1 += partial[2 * i + 1];
+  }
+  s0 = blockSum(s0);
+  s1 = blockSum(s1);
+  if (threadIdx.x == 0) { out[0] = s0; out[1] = s1; }
+}
+
+// ---------------------------------------------------------------------------------
+// CG vector kernels on level 0 (n a multiple of 4), 4 values per thread; FP32
+// products summed per group of 4, then accumulated in FP64.
+// ---------------------------------------------------------------------------------
+#define QUAD_STRIDE(q, nq) \
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < (nq); q += (int64_t)gridDim.x * blockDim.x)
+
+template <typename V>
+__global__ void __launch_bounds__(256) kDotQuad(const V *__restrict__ a, const V *__restrict__ b, int64_t nq,
+                                                double *__restrict__ partial) {
+  double s = 0.0;
+  QUAD_STRIDE(q, nq) {
+    float av[4], bv[4];
+    ldRow<4>(a + 4 * q, av);
+    ldRow<4>(b + 4 * q, bv);
+    float t = 0.f;
+#pragma unroll
+    for (int i = 0; i < 4; i++) t = fmaf(av[i], bv[i], t);
+    s += (double)t;
+  }
+  s = blockSum(s);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+// alpha = sc[0] / sc[1]; x += alpha p; r -= alpha q; partial = sum r^2 (stored r)
+template <typename V>
+__global__ void __launch_bounds__(256) kUpdateXRQuad(const double *__restrict__ sc, const V *__restrict__ p,
+                                                     const V *__restrict__ q, V *__restrict__ x, V *__restrict__ r,
+                                                     int64_t nq, double *__restrict__ partial) {
+  const float alpha = sc[1] != 0.0 ? (float)(sc[0] / sc[1]) : 0.0f;
+  double rr = 0.0;
+  QUAD_STRIDE(k, nq) {
+    float pv[4], qv[4], xv[4], rv[4];
+    ldRow<4>(p + 4 * k, pv);
+    ldRow<4>(q + 4 * k, qv);
+    ldRow<4>(x + 4 * k, xv);
+    ldRow<4>(r + 4 * k, rv);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      xv[i] = fmaf(alpha, pv[i], xv[i]);
+      rv[i] = fmaf(-alpha, qv[i], rv[i]);
+    }
+    stRow<4>(x + 4 * k, xv);
+    stRow<4>(r + 4 * k, rv);
+    float rs[4];
+    ldRow<4>(r + 4 * k, rs);  // the values as stored
+    float t = 0.f;
+#pragma unroll
+    for (int i = 0; i < 4; i++) t = fmaf(rs[i], rs[i], t);
+    rr += (double)t;
+  }
+  rr = blockSum(rr);
+  if (threadIdx.x == 0) partial[blockIdx.x] = rr;
+}
+// beta = sc[2] / sc[0]; p = z + beta p
+template <typename V>
+__global__ void __launch_bounds__(256) kUpdatePQuad(const double *__restrict__ sc, const V *__restrict__ z,
+                                                    V *__restrict__ p, int64_t nq) {
+  const float beta = sc[0] != 0.0 ? (float)(sc[2] / sc[0]) : 0.0f;
+  QUAD_STRIDE(k, nq) {
+    float zv[4], pv[4];
+    ldRow<4>(z + 4 * k, zv);
+    ldRow<4>(p + 4 * k, pv);
+#pragma unroll
+    for (int i = 0; i < 4; i++) pv[i] = fmaf(beta, pv[i], zv[i]);
+    stRow<4>(p + 4 * k, pv);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// tables
+// ---------------------------------------------------------------------------------
+__global__ void kNbrTable(const int32_t *__restrict__ active, int64_t nAct, int nbx, int nby, int nbz,
+                          const int32_t *__restrict__ slot, int32_t *__restrict__ nbr, int32_t *__restrict__ even,
+                          uint8_t *__restrict__ bpar) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nAct) return;
+  const int bid = active[s];
+  const int bx = bid % nbx, by = (bid / nbx) % nby, bz = bid / (nbx * nby);
+  const int dx[6] = {-1, 1, 0, 0, 0, 0}, dy[6] = {0, 0, -1, 1, 0, 0}, dz[6] = {0, 0, 0, 0, -1, 1};
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    const int x = bx + dx[k], y = by + dy[k], z = bz + dz[k];
+    int v = -1;
+    if (x >= 0 && y >= 0 && z >= 0 && x < nbx && y < nby && z < nbz) v = slot[((int64_t)z * nby + y) * nbx + x];
+    nbr[s * 6 + k] = v;
+  }
+  even[s] = ((bx + by + bz) & 1) == 0;
+  bpar[s] = (uint8_t)((bx & 1) | ((by & 1) << 1) | ((bz & 1) << 2));
+}
+__global__ void kParityList(const int32_t *__restrict__ even, const int64_t *__restrict__ off, int64_t nAct,
+                            const int64_t *__restrict__ nEvenPtr, int32_t *__restrict__ list) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nAct) return;
+  const int64_t nEven = *nEvenPtr;
+  list[even[s] ? off[s] : nEven + (s - off[s])] = (int32_t)s;
+}
+
+int blkBuildTables(msbg_gpu_ctx *ctx, PoissonState *ps) {
+  const MgLevel &L0 = ps->levels[0];
+  const int64_t n = L0.nAct;
+  MSBG_CUDA(ctx, cudaMalloc(&ps->dNbr, (size_t)(n > 0 ? n : 1) * 6 * 4));
+  MSBG_CUDA(ctx, cudaMalloc(&ps->dParList, (size_t)(n > 0 ? n : 1) * 4));
+  MSBG_CUDA(ctx, cudaMalloc(&ps->dBpar, (size_t)(n > 0 ? n : 1)));
+  int rc;
+  if ((rc = ensureTmpSlab(ctx, (size_t)(n + 1) * 12 + 64))) return rc;
+  int32_t *even = (int32_t *)ctx->dTmpSlab;
+  int64_t *off = (int64_t *)((char *)ctx->dTmpSlab + (((size_t)(n + 1) * 4 + 15) & ~size_t(15)));
+  if (n > 0) {
+    MSBG_LAUNCH(ctx, kNbrTable, gridFor(n, 256), 256, 0, L0.active, n, L0.nbx, L0.nby, L0.nbz, L0.slot, ps->dNbr,
+                even, ps->dBpar);
+  }
+  if ((rc = exclusiveScanFlags(ctx, even, n, off, ctx->dCounters + 6))) return rc;
+  if (n > 0) MSBG_LAUNCH(ctx, kParityList, gridFor(n, 256), 256, 0, even, off, n, ctx->dCounters + 6, ps->dParList);
+  int64_t ne = 0;
+  MSBG_CUDA(ctx, cudaMemcpyAsync(&ne, ctx->dCounters + 6, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ps->nEven = ne;
+  return MSBG_GPU_OK;
+}
+
+BlkGeom blkOf(const PoissonState *ps, const MgLevel &L) {
+  BlkGeom g;
+  g.bs = L.bs; g.log2bs = L.log2bs; g.nAct = L.nAct;
+  g.nbr = ps->dNbr; g.parList = ps->dParList; g.nEven = ps->nEven; g.bpar = ps->dBpar;
+  return g;
+}
+
+// ---------------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------------
+template <typename V>
+int blkApply(msbg_gpu_ctx *ctx, PoissonState *ps, size_t l, const PrecSet &P, const V *x, const V *b, V *y,
+             int mode, double *dotOut, V *bc, V *xc) {
+  const MgLevel &Lv = ps->levels[l];
+  const int64_t nQuad = Lv.nCell / 4;
+  int64_t grid = (nQuad + 255) / 256;
+  if (grid > ps->nPartial) grid = ps->nPartial;
+  if (grid < 1) grid = 1;
+  MSBG_LAUNCH(ctx, kApplyRows<V>, (unsigned)grid, 256, 0, blkOf(ps, Lv), x, b, (const V *)P.cx[l],
+              (const V *)P.cy[l], (const V *)P.cz[l], (const V *)P.d[l], y, mode,
+              dotOut ? ps->dPartial : nullptr, bc, xc);
+  if (dotOut && mode == 2) MSBG_LAUNCH(ctx, kSumPartialsBlk2, 1, kRedThreads, 0, ps->dPartial, (int)grid, dotOut);
+  else if (dotOut) MSBG_LAUNCH(ctx, kSumPartialsBlk, 1, kRedThreads, 0, ps->dPartial, (int)grid, dotOut);
+  return MSBG_GPU_OK;
+}
+
+static unsigned quadGrid(const PoissonState *ps, int64_t nq) {
+  int64_t g = (nq + 255) / 256;
+  if (g > ps->nPartial) g = ps->nPartial;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+template <typename V>
+int blkDot(msbg_gpu_ctx *ctx, PoissonState *ps, const V *a, const V *b, int64_t n, double *dOut) {
+  const unsigned g = quadGrid(ps, n / 4);
+  MSBG_LAUNCH(ctx, kDotQuad<V>, g, 256, 0, a, b, n / 4, ps->dPartial);
+  MSBG_LAUNCH(ctx, kSumPartialsBlk, 1, kRedThreads, 0, ps->dPartial, (int)g, dOut);
+  return MSBG_GPU_OK;
+}
+template <typename V>
+int blkUpdateXR(msbg_gpu_ctx *ctx, PoissonState *ps, const double *sc, const V *p, const V *q, V *x, V *r, int64_t n,
+                double *rrOut) {
+  const unsigned g = quadGrid(ps, n / 4);
+  MSBG_LAUNCH(ctx, kUpdateXRQuad<V>, g, 256, 0, sc, p, q, x, r, n / 4, ps->dPartial);
+  MSBG_LAUNCH(ctx, kSumPartialsBlk, 1, kRedThreads, 0, ps->dPartial, (int)g, rrOut);
+  return MSBG_GPU_OK;
+}
+template <typename V>
+int blkUpdateP(msbg_gpu_ctx *ctx, PoissonState *ps, const double *sc, const V *z, V *p, int64_t n) {
+  MSBG_LAUNCH(ctx, kUpdatePQuad<V>, quadGrid(ps, n / 4), 256, 0, sc, z, p, n / 4);
+  return MSBG_GPU_OK;
+}
+
+// cuTensorMapEncodeTiled from the driver (no link against libcuda)
+static PFN_cuTensorMapEncodeTiled_v12000 encodeTiled() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  });
+  return fn;
+}
+
+// Tensor map of a level array viewed as [bs * nAct][bs][bs] with box (bx, by, bz),
+// cached per (address, level, box kind).
+static int tileMap(msbg_gpu_ctx *ctx, PoissonState *ps, size_t l, const void *ptr, int elem, int kind,
+                   const int *T, CUtensorMap *out) {
+  const auto key = std::make_tuple(ptr, (int)l, (kind * 8 + elem) * 64 + T[2]);
+  auto it = ps->tmaMaps.find(key);
+  if (it != ps->tmaMaps.end()) { *out = it->second; return MSBG_GPU_OK; }
+  auto fn = encodeTiled();
+  if (!fn) return fail(ctx, MSBG_GPU_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  const MgLevel &Lv = ps->levels[l];
+  const cuuint64_t bs = (cuuint64_t)Lv.bs;
+  cuuint64_t dims[3] = {bs, bs, bs * (cuuint64_t)Lv.nAct};
+  cuuint64_t strides[2] = {bs * elem, bs * bs * elem};
+  cuuint32_t box[3] = {(cuuint32_t)T[0], kind == 1 ? 1u : (cuuint32_t)T[1], kind == 2 ? 1u : (cuuint32_t)T[2]};
+  cuuint32_t es[3] = {1, 1, 1};
+  CUtensorMap m;
+  const CUresult r = fn(&m, elem == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3,
+                        const_cast<void *>(ptr), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(ctx, MSBG_GPU_ERR_CUDA, "tensor map encode failed (%d)", (int)r);
+  ps->tmaMaps.emplace(key, m);
+  *out = m;
+  return MSBG_GPU_OK;
+}
+
+template <typename V, int BS>
+static int smoothLaunch(msbg_gpu_ctx *ctx, PoissonState *ps, const MgLevel &Lv, const PrecSet &P, size_t l, V *x,
+                        const V *b, const V *xc, int tc, int k, int reverse, int flags) {
+  using Sh = TileShape<BS>;
+  constexpr int NT = Sh::NT;
+  constexpr size_t smem = tileSmemBytes<V, BS>();
+  static bool attrSet[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !attrSet[dev]) {
+    MSBG_CUDA(ctx, cudaFuncSetAttribute(kTileSmooth<V, BS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attrSet[dev] = true;
+  }
+  const int64_t nUnits = BS == 32 ? Lv.nAct * 4 : (tc == 0 ? ps->nEven : Lv.nAct - ps->nEven);
+  if (nUnits <= 0) return MSBG_GPU_OK;
+  constexpr int E = (int)sizeof(V);
+  const int bx[3] = {Sh::TX, Sh::TY, Sh::TZ};
+  TileMaps maps;
+  int rc;
+  if ((rc = tileMap(ctx, ps, l, x, E, 0, bx, &maps.xM)) || (rc = tileMap(ctx, ps, l, x, E, 1, bx, &maps.xY)) ||
+      (rc = tileMap(ctx, ps, l, x, E, 2, bx, &maps.xZ)) || (rc = tileMap(ctx, ps, l, b, E, 0, bx, &maps.b)) ||
+      (rc = tileMap(ctx, ps, l, P.d[l], E, 0, bx, &maps.d)) ||
+      (rc = tileMap(ctx, ps, l, P.cx[l], E, 0, bx, &maps.cx)) ||
+      (rc = tileMap(ctx, ps, l, P.cy[l], E, 0, bx, &maps.cy)) ||
+      (rc = tileMap(ctx, ps, l, P.cy[l], E, 1, bx, &maps.cyY)) ||
+      (rc = tileMap(ctx, ps, l, P.cz[l], E, 0, bx, &maps.cz)) ||
+      (rc = tileMap(ctx, ps, l, P.cz[l], E, 2, bx, &maps.czZ)))
+    return rc;
+  const int64_t grid = (nUnits + NT - 1) / NT;
+  MSBG_LAUNCH(ctx, (kTileSmooth<V, BS>), (unsigned)grid, tileThreads<BS>(), smem, maps, blkOf(ps, Lv), x,
+              (const V *)P.cx[l], xc, tc, k, reverse, flags, ctx->dStatus);
+  return MSBG_GPU_OK;
+}
+
+template <typename V>
+int blkSmoothColor(msbg_gpu_ctx *ctx, PoissonState *ps, size_t l, const PrecSet &P, V *x, const V *b,
+                   const V *xc, int tileColor, int k, int reverse, int flags) {
+  const MgLevel &Lv = ps->levels[l];
+  if (Lv.tile == 32) return smoothLaunch<V, 32>(ctx, ps, Lv, P, l, x, b, xc, tileColor, k, reverse, flags);
+  if (Lv.tile == 16) return smoothLaunch<V, 16>(ctx, ps, Lv, P, l, x, b, xc, tileColor, k, reverse, flags);
+  if (Lv.tile == 8) return smoothLaunch<V, 8>(ctx, ps, Lv, P, l, x, b, xc, tileColor, k, reverse, flags);
+  return fail(ctx, MSBG_GPU_ERR_STATE, "level %zu has no tile smoother", l);
+}
+
+template int blkApply<float>(msbg_gpu_ctx *, PoissonState *, size_t, const PrecSet &, const float *, const float *,
+                             float *, int, double *, float *, float *);
+template int blkApply<__half>(msbg_gpu_ctx *, PoissonState *, size_t, const PrecSet &, const __half *,
+                              const __half *, __half *, int, double *, __half *, __half *);
+#define INST_VEC(V)                                                                                         \
+  template int blkDot<V>(msbg_gpu_ctx *, PoissonState *, const V *, const V *, int64_t, double *);                 \
+  template int blkUpdateXR<V>(msbg_gpu_ctx *, PoissonState *, const double *, const V *, const V *, V *, V *,     \
+                              int64_t, double *);                                                                  \
+  template int blkUpdateP<V>(msbg_gpu_ctx *, PoissonState *, const double *, const V *, V *, int64_t);
+INST_VEC(float)
+INST_VEC(__half)
+template int blkSmoothColor<float>(msbg_gpu_ctx *, PoissonState *, size_t, const PrecSet &, float *, const float *,
+                                   const float *, int, int, int, int);
+template int blkSmoothColor<__half>(msbg_gpu_ctx *, PoissonState *, size_t, const PrecSet &, __half *,
+                                    const __half *, const __half *, int, int, int, int);
+
+}  // namespace msbg

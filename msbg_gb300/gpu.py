@@ -81,6 +81,7 @@ SIGNATURES = {
     "msbg_gpu_axpby_combined": (I, [P, D, D, I, I, I]),
     "msbg_gpu_mgpcg_solve": (I, [P, I, I, D, I, C.POINTER(I), C.POINTER(D)]),
     "msbg_gpu_mg_info": (I, [P, C.POINTER(I), P, I]),
+    "msbg_gpu_poisson_set_params": (I, [P, I, I, I, I]),
     "msbg_gpu_mgpcg_solve_mixed": (I, [P, I, I, D, I, D, I, C.POINTER(I), C.POINTER(I), C.POINTER(D)]),
 }
 
@@ -352,6 +353,9 @@ class MultiresSparseGrid:
         self._check(self.L.msbg_gpu_mgpcg_solve_mixed(self.h, chanX, chanB, tol, max_outer, inner_tol,
                                                       max_inner, C.byref(o), C.byref(i), C.byref(rel)))
         return o.value, i.value, rel.value
+
+    def poisson_set_params(self, pre: int = 2, post: int = 2, tile_iters: int = 1, coarsest_iter: int = 0):
+        self._check(self.L.msbg_gpu_poisson_set_params(self.h, pre, post, tile_iters, coarsest_iter))
 
     def mg_info(self):
         n = C.c_int()

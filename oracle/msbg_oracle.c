@@ -724,6 +724,57 @@ static void prbgs(const plev *L, double *x, const double *b, int nSweeps, int re
     }
 }
 
+/* Smoother tiles on a level whose blocks have edge bs: 32x16x8 (bs 32), 16^3 (bs 16),
+ * 8^3 (bs 8); pointwise red-black below (tile[0] = 0). */
+static void ptile(int bsl, int t[3]) {
+  if (bsl >= 32) { t[0] = 32; t[1] = 16; t[2] = 8; }
+  else if (bsl == 16) { t[0] = t[1] = t[2] = 16; }
+  else if (bsl == 8) { t[0] = t[1] = t[2] = 8; }
+  else { t[0] = t[1] = t[2] = 0; }
+}
+
+/* One smoothing pass.  Pointwise levels: k red-black sweeps.  Tile levels: tiles
+ * (TX,TY,TZ) are coloured by (gx/TX + gy/TY + gz/TZ) & 1; for each tile colour,
+ * every tile of that colour does k in-tile red-black Gauss-Seidel sweeps with the
+ * cells outside the tile held fixed.  Same-colour tiles share no face, so the
+ * order among them does not matter.  reverse: tile colours 1,0 and in-tile cell
+ * colours black,red (the adjoint order, for the post-smoother). */
+static void psmooth_pass(const plev *L, const int *T, double *x, const double *b, int k, int reverse) {
+  if (T[0] == 0) {
+    prbgs(L, x, b, k, !reverse);
+    return;
+  }
+  const int64_t sl = (int64_t)L->nx * L->ny;
+  for (int tci = 0; tci < 2; tci++) {
+    const int tc = reverse ? 1 - tci : tci;
+    for (int it = 0; it < k; it++)
+      for (int cci = 0; cci < 2; cci++) {
+        const int cc = reverse ? 1 - cci : cci;
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int z = 0; z < L->nz; z++)
+          for (int yy = 0; yy < L->ny; yy++)
+            for (int xx = 0; xx < L->nx; xx++) {
+              if (((xx + yy + z) & 1) != cc) continue;
+              if (((xx / T[0] + yy / T[1] + z / T[2]) & 1) != tc) continue;
+              const int64_t i = PIDX(L, xx, yy, z);
+              if (!L->act[i]) continue;
+              double s = b[i];
+              if (pin(L, xx - 1, yy, z)) s += L->cx[i] * x[i - 1];
+              if (pin(L, xx + 1, yy, z)) s += L->cx[i + 1] * x[i + 1];
+              if (pin(L, xx, yy - 1, z)) s += L->cy[i] * x[i - L->nx];
+              if (pin(L, xx, yy + 1, z)) s += L->cy[i + L->nx] * x[i + L->nx];
+              if (pin(L, xx, yy, z - 1)) s += L->cz[i] * x[i - sl];
+              if (pin(L, xx, yy, z + 1)) s += L->cz[i + sl] * x[i + sl];
+              x[i] = s / L->d[i];
+            }
+      }
+  }
+}
+
+static void psmooth(const plev *L, const int *T, double *x, const double *b, int passes, int k, int reverse) {
+  for (int p = 0; p < passes; p++) psmooth_pass(L, T, x, b, k, reverse);
+}
+
 static plev *pcoarsen(const plev *F) {
   plev *C = (plev *)calloc(1, sizeof(plev));
   C->nx = (F->nx + 1) / 2; C->ny = (F->ny + 1) / 2; C->nz = (F->nz + 1) / 2;
@@ -770,9 +821,69 @@ static void pfree(plev *L, int ownsCoeffs) {
 
 typedef struct {
   plev *lv[40];
+  int tile[40][3];
   int n;
-  int pre, post, coarsestIter;
+  int pre, post, k, coarsestIter;
+  /* exact coarsest solve (coarsestIter == 0): Cholesky factor over the active cells */
+  int nc;
+  int64_t *cidx;  /* dense index of each active coarsest cell */
+  double *chol;   /* [nc][nc] lower factor */
 } phier;
+
+static void pchol_build(phier *H) {
+  const plev *C = H->lv[H->n - 1];
+  const int64_t nd = (int64_t)C->nx * C->ny * C->nz;
+  int64_t *map = (int64_t *)malloc((size_t)nd * sizeof(int64_t));
+  int n = 0;
+  for (int64_t i = 0; i < nd; i++) map[i] = C->act[i] ? n++ : -1;
+  H->nc = n;
+  H->cidx = (int64_t *)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
+  for (int64_t i = 0; i < nd; i++) if (map[i] >= 0) H->cidx[map[i]] = i;
+  double *A = (double *)calloc((size_t)n * n + 1, sizeof(double));
+  const int64_t sl = (int64_t)C->nx * C->ny;
+  for (int k = 0; k < n; k++) {
+    const int64_t i = H->cidx[k];
+    const int x = (int)(i % C->nx), y = (int)((i / C->nx) % C->ny), z = (int)(i / sl);
+    A[(size_t)k * n + k] = C->d[i];
+    if (pin(C, x - 1, y, z)) A[(size_t)k * n + map[i - 1]] = -C->cx[i];
+    if (pin(C, x + 1, y, z)) A[(size_t)k * n + map[i + 1]] = -C->cx[i + 1];
+    if (pin(C, x, y - 1, z)) A[(size_t)k * n + map[i - C->nx]] = -C->cy[i];
+    if (pin(C, x, y + 1, z)) A[(size_t)k * n + map[i + C->nx]] = -C->cy[i + C->nx];
+    if (pin(C, x, y, z - 1)) A[(size_t)k * n + map[i - sl]] = -C->cz[i];
+    if (pin(C, x, y, z + 1)) A[(size_t)k * n + map[i + sl]] = -C->cz[i + sl];
+  }
+  for (int j = 0; j < n; j++) {
+    double t = A[(size_t)j * n + j];
+    for (int k = 0; k < j; k++) t -= A[(size_t)j * n + k] * A[(size_t)j * n + k];
+    const double dj = sqrt(t > 0 ? t : 1e-300);
+    A[(size_t)j * n + j] = dj;
+    for (int i = j + 1; i < n; i++) {
+      double u = A[(size_t)i * n + j];
+      for (int k = 0; k < j; k++) u -= A[(size_t)i * n + k] * A[(size_t)j * n + k];
+      A[(size_t)i * n + j] = u / dj;
+    }
+  }
+  H->chol = A;
+  free(map);
+}
+
+static void pchol_solve(const phier *H, const double *b, double *x) {
+  const int n = H->nc;
+  const double *L = H->chol;
+  double *y = (double *)malloc((size_t)(n > 0 ? n : 1) * sizeof(double));
+  for (int i = 0; i < n; i++) {
+    double t = b[H->cidx[i]];
+    for (int k = 0; k < i; k++) t -= L[(size_t)i * n + k] * y[k];
+    y[i] = t / L[(size_t)i * n + i];
+  }
+  for (int i = n - 1; i >= 0; i--) {
+    double t = y[i];
+    for (int k = i + 1; k < n; k++) t -= L[(size_t)k * n + i] * y[k];
+    y[i] = t / L[(size_t)i * n + i];
+  }
+  for (int i = 0; i < n; i++) x[H->cidx[i]] = y[i];
+  free(y);
+}
 
 static void pbuild(phier *H, const orc_level0 *L0, int log2bs0, int64_t coarsestCells) {
   plev *F = (plev *)calloc(1, sizeof(plev));
@@ -784,22 +895,27 @@ static void pbuild(phier *H, const orc_level0 *L0, int log2bs0, int64_t coarsest
   F->x = (double *)calloc((size_t)n, 8); F->b = (double *)calloc((size_t)n, 8); F->r = (double *)calloc((size_t)n, 8);
   for (int64_t i = 0; i < n; i++) F->nAct += F->act[i];
   H->lv[0] = F;
+  ptile(1 << log2bs0, H->tile[0]);
   H->n = 1;
   for (int l = 0; l < log2bs0; l++) {
     plev *c = pcoarsen(H->lv[H->n - 1]);
     H->lv[H->n] = c;
+    ptile(1 << (log2bs0 - l - 1), H->tile[H->n]);
     H->n++;
   }
   while (H->n < 40) {
     const plev *f = H->lv[H->n - 1];
     if (f->nAct <= coarsestCells || (f->nx <= 2 && f->ny <= 2 && f->nz <= 2)) break;
     H->lv[H->n] = pcoarsen(f);
+    ptile(1, H->tile[H->n]);
     H->n++;
   }
 }
 
 static void phfree(phier *H) {
   for (int l = 0; l < H->n; l++) pfree(H->lv[l], l > 0);
+  free(H->cidx);
+  free(H->chol);
 }
 
 static void pvcycle(phier *H, int l, double *x, const double *b, double *r) {
@@ -807,10 +923,11 @@ static void pvcycle(phier *H, int l, double *x, const double *b, double *r) {
   const int64_t n = (int64_t)L->nx * L->ny * L->nz;
   memset(x, 0, (size_t)n * 8);
   if (l == H->n - 1) {
-    prbgs(L, x, b, H->coarsestIter, 1);
+    if (H->coarsestIter > 0) prbgs(L, x, b, H->coarsestIter, 1);
+    else pchol_solve(H, b, x);
     return;
   }
-  prbgs(L, x, b, H->pre, 1);
+  psmooth(L, H->tile[l], x, b, H->pre, H->k, 0);
   papply(L, x, b, r, 1);
   plev *C = H->lv[l + 1];
   for (int z = 0; z < C->nz; z++)
@@ -831,7 +948,7 @@ static void pvcycle(phier *H, int l, double *x, const double *b, double *r) {
         const int64_t i = PIDX(L, xx, y, z);
         if (L->act[i]) x[i] += C->x[PIDX(C, xx >> 1, y >> 1, z >> 1)];
       }
-  prbgs(L, x, b, H->post, 0);
+  psmooth(L, H->tile[l], x, b, H->post, H->k, 1);
 }
 
 static plev view0(const orc_level0 *L0) {
@@ -853,12 +970,21 @@ void orc_poisson_rbgs(const orc_level0 *L0, double *x, const double *b, int nSwe
   prbgs(&v, x, b, nSweeps, redFirst);
 }
 
+void orc_poisson_smooth(const orc_level0 *L0, int log2bs, double *x, const double *b, int passes, int k,
+                        int reverse) {
+  plev v = view0(L0);
+  int t[3];
+  ptile(1 << log2bs, t);
+  psmooth(&v, t, x, b, passes, k, reverse);
+}
+
 int orc_poisson_vcycle(const orc_level0 *L0, int log2bs0, const double *b, double *x, int preSweeps,
-                       int postSweeps, int coarsestIter, int64_t coarsestCells) {
+                       int postSweeps, int tileIters, int coarsestIter, int64_t coarsestCells) {
   phier H;
   memset(&H, 0, sizeof(H));
-  H.pre = preSweeps; H.post = postSweeps; H.coarsestIter = coarsestIter;
+  H.pre = preSweeps; H.post = postSweeps; H.k = tileIters; H.coarsestIter = coarsestIter;
   pbuild(&H, L0, log2bs0, coarsestCells);
+  if (coarsestIter == 0) pchol_build(&H);
   pvcycle(&H, 0, x, b, H.lv[0]->r);
   const int n = H.n;
   phfree(&H);
@@ -873,11 +999,13 @@ static double pdot(const double *a, const double *b, int64_t n) {
 }
 
 int orc_poisson_mgpcg(const orc_level0 *L0, int log2bs0, const double *b, double *x, double tol,
-                      int maxIter, int *iters, double *relres) {
+                      int maxIter, int preSweeps, int postSweeps, int tileIters, int coarsestIter,
+                      int64_t coarsestCells, int *iters, double *relres) {
   phier H;
   memset(&H, 0, sizeof(H));
-  H.pre = 2; H.post = 2; H.coarsestIter = 200;
-  pbuild(&H, L0, log2bs0, 512);
+  H.pre = preSweeps; H.post = postSweeps; H.k = tileIters; H.coarsestIter = coarsestIter;
+  pbuild(&H, L0, log2bs0, coarsestCells);
+  if (coarsestIter == 0) pchol_build(&H);
   plev *L = H.lv[0];
   const int64_t n = (int64_t)L->nx * L->ny * L->nz;
   double *r = (double *)calloc((size_t)n, 8), *z = (double *)calloc((size_t)n, 8),

@@ -107,10 +107,16 @@ float orc_f16_to_f32(uint16_t h);
  *   (A x)_i = d_i x_i - sum_f c_f x_nb(f)            (src/msbg3.cpp:1281-1296)
  * cx/cy/cz hold each cell's lower-face coefficient, d the diagonal.  Level l+1 has
  * ceil(n/2) cells per axis; a coarse cell is active when any child is; coarse
- * operator = P^T A P / 2 with piecewise-constant P; red-black Gauss-Seidel
- * smoothing (pre: red first, post: black first); coarsest level: coarsestIter RB
- * sweeps from zero.  Levels: log2(bs0) halvings, then more while the coarse level
- * has more than coarsestCells active cells and a side longer than 2. */
+ * operator = P^T A P / 2 with piecewise-constant P.  Smoothing pass on a level of
+ * block edge bs: tiles (TX,TY,TZ) = 32x16x8 (bs 32), 16^3 (bs 16) or 8^3 (bs 8)
+ * coloured by (gx/TX+gy/TY+gz/TZ)&1, each tile colour in turn doing k in-tile
+ * red-black Gauss-Seidel sweeps with the outside held fixed; pointwise red-black
+ * GS (k sweeps) on levels with bs < 8.  Pre-smoothing: tile colours 0,1 and cells red
+ * first; post-smoothing the adjoint order (1,0; black first).  Coarsest level:
+ * exact solve (Cholesky) when coarsestIter == 0, else coarsestIter RB sweeps
+ * from zero.  Levels: log2(bs0) halvings, then more while
+ * the coarse level has more than coarsestCells active cells and a side longer
+ * than 2. */
 typedef struct {
   int nx, ny, nz;
   const uint8_t *act;  /* [nz][ny][nx] */
@@ -121,10 +127,14 @@ typedef struct {
 float orc_face_coeff(uint32_t seed, int axis, int gx, int gy, int gz);
 void orc_poisson_apply(const orc_level0 *L, const double *x, const double *b, double *y, int residual);
 void orc_poisson_rbgs(const orc_level0 *L, double *x, const double *b, int nSweeps, int redFirst);
+/* passes smoothing passes of level 0 (block edge 1<<log2bs), k in-tile sweeps. */
+void orc_poisson_smooth(const orc_level0 *L, int log2bs, double *x, const double *b, int passes, int k,
+                        int reverse);
 int orc_poisson_vcycle(const orc_level0 *L, int log2bs0, const double *b, double *x, int preSweeps,
-                       int postSweeps, int coarsestIter, int64_t coarsestCells);
+                       int postSweeps, int tileIters, int coarsestIter, int64_t coarsestCells);
 int orc_poisson_mgpcg(const orc_level0 *L, int log2bs0, const double *b, double *x, double tol,
-                      int maxIter, int *iters, double *relres);
+                      int maxIter, int preSweeps, int postSweeps, int tileIters, int coarsestIter,
+                      int64_t coarsestCells, int *iters, double *relres);
 /* The GPU's seeded coefficients (float values) on a dense grid: lower faces + diagonal. */
 void orc_poisson_coeffs_dense(uint32_t seed, int nx, int ny, int nz, const uint8_t *act, double *cx,
                               double *cy, double *cz, double *d);

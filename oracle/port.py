@@ -63,10 +63,11 @@ def lib():
         L.orc_face_coeff.restype = C.c_float
         L.orc_poisson_apply.argtypes = [P, P, P, P, C.c_int]
         L.orc_poisson_rbgs.argtypes = [P, P, P, C.c_int, C.c_int]
-        L.orc_poisson_vcycle.argtypes = [P, C.c_int, P, P, C.c_int, C.c_int, C.c_int, C.c_int64]
+        L.orc_poisson_smooth.argtypes = [P, C.c_int, P, P, C.c_int, C.c_int, C.c_int]
+        L.orc_poisson_vcycle.argtypes = [P, C.c_int, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int64]
         L.orc_poisson_vcycle.restype = C.c_int
-        L.orc_poisson_mgpcg.argtypes = [P, C.c_int, P, P, C.c_double, C.c_int, C.POINTER(C.c_int),
-                                        C.POINTER(C.c_double)]
+        L.orc_poisson_mgpcg.argtypes = [P, C.c_int, P, P, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
+                                        C.c_int, C.c_int64, C.POINTER(C.c_int), C.POINTER(C.c_double)]
         L.orc_poisson_coeffs_dense.argtypes = [C.c_uint32, C.c_int, C.c_int, C.c_int, P, P, P, P, P]
         L.orc_f32_to_f16.argtypes = [C.c_float]
         L.orc_f32_to_f16.restype = C.c_uint16
@@ -239,11 +240,22 @@ def active_mask(bids: np.ndarray, nb, bs: int) -> np.ndarray:
     return payload_to_dense(np.ones((len(bids), bs ** 3), np.uint8), bids, nb, bs, np.uint8)
 
 
+# Multigrid parameters shared with the GPU solver's defaults: smoothing passes
+# before / after the coarse correction, in-tile red-black sweeps per pass, the
+# coarsest level's red-black sweeps (0 = exact Cholesky solve), and the cell
+# count at which coarsening stops.
+MG_PRE, MG_POST, MG_TILE_ITERS, MG_COARSEST_ITER, MG_COARSEST_CELLS = 2, 2, 1, 0, 512
+
+
 class PoissonProblem:
     """Dense FP64 restatement of one Poisson problem on a value-block layout."""
 
-    def __init__(self, bids: np.ndarray, nb, bs: int, seed: int):
+    def __init__(self, bids: np.ndarray, nb, bs: int, seed: int, pre: int = MG_PRE, post: int = MG_POST,
+                 tile_iters: int = MG_TILE_ITERS, coarsest_iter: int = MG_COARSEST_ITER,
+                 coarsest_cells: int = MG_COARSEST_CELLS):
         self.bids, self.nb, self.bs, self.seed = np.asarray(bids, np.int64), nb, bs, seed
+        self.pre, self.post, self.k = pre, post, tile_iters
+        self.coarsest_iter, self.coarsest_cells = coarsest_iter, coarsest_cells
         self.act = np.ascontiguousarray(active_mask(self.bids, nb, bs))
         nz, ny, nx = self.act.shape
         self.cx, self.cy, self.cz, self.d = (np.zeros(self.act.shape) for _ in range(4))
@@ -272,17 +284,26 @@ class PoissonProblem:
                                int(red_first))
         return x
 
+    def smooth(self, x, b, passes, reverse=False):
+        """Smoothing passes of level 0 (tile or pointwise red-black, k in-tile sweeps)."""
+        x = np.ascontiguousarray(x, np.float64).copy()
+        lib().orc_poisson_smooth(C.byref(self.L), self.log2bs, _p(x), _p(np.ascontiguousarray(b, np.float64)),
+                                 passes, self.k, int(reverse))
+        return x
+
     def vcycle(self, b):
         x = np.zeros_like(self.d)
         nlev = lib().orc_poisson_vcycle(C.byref(self.L), self.log2bs, _p(np.ascontiguousarray(b, np.float64)),
-                                        _p(x), 2, 2, 200, 512)
+                                        _p(x), self.pre, self.post, self.k, self.coarsest_iter,
+                                        self.coarsest_cells)
         return x, nlev
 
     def solve(self, b, tol=1e-6, max_iter=200, x0=None):
         x = np.zeros_like(self.d) if x0 is None else np.ascontiguousarray(x0, np.float64).copy()
         it, rel = C.c_int(), C.c_double()
         lib().orc_poisson_mgpcg(C.byref(self.L), self.log2bs, _p(np.ascontiguousarray(b, np.float64)),
-                                _p(x), tol, max_iter, C.byref(it), C.byref(rel))
+                                _p(x), tol, max_iter, self.pre, self.post, self.k, self.coarsest_iter,
+                                self.coarsest_cells, C.byref(it), C.byref(rel))
         return x, it.value, rel.value
 
     def rel_residual(self, x, b):

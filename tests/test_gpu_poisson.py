@@ -40,9 +40,10 @@ def _rand(prob, rng):
     return np.where(prob.act > 0, rng.standard_normal(prob.act.shape), 0.0)
 
 
-@pytest.fixture(scope="module")
-def setup(gpulib, port):
-    g, prob = _layout(gpulib, port)
+@pytest.fixture(scope="module", params=[(128, 16), (256, 32), (64, 8)], ids=["bs16", "bs32", "bs8"])
+def setup(request, gpulib, port):
+    res, bs = request.param
+    g, prob = _layout(gpulib, port, res=res, bs=bs)
     yield gpulib, port, g, prob
     g.close()
 
@@ -67,14 +68,34 @@ def test_multiply_and_residual(setup):
 
 
 @pytest.mark.parametrize("reverse", [False, True])
-def test_relax_red_black(setup, reverse):
+def test_relax_tiles(setup, reverse):
+    """relax = tile-coloured smoothing passes (16^3 / 8^3 tiles, in-tile red-black)."""
     G, P, g, prob = setup
     rng = np.random.default_rng(2)
     x, b = _rand(prob, rng).astype(np.float32), _rand(prob, rng).astype(np.float32)
     g.upload_payload(prob.payload(x), CH_X)
     g.upload_payload(prob.payload(b), CH_B)
     g.relax(CH_X, CH_B, 2, reverseOrder=reverse)
-    want = prob.rbgs(x, b, 2, red_first=not reverse)
+    want = prob.smooth(x, b, 2, reverse=reverse)
+    assert rel_l2(prob.dense(g.payload(CH_X)), want) < 1e-5
+
+
+@pytest.mark.parametrize("pre,post,k,coarsest", [(1, 1, 3, 0), (2, 1, 2, 200)])
+def test_vcycle_params_match_fp64(setup, pre, post, k, coarsest):
+    """Other pass / in-tile sweep counts and the red-black coarsest solver give the
+    restatement's V-cycle too."""
+    G, P, g, prob = setup
+    p2 = P.PoissonProblem(prob.bids, prob.nb, prob.bs, seed=4242, pre=pre, post=post, tile_iters=k,
+                          coarsest_iter=coarsest)
+    rng = np.random.default_rng(8)
+    b = _rand(prob, rng).astype(np.float32)
+    g.upload_payload(prob.payload(b), CH_B)
+    g.poisson_set_params(pre, post, k, coarsest)
+    try:
+        g.vcycle(CH_X, CH_B)
+    finally:
+        g.poisson_set_params()
+    want, _ = p2.vcycle(b)
     assert rel_l2(prob.dense(g.payload(CH_X)), want) < 1e-5
 
 
