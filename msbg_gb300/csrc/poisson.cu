@@ -322,20 +322,6 @@ __global__ void kAxpbyCombined(double a, double b, const float *__restrict__ q, 
 __global__ void kAxpby(double a, const float *__restrict__ x, double b, float *__restrict__ y, int64_t n) {
   GRID_STRIDE(i, n) y[i] = (float)(a * (double)x[i] + b * (double)y[i]);
 }
-// mixed precision: rh = r / scale (FP16), scale from sc[0] = sum r^2
-__global__ void kScaleToHalf(const float *__restrict__ r, const double *__restrict__ sc, int64_t nCell,
-                             __half *__restrict__ rh, int64_t n) {
-  const double rms = sqrt(sc[0] / (double)(nCell > 0 ? nCell : 1));
-  const float inv = rms > 0.0 ? (float)(1.0 / rms) : 0.0f;
-  GRID_STRIDE(i, n) rh[i] = __float2half_rn(r[i] * inv);
-}
-// x += scale * e
-__global__ void kAddScaledHalf(const __half *__restrict__ e, const double *__restrict__ sc, int64_t nCell,
-                               float *__restrict__ x, int64_t n) {
-  const float rms = (float)sqrt(sc[0] / (double)(nCell > 0 ? nCell : 1));
-  GRID_STRIDE(i, n) x[i] = fmaf(rms, __half2float(e[i]), x[i]);
-}
-
 // Coarse level blocks: parent of every fine active block (block grid halved).
 __global__ void kMarkParents(const int32_t *__restrict__ activeF, int64_t nAct, int nbxF, int nbyF, int nbxC,
                              int nbyC, int32_t *__restrict__ markC) {
@@ -996,36 +982,44 @@ extern "C" int msbg_gpu_mgpcg_solve_mixed(msbg_gpu_ctx *ctx, int chanX, int chan
   PoissonState *ps = ctx->poisson;
   if ((rc = ensureHalf(ctx, ps))) return rc;
   const int64_t n = ps->levels[0].nCell;
-  float *r = (float *)ps->f32.vr;
-  __half *rh = (__half *)ps->f16.vb, *rw = (__half *)ps->f16.vr, *e = (__half *)ps->f16.ve;
-  double *sc = ps->dScal;
-  // outer residual in FP32 with the FP32 operator; its norm in FP64
-  double rr, bb;
-  if ((rc = trueResidual(ctx, ps, x, b, &rr, &bb))) return rc;
-  const double bnorm = sqrt(bb);
-  double rel = bnorm > 0 ? sqrt(rr) / bnorm : 0.0;
+  __half *rw = (__half *)ps->f16.vr, *e = (__half *)ps->f16.ve;
+  // Each outer step: x += s e (the pending correction), then one pass forms the
+  // residual b - A x in double-float arithmetic with the FP32 operator, its FP64
+  // norm, and the FP16 right-hand side rw = (b - A x) / s' of the next correction
+  // solve, s' being the predicted rms of that residual (recomputed exactly and
+  // the pass redone when the prediction is off by more than 30x).
+  float invScale = 1.0f, eScale = 0.0f;
+  bool haveE = false;
   int outer = 0, innerTotal = 0;
-  while (bnorm > 0 && rel > tol && outer < maxOuter) {
+  double rel = 0.0;
+  for (;;) {
+    if (haveE && (rc = blkAddScaled(ctx, ps, e, eScale, x, n))) return rc;
+    haveE = false;
+    if ((rc = blkApply<float>(ctx, ps, 0, ps->f32, x, b, nullptr, 2, ps->dScal + 8, nullptr, nullptr, rw, invScale)))
+      return rc;
+    if ((rc = fetchScal(ctx, ps, 8, 2))) return rc;
+    const double rr = ps->hScal[8], bb = ps->hScal[9];
+    if (!isfinite(rr)) return fail(ctx, MSBG_GPU_ERR_DIVERGED, "outer residual not finite");
+    const double bnorm = sqrt(bb);
+    rel = bnorm > 0 ? sqrt(rr) / bnorm : 0.0;
+    if (bnorm == 0.0 || rel <= tol || outer >= maxOuter) break;
+    const double rms = sqrt(rr / (double)n);
+    const double ratio = rms * invScale;
+    if (!(ratio > 1.0 / 30.0 && ratio < 30.0)) {  // rescale the FP16 right-hand side
+      invScale = (float)(1.0 / rms);
+      continue;
+    }
     outer++;
-    if ((rc = applyT<float>(ctx, ps, ps->f32, 0, x, b, r, 1))) return rc;
-    // rh = r / rms(r) in FP16 (keeps the inner problem O(1) in half range)
-    if ((rc = blkDot<float>(ctx, ps, r, r, n, sc + 16))) return rc;
-    MSBG_LAUNCH(ctx, kScaleToHalf, gridCells(n), 256, 0, r, sc + 16, n, rh, n);
     MSBG_LAUNCH(ctx, (kZero<__half>), gridCells(n), 256, 0, e, n);
-    MSBG_LAUNCH(ctx, (kCopy<__half>), gridCells(n), 256, 0, rh, rw, n);
-    // inner FP16-storage MG-PCG on A e = rh to innerTol (relative to ||rh||)
-    if ((rc = blkDot<__half>(ctx, ps, rh, rh, n, sc + 17))) return rc;
-    if ((rc = fetchScal(ctx, ps, 17, 1))) return rc;
-    const double rhn = sqrt(ps->hScal[17]);
+    const double rhn = sqrt(rr) * invScale;
     int itIn = 0;
     double relIn = 0.0;
-    if ((rc = pcgT<__half>(ctx, ps, ps->f16, e, rh, rw, innerTol * rhn, maxInner, false, rhn, &itIn, &relIn)))
+    if ((rc = pcgT<__half>(ctx, ps, ps->f16, e, rw, rw, innerTol * rhn, maxInner, false, rhn, &itIn, &relIn)))
       return rc;
     innerTotal += itIn;
-    MSBG_LAUNCH(ctx, kAddScaledHalf, gridCells(n), 256, 0, e, sc + 16, n, x, n);
-    if ((rc = trueResidual(ctx, ps, x, b, &rr, &bb))) return rc;
-    rel = sqrt(rr) / bnorm;
-    if (!isfinite(rel)) return fail(ctx, MSBG_GPU_ERR_DIVERGED, "outer residual not finite");
+    eScale = 1.0f / invScale;
+    haveE = true;
+    invScale = (float)(1.0 / (rms * fmax(relIn, 1e-3)));
   }
   if (outerOut) *outerOut = outer;
   if (innerTotalOut) *innerTotalOut = innerTotal;

@@ -172,10 +172,13 @@ int blkBuildTables(msbg_gpu_ctx *ctx, PoissonState *ps);
 // into *dotOut); mode 1: r = b - A x written to y, or, when bc != null,
 // restricted (sum of 8 children) into the coarse b and the coarse x zeroed;
 // mode 2: dotOut[0] = sum (b - A x)^2 with the residual formed in double-float
-// arithmetic, dotOut[1] = sum b^2 (nothing written).
+// arithmetic, dotOut[1] = sum b^2; rhOut != null: also rhOut = (b - A x) * rhScale
+// in FP16.
 template <typename V>
 int blkApply(msbg_gpu_ctx *ctx, PoissonState *ps, size_t l, const PrecSet &P, const V *x, const V *b, V *y,
-             int mode, double *dotOut, V *bc, V *xc);
+             int mode, double *dotOut, V *bc, V *xc, __half *rhOut = nullptr, float rhScale = 0.f);
+// x += scale * e on level-0 vectors
+int blkAddScaled(msbg_gpu_ctx *ctx, PoissonState *ps, const __half *e, float scale, float *x, int64_t n);
 // CG vector operations on level-0 vectors (n a multiple of 4): dot into *dOut;
 // x += alpha p, r -= alpha q with alpha = sc[0]/sc[1] and *rrOut = r.r; p = z + beta p
 // with beta = sc[2]/sc[0].  Products are summed in FP32 per 4 values, then in FP64.

@@ -88,7 +88,8 @@ __global__ void __launch_bounds__(256) kApplyRows(BlkGeom g, const V *__restrict
                                                   const V *__restrict__ cx, const V *__restrict__ cy,
                                                   const V *__restrict__ cz, const V *__restrict__ d,
                                                   V *__restrict__ y, int mode, double *__restrict__ dotPartial,
-                                                  V *__restrict__ bc, V *__restrict__ xc) {
+                                                  V *__restrict__ bc, V *__restrict__ xc,
+                                                  __half *__restrict__ rhOut, float rhScale) {
   const int L = g.log2bs, bs = g.bs;
   const int xb = L - 2;
   const int qPerBlockLog = 3 * L - 2;
@@ -170,6 +171,12 @@ __global__ void __launch_bounds__(256) kApplyRows(BlkGeom g, const V *__restrict
       if (act) {
         dot += (double)rq;
         dot2 += (double)bq;
+        if (rhOut) {  // the scaled residual in FP16 (right-hand side of a correction solve)
+          float sc[4];
+#pragma unroll
+          for (int i = 0; i < 4; i++) sc[i] = r[i] * rhScale;
+          stRow<4>(rhOut + c, sc);
+        }
       }
       continue;
     }
@@ -237,22 +244,21 @@ __global__ void __launch_bounds__(256) kApplyRows(BlkGeom g, const V *__restrict
 // ---------------------------------------------------------------------------------
 // Tiles: 32x16x8 cells on bs-32 levels (full 128-byte block rows, 8 tiles per
 // block), the whole block on bs-16 and bs-8 levels.  Tile colour =
-// (gx/TX + gy/TY + gz/TZ) & 1.  A CTA relaxes NT tiles; thread (tx, ty) of a tile
-// owns the column of cells (tx, ty, 0..TZ-1): its x values with the two z-halo
-// cells, b, 1/d and the z-face coefficients live in registers; the x values of
-// the whole tile live in shared memory ([z][y][x], dense), where the x and y
-// neighbours are read.  Lanes of a warp hold consecutive tx, so every shared
-// access of a warp is to consecutive words.  Both cell colours of a half step are
-// handled without divergence (each thread updates every other cell of its
-// column, starting at its parity).
+// (gx/TX + gy/TY + gz/TZ) & 1.  A CTA relaxes NT tiles; each thread owns one
+// column of cells (cx, cy, 0..TZ-1) of a tile, whose x (with the two z-halo
+// cells), b, 1/d and z-face coefficients it keeps in registers; the x values of
+// the whole tile are mirrored in shared memory with an x / y halo ring, where the
+// x and y neighbours are read.  The columns of a warp all have the same parity of
+// cx + cy (every other x of whole rows), so in a red-black half step a warp
+// updates the same z cells in every lane: no divergence, and since the padded row
+// stride is even, the two half rows of a warp use the even and the odd banks.
 //
 // Loading: one thread per tile issues 3-D TMA boxes (cp.async.bulk.tensor) for the
-// tile's x, b, d, cx, cy, cz and for the y and z halo faces of x and the upper
-// y / z faces of cy / cz, all completing on one mbarrier.  A face whose
-// neighbour block is absent is requested at a coordinate outside the tensor and
-// arrives as zeros.  The x halo faces (x = -1, x = TX) and the upper x face of cx
-// start at an x not aligned to 16 bytes, so threads load them with plain loads
-// while the boxes are in flight.
+// tile's x, b, d, cx, cy, cz, for the y and z halo faces of x and for the upper
+// y / z faces of cy / cz, all completing on one mbarrier.  A face whose neighbour
+// block is absent is requested at a coordinate outside the tensor and arrives as
+// zeros.  The x halo columns (x = -1, x = TX) and cx at x = TX start at an x not
+// aligned to 16 bytes and are loaded with plain loads while the boxes fly.
 struct TileMaps {
   CUtensorMap xM, xY, xZ, b, d, cx, cy, cyY, cz, czZ;
 };
@@ -276,30 +282,35 @@ struct TileSmem {
   using Sh = TileShape<BS>;
   static constexpr int TX = Sh::TX, TY = Sh::TY, TZ = Sh::TZ;
   static constexpr int E = (int)sizeof(V);
+  static constexpr bool H = E != 4;  // FP16 storage: FP32 working copies of cx, cy
   static constexpr int C3 = TX * TY * TZ, CY2 = TX * TZ, CZ2 = TX * TY, CX2 = TY * TZ;
   static constexpr int al(int b) { return (b + 127) & ~127; }
-  static constexpr int X = 0;                       // main boxes [z][y][x] (V)
+  // FP32 x of the tile with its x and y halo: [TZ][TY + 2][TX + 2], cell (x, y, z)
+  // at z*XPS + (y+1)*XRS + x+1 (even row stride)
+  static constexpr int XRS = TX + 2, XPS = (TY + 2) * XRS, XSB = al(TZ * XPS * 4);
+  static constexpr int X = 0;                       // TMA boxes [z][y][x] (V)
   static constexpr int B = X + al(C3 * E);
   static constexpr int D = B + al(C3 * E);
-  static constexpr int CX = D + al(C3 * E);
+  static constexpr int CZ = D + al(C3 * E);
+  static constexpr int CX = CZ + al(C3 * E);
   static constexpr int CY = CX + al(C3 * E);
-  static constexpr int CZ = CY + al(C3 * E);
-  static constexpr int XYLO = CZ + al(C3 * E);      // x at y = -1, y = TY ([z][x], V)
+  static constexpr int XYLO = CY + al(C3 * E);      // x at y = -1, y = TY ([z][x], V)
   static constexpr int XYHI = XYLO + al(CY2 * E);
   static constexpr int XZLO = XYHI + al(CY2 * E);   // x at z = -1, z = TZ ([y][x], V)
   static constexpr int XZHI = XZLO + al(CZ2 * E);
   static constexpr int CYHI = XZHI + al(CZ2 * E);   // cy at y = TY ([z][x], V)
   static constexpr int CZHI = CYHI + al(CY2 * E);   // cz at z = TZ ([y][x], V)
-  static constexpr int XXLO = CZHI + al(CZ2 * E);   // x at x = -1, x = TX ([z][y], float)
-  static constexpr int XXHI = XXLO + al(CX2 * 4);
-  static constexpr int CXHI = XXHI + al(CX2 * 4);   // cx at x = TX ([z][y], V)
-  // FP32 working copies (FP16 storage only): x and its y / z faces
-  static constexpr int WX = CXHI + al(CX2 * E);
-  static constexpr int WYLO = WX + (E == 4 ? 0 : al(C3 * 4));
-  static constexpr int WYHI = WYLO + (E == 4 ? 0 : al(CY2 * 4));
-  static constexpr int WZLO = WYHI + (E == 4 ? 0 : al(CY2 * 4));
-  static constexpr int WZHI = WZLO + (E == 4 ? 0 : al(CZ2 * 4));
-  static constexpr int BYTES = WZHI + (E == 4 ? 0 : al(CZ2 * 4));
+  static constexpr int CXHI = CZHI + al(CZ2 * E);   // cx at x = TX ([z][y], float)
+  static constexpr int END0 = CXHI + al(CX2 * 4);
+  // the padded x array: over the x/b/d/cz boxes once they sit in registers when
+  // it fits there (FP32), else after everything
+  static constexpr bool XS_OVER = XSB <= CX;
+  static constexpr int XS = XS_OVER ? 0 : END0;
+  static constexpr int END1 = XS_OVER ? END0 : END0 + XSB;
+  static constexpr int WCX = END1;                  // FP16 storage: FP32 cx, cy, cy face
+  static constexpr int WCY = WCX + (H ? al(C3 * 4) : 0);
+  static constexpr int WCYHI = WCY + (H ? al(C3 * 4) : 0);
+  static constexpr int BYTES = WCYHI + (H ? al(CY2 * 4) : 0);
 };
 template <int BS>
 constexpr int tileThreads() {
@@ -311,6 +322,29 @@ constexpr size_t tileSmemBytes() {
   return (size_t)TileShape<BS>::NT * TileSmem<V, BS>::BYTES + 128;  // + mbarrier
 }
 
+// One red-black half step of a column: cells z = P, P+2, ... (all lanes of a warp
+// share P).  xp points at the cell (tx, ty, 0) of the padded x array; the upper
+// x / y face coefficients come from (pointer, stride per z).
+template <int TZ, int TXY, int XRS, int XPS, int P>
+__device__ __forceinline__ void colStep(float *xr, const float *bb, const float *rd, const float *czr, float *xp,
+                                        const float *cxs, const float *pcxu, int scxu, const float *cys,
+                                        const float *pcyu, int scyu) {
+#pragma unroll
+  for (int z = P; z < TZ; z += 2) {
+    float *q = xp + z * XPS;
+    float acc = bb[z];
+    acc += cxs[z * TXY] * q[-1];
+    acc += pcxu[z * scxu] * q[1];
+    acc += cys[z * TXY] * q[-XRS];
+    acc += pcyu[z * scyu] * q[XRS];
+    acc += czr[z] * xr[z];
+    acc += czr[z + 1] * xr[z + 2];
+    const float v = acc * rd[z];
+    xr[z + 1] = v;
+    q[0] = v;
+  }
+}
+
 template <typename V, int BS>
 __global__ void __launch_bounds__(tileThreads<BS>(), 2)
     kTileSmooth(const __grid_constant__ TileMaps maps, BlkGeom g, V *__restrict__ x, const V *__restrict__ cxg,
@@ -318,9 +352,15 @@ __global__ void __launch_bounds__(tileThreads<BS>(), 2)
   using S = TileSmem<V, BS>;
   using Sh = TileShape<BS>;
   constexpr int TX = Sh::TX, TY = Sh::TY, TZ = Sh::TZ, NT = Sh::NT, TXY = TX * TY;
+  constexpr int HX = TX / 2, RW = 64 / TX;  // lanes per half row, rows per warp
   extern __shared__ __align__(128) unsigned char smem[];
   const int tIn = threadIdx.x / TXY, r = threadIdx.x % TXY;
-  const int tx = r % TX, ty = r / TX;
+  // column of this thread: warp w of the tile takes rows RW*(w/2).. with
+  // (x + y) & 1 == w & 1
+  const int wq = r >> 5, lane = r & 31;
+  const int P = wq & 1;
+  const int ty = (wq >> 1) * RW + lane / HX;
+  const int tx = 2 * (lane % HX) + ((P + ty) & 1);
   unsigned char *tb = smem + tIn * S::BYTES;
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem + NT * S::BYTES);
 
@@ -328,14 +368,14 @@ __global__ void __launch_bounds__(tileThreads<BS>(), 2)
   const int64_t unit = (int64_t)blockIdx.x * NT + tIn;
   int s = 0, ox = 0, oy = 0, oz = 0;
   bool valid;
-  if (BS == 32) {  // 4 tiles of each colour per block: tz = j, ty from the colour
+  if (BS == 32) {  // 4 tiles of each colour per block: z tile j, y tile from the colour
     valid = unit < g.nAct * 4;
     if (valid) {
       s = (int)(unit >> 2);
       const int j = (int)(unit & 3);
       const int bxp = g.bpar[s] & 1;
-      oy = ((tc + bxp + j) & 1) * TY;
       oz = j * TZ;
+      oy = ((tc + bxp + j) & 1) * TY;
     }
   } else {         // the tile is the block: block parity lists
     const int64_t nUnits = tc == 0 ? g.nEven : g.nAct - g.nEven;
@@ -359,9 +399,9 @@ __global__ void __launch_bounds__(tileThreads<BS>(), 2)
       if (!ownZero) tmaLoad3(tb + S::X, &maps.xM, ox, oy, zb + oz, bar);
       tmaLoad3(tb + S::B, &maps.b, ox, oy, zb + oz, bar);
       tmaLoad3(tb + S::D, &maps.d, ox, oy, zb + oz, bar);
+      tmaLoad3(tb + S::CZ, &maps.cz, ox, oy, zb + oz, bar);
       tmaLoad3(tb + S::CX, &maps.cx, ox, oy, zb + oz, bar);
       tmaLoad3(tb + S::CY, &maps.cy, ox, oy, zb + oz, bar);
-      tmaLoad3(tb + S::CZ, &maps.cz, ox, oy, zb + oz, bar);
       const int32_t *nb = g.nbr + (int64_t)s * 6;
       // y faces (box TX x 1 x TZ), z faces (box TX x TY x 1); absent -> outside -> zeros
       int ylo, ylz, yhi, yhz, zlo, zhi;
@@ -385,50 +425,41 @@ __global__ void __launch_bounds__(tileThreads<BS>(), 2)
       mbarExpectTx(bar, 0);
     }
   }
-  // plain loads of the x halo faces (x = -1, x = TX) and of cx at x = TX:
-  // face cell (y, z) = (r % TY, r / TY), layout [z][y]
-  float *xxlo = reinterpret_cast<float *>(tb + S::XXLO);
-  float *xxhi = reinterpret_cast<float *>(tb + S::XXHI);
-  V *cxhi = reinterpret_cast<V *>(tb + S::CXHI);
-  if (valid && r < S::CX2) {
-    const int j = r % TY, kk = r / TY;
-    const int64_t lo = cellAt(g, s, ox - 1, oy + j, oz + kk);
-    const int64_t hi = cellAt(g, s, ox + TX, oy + j, oz + kk);
-    float vlo = 0.f, vhi = 0.f;
-    V chi = V(0.f);
-    if (lo >= 0 && !haloZero) vlo = ldv(x + lo) + (haloCorr ? ldv(xc + parentOf(lo, L)) : 0.f);
-    if (hi >= 0) {
-      chi = cxg[hi];
-      if (!haloZero) vhi = ldv(x + hi) + (haloCorr ? ldv(xc + parentOf(hi, L)) : 0.f);
+  // while the boxes fly: the x halo columns (x = -1, x = TX) and cx at x = TX by
+  // plain loads (face cell (y, z) = (q % TY, q / TY)), coarse corrections
+  constexpr int NXF = (S::CX2 + TXY - 1) / TXY;
+  float xlo[NXF], xhi[NXF];
+  float *cxhi = reinterpret_cast<float *>(tb + S::CXHI);
+#pragma unroll
+  for (int i = 0; i < NXF; i++) {
+    const int q = r + i * TXY;
+    xlo[i] = xhi[i] = 0.f;
+    if (valid && q < S::CX2) {
+      const int j = q % TY, kk = q / TY;
+      const int64_t lo = cellAt(g, s, ox - 1, oy + j, oz + kk);
+      const int64_t hi = cellAt(g, s, ox + TX, oy + j, oz + kk);
+      float chi = 0.f;
+      if (lo >= 0 && !haloZero) xlo[i] = ldv(x + lo) + (haloCorr ? ldv(xc + parentOf(lo, L)) : 0.f);
+      if (hi >= 0) {
+        chi = ldv(cxg + hi);
+        if (!haloZero) xhi[i] = ldv(x + hi) + (haloCorr ? ldv(xc + parentOf(hi, L)) : 0.f);
+      }
+      cxhi[q] = chi;
     }
-    xxlo[r] = vlo;
-    xxhi[r] = vhi;
-    cxhi[r] = chi;
   }
-  // coarse corrections of this thread's column (one parent per z pair)
-  float corr[TZ / 2];
+  float corr[TZ / 2], czc0 = 0.f, czc1 = 0.f;
+#pragma unroll
+  for (int z = 0; z < TZ / 2; z++) corr[z] = 0.f;
   if (valid && ownCorr) {
     const int Lc = L - 1;
     const int64_t pb = ((int64_t)s << (3 * Lc)) + ((ox + tx) >> 1) + ((int64_t)((oy + ty) >> 1) << Lc);
 #pragma unroll
     for (int z = 0; z < TZ / 2; z++) corr[z] = ldv(xc + pb + ((int64_t)((oz >> 1) + z) << (2 * Lc)));
-  } else {
-#pragma unroll
-    for (int z = 0; z < TZ / 2; z++) corr[z] = 0.f;
   }
-  // halo-face corrections (first post-smoothing launch), computed while the boxes fly:
-  // y-face cell (x, z) = (r % TX, r / TX) for r < TX*TZ; z-face cell (x, y) = (tx, ty)
-  float cy0 = 0.f, cy1 = 0.f, cz0 = 0.f, cz1 = 0.f;
-  if (valid && haloCorr) {
-    if (r < S::CY2) {
-      const int fx = r % TX, fz = r / TX;
-      const int64_t j0 = cellAt(g, s, ox + fx, oy - 1, oz + fz), j1 = cellAt(g, s, ox + fx, oy + TY, oz + fz);
-      if (j0 >= 0) cy0 = ldv(xc + parentOf(j0, L));
-      if (j1 >= 0) cy1 = ldv(xc + parentOf(j1, L));
-    }
+  if (valid && haloCorr) {  // the z-halo cells of this column
     const int64_t j2 = cellAt(g, s, ox + tx, oy + ty, oz - 1), j3 = cellAt(g, s, ox + tx, oy + ty, oz + TZ);
-    if (j2 >= 0) cz0 = ldv(xc + parentOf(j2, L));
-    if (j3 >= 0) cz1 = ldv(xc + parentOf(j3, L));
+    if (j2 >= 0) czc0 = ldv(xc + parentOf(j2, L));
+    if (j3 >= 0) czc1 = ldv(xc + parentOf(j3, L));
   }
   // wait for the boxes (bounded): one warp polls the barrier, the others sleep in
   // __syncthreads, which also publishes the landed data to them; the decision is
@@ -446,18 +477,7 @@ __global__ void __launch_bounds__(tileThreads<BS>(), 2)
       if (mbarTryWait(bar, 0)) break;  // no copy may land after exit
     return;
   }
-
-  // FP32 working copy of x and of its y / z halo faces
-  float *xs, *wylo, *wyhi, *wzlo, *wzhi;
-  if constexpr (S::E == 4) {
-    xs = reinterpret_cast<float *>(tb + S::X);
-    wylo = reinterpret_cast<float *>(tb + S::XYLO); wyhi = reinterpret_cast<float *>(tb + S::XYHI);
-    wzlo = reinterpret_cast<float *>(tb + S::XZLO); wzhi = reinterpret_cast<float *>(tb + S::XZHI);
-  } else {
-    xs = reinterpret_cast<float *>(tb + S::WX);
-    wylo = reinterpret_cast<float *>(tb + S::WYLO); wyhi = reinterpret_cast<float *>(tb + S::WYHI);
-    wzlo = reinterpret_cast<float *>(tb + S::WZLO); wzhi = reinterpret_cast<float *>(tb + S::WZHI);
-  }
+  // the column into registers
   const int own = ty * TX + tx;
   float xr[TZ + 2], bb[TZ], rd[TZ], czr[TZ + 1];
   {
@@ -465,73 +485,92 @@ __global__ void __launch_bounds__(tileThreads<BS>(), 2)
     const V *sd = reinterpret_cast<const V *>(tb + S::D), *scz = reinterpret_cast<const V *>(tb + S::CZ);
 #pragma unroll
     for (int z = 0; z < TZ; z++) {
-      float v = ownZero ? 0.f : ldv(sx + own + z * TXY);
-      v += corr[z >> 1];
-      xr[z + 1] = v;
-      xs[own + z * TXY] = v;
+      xr[z + 1] = (ownZero ? 0.f : ldv(sx + own + z * TXY)) + corr[z >> 1];
       bb[z] = ldv(sb + own + z * TXY);
       rd[z] = __frcp_rn(ldv(sd + own + z * TXY));
       czr[z] = ldv(scz + own + z * TXY);
     }
     czr[TZ] = ldv(reinterpret_cast<const V *>(tb + S::CZHI) + own);
+    const V *fz0 = reinterpret_cast<const V *>(tb + S::XZLO), *fz1 = reinterpret_cast<const V *>(tb + S::XZHI);
+    xr[0] = haloZero ? 0.f : ldv(fz0 + own) + czc0;
+    xr[TZ + 1] = haloZero ? 0.f : ldv(fz1 + own) + czc1;
   }
-  // halo faces in FP32: zero (first pre-smoothing launch) or + coarse correction
+  // y faces (+ coarse correction) and the FP32 coefficient copies, read before
+  // the padded x array may overwrite the staged boxes
+  constexpr int NYF = (S::CY2 + TXY - 1) / TXY;
+  float ya[NYF], yb[NYF];
   {
     const V *fy0 = reinterpret_cast<const V *>(tb + S::XYLO), *fy1 = reinterpret_cast<const V *>(tb + S::XYHI);
-    const V *fz0 = reinterpret_cast<const V *>(tb + S::XZLO), *fz1 = reinterpret_cast<const V *>(tb + S::XZHI);
-    if (r < S::CY2) {
-      wylo[r] = haloZero ? 0.f : ldv(fy0 + r) + cy0;
-      wyhi[r] = haloZero ? 0.f : ldv(fy1 + r) + cy1;
+#pragma unroll
+    for (int i = 0; i < NYF; i++) {
+      const int q = r + i * TXY;
+      ya[i] = yb[i] = 0.f;
+      if (valid && !haloZero && q < S::CY2) {
+        ya[i] = ldv(fy0 + q);
+        yb[i] = ldv(fy1 + q);
+        if (haloCorr) {
+          const int fx = q % TX, fz = q / TX;
+          const int64_t j0 = cellAt(g, s, ox + fx, oy - 1, oz + fz), j1 = cellAt(g, s, ox + fx, oy + TY, oz + fz);
+          if (j0 >= 0) ya[i] += ldv(xc + parentOf(j0, L));
+          if (j1 >= 0) yb[i] += ldv(xc + parentOf(j1, L));
+        }
+      }
     }
-    wzlo[own] = haloZero ? 0.f : ldv(fz0 + own) + cz0;
-    wzhi[own] = haloZero ? 0.f : ldv(fz1 + own) + cz1;
+  }
+  float *cxw, *cyw, *cyhw;
+  if constexpr (!S::H) {
+    cxw = reinterpret_cast<float *>(tb + S::CX); cyw = reinterpret_cast<float *>(tb + S::CY);
+    cyhw = reinterpret_cast<float *>(tb + S::CYHI);
+  } else {
+    cxw = reinterpret_cast<float *>(tb + S::WCX); cyw = reinterpret_cast<float *>(tb + S::WCY);
+    cyhw = reinterpret_cast<float *>(tb + S::WCYHI);
+    const V *scx = reinterpret_cast<const V *>(tb + S::CX), *scy = reinterpret_cast<const V *>(tb + S::CY);
+    const V *fcy = reinterpret_cast<const V *>(tb + S::CYHI);
+#pragma unroll
+    for (int z = 0; z < TZ; z++) {
+      cxw[own + z * TXY] = ldv(scx + own + z * TXY);
+      cyw[own + z * TXY] = ldv(scy + own + z * TXY);
+    }
+    for (int q = r; q < S::CY2; q += TXY) cyhw[q] = ldv(fcy + q);
+  }
+  if (S::XS_OVER) __syncthreads();  // the boxes under the padded array are read
+  float *xs = reinterpret_cast<float *>(tb + S::XS);
+  float *xp = xs + (ty + 1) * S::XRS + tx + 1;
+#pragma unroll
+  for (int z = 0; z < TZ; z++) xp[z * S::XPS] = xr[z + 1];
+#pragma unroll
+  for (int i = 0; i < NXF; i++) {
+    const int q = r + i * TXY;
+    if (q < S::CX2) {
+      const int j = q % TY, kk = q / TY;
+      xs[kk * S::XPS + (j + 1) * S::XRS] = xlo[i];
+      xs[kk * S::XPS + (j + 1) * S::XRS + TX + 1] = xhi[i];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < NYF; i++) {
+    const int q = r + i * TXY;
+    if (q < S::CY2) {
+      const int fx = q % TX, fz = q / TX;
+      xs[fz * S::XPS + fx + 1] = ya[i];                      // y = -1
+      xs[fz * S::XPS + (TY + 1) * S::XRS + fx + 1] = yb[i];  // y = TY
+    }
   }
   __syncthreads();
-  xr[0] = wzlo[own];
-  xr[TZ + 1] = wzhi[own];
-  // neighbour sources (pointer, stride per z) inside the tile or on a halo face
-  const float *pxm = tx > 0 ? xs + own - 1 : xxlo + ty;
-  const int sxm = tx > 0 ? TXY : TY;
-  const float *pxp = tx < TX - 1 ? xs + own + 1 : xxhi + ty;
-  const int sxp = tx < TX - 1 ? TXY : TY;
-  const float *pym = ty > 0 ? xs + own - TX : wylo + tx;
-  const int sym = ty > 0 ? TXY : TX;
-  const float *pyp = ty < TY - 1 ? xs + own + TX : wyhi + tx;
-  const int syp = ty < TY - 1 ? TXY : TX;
-  const V *cxs = reinterpret_cast<const V *>(tb + S::CX) + own;
-  const V *cys = reinterpret_cast<const V *>(tb + S::CY) + own;
-  const V *pcxu = tx < TX - 1 ? cxs + 1 : cxhi + ty;
+  // upper-face coefficients inside the tile or on a face (pointer, stride per z)
+  const float *cxs = cxw + own, *cys = cyw + own;
+  const float *pcxu = tx < TX - 1 ? cxs + 1 : cxhi + ty;
   const int scxu = tx < TX - 1 ? TXY : TY;
-  const V *pcyu = ty < TY - 1 ? cys + TX : reinterpret_cast<const V *>(tb + S::CYHI) + tx;
+  const float *pcyu = ty < TY - 1 ? cys + TX : cyhw + tx;
   const int scyu = ty < TY - 1 ? TXY : TX;
-  const int colPar = (tx + ty) & 1;
   for (int it = 0; it < k; it++) {
     for (int ci = 0; ci < 2; ci++) {
       const int cc = reverse ? 1 - ci : ci;
-      if (valid) {
-        // cells z = 2m + p of this column have colour cc
-        const bool p = ((cc - colPar) & 1) != 0;
-        const int pz = p ? 1 : 0;
-#pragma unroll
-        for (int m = 0; m < TZ / 2; m++) {
-          const int z = 2 * m + pz;
-          const float zm = p ? xr[2 * m + 1] : xr[2 * m];
-          const float zp = p ? xr[2 * m + 3] : xr[2 * m + 2];
-          const float c0 = p ? czr[2 * m + 1] : czr[2 * m];
-          const float c1 = p ? czr[2 * m + 2] : czr[2 * m + 1];
-          float acc = p ? bb[2 * m + 1] : bb[2 * m];
-          const float rr = p ? rd[2 * m + 1] : rd[2 * m];
-          acc += ldv(cxs + z * TXY) * pxm[z * sxm];
-          acc += ldv(pcxu + z * scxu) * pxp[z * sxp];
-          acc += ldv(cys + z * TXY) * pym[z * sym];
-          acc += ldv(pcyu + z * scyu) * pyp[z * syp];
-          acc += c0 * zm;
-          acc += c1 * zp;
-          const float v = acc * rr;
-          xr[2 * m + 1] = p ? xr[2 * m + 1] : v;
-          xr[2 * m + 2] = p ? v : xr[2 * m + 2];
-          xs[own + z * TXY] = v;
-        }
+      if (valid) {  // cells z with (tx + ty + z) & 1 == cc: z = ((cc - P) & 1) + 2m
+        if (((cc - P) & 1) == 0)
+          colStep<TZ, TXY, S::XRS, S::XPS, 0>(xr, bb, rd, czr, xp, cxs, pcxu, scxu, cys, pcyu, scyu);
+        else
+          colStep<TZ, TXY, S::XRS, S::XPS, 1>(xr, bb, rd, czr, xp, cxs, pcxu, scxu, cys, pcyu, scyu);
       }
       __syncthreads();
     }
@@ -613,6 +652,18 @@ __global__ void __launch_bounds__(256) kUpdateXRQuad(const double *__restrict__ 
   rr = blockSum(rr);
   if (threadIdx.x == 0) partial[blockIdx.x] = rr;
 }
+// x += scale * e (FP32 x, FP16 correction)
+__global__ void __launch_bounds__(256) kAddScaledQuad(const __half *__restrict__ e, float scale, float *__restrict__ x,
+                                                      int64_t nq) {
+  QUAD_STRIDE(k, nq) {
+    float ev[4], xv[4];
+    ldRow<4>(e + 4 * k, ev);
+    ldRow<4>(x + 4 * k, xv);
+#pragma unroll
+    for (int i = 0; i < 4; i++) xv[i] = fmaf(scale, ev[i], xv[i]);
+    stRow<4>(x + 4 * k, xv);
+  }
+}
 // beta = sc[2] / sc[0]; p = z + beta p
 template <typename V>
 __global__ void __launch_bounds__(256) kUpdatePQuad(const double *__restrict__ sc, const V *__restrict__ z,
@@ -692,7 +743,7 @@ BlkGeom blkOf(const PoissonState *ps, const MgLevel &L) {
 // ---------------------------------------------------------------------------------
 template <typename V>
 int blkApply(msbg_gpu_ctx *ctx, PoissonState *ps, size_t l, const PrecSet &P, const V *x, const V *b, V *y,
-             int mode, double *dotOut, V *bc, V *xc) {
+             int mode, double *dotOut, V *bc, V *xc, __half *rhOut, float rhScale) {
   const MgLevel &Lv = ps->levels[l];
   const int64_t nQuad = Lv.nCell / 4;
   int64_t grid = (nQuad + 255) / 256;
@@ -700,7 +751,7 @@ int blkApply(msbg_gpu_ctx *ctx, PoissonState *ps, size_t l, const PrecSet &P, co
   if (grid < 1) grid = 1;
   MSBG_LAUNCH(ctx, kApplyRows<V>, (unsigned)grid, 256, 0, blkOf(ps, Lv), x, b, (const V *)P.cx[l],
               (const V *)P.cy[l], (const V *)P.cz[l], (const V *)P.d[l], y, mode,
-              dotOut ? ps->dPartial : nullptr, bc, xc);
+              dotOut ? ps->dPartial : nullptr, bc, xc, rhOut, rhScale);
   if (dotOut && mode == 2) MSBG_LAUNCH(ctx, kSumPartialsBlk2, 1, kRedThreads, 0, ps->dPartial, (int)grid, dotOut);
   else if (dotOut) MSBG_LAUNCH(ctx, kSumPartialsBlk, 1, kRedThreads, 0, ps->dPartial, (int)grid, dotOut);
   return MSBG_GPU_OK;
@@ -725,6 +776,10 @@ int blkUpdateXR(msbg_gpu_ctx *ctx, PoissonState *ps, const double *sc, const V *
   const unsigned g = quadGrid(ps, n / 4);
   MSBG_LAUNCH(ctx, kUpdateXRQuad<V>, g, 256, 0, sc, p, q, x, r, n / 4, ps->dPartial);
   MSBG_LAUNCH(ctx, kSumPartialsBlk, 1, kRedThreads, 0, ps->dPartial, (int)g, rrOut);
+  return MSBG_GPU_OK;
+}
+int blkAddScaled(msbg_gpu_ctx *ctx, PoissonState *ps, const __half *e, float scale, float *x, int64_t n) {
+  MSBG_LAUNCH(ctx, kAddScaledQuad, quadGrid(ps, n / 4), 256, 0, e, scale, x, n / 4);
   return MSBG_GPU_OK;
 }
 template <typename V>
@@ -819,9 +874,9 @@ int blkSmoothColor(msbg_gpu_ctx *ctx, PoissonState *ps, size_t l, const PrecSet 
 }
 
 template int blkApply<float>(msbg_gpu_ctx *, PoissonState *, size_t, const PrecSet &, const float *, const float *,
-                             float *, int, double *, float *, float *);
+                             float *, int, double *, float *, float *, __half *, float);
 template int blkApply<__half>(msbg_gpu_ctx *, PoissonState *, size_t, const PrecSet &, const __half *,
-                              const __half *, __half *, int, double *, __half *, __half *);
+                              const __half *, __half *, int, double *, __half *, __half *, __half *, float);
 #define INST_VEC(V)                                                                                         \
   template int blkDot<V>(msbg_gpu_ctx *, PoissonState *, const V *, const V *, int64_t, double *);                 \
   template int blkUpdateXR<V>(msbg_gpu_ctx *, PoissonState *, const double *, const V *, const V *, V *, V *,     \
