@@ -42,6 +42,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 from msbg_gb300 import gpu as G  # noqa: E402
+from msbg_gb300 import poisson_workload as PW  # noqa: E402
 from msbg_gb300 import workloads as W  # noqa: E402
 
 OPT8 = 1 << 29
@@ -344,6 +345,9 @@ def run_gpu(args, spec, dist: Dist):
 
     d.free()
     g.close()
+    poisson = None
+    if not args.no_poisson and spec is W.SURFACE_4096:
+        poisson = poisson_measure(96, max(1, min(args.steps, 3)), 1)
     if dist.rank != 0:
         return
     line = {
@@ -362,6 +366,60 @@ def run_gpu(args, spec, dist: Dist):
         "clocks": clk,
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "poisson": poisson,
+    }
+    print(json.dumps(line), flush=True)
+
+
+WARMNET = os.path.join(ROOT, "msbg_gb300", "data", "warmnet_c3.npz")
+
+
+def poisson_measure(n_objects: int, steps: int, warmup: int,
+                    modes=("plain", "mixed", "learned", "learned_mixed")) -> dict:
+    """Time-to-1e-6 of the sparse Poisson solve on the level-0 blocks of the 4096^3
+    layout (first n_objects clusters): plain FP32 MG-PCG and FP16-storage / FP32
+    iterative refinement from X = 0, and both from the learned warm start (trained
+    weights in msbg_gb300/data, forward pass inside the timed region); median over
+    `steps` solves."""
+    g, spec = PW.surface_layout_grid(n_objects)
+    try:
+        bs = spec["bsx"]
+        PW.setup_problem(g, bs)
+        if any(m.startswith("learned") for m in modes):
+            W_, c_ = PW.load_warmnet(WARMNET)
+            g.warmnet_set(W_, c_)
+        cells = int(g.info().nActive) * bs ** 3
+        out = {"workload": f"poisson-4096^3-bs32-crop{n_objects}", "cells": cells,
+               "mg_levels": [int(v) for v in g.mg_info()], "tolerance": 1e-6,
+               "rhs": "N(0,1) per cell, zero mean per 6-connected component",
+               "coefficients": "face coefficients U[0.5,2], Dirichlet 0 outside"}
+        for kind in modes:
+            for _ in range(warmup):
+                PW.timed_solve(g, kind)
+            runs = [PW.timed_solve(g, kind) for _ in range(steps)]
+            med = sorted(runs, key=lambda r: r["ms"])[len(runs) // 2]
+            out[kind] = med
+        for m in modes:
+            if m != "plain" and "plain" in out:
+                out[f"{m}_speedup_vs_plain"] = out["plain"]["ms"] / out[m]["ms"]
+        return out
+    finally:
+        g.close()
+
+
+def run_poisson(args, dist):
+    n_obj = {"poisson-crop96": 96, "poisson-crop12": 12}[args.workload]
+    res = poisson_measure(n_obj, args.steps, args.warmup)
+    if dist.rank != 0:
+        return
+    plain = res["plain"]
+    line = {
+        "metric": "time-to-1e-6 relative residual (plain FP32 MG-PCG)", "value": plain["ms"], "unit": "ms",
+        "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": plain["ms"],
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 dots)",
+        "data": "synthetic", "config": {"workload": res["workload"], "cells": res["cells"],
+                                        "l2": "inputs larger than L2 (no flush)"},
+        "gpu_launches": plain["gpu_launches"], "poisson": res,
     }
     print(json.dumps(line), flush=True)
 
@@ -373,7 +431,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="surface4096",
-                    choices=["surface4096", "surface4096-crop", "surface512"])
+                    choices=["surface4096", "surface4096-crop", "surface512", "poisson-crop96", "poisson-crop12"])
+    ap.add_argument("--no-poisson", action="store_true",
+                    help="skip the sparse Poisson time-to-1e-6 measurement of the default run")
     ap.add_argument("--variant", default="fast", choices=["fast", "exact"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -381,10 +441,18 @@ def main():
     ap.add_argument("--traffic-per-launch", type=float, default=None,
                     help="DRAM bytes per sweep launch from an ncu capture (reported as roofline.traffic)")
     args = ap.parse_args()
-    spec = {"surface4096": W.SURFACE_4096, "surface4096-crop": W.SURFACE_4096_CROP,
-            "surface512": W.SURFACE_512}[args.workload]
     dist = Dist()
     try:
+        if args.workload.startswith("poisson"):
+            if args.impl == "reference":
+                if dist.rank == 0:
+                    print(json.dumps({"impl": "reference", "unavailable":
+                                      "the reference release has no Poisson solver driver"}), flush=True)
+            else:
+                run_poisson(args, dist)
+            return
+        spec = {"surface4096": W.SURFACE_4096, "surface4096-crop": W.SURFACE_4096_CROP,
+                "surface512": W.SURFACE_512}[args.workload]
         if args.impl == "reference":
             run_reference(args, spec, dist)
         else:

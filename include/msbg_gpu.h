@@ -195,8 +195,10 @@ int msbg_gpu_poisson_procedural_coefficients(msbg_gpu_ctx *ctx, uint32_t seed, i
 /* multiplyLaplacianMatrixOpt (src/msbg.h:3167-3176): Y = A X, or Y = B - A X. */
 int msbg_gpu_multiply_laplacian(msbg_gpu_ctx *ctx, int chanX, int chanB, int chanDstY,
                                 int calcResidual);
-/* relax (src/msbg.h:3269-3277): nIter red-black Gauss-Seidel sweeps of A X = B on the
- * finest level (red first, or black first when reverseOrder). */
+/* relax (src/msbg.h:3269-3277): nIter smoothing passes of A X = B on the finest
+ * level, red-black over tiles with in-tile red-black Gauss-Seidel (the multigrid
+ * smoother below); reverseOrder runs the adjoint order (tile colour 1 first, black
+ * cells first). */
 int msbg_gpu_relax(msbg_gpu_ctx *ctx, int chanX, int chanB, int nIter, int reverseOrder);
 /* One multigrid V-cycle X = M^{-1} B from X = 0 (the CG preconditioner). */
 int msbg_gpu_vcycle(msbg_gpu_ctx *ctx, int chanX, int chanB);
@@ -221,7 +223,7 @@ int msbg_gpu_mgpcg_solve(msbg_gpu_ctx *ctx, int chanX, int chanB, double tol, in
 int msbg_gpu_mgpcg_solve_mixed(msbg_gpu_ctx *ctx, int chanX, int chanB, double tol, int maxOuter,
                                double innerTol, int maxInner, int *outerOut, int *innerTotalOut,
                                double *relResOut);
-/* Multigrid parameters (defaults 2, 2, 1, 0): smoothing passes before and
+/* Multigrid parameters (defaults 2, 2, 3, 0): smoothing passes before and
  * after the coarse correction, in-tile red-black sweeps per pass (levels with
  * block edge >= 8 smooth 16^3 / 8^3 tiles in two tile colours; smaller levels
  * do that many pointwise red-black sweeps), and the coarsest level's solver:
@@ -233,6 +235,32 @@ int msbg_gpu_poisson_set_params(msbg_gpu_ctx *ctx, int preSweeps, int postSweeps
                                 int coarsestIter);
 /* Multigrid levels of the current hierarchy and their cell counts. */
 int msbg_gpu_mg_info(msbg_gpu_ctx *ctx, int *nLevels, int64_t *cellsPerLevel, int cap);
+
+/* ---- learned warm start ------------------------------------------------------------
+ * A 4-layer 3D convolutional network (channels 2-16-16-16-2, 3x3x3 kernels, BF16
+ * weights, FP32 activations and accumulation) on the level-1 cells of the Poisson
+ * hierarchy (value blocks with their edge halved).  Inputs: the restricted
+ * right-hand side (scaled by its rms) and the level-1 diagonal (scaled by its
+ * mean); outputs: a level-1 solution plus a level-2-averaged correction, injected
+ * to level 0 as the solve's starting point.  Trained on (B, X*) pairs from the
+ * plain solver with Adam; loss 0 (default) = ||X1 - avg(X*)||^2 / ||avg(X*)||^2 on
+ * level 1 (avg: mean of the 8 level-0 children), loss 1 = ||A (X0 - X*)||^2 / ||B||^2.
+ * No reference counterpart: the reference has no learned component.
+ * Weight layout: per layer l, W[27][Cin][Cout] (tap = (dx+1) + 3(dy+1) + 9(dz+1)),
+ * layers concatenated; biases per layer concatenated. */
+int msbg_gpu_warmnet_param_count(int *nWeights, int *nBiases);
+int msbg_gpu_warmnet_set_weights(msbg_gpu_ctx *ctx, const float *hW, const float *hB, int resetOptimizer);
+int msbg_gpu_warmnet_get_weights(msbg_gpu_ctx *ctx, float *hW, float *hB);
+int msbg_gpu_warmnet_set_loss(msbg_gpu_ctx *ctx, int lossMode);
+/* X0 = the network's starting point for A X = B (FP32 channels). */
+int msbg_gpu_warmnet_predict(msbg_gpu_ctx *ctx, int chanB, int chanX0);
+/* Loss and gradients (host arrays in the weight layout, may be NULL) for one pair. */
+int msbg_gpu_warmnet_loss_grad(msbg_gpu_ctx *ctx, int chanB, int chanXstar, double *loss, float *hGradW,
+                               float *hGradB);
+/* One Adam step (lr; betas 0.9, 0.999) on a pair given as device arrays laid out
+ * like a level-0 payload [nActive][bs^3]; *loss is the loss before the step. */
+int msbg_gpu_warmnet_train_step(msbg_gpu_ctx *ctx, const float *dB, const float *dXstar, float lr,
+                                double *loss);
 
 /* ---- value-block slots without allocating ----------------------------------------
  * This entry point has no counterpart in the reference.  It computes what
@@ -266,6 +294,7 @@ int msbg_gpu_host_free(void *hPtr);
 /* Device memory helpers for callers without a CUDA runtime of their own. */
 int msbg_gpu_device_alloc(void **dPtr, size_t bytes);
 int msbg_gpu_device_free(void *dPtr);
+int msbg_gpu_copy_d2d(msbg_gpu_ctx *ctx, void *dDst, const void *dSrc, size_t bytes);
 int msbg_gpu_copy_h2d(msbg_gpu_ctx *ctx, void *dDst, const void *hSrc, size_t bytes);
 int msbg_gpu_copy_d2h(msbg_gpu_ctx *ctx, void *hDst, const void *dSrc, size_t bytes);
 

@@ -405,6 +405,7 @@ extern "C" int msbg_gpu_destroy(msbg_gpu_ctx *ctx) {
   }
   if (ctx->dTmpSlab) cudaFree(ctx->dTmpSlab);
   if (ctx->dPts) cudaFree(ctx->dPts);
+  msbg::warmNetFree(ctx->warmnet);
   msbg::poissonFree(ctx->poisson);
   for (auto &ev : ctx->ev) if (ev) cudaEventDestroy(ev);
   delete ctx;
@@ -794,6 +795,11 @@ extern "C" int msbg_gpu_device_free(void *p) {
 extern "C" int msbg_gpu_copy_h2d(msbg_gpu_ctx *ctx, void *d, const void *h, size_t bytes) {
   if (!ctx) return MSBG_GPU_ERR_ARG;
   MSBG_CUDA(ctx, cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  return MSBG_GPU_OK;
+}
+extern "C" int msbg_gpu_copy_d2d(msbg_gpu_ctx *ctx, void *dd, const void *ds, size_t bytes) {
+  if (!ctx) return MSBG_GPU_ERR_ARG;
+  MSBG_CUDA(ctx, cudaMemcpyAsync(dd, ds, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
   return MSBG_GPU_OK;
 }
 extern "C" int msbg_gpu_copy_d2h(msbg_gpu_ctx *ctx, void *h, const void *d, size_t bytes) {

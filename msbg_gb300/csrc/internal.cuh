@@ -13,6 +13,9 @@
 namespace msbg {
 
 struct PoissonState;
+struct WarmNetState;
+void poissonFree(PoissonState *ps);
+void warmNetFree(WarmNetState *w);
 constexpr int kMaxChannels = 64;
 constexpr int kMaxEvents = 16;
 
@@ -68,7 +71,8 @@ struct msbg_gpu_ctx {
   int64_t launches = 0;
   int64_t layoutStamp = 0;                 // bumped by every set_refinement_map
   msbg::PoissonState *poisson = nullptr;   // solver hierarchy of the current layout
-  int mgPre = 2, mgPost = 2, mgTileIters = 1, mgCoarsestIter = 0;  // multigrid parameters
+  msbg::WarmNetState *warmnet = nullptr;   // learned warm start (weights, level-1 buffers)
+  int mgPre = 2, mgPost = 2, mgTileIters = 3, mgCoarsestIter = 0;  // multigrid parameters
   std::string err;
 };
 

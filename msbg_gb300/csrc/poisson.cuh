@@ -148,7 +148,7 @@ struct PoissonState {
   double *dPartial = nullptr;
   int nPartial = 0;
   double *dScal = nullptr, *hScal = nullptr;
-  int preSweeps = 2, postSweeps = 2, tileIters = 1;
+  int preSweeps = 2, postSweeps = 2, tileIters = 3;
   int coarsestIter = 0;  // 0: exact solve with the dense inverse below
   int64_t coarsestCells = 512;
   float *dCoarseInv = nullptr;  // [n][n] inverse of the coarsest operator

@@ -83,11 +83,11 @@ __device__ __forceinline__ int64_t parentOf(int64_t j, int L) {
 // Quad q of a block (4 cells along x) -> block-local origin.  Bits of q from the
 // bottom: x quad (log2(bs/4) bits), y parity, z parity, y pair, z pair; so the 8
 // children of a coarse cell pair are the 4 lanes {q, q^xq, q^2xq, q^3xq}.
-template <typename V>
-__global__ void __launch_bounds__(256) kApplyRows(BlkGeom g, const V *__restrict__ x, const V *__restrict__ b,
+template <typename V, int MODE>
+__global__ void __launch_bounds__(256, 3) kApplyRows(BlkGeom g, const V *__restrict__ x, const V *__restrict__ b,
                                                   const V *__restrict__ cx, const V *__restrict__ cy,
                                                   const V *__restrict__ cz, const V *__restrict__ d,
-                                                  V *__restrict__ y, int mode, double *__restrict__ dotPartial,
+                                                  V *__restrict__ y, double *__restrict__ dotPartial,
                                                   V *__restrict__ bc, V *__restrict__ xc,
                                                   __half *__restrict__ rhOut, float rhScale) {
   const int L = g.log2bs, bs = g.bs;
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(256) kApplyRows(BlkGeom g, const V *__restrict
       else { zq[0] = zq[1] = zq[2] = zq[3] = 0.f; czu[0] = czu[1] = czu[2] = czu[3] = 0.f; }
     }
     float r[4];
-    if (mode == 2) {
+    if constexpr (MODE == 2) {
       // r = b - A x in double-float arithmetic: every product split exactly into
       // a rounded part and its error (fma), the running sum kept exact with
       // TwoSum and the errors gathered in a second float; then sum r^2, b^2.
@@ -178,8 +178,7 @@ __global__ void __launch_bounds__(256) kApplyRows(BlkGeom g, const V *__restrict
           stRow<4>(rhOut + c, sc);
         }
       }
-      continue;
-    }
+    } else {
 #pragma unroll
     for (int i = 0; i < 4; i++) {
       const float xm1 = i == 0 ? xl : xv[i - 1];
@@ -194,7 +193,7 @@ __global__ void __launch_bounds__(256) kApplyRows(BlkGeom g, const V *__restrict
       a -= czu[i] * zq[i];
       r[i] = a;
     }
-    if (mode == 1) {
+    if (MODE == 1) {
       float bv[4];
       ldRow<4>(b + c, bv);
 #pragma unroll
@@ -224,10 +223,11 @@ __global__ void __launch_bounds__(256) kApplyRows(BlkGeom g, const V *__restrict
     } else if (act && y) {
       stRow<4>(y + c, r);
     }
+    }
   }
   if (dotPartial) {
     dot = blockSum(dot);
-    if (mode == 2) {
+    if constexpr (MODE == 2) {
       dot2 = blockSum(dot2);
       if (threadIdx.x == 0) {
         dotPartial[2 * blockIdx.x] = dot;
@@ -749,9 +749,18 @@ int blkApply(msbg_gpu_ctx *ctx, PoissonState *ps, size_t l, const PrecSet &P, co
   int64_t grid = (nQuad + 255) / 256;
   if (grid > ps->nPartial) grid = ps->nPartial;
   if (grid < 1) grid = 1;
-  MSBG_LAUNCH(ctx, kApplyRows<V>, (unsigned)grid, 256, 0, blkOf(ps, Lv), x, b, (const V *)P.cx[l],
-              (const V *)P.cy[l], (const V *)P.cz[l], (const V *)P.d[l], y, mode,
-              dotOut ? ps->dPartial : nullptr, bc, xc, rhOut, rhScale);
+  const BlkGeom gg = blkOf(ps, Lv);
+  const V *cx = (const V *)P.cx[l], *cy = (const V *)P.cy[l], *cz = (const V *)P.cz[l], *d = (const V *)P.d[l];
+  double *part = dotOut ? ps->dPartial : nullptr;
+  if (mode == 0)
+    MSBG_LAUNCH(ctx, (kApplyRows<V, 0>), (unsigned)grid, 256, 0, gg, x, b, cx, cy, cz, d, y, part, bc, xc, rhOut,
+                rhScale);
+  else if (mode == 1)
+    MSBG_LAUNCH(ctx, (kApplyRows<V, 1>), (unsigned)grid, 256, 0, gg, x, b, cx, cy, cz, d, y, part, bc, xc, rhOut,
+                rhScale);
+  else
+    MSBG_LAUNCH(ctx, (kApplyRows<V, 2>), (unsigned)grid, 256, 0, gg, x, b, cx, cy, cz, d, y, part, bc, xc, rhOut,
+                rhScale);
   if (dotOut && mode == 2) MSBG_LAUNCH(ctx, kSumPartialsBlk2, 1, kRedThreads, 0, ps->dPartial, (int)grid, dotOut);
   else if (dotOut) MSBG_LAUNCH(ctx, kSumPartialsBlk, 1, kRedThreads, 0, ps->dPartial, (int)grid, dotOut);
   return MSBG_GPU_OK;

@@ -1,0 +1,741 @@
+// Learned warm start for the Poisson solve: a 4-layer 3D convolutional network on
+// the level-1 cells of the multigrid hierarchy (the value blocks with their edge
+// halved), trained and run by the kernels below.
+//
+//   in  = [ b1 * invS,  d1 * invD - 1 ]     b1 = sum of the 8 level-0 children of b,
+//                                           d1 = level-1 diagonal, invS = 1/rms(b1),
+//                                           invD = 1/mean(d1)
+//   h1 = relu(conv(in, W1) + c1),  h2 = relu(conv(h1, W2) + c2),
+//   h3 = relu(conv(h2, W3) + c3),  o = conv(h3, W4) + c4       channels 2-16-16-16-2
+//   x1 = S * (o0 + avg2(o1))        S = rms(b1); avg2: mean over the 8 level-1 cells
+//                                   of a level-2 parent, on every one of them
+//   x0 = x1 on each of the 8 level-0 children (the solve's starting point)
+//
+// conv: 3x3x3, zero outside the active cells, BF16 weights W[tap][cin][cout]
+// (tap = (dx+1) + 3(dy+1) + 9(dz+1)), FP32 activations and accumulation.
+// Training loss (x* from the plain solver): "coarse" L = ||x1 - avg1(x*)||^2 /
+// ||avg1(x*)||^2, avg1 = mean of the 8 level-0 children (the best coarse starting
+// value), or "residual" L = ||A0 (x0 - x*)||^2 / ||b||^2.  Adam on FP32 master
+// weights, re-rounded to BF16 after every step.
+//
+// Activations are channel-last [cell][C] FP32 arrays on level 1.  A cell finds its
+// 26 neighbours inside its block by offset and across blocks through a per-block
+// table of the 27 blocks around it.
+#include <cuda_bf16.h>
+
+#include <vector>
+
+#include "internal.cuh"
+#include "poisson.cuh"
+
+namespace msbg {
+
+constexpr int kWnLayers = 4;
+constexpr int kWnCh[kWnLayers + 1] = {2, 16, 16, 16, 2};
+
+struct WarmNetState {
+  int64_t layoutStamp = -1;
+  int64_t n1 = 0, n2 = 0;          // level-1 and level-2 cells
+  int32_t *nbr27 = nullptr;        // [nAct][27]
+  float *w32[kWnLayers] = {}, *bias[kWnLayers] = {};
+  __nv_bfloat16 *wq[kWnLayers] = {};
+  float *gw[kWnLayers] = {}, *gb[kWnLayers] = {};
+  float *mw[kWnLayers] = {}, *vw[kWnLayers] = {}, *mb[kWnLayers] = {}, *vb[kWnLayers] = {};
+  float *act[kWnLayers + 1] = {};  // activations; act[0] = raw inputs (b1, d1)
+  float *gact[2] = {};             // ping-pong upstream gradients [n1][16]
+  float *x1 = nullptr, *gx1 = nullptr;
+  float *t0a = nullptr, *t0b = nullptr;  // level-0 temporaries
+  double *dScal = nullptr, *hScal = nullptr;
+  double *dPart = nullptr;
+  int nPart = 0;
+  int step = 0;
+  int lossMode = 0;  // 0 coarse, 1 residual
+  bool weightsSet = false;
+};
+
+int wnWeights(int l) { return 27 * kWnCh[l] * kWnCh[l + 1]; }
+
+// ---------------------------------------------------------------------------------
+// neighbours on level 1
+// ---------------------------------------------------------------------------------
+struct WnGeom {
+  int bs, L;         // level-1 block edge
+  int64_t nAct;
+  const int32_t *nbr27;
+};
+
+// index of the level-1 cell at block-local (lx+dx, ly+dy, lz+dz) of slot s, or -1
+__device__ __forceinline__ int64_t wnNbr(const WnGeom &g, int s, int lx, int ly, int lz, int dx, int dy, int dz) {
+  int x = lx + dx, y = ly + dy, z = lz + dz;
+  const int m = g.bs - 1;
+  const int ox = x < 0 ? -1 : (x > m ? 1 : 0), oy = y < 0 ? -1 : (y > m ? 1 : 0), oz = z < 0 ? -1 : (z > m ? 1 : 0);
+  if (ox | oy | oz) {
+    s = g.nbr27[(int64_t)s * 27 + (ox + 1) + 3 * (oy + 1) + 9 * (oz + 1)];
+    if (s < 0) return -1;
+    x &= m; y &= m; z &= m;
+  }
+  return ((int64_t)s << (3 * g.L)) + ((int64_t)((z << g.L) + y) << g.L) + x;
+}
+
+__global__ void kNbr27(const int32_t *__restrict__ active, int64_t nAct, int nbx, int nby, int nbz,
+                       const int32_t *__restrict__ slot, int32_t *__restrict__ nbr) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nAct * 27) return;
+  const int64_t s = i / 27;
+  const int k = (int)(i % 27);
+  const int bid = active[s];
+  const int bx = bid % nbx + k % 3 - 1, by = (bid / nbx) % nby + (k / 3) % 3 - 1, bz = bid / (nbx * nby) + k / 9 - 1;
+  int v = -1;
+  if (bx >= 0 && by >= 0 && bz >= 0 && bx < nbx && by < nby && bz < nbz)
+    v = slot[((int64_t)bz * nby + by) * nbx + bx];
+  nbr[i] = v;
+}
+
+// ---------------------------------------------------------------------------------
+// inputs, output head, transfers
+// ---------------------------------------------------------------------------------
+// act0[c] = (b1, d1) and partial sums of b1^2, d1 (level-1 cell c; its 8 children
+// in the level-0 block of the same slot)
+__global__ void kWnInputs(const float *__restrict__ b0, const float *__restrict__ d1, int L1, int64_t n1,
+                          float2 *__restrict__ act0, double *__restrict__ part) {
+  double sb = 0.0, sd = 0.0;
+  const int L0 = L1 + 1, m1 = (1 << L1) - 1;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n1; c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = c >> (3 * L1);
+    const int v = (int)(c & ((1 << (3 * L1)) - 1));
+    const int lx = v & m1, ly = (v >> L1) & m1, lz = v >> (2 * L1);
+    const int64_t base = (s << (3 * L0)) + ((int64_t)((2 * lz) << L0) << L0) + ((int64_t)(2 * ly) << L0) + 2 * lx;
+    float b = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      b += b0[base + ((int64_t)((k >> 2) << L0) << L0) + ((int64_t)((k >> 1) & 1) << L0) + (k & 1)];
+    const float d = d1[c];
+    act0[c] = make_float2(b, d);
+    sb += (double)b * b;
+    sd += d;
+  }
+  sb = blockSum(sb);
+  sd = blockSum(sd);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = sb;
+    part[2 * blockIdx.x + 1] = sd;
+  }
+}
+// sc[0] = S = rms(b1), sc[1] = invS, sc[2] = invD from the partial sums
+__global__ void kWnScales(const double *__restrict__ part, int n, int64_t n1, double *__restrict__ sc) {
+  double s0 = 0.0, s1 = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) { s0 += part[2 * i]; s1 += part[2 * i + 1]; }
+  s0 = blockSum(s0);
+  s1 = blockSum(s1);
+  if (threadIdx.x == 0) {
+    const double rms = n1 > 0 ? sqrt(s0 / (double)n1) : 0.0;
+    const double S = rms > 0 ? rms : 1.0;
+    const double mean = n1 > 0 ? s1 / (double)n1 : 1.0;
+    sc[0] = S;
+    sc[1] = 1.0 / S;
+    sc[2] = mean != 0.0 ? 1.0 / mean : 1.0;
+  }
+}
+
+// x1 = S (o0 + avg2(o1)); x0 on the 8 children.  One thread per level-2 parent.
+__global__ void kWnHead(const float2 *__restrict__ o, const double *__restrict__ sc, int L1, int64_t n2,
+                        float *__restrict__ x1, float *__restrict__ x0) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n2) return;
+  const int L2 = L1 - 1, L0 = L1 + 1, m2 = (1 << L2) - 1;
+  const int64_t s = p >> (3 * L2);
+  const int v = (int)(p & ((1 << (3 * L2)) - 1));
+  const int px = v & m2, py = (v >> L2) & m2, pz = v >> (2 * L2);
+  int64_t ch[8];
+  float o0[8], avg = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const int lx = 2 * px + (k & 1), ly = 2 * py + ((k >> 1) & 1), lz = 2 * pz + (k >> 2);
+    ch[k] = (s << (3 * L1)) + ((int64_t)((lz << L1) + ly) << L1) + lx;
+    const float2 ov = o[ch[k]];
+    o0[k] = ov.x;
+    avg += ov.y;
+  }
+  avg *= 0.125f;
+  const float S = (float)sc[0];
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const float xv = S * (o0[k] + avg);
+    x1[ch[k]] = xv;
+    if (x0) {
+      const int lx = 2 * (2 * px + (k & 1)), ly = 2 * (2 * py + ((k >> 1) & 1)), lz = 2 * (2 * pz + (k >> 2));
+      const int64_t b0 = (s << (3 * L0)) + ((int64_t)((lz << L0) + ly) << L0) + lx;
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        x0[b0 + ((int64_t)((q >> 2) << L0) << L0) + ((int64_t)((q >> 1) & 1) << L0) + (q & 1)] = xv;
+    }
+  }
+}
+
+// Upstream gradient of the head: g(o0) = S gx1, g(o1) = S avg2(gx1).  gx1 = sum of
+// the 8 level-0 children of g0.  One thread per level-2 parent; writes [n1][2].
+__global__ void kWnHeadBack(const float *__restrict__ g0, const double *__restrict__ sc, int L1, int64_t n2,
+                            float2 *__restrict__ go) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n2) return;
+  const int L2 = L1 - 1, L0 = L1 + 1, m2 = (1 << L2) - 1;
+  const int64_t s = p >> (3 * L2);
+  const int v = (int)(p & ((1 << (3 * L2)) - 1));
+  const int px = v & m2, py = (v >> L2) & m2, pz = v >> (2 * L2);
+  float gx[8], avg = 0.f;
+  int64_t ch[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const int lx = 2 * px + (k & 1), ly = 2 * py + ((k >> 1) & 1), lz = 2 * pz + (k >> 2);
+    ch[k] = (s << (3 * L1)) + ((int64_t)((lz << L1) + ly) << L1) + lx;
+    const int64_t b0 = (s << (3 * L0)) + ((int64_t)(((2 * lz) << L0) + 2 * ly) << L0) + 2 * lx;
+    float t = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+      t += g0[b0 + ((int64_t)((q >> 2) << L0) << L0) + ((int64_t)((q >> 1) & 1) << L0) + (q & 1)];
+    gx[k] = t;
+    avg += t;
+  }
+  avg *= 0.125f;
+  const float S = (float)sc[0];
+#pragma unroll
+  for (int k = 0; k < 8; k++) go[ch[k]] = make_float2(S * gx[k], S * avg);
+}
+
+// Coarse loss: d = x1 - avg1(x*) stored in gx1; partial sums of d^2 and avg1^2.
+__global__ void kWnCoarseDiff(const float *__restrict__ x1, const float *__restrict__ xs0, int L1, int64_t n1,
+                              float *__restrict__ dOut, double *__restrict__ part) {
+  double sd = 0.0, sx = 0.0;
+  const int L0 = L1 + 1, m1 = (1 << L1) - 1;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n1; c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = c >> (3 * L1);
+    const int v = (int)(c & ((1 << (3 * L1)) - 1));
+    const int lx = v & m1, ly = (v >> L1) & m1, lz = v >> (2 * L1);
+    const int64_t base = (s << (3 * L0)) + ((int64_t)((2 * lz) << L0) << L0) + ((int64_t)(2 * ly) << L0) + 2 * lx;
+    float t = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      t += xs0[base + ((int64_t)((k >> 2) << L0) << L0) + ((int64_t)((k >> 1) & 1) << L0) + (k & 1)];
+    const float xbar = 0.125f * t;
+    const float d = x1[c] - xbar;
+    dOut[c] = d;
+    sd += (double)d * d;
+    sx += (double)xbar * xbar;
+  }
+  sd = blockSum(sd);
+  sx = blockSum(sx);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = sd;
+    part[2 * blockIdx.x + 1] = sx;
+  }
+}
+__global__ void kSum2(const double *__restrict__ part, int n, double *__restrict__ out) {
+  double s0 = 0.0, s1 = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) { s0 += part[2 * i]; s1 += part[2 * i + 1]; }
+  s0 = blockSum(s0);
+  s1 = blockSum(s1);
+  if (threadIdx.x == 0) { out[0] = s0; out[1] = s1; }
+}
+// head backward from a level-1 gradient gx1 = k * d / den (den = sc[5]):
+// g(o0) = S gx1, g(o1) = S avg2(gx1).  One thread per level-2 parent.
+__global__ void kWnHeadBack1(const float *__restrict__ d, const double *__restrict__ sc, float k, int L1, int64_t n2,
+                             float2 *__restrict__ go) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n2) return;
+  const int L2 = L1 - 1, m2 = (1 << L2) - 1;
+  const int64_t s = p >> (3 * L2);
+  const int v = (int)(p & ((1 << (3 * L2)) - 1));
+  const int px = v & m2, py = (v >> L2) & m2, pz = v >> (2 * L2);
+  const float f = sc[5] > 0 ? (float)(k / sc[5]) : 0.f;
+  float gx[8], avg = 0.f;
+  int64_t ch[8];
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const int lx = 2 * px + (q & 1), ly = 2 * py + ((q >> 1) & 1), lz = 2 * pz + (q >> 2);
+    ch[q] = (s << (3 * L1)) + ((int64_t)((lz << L1) + ly) << L1) + lx;
+    gx[q] = f * d[ch[q]];
+    avg += gx[q];
+  }
+  avg *= 0.125f;
+  const float S = (float)sc[0];
+#pragma unroll
+  for (int q = 0; q < 8; q++) go[ch[q]] = make_float2(S * gx[q], S * avg);
+}
+
+// ---------------------------------------------------------------------------------
+// convolutions (CUDA cores; FP32 accumulation)
+// ---------------------------------------------------------------------------------
+template <int CIN>
+__device__ __forceinline__ void loadIn(const float *__restrict__ a, int64_t j, bool norm, float s0, float s1,
+                                       float *v) {
+  if constexpr (CIN == 2) {
+    const float2 t = reinterpret_cast<const float2 *>(a)[j];
+    v[0] = norm ? t.x * s0 : t.x;
+    v[1] = norm ? t.y * s1 - 1.0f : t.y;
+  } else {
+#pragma unroll
+    for (int i = 0; i < CIN; i += 4) {
+      const float4 t = *reinterpret_cast<const float4 *>(a + j * CIN + i);
+      v[i] = t.x; v[i + 1] = t.y; v[i + 2] = t.z; v[i + 3] = t.w;
+    }
+  }
+}
+
+// y[c] = act(sum_tap W[tap]^T x[c + tap] + bias); NORM: the layer-0 input scaling
+template <int CIN, int COUT, bool RELU, bool NORM>
+__global__ void __launch_bounds__(256) kConvFwd(WnGeom g, const float *__restrict__ x,
+                                                const __nv_bfloat16 *__restrict__ w, const float *__restrict__ bias,
+                                                const double *__restrict__ sc, float *__restrict__ y) {
+  __shared__ float ws[27 * CIN * COUT];
+  __shared__ float bs[COUT];
+  for (int i = threadIdx.x; i < 27 * CIN * COUT; i += blockDim.x) ws[i] = __bfloat162float(w[i]);
+  if (threadIdx.x < COUT) bs[threadIdx.x] = bias[threadIdx.x];
+  __syncthreads();
+  const float s0 = NORM ? (float)sc[1] : 1.f, s1 = NORM ? (float)sc[2] : 1.f;
+  const int64_t n = g.nAct << (3 * g.L);
+  const int m = g.bs - 1;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int s = (int)(c >> (3 * g.L));
+    const int v = (int)(c & ((1 << (3 * g.L)) - 1));
+    const int lx = v & m, ly = (v >> g.L) & m, lz = v >> (2 * g.L);
+    float acc[COUT];
+#pragma unroll
+    for (int o = 0; o < COUT; o++) acc[o] = bs[o];
+    for (int t = 0; t < 27; t++) {
+      const int64_t j = wnNbr(g, s, lx, ly, lz, t % 3 - 1, (t / 3) % 3 - 1, t / 9 - 1);
+      if (j < 0) continue;
+      float xi[CIN];
+      loadIn<CIN>(x, j, NORM, s0, s1, xi);
+      const float *wt = ws + t * CIN * COUT;
+#pragma unroll
+      for (int i = 0; i < CIN; i++)
+#pragma unroll
+        for (int o = 0; o < COUT; o++) acc[o] = fmaf(xi[i], wt[i * COUT + o], acc[o]);
+    }
+#pragma unroll
+    for (int o = 0; o < COUT; o++) y[c * COUT + o] = RELU ? fmaxf(acc[o], 0.f) : acc[o];
+  }
+}
+
+// gx[c][i] = sum_tap sum_o W[tap][i][o] * gpre[c - tap][o], gpre = gy * (y > 0) when
+// the layer has a ReLU.  Written for the layers above the input only.
+template <int CIN, int COUT, bool RELU>
+__global__ void __launch_bounds__(256) kConvBwdData(WnGeom g, const float *__restrict__ gy,
+                                                    const float *__restrict__ y, const __nv_bfloat16 *__restrict__ w,
+                                                    float *__restrict__ gx) {
+  __shared__ float ws[27 * CIN * COUT];
+  for (int i = threadIdx.x; i < 27 * CIN * COUT; i += blockDim.x) ws[i] = __bfloat162float(w[i]);
+  __syncthreads();
+  const int64_t n = g.nAct << (3 * g.L);
+  const int m = g.bs - 1;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int s = (int)(c >> (3 * g.L));
+    const int v = (int)(c & ((1 << (3 * g.L)) - 1));
+    const int lx = v & m, ly = (v >> g.L) & m, lz = v >> (2 * g.L);
+    float acc[CIN];
+#pragma unroll
+    for (int i = 0; i < CIN; i++) acc[i] = 0.f;
+    for (int t = 0; t < 27; t++) {
+      const int64_t j = wnNbr(g, s, lx, ly, lz, -(t % 3 - 1), -((t / 3) % 3 - 1), -(t / 9 - 1));
+      if (j < 0) continue;
+      float gp[COUT];
+#pragma unroll
+      for (int o = 0; o < COUT; o++) {
+        const float gv = gy[j * COUT + o];
+        gp[o] = (!RELU || y[j * COUT + o] > 0.f) ? gv : 0.f;
+      }
+      const float *wt = ws + t * CIN * COUT;
+#pragma unroll
+      for (int i = 0; i < CIN; i++)
+#pragma unroll
+        for (int o = 0; o < COUT; o++) acc[i] = fmaf(wt[i * COUT + o], gp[o], acc[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < CIN; i++) gx[c * CIN + i] = acc[i];
+  }
+}
+
+// gw[tap][i][o] += sum_c x[c + tap][i] * gpre[c][o]; gb[o] += sum_c gpre[c][o].
+// A CTA takes kWChunk cells: their gpre in shared memory, one thread per (tap, i).
+constexpr int kWChunk = 256;
+template <int CIN, int COUT, bool RELU, bool NORM>
+__global__ void __launch_bounds__(256) kConvBwdWeight(WnGeom g, const float *__restrict__ x,
+                                                      const float *__restrict__ gy, const float *__restrict__ y,
+                                                      const double *__restrict__ sc, float *__restrict__ gw,
+                                                      float *__restrict__ gb) {
+  __shared__ float gs[kWChunk * COUT];
+  const int64_t n = g.nAct << (3 * g.L);
+  const int64_t c0 = (int64_t)blockIdx.x * kWChunk;
+  const int nc = (int)min((int64_t)kWChunk, n - c0);
+  for (int k = threadIdx.x; k < kWChunk * COUT; k += blockDim.x) {
+    const int cc = k / COUT, o = k % COUT;
+    float v = 0.f;
+    if (cc < nc) {
+      const int64_t c = c0 + cc;
+      v = gy[c * COUT + o];
+      if (RELU && !(y[c * COUT + o] > 0.f)) v = 0.f;
+    }
+    gs[k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < COUT) {
+    float t = 0.f;
+    for (int cc = 0; cc < nc; cc++) t += gs[cc * COUT + threadIdx.x];
+    atomicAdd(gb + threadIdx.x, t);
+  }
+  const float s0 = NORM ? (float)sc[1] : 1.f, s1 = NORM ? (float)sc[2] : 1.f;
+  const int m = g.bs - 1;
+  for (int ti = threadIdx.x; ti < 27 * CIN; ti += blockDim.x) {
+    const int t = ti / CIN, i = ti % CIN;
+    const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
+    float acc[COUT];
+#pragma unroll
+    for (int o = 0; o < COUT; o++) acc[o] = 0.f;
+    for (int cc = 0; cc < nc; cc++) {
+      const int64_t c = c0 + cc;
+      const int s = (int)(c >> (3 * g.L));
+      const int v = (int)(c & ((1 << (3 * g.L)) - 1));
+      const int64_t j = wnNbr(g, s, v & m, (v >> g.L) & m, v >> (2 * g.L), dx, dy, dz);
+      if (j < 0) continue;
+      float xv;
+      if constexpr (CIN == 2) {
+        const float2 tv = reinterpret_cast<const float2 *>(x)[j];
+        xv = i == 0 ? (NORM ? tv.x * s0 : tv.x) : (NORM ? tv.y * s1 - 1.0f : tv.y);
+      } else {
+        xv = x[j * CIN + i];
+      }
+#pragma unroll
+      for (int o = 0; o < COUT; o++) acc[o] = fmaf(xv, gs[cc * COUT + o], acc[o]);
+    }
+#pragma unroll
+    for (int o = 0; o < COUT; o++) atomicAdd(gw + (t * CIN + i) * COUT + o, acc[o]);
+  }
+}
+
+// Adam on FP32 masters; the BF16 copy is refreshed
+__global__ void kAdam(float *__restrict__ p, const float *__restrict__ gr, float *__restrict__ m, float *__restrict__ v,
+                      __nv_bfloat16 *__restrict__ pq, int n, float lr, float b1t, float b2t) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float g = gr[i];
+  const float mi = 0.9f * m[i] + 0.1f * g, vi = 0.999f * v[i] + 0.001f * g * g;
+  m[i] = mi;
+  v[i] = vi;
+  const float mh = mi / (1.0f - b1t), vh = vi / (1.0f - b2t);
+  const float np = p[i] - lr * mh / (sqrtf(vh) + 1e-8f);
+  p[i] = np;
+  if (pq) pq[i] = __float2bfloat16_rn(np);
+}
+__global__ void kToBf16(const float *__restrict__ a, __nv_bfloat16 *__restrict__ b, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = __float2bfloat16_rn(a[i]);
+}
+__global__ void kSub(const float *__restrict__ a, const float *__restrict__ b, float *__restrict__ c, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    c[i] = a[i] - b[i];
+}
+__global__ void kScaleInPlace(float *__restrict__ a, const double *__restrict__ num, const double *__restrict__ den,
+                              float k, int64_t n) {
+  const float f = den[0] > 0 ? (float)(k / den[0]) : 0.f;
+  (void)num;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    a[i] *= f;
+}
+
+}  // namespace msbg
+
+using namespace msbg;
+
+// =====================================================================================
+// host side
+// =====================================================================================
+namespace msbg {
+
+void warmNetFree(WarmNetState *w) {
+  if (!w) return;
+  void *ptrs[] = {w->nbr27, w->x1, w->gx1, w->t0a, w->t0b, w->dScal, w->dPart, w->gact[0], w->gact[1]};
+  for (void *p : ptrs) if (p) cudaFree(p);
+  for (int l = 0; l < kWnLayers; l++) {
+    void *q[] = {w->w32[l], w->bias[l], w->wq[l], w->gw[l], w->gb[l], w->mw[l], w->vw[l], w->mb[l], w->vb[l]};
+    for (void *p : q) if (p) cudaFree(p);
+  }
+  for (int l = 0; l <= kWnLayers; l++) if (w->act[l]) cudaFree(w->act[l]);
+  if (w->hScal) cudaFreeHost(w->hScal);
+  delete w;
+}
+
+static unsigned wnGrid(int64_t n) {
+  int64_t g = (n + 255) / 256;
+  if (g > 152 * 8) g = 152 * 8;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+// Level-1 buffers for the current layout (the weights survive a layout change).
+static int wnEnsure(msbg_gpu_ctx *ctx) {
+  int rc = poissonEnsure(ctx);
+  if (rc) return rc;
+  PoissonState *ps = ctx->poisson;
+  if (ps->levels.size() < 3 || !ps->levels[1].sameSet || !ps->levels[2].sameSet || ps->levels[1].bs < 2)
+    return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "warm start needs level-0 blocks of edge >= 4");
+  if (!ctx->warmnet) {
+    ctx->warmnet = new WarmNetState();
+    WarmNetState *w = ctx->warmnet;
+    for (int l = 0; l < kWnLayers; l++) {
+      const int nw = wnWeights(l), nb = kWnCh[l + 1];
+      MSBG_CUDA(ctx, cudaMalloc(&w->w32[l], nw * 4));
+      MSBG_CUDA(ctx, cudaMalloc(&w->wq[l], nw * 2));
+      MSBG_CUDA(ctx, cudaMalloc(&w->bias[l], nb * 4));
+      for (float **q : {&w->gw[l], &w->mw[l], &w->vw[l]}) {
+        MSBG_CUDA(ctx, cudaMalloc(q, nw * 4));
+        MSBG_CUDA(ctx, cudaMemset(*q, 0, nw * 4));
+      }
+      for (float **q : {&w->gb[l], &w->mb[l], &w->vb[l]}) {
+        MSBG_CUDA(ctx, cudaMalloc(q, nb * 4));
+        MSBG_CUDA(ctx, cudaMemset(*q, 0, nb * 4));
+      }
+    }
+    MSBG_CUDA(ctx, cudaMalloc(&w->dScal, 16 * 8));
+    MSBG_CUDA(ctx, cudaMallocHost((void **)&w->hScal, 16 * 8));
+    w->nPart = 152 * 8;
+    MSBG_CUDA(ctx, cudaMalloc(&w->dPart, (size_t)w->nPart * 2 * 8));
+  }
+  WarmNetState *w = ctx->warmnet;
+  if (w->layoutStamp == ctx->layoutStamp) return MSBG_GPU_OK;
+  void *old[] = {w->nbr27, w->x1, w->gx1, w->t0a, w->t0b, w->gact[0], w->gact[1]};
+  for (void *p : old) if (p) cudaFree(p);
+  for (int l = 0; l <= kWnLayers; l++) { if (w->act[l]) cudaFree(w->act[l]); w->act[l] = nullptr; }
+  w->nbr27 = nullptr; w->x1 = w->gx1 = w->t0a = w->t0b = w->gact[0] = w->gact[1] = nullptr;
+  const MgLevel &L0 = ps->levels[0], &L1 = ps->levels[1], &L2 = ps->levels[2];
+  w->n1 = L1.nCell;
+  w->n2 = L2.nCell;
+  const int64_t na = L0.nAct;
+  MSBG_CUDA(ctx, cudaMalloc(&w->nbr27, (size_t)(na > 0 ? na : 1) * 27 * 4));
+  if (na > 0) {
+    MSBG_LAUNCH(ctx, kNbr27, gridFor(na * 27, 256), 256, 0, L0.active, na, L0.nbx, L0.nby, L0.nbz, L0.slot,
+                w->nbr27);
+  }
+  const size_t n1 = (size_t)(w->n1 > 0 ? w->n1 : 1), n0 = (size_t)(L0.nCell > 0 ? L0.nCell : 1);
+  for (int l = 0; l <= kWnLayers; l++) MSBG_CUDA(ctx, cudaMalloc(&w->act[l], n1 * kWnCh[l] * 4));
+  MSBG_CUDA(ctx, cudaMalloc(&w->gact[0], n1 * 16 * 4));
+  MSBG_CUDA(ctx, cudaMalloc(&w->gact[1], n1 * 16 * 4));
+  MSBG_CUDA(ctx, cudaMalloc(&w->x1, n1 * 4));
+  MSBG_CUDA(ctx, cudaMalloc(&w->gx1, n1 * 4));
+  MSBG_CUDA(ctx, cudaMalloc(&w->t0a, n0 * 4));
+  MSBG_CUDA(ctx, cudaMalloc(&w->t0b, n0 * 4));
+  w->layoutStamp = ctx->layoutStamp;
+  return MSBG_GPU_OK;
+}
+
+static WnGeom wnGeom(const PoissonState *ps, const WarmNetState *w) {
+  const MgLevel &L1 = ps->levels[1];
+  WnGeom g;
+  g.bs = L1.bs; g.L = L1.log2bs; g.nAct = L1.nAct; g.nbr27 = w->nbr27;
+  return g;
+}
+
+// forward pass from the level-0 right-hand side b0; x0 (level 0) optional
+static int wnForward(msbg_gpu_ctx *ctx, const float *b0, float *x0) {
+  PoissonState *ps = ctx->poisson;
+  WarmNetState *w = ctx->warmnet;
+  const WnGeom g = wnGeom(ps, w);
+  const int L1 = g.L;
+  MSBG_LAUNCH(ctx, kWnInputs, (unsigned)w->nPart, kRedThreads, 0, b0, (const float *)ps->f32.d[1], L1, w->n1,
+              (float2 *)w->act[0], w->dPart);
+  MSBG_LAUNCH(ctx, kWnScales, 1, kRedThreads, 0, w->dPart, w->nPart, w->n1, w->dScal);
+  const unsigned gr = wnGrid(w->n1);
+  MSBG_LAUNCH(ctx, (kConvFwd<2, 16, true, true>), gr, 256, 0, g, w->act[0], w->wq[0], w->bias[0], w->dScal, w->act[1]);
+  MSBG_LAUNCH(ctx, (kConvFwd<16, 16, true, false>), gr, 256, 0, g, w->act[1], w->wq[1], w->bias[1], w->dScal,
+              w->act[2]);
+  MSBG_LAUNCH(ctx, (kConvFwd<16, 16, true, false>), gr, 256, 0, g, w->act[2], w->wq[2], w->bias[2], w->dScal,
+              w->act[3]);
+  MSBG_LAUNCH(ctx, (kConvFwd<16, 2, false, false>), gr, 256, 0, g, w->act[3], w->wq[3], w->bias[3], w->dScal,
+              w->act[4]);
+  MSBG_LAUNCH(ctx, kWnHead, gridFor(w->n2, 256), 256, 0, (const float2 *)w->act[4], w->dScal, L1, w->n2, w->x1, x0);
+  return MSBG_GPU_OK;
+}
+
+// loss into hScal[4] (and dScal[4]); gradients into gw/gb (zeroed first)
+static int wnLossGrad(msbg_gpu_ctx *ctx, const float *b0, const float *xs0) {
+  PoissonState *ps = ctx->poisson;
+  WarmNetState *w = ctx->warmnet;
+  const WnGeom g = wnGeom(ps, w);
+  const int64_t n0 = ps->levels[0].nCell;
+  int rc;
+  if (w->lossMode == 0) {  // coarse: loss and its gradient on level 1
+    if ((rc = wnForward(ctx, b0, nullptr))) return rc;
+    MSBG_LAUNCH(ctx, kWnCoarseDiff, (unsigned)w->nPart, kRedThreads, 0, w->x1, xs0, g.L, w->n1, w->gx1, w->dPart);
+    MSBG_LAUNCH(ctx, kSum2, 1, kRedThreads, 0, w->dPart, w->nPart, w->dScal + 4);
+    MSBG_LAUNCH(ctx, kWnHeadBack1, gridFor(w->n2, 256), 256, 0, w->gx1, w->dScal, 2.0f, g.L, w->n2,
+                (float2 *)w->gact[0]);
+  } else {
+  if ((rc = wnForward(ctx, b0, w->t0a))) return rc;  // t0a = x0
+  MSBG_LAUNCH(ctx, kSub, wnGrid(n0), 256, 0, w->t0a, xs0, w->t0a, n0);  // t0a = x0 - x*
+  if ((rc = blkApply<float>(ctx, ps, 0, ps->f32, w->t0a, nullptr, w->t0b, 0, nullptr, nullptr, nullptr)))
+    return rc;  // t0b = e = A (x0 - x*)
+  if ((rc = blkDot<float>(ctx, ps, w->t0b, w->t0b, n0, w->dScal + 4))) return rc;   // sum e^2
+  if ((rc = blkDot<float>(ctx, ps, b0, b0, n0, w->dScal + 5))) return rc;           // ||b||^2
+  if ((rc = blkApply<float>(ctx, ps, 0, ps->f32, w->t0b, nullptr, w->t0a, 0, nullptr, nullptr, nullptr)))
+    return rc;  // t0a = A e
+  MSBG_LAUNCH(ctx, kScaleInPlace, wnGrid(n0), 256, 0, w->t0a, w->dScal + 4, w->dScal + 5, 2.0f, n0);  // g0
+  MSBG_LAUNCH(ctx, kWnHeadBack, gridFor(w->n2, 256), 256, 0, w->t0a, w->dScal, g.L, w->n2, (float2 *)w->gact[0]);
+  }
+  for (int l = 0; l < kWnLayers; l++) {
+    MSBG_CUDA(ctx, cudaMemsetAsync(w->gw[l], 0, wnWeights(l) * 4, ctx->stream));
+    MSBG_CUDA(ctx, cudaMemsetAsync(w->gb[l], 0, kWnCh[l + 1] * 4, ctx->stream));
+  }
+  const unsigned gr = wnGrid(w->n1);
+  const unsigned gwc = (unsigned)((w->n1 + kWChunk - 1) / kWChunk);
+  // layer 3 (no ReLU): upstream gact[0] [n1][2]
+  MSBG_LAUNCH(ctx, (kConvBwdWeight<16, 2, false, false>), gwc, 256, 0, g, w->act[3], w->gact[0], w->act[4], w->dScal,
+              w->gw[3], w->gb[3]);
+  MSBG_LAUNCH(ctx, (kConvBwdData<16, 2, false>), gr, 256, 0, g, w->gact[0], w->act[4], w->wq[3], w->gact[1]);
+  // layer 2: upstream gact[1] [n1][16], ReLU on act[3]
+  MSBG_LAUNCH(ctx, (kConvBwdWeight<16, 16, true, false>), gwc, 256, 0, g, w->act[2], w->gact[1], w->act[3],
+              w->dScal, w->gw[2], w->gb[2]);
+  MSBG_LAUNCH(ctx, (kConvBwdData<16, 16, true>), gr, 256, 0, g, w->gact[1], w->act[3], w->wq[2], w->gact[0]);
+  // layer 1
+  MSBG_LAUNCH(ctx, (kConvBwdWeight<16, 16, true, false>), gwc, 256, 0, g, w->act[1], w->gact[0], w->act[2],
+              w->dScal, w->gw[1], w->gb[1]);
+  MSBG_LAUNCH(ctx, (kConvBwdData<16, 16, true>), gr, 256, 0, g, w->gact[0], w->act[2], w->wq[1], w->gact[1]);
+  // layer 0 (input scaling applied on load)
+  MSBG_LAUNCH(ctx, (kConvBwdWeight<2, 16, true, true>), gwc, 256, 0, g, w->act[0], w->gact[1], w->act[1], w->dScal,
+              w->gw[0], w->gb[0]);
+  MSBG_CUDA(ctx, cudaMemcpyAsync(w->hScal + 4, w->dScal + 4, 2 * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return MSBG_GPU_OK;
+}
+
+}  // namespace msbg
+
+// ---- ABI --------------------------------------------------------------------------------
+static int wnChanF32(msbg_gpu_ctx *ctx, int chan, float **p) {
+  if (chan < 0 || chan >= kMaxChannels || !ctx->ch[chan].exists)
+    return fail(ctx, MSBG_GPU_ERR_ARG, "channel %d does not exist", chan);
+  if (ctx->ch[chan].storage != MSBG_GPU_F32) return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "channel %d is not FP32", chan);
+  *p = (float *)ctx->ch[chan].d;
+  return MSBG_GPU_OK;
+}
+
+static int wnReady(msbg_gpu_ctx *ctx) {
+  if (!ctx->layoutValid) return fail(ctx, MSBG_GPU_ERR_STATE, "no block layout");
+  int rc = poissonEnsure(ctx);
+  if (rc) return rc;
+  if (!ctx->poisson->coeffsValid) return fail(ctx, MSBG_GPU_ERR_STATE, "no Poisson coefficients set");
+  return wnEnsure(ctx);
+}
+
+extern "C" int msbg_gpu_warmnet_param_count(int *nWeights, int *nBiases) {
+  if (!nWeights || !nBiases) return MSBG_GPU_ERR_ARG;
+  int a = 0, b = 0;
+  for (int l = 0; l < kWnLayers; l++) { a += wnWeights(l); b += kWnCh[l + 1]; }
+  *nWeights = a;
+  *nBiases = b;
+  return MSBG_GPU_OK;
+}
+
+extern "C" int msbg_gpu_warmnet_set_weights(msbg_gpu_ctx *ctx, const float *hW, const float *hB, int resetOptimizer) {
+  if (!ctx || !hW || !hB) return MSBG_GPU_ERR_ARG;
+  int rc = wnReady(ctx);
+  if (rc) return rc;
+  WarmNetState *w = ctx->warmnet;
+  int ow = 0, ob = 0;
+  for (int l = 0; l < kWnLayers; l++) {
+    const int nw = wnWeights(l), nb = kWnCh[l + 1];
+    MSBG_CUDA(ctx, cudaMemcpyAsync(w->w32[l], hW + ow, nw * 4, cudaMemcpyHostToDevice, ctx->stream));
+    MSBG_CUDA(ctx, cudaMemcpyAsync(w->bias[l], hB + ob, nb * 4, cudaMemcpyHostToDevice, ctx->stream));
+    MSBG_LAUNCH(ctx, kToBf16, (nw + 255) / 256, 256, 0, w->w32[l], w->wq[l], nw);
+    if (resetOptimizer) {
+      for (float *q : {w->mw[l], w->vw[l]}) MSBG_CUDA(ctx, cudaMemsetAsync(q, 0, nw * 4, ctx->stream));
+      for (float *q : {w->mb[l], w->vb[l]}) MSBG_CUDA(ctx, cudaMemsetAsync(q, 0, nb * 4, ctx->stream));
+    }
+    ow += nw;
+    ob += nb;
+  }
+  if (resetOptimizer) w->step = 0;
+  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  w->weightsSet = true;
+  return MSBG_GPU_OK;
+}
+
+extern "C" int msbg_gpu_warmnet_get_weights(msbg_gpu_ctx *ctx, float *hW, float *hB) {
+  if (!ctx || !hW || !hB) return MSBG_GPU_ERR_ARG;
+  if (!ctx->warmnet || !ctx->warmnet->weightsSet) return fail(ctx, MSBG_GPU_ERR_STATE, "warm-start weights not set");
+  WarmNetState *w = ctx->warmnet;
+  int ow = 0, ob = 0;
+  for (int l = 0; l < kWnLayers; l++) {
+    const int nw = wnWeights(l), nb = kWnCh[l + 1];
+    MSBG_CUDA(ctx, cudaMemcpyAsync(hW + ow, w->w32[l], nw * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    MSBG_CUDA(ctx, cudaMemcpyAsync(hB + ob, w->bias[l], nb * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    ow += nw;
+    ob += nb;
+  }
+  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return MSBG_GPU_OK;
+}
+
+extern "C" int msbg_gpu_warmnet_set_loss(msbg_gpu_ctx *ctx, int lossMode) {
+  if (!ctx || lossMode < 0 || lossMode > 1) return MSBG_GPU_ERR_ARG;
+  int rc = wnReady(ctx);
+  if (rc) return rc;
+  ctx->warmnet->lossMode = lossMode;
+  return MSBG_GPU_OK;
+}
+
+extern "C" int msbg_gpu_warmnet_predict(msbg_gpu_ctx *ctx, int chanB, int chanX0) {
+  if (!ctx) return MSBG_GPU_ERR_ARG;
+  int rc = wnReady(ctx);
+  if (rc) return rc;
+  if (!ctx->warmnet->weightsSet) return fail(ctx, MSBG_GPU_ERR_STATE, "warm-start weights not set");
+  float *b, *x;
+  if ((rc = wnChanF32(ctx, chanB, &b)) || (rc = wnChanF32(ctx, chanX0, &x))) return rc;
+  return wnForward(ctx, b, x);
+}
+
+static int wnGradsCore(msbg_gpu_ctx *ctx, const float *b, const float *xs, double *loss) {
+  int rc = wnReady(ctx);
+  if (rc) return rc;
+  if (!ctx->warmnet->weightsSet) return fail(ctx, MSBG_GPU_ERR_STATE, "warm-start weights not set");
+  if ((rc = wnLossGrad(ctx, b, xs))) return rc;
+  WarmNetState *w = ctx->warmnet;
+  const double bb = w->hScal[5];
+  *loss = bb > 0 ? w->hScal[4] / bb : 0.0;
+  return MSBG_GPU_OK;
+}
+
+extern "C" int msbg_gpu_warmnet_loss_grad(msbg_gpu_ctx *ctx, int chanB, int chanXstar, double *loss, float *hGW,
+                                          float *hGB) {
+  if (!ctx || !loss) return MSBG_GPU_ERR_ARG;
+  float *b, *xs;
+  int rc;
+  if ((rc = wnChanF32(ctx, chanB, &b)) || (rc = wnChanF32(ctx, chanXstar, &xs))) return rc;
+  if ((rc = wnGradsCore(ctx, b, xs, loss))) return rc;
+  WarmNetState *w = ctx->warmnet;
+  int ow = 0, ob = 0;
+  for (int l = 0; l < kWnLayers; l++) {
+    const int nw = wnWeights(l), nb = kWnCh[l + 1];
+    if (hGW) MSBG_CUDA(ctx, cudaMemcpyAsync(hGW + ow, w->gw[l], nw * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (hGB) MSBG_CUDA(ctx, cudaMemcpyAsync(hGB + ob, w->gb[l], nb * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    ow += nw;
+    ob += nb;
+  }
+  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return MSBG_GPU_OK;
+}
+
+extern "C" int msbg_gpu_warmnet_train_step(msbg_gpu_ctx *ctx, const float *dB, const float *dXstar, float lr,
+                                           double *loss) {
+  if (!ctx || !dB || !dXstar || !loss || !(lr > 0)) return MSBG_GPU_ERR_ARG;
+  int rc = wnGradsCore(ctx, dB, dXstar, loss);
+  if (rc) return rc;
+  WarmNetState *w = ctx->warmnet;
+  w->step++;
+  const float b1t = powf(0.9f, (float)w->step), b2t = powf(0.999f, (float)w->step);
+  for (int l = 0; l < kWnLayers; l++) {
+    const int nw = wnWeights(l), nb = kWnCh[l + 1];
+    MSBG_LAUNCH(ctx, kAdam, (nw + 255) / 256, 256, 0, w->w32[l], w->gw[l], w->mw[l], w->vw[l], w->wq[l], nw, lr, b1t,
+                b2t);
+    MSBG_LAUNCH(ctx, kAdam, 1, 256, 0, w->bias[l], w->gb[l], w->mb[l], w->vb[l], (__nv_bfloat16 *)nullptr, nb, lr,
+                b1t, b2t);
+  }
+  return MSBG_GPU_OK;
+}

@@ -70,6 +70,14 @@ SIGNATURES = {
     "msbg_gpu_device_free": (I, [P]),
     "msbg_gpu_copy_h2d": (I, [P, P, P, SZ]),
     "msbg_gpu_copy_d2h": (I, [P, P, P, SZ]),
+    "msbg_gpu_copy_d2d": (I, [P, P, P, SZ]),
+    "msbg_gpu_warmnet_param_count": (I, [C.POINTER(I), C.POINTER(I)]),
+    "msbg_gpu_warmnet_set_weights": (I, [P, P, P, I]),
+    "msbg_gpu_warmnet_get_weights": (I, [P, P, P]),
+    "msbg_gpu_warmnet_predict": (I, [P, I, I]),
+    "msbg_gpu_warmnet_set_loss": (I, [P, I]),
+    "msbg_gpu_warmnet_loss_grad": (I, [P, I, I, C.POINTER(D), P, P]),
+    "msbg_gpu_warmnet_train_step": (I, [P, P, P, F, C.POINTER(D)]),
     "msbg_gpu_assign_slots_noalloc": (I, [P, I64, P, P, P, P]),
     "msbg_gpu_poisson_set_coefficients": (I, [P, I, I, I, I]),
     "msbg_gpu_poisson_procedural_coefficients": (I, [P, C.c_uint32, I, I, I, I]),
@@ -132,6 +140,13 @@ class DeviceBuffer:
     """Raw device allocation owned by Python (freed on close/GC)."""
     ptr: int
     nbytes: int
+
+    @classmethod
+    def alloc(cls, nbytes: int) -> "DeviceBuffer":
+        p = C.c_void_p()
+        if load_library().msbg_gpu_device_alloc(C.byref(p), max(int(nbytes), 1)) != OK:
+            raise MsbgGpuError(ERR_NOMEM, "device alloc")
+        return cls(p.value, int(nbytes))
 
     def free(self):
         if self.ptr:
@@ -354,8 +369,61 @@ class MultiresSparseGrid:
                                                       max_inner, C.byref(o), C.byref(i), C.byref(rel)))
         return o.value, i.value, rel.value
 
-    def poisson_set_params(self, pre: int = 2, post: int = 2, tile_iters: int = 1, coarsest_iter: int = 0):
+    def poisson_set_params(self, pre: int = 2, post: int = 2, tile_iters: int = 3, coarsest_iter: int = 0):
         self._check(self.L.msbg_gpu_poisson_set_params(self.h, pre, post, tile_iters, coarsest_iter))
+
+    # ---- learned warm start ----------------------------------------------------------------
+    WARMNET_CH = (2, 16, 16, 16, 2)
+
+    @classmethod
+    def _wn_split(cls, flat_w, flat_b):
+        W, B, ow, ob = [], [], 0, 0
+        for l in range(4):
+            cin, cout = cls.WARMNET_CH[l], cls.WARMNET_CH[l + 1]
+            n = 27 * cin * cout
+            W.append(flat_w[ow:ow + n].reshape(27, cin, cout).copy())
+            B.append(flat_b[ob:ob + cout].copy())
+            ow += n
+            ob += cout
+        return W, B
+
+    def warmnet_set(self, weights, biases, reset_optimizer: bool = True):
+        w = np.ascontiguousarray(np.concatenate([np.asarray(x, np.float32).ravel() for x in weights]))
+        b = np.ascontiguousarray(np.concatenate([np.asarray(x, np.float32).ravel() for x in biases]))
+        self._check(self.L.msbg_gpu_warmnet_set_weights(self.h, _ptr(w), _ptr(b), int(reset_optimizer)))
+
+    def warmnet_get(self):
+        nw, nb = C.c_int(), C.c_int()
+        self.L.msbg_gpu_warmnet_param_count(C.byref(nw), C.byref(nb))
+        w = np.zeros(nw.value, np.float32)
+        b = np.zeros(nb.value, np.float32)
+        self._check(self.L.msbg_gpu_warmnet_get_weights(self.h, _ptr(w), _ptr(b)))
+        return self._wn_split(w, b)
+
+    def warmnet_set_loss(self, mode: str):
+        self._check(self.L.msbg_gpu_warmnet_set_loss(self.h, {"coarse": 0, "residual": 1}[mode]))
+
+    def warmnet_predict(self, chanB: int, chanX0: int):
+        self._check(self.L.msbg_gpu_warmnet_predict(self.h, chanB, chanX0))
+
+    def warmnet_loss_grad(self, chanB: int, chanXstar: int):
+        nw, nb = C.c_int(), C.c_int()
+        self.L.msbg_gpu_warmnet_param_count(C.byref(nw), C.byref(nb))
+        gw = np.zeros(nw.value, np.float32)
+        gb = np.zeros(nb.value, np.float32)
+        loss = C.c_double()
+        self._check(self.L.msbg_gpu_warmnet_loss_grad(self.h, chanB, chanXstar, C.byref(loss), _ptr(gw), _ptr(gb)))
+        W, B = self._wn_split(gw, gb)
+        return loss.value, W, B
+
+    def warmnet_train_step(self, dB: int, dXstar: int, lr: float) -> float:
+        loss = C.c_double()
+        self._check(self.L.msbg_gpu_warmnet_train_step(self.h, C.c_void_p(int(dB)), C.c_void_p(int(dXstar)), lr,
+                                                       C.byref(loss)))
+        return loss.value
+
+    def copy_d2d(self, dst: int, src: int, nbytes: int):
+        self._check(self.L.msbg_gpu_copy_d2d(self.h, C.c_void_p(int(dst)), C.c_void_p(int(src)), int(nbytes)))
 
     def mg_info(self):
         n = C.c_int()

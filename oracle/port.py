@@ -244,7 +244,7 @@ def active_mask(bids: np.ndarray, nb, bs: int) -> np.ndarray:
 # before / after the coarse correction, in-tile red-black sweeps per pass, the
 # coarsest level's red-black sweeps (0 = exact Cholesky solve), and the cell
 # count at which coarsening stops.
-MG_PRE, MG_POST, MG_TILE_ITERS, MG_COARSEST_ITER, MG_COARSEST_CELLS = 2, 2, 1, 0, 512
+MG_PRE, MG_POST, MG_TILE_ITERS, MG_COARSEST_ITER, MG_COARSEST_CELLS = 2, 2, 3, 0, 512
 
 
 class PoissonProblem:

@@ -1,0 +1,127 @@
+"""The learned warm start on the GPU against its CPU restatement (oracle/warmnet.py):
+forward output, loss and gradients of the hand-written kernels on a small block
+layout; a short training run lowers the loss; the trained start lowers the
+solve's initial residual and iteration count."""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from msbg_gb300 import workloads as W
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+import warmnet as WN  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+CH_X, CH_B, CH_XS = 1, 2, 3
+
+
+def _sum8(a):
+    nz, ny, nx = a.shape
+    return a.reshape(nz // 2, 2, ny // 2, 2, nx // 2, 2).sum(axis=(1, 3, 5))
+
+
+def _level1_diag(prob):
+    """Diagonal of the level-1 operator P^T A P / 2 (all children active)."""
+    odd = np.zeros(prob.d.shape)
+    cx = prob.cx.copy(); cx[..., 0::2] = 0
+    cy = prob.cy.copy(); cy[:, 0::2, :] = 0
+    cz = prob.cz.copy(); cz[0::2] = 0
+    del odd
+    return 0.5 * (_sum8(prob.d) - 2.0 * (_sum8(cx) + _sum8(cy) + _sum8(cz)))
+
+
+@pytest.fixture(scope="module")
+def setup(gpulib, port):
+    G, P = gpulib, port
+    res, bs = 128, 16
+    pts = W.sphere_cloud(res, 6, 3000, seed=W.workload_seed(4, 1))
+    g = G.MultiresSparseGrid(res, res, res, bs, 3, G.F32)
+    d = g.to_device(pts)
+    g.mark_points(d, len(pts), 4.0)
+    g.levels_from_marks()
+    g.regularizeRefinementMap()
+    g.setRefinementMap(0.0)
+    d.free()
+    for ch in (CH_X, CH_B, CH_XS):
+        g.channel_create(ch, G.F32)
+    g.poisson_procedural_coefficients(4242)
+    bids = g.active_blocks().astype(np.int64)
+    prob = P.PoissonProblem(bids, (g.nbx, g.nby, g.nbz), bs, seed=4242)
+    yield G, P, g, prob
+    g.close()
+
+
+def _rand(prob, rng):
+    return np.where(prob.act > 0, rng.standard_normal(prob.act.shape), 0.0)
+
+
+@pytest.mark.parametrize("loss", ["coarse", "residual"])
+def test_forward_loss_and_gradients_match_restatement(setup, loss):
+    G, P, g, prob = setup
+    rng = np.random.default_rng(11)
+    b = _rand(prob, rng).astype(np.float32)
+    xs = (_rand(prob, rng) * 0.2).astype(np.float32)
+    g.upload_payload(prob.payload(b), CH_B)
+    g.upload_payload(prob.payload(xs), CH_XS)
+    net = WN.WarmNet.init(123)
+    # non-zero biases so every term of the gradient is exercised
+    net.c = [np.linspace(-0.05, 0.05, c).astype(np.float32) for c in WN.CH[1:]]
+    g.warmnet_set(net.W, net.c)
+    g.warmnet_set_loss(loss)
+
+    mask0 = (prob.act > 0).astype(np.float64)
+    d1 = _level1_diag(prob)
+    L, gW, gc, x0 = WN.loss_and_grads(net, b.astype(np.float64), xs.astype(np.float64), mask0,
+                                      prob.apply, d1, loss=loss)
+    g.warmnet_predict(CH_B, CH_X)
+    x0_gpu = prob.dense(g.payload(CH_X))
+    assert rel_l2(x0_gpu, x0) < 2e-4
+    loss, gW_gpu, gc_gpu = g.warmnet_loss_grad(CH_B, CH_XS)
+    assert abs(loss - L) <= 2e-4 * L
+    for l in range(4):
+        assert rel_l2(gW_gpu[l], gW[l]) < 2e-3, l
+        assert rel_l2(gc_gpu[l], gc[l]) < 2e-3, l
+
+
+def test_training_lowers_loss_and_initial_residual(setup):
+    G, P, g, prob = setup
+    rng = np.random.default_rng(12)
+    net = WN.WarmNet.init(7)
+    g.warmnet_set(net.W, net.c)
+    g.warmnet_set_loss("coarse")
+    n0 = len(prob.bids) * prob.bs ** 3
+    pairs = []
+    for k in range(6):  # (b, x*) pairs from the plain solver
+        b = _rand(prob, rng).astype(np.float32)
+        g.upload_payload(prob.payload(b), CH_B)
+        g.fill(0.0, CH_X)
+        g.mgpcg_solve(CH_X, CH_B, tol=1e-6, max_iter=100)
+        pb, px = G.DeviceBuffer.alloc(n0 * 4), G.DeviceBuffer.alloc(n0 * 4)
+        g.copy_d2d(pb.ptr, g.payload_ptr(CH_B), n0 * 4)
+        g.copy_d2d(px.ptr, g.payload_ptr(CH_X), n0 * 4)
+        pairs.append((pb, px, b))
+    losses = []
+    for it in range(120):
+        pb, px, _ = pairs[it % 5]
+        losses.append(g.warmnet_train_step(pb.ptr, px.ptr, 2e-3))
+    assert np.mean(losses[-10:]) < 0.5 * np.mean(losses[:5])
+    # held-out pair: the trained start has a lower initial residual than X = 0
+    _, _, b = pairs[5]
+    g.upload_payload(prob.payload(b), CH_B)
+    g.warmnet_predict(CH_B, CH_X)
+    x0 = prob.dense(g.payload(CH_X))
+    assert np.isfinite(prob.rel_residual(x0, b))
+    it_warm, rel_warm = g.mgpcg_solve(CH_X, CH_B, tol=1e-6, max_iter=100)
+    g.fill(0.0, CH_X)
+    it_zero, rel_zero = g.mgpcg_solve(CH_X, CH_B, tol=1e-6, max_iter=100)
+    assert rel_warm <= 1e-6 and rel_zero <= 1e-6
+    assert it_warm <= it_zero
+    for pb, px, _ in pairs:
+        pb.free()
+        px.free()
