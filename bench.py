@@ -408,6 +408,22 @@ def poisson_measure(n_objects: int, steps: int, warmup: int,
 
 
 def run_poisson(args, dist):
+    if args.workload == "poisson-batch256":
+        from msbg_gb300 import batch_workload as BW
+        res = BW.run_batch(args.steps, args.warmup, WARMNET)
+        if dist.rank != 0:
+            return
+        pl = res["plain"]
+        line = {
+            "metric": "batched Poisson solves/s (256 volumes, 1e-6)", "value": pl["solves_per_s"], "unit": "solves/s",
+            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": pl["batch_ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 dots)",
+            "data": "synthetic", "config": {"workload": res["workload"], "cells": res["cells"],
+                                            "l2": "inputs larger than L2 (no flush)"},
+            "poisson_batch": res,
+        }
+        print(json.dumps(line), flush=True)
+        return
     n_obj = {"poisson-crop96": 96, "poisson-crop12": 12}[args.workload]
     res = poisson_measure(n_obj, args.steps, args.warmup)
     if dist.rank != 0:
@@ -431,7 +447,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="surface4096",
-                    choices=["surface4096", "surface4096-crop", "surface512", "poisson-crop96", "poisson-crop12"])
+                    choices=["surface4096", "surface4096-crop", "surface512", "poisson-crop96", "poisson-crop12",
+                             "poisson-batch256"])
     ap.add_argument("--no-poisson", action="store_true",
                     help="skip the sparse Poisson time-to-1e-6 measurement of the default run")
     ap.add_argument("--variant", default="fast", choices=["fast", "exact"])

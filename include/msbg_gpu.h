@@ -236,6 +236,22 @@ int msbg_gpu_poisson_set_params(msbg_gpu_ctx *ctx, int preSweeps, int postSweeps
 /* Multigrid levels of the current hierarchy and their cell counts. */
 int msbg_gpu_mg_info(msbg_gpu_ctx *ctx, int *nLevels, int64_t *cellsPerLevel, int cap);
 
+/* ---- batched solves ------------------------------------------------------------------
+ * Many independent volumes on one layout: every value block belongs to one volume
+ * (hVolOfBlock[nBlocks], -1 for blocks without data; volumes must not share a
+ * block face, and each volume must lie in its own aligned region of the block grid
+ * so that the multigrid aggregation never merges two volumes).  The solve runs a
+ * segmented MG-PCG: CG scalars per volume, a volume freezes once its recurrence
+ * residual is <= tol * ||B_v||.  useGraph: one captured CUDA graph per iteration,
+ * replayed.  Outputs per volume (host arrays of nVol, may be NULL): iterations
+ * (-1 not converged, 0 converged at the start), milliseconds from the start to the
+ * iteration it converged in, FP64-checked relative residual; *hTotalMs = the whole
+ * batch.  No reference counterpart (the reference solves one grid at a time). */
+int msbg_gpu_batch_set_volumes(msbg_gpu_ctx *ctx, const int32_t *hVolOfBlock, int nVol);
+int msbg_gpu_batch_mgpcg_solve(msbg_gpu_ctx *ctx, int chanX, int chanB, double tol, int maxIter,
+                               int useGraph, int32_t *hIters, float *hMsToTol, double *hRelRes,
+                               float *hTotalMs);
+
 /* ---- learned warm start ------------------------------------------------------------
  * A 4-layer 3D convolutional network (channels 2-16-16-16-2, 3x3x3 kernels, BF16
  * weights, FP32 activations and accumulation) on the level-1 cells of the Poisson

@@ -14,8 +14,10 @@ namespace msbg {
 
 struct PoissonState;
 struct WarmNetState;
+struct BatchState;
 void poissonFree(PoissonState *ps);
 void warmNetFree(WarmNetState *w);
+void batchFree(BatchState *b);
 constexpr int kMaxChannels = 64;
 constexpr int kMaxEvents = 16;
 
@@ -72,6 +74,7 @@ struct msbg_gpu_ctx {
   int64_t layoutStamp = 0;                 // bumped by every set_refinement_map
   msbg::PoissonState *poisson = nullptr;   // solver hierarchy of the current layout
   msbg::WarmNetState *warmnet = nullptr;   // learned warm start (weights, level-1 buffers)
+  msbg::BatchState *batch = nullptr;       // batched solves: volumes of the layout, graph
   int mgPre = 2, mgPost = 2, mgTileIters = 3, mgCoarsestIter = 0;  // multigrid parameters
   std::string err;
 };

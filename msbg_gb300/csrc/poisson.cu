@@ -806,6 +806,15 @@ static int checkStatus(msbg_gpu_ctx *ctx) {
   return MSBG_GPU_OK;
 }
 
+// level-0 operator and V-cycle for the batched solver (FP32)
+int batchApply(msbg_gpu_ctx *ctx, const float *x, const float *b, float *y, int mode) {
+  return applyT<float>(ctx, ctx->poisson, ctx->poisson->f32, 0, x, b, y, mode);
+}
+int batchVcycle(msbg_gpu_ctx *ctx, float *x, const float *b) {
+  PoissonState *ps = ctx->poisson;
+  return vcycleT<float>(ctx, ps, ps->f32, 0, x, b, (float *)ps->f32.vs);
+}
+
 int poissonEnsure(msbg_gpu_ctx *ctx) {
   if (ctx->poisson && ctx->poisson->layoutStamp == ctx->layoutStamp) return MSBG_GPU_OK;
   if (ctx->poisson) { poissonFree(ctx->poisson); ctx->poisson = nullptr; }

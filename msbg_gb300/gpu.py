@@ -76,6 +76,8 @@ SIGNATURES = {
     "msbg_gpu_warmnet_get_weights": (I, [P, P, P]),
     "msbg_gpu_warmnet_predict": (I, [P, I, I]),
     "msbg_gpu_warmnet_set_loss": (I, [P, I]),
+    "msbg_gpu_batch_set_volumes": (I, [P, P, I]),
+    "msbg_gpu_batch_mgpcg_solve": (I, [P, I, I, D, I, I, P, P, P, C.POINTER(F)]),
     "msbg_gpu_warmnet_loss_grad": (I, [P, I, I, C.POINTER(D), P, P]),
     "msbg_gpu_warmnet_train_step": (I, [P, P, P, F, C.POINTER(D)]),
     "msbg_gpu_assign_slots_noalloc": (I, [P, I64, P, P, P, P]),
@@ -371,6 +373,23 @@ class MultiresSparseGrid:
 
     def poisson_set_params(self, pre: int = 2, post: int = 2, tile_iters: int = 3, coarsest_iter: int = 0):
         self._check(self.L.msbg_gpu_poisson_set_params(self.h, pre, post, tile_iters, coarsest_iter))
+
+    # ---- batched solves ---------------------------------------------------------------------
+    def batch_set_volumes(self, vol_of_block: np.ndarray, n_vol: int):
+        v = np.ascontiguousarray(vol_of_block, np.int32)
+        self._check(self.L.msbg_gpu_batch_set_volumes(self.h, _ptr(v), int(n_vol)))
+        self._n_vol = int(n_vol)
+
+    def batch_mgpcg_solve(self, chanX: int, chanB: int, tol: float = 1e-6, max_iter: int = 100,
+                          use_graph: bool = True):
+        nv = self._n_vol
+        its = np.zeros(nv, np.int32)
+        ms = np.zeros(nv, np.float32)
+        rel = np.zeros(nv, np.float64)
+        tot = C.c_float()
+        self._check(self.L.msbg_gpu_batch_mgpcg_solve(self.h, chanX, chanB, tol, max_iter, int(use_graph),
+                                                      _ptr(its), _ptr(ms), _ptr(rel), C.byref(tot)))
+        return its, ms, rel, tot.value
 
     # ---- learned warm start ----------------------------------------------------------------
     WARMNET_CH = (2, 16, 16, 16, 2)
