@@ -47,6 +47,10 @@ from msbg_gb300 import workloads as W  # noqa: E402
 
 OPT8 = 1 << 29
 MCF8 = -(4 + OPT8)
+JAC8 = -(17 + OPT8)  # Jacobi diffusion (phi + dt sum f_i) / (1 + 6 dt), 8-colour in place
+# DRAM bytes (read + write) of one sweep launch of the 4096^3 workload, from the ncu
+# capture summarised in profiles/sweep_mcf_surface4096.md (mean of 8 launches)
+SWEEP_TRAFFIC_4096 = 2.63e9
 
 
 # ------------------------------------------------------------------------------------
@@ -303,8 +307,30 @@ def run_gpu(args, spec, dist: Dist):
     per_launch_s = (ms / 1e3) / launches
     achieved = per_launch_bytes / per_launch_s / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": args.traffic_per_launch,
+                "frac": achieved / peaks["hbm_gbs"],
+                "traffic": args.traffic_per_launch if args.traffic_per_launch is not None
+                else (SWEEP_TRAFFIC_4096 if spec is W.SURFACE_4096 and args.variant == "fast" else None),
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"}
+
+    # the same sweep machinery with the cheap Jacobi stencil (same layout and field)
+    jacobi = None
+    if not args.no_jacobi:
+        for _ in range(max(1, args.warmup)):
+            g.applyChannelPdeFast(0, JAC8, 1, n_iter, spec["dt"], 0.0, variant)
+        g.synchronize()
+        lj = g.launch_count()
+        g.event_record(2)
+        for _ in range(args.steps):
+            g.applyChannelPdeFast(0, JAC8, 1, n_iter, spec["dt"], 0.0, variant)
+        g.event_record(3)
+        g.synchronize()
+        msj = dist.max(g.event_elapsed_ms(2, 3))
+        nlj = g.launch_count() - lj
+        vj = updates_per_step * args.steps * dist.world / (msj / 1e3)
+        achj = (updates_per_step * bytes_per_update / (nlj / args.steps)) / ((msj / 1e3) / nlj) / 1e9
+        jacobi = {"laplTyp": 17, "value": vj, "unit": "voxel-updates/s", "ms_per_step": msj / args.steps,
+                  "roofline": {"bound": "hbm", "achieved": achj, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                               "frac": achj / peaks["hbm_gbs"]}}
 
     # e2e through the host-buffer entry point
     e2e = None
@@ -366,6 +392,7 @@ def run_gpu(args, spec, dist: Dist):
         "clocks": clk,
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "jacobi_sweeps": jacobi,
         "poisson": poisson,
     }
     print(json.dumps(line), flush=True)
@@ -449,6 +476,7 @@ def main():
     ap.add_argument("--workload", default="surface4096",
                     choices=["surface4096", "surface4096-crop", "surface512", "poisson-crop96", "poisson-crop12",
                              "poisson-batch256"])
+    ap.add_argument("--no-jacobi", action="store_true", help="skip the Jacobi-sweep throughput of the default run")
     ap.add_argument("--no-poisson", action="store_true",
                     help="skip the sparse Poisson time-to-1e-6 measurement of the default run")
     ap.add_argument("--variant", default="fast", choices=["fast", "exact"])

@@ -152,6 +152,21 @@ __device__ __forceinline__ void mcfFastStrip(const float Pm[3][6], const float P
   }
 }
 
+// Fast Jacobi diffusion of four x-consecutive voxels: (phi + dt s6) * 1/(1 + 6 dt),
+// the reference's division replaced by a multiplication with the reciprocal.
+__device__ __forceinline__ void jacobiFastStrip(const float Pm[3][6], const float P0[3][6],
+                                                const float Pp[3][6], float dt, bool clamp01,
+                                                float out[4]) {
+  const float inv = 1.0f / fmaf(6.0f, dt, 1.0f);
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int c = i + 1;
+    const float s6 = (P0[1][c - 1] + P0[1][c + 1]) + (P0[0][c] + P0[2][c]) + (Pm[1][c] + Pp[1][c]);
+    const float v = fmaf(dt, s6, P0[1][c]) * inv;
+    out[i] = clamp01 ? __saturatef(v) : v;
+  }
+}
+
 // Four voxels of a strip, any kernel, from the register window.
 template <bool EXACT>
 __device__ __forceinline__ void computeStrip(const float Pm[3][6], const float P0[3][6],
@@ -159,6 +174,10 @@ __device__ __forceinline__ void computeStrip(const float Pm[3][6], const float P
                                              float out[4]) {
   if (!EXACT && p.kind == K_MCF) {
     mcfFastStrip(Pm, P0, Pp, p.dt, p.constr01 != 0, out);
+    return;
+  }
+  if (!EXACT && p.kind == K_JACOBI) {
+    jacobiFastStrip(Pm, P0, Pp, p.dt, p.constr01 != 0, out);
     return;
   }
 #pragma unroll

@@ -128,11 +128,13 @@ def test_gpu_vs_port_seeded(gpulib, port, storage, bsx):
     assert np.array_equal(_as_bits(r["pde"]), _as_bits(p.after_pde))
 
 
-def test_gpu_fast_variant_within_tolerance(gpulib, port):
+@pytest.mark.parametrize("lapl", ["mcf", "jacobi"])
+def test_gpu_fast_variant_within_tolerance(gpulib, port, lapl):
     res = 256
+    typ = MCF8 if lapl == "mcf" else -(17 + (1 << 29))
     pts = W.sphere_cloud(res, 12, 6000, seed=W.workload_seed(1, 77))
-    r = _gpu_pipeline(gpulib, pts, res, 16, gpulib.F32, 20, MCF8, 0.1, variant=gpulib.SWEEP_FAST)
-    p = port.surface_pipeline(pts, res, 16, storage=port.F32, n_iter=20, dt=0.1)
+    r = _gpu_pipeline(gpulib, pts, res, 16, gpulib.F32, 20, typ, 0.1, variant=gpulib.SWEEP_FAST)
+    p = port.surface_pipeline(pts, res, 16, storage=port.F32, n_iter=20, dt=0.1, lapl_typ=typ)
     assert np.array_equal(r["bids"], p.active_bids)
     err = rel_l2(r["pde"], p.after_pde)
     assert err <= REL_TOL, err
