@@ -223,3 +223,40 @@ def test_gpu_error_codes(gpulib):
         assert e.value.code == G.ERR_ARG
     finally:
         g.close()
+
+
+def test_full_size_surface512_matches_restatement(gpulib, port):
+    """The 512^3 surface workload at full size (64 spheres x 32,000 points, bs16,
+    20 MCF iterations, FP32; EXACT sweep variant): active set, levels, flags and the
+    particle counters bit for bit, the field after finalize and after the sweeps bit
+    for bit as well (same expression order), against the CPU restatement."""
+    spec = W.SURFACE_512
+    pts = W.make_points(spec, 1)
+    r = _gpu_pipeline(gpulib, pts, spec["res"], spec["bsx"], gpulib.F32, spec["n_iter"], MCF8, spec["dt"],
+                      variant=gpulib.SWEEP_EXACT)
+    p = port.surface_pipeline(pts, spec["res"], spec["bsx"], storage=port.F32, n_iter=spec["n_iter"],
+                              dt=spec["dt"])
+    assert np.array_equal(r["bids"], p.active_bids)
+    assert np.array_equal(r["levels"], p.levels) and np.array_equal(r["flags"], p.flags)
+    assert r["info"].nActParticles == p.n_act_particles and r["info"].nAborted == p.n_aborted
+    assert np.array_equal(r["final"], p.after_finalize)
+    assert np.array_equal(r["pde"], p.after_pde)
+    assert len(r["bids"]) > 1000
+
+
+def test_full_size_surface4096_layout_and_splat_match_restatement(gpulib, port):
+    """The 4096^3 three-level FP16 workload at full size (1,024 clusters x 32,000
+    points, bands 8 / 16 voxels): levels, flags, active set, particle counters and the
+    FP16 field after splat + finalize, bit for bit against the CPU restatement."""
+    spec = W.SURFACE_4096
+    pts = W.make_points(spec, 2)
+    bands = (spec["fine_band"], spec["mid_band"])
+    r = _gpu_pipeline(gpulib, pts, spec["res"], spec["bsx"], gpulib.F16, 0, MCF8, spec["dt"], bands=bands,
+                      n_levels=spec["n_levels"])
+    p = port.surface_pipeline(pts, spec["res"], spec["bsx"], storage=port.F16, n_iter=0, bands=bands,
+                              n_levels=spec["n_levels"])
+    assert np.array_equal(r["bids"], p.active_bids)
+    assert np.array_equal(r["levels"], p.levels) and np.array_equal(r["flags"], p.flags)
+    assert r["info"].nActParticles == p.n_act_particles and r["info"].nAborted == p.n_aborted
+    assert np.array_equal(_as_bits(r["final"]), _as_bits(p.after_finalize))
+    assert len(r["bids"]) == 144191
