@@ -27,6 +27,8 @@
 // a 16-byte aligned address, as cp.async.bulk requires.
 #include <string.h>
 
+#include <type_traits>
+
 #include "internal.cuh"
 #include "sweep_common.cuh"
 
@@ -70,6 +72,7 @@ struct ColorSweep {
   static constexpr int RS = BS + 8;          // ring row stride (floats); x in [-1,BS] at col x+4
   static constexpr int WR = RPW + 2;         // rows of a warp's ring plane (its rows +-1)
   static constexpr int PL = WR * RS;         // floats per warp ring plane (2 slots per warp)
+  static constexpr int PLX = PL + 4;         // slot stride: a 4-float tail takes the fills of idle lanes
   static constexpr int NG = WR * SPR;        // 4-value groups of a warp ring plane
   static constexpr int NGP = (NG + 31) / 32; // groups per lane
   static constexpr int NXH = 2 * WR;         // x-halo values of a warp ring plane
@@ -92,6 +95,7 @@ struct RawTile {
   T yr[2][BS * BS];      // row y=-1 (0) and y=BS (1), [z][x]
   T cn[4][BS];           // corner columns (x=-1|BS, y=-1|BS), k = (dx>0) + 2*(dy>0), [z]
   T zh[2][4][BS];        // planes -1 / BS: x=-1 row, x=BS row (over y), y=-1 row, y=BS row (over x)
+  alignas(16) T er[16];  // the empty value (source of every fill from an empty block)
 };
 
 __device__ __forceinline__ uint32_t smemAddr(const void *p) {
@@ -233,7 +237,7 @@ constexpr size_t rawTileBytes() {
 
 template <typename T, int BS>
 constexpr size_t colorSmemBytes() {
-  return rawTileBytes<T, BS>() + 2 * sizeof(float) * ColorSweep<T, BS>::PL * ColorSweep<T, BS>::NW;
+  return rawTileBytes<T, BS>() + 2 * sizeof(float) * ColorSweep<T, BS>::PLX * ColorSweep<T, BS>::NW;
 }
 
 template <typename T>
@@ -241,11 +245,14 @@ __device__ __forceinline__ float ldval(const T *p) {
   if constexpr (sizeof(T) == 4) return *p; else return Store<T>::load(p);
 }
 
-template <typename T, int BS, bool EXACT>
+// FK: the stencil, fixed at compile time.  0 = any kind in the reference's
+// operation order (computeStrip); K_MCF / K_JACOBI = the fast forms, plus
+// FK_CLAMP when the result is clamped to [0,1].
+template <typename T, int BS, int FK>
 __global__ void __launch_bounds__(ColorSweep<T, BS>::NT, 2) kSweepColor(ColorArgs a) {
   using C = ColorSweep<T, BS>;
   using V4 = typename Vec4T<T>::V;
-  constexpr int NT = C::NT, RS = C::RS, PL = C::PL, NH = C::NH, CZ = C::CZ, NCH = C::NCH;
+  constexpr int RS = C::RS, PL = C::PL, PLX = C::PLX, CZ = C::CZ, NCH = C::NCH;
   extern __shared__ __align__(128) unsigned char dynSmem[];
   RawTile<T, BS> &t = *reinterpret_cast<RawTile<T, BS> *>(dynSmem);
   __shared__ int nbs[27];
@@ -265,6 +272,11 @@ __global__ void __launch_bounds__(ColorSweep<T, BS>::NT, 2) kSweepColor(ColorArg
   }
   if (tid < NCH) mbarInit(&bar[tid], 1);
   if (tid == 0) asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  if (tid < 16) {
+    T e;
+    if constexpr (sizeof(T) == 4) e = a.emptyValue; else Store<T>::storeRNE(&e, a.emptyValue);
+    t.er[tid] = e;
+  }
   __syncthreads();
   if (tid < 32) {
     // warp 0, chunk by chunk: announce the chunk's bytes, then issue its copies lane-parallel
@@ -287,7 +299,7 @@ __global__ void __launch_bounds__(ColorSweep<T, BS>::NT, 2) kSweepColor(ColorArg
   const int ty = tid / C::SPR, tx = (tid % C::SPR) * 4;  // this thread's strip
   const int y0w = warp * C::RPW;                          // first row of this warp
   const int tyl = ty - y0w;                               // row inside the warp
-  float *wring = reinterpret_cast<float *>(dynSmem + rawTileBytes<T, BS>()) + warp * 2 * PL;
+  float *wring = reinterpret_cast<float *>(dynSmem + rawTileBytes<T, BS>()) + warp * 2 * PLX;
   float emptyF;
   {
     T e;
@@ -297,78 +309,88 @@ __global__ void __launch_bounds__(ColorSweep<T, BS>::NT, 2) kSweepColor(ColorArg
 
   // ---- per-lane fill sources for the interior planes 0..BS-1 ------------------
   // Quad groups: ring row rr (y = y0w-1+rr), x = 4j..4j+3; source = base + p*stride.
+  // Every lane gets a source for each of its groups: an empty block (and a lane
+  // without a k-th group) reads the empty row with stride 0; an idle lane writes to
+  // the slot's 4-float tail.  The fill then has no branches.
   const T *gSrc[C::NGP];
   int gStride[C::NGP], gDst[C::NGP];
-  bool gOn[C::NGP], gEmpty[C::NGP];
 #pragma unroll
   for (int k = 0; k < C::NGP; k++) {
     const int g = lane + 32 * k;
-    gOn[k] = g < C::NG;
     const int rr = g / C::SPR, j = g % C::SPR, y = y0w - 1 + rr, x = 4 * j;
-    gDst[k] = rr * RS + x + 4;
-    gEmpty[k] = false;
-    gSrc[k] = t.blk;
+    gDst[k] = g < C::NG ? rr * RS + x + 4 : PL;
+    gSrc[k] = t.er;
     gStride[k] = 0;
-    if (y >= 0 && y < BS) {
-      gSrc[k] = t.blk + y * BS + x; gStride[k] = BS * BS;
-    } else {
-      const int side = y < 0 ? 0 : 1;
-      const int s = nbs[9 + (side ? 2 : 0) * 3 + 1];
-      if (s >= 0) { gSrc[k] = t.yr[side] + x; gStride[k] = BS; }
-      else if (s == -1) gEmpty[k] = true;
-      else { gSrc[k] = t.blk + (side ? BS - 1 : 0) * BS + x; gStride[k] = BS * BS; }  // Neumann
+    if (g < C::NG) {
+      if (y >= 0 && y < BS) {
+        gSrc[k] = t.blk + y * BS + x; gStride[k] = BS * BS;
+      } else {
+        const int side = y < 0 ? 0 : 1;
+        const int s = nbs[9 + (side ? 2 : 0) * 3 + 1];
+        if (s >= 0) { gSrc[k] = t.yr[side] + x; gStride[k] = BS; }
+        else if (s != -1) { gSrc[k] = t.blk + (side ? BS - 1 : 0) * BS + x; gStride[k] = BS * BS; }  // Neumann
+      }
     }
   }
   // x-halo values: side = lane / WR (x=-1 | x=BS), ring row rr = lane % WR
-  const T *hSrc = t.blk;
-  int hStride = 0, hDst = 0;
-  bool hOn = lane < C::NXH, hEmpty = false;
-  {
+  const T *hSrc = t.er;
+  int hStride = 0, hDst = PL;
+  if (lane < C::NXH) {
     const int side = lane / C::WR, rr = lane % C::WR, y = y0w - 1 + rr;
     const int dx = side ? 1 : -1, xc = side ? BS - 1 : 0;
     hDst = rr * RS + (side ? BS + 4 : 3);
     if (y >= 0 && y < BS) {
       const int s = nbs[9 + 3 + (dx + 1)];
       if (s >= 0) { hSrc = t.xf[side] + y; hStride = BS; }
-      else if (s == -1) hEmpty = true;
-      else { hSrc = t.blk + y * BS + xc; hStride = BS * BS; }
+      else if (s != -1) { hSrc = t.blk + y * BS + xc; hStride = BS * BS; }
     } else {  // corner column of the diagonal neighbour
       const int dy = y < 0 ? -1 : 1, yc = dy < 0 ? 0 : BS - 1;
       const int s = nbs[9 + (dy + 1) * 3 + (dx + 1)];
       if (s >= 0) { hSrc = t.cn[(dx > 0 ? 1 : 0) + 2 * (dy > 0 ? 1 : 0)]; hStride = 1; }
-      else if (s == -1) hEmpty = true;
-      else { hSrc = t.blk + yc * BS + xc; hStride = BS * BS; }
+      else if (s != -1) { hSrc = t.blk + yc * BS + xc; hStride = BS * BS; }
     }
   }
 
-  unsigned ready = 0;
+  // planes are consumed in increasing order (fillZ(-1) needs chunk 0, fillZ(BS)
+  // comes after plane BS-1), so one counter of the planes known to have landed
+  // replaces per-chunk flags
+  int readyPlanes = 0;
   bool timedOut = false;
-  auto need = [&](int k) {
-    if (!(ready & (1u << k))) {
-      if (!waitChunk(&bar[k])) timedOut = true;
-      ready |= 1u << k;
+  auto need = [&](int p) {
+    if (p >= readyPlanes) {
+      if (!waitChunk(&bar[p / CZ])) timedOut = true;
+      readyPlanes = (p / CZ + 1) * CZ;
     }
   };
 
-  // ---- interior plane p (0..BS-1) -> this warp's ring slot ----
-  auto fillInterior = [&](int p, float *pl) {
-    need(p / CZ);
+  // ---- interior plane p (0..BS-1) -> this warp's ring slot, in two halves so
+  // that the shared-memory reads of plane p overlap the previous plane's update ----
+  V4 rawG[C::NGP];
+  T rawH;
+  auto loadRaw = [&](int p) {
+    need(p);
+#pragma unroll
+    for (int k = 0; k < C::NGP; k++) rawG[k] = *reinterpret_cast<const V4 *>(gSrc[k] + p * gStride[k]);
+    rawH = hSrc[p * hStride];
+  };
+  auto storeRaw = [&](float *pl) {
 #pragma unroll
     for (int k = 0; k < C::NGP; k++) {
-      if (gOn[k]) {
-        float q[4];
-        if (gEmpty[k]) q[0] = q[1] = q[2] = q[3] = emptyF;
-        else unpack4<T>(*reinterpret_cast<const V4 *>(gSrc[k] + p * gStride[k]), q);
-        *reinterpret_cast<float4 *>(pl + gDst[k]) = make_float4(q[0], q[1], q[2], q[3]);
-      }
+      float q[4];
+      unpack4<T>(rawG[k], q);
+      *reinterpret_cast<float4 *>(pl + gDst[k]) = make_float4(q[0], q[1], q[2], q[3]);
     }
-    if (hOn) pl[hDst] = hEmpty ? emptyF : ldval<T>(hSrc + p * hStride);
+    pl[hDst] = ldval<T>(&rawH);
+  };
+  auto fillInterior = [&](int p, float *pl) {
+    loadRaw(p);
+    storeRaw(pl);
   };
 
   // ---- z-halo plane p = -1 or BS -> this warp's ring slot (twice per block) ----
   auto fillZ = [&](int p, float *pl) {
     const int zi = p < 0 ? 0 : 1;
-    need(zi ? NCH - 1 : 0);
+    need(zi ? BS - 1 : 0);
     const int dzb = zi ? 1 : -1;
     const int pc = zi ? BS - 1 : 0;  // Neumann clamp inside the own block
     for (int g = lane; g < C::NG; g += 32) {
@@ -416,58 +438,88 @@ __global__ void __launch_bounds__(ColorSweep<T, BS>::NT, 2) kSweepColor(ColorArg
   const bool faceThread = tx == 0 || tx == BS - 4;
   const int kx = tx == 0 ? 0 : 1;
   T *facep = (T *)a.faces + ((int64_t)ownSlot * 2 + kx) * C::FACE + ty;
-  T *cornp = (ty == 0 || ty == BS - 1)
-                 ? (T *)a.corners + ((int64_t)ownSlot * 4 + kx + 2 * (ty == 0 ? 0 : 1)) * C::CORN
-                 : nullptr;
+  const bool cornThread = faceThread && (ty == 0 || ty == BS - 1);
+  T *cornp = (T *)a.corners + ((int64_t)ownSlot * 4 + kx + 2 * (ty == 0 ? 0 : 1)) * C::CORN;
   float Wa[3][6], Wb[3][6], Wc[3][6];
 
   auto emit = [&](int z, const float (&Wm)[3][6], const float (&W0)[3][6], const float (&Wp)[3][6]) {
     float out[4];
-    computeStrip<EXACT>(Wm, W0, Wp, a.p, out);
+    constexpr bool CL = (FK & FK_CLAMP) != 0;
+    if constexpr ((FK & ~FK_CLAMP) == K_MCF) mcfFastStrip<CL>(Wm, W0, Wp, a.p.dt, out);
+    else if constexpr ((FK & ~FK_CLAMP) == K_JACOBI) jacobiFastStrip<CL>(Wm, W0, Wp, a.p.dt, out);
+    else computeStrip(Wm, W0, Wp, a.p, out);
     const V4 pk = pack4<T>(out);
     *reinterpret_cast<V4 *>(outp + z * BS * BS) = pk;
-    if (faceThread) {
-      T v;
-      if constexpr (sizeof(T) == 4) {
-        v = kx ? pk.w : pk.x;
-      } else {
-        const uint16_t bits = kx ? (uint16_t)(pk.y >> 16) : (uint16_t)(pk.x & 0xffffu);
-        v = *reinterpret_cast<const T *>(&bits);
-      }
-      facep[z * BS] = v;
-      if (cornp) cornp[z] = v;
+    T v;
+    if constexpr (sizeof(T) == 4) {
+      v = kx ? pk.w : pk.x;
+    } else {
+      const uint16_t bits = kx ? (uint16_t)(pk.y >> 16) : (uint16_t)(pk.x & 0xffffu);
+      v = *reinterpret_cast<const T *>(&bits);
     }
+    if (faceThread) facep[z * BS] = v;
+    if (cornThread) cornp[z] = v;
   };
-  // One plane.  On entry A, B, C hold planes z-1, z, z+1.  Plane z+2 is staged
-  // into the warp's ring slot (z & 1), which held plane z, last read before the
-  // previous step's __syncwarp; on exit A holds plane z+2.
-  auto step = [&](int z, float (&A)[3][6], float (&B)[3][6], float (&Cw)[3][6]) {
-    float *slot = wring + (z & 1) * PL;
-    if (z + 2 < BS) fillInterior(z + 2, slot);
-    else if (z + 2 == BS) fillZ(BS, slot);
+  // One plane.  On entry A, B, C hold planes z-1, z, z+1 and, for an interior
+  // plane z+2, its raw values are in registers.  Plane z+2 is staged into the
+  // warp's ring slot (z & 1), which held plane z, last read before the previous
+  // step's __syncwarp; the raw values of plane z+3 are read; on exit A holds
+  // plane z+2.  KIND: 0 = planes z+2 and z+3 are interior planes, 3 = only plane
+  // z+2 is, 1 = plane z+2 is the z-halo plane BS, 2 = there is no plane z+2.
+  auto step = [&](auto kind, int z, float (&A)[3][6], float (&B)[3][6], float (&Cw)[3][6]) {
+    constexpr int KIND = decltype(kind)::value;
+    float *slot = wring + (z & 1) * PLX;
+    if constexpr (KIND == 0 || KIND == 3) {
+      storeRaw(slot);
+      if constexpr (KIND == 0) loadRaw(z + 3);
+    } else if constexpr (KIND == 1) {
+      fillZ(BS, slot);
+    }
     __syncwarp();
     emit(z, A, B, Cw);
-    if (z + 2 <= BS) window(slot, A);
+    if constexpr (KIND != 2) window(slot, A);
   };
+  using Interior = std::integral_constant<int, 0>;
 
   // planes -1, 0, 1 into the windows (warp-local ring slots 0/1)
   fillZ(-1, wring);
-  fillInterior(0, wring + PL);
+  fillInterior(0, wring + PLX);
   __syncwarp();
   window(wring, Wa);
-  window(wring + PL, Wb);
+  window(wring + PLX, Wb);
   __syncwarp();
   fillInterior(1, wring);
+  loadRaw(2);
   __syncwarp();
   window(wring, Wc);
   __syncwarp();
-  // the window roles rotate every plane: (a,b,c) -> (b,c,a)
+  // The window roles rotate every plane: (a,b,c) -> (b,c,a).  The main loop runs
+  // the planes z whose planes z+2 and z+3 are interior, three at a time; the
+  // last planes follow with their kinds known at compile time.
+  constexpr int MAIN = 3 * ((BS - 3) / 3);
 #pragma unroll 1
-  for (int z = 0; z < BS; z += 3) {
-    step(z, Wa, Wb, Wc);
-    if (z + 1 < BS) step(z + 1, Wb, Wc, Wa);
-    if (z + 2 < BS) step(z + 2, Wc, Wa, Wb);
+  for (int z = 0; z < MAIN; z += 3) {
+    step(Interior{}, z, Wa, Wb, Wc);
+    step(Interior{}, z + 1, Wb, Wc, Wa);
+    step(Interior{}, z + 2, Wc, Wa, Wb);
   }
+  static_assert(BS - MAIN >= 3 && BS - MAIN <= 5, "tail of 3..5 planes");
+  auto tail = [&](auto zc) {
+    constexpr int z = decltype(zc)::value;
+    if constexpr (z < BS) {
+      constexpr int K = z + 3 < BS ? 0 : z + 2 < BS ? 3 : (z + 2 == BS ? 1 : 2);
+      using KT = std::integral_constant<int, K>;
+      constexpr int r = (z - MAIN) % 3;
+      if constexpr (r == 0) step(KT{}, z, Wa, Wb, Wc);
+      else if constexpr (r == 1) step(KT{}, z, Wb, Wc, Wa);
+      else step(KT{}, z, Wc, Wa, Wb);
+    }
+  };
+  tail(std::integral_constant<int, MAIN>{});
+  tail(std::integral_constant<int, MAIN + 1>{});
+  tail(std::integral_constant<int, MAIN + 2>{});
+  tail(std::integral_constant<int, MAIN + 3>{});
+  tail(std::integral_constant<int, MAIN + 4>{});
   if (timedOut) {
     atomicOr(a.status, 1);
     for (int k = 0; k < NCH; k++) waitChunk(&bar[k]);  // no copy may land after exit
@@ -519,13 +571,17 @@ static int runColorT(msbg_gpu_ctx *ctx, Channel &c, bool exact, bool color8, int
   a.status = ctx->dStatus;
   a.p = p;
   constexpr size_t smem = colorSmemBytes<T, BS>();
-  static bool attrSet[2] = {false, false};
-  if (!attrSet[exact]) {
-    if (exact)
-      MSBG_CUDA(ctx, cudaFuncSetAttribute(kSweepColor<T, BS, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    else
-      MSBG_CUDA(ctx, cudaFuncSetAttribute(kSweepColor<T, BS, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attrSet[exact] = true;
+  void (*const kerns[5])(ColorArgs) = {kSweepColor<T, BS, 0>, kSweepColor<T, BS, K_MCF>,
+                                       kSweepColor<T, BS, K_MCF | FK_CLAMP>, kSweepColor<T, BS, K_JACOBI>,
+                                       kSweepColor<T, BS, K_JACOBI | FK_CLAMP>};
+  int ki = 0;  // the exact variant and the other kinds: the generic kernel
+  if (!exact && p.kind == K_MCF) ki = p.constr01 ? 2 : 1;
+  else if (!exact && p.kind == K_JACOBI) ki = p.constr01 ? 4 : 3;
+  const auto kern = kerns[ki];
+  static bool attrSet[5] = {false, false, false, false, false};
+  if (!attrSet[ki]) {
+    MSBG_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attrSet[ki] = true;
   }
   static const int rbOrder[2][4] = {{1, 2, 4, 7}, {0, 3, 5, 6}};
   const int *cs = ctx->colorStart;
@@ -536,10 +592,7 @@ static int runColorT(msbg_gpu_ctx *ctx, Channel &c, bool exact, bool color8, int
       const int cnt = cs[col + 1] - cs[col];
       if (cnt <= 0) continue;
       a.bids = ctx->dColorBids + cs[col];
-      if (exact)
-        MSBG_LAUNCH(ctx, (kSweepColor<T, BS, true>), (unsigned)cnt, NT, smem, a);
-      else
-        MSBG_LAUNCH(ctx, (kSweepColor<T, BS, false>), (unsigned)cnt, NT, smem, a);
+      MSBG_LAUNCH(ctx, kern, (unsigned)cnt, NT, smem, a);
     }
   }
   return MSBG_GPU_OK;

@@ -7,6 +7,7 @@
 namespace msbg {
 
 enum { K_MCF = 4, K_JACOBI = 17, K_PM_JACOBI = 15, K_PM = 14, K_DIFF = 3, K_LAPL = 1 };
+enum { FK_CLAMP = 256 };  // sweep kernel flag: results clamped to [0,1]
 
 struct SweepParams {
   int kind, constr01;
@@ -120,66 +121,94 @@ __device__ __forceinline__ R stencil7(const P &F, const SweepParams &g) {
 //   H = [ (gy^2+gz^2) fxx + (gx^2+gz^2) fyy + (gx^2+gy^2) fzz
 //         - (gx gy Gyx + gx gz Gzx + gy gz Gzy) / 2 ] / |g|^2
 // which is the reference's H with |grad f|^2 = |g|^2 / 4 (threshold 4e-7).
+__device__ __forceinline__ float2 pr(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// The strip's voxels go through the arithmetic in pairs (columns 1,2 and 3,4 of
+// the window) on the packed FP32 pipe (add/mul/fma.rn.f32x2): per lane the same
+// correctly rounded operations as scalar code, so the results are those of the
+// scalar form.  Differences along x (whose operands straddle the pairs) and the
+// reciprocal and clamps stay scalar.
+// 1/x from the hardware's approximate reciprocal (PTX rcp.approx.ftz.f32).
+__device__ __forceinline__ float rcpApprox(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+template <bool CLAMP01>
 __device__ __forceinline__ void mcfFastStrip(const float Pm[3][6], const float P0[3][6],
-                                             const float Pp[3][6], float dt, bool clamp01,
-                                             float out[4]) {
+                                             const float Pp[3][6], float dt, float out[4]) {
   float Dy[6], Dz[6];
 #pragma unroll
-  for (int c = 0; c < 6; c++) {
-    Dy[c] = P0[2][c] - P0[0][c];
-    Dz[c] = Pp[1][c] - Pm[1][c];
+  for (int h = 0; h < 2; h++) {
+    const int c = 1 + 2 * h;
+    const float2 dy = sub2(pr(P0[2][c], P0[2][c + 1]), pr(P0[0][c], P0[0][c + 1]));
+    const float2 dz = sub2(pr(Pp[1][c], Pp[1][c + 1]), pr(Pm[1][c], Pm[1][c + 1]));
+    Dy[c] = dy.x; Dy[c + 1] = dy.y; Dz[c] = dz.x; Dz[c + 1] = dz.y;
   }
+  Dy[0] = P0[2][0] - P0[0][0]; Dy[5] = P0[2][5] - P0[0][5];
+  Dz[0] = Pp[1][0] - Pm[1][0]; Dz[5] = Pp[1][5] - Pm[1][5];
 #pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const int c = i + 1;
-    const float f0 = P0[1][c];
-    const float gx = P0[1][c + 1] - P0[1][c - 1], gy = Dy[c], gz = Dz[c];
-    const float fxx = fmaf(-2.0f, f0, P0[1][c - 1] + P0[1][c + 1]);
-    const float fyy = fmaf(-2.0f, f0, P0[0][c] + P0[2][c]);
-    const float fzz = fmaf(-2.0f, f0, Pm[1][c] + Pp[1][c]);
-    const float Gyx = Dy[c + 1] - Dy[c - 1];
-    const float Gzx = Dz[c + 1] - Dz[c - 1];
-    const float Gzy = (Pp[2][c] - Pm[2][c]) - (Pp[0][c] - Pm[0][c]);
-    const float xx = gx * gx, yy = gy * gy, zz = gz * gz;
-    const float A = yy + zz, B = xx + zz, Cc = xx + yy;
-    const float g2 = A + xx;
-    const float n1 = fmaf(A, fxx, fmaf(B, fyy, Cc * fzz));
-    const float n2 = fmaf(gx, fmaf(gy, Gyx, gz * Gzx), gy * gz * Gzy);
-    const float Hn = fmaf(-0.5f, n2, n1);
-    const float r = g2 > 4e-7f ? __fdividef(dt, g2) : 0.0f;
-    const float D = fminf(fmaxf(Hn * r, -0.1f), 0.1f);
-    out[i] = clamp01 ? __saturatef(f0 + D) : f0 + D;
+  for (int h = 0; h < 2; h++) {
+    const int c = 1 + 2 * h;
+    const float *w = P0[1];
+    const float2 f0 = pr(w[c], w[c + 1]);
+    const float2 gx = pr(w[c + 1] - w[c - 1], w[c + 2] - w[c]);
+    const float2 gy = pr(Dy[c], Dy[c + 1]), gz = pr(Dz[c], Dz[c + 1]);
+    // second differences as s - 2 f0 with s the neighbour sums; with A = g2 - xx,
+    // B = g2 - yy, C = g2 - zz the first numerator term is
+    //   A fxx + B fyy + C fzz = g2 (sx + sy + sz - 4 f0) - (xx sx + yy sy + zz sz)
+    const float2 sx = pr(w[c - 1] + w[c + 1], w[c] + w[c + 2]);
+    const float2 sy = add2(pr(P0[0][c], P0[0][c + 1]), pr(P0[2][c], P0[2][c + 1]));
+    const float2 sz = add2(pr(Pm[1][c], Pm[1][c + 1]), pr(Pp[1][c], Pp[1][c + 1]));
+    const float2 Gyx = pr(Dy[c + 1] - Dy[c - 1], Dy[c + 2] - Dy[c]);
+    const float2 Gzx = pr(Dz[c + 1] - Dz[c - 1], Dz[c + 2] - Dz[c]);
+    const float2 Gzy = sub2(sub2(pr(Pp[2][c], Pp[2][c + 1]), pr(Pm[2][c], Pm[2][c + 1])),
+                            sub2(pr(Pp[0][c], Pp[0][c + 1]), pr(Pm[0][c], Pm[0][c + 1])));
+    const float2 xx = mul2(gx, gx), yy = mul2(gy, gy), zz = mul2(gz, gz);
+    const float2 g2 = add2(add2(xx, yy), zz);
+    const float2 L = fma2(pr(-4.0f, -4.0f), f0, add2(add2(sx, sy), sz));
+    const float2 T3 = fma2(xx, sx, fma2(yy, sy, mul2(zz, sz)));
+    const float2 n1 = fma2(g2, L, neg2(T3));
+    const float2 n2 = fma2(gx, fma2(gy, Gyx, mul2(gz, Gzx)), mul2(mul2(gy, gz), Gzy));
+    const float2 Hn = fma2(pr(-0.5f, -0.5f), n2, n1);
+    const float2 r = pr(g2.x > 4e-7f ? rcpApprox(g2.x) : 0.0f, g2.y > 4e-7f ? rcpApprox(g2.y) : 0.0f);
+    const float2 Hr = mul2(Hn, mul2(r, pr(dt, dt)));
+    const float D0 = fminf(fmaxf(Hr.x, -0.1f), 0.1f), D1 = fminf(fmaxf(Hr.y, -0.1f), 0.1f);
+    out[2 * h] = CLAMP01 ? __saturatef(f0.x + D0) : f0.x + D0;
+    out[2 * h + 1] = CLAMP01 ? __saturatef(f0.y + D1) : f0.y + D1;
   }
 }
 
 // Fast Jacobi diffusion of four x-consecutive voxels: (phi + dt s6) * 1/(1 + 6 dt),
 // the reference's division replaced by a multiplication with the reciprocal.
+template <bool CLAMP01>
 __device__ __forceinline__ void jacobiFastStrip(const float Pm[3][6], const float P0[3][6],
-                                                const float Pp[3][6], float dt, bool clamp01,
-                                                float out[4]) {
+                                                const float Pp[3][6], float dt, float out[4]) {
   const float inv = 1.0f / fmaf(6.0f, dt, 1.0f);
 #pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const int c = i + 1;
-    const float s6 = (P0[1][c - 1] + P0[1][c + 1]) + (P0[0][c] + P0[2][c]) + (Pm[1][c] + Pp[1][c]);
-    const float v = fmaf(dt, s6, P0[1][c]) * inv;
-    out[i] = clamp01 ? __saturatef(v) : v;
+  for (int h = 0; h < 2; h++) {
+    const int c = 1 + 2 * h;
+    const float *w = P0[1];
+    const float2 sxy = add2(pr(w[c - 1] + w[c + 1], w[c] + w[c + 2]),
+                            add2(pr(P0[0][c], P0[0][c + 1]), pr(P0[2][c], P0[2][c + 1])));
+    const float2 s6 = add2(sxy, add2(pr(Pm[1][c], Pm[1][c + 1]), pr(Pp[1][c], Pp[1][c + 1])));
+    const float2 v = mul2(fma2(pr(dt, dt), s6, pr(w[c], w[c + 1])), pr(inv, inv));
+    out[2 * h] = CLAMP01 ? __saturatef(v.x) : v.x;
+    out[2 * h + 1] = CLAMP01 ? __saturatef(v.y) : v.y;
   }
 }
 
-// Four voxels of a strip, any kernel, from the register window.
-template <bool EXACT>
+// Four voxels of a strip, any kernel, from the register window, in the
+// reference's operation order.
 __device__ __forceinline__ void computeStrip(const float Pm[3][6], const float P0[3][6],
                                              const float Pp[3][6], const SweepParams &p,
                                              float out[4]) {
-  if (!EXACT && p.kind == K_MCF) {
-    mcfFastStrip(Pm, P0, Pp, p.dt, p.constr01 != 0, out);
-    return;
-  }
-  if (!EXACT && p.kind == K_JACOBI) {
-    jacobiFastStrip(Pm, P0, Pp, p.dt, p.constr01 != 0, out);
-    return;
-  }
 #pragma unroll
   for (int i = 0; i < 4; i++) {
     const int c = i + 1;
