@@ -422,16 +422,11 @@ __global__ void __launch_bounds__(ColorSweep<T, BS>::NT, 2) kSweepColor(ColorArg
     }
   };
 
-  // ---- warp ring slot -> register window rows (y-1..y+1, x-1..x+4) ----
+  // ---- warp ring slot -> this thread's plane (rows y-1..y+1, x-1..x+4) ----
+  constexpr int FKK = FK & ~FK_CLAMP;
+  using PW = std::conditional_t<FKK == K_MCF, PlaneMcf, std::conditional_t<FKK == K_JACOBI, PlaneJac, PlaneRaw>>;
   const int winOff = tyl * RS + tx + 3;
-  auto window = [&](const float *pl, float (&w)[3][6]) {
-#pragma unroll
-    for (int r = 0; r < 3; r++) {
-      const float *row = pl + winOff + r * RS;
-      const float4 m = *reinterpret_cast<const float4 *>(row + 1);
-      w[r][0] = row[0]; w[r][1] = m.x; w[r][2] = m.y; w[r][3] = m.z; w[r][4] = m.w; w[r][5] = row[5];
-    }
-  };
+  auto window = [&](const float *pl, PW &w) { loadPlane<RS>(pl + winOff, w); };
 
   T *outp = (T *)a.payload + (int64_t)ownSlot * C::VPB + ty * BS + tx;
   // x-face / corner cache entries this thread maintains (x = 0 or BS-1 strips)
@@ -440,14 +435,14 @@ __global__ void __launch_bounds__(ColorSweep<T, BS>::NT, 2) kSweepColor(ColorArg
   T *facep = (T *)a.faces + ((int64_t)ownSlot * 2 + kx) * C::FACE + ty;
   const bool cornThread = faceThread && (ty == 0 || ty == BS - 1);
   T *cornp = (T *)a.corners + ((int64_t)ownSlot * 4 + kx + 2 * (ty == 0 ? 0 : 1)) * C::CORN;
-  float Wa[3][6], Wb[3][6], Wc[3][6];
+  PW Wa, Wb, Wc;
 
-  auto emit = [&](int z, const float (&Wm)[3][6], const float (&W0)[3][6], const float (&Wp)[3][6]) {
+  auto emit = [&](int z, const PW &Wm, const PW &W0, const PW &Wp) {
     float out[4];
     constexpr bool CL = (FK & FK_CLAMP) != 0;
-    if constexpr ((FK & ~FK_CLAMP) == K_MCF) mcfFastStrip<CL>(Wm, W0, Wp, a.p.dt, out);
-    else if constexpr ((FK & ~FK_CLAMP) == K_JACOBI) jacobiFastStrip<CL>(Wm, W0, Wp, a.p.dt, out);
-    else computeStrip(Wm, W0, Wp, a.p, out);
+    if constexpr (FKK == K_MCF) mcfFastStrip<CL>(Wm, W0, Wp, a.p.dt, out);
+    else if constexpr (FKK == K_JACOBI) jacobiFastStrip<CL>(Wm, W0, Wp, a.p.dt, out);
+    else computeStrip(Wm.w, W0.w, Wp.w, a.p, out);
     const V4 pk = pack4<T>(out);
     *reinterpret_cast<V4 *>(outp + z * BS * BS) = pk;
     T v;
@@ -466,7 +461,7 @@ __global__ void __launch_bounds__(ColorSweep<T, BS>::NT, 2) kSweepColor(ColorArg
   // step's __syncwarp; the raw values of plane z+3 are read; on exit A holds
   // plane z+2.  KIND: 0 = planes z+2 and z+3 are interior planes, 3 = only plane
   // z+2 is, 1 = plane z+2 is the z-halo plane BS, 2 = there is no plane z+2.
-  auto step = [&](auto kind, int z, float (&A)[3][6], float (&B)[3][6], float (&Cw)[3][6]) {
+  auto step = [&](auto kind, int z, PW &A, PW &B, PW &Cw) {
     constexpr int KIND = decltype(kind)::value;
     float *slot = wring + (z & 1) * PLX;
     if constexpr (KIND == 0 || KIND == 3) {

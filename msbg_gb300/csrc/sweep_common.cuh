@@ -128,11 +128,59 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
-// The strip's voxels go through the arithmetic in pairs (columns 1,2 and 3,4 of
-// the window) on the packed FP32 pipe (add/mul/fma.rn.f32x2): per lane the same
-// correctly rounded operations as scalar code, so the results are those of the
-// scalar form.  Differences along x (whose operands straddle the pairs) and the
-// reciprocal and clamps stay scalar.
+// What the z-marching kernel keeps of one plane of a thread's neighbourhood
+// (rows y-1..y+1, columns x-1..x+4 of the strip x..x+3).  The generic form keeps
+// the raw values; the fast forms keep per-plane summaries, computed once when the
+// plane is read, so fewer values stay live across the three planes.
+struct PlaneRaw {
+  float w[3][6];
+};
+// MCF: centre row, y-difference (row y+1 - row y-1) and y-sum (centre columns).
+struct PlaneMcf {
+  float r1[6], dy[6], sy[4];
+};
+// Jacobi: centre row and y-sum (centre columns).
+struct PlaneJac {
+  float r1[6], sy[4];
+};
+
+// Reads one plane from the FP32 ring: row0 = row y-1 at column x-1; rows RS apart.
+template <int RS>
+__device__ __forceinline__ void loadPlane(const float *row0, PlaneRaw &P) {
+#pragma unroll
+  for (int r = 0; r < 3; r++) {
+    const float *row = row0 + r * RS;
+    const float4 m = *reinterpret_cast<const float4 *>(row + 1);
+    P.w[r][0] = row[0]; P.w[r][1] = m.x; P.w[r][2] = m.y; P.w[r][3] = m.z; P.w[r][4] = m.w; P.w[r][5] = row[5];
+  }
+}
+template <int RS>
+__device__ __forceinline__ void loadRow1(const float *row0, float (&r1)[6]) {
+  const float *row = row0 + RS;
+  const float4 m = *reinterpret_cast<const float4 *>(row + 1);
+  r1[0] = row[0]; r1[1] = m.x; r1[2] = m.y; r1[3] = m.z; r1[4] = m.w; r1[5] = row[5];
+}
+template <int RS>
+__device__ __forceinline__ void loadPlane(const float *row0, PlaneMcf &P) {
+  loadRow1<RS>(row0, P.r1);
+  const float4 u = *reinterpret_cast<const float4 *>(row0 + 1);
+  const float4 v = *reinterpret_cast<const float4 *>(row0 + 2 * RS + 1);
+  const float2 d01 = sub2(pr(v.x, v.y), pr(u.x, u.y)), d23 = sub2(pr(v.z, v.w), pr(u.z, u.w));
+  const float2 s01 = add2(pr(u.x, u.y), pr(v.x, v.y)), s23 = add2(pr(u.z, u.w), pr(v.z, v.w));
+  P.dy[0] = row0[2 * RS] - row0[0];
+  P.dy[1] = d01.x; P.dy[2] = d01.y; P.dy[3] = d23.x; P.dy[4] = d23.y;
+  P.dy[5] = row0[2 * RS + 5] - row0[5];
+  P.sy[0] = s01.x; P.sy[1] = s01.y; P.sy[2] = s23.x; P.sy[3] = s23.y;
+}
+template <int RS>
+__device__ __forceinline__ void loadPlane(const float *row0, PlaneJac &P) {
+  loadRow1<RS>(row0, P.r1);
+  const float4 u = *reinterpret_cast<const float4 *>(row0 + 1);
+  const float4 v = *reinterpret_cast<const float4 *>(row0 + 2 * RS + 1);
+  const float2 s01 = add2(pr(u.x, u.y), pr(v.x, v.y)), s23 = add2(pr(u.z, u.w), pr(v.z, v.w));
+  P.sy[0] = s01.x; P.sy[1] = s01.y; P.sy[2] = s23.x; P.sy[3] = s23.y;
+}
+
 // 1/x from the hardware's approximate reciprocal (PTX rcp.approx.ftz.f32).
 __device__ __forceinline__ float rcpApprox(float x) {
   float r;
@@ -140,23 +188,31 @@ __device__ __forceinline__ float rcpApprox(float x) {
   return r;
 }
 
+// Fast MCF of the strip's four voxels.  The voxels go through the arithmetic in
+// pairs (columns 1,2 and 3,4) on the packed FP32 pipe (add/mul/fma.rn.f32x2);
+// differences along x (whose operands straddle the pairs), the reciprocal and the
+// clamps stay scalar.  With central differences g = 2 grad f and the plane
+// summaries (Dz = centre row of z+1 - that of z-1):
+//   gx = f(x+1) - f(x-1), gy = dy0, gz = Dz
+//   Gyx = dy0(x+1) - dy0(x-1), Gzx = Dz(x+1) - Dz(x-1), Gzy = dy(z+1) - dy(z-1)
+//   H = [ (gy^2+gz^2) fxx + (gx^2+gz^2) fyy + (gx^2+gy^2) fzz
+//         - (gx gy Gyx + gx gz Gzx + gy gz Gzy) / 2 ] / |g|^2
+// which is the reference's H with |grad f|^2 = |g|^2 / 4 (threshold 4e-7).
 template <bool CLAMP01>
-__device__ __forceinline__ void mcfFastStrip(const float Pm[3][6], const float P0[3][6],
-                                             const float Pp[3][6], float dt, float out[4]) {
-  float Dy[6], Dz[6];
+__device__ __forceinline__ void mcfFastStrip(const PlaneMcf &Pm, const PlaneMcf &P0, const PlaneMcf &Pp,
+                                             float dt, float out[4]) {
+  float Dz[6];
 #pragma unroll
   for (int h = 0; h < 2; h++) {
     const int c = 1 + 2 * h;
-    const float2 dy = sub2(pr(P0[2][c], P0[2][c + 1]), pr(P0[0][c], P0[0][c + 1]));
-    const float2 dz = sub2(pr(Pp[1][c], Pp[1][c + 1]), pr(Pm[1][c], Pm[1][c + 1]));
-    Dy[c] = dy.x; Dy[c + 1] = dy.y; Dz[c] = dz.x; Dz[c + 1] = dz.y;
+    const float2 dz = sub2(pr(Pp.r1[c], Pp.r1[c + 1]), pr(Pm.r1[c], Pm.r1[c + 1]));
+    Dz[c] = dz.x; Dz[c + 1] = dz.y;
   }
-  Dy[0] = P0[2][0] - P0[0][0]; Dy[5] = P0[2][5] - P0[0][5];
-  Dz[0] = Pp[1][0] - Pm[1][0]; Dz[5] = Pp[1][5] - Pm[1][5];
+  Dz[0] = Pp.r1[0] - Pm.r1[0]; Dz[5] = Pp.r1[5] - Pm.r1[5];
 #pragma unroll
   for (int h = 0; h < 2; h++) {
     const int c = 1 + 2 * h;
-    const float *w = P0[1];
+    const float *w = P0.r1, *Dy = P0.dy;
     const float2 f0 = pr(w[c], w[c + 1]);
     const float2 gx = pr(w[c + 1] - w[c - 1], w[c + 2] - w[c]);
     const float2 gy = pr(Dy[c], Dy[c + 1]), gz = pr(Dz[c], Dz[c + 1]);
@@ -164,12 +220,11 @@ __device__ __forceinline__ void mcfFastStrip(const float Pm[3][6], const float P
     // B = g2 - yy, C = g2 - zz the first numerator term is
     //   A fxx + B fyy + C fzz = g2 (sx + sy + sz - 4 f0) - (xx sx + yy sy + zz sz)
     const float2 sx = pr(w[c - 1] + w[c + 1], w[c] + w[c + 2]);
-    const float2 sy = add2(pr(P0[0][c], P0[0][c + 1]), pr(P0[2][c], P0[2][c + 1]));
-    const float2 sz = add2(pr(Pm[1][c], Pm[1][c + 1]), pr(Pp[1][c], Pp[1][c + 1]));
+    const float2 sy = pr(P0.sy[c - 1], P0.sy[c]);
+    const float2 sz = add2(pr(Pm.r1[c], Pm.r1[c + 1]), pr(Pp.r1[c], Pp.r1[c + 1]));
     const float2 Gyx = pr(Dy[c + 1] - Dy[c - 1], Dy[c + 2] - Dy[c]);
     const float2 Gzx = pr(Dz[c + 1] - Dz[c - 1], Dz[c + 2] - Dz[c]);
-    const float2 Gzy = sub2(sub2(pr(Pp[2][c], Pp[2][c + 1]), pr(Pm[2][c], Pm[2][c + 1])),
-                            sub2(pr(Pp[0][c], Pp[0][c + 1]), pr(Pm[0][c], Pm[0][c + 1])));
+    const float2 Gzy = sub2(pr(Pp.dy[c], Pp.dy[c + 1]), pr(Pm.dy[c], Pm.dy[c + 1]));
     const float2 xx = mul2(gx, gx), yy = mul2(gy, gy), zz = mul2(gz, gz);
     const float2 g2 = add2(add2(xx, yy), zz);
     const float2 L = fma2(pr(-4.0f, -4.0f), f0, add2(add2(sx, sy), sz));
@@ -188,16 +243,15 @@ __device__ __forceinline__ void mcfFastStrip(const float Pm[3][6], const float P
 // Fast Jacobi diffusion of four x-consecutive voxels: (phi + dt s6) * 1/(1 + 6 dt),
 // the reference's division replaced by a multiplication with the reciprocal.
 template <bool CLAMP01>
-__device__ __forceinline__ void jacobiFastStrip(const float Pm[3][6], const float P0[3][6],
-                                                const float Pp[3][6], float dt, float out[4]) {
+__device__ __forceinline__ void jacobiFastStrip(const PlaneJac &Pm, const PlaneJac &P0, const PlaneJac &Pp,
+                                                float dt, float out[4]) {
   const float inv = 1.0f / fmaf(6.0f, dt, 1.0f);
 #pragma unroll
   for (int h = 0; h < 2; h++) {
     const int c = 1 + 2 * h;
-    const float *w = P0[1];
-    const float2 sxy = add2(pr(w[c - 1] + w[c + 1], w[c] + w[c + 2]),
-                            add2(pr(P0[0][c], P0[0][c + 1]), pr(P0[2][c], P0[2][c + 1])));
-    const float2 s6 = add2(sxy, add2(pr(Pm[1][c], Pm[1][c + 1]), pr(Pp[1][c], Pp[1][c + 1])));
+    const float *w = P0.r1;
+    const float2 sxy = add2(pr(w[c - 1] + w[c + 1], w[c] + w[c + 2]), pr(P0.sy[c - 1], P0.sy[c]));
+    const float2 s6 = add2(sxy, add2(pr(Pm.r1[c], Pm.r1[c + 1]), pr(Pp.r1[c], Pp.r1[c + 1])));
     const float2 v = mul2(fma2(pr(dt, dt), s6, pr(w[c], w[c + 1])), pr(inv, inv));
     out[2 * h] = CLAMP01 ? __saturatef(v.x) : v.x;
     out[2 * h + 1] = CLAMP01 ? __saturatef(v.y) : v.y;
