@@ -332,6 +332,31 @@ def run_gpu(args, spec, dist: Dist):
                   "roofline": {"bound": "hbm", "achieved": achj, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                                "frac": achj / peaks["hbm_gbs"]}}
 
+    # restriction of the swept field to the next coarser level (downsampleFloatChannelNew):
+    # S bytes read per fine voxel, 4 bytes written per coarse cell (one per 8 fine voxels)
+    restriction = None
+    if not args.no_jacobi:
+        cb3 = (bsx // 2) ** 3
+        dst = G.DeviceBuffer.alloc(n_act * cb3 * 4)
+        for _ in range(max(3, args.warmup)):
+            g._check(g.L.msbg_gpu_downsample_channel(g.h, 0, C.c_void_p(dst.ptr), 0))
+        g.synchronize()
+        lr = g.launch_count()
+        g.event_record(4)
+        for _ in range(args.steps):
+            g._check(g.L.msbg_gpu_downsample_channel(g.h, 0, C.c_void_p(dst.ptr), 0))
+        g.event_record(5)
+        g.synchronize()
+        msr = dist.max(g.event_elapsed_ms(4, 5)) / args.steps
+        dst.free()
+        nbytes = vox * elem + n_act * cb3 * 4
+        restriction = {"kernel": "kDownsample (4^3 Gauss-like weights)", "ms_per_call": msr,
+                       "fine_voxels_per_s": vox * dist.world / (msr / 1e3),
+                       "launches_per_call": (g.launch_count() - lr) // args.steps,
+                       "roofline": {"bound": "hbm", "achieved": nbytes / (msr / 1e3) / 1e9,
+                                    "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                                    "frac": nbytes / (msr / 1e3) / 1e9 / peaks["hbm_gbs"]}}
+
     # e2e through the host-buffer entry point
     e2e = None
     if not args.no_e2e:
@@ -393,6 +418,7 @@ def run_gpu(args, spec, dist: Dist):
         "e2e": e2e,
         "cpu_baseline": cpu,
         "jacobi_sweeps": jacobi,
+        "restriction": restriction,
         "poisson": poisson,
     }
     print(json.dumps(line), flush=True)

@@ -200,6 +200,17 @@ int msbg_gpu_multiply_laplacian(msbg_gpu_ctx *ctx, int chanX, int chanB, int cha
  * smoother below); reverseOrder runs the adjoint order (tile colour 1 first, black
  * cells first). */
 int msbg_gpu_relax(msbg_gpu_ctx *ctx, int chanX, int chanB, int nIter, int reverseOrder);
+/* downsampleFloatChannelNew (src/msbg4.cpp:1035-1379, levelMg = 1, OPT_ALL_CELLS): the
+ * restriction of channel chSrc (FP32, FP16 or uint16 storage) to the next coarser
+ * multigrid level, for every value block.  dDst (device, FP32) receives
+ * nActive * (bs/2)^3 values, block by block in slot order, x fastest.  A coarse cell v
+ * is the sum over the fine cells 2v-1 .. 2v+2 (4 per axis) with weights
+ * (1,3,3,1)x(1,3,3,1)x(1,3,3,1)/512 (G3D_GetGausslikeKernel4x4x4, src/grid.c:30-70); with
+ * simpleAverage != 0 (OPT_SIMPLE_AVERAGE) the mean of its 8 children.  Fine cells
+ * outside the block come from the halo fill with OPT_BC_COARSE_LEVEL (src/halo.h:288-300):
+ * outside the domain, the value at the clamped position; in a block without payload, the
+ * channel's empty value. */
+int msbg_gpu_downsample_channel(msbg_gpu_ctx *ctx, int chSrc, float *dDst, int simpleAverage);
 /* One multigrid V-cycle X = M^{-1} B from X = 0 (the CG preconditioner). */
 int msbg_gpu_vcycle(msbg_gpu_ctx *ctx, int chanX, int chanB);
 /* dotProdChannel (src/msbg.h:3331-3341): FP64-accumulated sum; MSBG_GPU_ERR_NONFINITE

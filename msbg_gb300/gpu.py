@@ -85,6 +85,7 @@ SIGNATURES = {
     "msbg_gpu_poisson_procedural_coefficients": (I, [P, C.c_uint32, I, I, I, I]),
     "msbg_gpu_multiply_laplacian": (I, [P, I, I, I, I]),
     "msbg_gpu_relax": (I, [P, I, I, I, I]),
+    "msbg_gpu_downsample_channel": (I, [P, I, P, I]),
     "msbg_gpu_vcycle": (I, [P, I, I]),
     "msbg_gpu_dot": (I, [P, I, I, C.POINTER(D)]),
     "msbg_gpu_axpby": (I, [P, D, I, D, I]),
@@ -347,6 +348,22 @@ class MultiresSparseGrid:
 
     def vcycle(self, chanX: int, chanB: int):
         self._check(self.L.msbg_gpu_vcycle(self.h, chanX, chanB))
+
+    def downsampleFloatChannelNew(self, chSrc: int, simpleAverage: bool = False) -> np.ndarray:
+        """Restriction of channel chSrc to the next coarser level, per value block:
+        [nActive][(bs/2)^3] float32 (src/msbg4.cpp:1035-1379)."""
+        cb = self.bsx // 2
+        n = self.info().nActive * cb ** 3
+        out = np.empty(n, np.float32)
+        buf = DeviceBuffer.alloc(max(n, 1) * 4)
+        try:
+            self._check(self.L.msbg_gpu_downsample_channel(self.h, chSrc, C.c_void_p(buf.ptr), int(simpleAverage)))
+            if n:
+                self._check(self.L.msbg_gpu_copy_d2h(self.h, _ptr(out), C.c_void_p(buf.ptr), n * 4))
+            self.synchronize()
+        finally:
+            buf.free()
+        return out.reshape(-1, cb ** 3)
 
     def dotProdChannel(self, a: int, b: int) -> float:
         out = C.c_double()

@@ -1055,3 +1055,59 @@ void orc_poisson_coeffs_dense(uint32_t seed, int nx, int ny, int nz, const uint8
         d[i] = (float)(((lx + ux) + (ly + uy)) + (lz + uz));
       }
 }
+
+/* ------------------------------------------------------------------------- */
+/* Restriction to the next coarser multigrid level (src/msbg4.cpp:1035-1379)  */
+/* ------------------------------------------------------------------------- */
+
+/* Fine value at global cell (x, y, z) with the OPT_BC_COARSE_LEVEL halo rule. */
+static float ds_fetch(const orc_grid *g, const int32_t *slot, const void *payload, int x, int y, int z) {
+  const int bs = g->bsx, L = ilog2(bs), m = bs - 1;
+  x = imin(imax(x, 0), g->sx - 1);
+  y = imin(imax(y, 0), g->sy - 1);
+  z = imin(imax(z, 0), g->sz - 1);
+  const int64_t bid = (int64_t)(x >> L) + (int64_t)(y >> L) * g->nbx + (int64_t)(z >> L) * g->nbx * g->nby;
+  const int32_t s = slot[bid];
+  if (s < 0) return (float)g->emptyValue;
+  return (float)load_val(g, payload, (int64_t)s * bs * bs * bs + (((z & m) * bs + (y & m)) << L) + (x & m));
+}
+
+void orc_downsample(const orc_grid *g, const int32_t *slot, const int32_t *activeBids, int32_t nActive,
+                    const void *payload, int simpleAverage, float *out) {
+  const int bs = g->bsx, cb = bs / 2;
+  const float k1[4] = {1.f, 3.f, 3.f, 1.f};
+  float w[4][4][4];
+  for (int k = 0; k < 4; k++)
+    for (int j = 0; j < 4; j++)
+      for (int i = 0; i < 4; i++) w[k][j][i] = k1[k] * k1[j] * k1[i] / 512.f;
+#pragma omp parallel for schedule(static)
+  for (int32_t t = 0; t < nActive; t++) {
+    const int32_t bid = activeBids[t];
+    const int bx = bid % g->nbx, by = (bid / g->nbx) % g->nby, bz = bid / (g->nbx * g->nby);
+    for (int vz = 0; vz < cb; vz++)
+      for (int vy = 0; vy < cb; vy++)
+        for (int vx = 0; vx < cb; vx++) {
+          const int x0 = bx * bs + 2 * vx, y0 = by * bs + 2 * vy, z0 = bz * bs + 2 * vz;
+          float val;
+          if (simpleAverage) {
+            float sum = 0.f;
+            for (int c = 0; c < 8; c++) {  /* iv0..iv7: x fastest, then y, then z */
+              const float f = ds_fetch(g, slot, payload, x0 + (c & 1), y0 + ((c >> 1) & 1), z0 + (c >> 2));
+              sum = c == 0 ? f : sum + f;
+            }
+            val = sum * (1.f / 8.f);
+          } else {
+            float S[4][4] = {{0.f}};
+            for (int k = 0; k < 4; k++)
+              for (int j = 0; j < 4; j++)
+                for (int i = 0; i < 4; i++)
+                  S[j][i] = fmaf(w[k][j][i], ds_fetch(g, slot, payload, x0 - 1 + i, y0 - 1 + j, z0 - 1 + k),
+                                 S[j][i]);
+            float T[4];
+            for (int i = 0; i < 4; i++) T[i] = ((S[0][i] + S[1][i]) + S[2][i]) + S[3][i];
+            val = (T[0] + T[1]) + (T[2] + T[3]);
+          }
+          out[(int64_t)t * cb * cb * cb + ((int64_t)vz * cb + vy) * cb + vx] = val;
+        }
+  }
+}

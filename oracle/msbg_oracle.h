@@ -97,6 +97,19 @@ int orc_pde(const orc_grid *g, const int32_t *slot, const int32_t *activeBids, i
             void *payload, void *payloadTmp, int laplTyp, int constr01, int numIter, float dt,
             float anisAlpha);
 
+/* ---- restriction to the next coarser multigrid level -------------------------
+ * downsampleFloatChannelNew (src/msbg4.cpp:1035-1379) for the value blocks: coarse
+ * cell v of a block (edge bs/2) = sum over the fine cells 2v-1 .. 2v+2 with weights
+ * (1,3,3,1)^3/512 (src/grid.c:30-70); simpleAverage: the mean of the 8 children.
+ * Fine halo as fillHaloBlock_ with OPT_BC_COARSE_LEVEL (src/halo.h:288-300): clamp to
+ * the domain, empty blocks read emptyValue.  out: [nActive][(bs/2)^3] floats.
+ * Summation order (FP32, one rounding per operation): per x offset i and row j,
+ * S[j][i] = fma(w, f, S[j][i]) over the 4 planes; T[i] = ((S0+S1)+S2)+S3 over the
+ * rows; value = (T0+T1)+(T2+T3) -- the reference's 4-wide accumulators and its
+ * horizontal add.  The 8-child mean sums in the reference's order, then * 1/8. */
+void orc_downsample(const orc_grid *g, const int32_t *slot, const int32_t *activeBids, int32_t nActive,
+                    const void *payload, int simpleAverage, float *out);
+
 /* ---- conversions (exposed for tests) ---- */
 uint16_t orc_f32_to_f16(float f);
 float orc_f16_to_f32(uint16_t h);

@@ -69,6 +69,7 @@ def lib():
         L.orc_poisson_mgpcg.argtypes = [P, C.c_int, P, P, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
                                         C.c_int, C.c_int64, C.POINTER(C.c_int), C.POINTER(C.c_double)]
         L.orc_poisson_coeffs_dense.argtypes = [C.c_uint32, C.c_int, C.c_int, C.c_int, P, P, P, P, P]
+        L.orc_downsample.argtypes = [C.POINTER(Grid), P, P, C.c_int32, P, C.c_int, P]
         L.orc_f32_to_f16.argtypes = [C.c_float]
         L.orc_f32_to_f16.restype = C.c_uint16
         L.orc_f16_to_f32.argtypes = [C.c_uint16]
@@ -136,6 +137,17 @@ def pde(g: Grid, slot, active_bids, payload: np.ndarray, lapl_typ: int, constr01
     if rc != 0:
         raise ValueError(f"orc_pde rc={rc}")
     return payload
+
+
+def downsample(g: Grid, slot, active_bids, payload: np.ndarray, simple_average: bool = False) -> np.ndarray:
+    """downsampleFloatChannelNew restated (src/msbg4.cpp:1035-1379): [nActive][(bs/2)^3]."""
+    cb = g.bsx // 2
+    slot = np.ascontiguousarray(slot, np.int32)
+    bids = np.ascontiguousarray(active_bids, np.int32)
+    payload = np.ascontiguousarray(payload)
+    out = np.zeros((len(bids), cb ** 3), np.float32)
+    lib().orc_downsample(C.byref(g), _p(slot), _p(bids), len(bids), _p(payload), int(simple_average), _p(out))
+    return out
 
 
 def surface_pipeline(pts: np.ndarray, res, bsx: int, storage: int = F32, n_iter: int = 20,
