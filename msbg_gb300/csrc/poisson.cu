@@ -801,7 +801,7 @@ static int checkStatus(msbg_gpu_ctx *ctx) {
   MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (st) {
     MSBG_CUDA(ctx, cudaMemsetAsync(ctx->dStatus, 0, sizeof(int), ctx->stream));
-    return fail(ctx, MSBG_GPU_ERR_TIMEOUT, "a smoother tile wait timed out (status %d)", st);
+    return fail(ctx, MSBG_GPU_ERR_TIMEOUT, "a bounded device wait timed out (status bits %d)", st);
   }
   return MSBG_GPU_OK;
 }

@@ -12,7 +12,9 @@
 //   x0 = x1 on each of the 8 level-0 children (the solve's starting point)
 //
 // conv: 3x3x3, zero outside the active cells, BF16 weights W[tap][cin][cout]
-// (tap = (dx+1) + 3(dy+1) + 9(dz+1)), FP32 activations and accumulation.
+// (tap = (dx+1) + 3(dy+1) + 9(dz+1)), FP32 accumulation.  The forward convolutions
+// run on the tensor cores and read their input activations rounded to BF16; the
+// backward convolutions (CUDA cores) use the FP32 activations.
 // Training loss (x* from the plain solver): "coarse" L = ||x1 - avg1(x*)||^2 /
 // ||avg1(x*)||^2, avg1 = mean of the 8 level-0 children (the best coarse starting
 // value), or "residual" L = ||A0 (x0 - x*)||^2 / ||b||^2.  Adam on FP32 master
@@ -263,60 +265,334 @@ __global__ void kWnHeadBack1(const float *__restrict__ d, const double *__restri
 }
 
 // ---------------------------------------------------------------------------------
-// convolutions (CUDA cores; FP32 accumulation)
+// forward convolution on the tensor cores (tcgen05, BF16 x BF16 -> FP32 in TMEM)
 // ---------------------------------------------------------------------------------
-template <int CIN>
-__device__ __forceinline__ void loadIn(const float *__restrict__ a, int64_t j, bool norm, float s0, float s1,
-                                       float *v) {
-  if constexpr (CIN == 2) {
-    const float2 t = reinterpret_cast<const float2 *>(a)[j];
-    v[0] = norm ? t.x * s0 : t.x;
-    v[1] = norm ? t.y * s1 - 1.0f : t.y;
-  } else {
-#pragma unroll
-    for (int i = 0; i < CIN; i += 4) {
-      const float4 t = *reinterpret_cast<const float4 *>(a + j * CIN + i);
-      v[i] = t.x; v[i + 1] = t.y; v[i + 2] = t.z; v[i + 3] = t.w;
-    }
-  }
+// Implicit GEMM per tile of 128 consecutive level-1 cells: D[128][16] = sum over the
+// 27 taps of A_t[128][16] * B_t[16][16]^T, where row r of A_t holds the input channels
+// of the cell at tap t from cell r (BF16, zero where the neighbour is absent; channels
+// beyond CIN are zero) and B_t[o][i] = W[t][i][o] (BF16; outputs beyond COUT are zero).
+// One thread per cell gathers its rows; thread 0 issues one tcgen05.mma per tap
+// (M = 128, N = 16, K = 16) into a 16-column TMEM accumulator and commits it to the
+// mbarrier of the A buffer, which frees the buffer for tap t + 4.  The epilogue reads
+// row r of D with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31), adds the bias and
+// applies the ReLU.  Operands use the K-major, no-swizzle layout of 8-row x 16-byte
+// core matrices: K-adjacent core matrices 128 B apart, row groups 256 B apart.
+namespace tc {
+__device__ __forceinline__ uint32_t sAddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint64_t desc(const void *base) {
+  uint64_t d = (uint64_t)((sAddr(base) >> 4) & 0x3FFF);
+  d |= (uint64_t)(128 >> 4) << 16;  // leading byte offset: K-adjacent core matrices
+  d |= (uint64_t)(256 >> 4) << 32;  // stride byte offset: the next 8 rows
+  d |= (uint64_t)1 << 46;           // descriptor version; base offset 0, no swizzle
+  return d;
 }
+// kind::f16 instruction descriptor: FP32 accumulator, BF16 A and B, both K-major, N, M
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+__device__ __forceinline__ bool tryWait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+               : "=r"(ok)
+               : "r"(sAddr(bar)), "r"(parity)
+               : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool waitBounded(uint64_t *bar, uint32_t parity) {
+  for (int it = 0; it < (1 << 22); it++)
+    if (tryWait(bar, parity)) return true;
+  return false;
+}
+// offset (elements) of row r, channels 8kb..8kb+7 in a 16-wide K-major operand
+__device__ __forceinline__ int coreOff(int r, int kb) { return (r >> 3) * 128 + kb * 64 + (r & 7) * 8; }
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t *>(&h);
+}
+}  // namespace tc
 
-// y[c] = act(sum_tap W[tap]^T x[c + tap] + bias); NORM: the layer-0 input scaling
+constexpr int kTcThreads = 128, kTcBuf = 4;
+
 template <int CIN, int COUT, bool RELU, bool NORM>
-__global__ void __launch_bounds__(256) kConvFwd(WnGeom g, const float *__restrict__ x,
-                                                const __nv_bfloat16 *__restrict__ w, const float *__restrict__ bias,
-                                                const double *__restrict__ sc, float *__restrict__ y) {
-  __shared__ float ws[27 * CIN * COUT];
-  __shared__ float bs[COUT];
-  for (int i = threadIdx.x; i < 27 * CIN * COUT; i += blockDim.x) ws[i] = __bfloat162float(w[i]);
-  if (threadIdx.x < COUT) bs[threadIdx.x] = bias[threadIdx.x];
+__global__ void __launch_bounds__(kTcThreads) kConvTc(WnGeom g, const float *__restrict__ x,
+                                                    const __nv_bfloat16 *__restrict__ w,
+                                                    const float *__restrict__ bias, const double *__restrict__ sc,
+                                                    float *__restrict__ y, int *__restrict__ status) {
+  static_assert(CIN <= 16 && COUT <= 16 && (CIN == 2 || CIN == 16), "padded to K = N = 16");
+  __shared__ __align__(1024) __nv_bfloat16 sA[kTcBuf][128 * 16];
+  __shared__ __align__(1024) __nv_bfloat16 sB[27][16 * 16];
+  __shared__ float sBias[16];
+  __shared__ __align__(8) uint64_t bar[kTcBuf];
+  __shared__ uint32_t tmemSlot;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(tc::sAddr(&tmemSlot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid < kTcBuf) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::sAddr(&bar[tid])));
+  if (tid == 0) asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  for (int i = tid; i < 27 * 16 * 16; i += kTcThreads) {  // B_t[o][i] = W[t][i][o], zero padded
+    const int t = i / 256, o = (i / 16) % 16, c = i % 16;
+    const __nv_bfloat16 v = (o < COUT && c < CIN) ? w[(t * CIN + c) * COUT + o] : __float2bfloat16(0.0f);
+    sB[t][tc::coreOff(o, c >> 3) + (c & 7)] = v;
+  }
+  if (tid < 16) sBias[tid] = tid < COUT ? bias[tid] : 0.0f;
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmemSlot;
   const float s0 = NORM ? (float)sc[1] : 1.f, s1 = NORM ? (float)sc[2] : 1.f;
   const int64_t n = g.nAct << (3 * g.L);
+  const int64_t nTiles = (n + 127) >> 7;
   const int m = g.bs - 1;
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+  uint32_t q = 0;  // MMAs issued by this CTA: buffer q % kTcBuf, use q / kTcBuf
+  bool ok = true;
+
+  // the 16 (padded) input channels of cell c's neighbour at tap t, as 8 BF16 pairs
+  auto gather = [&](int64_t c, int t, uint32_t (&v)[8]) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) v[k] = 0u;
+    if (c >= n) return;
     const int s = (int)(c >> (3 * g.L));
-    const int v = (int)(c & ((1 << (3 * g.L)) - 1));
-    const int lx = v & m, ly = (v >> g.L) & m, lz = v >> (2 * g.L);
-    float acc[COUT];
+    const int vv = (int)(c & ((1 << (3 * g.L)) - 1));
+    const int64_t j = wnNbr(g, s, vv & m, (vv >> g.L) & m, vv >> (2 * g.L), t % 3 - 1, (t / 3) % 3 - 1, t / 9 - 1);
+    if (j < 0) return;
+    if constexpr (CIN == 2) {
+      const float2 a = reinterpret_cast<const float2 *>(x)[j];
+      v[0] = tc::pack2(NORM ? a.x * s0 : a.x, NORM ? a.y * s1 - 1.0f : a.y);
+    } else {
 #pragma unroll
-    for (int o = 0; o < COUT; o++) acc[o] = bs[o];
-    for (int t = 0; t < 27; t++) {
-      const int64_t j = wnNbr(g, s, lx, ly, lz, t % 3 - 1, (t / 3) % 3 - 1, t / 9 - 1);
-      if (j < 0) continue;
-      float xi[CIN];
-      loadIn<CIN>(x, j, NORM, s0, s1, xi);
-      const float *wt = ws + t * CIN * COUT;
-#pragma unroll
-      for (int i = 0; i < CIN; i++)
-#pragma unroll
-        for (int o = 0; o < COUT; o++) acc[o] = fmaf(xi[i], wt[i * COUT + o], acc[o]);
+      for (int k = 0; k < 4; k++) {
+        const float4 a = *reinterpret_cast<const float4 *>(x + j * 16 + 4 * k);
+        v[2 * k] = tc::pack2(a.x, a.y);
+        v[2 * k + 1] = tc::pack2(a.z, a.w);
+      }
     }
+  };
+
+  for (int64_t tile = blockIdx.x; tile < nTiles && ok; tile += gridDim.x) {
+    const int64_t c = (tile << 7) + tid;
+    uint32_t cur[8], nxt[8];
+    gather(c, 0, cur);
+    for (int t = 0; t < 27; t++) {
+      if (t + 1 < 27) gather(c, t + 1, nxt);  // in flight while this tap's row is stored
+      const int b = (int)(q % kTcBuf);
+      const uint32_t use = q / kTcBuf;
+      bool okw = true;
+      if (use > 0) okw = tc::waitBounded(&bar[b], (use - 1) & 1u);  // the MMA that last read buffer b
+      __nv_bfloat16 *A = sA[b];
+      *reinterpret_cast<uint4 *>(A + tc::coreOff(tid, 0)) = make_uint4(cur[0], cur[1], cur[2], cur[3]);
+      *reinterpret_cast<uint4 *>(A + tc::coreOff(tid, 1)) = make_uint4(cur[4], cur[5], cur[6], cur[7]);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      ok = __syncthreads_and(okw);
+      if (!ok) break;
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint64_t ad = tc::desc(A), bd = tc::desc(sB[t]);
+        asm volatile(
+            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(tc::kIdesc), "r"((uint32_t)(t > 0)));
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         tc::sAddr(&bar[b]))
+                     : "memory");
+      }
+      q++;
 #pragma unroll
-    for (int o = 0; o < COUT; o++) y[c * COUT + o] = RELU ? fmaxf(acc[o], 0.f) : acc[o];
+      for (int k = 0; k < 8; k++) cur[k] = nxt[k];
+    }
+    if (!ok) break;
+    // the tile's last MMA (and with it all earlier ones) has completed
+    const uint32_t last = q - 1;
+    ok = __syncthreads_and(tc::waitBounded(&bar[last % kTcBuf], (last / kTcBuf) & 1u));
+    if (!ok) break;
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    uint32_t d[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7]),
+          "=r"(d[8]), "=r"(d[9]), "=r"(d[10]), "=r"(d[11]), "=r"(d[12]), "=r"(d[13]), "=r"(d[14]), "=r"(d[15])
+        : "r"(tmem + ((uint32_t)(warp * 32) << 16)));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    if (c < n) {
+      float o[16];
+#pragma unroll
+      for (int k = 0; k < 16; k++) {
+        const float v = __uint_as_float(d[k]) + sBias[k];
+        o[k] = RELU ? fmaxf(v, 0.0f) : v;
+      }
+      if constexpr (COUT == 16) {
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+          reinterpret_cast<float4 *>(y + c * 16)[k] = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < COUT; k++) y[c * COUT + k] = o[k];
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+  }
+  if (!ok && tid == 0) atomicOr(status, 4);
+  // every committed MMA has been waited for on the normal path; after a timeout,
+  // wait (bounded) for the last one before the accumulator is freed
+  if (!ok && tid == 0 && q > 0) tc::waitBounded(&bar[(q - 1) % kTcBuf], ((q - 1) / kTcBuf) & 1u);
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmem));
   }
 }
 
+// The same convolution for level-1 blocks of edge 16 with the gather done by the
+// tensor core's operand addressing.  A tile is 8 rows of 16 cells (y0..y0+7 of one
+// plane lz of one block).  Its input neighbourhood (planes lz-1..lz+1, rows
+// y0-1..y0+8, columns -1..16) is staged once, as BF16, in three copies shifted by
+// dx = -1, 0, +1: copy dx holds at column x the input of column x + dx, rows 16 cells
+// apart.  Row r = 16 y + x of the tap (dx, dy, dz) operand is then row
+// ((dz+1) 10 + dy+1) 16 + r of copy dx, so each tap's A operand is a shifted
+// descriptor into the staged copy (8-row core matrices 128 B apart, the two channel
+// halves a copy-plane apart) and the 27 MMAs issue back to back.
+constexpr int kStRows = 3 * 10 * 16;            // staged rows per copy and channel half
+constexpr int kStHalf = kStRows * 8;            // elements per channel half (16 B rows)
+constexpr int kStCopy = 2 * kStHalf;            // elements per shifted copy
+
+template <int CIN, int COUT, bool RELU, bool NORM>
+__global__ void __launch_bounds__(kTcThreads) kConvTcStaged(WnGeom g, const float *__restrict__ x,
+                                                          const __nv_bfloat16 *__restrict__ w,
+                                                          const float *__restrict__ bias,
+                                                          const double *__restrict__ sc, float *__restrict__ y,
+                                                          int *__restrict__ status) {
+  static_assert(CIN <= 16 && COUT <= 16 && (CIN == 2 || CIN == 16), "padded to K = N = 16");
+  extern __shared__ __align__(1024) unsigned char wnSmem[];
+  __nv_bfloat16 *sX = reinterpret_cast<__nv_bfloat16 *>(wnSmem);   // [3 copies][2 halves][kStRows][8]
+  __nv_bfloat16 *sB = sX + 3 * kStCopy;                              // [27][16 x 16] core-matrix layout
+  __shared__ float sBias[16];
+  __shared__ int nb[27];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmemSlot;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(tc::sAddr(&tmemSlot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::sAddr(&bar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int i = tid; i < 27 * 16 * 16; i += kTcThreads) {  // B_t[o][i] = W[t][i][o], zero padded
+    const int t = i / 256, o = (i / 16) % 16, c = i % 16;
+    const __nv_bfloat16 v = (o < COUT && c < CIN) ? w[(t * CIN + c) * COUT + o] : __float2bfloat16(0.0f);
+    sB[t * 256 + tc::coreOff(o, c >> 3) + (c & 7)] = v;
+  }
+  if (tid < 16) sBias[tid] = tid < COUT ? bias[tid] : 0.0f;
+  const float s0 = NORM ? (float)sc[1] : 1.f, s1 = NORM ? (float)sc[2] : 1.f;
+  const int64_t n = g.nAct << 12;  // 16^3 cells per block
+  const int64_t nTiles = n >> 7;
+  uint32_t phase = 0;
+  bool ok = true;
+  for (int64_t tile = blockIdx.x; tile < nTiles && ok; tile += gridDim.x) {
+    const int s = (int)(tile >> 5), lz = (int)((tile >> 1) & 15), y0 = (int)(tile & 1) * 8;
+    __syncthreads();  // the previous tile's staged data and neighbour table are no longer read
+    if (tid < 27) nb[tid] = g.nbr27[(int64_t)s * 27 + tid];
+    __syncthreads();
+    // stage the neighbourhood: 3 planes x 10 rows x 18 columns of input cells
+    for (int e = tid; e < 3 * 10 * 18; e += kTcThreads) {
+      const int xi = e % 18, yi = (e / 18) % 10, zi = e / 180;
+      const int cx = xi - 1, cy = y0 + yi - 1, cz = lz + zi - 1;
+      const int ox = cx < 0 ? -1 : (cx > 15 ? 1 : 0), oy = cy < 0 ? -1 : (cy > 15 ? 1 : 0),
+                oz = cz < 0 ? -1 : (cz > 15 ? 1 : 0);
+      const int sn = nb[(ox + 1) + 3 * (oy + 1) + 9 * (oz + 1)];
+      uint32_t v[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+      if (sn >= 0) {
+        const int64_t j = ((int64_t)sn << 12) + (((cz & 15) << 4) + (cy & 15)) * 16 + (cx & 15);
+        if constexpr (CIN == 2) {
+          const float2 a = reinterpret_cast<const float2 *>(x)[j];
+          v[0] = tc::pack2(NORM ? a.x * s0 : a.x, NORM ? a.y * s1 - 1.0f : a.y);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            const float4 a = *reinterpret_cast<const float4 *>(x + j * 16 + 4 * k);
+            v[2 * k] = tc::pack2(a.x, a.y);
+            v[2 * k + 1] = tc::pack2(a.z, a.w);
+          }
+        }
+      }
+      const int srow = (zi * 10 + yi) * 16;
+#pragma unroll
+      for (int d = 0; d < 3; d++) {  // copy of shift dx = d - 1 holds this cell at column cx - dx
+        const int col = cx - (d - 1);
+        if (col < 0 || col > 15) continue;
+        __nv_bfloat16 *dst = sX + d * kStCopy + (srow + col) * 8;
+        *reinterpret_cast<uint4 *>(dst) = make_uint4(v[0], v[1], v[2], v[3]);
+        *reinterpret_cast<uint4 *>(dst + kStHalf) = make_uint4(v[4], v[5], v[6], v[7]);
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    const uint32_t tmem = tmemSlot;
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll 1
+      for (int t = 0; t < 27; t++) {
+        const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
+        const __nv_bfloat16 *A = sX + (dx + 1) * kStCopy + (((dz + 1) * 10 + dy + 1) * 16) * 8;
+        uint64_t ad = (uint64_t)((tc::sAddr(A) >> 4) & 0x3FFF);
+        ad |= (uint64_t)((kStHalf * 2) >> 4) << 16;  // leading byte offset: the other channel half
+        ad |= (uint64_t)(128 >> 4) << 32;            // stride byte offset: the next 8 rows
+        ad |= (uint64_t)1 << 46;
+        const uint64_t bd = tc::desc(sB + t * 256);
+        asm volatile(
+            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(tc::kIdesc), "r"((uint32_t)(t > 0)));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       tc::sAddr(&bar))
+                   : "memory");
+    }
+    ok = __syncthreads_and(tc::waitBounded(&bar, phase));
+    phase ^= 1u;
+    if (!ok) break;
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    uint32_t d[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7]),
+          "=r"(d[8]), "=r"(d[9]), "=r"(d[10]), "=r"(d[11]), "=r"(d[12]), "=r"(d[13]), "=r"(d[14]), "=r"(d[15])
+        : "r"(tmem + ((uint32_t)(warp * 32) << 16)));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    const int64_t c = (tile << 7) + tid;
+    float o[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      const float v = __uint_as_float(d[k]) + sBias[k];
+      o[k] = RELU ? fmaxf(v, 0.0f) : v;
+    }
+    if constexpr (COUT == 16) {
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        reinterpret_cast<float4 *>(y + c * 16)[k] = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < COUT; k++) y[c * COUT + k] = o[k];
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+  }
+  if (!ok && tid == 0) atomicOr(status, 4);
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmemSlot));
+  }
+}
+constexpr size_t kStSmem = (size_t)(3 * kStCopy + 27 * 256) * sizeof(__nv_bfloat16);
+
+// ---------------------------------------------------------------------------------
+// backward convolutions (CUDA cores; FP32)
+// ---------------------------------------------------------------------------------
 // gx[c][i] = sum_tap sum_o W[tap][i][o] * gpre[c - tap][o], gpre = gy * (y > 0) when
 // the layer has a ReLU.  Written for the layers above the input only.
 template <int CIN, int COUT, bool RELU>
@@ -464,6 +740,15 @@ void warmNetFree(WarmNetState *w) {
   delete w;
 }
 
+// persistent tensor-core convolutions: ctasPerSm resident CTAs per SM (each holds 32
+// TMEM columns of the 512)
+static unsigned wnTcGrid(int64_t n, int ctasPerSm) {
+  int dev = 0, nSm = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&nSm, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t tiles = (n + 127) / 128, cap = (int64_t)nSm * ctasPerSm;
+  return (unsigned)(tiles < 1 ? 1 : tiles < cap ? tiles : cap);
+}
+
 static unsigned wnGrid(int64_t n) {
   int64_t g = (n + 255) / 256;
   if (g > 152 * 8) g = 152 * 8;
@@ -542,14 +827,33 @@ static int wnForward(msbg_gpu_ctx *ctx, const float *b0, float *x0) {
   MSBG_LAUNCH(ctx, kWnInputs, (unsigned)w->nPart, kRedThreads, 0, b0, (const float *)ps->f32.d[1], L1, w->n1,
               (float2 *)w->act[0], w->dPart);
   MSBG_LAUNCH(ctx, kWnScales, 1, kRedThreads, 0, w->dPart, w->nPart, w->n1, w->dScal);
-  const unsigned gr = wnGrid(w->n1);
-  MSBG_LAUNCH(ctx, (kConvFwd<2, 16, true, true>), gr, 256, 0, g, w->act[0], w->wq[0], w->bias[0], w->dScal, w->act[1]);
-  MSBG_LAUNCH(ctx, (kConvFwd<16, 16, true, false>), gr, 256, 0, g, w->act[1], w->wq[1], w->bias[1], w->dScal,
-              w->act[2]);
-  MSBG_LAUNCH(ctx, (kConvFwd<16, 16, true, false>), gr, 256, 0, g, w->act[2], w->wq[2], w->bias[2], w->dScal,
-              w->act[3]);
-  MSBG_LAUNCH(ctx, (kConvFwd<16, 2, false, false>), gr, 256, 0, g, w->act[3], w->wq[3], w->bias[3], w->dScal,
-              w->act[4]);
+  const unsigned gt = wnTcGrid(w->n1, g.bs == 16 ? 3 : 4);  // 3: the staged form's 58.5 KB shared memory
+  if (g.bs == 16) {  // staged-neighbourhood tensor-core convolutions
+    static bool attr = false;
+    if (!attr) {
+      MSBG_CUDA(ctx, cudaFuncSetAttribute(kConvTcStaged<2, 16, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStSmem));
+      MSBG_CUDA(ctx, cudaFuncSetAttribute(kConvTcStaged<16, 16, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStSmem));
+      MSBG_CUDA(ctx, cudaFuncSetAttribute(kConvTcStaged<16, 2, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStSmem));
+      attr = true;
+    }
+    MSBG_LAUNCH(ctx, (kConvTcStaged<2, 16, true, true>), gt, kTcThreads, kStSmem, g, w->act[0], w->wq[0], w->bias[0],
+                w->dScal, w->act[1], ctx->dStatus);
+    MSBG_LAUNCH(ctx, (kConvTcStaged<16, 16, true, false>), gt, kTcThreads, kStSmem, g, w->act[1], w->wq[1],
+                w->bias[1], w->dScal, w->act[2], ctx->dStatus);
+    MSBG_LAUNCH(ctx, (kConvTcStaged<16, 16, true, false>), gt, kTcThreads, kStSmem, g, w->act[2], w->wq[2],
+                w->bias[2], w->dScal, w->act[3], ctx->dStatus);
+    MSBG_LAUNCH(ctx, (kConvTcStaged<16, 2, false, false>), gt, kTcThreads, kStSmem, g, w->act[3], w->wq[3],
+                w->bias[3], w->dScal, w->act[4], ctx->dStatus);
+  } else {
+  MSBG_LAUNCH(ctx, (kConvTc<2, 16, true, true>), gt, kTcThreads, 0, g, w->act[0], w->wq[0], w->bias[0], w->dScal,
+              w->act[1], ctx->dStatus);
+  MSBG_LAUNCH(ctx, (kConvTc<16, 16, true, false>), gt, kTcThreads, 0, g, w->act[1], w->wq[1], w->bias[1], w->dScal,
+              w->act[2], ctx->dStatus);
+  MSBG_LAUNCH(ctx, (kConvTc<16, 16, true, false>), gt, kTcThreads, 0, g, w->act[2], w->wq[2], w->bias[2], w->dScal,
+              w->act[3], ctx->dStatus);
+  MSBG_LAUNCH(ctx, (kConvTc<16, 2, false, false>), gt, kTcThreads, 0, g, w->act[3], w->wq[3], w->bias[3], w->dScal,
+              w->act[4], ctx->dStatus);
+  }
   MSBG_LAUNCH(ctx, kWnHead, gridFor(w->n2, 256), 256, 0, (const float2 *)w->act[4], w->dScal, L1, w->n2, w->x1, x0);
   return MSBG_GPU_OK;
 }

@@ -108,8 +108,10 @@ class WarmNet:
             c.append(np.zeros(cout, np.float32))
         return WarmNet(W, c)
 
-    def forward(self, b1: np.ndarray, d1: np.ndarray, mask1: np.ndarray):
-        """Level-1 warm start x1 and the cache for backward."""
+    def forward(self, b1: np.ndarray, d1: np.ndarray, mask1: np.ndarray, act_bf16: bool = False):
+        """Level-1 warm start x1 and the cache for backward.  act_bf16: every
+        convolution reads its input activations rounded to BF16, as the tensor-core
+        forward does (the backward pass, like the GPU's, uses the unrounded ones)."""
         act = mask1 > 0
         s = float(np.sqrt(np.mean(b1[act] ** 2))) if act.any() else 1.0
         s = s if s > 0 else 1.0
@@ -118,7 +120,8 @@ class WarmNet:
         Wq = [bf16_round(w) for w in self.W]
         hs = [inp]
         for l in range(4):
-            h = conv(hs[-1], Wq[l], self.c[l].astype(np.float64), mask1)
+            a = bf16_round(hs[-1]) if act_bf16 else hs[-1]
+            h = conv(a, Wq[l], self.c[l].astype(np.float64), mask1)
             if l < 3:
                 h = np.maximum(h, 0.0)
             hs.append(h)
@@ -141,12 +144,12 @@ class WarmNet:
         return gW, gc
 
 
-def loss_and_grads(net: WarmNet, b0, xstar0, mask0, apply_a0, d1, loss: str = "coarse"):
+def loss_and_grads(net: WarmNet, b0, xstar0, mask0, apply_a0, d1, loss: str = "coarse", act_bf16: bool = False):
     """The loss and its gradients (dense level-0 arrays; apply_a0(x) applies the
     level-0 operator)."""
     mask1 = (restrict_sum(mask0.astype(np.float64)) > 0).astype(np.float64)
     b1 = restrict_sum(b0 * mask0)
-    x1, cache = net.forward(b1, d1, mask1)
+    x1, cache = net.forward(b1, d1, mask1, act_bf16)
     x0 = prolong(x1) * mask0
     if loss == "residual":
         e = apply_a0(x0 - xstar0)

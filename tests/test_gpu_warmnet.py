@@ -36,10 +36,12 @@ def _level1_diag(prob):
     return 0.5 * (_sum8(prob.d) - 2.0 * (_sum8(cx) + _sum8(cy) + _sum8(cz)))
 
 
-@pytest.fixture(scope="module")
-def setup(gpulib, port):
+@pytest.fixture(scope="module", params=[16, 32])
+def setup(gpulib, port, request):
+    """bs 16: level-1 blocks of edge 8 (per-tap tensor-core gather); bs 32: edge 16
+    (the staged-neighbourhood tensor-core convolution)."""
     G, P = gpulib, port
-    res, bs = 128, 16
+    res, bs = 128, request.param
     pts = W.sphere_cloud(res, 6, 3000, seed=W.workload_seed(4, 1))
     g = G.MultiresSparseGrid(res, res, res, bs, 3, G.F32)
     d = g.to_device(pts)
@@ -77,8 +79,9 @@ def test_forward_loss_and_gradients_match_restatement(setup, loss):
 
     mask0 = (prob.act > 0).astype(np.float64)
     d1 = _level1_diag(prob)
+    # the tensor-core forward reads BF16-rounded activations
     L, gW, gc, x0 = WN.loss_and_grads(net, b.astype(np.float64), xs.astype(np.float64), mask0,
-                                      prob.apply, d1, loss=loss)
+                                      prob.apply, d1, loss=loss, act_bf16=True)
     g.warmnet_predict(CH_B, CH_X)
     x0_gpu = prob.dense(g.payload(CH_X))
     assert rel_l2(x0_gpu, x0) < 2e-4
@@ -91,6 +94,8 @@ def test_forward_loss_and_gradients_match_restatement(setup, loss):
 
 def test_training_lowers_loss_and_initial_residual(setup):
     G, P, g, prob = setup
+    if prob.bs != 16:
+        pytest.skip("training is covered on the bs-16 layout")
     rng = np.random.default_rng(12)
     net = WN.WarmNet.init(7)
     g.warmnet_set(net.W, net.c)
