@@ -458,7 +458,7 @@ constexpr int kStHalf = kStRows * 8;            // elements per channel half (16
 constexpr int kStCopy = 2 * kStHalf;            // elements per shifted copy
 
 template <int CIN, int COUT, bool RELU, bool NORM>
-__global__ void __launch_bounds__(kTcThreads) kConvTcStaged(WnGeom g, const float *__restrict__ x,
+__global__ void __launch_bounds__(kTcThreads, 3) kConvTcStaged(WnGeom g, const float *__restrict__ x,
                                                           const __nv_bfloat16 *__restrict__ w,
                                                           const float *__restrict__ bias,
                                                           const double *__restrict__ sc, float *__restrict__ y,
@@ -468,7 +468,6 @@ __global__ void __launch_bounds__(kTcThreads) kConvTcStaged(WnGeom g, const floa
   __nv_bfloat16 *sX = reinterpret_cast<__nv_bfloat16 *>(wnSmem);   // [3 copies][2 halves][kStRows][8]
   __nv_bfloat16 *sB = sX + 3 * kStCopy;                              // [27][16 x 16] core-matrix layout
   __shared__ float sBias[16];
-  __shared__ int nb[27];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tmemSlot;
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -491,30 +490,56 @@ __global__ void __launch_bounds__(kTcThreads) kConvTcStaged(WnGeom g, const floa
   const int64_t nTiles = n >> 7;
   uint32_t phase = 0;
   bool ok = true;
-  for (int64_t tile = blockIdx.x; tile < nTiles && ok; tile += gridDim.x) {
+  // A tile's neighbourhood: 3 planes x 10 rows x 18 columns of input cells, PER per
+  // thread.  load issues all of a thread's global loads (into raw); stage converts
+  // them to BF16 and writes the three shifted copies.
+  constexpr int NE = 3 * 10 * 18, PER = (NE + kTcThreads - 1) / kTcThreads;
+  float4 raw[PER][CIN == 2 ? 1 : 4];
+  bool have[PER];
+  auto load = [&](int64_t tile) {
     const int s = (int)(tile >> 5), lz = (int)((tile >> 1) & 15), y0 = (int)(tile & 1) * 8;
-    __syncthreads();  // the previous tile's staged data and neighbour table are no longer read
-    if (tid < 27) nb[tid] = g.nbr27[(int64_t)s * 27 + tid];
-    __syncthreads();
-    // stage the neighbourhood: 3 planes x 10 rows x 18 columns of input cells
-    for (int e = tid; e < 3 * 10 * 18; e += kTcThreads) {
+    const int32_t *nbg = g.nbr27 + (int64_t)s * 27;
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+      const int e = tid + k * kTcThreads;
+      have[k] = false;
+      if (e < NE) {
+        const int xi = e % 18, yi = (e / 18) % 10, zi = e / 180;
+        const int cx = xi - 1, cy = y0 + yi - 1, cz = lz + zi - 1;
+        const int ox = cx < 0 ? -1 : (cx > 15 ? 1 : 0), oy = cy < 0 ? -1 : (cy > 15 ? 1 : 0),
+                  oz = cz < 0 ? -1 : (cz > 15 ? 1 : 0);
+        const int sn = (ox | oy | oz) ? nbg[(ox + 1) + 3 * (oy + 1) + 9 * (oz + 1)] : s;
+        if (sn >= 0) {
+          have[k] = true;
+          const int64_t j = ((int64_t)sn << 12) + (((cz & 15) << 4) + (cy & 15)) * 16 + (cx & 15);
+          if constexpr (CIN == 2) {
+            const float2 v = reinterpret_cast<const float2 *>(x)[j];
+            raw[k][0] = make_float4(v.x, v.y, 0.f, 0.f);
+          } else {
+#pragma unroll
+            for (int q = 0; q < 4; q++) raw[k][q] = *reinterpret_cast<const float4 *>(x + j * 16 + 4 * q);
+          }
+        }
+      }
+    }
+  };
+  auto stage = [&]() {
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+      const int e = tid + k * kTcThreads;
+      if (e >= NE) continue;
       const int xi = e % 18, yi = (e / 18) % 10, zi = e / 180;
-      const int cx = xi - 1, cy = y0 + yi - 1, cz = lz + zi - 1;
-      const int ox = cx < 0 ? -1 : (cx > 15 ? 1 : 0), oy = cy < 0 ? -1 : (cy > 15 ? 1 : 0),
-                oz = cz < 0 ? -1 : (cz > 15 ? 1 : 0);
-      const int sn = nb[(ox + 1) + 3 * (oy + 1) + 9 * (oz + 1)];
+      const int cx = xi - 1;
       uint32_t v[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
-      if (sn >= 0) {
-        const int64_t j = ((int64_t)sn << 12) + (((cz & 15) << 4) + (cy & 15)) * 16 + (cx & 15);
+      if (have[k]) {
         if constexpr (CIN == 2) {
-          const float2 a = reinterpret_cast<const float2 *>(x)[j];
+          const float4 a = raw[k][0];
           v[0] = tc::pack2(NORM ? a.x * s0 : a.x, NORM ? a.y * s1 - 1.0f : a.y);
         } else {
 #pragma unroll
-          for (int k = 0; k < 4; k++) {
-            const float4 a = *reinterpret_cast<const float4 *>(x + j * 16 + 4 * k);
-            v[2 * k] = tc::pack2(a.x, a.y);
-            v[2 * k + 1] = tc::pack2(a.z, a.w);
+          for (int q = 0; q < 4; q++) {
+            v[2 * q] = tc::pack2(raw[k][q].x, raw[k][q].y);
+            v[2 * q + 1] = tc::pack2(raw[k][q].z, raw[k][q].w);
           }
         }
       }
@@ -528,21 +553,32 @@ __global__ void __launch_bounds__(kTcThreads) kConvTcStaged(WnGeom g, const floa
         *reinterpret_cast<uint4 *>(dst + kStHalf) = make_uint4(v[4], v[5], v[6], v[7]);
       }
     }
+  };
+  // descriptors of the first tap's operands; tap t adds its byte offset (>> 4) to the
+  // start-address field (all addresses stay below 256 KB)
+  uint64_t adBase = (uint64_t)((tc::sAddr(sX) >> 4) & 0x3FFF);
+  adBase |= (uint64_t)((kStHalf * 2) >> 4) << 16;  // leading byte offset: the other channel half
+  adBase |= (uint64_t)(128 >> 4) << 32;            // stride byte offset: the next 8 rows
+  adBase |= (uint64_t)1 << 46;
+  const uint64_t bdBase = tc::desc(sB);
+
+  int64_t tile = blockIdx.x;
+  if (tile < nTiles) load(tile);
+  for (; tile < nTiles && ok; tile += gridDim.x) {
+    // the previous tile's MMAs have completed (waited below), so its staged copies
+    // may be overwritten
+    stage();
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     const uint32_t tmem = tmemSlot;
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;");
-#pragma unroll 1
+#pragma unroll
       for (int t = 0; t < 27; t++) {
         const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
-        const __nv_bfloat16 *A = sX + (dx + 1) * kStCopy + (((dz + 1) * 10 + dy + 1) * 16) * 8;
-        uint64_t ad = (uint64_t)((tc::sAddr(A) >> 4) & 0x3FFF);
-        ad |= (uint64_t)((kStHalf * 2) >> 4) << 16;  // leading byte offset: the other channel half
-        ad |= (uint64_t)(128 >> 4) << 32;            // stride byte offset: the next 8 rows
-        ad |= (uint64_t)1 << 46;
-        const uint64_t bd = tc::desc(sB + t * 256);
+        const uint32_t aOff = ((dx + 1) * kStCopy + (((dz + 1) * 10 + dy + 1) * 16) * 8) * 2;  // bytes
+        const uint64_t ad = adBase + (aOff >> 4), bd = bdBase + ((uint32_t)(t * 256 * 2) >> 4);
         asm volatile(
             "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
@@ -552,6 +588,8 @@ __global__ void __launch_bounds__(kTcThreads) kConvTcStaged(WnGeom g, const floa
                        tc::sAddr(&bar))
                    : "memory");
     }
+    // the next tile's loads fly while the tensor core works on this one
+    if (tile + gridDim.x < nTiles) load(tile + gridDim.x);
     ok = __syncthreads_and(tc::waitBounded(&bar, phase));
     phase ^= 1u;
     if (!ok) break;
