@@ -113,6 +113,19 @@ __global__ void kVolInit(double *__restrict__ vs, int nVol, double tol, int32_t 
   }
 }
 
+// after every volume met the tolerance on its recurrence residual: vs[rr] now holds
+// the true ||b - A x||^2 of each volume; volumes that miss the tolerance on it resume
+__global__ void kVolRecheck(const double *__restrict__ vs, int nVol, double tol, int32_t *__restrict__ conv,
+                            int32_t *__restrict__ counters) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nVol) return;
+  const double bn = vs[kVsBn * nVol + v], rr = vs[kVsRr * nVol + v];
+  if (conv[v] != 0 && !(bn == 0.0 || sqrt(rr) <= tol * sqrt(bn))) {
+    conv[v] = 0;
+    atomicSub(counters, 1);
+  }
+}
+
 template <typename V>
 __global__ void __launch_bounds__(256) kUpdateXRVol(const double *__restrict__ alpha, const int32_t *__restrict__ vol,
                                                     int log2vpb, const V *__restrict__ p, const V *__restrict__ q,
@@ -182,6 +195,8 @@ int segDot(msbg_gpu_ctx *ctx, BatchState *bs, const float *a, const float *b, do
   return MSBG_GPU_OK;
 }
 
+constexpr double kRecurMargin = 0.8;
+
 // One PCG iteration on every volume (what the graph holds).
 int batchIteration(msbg_gpu_ctx *ctx, BatchState *bs, float *x, double tol) {
   PoissonState *ps = ctx->poisson;
@@ -197,7 +212,9 @@ int batchIteration(msbg_gpu_ctx *ctx, BatchState *bs, float *x, double tol) {
   MSBG_LAUNCH(ctx, kUpdateXRVol<float>, (unsigned)bs->updGrid, 256, 0, vs + kVsAlpha * nV, bs->volOfSlot, lv, p, s,
               x, r, n / 4);
   if ((rc = segDot(ctx, bs, r, r, vs + kVsRr * nV))) return rc;
-  MSBG_LAUNCH(ctx, kVolScalars, 1, 1024, 0, vs, nV, 1, tol, bs->conv, bs->dCounters);
+  // the recurrence residual may drift from the true one by a few FP32 roundings: stop
+  // it at kRecurMargin * tol so that the true-residual confirmation rarely restarts
+  MSBG_LAUNCH(ctx, kVolScalars, 1, 1024, 0, vs, nV, 1, kRecurMargin * tol, bs->conv, bs->dCounters);
   if ((rc = batchVcycle(ctx, z, r))) return rc;
   if ((rc = segDot(ctx, bs, r, z, vs + kVsRzn * nV))) return rc;
   MSBG_LAUNCH(ctx, kVolScalars, 1, 1024, 0, vs, nV, 2, tol, bs->conv, bs->dCounters);
@@ -340,32 +357,54 @@ extern "C" int msbg_gpu_batch_mgpcg_solve(msbg_gpu_ctx *ctx, int chanX, int chan
   if ((rc = segDot(ctx, bs, r, z, bs->vs + kVsRz * nV))) return rc;
 
   const bool graphOk = useGraph && bs->graph && bs->graphKey[0] == x && bs->graphKey[1] == b && bs->graphTol == tol;
-  int it = 0;
-  for (it = 1; it <= maxIter; it++) {
-    if (useGraph && !graphOk && it == 2) {  // capture after one eager iteration (caches warm)
-      if (bs->graph) { cudaGraphExecDestroy(bs->graph); bs->graph = nullptr; }
-      cudaGraph_t gr;
-      MSBG_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      const int64_t l0 = ctx->launches;
-      rc = batchIteration(ctx, bs, x, tol);
-      cudaError_t ce = cudaStreamEndCapture(ctx->stream, &gr);
-      if (rc) return rc;
-      MSBG_CUDA(ctx, ce);
-      MSBG_CUDA(ctx, cudaGraphInstantiate(&bs->graph, gr, 0));
-      cudaGraphDestroy(gr);
-      ctx->launches = l0;  // captured, not launched
-      bs->graphKey[0] = x; bs->graphKey[1] = b; bs->graphTol = tol;
+  int it = 1;
+  // iterations it, it+1, ... until every volume has met the tolerance on its
+  // recurrence residual (it is then the last iteration run) or maxIter has run
+  auto iterate = [&]() -> int {
+    for (; it <= maxIter; it++) {
+      if (useGraph && !graphOk && it == 2) {  // capture after one eager iteration (caches warm)
+        if (bs->graph) { cudaGraphExecDestroy(bs->graph); bs->graph = nullptr; }
+        cudaGraph_t gr;
+        MSBG_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        const int64_t l0 = ctx->launches;
+        int rc2 = batchIteration(ctx, bs, x, tol);
+        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &gr);
+        if (rc2) return rc2;
+        MSBG_CUDA(ctx, ce);
+        MSBG_CUDA(ctx, cudaGraphInstantiate(&bs->graph, gr, 0));
+        cudaGraphDestroy(gr);
+        ctx->launches = l0;  // captured, not launched
+        bs->graphKey[0] = x; bs->graphKey[1] = b; bs->graphTol = tol;
+      }
+      if (useGraph && bs->graph && (graphOk || it >= 2)) {
+        MSBG_CUDA(ctx, cudaGraphLaunch(bs->graph, ctx->stream));
+        ctx->launches += 1;
+      } else {
+        int rc2 = batchIteration(ctx, bs, x, tol);
+        if (rc2) return rc2;
+      }
+      MSBG_CUDA(ctx, cudaEventRecord(ev[it], ctx->stream));
+      MSBG_CUDA(ctx, cudaMemcpyAsync(bs->hCounters, bs->dCounters, 8, cudaMemcpyDeviceToHost, ctx->stream));
+      MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      if (bs->hCounters[0] >= nV) return MSBG_GPU_OK;
     }
-    if (useGraph && bs->graph && (graphOk || it >= 2)) {
-      MSBG_CUDA(ctx, cudaGraphLaunch(bs->graph, ctx->stream));
-      ctx->launches += 1;
-    } else {
-      if ((rc = batchIteration(ctx, bs, x, tol))) return rc;
-    }
-    MSBG_CUDA(ctx, cudaEventRecord(ev[it], ctx->stream));
+    return MSBG_GPU_OK;
+  };
+  if ((rc = iterate())) return rc;
+  // Confirm on the true residual (as the single solve does): volumes whose
+  // ||b - A x|| misses the tolerance resume CG from it; the others stay frozen.
+  for (int check = 0; check < 8 && it < maxIter && bs->hCounters[0] >= nV; check++) {
+    if ((rc = batchApply(ctx, x, b, r, 1))) return rc;
+    if ((rc = segDot(ctx, bs, r, r, bs->vs + kVsRr * nV))) return rc;
+    MSBG_LAUNCH(ctx, kVolRecheck, (unsigned)((nV + 127) / 128), 128, 0, bs->vs, nV, tol, bs->conv, bs->dCounters);
     MSBG_CUDA(ctx, cudaMemcpyAsync(bs->hCounters, bs->dCounters, 8, cudaMemcpyDeviceToHost, ctx->stream));
     MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (bs->hCounters[0] >= nV) break;
+    if ((rc = batchVcycle(ctx, z, r))) return rc;
+    MSBG_CUDA(ctx, cudaMemcpyAsync(p, z, (size_t)n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    if ((rc = segDot(ctx, bs, r, z, bs->vs + kVsRz * nV))) return rc;
+    it++;
+    if ((rc = iterate())) return rc;
   }
   if (it > maxIter) it = maxIter;
   // per-volume results: iterations, time to tolerance, FP64-checked relative residual
@@ -398,7 +437,7 @@ extern "C" int msbg_gpu_batch_mgpcg_solve(msbg_gpu_ctx *ctx, int chanX, int chan
   MSBG_CUDA(ctx, cudaMemcpy(&st, ctx->dStatus, sizeof(int), cudaMemcpyDeviceToHost));
   if (st) {
     MSBG_CUDA(ctx, cudaMemset(ctx->dStatus, 0, sizeof(int)));
-    return fail(ctx, MSBG_GPU_ERR_TIMEOUT, "a smoother tile wait timed out (status %d)", st);
+    return fail(ctx, MSBG_GPU_ERR_TIMEOUT, "a bounded device wait timed out (status bits %d)", st);
   }
   return MSBG_GPU_OK;
 }

@@ -63,7 +63,8 @@ def test_batch_matches_fp64_solve(batch):
     g.upload_payload(prob.payload(b), CH_B)
     g.fill(0.0, CH_X)
     its, ms, rel, tot = g.batch_mgpcg_solve(CH_X, CH_B, tol=1e-6, max_iter=60)
-    assert np.all(its >= 1) and np.all(rel <= 1.5e-6), (its, rel)
+    # convergence is confirmed on the true residual, so every volume meets the tolerance
+    assert np.all(its >= 1) and np.all(rel <= 1e-6), (its, rel)
     assert np.all(ms > 0) and np.all(ms <= tot + 1e-3)
     x = prob.dense(g.payload(CH_X))
     xs, _, _ = prob.solve(b.astype(np.float64), 1e-9, 200)
@@ -81,7 +82,7 @@ def test_volume_iterations_equal_solo_solves(batch):
     g.upload_payload(bpay.astype(np.float32), CH_B)
     g.fill(0.0, CH_X)
     its, ms, rel, tot = g.batch_mgpcg_solve(CH_X, CH_B, tol=1e-6, max_iter=60)
-    assert np.all(rel <= 1.5e-6)
+    assert np.all(rel <= 1e-6)
     for v in range(8):
         solo = np.where((slot_vol == v)[:, None], bpay, 0.0).astype(np.float32)
         g.upload_payload(solo, CH_B)
