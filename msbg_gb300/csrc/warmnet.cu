@@ -444,29 +444,44 @@ __global__ void __launch_bounds__(kTcThreads) kConvTc(WnGeom g, const float *__r
   }
 }
 
-// The same convolution for level-1 blocks of edge 16 with the gather done by the
-// tensor core's operand addressing.  A tile is 8 rows of 16 cells (y0..y0+7 of one
-// plane lz of one block).  Its input neighbourhood (planes lz-1..lz+1, rows
-// y0-1..y0+8, columns -1..16) is staged once, as BF16, in three copies shifted by
-// dx = -1, 0, +1: copy dx holds at column x the input of column x + dx, rows 16 cells
-// apart.  Row r = 16 y + x of the tap (dx, dy, dz) operand is then row
-// ((dz+1) 10 + dy+1) 16 + r of copy dx, so each tap's A operand is a shifted
-// descriptor into the staged copy (8-row core matrices 128 B apart, the two channel
-// halves a copy-plane apart) and the 27 MMAs issue back to back.
-constexpr int kStRows = 3 * 10 * 16;            // staged rows per copy and channel half
-constexpr int kStHalf = kStRows * 8;            // elements per channel half (16 B rows)
-constexpr int kStCopy = 2 * kStHalf;            // elements per shifted copy
+// The same convolution with the gather done by the tensor core's operand
+// addressing.  A tile's input neighbourhood is staged once, as BF16, in copies
+// shifted so that every tap's A operand is a run of consecutive 16-byte rows of one
+// copy: a shifted descriptor (8-row core matrices 128 B apart, the two channel halves
+// a copy-half apart), and the 27 MMAs issue back to back.
+//  - Level-1 blocks of edge 16: a tile is 8 rows of 16 cells (y0..y0+7 of plane lz).
+//    The neighbourhood (planes lz-1..lz+1, rows y0-1..y0+8, columns -1..16) is kept in
+//    three copies shifted by dx = -1, 0, +1 (copy dx holds at column x the input of
+//    column x + dx), rows of 16 cells; row r = 16 y + x of tap (dx, dy, dz) is row
+//    ((dz+1) 10 + dy+1) 16 + r of copy dx.
+//  - Level-1 blocks of edge 8: a tile is two planes lz0, lz0+1 of 8 x 8 cells.  The
+//    neighbourhood (planes lz0-1..lz0+2, rows and columns -1..8) is kept in nine copies
+//    shifted by (dx, dy), planes of 8 x 8; row r = 64 z + 8 y + x of tap (dx, dy, dz)
+//    is row 64 (dz+1) + r of copy (dx, dy).
+template <int BS1> struct StGeom;
+template <> struct StGeom<16> {
+  static constexpr int L = 4, NX = 18, NY = 10, NZ = 3, NCOPY = 3, ROWS = 3 * 10 * 16, TPB_LOG = 5;
+};
+template <> struct StGeom<8> {
+  static constexpr int L = 3, NX = 10, NY = 10, NZ = 4, NCOPY = 9, ROWS = 4 * 64, TPB_LOG = 2;
+};
+template <int BS1>
+constexpr size_t stSmemBytes() {
+  return (size_t)(StGeom<BS1>::NCOPY * 2 * StGeom<BS1>::ROWS * 8 + 27 * 256) * sizeof(__nv_bfloat16);
+}
 
-template <int CIN, int COUT, bool RELU, bool NORM>
-__global__ void __launch_bounds__(kTcThreads, 3) kConvTcStaged(WnGeom g, const float *__restrict__ x,
-                                                          const __nv_bfloat16 *__restrict__ w,
-                                                          const float *__restrict__ bias,
-                                                          const double *__restrict__ sc, float *__restrict__ y,
-                                                          int *__restrict__ status) {
+template <int BS1, int CIN, int COUT, bool RELU, bool NORM>
+__global__ void __launch_bounds__(kTcThreads, BS1 == 16 ? 3 : 2) kConvTcStaged(WnGeom g, const float *__restrict__ x,
+                                                             const __nv_bfloat16 *__restrict__ w,
+                                                             const float *__restrict__ bias,
+                                                             const double *__restrict__ sc, float *__restrict__ y,
+                                                             int *__restrict__ status) {
+  using SG = StGeom<BS1>;
+  constexpr int L = SG::L, m = BS1 - 1, kStHalf = SG::ROWS * 8, kStCopy = 2 * kStHalf;
   static_assert(CIN <= 16 && COUT <= 16 && (CIN == 2 || CIN == 16), "padded to K = N = 16");
   extern __shared__ __align__(1024) unsigned char wnSmem[];
-  __nv_bfloat16 *sX = reinterpret_cast<__nv_bfloat16 *>(wnSmem);   // [3 copies][2 halves][kStRows][8]
-  __nv_bfloat16 *sB = sX + 3 * kStCopy;                              // [27][16 x 16] core-matrix layout
+  __nv_bfloat16 *sX = reinterpret_cast<__nv_bfloat16 *>(wnSmem);   // [copies][2 halves][ROWS][8]
+  __nv_bfloat16 *sB = sX + SG::NCOPY * kStCopy;                      // [27][16 x 16] core-matrix layout
   __shared__ float sBias[16];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tmemSlot;
@@ -486,32 +501,40 @@ __global__ void __launch_bounds__(kTcThreads, 3) kConvTcStaged(WnGeom g, const f
   }
   if (tid < 16) sBias[tid] = tid < COUT ? bias[tid] : 0.0f;
   const float s0 = NORM ? (float)sc[1] : 1.f, s1 = NORM ? (float)sc[2] : 1.f;
-  const int64_t n = g.nAct << 12;  // 16^3 cells per block
+  const int64_t n = g.nAct << (3 * L);
   const int64_t nTiles = n >> 7;
   uint32_t phase = 0;
   bool ok = true;
   // A tile's neighbourhood: 3 planes x 10 rows x 18 columns of input cells, PER per
   // thread.  load issues all of a thread's global loads (into raw); stage converts
   // them to BF16 and writes the three shifted copies.
-  constexpr int NE = 3 * 10 * 18, PER = (NE + kTcThreads - 1) / kTcThreads;
+  constexpr int NE = SG::NX * SG::NY * SG::NZ, PER = (NE + kTcThreads - 1) / kTcThreads;
+  // origin of tile's neighbourhood cell (0, 0, 0) in block coordinates is (-1, oy0-1, oz0-1)
+  auto origin = [](int64_t tile, int &oy0, int &oz0) {
+    const int sub = (int)(tile & ((1 << SG::TPB_LOG) - 1));
+    if constexpr (BS1 == 16) { oy0 = (sub & 1) * 8; oz0 = sub >> 1; }
+    else { oy0 = 0; oz0 = 2 * sub; }
+  };
   float4 raw[PER][CIN == 2 ? 1 : 4];
   bool have[PER];
   auto load = [&](int64_t tile) {
-    const int s = (int)(tile >> 5), lz = (int)((tile >> 1) & 15), y0 = (int)(tile & 1) * 8;
+    const int s = (int)(tile >> SG::TPB_LOG);
+    int oy0, oz0;
+    origin(tile, oy0, oz0);
     const int32_t *nbg = g.nbr27 + (int64_t)s * 27;
 #pragma unroll
     for (int k = 0; k < PER; k++) {
       const int e = tid + k * kTcThreads;
       have[k] = false;
       if (e < NE) {
-        const int xi = e % 18, yi = (e / 18) % 10, zi = e / 180;
-        const int cx = xi - 1, cy = y0 + yi - 1, cz = lz + zi - 1;
-        const int ox = cx < 0 ? -1 : (cx > 15 ? 1 : 0), oy = cy < 0 ? -1 : (cy > 15 ? 1 : 0),
-                  oz = cz < 0 ? -1 : (cz > 15 ? 1 : 0);
+        const int xi = e % SG::NX, yi = (e / SG::NX) % SG::NY, zi = e / (SG::NX * SG::NY);
+        const int cx = xi - 1, cy = oy0 + yi - 1, cz = oz0 + zi - 1;
+        const int ox = cx < 0 ? -1 : (cx > m ? 1 : 0), oy = cy < 0 ? -1 : (cy > m ? 1 : 0),
+                  oz = cz < 0 ? -1 : (cz > m ? 1 : 0);
         const int sn = (ox | oy | oz) ? nbg[(ox + 1) + 3 * (oy + 1) + 9 * (oz + 1)] : s;
         if (sn >= 0) {
           have[k] = true;
-          const int64_t j = ((int64_t)sn << 12) + (((cz & 15) << 4) + (cy & 15)) * 16 + (cx & 15);
+          const int64_t j = ((int64_t)sn << (3 * L)) + ((((cz & m) << L) + (cy & m)) << L) + (cx & m);
           if constexpr (CIN == 2) {
             const float2 v = reinterpret_cast<const float2 *>(x)[j];
             raw[k][0] = make_float4(v.x, v.y, 0.f, 0.f);
@@ -528,7 +551,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) kConvTcStaged(WnGeom g, const f
     for (int k = 0; k < PER; k++) {
       const int e = tid + k * kTcThreads;
       if (e >= NE) continue;
-      const int xi = e % 18, yi = (e / 18) % 10, zi = e / 180;
+      const int xi = e % SG::NX, yi = (e / SG::NX) % SG::NY, zi = e / (SG::NX * SG::NY);
       const int cx = xi - 1;
       uint32_t v[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
       if (have[k]) {
@@ -543,14 +566,27 @@ __global__ void __launch_bounds__(kTcThreads, 3) kConvTcStaged(WnGeom g, const f
           }
         }
       }
-      const int srow = (zi * 10 + yi) * 16;
-#pragma unroll
-      for (int d = 0; d < 3; d++) {  // copy of shift dx = d - 1 holds this cell at column cx - dx
-        const int col = cx - (d - 1);
-        if (col < 0 || col > 15) continue;
-        __nv_bfloat16 *dst = sX + d * kStCopy + (srow + col) * 8;
+      auto put = [&](int copy, int row) {
+        __nv_bfloat16 *dst = sX + copy * kStCopy + row * 8;
         *reinterpret_cast<uint4 *>(dst) = make_uint4(v[0], v[1], v[2], v[3]);
         *reinterpret_cast<uint4 *>(dst + kStHalf) = make_uint4(v[4], v[5], v[6], v[7]);
+      };
+      if constexpr (BS1 == 16) {
+#pragma unroll
+        for (int d = 0; d < 3; d++) {  // copy of shift dx = d - 1 holds this cell at column cx - dx
+          const int col = cx - (d - 1);
+          if (col >= 0 && col <= 15) put(d, (zi * SG::NY + yi) * 16 + col);
+        }
+      } else {
+        const int cy = yi - 1;
+#pragma unroll
+        for (int dy = -1; dy <= 1; dy++) {
+#pragma unroll
+          for (int dx = -1; dx <= 1; dx++) {  // copy (dx, dy) holds this cell at (cx - dx, cy - dy)
+            const int xc = cx - dx, yc = cy - dy;
+            if (xc >= 0 && xc <= 7 && yc >= 0 && yc <= 7) put((dy + 1) * 3 + dx + 1, zi * 64 + yc * 8 + xc);
+          }
+        }
       }
     }
   };
@@ -577,7 +613,9 @@ __global__ void __launch_bounds__(kTcThreads, 3) kConvTcStaged(WnGeom g, const f
 #pragma unroll
       for (int t = 0; t < 27; t++) {
         const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
-        const uint32_t aOff = ((dx + 1) * kStCopy + (((dz + 1) * 10 + dy + 1) * 16) * 8) * 2;  // bytes
+        const uint32_t aOff =
+            BS1 == 16 ? ((dx + 1) * kStCopy + (((dz + 1) * SG::NY + dy + 1) * 16) * 8) * 2   // bytes
+                      : (((dy + 1) * 3 + dx + 1) * kStCopy + ((dz + 1) * 64) * 8) * 2;
         const uint64_t ad = adBase + (aOff >> 4), bd = bdBase + ((uint32_t)(t * 256 * 2) >> 4);
         asm volatile(
             "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
@@ -626,7 +664,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) kConvTcStaged(WnGeom g, const f
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmemSlot));
   }
 }
-constexpr size_t kStSmem = (size_t)(3 * kStCopy + 27 * 256) * sizeof(__nv_bfloat16);
+
 
 // ---------------------------------------------------------------------------------
 // backward convolutions (CUDA cores; FP32)
@@ -856,6 +894,33 @@ static WnGeom wnGeom(const PoissonState *ps, const WarmNetState *w) {
   return g;
 }
 
+// the four forward convolutions, staged-neighbourhood tensor-core form
+template <int BS1>
+static int wnConvStaged(msbg_gpu_ctx *ctx, WarmNetState *w, const WnGeom &g) {
+  constexpr size_t smem = stSmemBytes<BS1>();
+  static bool attr = false;
+  if (!attr) {
+    MSBG_CUDA(ctx, cudaFuncSetAttribute(kConvTcStaged<BS1, 2, 16, true, true>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MSBG_CUDA(ctx, cudaFuncSetAttribute(kConvTcStaged<BS1, 16, 16, true, false>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MSBG_CUDA(ctx, cudaFuncSetAttribute(kConvTcStaged<BS1, 16, 2, false, false>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  // resident CTAs per SM: 3 with the 58.5 KB of edge 16, 2 with the 87.5 KB of edge 8
+  const unsigned gt = wnTcGrid(w->n1, smem <= 75 * 1024 ? 3 : 2);
+  MSBG_LAUNCH(ctx, (kConvTcStaged<BS1, 2, 16, true, true>), gt, kTcThreads, smem, g, w->act[0], w->wq[0],
+              w->bias[0], w->dScal, w->act[1], ctx->dStatus);
+  MSBG_LAUNCH(ctx, (kConvTcStaged<BS1, 16, 16, true, false>), gt, kTcThreads, smem, g, w->act[1], w->wq[1],
+              w->bias[1], w->dScal, w->act[2], ctx->dStatus);
+  MSBG_LAUNCH(ctx, (kConvTcStaged<BS1, 16, 16, true, false>), gt, kTcThreads, smem, g, w->act[2], w->wq[2],
+              w->bias[2], w->dScal, w->act[3], ctx->dStatus);
+  MSBG_LAUNCH(ctx, (kConvTcStaged<BS1, 16, 2, false, false>), gt, kTcThreads, smem, g, w->act[3], w->wq[3],
+              w->bias[3], w->dScal, w->act[4], ctx->dStatus);
+  return MSBG_GPU_OK;
+}
+
 // forward pass from the level-0 right-hand side b0; x0 (level 0) optional
 static int wnForward(msbg_gpu_ctx *ctx, const float *b0, float *x0) {
   PoissonState *ps = ctx->poisson;
@@ -865,32 +930,21 @@ static int wnForward(msbg_gpu_ctx *ctx, const float *b0, float *x0) {
   MSBG_LAUNCH(ctx, kWnInputs, (unsigned)w->nPart, kRedThreads, 0, b0, (const float *)ps->f32.d[1], L1, w->n1,
               (float2 *)w->act[0], w->dPart);
   MSBG_LAUNCH(ctx, kWnScales, 1, kRedThreads, 0, w->dPart, w->nPart, w->n1, w->dScal);
-  const unsigned gt = wnTcGrid(w->n1, g.bs == 16 ? 3 : 4);  // 3: the staged form's 58.5 KB shared memory
-  if (g.bs == 16) {  // staged-neighbourhood tensor-core convolutions
-    static bool attr = false;
-    if (!attr) {
-      MSBG_CUDA(ctx, cudaFuncSetAttribute(kConvTcStaged<2, 16, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStSmem));
-      MSBG_CUDA(ctx, cudaFuncSetAttribute(kConvTcStaged<16, 16, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStSmem));
-      MSBG_CUDA(ctx, cudaFuncSetAttribute(kConvTcStaged<16, 2, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStSmem));
-      attr = true;
-    }
-    MSBG_LAUNCH(ctx, (kConvTcStaged<2, 16, true, true>), gt, kTcThreads, kStSmem, g, w->act[0], w->wq[0], w->bias[0],
-                w->dScal, w->act[1], ctx->dStatus);
-    MSBG_LAUNCH(ctx, (kConvTcStaged<16, 16, true, false>), gt, kTcThreads, kStSmem, g, w->act[1], w->wq[1],
-                w->bias[1], w->dScal, w->act[2], ctx->dStatus);
-    MSBG_LAUNCH(ctx, (kConvTcStaged<16, 16, true, false>), gt, kTcThreads, kStSmem, g, w->act[2], w->wq[2],
-                w->bias[2], w->dScal, w->act[3], ctx->dStatus);
-    MSBG_LAUNCH(ctx, (kConvTcStaged<16, 2, false, false>), gt, kTcThreads, kStSmem, g, w->act[3], w->wq[3],
-                w->bias[3], w->dScal, w->act[4], ctx->dStatus);
-  } else {
-  MSBG_LAUNCH(ctx, (kConvTc<2, 16, true, true>), gt, kTcThreads, 0, g, w->act[0], w->wq[0], w->bias[0], w->dScal,
-              w->act[1], ctx->dStatus);
-  MSBG_LAUNCH(ctx, (kConvTc<16, 16, true, false>), gt, kTcThreads, 0, g, w->act[1], w->wq[1], w->bias[1], w->dScal,
-              w->act[2], ctx->dStatus);
-  MSBG_LAUNCH(ctx, (kConvTc<16, 16, true, false>), gt, kTcThreads, 0, g, w->act[2], w->wq[2], w->bias[2], w->dScal,
-              w->act[3], ctx->dStatus);
-  MSBG_LAUNCH(ctx, (kConvTc<16, 2, false, false>), gt, kTcThreads, 0, g, w->act[3], w->wq[3], w->bias[3], w->dScal,
-              w->act[4], ctx->dStatus);
+  int rc;
+  if (g.bs == 16) {
+    if ((rc = wnConvStaged<16>(ctx, w, g))) return rc;
+  } else if (g.bs == 8) {
+    if ((rc = wnConvStaged<8>(ctx, w, g))) return rc;
+  } else {  // level-1 blocks of edge 4: rows gathered per tap
+    const unsigned gt = wnTcGrid(w->n1, 4);
+    MSBG_LAUNCH(ctx, (kConvTc<2, 16, true, true>), gt, kTcThreads, 0, g, w->act[0], w->wq[0], w->bias[0], w->dScal,
+                w->act[1], ctx->dStatus);
+    MSBG_LAUNCH(ctx, (kConvTc<16, 16, true, false>), gt, kTcThreads, 0, g, w->act[1], w->wq[1], w->bias[1],
+                w->dScal, w->act[2], ctx->dStatus);
+    MSBG_LAUNCH(ctx, (kConvTc<16, 16, true, false>), gt, kTcThreads, 0, g, w->act[2], w->wq[2], w->bias[2],
+                w->dScal, w->act[3], ctx->dStatus);
+    MSBG_LAUNCH(ctx, (kConvTc<16, 2, false, false>), gt, kTcThreads, 0, g, w->act[3], w->wq[3], w->bias[3],
+                w->dScal, w->act[4], ctx->dStatus);
   }
   MSBG_LAUNCH(ctx, kWnHead, gridFor(w->n2, 256), 256, 0, (const float2 *)w->act[4], w->dScal, L1, w->n2, w->x1, x0);
   return MSBG_GPU_OK;
