@@ -80,19 +80,21 @@ __device__ __forceinline__ int64_t parentOf(int64_t j, int L) {
 // ---------------------------------------------------------------------------------
 // operator rows
 // ---------------------------------------------------------------------------------
-// Quad q of a block (4 cells along x) -> block-local origin.  Bits of q from the
-// bottom: x quad (log2(bs/4) bits), y parity, z parity, y pair, z pair; so the 8
-// children of a coarse cell pair are the 4 lanes {q, q^xq, q^2xq, q^3xq}.
-template <typename V, int MODE>
-__global__ void __launch_bounds__(256, 3) kApplyRows(BlkGeom g, const V *__restrict__ x, const V *__restrict__ b,
-                                                  const V *__restrict__ cx, const V *__restrict__ cy,
-                                                  const V *__restrict__ cz, const V *__restrict__ d,
-                                                  V *__restrict__ y, double *__restrict__ dotPartial,
-                                                  V *__restrict__ bc, V *__restrict__ xc,
-                                                  __half *__restrict__ rhOut, float rhScale) {
+// Row segment q of a block (CPT cells along x: 4 for FP32 storage, 8 for FP16 on
+// levels with bs >= 8, so that a thread moves 16 bytes per row load) -> block-local
+// origin.  Bits of q from the bottom: x segment (log2(bs/CPT) bits), y parity,
+// z parity, y pair, z pair; so the 8 children of the coarse cells over a segment
+// pair are the 4 lanes {q, q^xq, q^2xq, q^3xq}.
+template <typename V, int MODE, int CPT = 4>
+__global__ void __launch_bounds__(256, CPT == 4 ? 3 : 2)
+    kApplyRows(BlkGeom g, const V *__restrict__ x, const V *__restrict__ b, const V *__restrict__ cx,
+               const V *__restrict__ cy, const V *__restrict__ cz, const V *__restrict__ d, V *__restrict__ y,
+               double *__restrict__ dotPartial, V *__restrict__ bc, V *__restrict__ xc,
+               __half *__restrict__ rhOut, float rhScale) {
+  constexpr int LC = CPT == 4 ? 2 : 3;
   const int L = g.log2bs, bs = g.bs;
-  const int xb = L - 2;
-  const int qPerBlockLog = 3 * L - 2;
+  const int xb = L - LC;
+  const int qPerBlockLog = 3 * L - LC;
   const int64_t nQuad = g.nAct << qPerBlockLog;
   const int64_t nQuadPad = (nQuad + 31) & ~int64_t(31);
   const int64_t sy = bs, sz = (int64_t)bs * bs;
@@ -107,50 +109,51 @@ __global__ void __launch_bounds__(256, 3) kApplyRows(BlkGeom g, const V *__restr
     const int yp = (qb >> xb) & 1, zp = (qb >> (xb + 1)) & 1;
     const int rest = qb >> (xb + 2);
     const int yh = rest & ((bs >> 1) - 1), zh = rest >> (L - 1);
-    const int lx = qx << 2, ly = 2 * yh + yp, lz = 2 * zh + zp;
+    const int lx = qx << LC, ly = 2 * yh + yp, lz = 2 * zh + zp;
     const int64_t base = (int64_t)s << (3 * L);
     const int64_t c = base + ((int64_t)((lz << L) + ly) << L) + lx;
 
-    float xv[4], dv[4], cxv[4], cyv[4], czv[4], ym[4], yq[4], zm[4], zq[4], cyu[4], czu[4];
-    ldRow<4>(x + c, xv);
-    ldRow<4>(d + c, dv);
-    ldRow<4>(cx + c, cxv);
-    ldRow<4>(cy + c, cyv);
-    ldRow<4>(cz + c, czv);
+    float xv[CPT], dv[CPT], cxv[CPT], cyv[CPT], czv[CPT], ym[CPT], yq[CPT], zm[CPT], zq[CPT], cyu[CPT], czu[CPT];
+    ldRow<CPT>(x + c, xv);
+    ldRow<CPT>(d + c, dv);
+    ldRow<CPT>(cx + c, cxv);
+    ldRow<CPT>(cy + c, cyv);
+    ldRow<CPT>(cz + c, czv);
     float xl = 0.f, xr = 0.f, cxr = 0.f;
     {
       const int64_t j = lx > 0 ? c - 1 : cellAt(g, s, lx - 1, ly, lz);
       if (j >= 0) xl = ldv(x + j);
-      const int64_t k = lx + 4 < bs ? c + 4 : cellAt(g, s, lx + 4, ly, lz);
+      const int64_t k = lx + CPT < bs ? c + CPT : cellAt(g, s, lx + CPT, ly, lz);
       if (k >= 0) { xr = ldv(x + k); cxr = ldv(cx + k); }
     }
     {
       const int64_t j = ly > 0 ? c - sy : cellAt(g, s, lx, ly - 1, lz);
-      if (j >= 0) ldRow<4>(x + j, ym); else ym[0] = ym[1] = ym[2] = ym[3] = 0.f;
+      if (j >= 0) ldRow<CPT>(x + j, ym); else for (int i = 0; i < CPT; i++) ym[i] = 0.f;
       const int64_t k = ly + 1 < bs ? c + sy : cellAt(g, s, lx, ly + 1, lz);
-      if (k >= 0) { ldRow<4>(x + k, yq); ldRow<4>(cy + k, cyu); }
-      else { yq[0] = yq[1] = yq[2] = yq[3] = 0.f; cyu[0] = cyu[1] = cyu[2] = cyu[3] = 0.f; }
+      if (k >= 0) { ldRow<CPT>(x + k, yq); ldRow<CPT>(cy + k, cyu); }
+      else for (int i = 0; i < CPT; i++) yq[i] = cyu[i] = 0.f;
     }
     {
       const int64_t j = lz > 0 ? c - sz : cellAt(g, s, lx, ly, lz - 1);
-      if (j >= 0) ldRow<4>(x + j, zm); else zm[0] = zm[1] = zm[2] = zm[3] = 0.f;
+      if (j >= 0) ldRow<CPT>(x + j, zm); else for (int i = 0; i < CPT; i++) zm[i] = 0.f;
       const int64_t k = lz + 1 < bs ? c + sz : cellAt(g, s, lx, ly, lz + 1);
-      if (k >= 0) { ldRow<4>(x + k, zq); ldRow<4>(cz + k, czu); }
-      else { zq[0] = zq[1] = zq[2] = zq[3] = 0.f; czu[0] = czu[1] = czu[2] = czu[3] = 0.f; }
+      if (k >= 0) { ldRow<CPT>(x + k, zq); ldRow<CPT>(cz + k, czu); }
+      else for (int i = 0; i < CPT; i++) zq[i] = czu[i] = 0.f;
     }
-    float r[4];
+    float r[CPT];
     if constexpr (MODE == 2) {
+      static_assert(MODE != 2 || CPT == 4, "the checked residual runs on FP32 storage");
       // r = b - A x in double-float arithmetic: every product split exactly into
       // a rounded part and its error (fma), the running sum kept exact with
       // TwoSum and the errors gathered in a second float; then sum r^2, b^2.
-      float bv[4];
-      ldRow<4>(b + c, bv);
+      float bv[CPT];
+      ldRow<CPT>(b + c, bv);
       float rq = 0.f, bq = 0.f;
 #pragma unroll
-      for (int i = 0; i < 4; i++) {
+      for (int i = 0; i < CPT; i++) {
         const float xm1 = i == 0 ? xl : xv[i - 1];
-        const float xp1 = i == 3 ? xr : xv[i + 1];
-        const float cxp = i == 3 ? cxr : cxv[i + 1];
+        const float xp1 = i == CPT - 1 ? xr : xv[i + 1];
+        const float cxp = i == CPT - 1 ? cxr : cxv[i + 1];
         const float fa[7] = {-dv[i], cxv[i], cxp, cyv[i], cyu[i], czv[i], czu[i]};
         const float fb[7] = {xv[i], xm1, xp1, ym[i], yq[i], zm[i], zq[i]};
         float S = bv[i], E = 0.f;
@@ -172,18 +175,18 @@ __global__ void __launch_bounds__(256, 3) kApplyRows(BlkGeom g, const V *__restr
         dot += (double)rq;
         dot2 += (double)bq;
         if (rhOut) {  // the scaled residual in FP16 (right-hand side of a correction solve)
-          float sc[4];
+          float sc[CPT];
 #pragma unroll
-          for (int i = 0; i < 4; i++) sc[i] = r[i] * rhScale;
-          stRow<4>(rhOut + c, sc);
+          for (int i = 0; i < CPT; i++) sc[i] = r[i] * rhScale;
+          stRow<CPT>(rhOut + c, sc);
         }
       }
     } else {
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
+    for (int i = 0; i < CPT; i++) {
       const float xm1 = i == 0 ? xl : xv[i - 1];
-      const float xp1 = i == 3 ? xr : xv[i + 1];
-      const float cxp = i == 3 ? cxr : cxv[i + 1];
+      const float xp1 = i == CPT - 1 ? xr : xv[i + 1];
+      const float cxp = i == CPT - 1 ? cxr : cxv[i + 1];
       float a = dv[i] * xv[i];
       a -= cxv[i] * xm1;
       a -= cxp * xp1;
@@ -194,34 +197,42 @@ __global__ void __launch_bounds__(256, 3) kApplyRows(BlkGeom g, const V *__restr
       r[i] = a;
     }
     if (MODE == 1) {
-      float bv[4];
-      ldRow<4>(b + c, bv);
+      float bv[CPT];
+      ldRow<CPT>(b + c, bv);
 #pragma unroll
-      for (int i = 0; i < 4; i++) r[i] = bv[i] - r[i];
+      for (int i = 0; i < CPT; i++) r[i] = bv[i] - r[i];
     }
     if (dotPartial && act) {
       float qd = 0.f;  // four products in FP32, then FP64 accumulation
 #pragma unroll
-      for (int i = 0; i < 4; i++) qd = fmaf(xv[i], r[i], qd);
+      for (int i = 0; i < CPT; i += 4) {
+        float q4 = 0.f;
+#pragma unroll
+        for (int k = i; k < i + 4; k++) q4 = fmaf(xv[k], r[k], q4);
+        qd += q4;
+      }
       dot += (double)qd;
     }
     if (bc) {
       // sum the 8 children: x pairs in-thread, y and z parities across lanes
-      float p[2] = {r[0] + r[1], r[2] + r[3]};
+      float p[CPT / 2];
 #pragma unroll
-      for (int i = 0; i < 2; i++) {
+      for (int i = 0; i < CPT / 2; i++) {
+        p[i] = r[2 * i] + r[2 * i + 1];
         p[i] += __shfl_xor_sync(0xffffffffu, p[i], 1 << xb);
         p[i] += __shfl_xor_sync(0xffffffffu, p[i], 2 << xb);
       }
       if (act && yp == 0 && zp == 0) {
         const int Lc = L - 1;
         const int64_t ci = ((int64_t)s << (3 * Lc)) + ((int64_t)((zh << Lc) + yh) << Lc) + (lx >> 1);
-        const float zz[2] = {0.f, 0.f};
-        stRow<2>(bc + ci, p);
-        stRow<2>(xc + ci, zz);
+        float zz[CPT / 2];
+#pragma unroll
+        for (int i = 0; i < CPT / 2; i++) zz[i] = 0.f;
+        stRow<CPT / 2>(bc + ci, p);
+        stRow<CPT / 2>(xc + ci, zz);
       }
     } else if (act && y) {
-      stRow<4>(y + c, r);
+      stRow<CPT>(y + c, r);
     }
     }
   }
@@ -741,29 +752,42 @@ BlkGeom blkOf(const PoissonState *ps, const MgLevel &L) {
 // ---------------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------------
-template <typename V>
-int blkApply(msbg_gpu_ctx *ctx, PoissonState *ps, size_t l, const PrecSet &P, const V *x, const V *b, V *y,
-             int mode, double *dotOut, V *bc, V *xc, __half *rhOut, float rhScale) {
-  const MgLevel &Lv = ps->levels[l];
-  const int64_t nQuad = Lv.nCell / 4;
-  int64_t grid = (nQuad + 255) / 256;
+template <typename V, int CPT>
+static int applyLaunch(msbg_gpu_ctx *ctx, PoissonState *ps, const MgLevel &Lv, const PrecSet &P, size_t l,
+                       const V *x, const V *b, V *y, int mode, double *dotOut, V *bc, V *xc, __half *rhOut,
+                       float rhScale) {
+  const int64_t nSeg = Lv.nCell / CPT;
+  int64_t grid = (nSeg + 255) / 256;
   if (grid > ps->nPartial) grid = ps->nPartial;
   if (grid < 1) grid = 1;
   const BlkGeom gg = blkOf(ps, Lv);
   const V *cx = (const V *)P.cx[l], *cy = (const V *)P.cy[l], *cz = (const V *)P.cz[l], *d = (const V *)P.d[l];
   double *part = dotOut ? ps->dPartial : nullptr;
   if (mode == 0)
-    MSBG_LAUNCH(ctx, (kApplyRows<V, 0>), (unsigned)grid, 256, 0, gg, x, b, cx, cy, cz, d, y, part, bc, xc, rhOut,
-                rhScale);
+    MSBG_LAUNCH(ctx, (kApplyRows<V, 0, CPT>), (unsigned)grid, 256, 0, gg, x, b, cx, cy, cz, d, y, part, bc, xc,
+                rhOut, rhScale);
   else if (mode == 1)
-    MSBG_LAUNCH(ctx, (kApplyRows<V, 1>), (unsigned)grid, 256, 0, gg, x, b, cx, cy, cz, d, y, part, bc, xc, rhOut,
-                rhScale);
+    MSBG_LAUNCH(ctx, (kApplyRows<V, 1, CPT>), (unsigned)grid, 256, 0, gg, x, b, cx, cy, cz, d, y, part, bc, xc,
+                rhOut, rhScale);
+  else if constexpr (CPT == 4)
+    MSBG_LAUNCH(ctx, (kApplyRows<V, 2, 4>), (unsigned)grid, 256, 0, gg, x, b, cx, cy, cz, d, y, part, bc, xc,
+                rhOut, rhScale);
   else
-    MSBG_LAUNCH(ctx, (kApplyRows<V, 2>), (unsigned)grid, 256, 0, gg, x, b, cx, cy, cz, d, y, part, bc, xc, rhOut,
-                rhScale);
+    return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "checked residual on FP16 storage");
   if (dotOut && mode == 2) MSBG_LAUNCH(ctx, kSumPartialsBlk2, 1, kRedThreads, 0, ps->dPartial, (int)grid, dotOut);
   else if (dotOut) MSBG_LAUNCH(ctx, kSumPartialsBlk, 1, kRedThreads, 0, ps->dPartial, (int)grid, dotOut);
   return MSBG_GPU_OK;
+}
+
+template <typename V>
+int blkApply(msbg_gpu_ctx *ctx, PoissonState *ps, size_t l, const PrecSet &P, const V *x, const V *b, V *y,
+             int mode, double *dotOut, V *bc, V *xc, __half *rhOut, float rhScale) {
+  const MgLevel &Lv = ps->levels[l];
+  if constexpr (sizeof(V) == 2) {
+    if (Lv.bs >= 8 && mode != 2)  // FP16: 8 cells (16 bytes) per row load
+      return applyLaunch<V, 8>(ctx, ps, Lv, P, l, x, b, y, mode, dotOut, bc, xc, rhOut, rhScale);
+  }
+  return applyLaunch<V, 4>(ctx, ps, Lv, P, l, x, b, y, mode, dotOut, bc, xc, rhOut, rhScale);
 }
 
 static unsigned quadGrid(const PoissonState *ps, int64_t nq) {
