@@ -617,76 +617,77 @@ static __global__ void kSumPartialsBlk2(const double *__restrict__ partial, int 
 #define QUAD_STRIDE(q, nq) \
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < (nq); q += (int64_t)gridDim.x * blockDim.x)
 
-template <typename V>
+// W cells per thread and step: 4 (FP32, 16-byte loads) or 8 (FP16, 16-byte loads)
+template <typename V, int W>
 __global__ void __launch_bounds__(256) kDotQuad(const V *__restrict__ a, const V *__restrict__ b, int64_t nq,
                                                 double *__restrict__ partial) {
   double s = 0.0;
   QUAD_STRIDE(q, nq) {
-    float av[4], bv[4];
-    ldRow<4>(a + 4 * q, av);
-    ldRow<4>(b + 4 * q, bv);
+    float av[W], bv[W];
+    ldRow<W>(a + W * q, av);
+    ldRow<W>(b + W * q, bv);
     float t = 0.f;
 #pragma unroll
-    for (int i = 0; i < 4; i++) t = fmaf(av[i], bv[i], t);
+    for (int i = 0; i < W; i++) t = fmaf(av[i], bv[i], t);
     s += (double)t;
   }
   s = blockSum(s);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 // alpha = sc[0] / sc[1]; x += alpha p; r -= alpha q; partial = sum r^2 (stored r)
-template <typename V>
+template <typename V, int W>
 __global__ void __launch_bounds__(256) kUpdateXRQuad(const double *__restrict__ sc, const V *__restrict__ p,
                                                      const V *__restrict__ q, V *__restrict__ x, V *__restrict__ r,
                                                      int64_t nq, double *__restrict__ partial) {
   const float alpha = sc[1] != 0.0 ? (float)(sc[0] / sc[1]) : 0.0f;
   double rr = 0.0;
   QUAD_STRIDE(k, nq) {
-    float pv[4], qv[4], xv[4], rv[4];
-    ldRow<4>(p + 4 * k, pv);
-    ldRow<4>(q + 4 * k, qv);
-    ldRow<4>(x + 4 * k, xv);
-    ldRow<4>(r + 4 * k, rv);
+    float pv[W], qv[W], xv[W], rv[W];
+    ldRow<W>(p + W * k, pv);
+    ldRow<W>(q + W * k, qv);
+    ldRow<W>(x + W * k, xv);
+    ldRow<W>(r + W * k, rv);
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
+    for (int i = 0; i < W; i++) {
       xv[i] = fmaf(alpha, pv[i], xv[i]);
       rv[i] = fmaf(-alpha, qv[i], rv[i]);
     }
-    stRow<4>(x + 4 * k, xv);
-    stRow<4>(r + 4 * k, rv);
-    float rs[4];
-    ldRow<4>(r + 4 * k, rs);  // the values as stored
+    stRow<W>(x + W * k, xv);
+    stRow<W>(r + W * k, rv);
+    float rs[W];
+    ldRow<W>(r + W * k, rs);  // the values as stored
     float t = 0.f;
 #pragma unroll
-    for (int i = 0; i < 4; i++) t = fmaf(rs[i], rs[i], t);
+    for (int i = 0; i < W; i++) t = fmaf(rs[i], rs[i], t);
     rr += (double)t;
   }
   rr = blockSum(rr);
   if (threadIdx.x == 0) partial[blockIdx.x] = rr;
 }
-// x += scale * e (FP32 x, FP16 correction)
+// x += scale * e (FP32 x, FP16 correction), 8 cells per step
 __global__ void __launch_bounds__(256) kAddScaledQuad(const __half *__restrict__ e, float scale, float *__restrict__ x,
                                                       int64_t nq) {
   QUAD_STRIDE(k, nq) {
-    float ev[4], xv[4];
-    ldRow<4>(e + 4 * k, ev);
-    ldRow<4>(x + 4 * k, xv);
+    float ev[8], xv[8];
+    ldRow<8>(e + 8 * k, ev);
+    ldRow<8>(x + 8 * k, xv);
 #pragma unroll
-    for (int i = 0; i < 4; i++) xv[i] = fmaf(scale, ev[i], xv[i]);
-    stRow<4>(x + 4 * k, xv);
+    for (int i = 0; i < 8; i++) xv[i] = fmaf(scale, ev[i], xv[i]);
+    stRow<8>(x + 8 * k, xv);
   }
 }
 // beta = sc[2] / sc[0]; p = z + beta p
-template <typename V>
+template <typename V, int W>
 __global__ void __launch_bounds__(256) kUpdatePQuad(const double *__restrict__ sc, const V *__restrict__ z,
                                                     V *__restrict__ p, int64_t nq) {
   const float beta = sc[0] != 0.0 ? (float)(sc[2] / sc[0]) : 0.0f;
   QUAD_STRIDE(k, nq) {
-    float zv[4], pv[4];
-    ldRow<4>(z + 4 * k, zv);
-    ldRow<4>(p + 4 * k, pv);
+    float zv[W], pv[W];
+    ldRow<W>(z + W * k, zv);
+    ldRow<W>(p + W * k, pv);
 #pragma unroll
-    for (int i = 0; i < 4; i++) pv[i] = fmaf(beta, pv[i], zv[i]);
-    stRow<4>(p + 4 * k, pv);
+    for (int i = 0; i < W; i++) pv[i] = fmaf(beta, pv[i], zv[i]);
+    stRow<W>(p + W * k, pv);
   }
 }
 
@@ -796,28 +797,42 @@ static unsigned quadGrid(const PoissonState *ps, int64_t nq) {
   return (unsigned)(g < 1 ? 1 : g);
 }
 
+// cells per thread and step of the vector kernels: 8 for FP16 (16-byte loads) when n
+// allows, else 4
+template <typename V>
+static int vecWidth(int64_t n) {
+  return (sizeof(V) == 2 && n % 8 == 0) ? 8 : 4;
+}
+
 template <typename V>
 int blkDot(msbg_gpu_ctx *ctx, PoissonState *ps, const V *a, const V *b, int64_t n, double *dOut) {
-  const unsigned g = quadGrid(ps, n / 4);
-  MSBG_LAUNCH(ctx, kDotQuad<V>, g, 256, 0, a, b, n / 4, ps->dPartial);
+  const int w = vecWidth<V>(n);
+  const unsigned g = quadGrid(ps, n / w);
+  if (w == 8) MSBG_LAUNCH(ctx, (kDotQuad<V, 8>), g, 256, 0, a, b, n / 8, ps->dPartial);
+  else MSBG_LAUNCH(ctx, (kDotQuad<V, 4>), g, 256, 0, a, b, n / 4, ps->dPartial);
   MSBG_LAUNCH(ctx, kSumPartialsBlk, 1, kRedThreads, 0, ps->dPartial, (int)g, dOut);
   return MSBG_GPU_OK;
 }
 template <typename V>
 int blkUpdateXR(msbg_gpu_ctx *ctx, PoissonState *ps, const double *sc, const V *p, const V *q, V *x, V *r, int64_t n,
                 double *rrOut) {
-  const unsigned g = quadGrid(ps, n / 4);
-  MSBG_LAUNCH(ctx, kUpdateXRQuad<V>, g, 256, 0, sc, p, q, x, r, n / 4, ps->dPartial);
+  const int w = vecWidth<V>(n);
+  const unsigned g = quadGrid(ps, n / w);
+  if (w == 8) MSBG_LAUNCH(ctx, (kUpdateXRQuad<V, 8>), g, 256, 0, sc, p, q, x, r, n / 8, ps->dPartial);
+  else MSBG_LAUNCH(ctx, (kUpdateXRQuad<V, 4>), g, 256, 0, sc, p, q, x, r, n / 4, ps->dPartial);
   MSBG_LAUNCH(ctx, kSumPartialsBlk, 1, kRedThreads, 0, ps->dPartial, (int)g, rrOut);
   return MSBG_GPU_OK;
 }
 int blkAddScaled(msbg_gpu_ctx *ctx, PoissonState *ps, const __half *e, float scale, float *x, int64_t n) {
-  MSBG_LAUNCH(ctx, kAddScaledQuad, quadGrid(ps, n / 4), 256, 0, e, scale, x, n / 4);
+  if (n % 8) return fail(ctx, MSBG_GPU_ERR_ARG, "add_scaled: %lld cells are not a multiple of 8", (long long)n);
+  MSBG_LAUNCH(ctx, kAddScaledQuad, quadGrid(ps, n / 8), 256, 0, e, scale, x, n / 8);
   return MSBG_GPU_OK;
 }
 template <typename V>
 int blkUpdateP(msbg_gpu_ctx *ctx, PoissonState *ps, const double *sc, const V *z, V *p, int64_t n) {
-  MSBG_LAUNCH(ctx, kUpdatePQuad<V>, quadGrid(ps, n / 4), 256, 0, sc, z, p, n / 4);
+  const int w = vecWidth<V>(n);
+  if (w == 8) MSBG_LAUNCH(ctx, (kUpdatePQuad<V, 8>), quadGrid(ps, n / 8), 256, 0, sc, z, p, n / 8);
+  else MSBG_LAUNCH(ctx, (kUpdatePQuad<V, 4>), quadGrid(ps, n / 4), 256, 0, sc, z, p, n / 4);
   return MSBG_GPU_OK;
 }
 
