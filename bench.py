@@ -130,7 +130,8 @@ class Dist:
             import torch
             import torch.distributed as dist
             os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-            torch.cuda.set_device(self.local)
+            if torch.cuda.is_available():
+                torch.cuda.set_device(self.local)
             dist.init_process_group("gloo")
             self.dist = dist
             self.torch = torch
