@@ -200,6 +200,12 @@ int msbg_gpu_multiply_laplacian(msbg_gpu_ctx *ctx, int chanX, int chanB, int cha
  * smoother below); reverseOrder runs the adjoint order (tile colour 1 first, black
  * cells first). */
 int msbg_gpu_relax(msbg_gpu_ctx *ctx, int chanX, int chanB, int nIter, int reverseOrder);
+/* Diagnostics of the failure path: one CTA waits on an mbarrier that nothing completes,
+ * with the same bounded try-wait loop as the library's kernels but a limit of `polls`
+ * (1..1<<20).  The kernel records the expired wait in the device status word and returns;
+ * the call returns MSBG_GPU_ERR_TIMEOUT, clears the word, and leaves the context usable.
+ * No GPU fault is involved. */
+int msbg_gpu_diag_wait_timeout(msbg_gpu_ctx *ctx, int polls);
 /* downsampleFloatChannelNew (src/msbg4.cpp:1035-1379, levelMg = 1, OPT_ALL_CELLS): the
  * restriction of channel chSrc (FP32, FP16 or uint16 storage) to the next coarser
  * multigrid level, for every value block.  dDst (device, FP32) receives

@@ -809,3 +809,42 @@ extern "C" int msbg_gpu_copy_d2h(msbg_gpu_ctx *ctx, void *h, const void *d, size
   MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return MSBG_GPU_OK;
 }
+
+// ---------------------------------------------------------------------------------
+// diagnostics: the bounded-wait failure path without a GPU fault
+// ---------------------------------------------------------------------------------
+namespace msbg {
+__global__ void kDiagWait(int polls, int *__restrict__ status) {
+  __shared__ __align__(8) uint64_t bar;
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(&bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(a) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  bool done = false;
+  for (int it = 0; it < polls && !done; it++) {  // phase 0 never completes: no arrival
+    uint32_t ok;
+    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok)
+                 : "r"(a)
+                 : "memory");
+    done = ok != 0;
+  }
+  if (!__syncthreads_and(done) && threadIdx.x == 0) atomicOr(status, 16);
+}
+}  // namespace msbg
+
+extern "C" int msbg_gpu_diag_wait_timeout(msbg_gpu_ctx *ctx, int polls) {
+  if (!ctx || polls < 1 || polls > (1 << 20)) return MSBG_GPU_ERR_ARG;
+  MSBG_LAUNCH(ctx, kDiagWait, 1, 32, 0, polls, ctx->dStatus);
+  int st = 0;
+  MSBG_CUDA(ctx, cudaMemcpyAsync(&st, ctx->dStatus, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (st) {
+    MSBG_CUDA(ctx, cudaMemsetAsync(ctx->dStatus, 0, sizeof(int), ctx->stream));
+    MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return fail(ctx, MSBG_GPU_ERR_TIMEOUT, "a bounded device wait timed out (status bits %d)", st);
+  }
+  return MSBG_GPU_OK;
+}

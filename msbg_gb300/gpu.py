@@ -86,6 +86,7 @@ SIGNATURES = {
     "msbg_gpu_multiply_laplacian": (I, [P, I, I, I, I]),
     "msbg_gpu_relax": (I, [P, I, I, I, I]),
     "msbg_gpu_downsample_channel": (I, [P, I, P, I]),
+    "msbg_gpu_diag_wait_timeout": (I, [P, I]),
     "msbg_gpu_vcycle": (I, [P, I, I]),
     "msbg_gpu_dot": (I, [P, I, I, C.POINTER(D)]),
     "msbg_gpu_axpby": (I, [P, D, I, D, I]),
@@ -348,6 +349,10 @@ class MultiresSparseGrid:
 
     def vcycle(self, chanX: int, chanB: int):
         self._check(self.L.msbg_gpu_vcycle(self.h, chanX, chanB))
+
+    def diag_wait_timeout(self, polls: int = 1000):
+        """Runs the bounded-wait failure path once (raises MsbgGpuError, code ERR_TIMEOUT)."""
+        self._check(self.L.msbg_gpu_diag_wait_timeout(self.h, polls))
 
     def downsampleFloatChannelNew(self, chSrc: int, simpleAverage: bool = False) -> np.ndarray:
         """Restriction of channel chSrc to the next coarser level, per value block:

@@ -277,3 +277,23 @@ def test_full_size_surface4096_layout_and_splat_match_restatement(gpulib, port):
     assert r["info"].nActParticles == p.n_act_particles and r["info"].nAborted == p.n_aborted
     assert np.array_equal(_as_bits(r["final"]), _as_bits(p.after_finalize))
     assert len(r["bids"]) == 144191
+
+
+def test_gpu_bounded_wait_times_out_and_context_stays_usable(gpulib):
+    """The failure path of the library's bounded waits, without a GPU fault: a wait on
+    an mbarrier that nothing completes gives up after its poll limit, the call returns
+    MSBG_GPU_ERR_TIMEOUT, and the next calls on the same context work."""
+    G = gpulib
+    g = G.MultiresSparseGrid(64, 64, 64, 16, 2, G.F32)
+    try:
+        with pytest.raises(G.MsbgGpuError) as e:
+            g.diag_wait_timeout(2000)
+        assert e.value.code == G.ERR_TIMEOUT
+        g.set_levels(np.zeros(64, np.int32))
+        g.setRefinementMap(0.5)
+        assert np.all(g.payload(0) == 0.5)
+        with pytest.raises(G.MsbgGpuError) as e:  # the status word was cleared: same result again
+            g.diag_wait_timeout(10)
+        assert e.value.code == G.ERR_TIMEOUT
+    finally:
+        g.close()
