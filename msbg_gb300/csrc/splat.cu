@@ -16,15 +16,27 @@
 namespace msbg {
 
 // Every voxel of a slab <- v (the demo fills value blocks with 1.0 before splatting).
+// Eight voxels per thread and step, stored as 16-byte vectors.
 template <typename T>
 __global__ void kFill(T *__restrict__ p, int64_t n, float v, double vd) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  if constexpr (sizeof(T) == 8) {
-    p[i] = vd;
-  } else {
-    Store<T>::storeRHA(p + i, v);
+  T e;
+  if constexpr (sizeof(T) == 8) e = vd; else Store<T>::storeRHA(&e, v);
+  T q[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) q[k] = e;
+  const int64_t n8 = n / 8;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n8; i += (int64_t)gridDim.x * blockDim.x) {
+    uint4 *dst = reinterpret_cast<uint4 *>(p + 8 * i);
+#pragma unroll
+    for (int k = 0; k < (int)(8 * sizeof(T) / 16); k++) dst[k] = reinterpret_cast<const uint4 *>(q)[k];
   }
+  for (int64_t i = 8 * n8 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = e;
+}
+
+static unsigned gridVec(int64_t n) {  // 8 elements per thread, grid-stride
+  const int64_t t = (n / 8 + 255) / 256;
+  return (unsigned)(t < 1 ? 1 : t > 152 * 64 ? 152 * 64 : t);
 }
 
 int fillChannel(msbg_gpu_ctx *ctx, int chan, double v) {
@@ -32,10 +44,10 @@ int fillChannel(msbg_gpu_ctx *ctx, int chan, double v) {
   const int64_t n = ctx->nActive * ctx->voxPerBlock;
   if (n == 0) return MSBG_GPU_OK;
   switch (c.storage) {
-    case MSBG_GPU_F32: MSBG_LAUNCH(ctx, kFill<float>, gridFor(n, 256), 256, 0, (float *)c.d, n, (float)v, v); break;
-    case MSBG_GPU_U16: MSBG_LAUNCH(ctx, kFill<uint16_t>, gridFor(n, 256), 256, 0, (uint16_t *)c.d, n, (float)v, v); break;
-    case MSBG_GPU_F16: MSBG_LAUNCH(ctx, kFill<__half>, gridFor(n, 256), 256, 0, (__half *)c.d, n, (float)v, v); break;
-    default: MSBG_LAUNCH(ctx, kFill<double>, gridFor(n, 256), 256, 0, (double *)c.d, n, (float)v, v); break;
+    case MSBG_GPU_F32: MSBG_LAUNCH(ctx, kFill<float>, gridVec(n), 256, 0, (float *)c.d, n, (float)v, v); break;
+    case MSBG_GPU_U16: MSBG_LAUNCH(ctx, kFill<uint16_t>, gridVec(n), 256, 0, (uint16_t *)c.d, n, (float)v, v); break;
+    case MSBG_GPU_F16: MSBG_LAUNCH(ctx, kFill<__half>, gridVec(n), 256, 0, (__half *)c.d, n, (float)v, v); break;
+    default: MSBG_LAUNCH(ctx, kFill<double>, gridVec(n), 256, 0, (double *)c.d, n, (float)v, v); break;
   }
   return MSBG_GPU_OK;
 }
@@ -130,13 +142,8 @@ __global__ void __launch_bounds__(256) kSplat(const float *__restrict__ pts, int
   }
 }
 
-template <typename T>
-__global__ void kFinalize(const float *__restrict__ splat, T *__restrict__ out, int64_t n, float rParticle,
-                          float nbDist, float distSqMax) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  // the demo reads back the quantized minimum (renderDensToFloat_)
-  float d = Store<T>::quant(splat[i]);
+// distance -> density of one voxel (q: the quantized minimum splat value)
+__device__ __forceinline__ float finalizeValue(float d, float rParticle, float nbDist, float distSqMax) {
   float f = 0.0f;
   if (d < 0.999f) {
     d = __fmul_rn(d, distSqMax);
@@ -151,7 +158,28 @@ __global__ void kFinalize(const float *__restrict__ splat, T *__restrict__ out, 
     else lin = __fmul_rn(__fsub_rn(dist, a), __frcp_rn(__fsub_rn(b, a)));
     f = __fsub_rn(1.0f, lin);
   }
-  Store<T>::storeRHA(out + i, f);
+  return f;
+}
+
+// Eight voxels per thread and step: two 16-byte reads of the FP32 minimum, one
+// 16-byte (2-byte storage) or two (FP32) writes.
+template <typename T>
+__global__ void kFinalize(const float *__restrict__ splat, T *__restrict__ out, int64_t n, float rParticle,
+                          float nbDist, float distSqMax) {
+  const int64_t n8 = n / 8;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n8; i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 a = reinterpret_cast<const float4 *>(splat)[2 * i], b = reinterpret_cast<const float4 *>(splat)[2 * i + 1];
+    const float in[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    T q[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++)  // the demo reads back the quantized minimum (renderDensToFloat_)
+      Store<T>::storeRHA(&q[k], finalizeValue(Store<T>::quant(in[k]), rParticle, nbDist, distSqMax));
+    uint4 *dst = reinterpret_cast<uint4 *>(out + 8 * i);
+#pragma unroll
+    for (int k = 0; k < (int)(8 * sizeof(T) / 16); k++) dst[k] = reinterpret_cast<const uint4 *>(q)[k];
+  }
+  for (int64_t i = 8 * n8 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    Store<T>::storeRHA(out + i, finalizeValue(Store<T>::quant(splat[i]), rParticle, nbDist, distSqMax));
 }
 
 template <>
@@ -159,24 +187,18 @@ __global__ void kFinalize<double>(const float *__restrict__ splat, double *__res
                                   float rParticle, float nbDist, float distSqMax) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  float d = splat[i];
-  float f = 0.0f;
-  if (d < 0.999f) {
-    d = __fmul_rn(d, distSqMax);
-    const float dist = __fsub_rn(__fsqrt_rn(d), rParticle);
-    const float a = -rParticle, b = __fadd_rn(rParticle, nbDist);
-    float lin;
-    if (dist < a) lin = 0.0f;
-    else if (dist >= b) lin = 1.0f;
-    else lin = __fmul_rn(__fsub_rn(dist, a), __frcp_rn(__fsub_rn(b, a)));
-    f = __fsub_rn(1.0f, lin);
-  }
-  out[i] = (double)f;
+  out[i] = (double)finalizeValue(splat[i], rParticle, nbDist, distSqMax);
 }
 
-__global__ void kFillF32(float *p, int64_t n, float v) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) p[i] = v;
+__global__ void kFillF32(float *p, int64_t n, float v) {  // 8 per thread and step
+  const int64_t n8 = n / 8;
+  const float4 q = make_float4(v, v, v, v);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n8; i += (int64_t)gridDim.x * blockDim.x) {
+    reinterpret_cast<float4 *>(p)[2 * i] = q;
+    reinterpret_cast<float4 *>(p)[2 * i + 1] = q;
+  }
+  for (int64_t i = 8 * n8 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = v;
 }
 
 int splatRun(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rParticle, float nbDist) {
@@ -189,7 +211,7 @@ int splatRun(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rParticle, f
     int rc = ensureTmpSlab(ctx, (size_t)(nVox > 0 ? nVox : 1) * 4);
     if (rc) return rc;
     dst = (float *)ctx->dTmpSlab;
-    if (nVox) MSBG_LAUNCH(ctx, kFillF32, gridFor(nVox, 256), 256, 0, dst, nVox, 1.0f);
+    if (nVox) MSBG_LAUNCH(ctx, kFillF32, gridVec(nVox), 256, 0, dst, nVox, 1.0f);
   }
   MSBG_CUDA(ctx, cudaMemsetAsync(ctx->dCounters + 1, 0, 8, ctx->stream));
   if (n == 0 || nVox == 0) return MSBG_GPU_OK;
@@ -215,9 +237,9 @@ int splatFinalizeRun(msbg_gpu_ctx *ctx, float rParticle, float nbDist) {
   if (c.storage != MSBG_GPU_F32 && ctx->tmpSlabBytes < (size_t)n * 4)
     return fail(ctx, MSBG_GPU_ERR_STATE, "finalize without a splat");
   switch (c.storage) {
-    case MSBG_GPU_F32: MSBG_LAUNCH(ctx, kFinalize<float>, gridFor(n, 256), 256, 0, src, (float *)c.d, n, rParticle, nbDist, distSqMax); break;
-    case MSBG_GPU_U16: MSBG_LAUNCH(ctx, kFinalize<uint16_t>, gridFor(n, 256), 256, 0, src, (uint16_t *)c.d, n, rParticle, nbDist, distSqMax); break;
-    case MSBG_GPU_F16: MSBG_LAUNCH(ctx, kFinalize<__half>, gridFor(n, 256), 256, 0, src, (__half *)c.d, n, rParticle, nbDist, distSqMax); break;
+    case MSBG_GPU_F32: MSBG_LAUNCH(ctx, kFinalize<float>, gridVec(n), 256, 0, src, (float *)c.d, n, rParticle, nbDist, distSqMax); break;
+    case MSBG_GPU_U16: MSBG_LAUNCH(ctx, kFinalize<uint16_t>, gridVec(n), 256, 0, src, (uint16_t *)c.d, n, rParticle, nbDist, distSqMax); break;
+    case MSBG_GPU_F16: MSBG_LAUNCH(ctx, kFinalize<__half>, gridVec(n), 256, 0, src, (__half *)c.d, n, rParticle, nbDist, distSqMax); break;
     default: MSBG_LAUNCH(ctx, kFinalize<double>, gridFor(n, 256), 256, 0, src, (double *)c.d, n, rParticle, nbDist, distSqMax); break;
   }
   return MSBG_GPU_OK;
