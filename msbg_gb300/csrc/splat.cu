@@ -126,6 +126,33 @@ __global__ void __launch_bounds__(256) kSplat(const float *__restrict__ pts, int
     abortAt = first;
     if (lane == 0 && abortAt < total) atomicAdd(nAborted, 1ull);
   }
+  if (abortAt == total) {
+    // Nothing aborts (every touched block holds data): lanes take whole (y, z) rows of
+    // the box, skip the rows outside the sphere (dz*dz + dy*dy already exceeds it, and
+    // adding dx*dx >= 0 cannot lower a float sum), and find the row's two possible
+    // blocks once.
+    const int nRows = ny * nz;
+    for (int row = lane; row < nRows; row += 32) {
+      const int ly = row % ny, lz = row / ny;
+      const int iy = iy1 + ly, iz = iz1 + lz;
+      const float dz = __fsub_rn((float)iz, z0), dy = __fsub_rn((float)iy, y0);
+      const float dzy = __fadd_rn(__fmul_rn(dz, dz), __fmul_rn(dy, dy));
+      if (dzy > g.distSqMax) continue;
+      const int64_t rowBlk = (int64_t)(iz >> s) * nxy + (int64_t)(iy >> s) * g.nbx;
+      const int bxa = ix1 >> s;
+      const int64_t sa = (int64_t)slot[rowBlk + bxa] * vpb, sb = (int64_t)slot[rowBlk + (ix2 >> s)] * vpb;
+      const int rowVid = ((iz & mask) << (2 * s)) + ((iy & mask) << s);
+      for (int ix = ix1; ix <= ix2; ix++) {
+        // distSq exactly as the demo forms it: (dz*dz + dy*dy) + dx*dx
+        const float dx = __fsub_rn((float)ix, x0);
+        const float d2 = __fadd_rn(dzy, __fmul_rn(dx, dx));
+        if (d2 > g.distSqMax) continue;
+        const int64_t base = (ix >> s) == bxa ? sa : sb;
+        atomicMin((int *)(dst + base + rowVid + (ix & mask)), __float_as_int(__fmul_rn(d2, g.distSqMaxInv)));
+      }
+    }
+    return;
+  }
   for (int t = lane; t < abortAt; t += 32) {
     const int lx = t % nx, rest = t / nx, ly = rest % ny, lz = rest / ny;
     const int ix = ix1 + lx, iy = iy1 + ly, iz = iz1 + lz;
