@@ -358,6 +358,31 @@ def run_gpu(args, spec, dist: Dist):
                                     "peak": peaks["hbm_gbs"], "unit": "GB/s",
                                     "frac": nbytes / (msr / 1e3) / 1e9 / peaks["hbm_gbs"]}}
 
+    # grid-to-particle interpolation of the swept field at every particle
+    # (interpolateFloatFast / interpolateUint16ToFloatFast per point): 12 bytes of position
+    # read and 4 bytes written per point; the 8 corner reads are gathers served by L1/L2
+    g2p = None
+    if not args.no_jacobi:
+        dout = G.DeviceBuffer.alloc(max(n, 1) * 4)
+        for _ in range(max(3, args.warmup)):
+            g.interpolate_device(0, d, n, dout, 0)
+        g.synchronize()
+        lg = g.launch_count()
+        g.event_record(6)
+        for _ in range(args.steps):
+            g.interpolate_device(0, d, n, dout, 0)
+        g.event_record(7)
+        g.synchronize()
+        msg = dist.max(g.event_elapsed_ms(6, 7)) / args.steps
+        dout.free()
+        gbs = n * 16 / (msg / 1e3) / 1e9
+        g2p = {"kernel": "kInterpolate (trilinear)", "points": int(n), "ms_per_call": msg,
+               "particles_per_s": n * dist.world / (msg / 1e3),
+               "launches_per_call": (g.launch_count() - lg) // args.steps,
+               "roofline": {"bound": "l2/latency (gathers)", "achieved": gbs, "peak": peaks["hbm_gbs"],
+                            "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
+                            "algorithmic_bytes_per_point": 16}}
+
     # e2e through the host-buffer entry point
     e2e = None
     if not args.no_e2e:
@@ -420,6 +445,7 @@ def run_gpu(args, spec, dist: Dist):
         "cpu_baseline": cpu,
         "jacobi_sweeps": jacobi,
         "restriction": restriction,
+        "g2p": g2p,
         "poisson": poisson,
     }
     print(json.dumps(line), flush=True)

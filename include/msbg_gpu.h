@@ -217,6 +217,36 @@ int msbg_gpu_diag_wait_timeout(msbg_gpu_ctx *ctx, int polls);
  * outside the domain, the value at the clamped position; in a block without payload, the
  * channel's empty value. */
 int msbg_gpu_downsample_channel(msbg_gpu_ctx *ctx, int chSrc, float *dDst, int simpleAverage);
+/* Grid-to-particle interpolation: dOut[i] (device, FP32) = the trilinear interpolant of
+ * channel chan (FP32, FP16 or uint16 storage) at dPts[3i..3i+2] (device, voxel units,
+ * voxel centres at i + 0.5), for i < n.
+ * Replaces SparseGrid<float>::interpolateFloatFast (src/sbg.h:1443-1444, body
+ * src/sbg.h:4623-4792) and SparseGrid<uint16_t>::interpolateUint16ToFloatFast
+ * (src/sbg.h:1445, body src/sbg.h:4920-5032), called per point; with
+ * MSBG_GPU_IP_RENDER_DENS, MSBG::interpolateRenderDensity (src/msbg.h:478-484).
+ *  - uint16 values are interpolated unscaled unless MSBG_GPU_IP_RENDER_DENS is given
+ *    (then times 1/65535); FP16 values are widened to FP32.
+ *  - A block without payload reads the empty value 0.
+ *  - Points whose lower corner is outside [0, s-2] on an axis take the reference's
+ *    generic path (interpolateGen0<IP_LINEAR>, src/sbg.h:3109-3246): corners clamped
+ *    to the domain, or the Dirichlet variants below.
+ *  - opt: the reference's bits MSBG_GPU_IP_CORNER (no half-voxel shift),
+ *    MSBG_GPU_IP_BC_DIRICHLET, MSBG_GPU_IP_BC_DIRICHLET_OLD, MSBG_GPU_IP_NO_BORDER_CHECK
+ *    (the border test is always made; results inside the domain are unchanged),
+ *    MSBG_GPU_IP_CHKBLK (no effect), plus MSBG_GPU_IP_RENDER_DENS.  Other bits:
+ *    MSBG_GPU_ERR_UNSUPPORTED.
+ * Asynchronous on the context's stream. */
+enum {
+  MSBG_GPU_IP_CORNER = 1 << 0,            /* OPT_IPCORNER           (src/sbg.h:142) */
+  MSBG_GPU_IP_CHKBLK = 1 << 5,            /* OPT_IPCHKBLK           (src/sbg.h:147) */
+  MSBG_GPU_IP_BC_DIRICHLET = 1 << 13,     /* OPT_IPBC_DIRICHLET     (src/sbg.h:155) */
+  MSBG_GPU_IP_BC_DIRICHLET_OLD = 1 << 14, /* OPT_IPBC_DIRICHLET_OLD (src/sbg.h:156) */
+  MSBG_GPU_IP_NO_BORDER_CHECK = 1 << 15,  /* OPT_IP_NO_BORDER_CHECK (src/sbg.h:157) */
+  MSBG_GPU_IP_RENDER_DENS = 1 << 18       /* uint16 render density; a bit the reference's
+                                             option enum leaves unused */
+};
+int msbg_gpu_interpolate(msbg_gpu_ctx *ctx, int chan, const float *dPts, int64_t n, float *dOut,
+                         int opt);
 /* One multigrid V-cycle X = M^{-1} B from X = 0 (the CG preconditioner). */
 int msbg_gpu_vcycle(msbg_gpu_ctx *ctx, int chanX, int chanB);
 /* dotProdChannel (src/msbg.h:3331-3341): FP64-accumulated sum; MSBG_GPU_ERR_NONFINITE

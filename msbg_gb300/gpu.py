@@ -29,6 +29,9 @@ OPT_8_COLOR_SCHEME = 1 << 29
 PDE_MEAN_CURVATURE = 4
 LAPL_MCF_8COLOR = -(PDE_MEAN_CURVATURE + OPT_8_COLOR_SCHEME)
 SWEEP_EXACT, SWEEP_FAST = 0, 1
+# interpolation options (src/sbg.h:140-170) and the uint16 render-density scale
+IP_CORNER, IP_CHKBLK, IP_BC_DIRICHLET, IP_BC_DIRICHLET_OLD = 1 << 0, 1 << 5, 1 << 13, 1 << 14
+IP_NO_BORDER_CHECK, IP_RENDER_DENS = 1 << 15, 1 << 18
 
 BLK_DOM_BORDER, BLK_COARSE_FINE, BLK_FINE_COARSE = 1 << 1, 1 << 2, 1 << 3
 BLK_EXISTS, BLK_UNIFORM_EMPTY = 1 << 12, 1 << 13
@@ -86,6 +89,7 @@ SIGNATURES = {
     "msbg_gpu_multiply_laplacian": (I, [P, I, I, I, I]),
     "msbg_gpu_relax": (I, [P, I, I, I, I]),
     "msbg_gpu_downsample_channel": (I, [P, I, P, I]),
+    "msbg_gpu_interpolate": (I, [P, I, P, I64, P, I]),
     "msbg_gpu_diag_wait_timeout": (I, [P, I]),
     "msbg_gpu_vcycle": (I, [P, I, I]),
     "msbg_gpu_dot": (I, [P, I, I, C.POINTER(D)]),
@@ -369,6 +373,34 @@ class MultiresSparseGrid:
         finally:
             buf.free()
         return out.reshape(-1, cb ** 3)
+
+    def interpolate_device(self, chan: int, d_pts: DeviceBuffer, n: int, d_out: DeviceBuffer,
+                           opt: int = 0):
+        """Trilinear interpolation of channel chan at n device points (xyz float32) into
+        n device floats; asynchronous on the context's stream."""
+        self._check(self.L.msbg_gpu_interpolate(self.h, chan, C.c_void_p(d_pts.ptr), n,
+                                                C.c_void_p(d_out.ptr), opt))
+
+    def interpolate(self, chan: int, pts: np.ndarray, opt: int = 0) -> np.ndarray:
+        """Per-point interpolateFloatFast / interpolateUint16ToFloatFast (src/sbg.h:4623-4792,
+        src/sbg.h:4920-5032); with IP_RENDER_DENS, interpolateRenderDensity
+        (src/msbg.h:478-484).  Host points in, host float32 values out."""
+        pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 3)
+        n = pts.shape[0]
+        out = np.empty(n, np.float32)
+        dp = DeviceBuffer.alloc(max(n, 1) * 12)
+        do = DeviceBuffer.alloc(max(n, 1) * 4)
+        try:
+            if n:
+                self._check(self.L.msbg_gpu_copy_h2d(self.h, C.c_void_p(dp.ptr), _ptr(pts), n * 12))
+            self.interpolate_device(chan, dp, n, do, opt)
+            if n:
+                self._check(self.L.msbg_gpu_copy_d2h(self.h, _ptr(out), C.c_void_p(do.ptr), n * 4))
+            self.synchronize()
+        finally:
+            dp.free()
+            do.free()
+        return out
 
     def dotProdChannel(self, a: int, b: int) -> float:
         out = C.c_double()

@@ -1111,3 +1111,68 @@ void orc_downsample(const orc_grid *g, const int32_t *slot, const int32_t *activ
         }
   }
 }
+
+/* ---- grid-to-particle interpolation ---------------------------------------------- */
+
+/* The stored value at a voxel as a float, without the uint16 density scale. */
+static float ip_raw(const orc_grid *g, const int32_t *slot, const void *payload, int x, int y, int z) {
+  const int bs = g->bsx, L = ilog2(bs), m = bs - 1;
+  const int64_t bid = (int64_t)(x >> L) + (int64_t)(y >> L) * g->nbx + (int64_t)(z >> L) * g->nbx * g->nby;
+  const int32_t s = slot[bid];
+  if (s < 0) return (float)g->emptyValue;
+  const int64_t i = (int64_t)s * bs * bs * bs + (((z & m) * bs + (y & m)) << L) + (x & m);
+  switch (g->storage) {
+    case ORC_F32: return ((const float *)payload)[i];
+    case ORC_U16: return (float)((const uint16_t *)payload)[i];
+    case ORC_F16: return orc_f16_to_f32(((const uint16_t *)payload)[i]);
+    default: return (float)((const double *)payload)[i];
+  }
+}
+
+static inline float ip_lerp(float t, float a, float b) { return fmaf(b - a, t, a); }
+static inline float ip_lin(float p0, float p1, float t) { return fmaf(p1, t, p0 * (1.0f - t)); }
+
+void orc_interpolate(const orc_grid *g, const int32_t *slot, const void *payload, const float *pts,
+                     int64_t n, int opt, float *out) {
+  const float po = (opt & ORC_IP_CORNER) ? 0.0f : 0.5f;
+  const int dom[3] = {g->sx, g->sy, g->sz};
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < n; k++) {
+    float pos[3], t[3];
+    int ip[3], inside = 1;
+    for (int a = 0; a < 3; a++) {
+      pos[a] = pts[3 * k + a] - po;
+      const float pf = floorf(pos[a]);
+      ip[a] = (int)pf;
+      t[a] = pos[a] - pf;
+      if (!(ip[a] >= 0 && ip[a] < dom[a] - 1)) inside = 0;
+    }
+    float c[8];
+    float val;
+    if (inside) {
+      for (int i = 0; i < 8; i++) c[i] = ip_raw(g, slot, payload, ip[0] + (i & 1), ip[1] + ((i >> 1) & 1), ip[2] + (i >> 2));
+      const float a0 = ip_lerp(t[0], c[0], c[1]), a1 = ip_lerp(t[0], c[2], c[3]);
+      const float a2 = ip_lerp(t[0], c[4], c[5]), a3 = ip_lerp(t[0], c[6], c[7]);
+      const float b0 = ip_lerp(t[1], a0, a1), b1 = ip_lerp(t[1], a2, a3);
+      val = ip_lerp(t[2], b0, b1);
+    } else if (opt & ORC_IP_BC_DIRICHLET_OLD) {
+      val = (float)g->emptyValue;
+    } else {
+      for (int i = 0; i < 8; i++) {
+        int cc[3] = {ip[0] + (i & 1), ip[1] + ((i >> 1) & 1), ip[2] + (i >> 2)}, clipped = 0;
+        for (int a = 0; a < 3; a++) {
+          if (cc[a] < 0) { cc[a] = 0; clipped = 1; }
+          if (cc[a] >= dom[a]) { cc[a] = dom[a] - 1; clipped = 1; }
+        }
+        c[i] = ((opt & ORC_IP_BC_DIRICHLET) && clipped) ? (float)g->emptyValue
+                                                        : ip_raw(g, slot, payload, cc[0], cc[1], cc[2]);
+      }
+      const float a0 = ip_lin(c[0], c[1], t[0]), a1 = ip_lin(c[2], c[3], t[0]);
+      const float a2 = ip_lin(c[4], c[5], t[0]), a3 = ip_lin(c[6], c[7], t[0]);
+      const float b0 = ip_lin(a0, a1, t[1]), b1 = ip_lin(a2, a3, t[1]);
+      val = ip_lin(b0, b1, t[2]);
+    }
+    if ((opt & ORC_IP_RENDER_DENS) && g->storage == ORC_U16) val *= kU16ToF;
+    out[k] = val;
+  }
+}

@@ -110,6 +110,36 @@ int orc_pde(const orc_grid *g, const int32_t *slot, const int32_t *activeBids, i
 void orc_downsample(const orc_grid *g, const int32_t *slot, const int32_t *activeBids, int32_t nActive,
                     const void *payload, int simpleAverage, float *out);
 
+/* ---- grid-to-particle interpolation (trilinear) ----------------------------
+ * SparseGrid<float>::interpolateFloatFast (src/sbg.h:4623-4792) and
+ * SparseGrid<uint16_t>::interpolateUint16ToFloatFast (src/sbg.h:4920-5032) at n points
+ * pts[3i..3i+2] (voxel units; the voxel centre of cell i is i + 0.5).
+ *  - pos = p - 0.5 (not with ORC_IP_CORNER); i = floor(pos); t = pos - i.
+ *  - Corner values are the stored values as floats: FP32 as is, uint16 unscaled, FP16
+ *    widened; a block without payload reads emptyValue.
+ *  - Inside (0 <= i <= s-2 on every axis): lerp(t, a, b) = fma(b - a, t, a)
+ *    (vlerp_ps, src/vectorclass_util.h:143-146) along x for the 4 corner pairs, then y,
+ *    then z.
+ *  - Otherwise the generic path interpolateGen0<IP_LINEAR> (src/sbg.h:3109-3246): corner
+ *    coordinates clamped to the domain (ORC_IP_BC_DIRICHLET: a corner with a clamped
+ *    coordinate reads emptyValue; ORC_IP_BC_DIRICHLET_OLD: the result is emptyValue),
+ *    lerps in the same order as Interpolate1D (src/sbg.h:2934-2940), p1*t + p0*(1-t),
+ *    which the reference's own flags (-O3 -ffast-math, FMA hardware) compile to
+ *    fma(p1, t, p0*(1-t)).  That form is pinned against the compiled reference.
+ *  - ORC_IP_RENDER_DENS (uint16 only): the value times 1/65535
+ *    (interpolateRenderDensity, src/msbg.h:478-484).
+ *  - ORC_IP_NO_BORDER_CHECK changes nothing for points inside the domain; the border
+ *    test is always made. */
+enum {
+  ORC_IP_CORNER = 1 << 0,
+  ORC_IP_BC_DIRICHLET = 1 << 13,
+  ORC_IP_BC_DIRICHLET_OLD = 1 << 14,
+  ORC_IP_NO_BORDER_CHECK = 1 << 15,
+  ORC_IP_RENDER_DENS = 1 << 18
+};
+void orc_interpolate(const orc_grid *g, const int32_t *slot, const void *payload, const float *pts,
+                     int64_t n, int opt, float *out);
+
 /* ---- conversions (exposed for tests) ---- */
 uint16_t orc_f32_to_f16(float f);
 float orc_f16_to_f32(uint16_t h);

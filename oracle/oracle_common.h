@@ -10,6 +10,12 @@
  *   finalize -> applyChannelPdeFast (in-place 8-color or plain schedules).
  * A "levels job" runs regularizeRefinementMap + setRefinementMap on a given
  * per-block level map with the multi-level grid (src/msbg.cpp:1202-2165).
+ * An "interp job" loads a given payload into the value blocks of a single-level
+ * grid (every other block is the constant empty block, value 0) and interpolates
+ * it at query points: SparseGrid<float>::interpolateFloatFast (src/sbg.h:4623-4792),
+ * SparseGrid<uint16_t>::interpolateUint16ToFloatFast (src/sbg.h:4920-5032), or, with
+ * ORACLE_IP_RENDER_DENS, MultiresSparseGrid::interpolateRenderDensity
+ * (src/msbg.h:478-484, a free function: the uint16 value times 1/65535).
  */
 #ifndef MSBG_ORACLE_COMMON_H
 #define MSBG_ORACLE_COMMON_H
@@ -20,7 +26,17 @@
 #define ORACLE_OUT_MAGIC "MSBGOUT2"
 
 enum { ORACLE_CHAN_F32 = 0, ORACLE_CHAN_U16 = 1 };
-enum { ORACLE_JOB_SURFACE = 1, ORACLE_JOB_LEVELS = 2 };
+enum { ORACLE_JOB_SURFACE = 1, ORACLE_JOB_LEVELS = 2, ORACLE_JOB_INTERP = 3 };
+
+/* Interp job option bits: the reference's own interpolation options (src/sbg.h:140-170)
+ * plus one bit that the reference's enum leaves unused, for the render-density scale. */
+enum {
+  ORACLE_IP_CORNER = 1 << 0,           /* OPT_IPCORNER: no half-voxel shift */
+  ORACLE_IP_BC_DIRICHLET = 1 << 13,    /* OPT_IPBC_DIRICHLET: clipped corners read empty */
+  ORACLE_IP_BC_DIRICHLET_OLD = 1 << 14,/* OPT_IPBC_DIRICHLET_OLD: border points give empty */
+  ORACLE_IP_NO_BORDER_CHECK = 1 << 15, /* OPT_IP_NO_BORDER_CHECK */
+  ORACLE_IP_RENDER_DENS = 1 << 18      /* uint16: interpolateRenderDensity */
+};
 
 typedef struct {
   char magic[8];
@@ -30,15 +46,17 @@ typedef struct {
   int32_t chanType; /* ORACLE_CHAN_* */
   int32_t nIter;    /* applyChannelPdeFast numIter (rounded up to even inside) */
   int32_t laplTyp;  /* applyChannelPdeFast laplTyp, signed as the reference wants */
-  int32_t constr01; /* doConstrZeroOne */
+  int32_t constr01; /* doConstrZeroOne; interp job: ORACLE_IP_* option bits */
   int32_t nThreads; /* OpenMP threads for the reference's parallel loops */
   float dt;         /* applyChannelPdeFast timeStep */
   float rParticle;  /* splat kernel radius (demo: 2) */
   float nbDist;     /* narrow band added to the scan radius (demo: 2) */
   float anisAlpha;  /* applyChannelPdeFast anisDiffAlpha (Perona-Malik) */
   int32_t reserved; /* keeps the int64 fields 8-byte aligned */
-  int64_t nPoints;  /* surface job: float32 xyz follow; levels job: 0 */
-  int64_t nBlocksIn;/* levels job: int32 levels[nBlocksIn] follow */
+  int64_t nPoints;  /* surface / interp job: float32 xyz follow; levels job: 0 */
+  int64_t nBlocksIn;/* levels job: int32 levels[nBlocksIn] follow;
+                       interp job: int32 activeBids[nBlocksIn] follow, then the
+                       payload [nBlocksIn][bsx^3] of the channel type */
 } OracleJobHeader;
 
 typedef struct {
@@ -52,7 +70,8 @@ typedef struct {
   int32_t nThreadsUsed;
   /* then: int8 levels[nBlocks]; uint16 flags[nBlocks];
    *       int32 activeBids[nActive];
-   *       payloadAfterFinalize[nActive*bsx^3]; payloadAfterPde[nActive*bsx^3] */
+   *       payloadAfterFinalize[nActive*bsx^3]; payloadAfterPde[nActive*bsx^3]
+   * interp job: tPdeSec = interpolation time; then float32 values[nPoints] */
 } OracleOutHeader;
 
 #endif

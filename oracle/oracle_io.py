@@ -26,7 +26,15 @@ REF_DRIVER = os.path.join(HERE, "_ref", "msbg_ref_driver")
 JOB_MAGIC = b"MSBGJOB2"
 OUT_MAGIC = b"MSBGOUT2"
 CHAN_F32, CHAN_U16 = 0, 1
-JOB_SURFACE, JOB_LEVELS = 1, 2
+JOB_SURFACE, JOB_LEVELS, JOB_INTERP = 1, 2, 3
+
+# interpolation options: the reference's bits (src/sbg.h:140-170) and the render-density
+# scale of the uint16 channel (a bit the reference's enum leaves unused)
+IP_CORNER = 1 << 0
+IP_BC_DIRICHLET = 1 << 13
+IP_BC_DIRICHLET_OLD = 1 << 14
+IP_NO_BORDER_CHECK = 1 << 15
+IP_RENDER_DENS = 1 << 18
 
 # OracleJobHeader: magic[8], 11 x int32, 4 x float, int32, 2 x int64
 _JOB_FMT = "<8s11i4fi2q"
@@ -96,6 +104,44 @@ def write_levels_job(path: str, sx: int, sy: int, sz: int, bsx: int, n_levels: i
     with open(path, "wb") as f:
         f.write(hdr)
         f.write(lv.tobytes())
+
+
+def write_interp_job(path: str, sx: int, sy: int, sz: int, bsx: int, chan: int,
+                     active_bids: np.ndarray, payload: np.ndarray, points: np.ndarray,
+                     opt: int = 0, n_threads: int = 0) -> None:
+    pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+    bids = np.ascontiguousarray(active_bids, dtype=np.int32).ravel()
+    pay = np.ascontiguousarray(payload, dtype=np.float32 if chan == CHAN_F32 else np.uint16)
+    if pay.size != bids.size * bsx ** 3:
+        raise ValueError("payload size does not match the active blocks")
+    hdr = struct.pack(_JOB_FMT, JOB_MAGIC, JOB_INTERP, sx, sy, sz, bsx, 3, chan, 0, 0, opt,
+                      n_threads, 0.0, 0.0, 0.0, 0.0, 0, pts.shape[0], bids.size)
+    with open(path, "wb") as f:
+        f.write(hdr)
+        f.write(pts.tobytes())
+        f.write(bids.tobytes())
+        f.write(pay.tobytes())
+
+
+def run_reference_interp(sx, sy, sz, bsx, chan, active_bids, payload, points, opt: int = 0,
+                         n_threads: int = 0, timeout: float = 600) -> tuple[np.ndarray, float, int]:
+    """Interpolate a payload at points with the reference's own functions.
+
+    Returns (values float32 [n], seconds spent in the interpolation loop, threads)."""
+    with tempfile.TemporaryDirectory() as td:
+        jp, op = os.path.join(td, "job.bin"), os.path.join(td, "out.bin")
+        write_interp_job(jp, sx, sy, sz, bsx, chan, active_bids, payload, points, opt, n_threads)
+        subprocess.run([REF_DRIVER, jp, op], check=True, cwd=td, timeout=timeout,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        with open(op, "rb") as f:
+            buf = f.read()
+    hsz = struct.calcsize(_OUT_FMT)
+    h = struct.unpack(_OUT_FMT, buf[:hsz])
+    if h[0] != OUT_MAGIC:
+        raise ValueError("bad oracle output")
+    n = np.asarray(points).reshape(-1, 3).shape[0]
+    vals = np.frombuffer(buf, np.float32, n, hsz).copy()
+    return vals, float(h[17]), int(h[19])
 
 
 def read_result(path: str, bsx: int, surface: bool = True) -> OracleResult:

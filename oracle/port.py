@@ -70,6 +70,7 @@ def lib():
                                         C.c_int, C.c_int64, C.POINTER(C.c_int), C.POINTER(C.c_double)]
         L.orc_poisson_coeffs_dense.argtypes = [C.c_uint32, C.c_int, C.c_int, C.c_int, P, P, P, P, P]
         L.orc_downsample.argtypes = [C.POINTER(Grid), P, P, C.c_int32, P, C.c_int, P]
+        L.orc_interpolate.argtypes = [C.POINTER(Grid), P, P, P, C.c_int64, C.c_int, P]
         L.orc_f32_to_f16.argtypes = [C.c_float]
         L.orc_f32_to_f16.restype = C.c_uint16
         L.orc_f16_to_f32.argtypes = [C.c_uint16]
@@ -147,6 +148,21 @@ def downsample(g: Grid, slot, active_bids, payload: np.ndarray, simple_average: 
     payload = np.ascontiguousarray(payload)
     out = np.zeros((len(bids), cb ** 3), np.float32)
     lib().orc_downsample(C.byref(g), _p(slot), _p(bids), len(bids), _p(payload), int(simple_average), _p(out))
+    return out
+
+
+IP_CORNER, IP_BC_DIRICHLET, IP_BC_DIRICHLET_OLD = 1 << 0, 1 << 13, 1 << 14
+IP_NO_BORDER_CHECK, IP_RENDER_DENS = 1 << 15, 1 << 18
+
+
+def interpolate(g: Grid, slot, payload: np.ndarray, pts: np.ndarray, opt: int = 0) -> np.ndarray:
+    """Trilinear interpolation at points, restated from interpolateFloatFast /
+    interpolateUint16ToFloatFast (src/sbg.h:4623-4792, src/sbg.h:4920-5032): float32 [n]."""
+    slot = np.ascontiguousarray(slot, np.int32)
+    payload = np.ascontiguousarray(payload)
+    pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 3)
+    out = np.zeros(pts.shape[0], np.float32)
+    lib().orc_interpolate(C.byref(g), _p(slot), _p(payload), _p(pts), pts.shape[0], int(opt), _p(out))
     return out
 
 

@@ -10,7 +10,8 @@
  * arithmetic and their control flow (including the "abort this particle on a
  * non-value block" rule at src/msbg_demo.cpp:613-618).  Everything else is the
  * library itself: MultiresSparseGrid::create, regularizeRefinementMap,
- * setRefinementMap, SparseGrid block management and applyChannelPdeFast<T>.
+ * setRefinementMap, SparseGrid block management, applyChannelPdeFast<T> and the
+ * trilinear interpolation functions (interp job).
  *
  * Differences from the demo, both forced by the workload definition:
  *  - points come from the job file (already in voxel coordinates) instead of
@@ -303,6 +304,69 @@ int runLevelsJob(const OracleJobHeader &job, const int32_t *levelsIn, FILE *fout
   return 0;
 }
 
+// Interpolation of a given payload at query points by the reference's own functions
+// (src/sbg.h:4623-4792, src/sbg.h:4920-5032, src/msbg.h:478-484).  The grid is the
+// single-level one of the surface job; value blocks get the caller's payload and every
+// other block is the constant empty block (empty value 0).
+template <typename T>
+int runInterpJob(const OracleJobHeader &job, const float *pts, const int32_t *bids,
+                 const T *payload, FILE *fout) {
+  OracleOutHeader out;
+  memset(&out, 0, sizeof(out));
+  memcpy(out.magic, ORACLE_OUT_MAGIC, 8);
+  const int chan = (sizeof(T) == 4) ? MSBG::CH_FLOAT_1 : MSBG::CH_UINT16_1;
+  MultiresSparseGrid *msbg = MultiresSparseGrid::create(
+      "TEST", job.sx, job.sy, job.sz, job.bsx, -1, 0, -1,
+      MSBG::OPT_SINGLE_LEVEL | MSBG::OPT_SINGLE_CHANNEL_FLOAT);
+  if (!msbg) return 2;
+  SparseGrid<T> *sg0 = MSBG::getChannel<T>(msbg, chan, 0);
+  if (!sg0) return 3;
+  const int nBlocks = msbg->nBlocks();
+  std::vector<int> levels(nBlocks, msbg->getNumLevels() - 1);
+  for (int64_t t = 0; t < job.nBlocksIn; t++) {
+    if (bids[t] < 0 || bids[t] >= nBlocks) return 4;
+    levels[bids[t]] = 0;
+  }
+  msbg->regularizeRefinementMap(levels.data());
+  msbg->setRefinementMap(levels.data(), NULL, -1, NULL, false);
+  sg0->reset();
+  sg0->prepareDataAccess();
+  sg0->setEmptyValue(Quant<T>::zero());
+  sg0->setFullValue(Quant<T>::one());
+  for (int bid = 0; bid < nBlocks; bid++) sg0->setEmptyBlock(bid);
+  const size_t nv = (size_t)sg0->nVoxelsInBlock();
+  for (int64_t t = 0; t < job.nBlocksIn; t++) {
+    T *data = sg0->getBlockDataPtr(bids[t], 1, 0);
+    memcpy(data, payload + (size_t)t * nv, nv * sizeof(T));
+  }
+  const int opt = job.constr01;
+  std::vector<float> vals((size_t)job.nPoints);
+  const double t0 = nowSec();
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < job.nPoints; i++) {
+    const Vec4f pos(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2], 0.f);
+    float f;
+    if constexpr (sizeof(T) == 4) {
+      f = sg0->interpolateFloatFast(pos, opt & ~ORACLE_IP_RENDER_DENS);
+    } else {
+      if (opt & ORACLE_IP_RENDER_DENS)
+        f = MSBG::interpolateRenderDensity(sg0, pos, opt & ~ORACLE_IP_RENDER_DENS);
+      else
+        f = sg0->interpolateUint16ToFloatFast(pos, opt);
+    }
+    vals[i] = f;
+  }
+  out.tPdeSec = nowSec() - t0;
+  out.nBlocks = nBlocks;
+  out.nActive = (int)job.nBlocksIn;
+  out.elemBytes = (int)sizeof(T);
+  out.nThreadsUsed = omp_get_max_threads();
+  fwrite(&out, sizeof(out), 1, fout);
+  fwrite(vals.data(), 4, vals.size(), fout);
+  MultiresSparseGrid::destroy(msbg);
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -321,6 +385,13 @@ int main(int argc, char **argv) {
   std::vector<int32_t> lv((size_t)job.nBlocksIn);
   if (job.nPoints && fread(pts.data(), 4, pts.size(), fin) != pts.size()) return 1;
   if (job.nBlocksIn && fread(lv.data(), 4, lv.size(), fin) != lv.size()) return 1;
+  std::vector<uint8_t> payload;
+  if (job.jobType == ORACLE_JOB_INTERP) {
+    const size_t elem = job.chanType == ORACLE_CHAN_U16 ? 2 : 4;
+    payload.resize((size_t)job.nBlocksIn * job.bsx * job.bsx * job.bsx * elem);
+    if (!payload.empty() && fread(payload.data(), 1, payload.size(), fin) != payload.size())
+      return 1;
+  }
   fclose(fin);
 
   if (job.nThreads > 0) {
@@ -334,6 +405,12 @@ int main(int argc, char **argv) {
   int rc;
   if (job.jobType == ORACLE_JOB_LEVELS)
     rc = runLevelsJob(job, lv.data(), fout);
+  else if (job.jobType == ORACLE_JOB_INTERP && job.chanType == ORACLE_CHAN_U16)
+    rc = runInterpJob<uint16_t>(job, pts.data(), lv.data(),
+                                reinterpret_cast<const uint16_t *>(payload.data()), fout);
+  else if (job.jobType == ORACLE_JOB_INTERP)
+    rc = runInterpJob<float>(job, pts.data(), lv.data(),
+                             reinterpret_cast<const float *>(payload.data()), fout);
   else if (job.chanType == ORACLE_CHAN_U16)
     rc = runSurfaceJob<uint16_t>(job, pts.data(), job.nBlocksIn ? lv.data() : nullptr, fout);
   else

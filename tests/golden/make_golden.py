@@ -8,6 +8,9 @@ This script needs the reference sources, so it runs in the build container,
 never on the GPU host; the .npz files it writes are committed.
 
     python tests/golden/make_golden.py
+
+It writes reference_small.npz (splat, levels, sweeps) and reference_interp.npz
+(trilinear interpolation).
 """
 from __future__ import annotations
 
@@ -99,6 +102,53 @@ def main() -> None:
         out[f"lvl{nl}_per_level"] = r.blocks_per_level
 
     path = os.path.join(HERE, "reference_small.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
+    make_interp(out)
+
+
+IP_OPTS = (0, O.IP_CORNER, O.IP_BC_DIRICHLET, O.IP_BC_DIRICHLET_OLD, O.IP_CORNER | O.IP_BC_DIRICHLET,
+           O.IP_RENDER_DENS)
+
+
+def interp_points(n: int, res: int, bsx: int, seed: int) -> np.ndarray:
+    """Points for the interpolation cases: uniform over the domain and 1.5 voxels beyond
+    it, a quarter snapped to integers, half-integers and block upper faces."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    p = rng.uniform(-1.5, res + 1.5, (n, 3)).astype(np.float32)
+    q = n // 4
+    p[:q] = np.floor(p[:q]) + rng.choice(np.array([0.0, 0.5, 0.25], np.float32), (q, 3))
+    p[q:2 * q, 0] = (rng.integers(0, res // bsx, q) * bsx + bsx - 0.5 +
+                     rng.uniform(0, 1, q)).astype(np.float32)
+    return p
+
+
+def make_interp(small: dict) -> None:
+    """Reference values of interpolateFloatFast / interpolateUint16ToFloatFast /
+    interpolateRenderDensity (oracle/ref_driver.cpp, interp job)."""
+    out = {}
+    # (1) the golden MCF fields at the golden points (the particles of the surface)
+    bids = small["active_bids"]
+    for name, chan, key in (("f32", O.CHAN_F32, "pde_mcf8_f32"), ("u16", O.CHAN_U16, "pde_mcf8_u16_odd")):
+        for opt in (0, O.IP_RENDER_DENS) if chan == O.CHAN_U16 else (0,):
+            v, _, _ = O.run_reference_interp(RES, RES, RES, BSX, chan, bids, small[key], small["points"], opt)
+            out[f"surf_{name}_{opt}"] = v
+    # (2) a seeded payload on a layout that touches every face of a 32^3 domain, bs 8
+    res, bs = 32, 8
+    nb = (res // bs) ** 3
+    rng = np.random.Generator(np.random.PCG64(20261203 + 920))
+    rbids = np.nonzero(rng.random(nb) < 0.8)[0].astype(np.int32)
+    u16 = rng.integers(0, 65536, (len(rbids), bs ** 3), dtype=np.uint16)
+    f32 = (u16.astype(np.float32) * np.float32(1.0 / 65536.0)).astype(np.float32)
+    pts = interp_points(2000, res, bs, 20261203 + 921)
+    out.update(rand_res=np.int32(res), rand_bsx=np.int32(bs), rand_bids=rbids, rand_u16=u16, rand_points=pts)
+    for name, chan, pay in (("f32", O.CHAN_F32, f32), ("u16", O.CHAN_U16, u16)):
+        for opt in IP_OPTS:
+            if chan == O.CHAN_F32 and opt & O.IP_RENDER_DENS:
+                continue
+            v, _, _ = O.run_reference_interp(res, res, res, bs, chan, rbids, pay, pts, opt)
+            out[f"rand_{name}_{opt}"] = v
+    path = os.path.join(HERE, "reference_interp.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
 
