@@ -383,6 +383,15 @@ def run_gpu(args, spec, dist: Dist):
                             "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
                             "algorithmic_bytes_per_point": 16}}
 
+    # cross-resolution halo fill (HaloBlockSet::fillHaloBlock_, OPT_BC_COARSE_LEVEL, halo 1)
+    # of every level-0 block of the swept field: level 0 of a level channel bound to the
+    # value-block slab (states: slots, "no block" off level 0), level 1 the level-1
+    # blocks.  Algorithmic bytes per block: the (bs+2)^3 box read once at S bytes per
+    # value and written once as FP32.
+    halo = None
+    if not args.no_jacobi:
+        halo = halo_measure(g, info, storage, elem, bsx, args.steps, dist, peaks)
+
     # e2e through the host-buffer entry point
     e2e = None
     if not args.no_e2e:
@@ -446,9 +455,58 @@ def run_gpu(args, spec, dist: Dist):
         "jacobi_sweeps": jacobi,
         "restriction": restriction,
         "g2p": g2p,
+        "halo_fill": halo,
         "poisson": poisson,
     }
     print(json.dumps(line), flush=True)
+
+
+def halo_measure(g, info, storage, elem, bsx, steps, dist, peaks, batch=16384) -> dict:
+    lv = g.levels()
+    slot = g.slots()
+    st0 = np.where(lv == 0, slot, G.LBLK_NONE).astype(np.int32)
+    n1 = int((lv == 1).sum())
+    st1 = np.full(lv.size, G.LBLK_NONE, np.int32)
+    st1[lv == 1] = np.arange(n1, dtype=np.int32)
+    d_st0 = g.to_device(st0)
+    g.level_grid_bind(0, 0, storage, d_st0.ptr, g.payload_ptr(0), 0.0, 1.0)
+    g.level_grid_set(0, 1, storage, st1, np.zeros((max(n1, 1), (bsx // 2) ** 3), G.NP_STORAGE[storage]),
+                     0.0, 1.0)
+    bids = np.nonzero(lv == 0)[0].astype(np.int32)
+    d_bids = g.to_device(bids)
+    hs = bsx + 2
+    nb = min(batch, len(bids))
+    d_out = G.DeviceBuffer.alloc(nb * hs ** 3 * 4)
+
+    def one_pass():
+        for k0 in range(0, len(bids), nb):
+            m = min(nb, len(bids) - k0)
+            g._check(g.L.msbg_gpu_fill_halo_blocks(g.h, 0, 0, C.c_void_p(d_bids.ptr + 4 * k0), m, 1,
+                                                   G.BC_COARSE_LEVEL, C.c_void_p(d_out.ptr), None))
+
+    for _ in range(3):
+        one_pass()
+    g.synchronize()
+    l0 = g.launch_count()
+    g.event_record(8)
+    for _ in range(steps):
+        one_pass()
+    g.event_record(9)
+    g.synchronize()
+    ms = dist.max(g.event_elapsed_ms(8, 9)) / steps
+    launches = (g.launch_count() - l0) // steps
+    sk = g.fill_halo_blocks_device(0, 0, d_bids, nb, 1, G.BC_COARSE_LEVEL, d_out, count_skipped=True)
+    d_out.free()
+    d_bids.free()
+    d_st0.free()
+    nbytes = len(bids) * hs ** 3 * (elem + 4)
+    gbs = nbytes / (ms / 1e3) / 1e9
+    return {"kernel": "kFillHalo (OPT_BC_COARSE_LEVEL, halo 1)", "blocks": int(len(bids)),
+            "level1_blocks": n1, "ms_per_pass": ms, "blocks_per_s": len(bids) * dist.world / (ms / 1e3),
+            "launches_per_pass": int(launches), "skipped": int(sk),
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": gbs / peaks["hbm_gbs"],
+                         "algorithmic_bytes_per_block": hs ** 3 * (elem + 4)}}
 
 
 WARMNET = os.path.join(ROOT, "msbg_gb300", "data", "warmnet_c3.npz")

@@ -247,6 +247,54 @@ enum {
 };
 int msbg_gpu_interpolate(msbg_gpu_ctx *ctx, int chan, const float *dPts, int64_t n, float *dOut,
                          int opt);
+/* ---- multi-level channels and the cross-resolution halo fill ----------------------
+ * A level grid is resolution level l of one channel of the reference's
+ * MultiresSparseGrid: the SparseGrid that getChannel<T>(msbg, chan, l) returns
+ * (src/msbg.h:720, src/msbg.h:3056-3076), with block edge bsx>>l, domain (sx>>l,
+ * sy>>l, sz>>l) and the block grid of level 0 (src/msbg.cpp:800-812).  A block has
+ * one state per level: payload (>= 0, the index of its data in hPayload), the
+ * constant empty block (MSBG_GPU_LBLK_EMPTY, SparseGrid::setEmptyBlock), the constant
+ * full block (MSBG_GPU_LBLK_FULL, setFullBlock) or no block (MSBG_GPU_LBLK_NONE, a
+ * NULL block-map entry).
+ * msbg_gpu_level_grid_set copies level `level` of level channel lchan (0..7, a
+ * namespace of its own, apart from the value-block channels) to the device: hState
+ * (host, nBlocks entries) and hPayload (host, nData blocks of (bsx>>level)^3 values of
+ * `storage`, x fastest).  emptyValue / fullValue are the constant blocks' values
+ * (setEmptyValue / setFullValue), stored in the storage type (uint16: v*65535 rounded
+ * half away from zero).  Every level of a level channel has the same storage (FP32,
+ * FP16 or uint16); setting a level with another storage clears the other levels. */
+enum { MSBG_GPU_LBLK_EMPTY = -1, MSBG_GPU_LBLK_FULL = -2, MSBG_GPU_LBLK_NONE = -3 };
+int msbg_gpu_level_grid_set(msbg_gpu_ctx *ctx, int lchan, int level, int storage, const int32_t *hState,
+                            const void *hPayload, int64_t nData, float emptyValue, float fullValue);
+/* The same for data already on the device: binds the caller's device arrays (dState:
+ * nBlocks states; dPayload: the payload blocks) without copying.  They must stay valid,
+ * and unchanged while a fill reads them, until the level is set or bound again or the
+ * context is destroyed.  A level-0 value-block channel binds as its slab
+ * (msbg_gpu_payload_ptr) with states = its slots, -3 for blocks that are not at level 0. */
+int msbg_gpu_level_grid_bind(msbg_gpu_ctx *ctx, int lchan, int level, int storage, const int32_t *dState,
+                             const void *dPayload, float emptyValue, float fullValue);
+/* HaloBlockSet::fillHaloBlock_<T>(iChan, bid, levelMg = 0, tid, options)
+ * (src/halo.h:385-391, body src/halo.cpp:266-479, out-of-block rule
+ * getOutOfBlockValue src/halo.h:270-330) for n blocks in one call.
+ * dBids (device, n entries): blocks whose level in the current layout is `level` and
+ * that have a block at that level of lchan.  dOut (device): per listed block k,
+ * (bs+2h)^3 floats at dOut + k*(bs+2h)^3, [z][y][x] over the positions origin-h ..
+ * origin+bs+h-1 of level `level` (bs = bsx>>level, h = haloSize, 1..4).  A position
+ * inside the domain whose block exists at that level reads it; otherwise
+ *  - MSBG_GPU_BC_NEUMANN (OPT_BC_NEUMANN): the own block at the position clamped to it;
+ *  - MSBG_GPU_BC_COARSE_LEVEL (OPT_BC_COARSE_LEVEL): outside the domain the position is
+ *    clamped to it and read at this level if that block exists; else the position,
+ *    halved, is read at level+1 (clamped to its domain) -- the cross-resolution fill;
+ *  - neither: the level's empty value.
+ * The reference needs a block at level+1 there; without one (or at the coarsest
+ * level) the empty value is used.  uint16 reads as v/65535, FP16 widened.
+ * OPT_INTERPOLATE (interpolateGhost) is not supported (MSBG_GPU_ERR_UNSUPPORTED).
+ * Blocks that do not satisfy the conditions are skipped (output not written); when
+ * hSkipped is not NULL the call synchronizes and stores their number there, else it
+ * is asynchronous on the context's stream. */
+enum { MSBG_GPU_BC_NEUMANN = 1 << 10, MSBG_GPU_BC_COARSE_LEVEL = 1 << 26 };
+int msbg_gpu_fill_halo_blocks(msbg_gpu_ctx *ctx, int lchan, int level, const int32_t *dBids, int64_t n,
+                              int haloSize, int opt, float *dOut, int64_t *hSkipped);
 /* One multigrid V-cycle X = M^{-1} B from X = 0 (the CG preconditioner). */
 int msbg_gpu_vcycle(msbg_gpu_ctx *ctx, int chanX, int chanB);
 /* dotProdChannel (src/msbg.h:3331-3341): FP64-accumulated sum; MSBG_GPU_ERR_NONFINITE

@@ -406,6 +406,7 @@ extern "C" int msbg_gpu_destroy(msbg_gpu_ctx *ctx) {
   if (ctx->dTmpSlab) cudaFree(ctx->dTmpSlab);
   if (ctx->dPts) cudaFree(ctx->dPts);
   msbg::batchFree(ctx->batch);
+  msbg::levelChannelsFree(ctx->levelCh);
   msbg::warmNetFree(ctx->warmnet);
   msbg::poissonFree(ctx->poisson);
   for (auto &ev : ctx->ev) if (ev) cudaEventDestroy(ev);

@@ -15,7 +15,9 @@ namespace msbg {
 struct PoissonState;
 struct WarmNetState;
 struct BatchState;
+struct LevelChannels;
 void poissonFree(PoissonState *ps);
+void levelChannelsFree(LevelChannels *lc);
 void warmNetFree(WarmNetState *w);
 void batchFree(BatchState *b);
 constexpr int kMaxChannels = 64;
@@ -75,6 +77,7 @@ struct msbg_gpu_ctx {
   msbg::PoissonState *poisson = nullptr;   // solver hierarchy of the current layout
   msbg::WarmNetState *warmnet = nullptr;   // learned warm start (weights, level-1 buffers)
   msbg::BatchState *batch = nullptr;       // batched solves: volumes of the layout, graph
+  msbg::LevelChannels *levelCh = nullptr;  // multi-level channels of the halo fill
   int mgPre = 2, mgPost = 2, mgTileIters = 3, mgCoarsestIter = 0;  // multigrid parameters
   std::string err;
 };

@@ -32,6 +32,10 @@ SWEEP_EXACT, SWEEP_FAST = 0, 1
 # interpolation options (src/sbg.h:140-170) and the uint16 render-density scale
 IP_CORNER, IP_CHKBLK, IP_BC_DIRICHLET, IP_BC_DIRICHLET_OLD = 1 << 0, 1 << 5, 1 << 13, 1 << 14
 IP_NO_BORDER_CHECK, IP_RENDER_DENS = 1 << 15, 1 << 18
+# halo fill options (OPT_BC_NEUMANN, OPT_BC_COARSE_LEVEL; src/msbg.h:101-131) and the
+# block states of a level grid
+BC_NEUMANN, BC_COARSE_LEVEL = 1 << 10, 1 << 26
+LBLK_EMPTY, LBLK_FULL, LBLK_NONE = -1, -2, -3
 
 BLK_DOM_BORDER, BLK_COARSE_FINE, BLK_FINE_COARSE = 1 << 1, 1 << 2, 1 << 3
 BLK_EXISTS, BLK_UNIFORM_EMPTY = 1 << 12, 1 << 13
@@ -90,6 +94,9 @@ SIGNATURES = {
     "msbg_gpu_relax": (I, [P, I, I, I, I]),
     "msbg_gpu_downsample_channel": (I, [P, I, P, I]),
     "msbg_gpu_interpolate": (I, [P, I, P, I64, P, I]),
+    "msbg_gpu_level_grid_set": (I, [P, I, I, I, P, P, I64, C.c_float, C.c_float]),
+    "msbg_gpu_level_grid_bind": (I, [P, I, I, I, P, P, C.c_float, C.c_float]),
+    "msbg_gpu_fill_halo_blocks": (I, [P, I, I, P, I64, I, I, P, C.POINTER(I64)]),
     "msbg_gpu_diag_wait_timeout": (I, [P, I]),
     "msbg_gpu_vcycle": (I, [P, I, I]),
     "msbg_gpu_dot": (I, [P, I, I, C.POINTER(D)]),
@@ -401,6 +408,52 @@ class MultiresSparseGrid:
             dp.free()
             do.free()
         return out
+
+    # ---- multi-level channels: HaloBlockSet::fillHaloBlock_ (src/halo.cpp:266-479) ----------
+    def level_grid_set(self, lchan: int, level: int, storage: int, state: np.ndarray,
+                       payload: np.ndarray | None, empty_value: float = 0.0, full_value: float = 1.0):
+        """Resolution level `level` of level channel lchan: per-block states (>= 0 payload
+        index, LBLK_EMPTY / LBLK_FULL / LBLK_NONE) and the payload [n][(bsx>>level)^3]."""
+        st = np.ascontiguousarray(state, np.int32)
+        n_data = 0 if payload is None else int(np.asarray(payload).reshape(-1).size // ((self.bsx >> level) ** 3))
+        pay = None if payload is None else np.ascontiguousarray(payload)
+        self._check(self.L.msbg_gpu_level_grid_set(self.h, lchan, level, storage, _ptr(st),
+                                                   None if pay is None else _ptr(pay), n_data,
+                                                   empty_value, full_value))
+
+    def level_grid_bind(self, lchan: int, level: int, storage: int, d_state: int, d_payload: int,
+                        empty_value: float = 0.0, full_value: float = 1.0):
+        """Binds device arrays (pointers) as level `level` of level channel lchan, no copy."""
+        self._check(self.L.msbg_gpu_level_grid_bind(self.h, lchan, level, storage, C.c_void_p(d_state),
+                                                    C.c_void_p(d_payload), empty_value, full_value))
+
+    def fill_halo_blocks_device(self, lchan: int, level: int, d_bids: DeviceBuffer, n: int, halo: int,
+                                opt: int, d_out: DeviceBuffer, count_skipped: bool = False) -> int:
+        """fillHaloBlock_ of n listed blocks (device int32 bids) into d_out
+        ([n][(bs+2h)^3] floats); returns the skipped count when asked (synchronizes)."""
+        sk = C.c_int64(-1)
+        self._check(self.L.msbg_gpu_fill_halo_blocks(self.h, lchan, level, C.c_void_p(d_bids.ptr), n, halo,
+                                                     opt, C.c_void_p(d_out.ptr),
+                                                     C.byref(sk) if count_skipped else None))
+        return int(sk.value)
+
+    def fill_halo_blocks(self, lchan: int, level: int, bids: np.ndarray, halo: int, opt: int):
+        """Host wrapper: (halo boxes float32 [n][(bs+2h)^3], skipped count)."""
+        bids = np.ascontiguousarray(bids, np.int32)
+        n = len(bids)
+        hs = (self.bsx >> max(level, 0)) + 2 * max(halo, 0)  # the call itself rejects bad values
+        out = np.empty((n, hs ** 3), np.float32)
+        db = self.to_device(bids)
+        do = DeviceBuffer.alloc(max(out.nbytes, 4))
+        try:
+            sk = self.fill_halo_blocks_device(lchan, level, db, n, halo, opt, do, count_skipped=True)
+            if n:
+                self._check(self.L.msbg_gpu_copy_d2h(self.h, _ptr(out), C.c_void_p(do.ptr), out.nbytes))
+            self.synchronize()
+        finally:
+            db.free()
+            do.free()
+        return out, sk
 
     def dotProdChannel(self, a: int, b: int) -> float:
         out = C.c_double()

@@ -1132,47 +1132,294 @@ static float ip_raw(const orc_grid *g, const int32_t *slot, const void *payload,
 static inline float ip_lerp(float t, float a, float b) { return fmaf(b - a, t, a); }
 static inline float ip_lin(float p0, float p1, float t) { return fmaf(p1, t, p0 * (1.0f - t)); }
 
-void orc_interpolate(const orc_grid *g, const int32_t *slot, const void *payload, const float *pts,
-                     int64_t n, int opt, float *out) {
+/* One point of orc_interpolate. */
+static float ip_point(const orc_grid *g, const int32_t *slot, const void *payload, const float p[3], int opt) {
   const float po = (opt & ORC_IP_CORNER) ? 0.0f : 0.5f;
   const int dom[3] = {g->sx, g->sy, g->sz};
-#pragma omp parallel for schedule(static)
-  for (int64_t k = 0; k < n; k++) {
-    float pos[3], t[3];
-    int ip[3], inside = 1;
-    for (int a = 0; a < 3; a++) {
-      pos[a] = pts[3 * k + a] - po;
-      const float pf = floorf(pos[a]);
-      ip[a] = (int)pf;
-      t[a] = pos[a] - pf;
-      if (!(ip[a] >= 0 && ip[a] < dom[a] - 1)) inside = 0;
-    }
-    float c[8];
-    float val;
-    if (inside) {
-      for (int i = 0; i < 8; i++) c[i] = ip_raw(g, slot, payload, ip[0] + (i & 1), ip[1] + ((i >> 1) & 1), ip[2] + (i >> 2));
-      const float a0 = ip_lerp(t[0], c[0], c[1]), a1 = ip_lerp(t[0], c[2], c[3]);
-      const float a2 = ip_lerp(t[0], c[4], c[5]), a3 = ip_lerp(t[0], c[6], c[7]);
-      const float b0 = ip_lerp(t[1], a0, a1), b1 = ip_lerp(t[1], a2, a3);
-      val = ip_lerp(t[2], b0, b1);
-    } else if (opt & ORC_IP_BC_DIRICHLET_OLD) {
-      val = (float)g->emptyValue;
-    } else {
-      for (int i = 0; i < 8; i++) {
-        int cc[3] = {ip[0] + (i & 1), ip[1] + ((i >> 1) & 1), ip[2] + (i >> 2)}, clipped = 0;
-        for (int a = 0; a < 3; a++) {
-          if (cc[a] < 0) { cc[a] = 0; clipped = 1; }
-          if (cc[a] >= dom[a]) { cc[a] = dom[a] - 1; clipped = 1; }
-        }
-        c[i] = ((opt & ORC_IP_BC_DIRICHLET) && clipped) ? (float)g->emptyValue
-                                                        : ip_raw(g, slot, payload, cc[0], cc[1], cc[2]);
-      }
-      const float a0 = ip_lin(c[0], c[1], t[0]), a1 = ip_lin(c[2], c[3], t[0]);
-      const float a2 = ip_lin(c[4], c[5], t[0]), a3 = ip_lin(c[6], c[7], t[0]);
-      const float b0 = ip_lin(a0, a1, t[1]), b1 = ip_lin(a2, a3, t[1]);
-      val = ip_lin(b0, b1, t[2]);
-    }
-    if ((opt & ORC_IP_RENDER_DENS) && g->storage == ORC_U16) val *= kU16ToF;
-    out[k] = val;
+  float pos[3], t[3];
+  int ip[3], inside = 1;
+  for (int a = 0; a < 3; a++) {
+    pos[a] = p[a] - po;
+    const float pf = floorf(pos[a]);
+    ip[a] = (int)pf;
+    t[a] = pos[a] - pf;
+    if (!(ip[a] >= 0 && ip[a] < dom[a] - 1)) inside = 0;
   }
+  float c[8];
+  float val;
+  if (inside) {
+    for (int i = 0; i < 8; i++) c[i] = ip_raw(g, slot, payload, ip[0] + (i & 1), ip[1] + ((i >> 1) & 1), ip[2] + (i >> 2));
+    const float a0 = ip_lerp(t[0], c[0], c[1]), a1 = ip_lerp(t[0], c[2], c[3]);
+    const float a2 = ip_lerp(t[0], c[4], c[5]), a3 = ip_lerp(t[0], c[6], c[7]);
+    const float b0 = ip_lerp(t[1], a0, a1), b1 = ip_lerp(t[1], a2, a3);
+    val = ip_lerp(t[2], b0, b1);
+  } else if (opt & ORC_IP_BC_DIRICHLET_OLD) {
+    val = (float)g->emptyValue;
+  } else {
+    for (int i = 0; i < 8; i++) {
+      int cc[3] = {ip[0] + (i & 1), ip[1] + ((i >> 1) & 1), ip[2] + (i >> 2)}, clipped = 0;
+      for (int a = 0; a < 3; a++) {
+        if (cc[a] < 0) { cc[a] = 0; clipped = 1; }
+        if (cc[a] >= dom[a]) { cc[a] = dom[a] - 1; clipped = 1; }
+      }
+      c[i] = ((opt & ORC_IP_BC_DIRICHLET) && clipped) ? (float)g->emptyValue
+                                                      : ip_raw(g, slot, payload, cc[0], cc[1], cc[2]);
+    }
+    const float a0 = ip_lin(c[0], c[1], t[0]), a1 = ip_lin(c[2], c[3], t[0]);
+    const float a2 = ip_lin(c[4], c[5], t[0]), a3 = ip_lin(c[6], c[7], t[0]);
+    const float b0 = ip_lin(a0, a1, t[1]), b1 = ip_lin(a2, a3, t[1]);
+    val = ip_lin(b0, b1, t[2]);
+  }
+  if ((opt & ORC_IP_RENDER_DENS) && g->storage == ORC_U16) val *= kU16ToF;
+  return val;
+}
+
+void orc_interpolate(const orc_grid *g, const int32_t *slot, const void *payload, const float *pts,
+                     int64_t n, int opt, float *out) {
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < n; k++) out[k] = ip_point(g, slot, payload, pts + 3 * k, opt);
+}
+
+/* ---- ray-march render (src/render.h:52-160, src/render.cpp:20-101) ---- */
+
+typedef struct { double x, y, z; } rv3;
+static inline rv3 rv(double x, double y, double z) { rv3 r = {x, y, z}; return r; }
+static inline rv3 rsub(rv3 a, rv3 b) { return rv(a.x - b.x, a.y - b.y, a.z - b.z); }
+/* dot(a, b) = a.x*b.x + a.y*b.y + a.z*b.z, contracted left to right */
+static inline double rdot(rv3 a, rv3 b) { return fma(a.z, b.z, fma(a.y, b.y, a.x * b.x)); }
+static inline rv3 rnormalize(rv3 v, int opt) {
+  const double len = sqrt(rdot(v, v));
+  if (!(len > (double)1e-20f)) return rv(0, 1, 0);
+  if (opt & ORC_RENDER_RECIP) {
+    const double r = 1.0 / len;
+    return rv(v.x * r, v.y * r, v.z * r);
+  }
+  return rv(v.x / len, v.y / len, v.z / len);
+}
+/* cross(a, b): a.y*b.z - a.z*b.y, ... contracted as fma(a.y, b.z, -(a.z*b.y)) */
+static inline rv3 rcross(rv3 a, rv3 b) {
+  return rv(fma(a.y, b.z, -(a.z * b.y)), fma(a.z, b.x, -(a.x * b.z)), fma(a.x, b.y, -(a.y * b.x)));
+}
+
+typedef struct {
+  const orc_grid *g;
+  const int32_t *slot;
+  const void *payload;
+  float res;
+  float domMin[3], domMax[3];
+} rnd_ctx;
+
+/* sampleDensity (src/render.h:89-117) */
+static double rnd_density(const rnd_ctx *c, rv3 p) {
+  const float q[3] = {c->res * (float)p.x, c->res * (float)p.y, c->res * (float)p.z};
+  const int dom[3] = {c->g->sx, c->g->sy, c->g->sz};
+  int ip[3];
+  for (int a = 0; a < 3; a++) {
+    ip[a] = (int)floorf(q[a]);
+    if (ip[a] < 0 || ip[a] > dom[a] - 1) return 0.0;
+  }
+  const int bs = c->g->bsx;
+  const int64_t bid = (int64_t)(ip[0] / bs) + (int64_t)(ip[1] / bs) * c->g->nbx +
+                      (int64_t)(ip[2] / bs) * c->g->nbx * c->g->nby;
+  if (c->slot[bid] < 0) return 0.0;  /* skip fast over empty blocks */
+  return (double)ip_point(c->g, c->slot, c->payload, q, ORC_IP_RENDER_DENS);
+}
+
+/* MtCubicBSplineWeights1D (src/mtool.h:344-362) */
+static void bspline3(float t, float w[4], float d[4]) {
+  const float s = 1.0f - t;
+  w[0] = (1.0f / 6.0f) * s * s * s;
+  w[1] = (2.0f / 3.0f) - 0.5f * t * t * (2.0f - t);
+  w[2] = (2.0f / 3.0f) - 0.5f * s * s * (1.0f + t);
+  w[3] = (1.0f / 6.0f) * t * t * t;
+  d[0] = -s * s / 2.0f;
+  d[1] = 0.5f * t * t - 1.0f * (2.0f - t) * t;
+  d[2] = 1.0f * s * (t + 1.0f) - 0.5f * s * s;
+  d[3] = t * t / 2.0f;
+}
+
+/* sampleDensityGradient (src/render.h:119-132): minus the gradient of the cubic
+ * B-spline interpolant, interpolateWithDerivs0<IP_BSPLINE_CUBIC> (src/sbg.h:3903-4133)
+ * with options 0: a window voxel outside the domain is clamped to it, a block without
+ * payload reads emptyValue; uint16 scaled by 1/65535. */
+static rv3 rnd_gradient(const rnd_ctx *c, rv3 p) {
+  const float q[3] = {c->res * (float)p.x, c->res * (float)p.y, c->res * (float)p.z};
+  for (int a = 0; a < 3; a++)
+    if (q[a] < c->domMin[a] || q[a] > c->domMax[a]) return rv(-0.0, -0.0, -0.0);
+  const int dom[3] = {c->g->sx, c->g->sy, c->g->sz};
+  float t[3], w[3][4], d[3][4];
+  int i0[3];
+  for (int a = 0; a < 3; a++) {
+    const float pos = q[a] - 0.5f, pf = floorf(pos);
+    t[a] = pos - pf;
+    i0[a] = (int)pf - 1;
+    bspline3(t[a], w[a], d[a]);
+  }
+  float gx = 0, gy = 0, gz = 0;
+  for (int dz = 0; dz < 4; dz++)
+    for (int dy = 0; dy < 4; dy++)
+      for (int dx = 0; dx < 4; dx++) {
+        int cc[3] = {i0[0] + dx, i0[1] + dy, i0[2] + dz};
+        for (int a = 0; a < 3; a++) cc[a] = cc[a] < 0 ? 0 : cc[a] >= dom[a] ? dom[a] - 1 : cc[a];
+        const float f = ip_raw(c->g, c->slot, c->payload, cc[0], cc[1], cc[2]);
+        const float wyz = w[2][dz] * w[1][dy];
+        gx = fmaf(wyz * d[0][dx], f, gx);
+        gy = fmaf(w[2][dz] * d[1][dy] * w[0][dx], f, gy);
+        gz = fmaf(d[2][dz] * w[1][dy] * w[0][dx], f, gz);
+      }
+  if (c->g->storage == ORC_U16) {
+    gx *= kU16ToF;
+    gy *= kU16ToF;
+    gz *= kU16ToF;
+  }
+  return rv(-1.0 * (double)gx, -1.0 * (double)gy, -1.0 * (double)gz);
+}
+
+void orc_render(const orc_grid *g, const int32_t *slot, const void *payload, int width, int height,
+                const orc_camera *cam, int opt, int32_t *pixels) {
+  rnd_ctx c;
+  c.g = g;
+  c.slot = slot;
+  c.payload = payload;
+  domain_limits(g, c.domMin, c.domMax);
+  const int res = g->sx > g->sy ? (g->sx > g->sz ? g->sx : g->sz) : (g->sy > g->sz ? g->sy : g->sz);
+  c.res = (float)res;
+  const double hstep = 1.0 / (double)res;
+  const int maxSteps = (int)(2.0 / hstep);
+  const double invW = 1.0 / (double)width, invH = 1.0 / (double)height;
+  const double aspect = (double)width / (double)height;
+  const rv3 camPos = rv(cam->pos[0], cam->pos[1], cam->pos[2]);
+  const rv3 fwd = rnormalize(rsub(rv(cam->lookAt[0], cam->lookAt[1], cam->lookAt[2]), camPos), opt);
+  const rv3 right = rnormalize(rcross(fwd, rv(0, 1, 0)), opt);
+  const rv3 up = rcross(right, fwd);
+  const rv3 sun = rv(cam->sun[0], cam->sun[1], cam->sun[2]);
+  const double zoom = cam->zoom;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int y = 0; y < height; y++) {
+    for (int x = 0; x < width; x++) {
+      const double ndcX = fma((double)((float)x + 0.5f), invW, -0.5) * 2.0 * aspect;
+      const double ndcY = fma(-(double)((float)y + 0.5f), invH, 0.5) * 2.0;
+      const rv3 dir = rnormalize(rv(fma(up.x, ndcY, fma(right.x, ndcX, fwd.x * zoom)),
+                                    fma(up.y, ndcY, fma(right.y, ndcX, fwd.y * zoom)),
+                                    fma(up.z, ndcY, fma(right.z, ndcX, fwd.z * zoom))), opt);
+      const rv3 inc = rv(dir.x * hstep, dir.y * hstep, dir.z * hstep);
+      rv3 pos = camPos, prevPos = camPos, hitPos = camPos;
+      double prev = rnd_density(&c, pos);
+      int hit = 0;
+      for (int step = 0; step < maxSteps; step++) {
+        pos = rv(pos.x + inc.x, pos.y + inc.y, pos.z + inc.z);
+        const double d = rnd_density(&c, pos);
+        if (prev < 0.5 && d >= 0.5) {
+          const double t = (0.5 - prev) / (d - prev);
+          hitPos = rv(fma(pos.x - prevPos.x, t, prevPos.x), fma(pos.y - prevPos.y, t, prevPos.y),
+                      fma(pos.z - prevPos.z, t, prevPos.z));
+          hit = 1;
+          break;
+        }
+        prev = d;
+        prevPos = pos;
+      }
+      int32_t col = 0x02000000;
+      if (hit) {
+        const rv3 nrm = rnormalize(rnd_gradient(&c, hitPos), opt);
+        const rv3 ld = rnormalize(rsub(sun, hitPos), opt);
+        double diff = rdot(nrm, ld);
+        diff = diff > 0.0 ? diff : 0.0;
+        int ch[3];
+        for (int k = 0; k < 3; k++) {
+          double v = cam->color[k] * diff;
+          v = v < 0.0 ? 0.0 : v > 1.0 ? 1.0 : v;
+          ch[k] = (int)(uint8_t)(int)fma(v, 255.0, 0.5);
+        }
+        col = 0x02000000 | (ch[2] << 16) | (ch[1] << 8) | ch[0];
+      }
+      pixels[(int64_t)y * width + x] = col;
+    }
+  }
+}
+
+/* ---- cross-resolution halo fill (src/halo.cpp:266-479, src/halo.h:270-330) ---- */
+
+/* A constant block's voxel value as stored, read back as a float. */
+static float lg_const(const orc_grid *g, float v) {
+  switch (g->storage) {
+    case ORC_U16: return (float)u16_rha(v) * kU16ToF;
+    case ORC_F16: return orc_f16_to_f32(orc_f32_to_f16(v));
+    default: return v;
+  }
+}
+
+/* Value of voxel (x, y, z) of level l, or 0 in *found when that block does not exist
+ * at level l.  (x, y, z) must lie inside the level's domain. */
+static float lg_value(const orc_grid *g, const orc_level_grid *lg, int l, int x, int y, int z,
+                      int *found) {
+  const int bs = g->bsx >> l;
+  const int64_t bid = (int64_t)(x / bs) + (int64_t)(y / bs) * g->nbx + (int64_t)(z / bs) * g->nbx * g->nby;
+  const int32_t st = lg[l].state[bid];
+  *found = st != ORC_LBLK_NONE;
+  if (st == ORC_LBLK_NONE) return 0.0f;
+  if (st == ORC_LBLK_EMPTY) return lg_const(g, lg[l].emptyValue);
+  if (st == ORC_LBLK_FULL) return lg_const(g, lg[l].fullValue);
+  const int64_t i = (int64_t)st * bs * bs * bs + ((int64_t)(z % bs) * bs + (y % bs)) * bs + (x % bs);
+  switch (g->storage) {
+    case ORC_F32: return ((const float *)lg[l].payload)[i];
+    case ORC_U16: return (float)((const uint16_t *)lg[l].payload)[i] * kU16ToF;
+    case ORC_F16: return orc_f16_to_f32(((const uint16_t *)lg[l].payload)[i]);
+    default: return (float)((const double *)lg[l].payload)[i];
+  }
+}
+
+static inline int clampi(int v, int lo, int hi) { return v < lo ? lo : v > hi ? hi : v; }
+
+int64_t orc_fill_halo(const orc_grid *g, int nLevels, const int32_t *levels,
+                      const orc_level_grid *lg, int level, const int32_t *bids, int64_t nBids,
+                      int haloSize, unsigned opt, float *out) {
+  const int bs = g->bsx >> level, h = haloSize, hs = bs + 2 * h;
+  const int s[3] = {g->sx >> level, g->sy >> level, g->sz >> level};
+  const int64_t per = (int64_t)hs * hs * hs;
+  int64_t skipped = 0;
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : skipped)
+  for (int64_t k = 0; k < nBids; k++) {
+    const int32_t bid = bids[k];
+    float *dst = out + k * per;
+    if (levels[bid] != level || lg[level].state[bid] == ORC_LBLK_NONE) {
+      skipped++;
+      continue;
+    }
+    const int b[3] = {bid % g->nbx, (bid / g->nbx) % g->nby, bid / (g->nbx * g->nby)};
+    const int o[3] = {b[0] * bs, b[1] * bs, b[2] * bs};
+    for (int hz = 0; hz < hs; hz++)
+      for (int hy = 0; hy < hs; hy++)
+        for (int hx = 0; hx < hs; hx++) {
+          int p[3] = {o[0] + hx - h, o[1] + hy - h, o[2] + hz - h};
+          const int inRange = p[0] >= 0 && p[0] < s[0] && p[1] >= 0 && p[1] < s[1] && p[2] >= 0 && p[2] < s[2];
+          int found = 0;
+          float v = 0.0f;
+          if (inRange) v = lg_value(g, lg, level, p[0], p[1], p[2], &found);
+          if (!found) {
+            if (opt & ORC_BC_NEUMANN) {
+              v = lg_value(g, lg, level, clampi(p[0], o[0], o[0] + bs - 1), clampi(p[1], o[1], o[1] + bs - 1),
+                           clampi(p[2], o[2], o[2] + bs - 1), &found);
+            } else if (opt & ORC_BC_COARSE_LEVEL) {
+              if (!inRange) {
+                for (int a = 0; a < 3; a++) p[a] = clampi(p[a], 0, s[a] - 1);
+                v = lg_value(g, lg, level, p[0], p[1], p[2], &found);
+              }
+              if (!found) {
+                v = lg_const(g, lg[level].emptyValue);
+                if (level + 1 < nLevels) {
+                  int c[3];
+                  for (int a = 0; a < 3; a++) c[a] = clampi(p[a] / 2, 0, (s[a] >> 1) - 1);
+                  const float vc = lg_value(g, lg, level + 1, c[0], c[1], c[2], &found);
+                  if (found) v = vc;
+                }
+              }
+            } else {
+              v = lg_const(g, lg[level].emptyValue);
+            }
+          }
+          dst[((int64_t)hz * hs + hy) * hs + hx] = v;
+        }
+  }
+  return skipped;
 }

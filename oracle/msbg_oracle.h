@@ -140,6 +140,61 @@ enum {
 void orc_interpolate(const orc_grid *g, const int32_t *slot, const void *payload, const float *pts,
                      int64_t n, int opt, float *out);
 
+/* ---- cross-resolution halo fill ------------------------------------------------
+ * HaloBlockSet::fillHaloBlock_<T> (src/halo.cpp:266-479) with getOutOfBlockValue
+ * (src/halo.h:270-330) on a multi-level channel.  Level l of the channel is the
+ * reference's SparseGrid of resolution level l: block edge bsx>>l, domain sx>>l, the
+ * same block grid (src/msbg.cpp:800-812).  lg[l].state[bid]: >= 0 index of the block's
+ * payload in lg[l].payload ([n][(bsx>>l)^3] of g->storage); ORC_LBLK_EMPTY the
+ * constant empty block, ORC_LBLK_FULL the constant full block (every voxel reads
+ * emptyValue / fullValue); ORC_LBLK_NONE no block at this level (a NULL block map
+ * entry).  For every listed block (its level levels[bid] must be `level`, and it must
+ * have a block at that level) out receives the (bs+2h)^3 floats [z][y][x] of
+ * positions origin-h .. origin+bs+h-1 in level coordinates:
+ *  - a position inside the domain whose block exists at this level: that value;
+ *  - otherwise, with ORC_BC_NEUMANN: the own block's value at the position clamped to
+ *    the block;
+ *  - otherwise, with ORC_BC_COARSE_LEVEL: a position outside the domain is clamped
+ *    to it and read at this level if that block exists; else the position is halved
+ *    (after the clamp) and read at level+1 (clamped to that level's domain);
+ *  - otherwise the level's empty value.
+ * A level+1 read with no block there, or from the coarsest level, gives the empty
+ * value (the reference requires data there).  uint16 reads as v/65535, FP16 widened.
+ * Returns the number of listed blocks that were skipped (wrong level, no own block). */
+enum { ORC_LBLK_EMPTY = -1, ORC_LBLK_FULL = -2, ORC_LBLK_NONE = -3 };
+enum { ORC_BC_NEUMANN = 1 << 10, ORC_BC_COARSE_LEVEL = 1 << 26 };
+typedef struct {
+  const int32_t *state;   /* [nBlocks] */
+  const void *payload;    /* [n][(bsx>>l)^3] */
+  float emptyValue, fullValue;
+} orc_level_grid;
+int64_t orc_fill_halo(const orc_grid *g, int nLevels, const int32_t *levels,
+                      const orc_level_grid *lg, int level, const int32_t *bids, int64_t nBids,
+                      int haloSize, unsigned opt, float *out);
+
+/* ---- ray-march render of the iso-0.5 surface ----------------------------------
+ * RDR::RaymarchRenderer (src/render.h:52-160, src/render.cpp:20-101): per pixel a
+ * primary ray from the camera (FP64), stepped by 1/res (res = max(sx,sy,sz)) for at
+ * most 2 units; the density at a point p is 0 outside the domain or in a block without
+ * payload, else the trilinear interpolant at res*p (FP32; uint16 times 1/65535).  The
+ * first step whose density crosses 0.5 upwards gives the hit, placed by linear
+ * interpolation; its normal is minus the cubic B-spline gradient
+ * (interpolateWithDerivs0<IP_BSPLINE_CUBIC>, src/sbg.h:3903-4133); Lambert shading
+ * with the sun, colour channels rounded to 8 bits.  pixels[y*width+x] = BMP_MKRGB
+ * (0x02000000 | b<<16 | g<<8 | r), 0x02000000 for a miss.  The gradient is taken
+ * inside the grid's float domain box of SparseGrid::inRange(Vec4f) (src/sbg.cpp:262-316)
+ * only; elsewhere the normal is (0, 1, 0).
+ * opt bits select the floating-point forms the reference's -ffast-math build may
+ * produce (ORC_RENDER_RECIP: v/len as v*(1/len)); 0 is the reference's as written,
+ * with fused multiply-adds where the compiler contracts. */
+typedef struct {
+  double pos[3], lookAt[3], sun[3], color[3];
+  double zoom;
+} orc_camera;
+enum { ORC_RENDER_RECIP = 1 };
+void orc_render(const orc_grid *g, const int32_t *slot, const void *payload, int width, int height,
+                const orc_camera *cam, int opt, int32_t *pixels);
+
 /* ---- conversions (exposed for tests) ---- */
 uint16_t orc_f32_to_f16(float f);
 float orc_f16_to_f32(uint16_t h);

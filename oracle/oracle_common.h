@@ -16,6 +16,14 @@
  * SparseGrid<uint16_t>::interpolateUint16ToFloatFast (src/sbg.h:4920-5032), or, with
  * ORACLE_IP_RENDER_DENS, MultiresSparseGrid::interpolateRenderDensity
  * (src/msbg.h:478-484, a free function: the uint16 value times 1/65535).
+ * A "halo job" builds a multi-level grid on a given (regular) level map, loads every
+ * resolution level of one channel with caller-given block states (payload block,
+ * constant empty, constant full, or no block) and payloads, and dumps
+ * HaloBlockSet::fillHaloBlock_<T> (src/halo.cpp:266-479) of every block at one level.
+ * A "render job" loads a uint16 payload like the interp job and renders it with
+ * RDR::RaymarchRenderer (src/render.h:52-160, src/render.cpp:20-101): the points are
+ * camera position, look-at point, sun position, surface colour and (zoom, 0, 0);
+ * nIter x laplTyp is the image size.
  */
 #ifndef MSBG_ORACLE_COMMON_H
 #define MSBG_ORACLE_COMMON_H
@@ -26,7 +34,8 @@
 #define ORACLE_OUT_MAGIC "MSBGOUT2"
 
 enum { ORACLE_CHAN_F32 = 0, ORACLE_CHAN_U16 = 1 };
-enum { ORACLE_JOB_SURFACE = 1, ORACLE_JOB_LEVELS = 2, ORACLE_JOB_INTERP = 3 };
+enum { ORACLE_JOB_SURFACE = 1, ORACLE_JOB_LEVELS = 2, ORACLE_JOB_INTERP = 3, ORACLE_JOB_HALO = 4,
+       ORACLE_JOB_RENDER = 5 };
 
 /* Interp job option bits: the reference's own interpolation options (src/sbg.h:140-170)
  * plus one bit that the reference's enum leaves unused, for the render-density scale. */
@@ -56,7 +65,12 @@ typedef struct {
   int64_t nPoints;  /* surface / interp job: float32 xyz follow; levels job: 0 */
   int64_t nBlocksIn;/* levels job: int32 levels[nBlocksIn] follow;
                        interp job: int32 activeBids[nBlocksIn] follow, then the
-                       payload [nBlocksIn][bsx^3] of the channel type */
+                       payload [nBlocksIn][bsx^3] of the channel type;
+                       halo job (nBlocksIn = nBlocks; nIter = halo size, laplTyp = the
+                       level whose blocks are filled, constr01 = option bits, dt / rParticle
+                       = empty / full value): int32 levels[nBlocks], int32
+                       state[nLevels][nBlocks] (>= 0 payload index, -1 empty, -2 full,
+                       -3 no block), then per level l the payload [max(state_l)+1][(bsx>>l)^3] */
 } OracleJobHeader;
 
 typedef struct {
@@ -71,7 +85,10 @@ typedef struct {
   /* then: int8 levels[nBlocks]; uint16 flags[nBlocks];
    *       int32 activeBids[nActive];
    *       payloadAfterFinalize[nActive*bsx^3]; payloadAfterPde[nActive*bsx^3]
-   * interp job: tPdeSec = interpolation time; then float32 values[nPoints] */
+   * interp job: tPdeSec = interpolation time; then float32 values[nPoints]
+   * halo job: nActive = filled blocks, tPdeSec = fill time; then int32 bids[nActive],
+   *           float32 halo[nActive][(bs_l+2h)^3]
+   * render job: tPdeSec = render time; then int32 pixels[height][width] (BMP_MKRGB) */
 } OracleOutHeader;
 
 #endif

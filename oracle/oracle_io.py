@@ -26,7 +26,7 @@ REF_DRIVER = os.path.join(HERE, "_ref", "msbg_ref_driver")
 JOB_MAGIC = b"MSBGJOB2"
 OUT_MAGIC = b"MSBGOUT2"
 CHAN_F32, CHAN_U16 = 0, 1
-JOB_SURFACE, JOB_LEVELS, JOB_INTERP = 1, 2, 3
+JOB_SURFACE, JOB_LEVELS, JOB_INTERP, JOB_HALO, JOB_RENDER = 1, 2, 3, 4, 5
 
 # interpolation options: the reference's bits (src/sbg.h:140-170) and the render-density
 # scale of the uint16 channel (a bit the reference's enum leaves unused)
@@ -142,6 +142,101 @@ def run_reference_interp(sx, sy, sz, bsx, chan, active_bids, payload, points, op
     n = np.asarray(points).reshape(-1, 3).shape[0]
     vals = np.frombuffer(buf, np.float32, n, hsz).copy()
     return vals, float(h[17]), int(h[19])
+
+
+# halo fill options (src/msbg.h:101-131) and level-grid block states
+BC_NEUMANN = 1 << 10
+BC_COARSE_LEVEL = 1 << 26
+LBLK_EMPTY, LBLK_FULL, LBLK_NONE = -1, -2, -3
+
+
+def write_halo_job(path: str, sx: int, sy: int, sz: int, bsx: int, n_levels: int, chan: int,
+                   levels: np.ndarray, states: list, payloads: list, level: int, halo: int,
+                   opt: int, empty_value: float = 0.0, full_value: float = 1.0) -> None:
+    lv = np.ascontiguousarray(levels, dtype=np.int32).ravel()
+    dt = np.float32 if chan == CHAN_F32 else np.uint16
+    hdr = struct.pack(_JOB_FMT, JOB_MAGIC, JOB_HALO, sx, sy, sz, bsx, n_levels, chan, halo, level, opt,
+                      1, empty_value, full_value, 0.0, 0.0, 0, 0, lv.size)
+    with open(path, "wb") as f:
+        f.write(hdr)
+        f.write(lv.tobytes())
+        for l in range(n_levels):
+            f.write(np.ascontiguousarray(states[l], dtype=np.int32).tobytes())
+        for l in range(n_levels):
+            n = int(np.max(states[l])) + 1 if len(states[l]) else 0
+            bs = bsx >> l
+            pay = np.ascontiguousarray(payloads[l], dtype=dt).reshape(-1)
+            if pay.size < n * bs ** 3:
+                raise ValueError(f"level {l}: payload smaller than its states need")
+            f.write(pay[: n * bs ** 3].tobytes())
+
+
+def run_reference_halo(sx, sy, sz, bsx, n_levels, chan, levels, states, payloads, level, halo, opt,
+                       empty_value=0.0, full_value=1.0, timeout: float = 600):
+    """HaloBlockSet::fillHaloBlock_ of every block at `level` by the reference itself.
+
+    Returns (bids int32 [m], halo float32 [m][(bs+2h)^3])."""
+    with tempfile.TemporaryDirectory() as td:
+        jp, op = os.path.join(td, "job.bin"), os.path.join(td, "out.bin")
+        write_halo_job(jp, sx, sy, sz, bsx, n_levels, chan, levels, states, payloads, level, halo, opt,
+                       empty_value, full_value)
+        r = subprocess.run([REF_DRIVER, jp, op], cwd=td, timeout=timeout,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference halo job failed with status {r.returncode}")
+        with open(op, "rb") as f:
+            buf = f.read()
+    hsz = struct.calcsize(_OUT_FMT)
+    h = struct.unpack(_OUT_FMT, buf[:hsz])
+    if h[0] != OUT_MAGIC:
+        raise ValueError("bad oracle output")
+    m = int(h[2])
+    hs = (bsx >> level) + 2 * halo
+    bids = np.frombuffer(buf, np.int32, m, hsz).copy()
+    vals = np.frombuffer(buf, np.float32, m * hs ** 3, hsz + 4 * m).copy().reshape(m, hs ** 3)
+    return bids, vals
+
+
+# the demo's camera (src/msbg_demo.cpp:123-127) and surface colour (src/msbg_demo.cpp:150)
+DEMO_CAMERA = {"pos": (0.5, 0.8, 0.7), "look_at": (0.5, 0.5, 0.5), "sun": (0.5, 5.0, 5.0),
+               "color": (0.8, 0.6, 0.4), "zoom": 1.0}
+
+
+def camera_array(cam: dict) -> np.ndarray:
+    """The 5 float32 triples of a render job: position, look-at, sun, colour, (zoom, 0, 0)."""
+    return np.array([*cam["pos"], *cam["look_at"], *cam["sun"], *cam["color"], cam["zoom"], 0.0, 0.0],
+                    np.float32)
+
+
+def run_reference_render(sx, sy, sz, bsx, active_bids, payload_u16, width, height, cam=None,
+                         n_threads: int = 0, timeout: float = 1200):
+    """RDR::RaymarchRenderer::render (src/render.cpp:20-101) of a uint16 payload.
+
+    Returns (pixels int32 [height][width] as BMP_MKRGB, seconds, threads)."""
+    cam = DEMO_CAMERA if cam is None else cam
+    bids = np.ascontiguousarray(active_bids, dtype=np.int32).ravel()
+    pay = np.ascontiguousarray(payload_u16, dtype=np.uint16)
+    with tempfile.TemporaryDirectory() as td:
+        jp, op = os.path.join(td, "job.bin"), os.path.join(td, "out.bin")
+        hdr = struct.pack(_JOB_FMT, JOB_MAGIC, JOB_RENDER, sx, sy, sz, bsx, 3, CHAN_U16, width, height, 0,
+                          n_threads, 0.0, 0.0, 0.0, 0.0, 0, 5, bids.size)
+        with open(jp, "wb") as f:
+            f.write(hdr)
+            f.write(camera_array(cam).tobytes())
+            f.write(bids.tobytes())
+            f.write(pay.tobytes())
+        r = subprocess.run([REF_DRIVER, jp, op], cwd=td, timeout=timeout,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference render job failed with status {r.returncode}")
+        with open(op, "rb") as f:
+            buf = f.read()
+    hsz = struct.calcsize(_OUT_FMT)
+    h = struct.unpack(_OUT_FMT, buf[:hsz])
+    if h[0] != OUT_MAGIC:
+        raise ValueError("bad oracle output")
+    px = np.frombuffer(buf, np.int32, width * height, hsz).copy().reshape(height, width)
+    return px, float(h[17]), int(h[19])
 
 
 def read_result(path: str, bsx: int, surface: bool = True) -> OracleResult:

@@ -71,6 +71,10 @@ def lib():
         L.orc_poisson_coeffs_dense.argtypes = [C.c_uint32, C.c_int, C.c_int, C.c_int, P, P, P, P, P]
         L.orc_downsample.argtypes = [C.POINTER(Grid), P, P, C.c_int32, P, C.c_int, P]
         L.orc_interpolate.argtypes = [C.POINTER(Grid), P, P, P, C.c_int64, C.c_int, P]
+        L.orc_fill_halo.argtypes = [C.POINTER(Grid), C.c_int, P, C.c_void_p, C.c_int, P, C.c_int64,
+                                    C.c_int, C.c_uint, P]
+        L.orc_fill_halo.restype = C.c_int64
+        L.orc_render.argtypes = [C.POINTER(Grid), P, P, C.c_int, C.c_int, C.c_void_p, C.c_int, P]
         L.orc_f32_to_f16.argtypes = [C.c_float]
         L.orc_f32_to_f16.restype = C.c_uint16
         L.orc_f16_to_f32.argtypes = [C.c_uint16]
@@ -163,6 +167,69 @@ def interpolate(g: Grid, slot, payload: np.ndarray, pts: np.ndarray, opt: int = 
     pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 3)
     out = np.zeros(pts.shape[0], np.float32)
     lib().orc_interpolate(C.byref(g), _p(slot), _p(payload), _p(pts), pts.shape[0], int(opt), _p(out))
+    return out
+
+
+BC_NEUMANN, BC_COARSE_LEVEL = 1 << 10, 1 << 26
+LBLK_EMPTY, LBLK_FULL, LBLK_NONE = -1, -2, -3
+
+
+class LevelGrid(C.Structure):
+    _fields_ = [("state", C.c_void_p), ("payload", C.c_void_p), ("emptyValue", C.c_float),
+                ("fullValue", C.c_float)]
+
+
+def fill_halo(g: Grid, levels, states: list, payloads: list, level: int, bids, halo: int, opt: int,
+              empty_value: float = 0.0, full_value: float = 1.0) -> tuple[np.ndarray, int]:
+    """fillHaloBlock_ restated (src/halo.cpp:266-479, src/halo.h:270-330) on a multi-level
+    channel: float32 [len(bids)][(bs+2h)^3] and the number of skipped blocks."""
+    n_levels = len(states)
+    levels = np.ascontiguousarray(levels, np.int32)
+    keep = []
+    lgs = (LevelGrid * n_levels)()
+    for l in range(n_levels):
+        st = np.ascontiguousarray(states[l], np.int32)
+        pay = np.ascontiguousarray(payloads[l]) if payloads[l] is not None else np.zeros(1, np.float32)
+        keep += [st, pay]
+        lgs[l] = LevelGrid(st.ctypes.data, pay.ctypes.data, empty_value, full_value)
+    bids = np.ascontiguousarray(bids, np.int32)
+    hs = (g.bsx >> level) + 2 * halo
+    out = np.zeros((len(bids), hs ** 3), np.float32)
+    skipped = lib().orc_fill_halo(C.byref(g), n_levels, _p(levels), C.cast(lgs, C.c_void_p), level,
+                                  _p(bids), len(bids),
+                                  halo, opt, _p(out))
+    return out, int(skipped)
+
+
+class Camera(C.Structure):
+    _fields_ = [("pos", C.c_double * 3), ("lookAt", C.c_double * 3), ("sun", C.c_double * 3),
+                ("color", C.c_double * 3), ("zoom", C.c_double)]
+
+
+# the demo's camera (src/msbg_demo.cpp:123-127) and surface colour (src/msbg_demo.cpp:150),
+# float literals as the demo passes them
+DEMO_CAMERA = {"pos": (0.5, 0.8, 0.7), "look_at": (0.5, 0.5, 0.5), "sun": (0.5, 5.0, 5.0),
+               "color": (0.8, 0.6, 0.4), "zoom": 1.0}
+
+
+def camera(cam: dict | None = None) -> Camera:
+    cam = DEMO_CAMERA if cam is None else cam
+    f = lambda v: [float(np.float32(x)) for x in v]  # noqa: E731
+    return Camera((C.c_double * 3)(*f(cam["pos"])), (C.c_double * 3)(*f(cam["look_at"])),
+                  (C.c_double * 3)(*f(cam["sun"])), (C.c_double * 3)(*f(cam["color"])),
+                  float(np.float32(cam["zoom"])))
+
+
+def render(g: Grid, slot, payload: np.ndarray, width: int, height: int, cam: dict | None = None,
+           opt: int = 0) -> np.ndarray:
+    """RaymarchRenderer::render restated (src/render.cpp:20-101): int32 [height][width]
+    pixels as BMP_MKRGB (0x02000000 | b<<16 | g<<8 | r)."""
+    slot = np.ascontiguousarray(slot, np.int32)
+    payload = np.ascontiguousarray(payload)
+    out = np.zeros((height, width), np.int32)
+    c = camera(cam)
+    lib().orc_render(C.byref(g), _p(slot), _p(payload), width, height, C.cast(C.byref(c), C.c_void_p), opt,
+                     _p(out))
     return out
 
 

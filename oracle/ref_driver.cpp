@@ -10,8 +10,9 @@
  * arithmetic and their control flow (including the "abort this particle on a
  * non-value block" rule at src/msbg_demo.cpp:613-618).  Everything else is the
  * library itself: MultiresSparseGrid::create, regularizeRefinementMap,
- * setRefinementMap, SparseGrid block management, applyChannelPdeFast<T> and the
- * trilinear interpolation functions (interp job).
+ * setRefinementMap, SparseGrid block management, applyChannelPdeFast<T>, the
+ * trilinear interpolation functions (interp job), HaloBlockSet::fillHaloBlock_<T>
+ * (halo job) and the ray-march renderer RDR::RaymarchRenderer (render job).
  *
  * Differences from the demo, both forced by the workload definition:
  *  - points come from the job file (already in voxel coordinates) instead of
@@ -24,11 +25,14 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <vector>
 
 #include "msbg.h"
+#include "halo.h"
+#include "render.h"
 #include "oracle_common.h"
 
 extern int nMaxThreads;
@@ -367,6 +371,124 @@ int runInterpJob(const OracleJobHeader &job, const float *pts, const int32_t *bi
   return 0;
 }
 
+// Cross-resolution halo fill by the reference's own HaloBlockSet::fillHaloBlock_<T>
+// (src/halo.cpp:266-479).  A multi-level grid on the job's level map; every resolution
+// level l of the channel gets the job's block states (payload / constant empty /
+// constant full / no block) and payloads; then every block at level job.laplTyp that
+// has a block at that level is filled with halo size job.nIter and options job.constr01.
+template <typename T>
+int runHaloJob(const OracleJobHeader &job, const int32_t *levelsIn, const int32_t *state,
+               const std::vector<std::vector<uint8_t>> &pay, FILE *fout) {
+  OracleOutHeader out;
+  memset(&out, 0, sizeof(out));
+  memcpy(out.magic, ORACLE_OUT_MAGIC, 8);
+  const int chan = (sizeof(T) == 4) ? MSBG::CH_FLOAT_1 : MSBG::CH_UINT16_1;
+  MultiresSparseGrid *msbg = MultiresSparseGrid::create(
+      "TEST", job.sx, job.sy, job.sz, job.bsx, -1, 0, -1, 0, NULL, NULL, job.nLevels);
+  if (!msbg) return 2;
+  const int nBlocks = msbg->nBlocks();
+  if ((int64_t)nBlocks != job.nBlocksIn) return 4;
+  std::vector<int> levels(levelsIn, levelsIn + nBlocks);
+  msbg->regularizeRefinementMap(levels.data());
+  for (int b = 0; b < nBlocks; b++)
+    if (levels[b] != levelsIn[b]) return 5;  // the job's map must already be regular
+  msbg->setRefinementMap(levels.data(), NULL, 0, NULL, false, false);
+  for (int l = 0; l < job.nLevels; l++) {
+    SparseGrid<T> *sg = MSBG::getChannel<T>(msbg, chan, l);
+    if (!sg) return 3;
+    sg->reset();
+    sg->prepareDataAccess();
+    sg->setEmptyValue(Quant<T>::fromFloat(job.dt));
+    sg->setFullValue(Quant<T>::fromFloat(job.rParticle));
+    const size_t nv = (size_t)sg->nVoxelsInBlock();
+    const int32_t *st = state + (size_t)l * nBlocks;
+    const T *src = reinterpret_cast<const T *>(pay[l].data());
+    for (int b = 0; b < nBlocks; b++) {
+      if (st[b] >= 0) {
+        T *data = sg->getBlockDataPtr(b, 1, 0);
+        memcpy(data, src + (size_t)st[b] * nv, nv * sizeof(T));
+      } else if (st[b] == -1) {
+        sg->setEmptyBlock(b);
+      } else if (st[b] == -2) {
+        sg->setFullBlock(b);
+      }
+    }
+  }
+  const int L = job.laplTyp, h = job.nIter;
+  const int bs = job.bsx >> L, hs = bs + 2 * h;
+  std::vector<int32_t> bids;
+  for (int b = 0; b < nBlocks; b++)
+    if (levels[b] == L && state[(size_t)L * nBlocks + b] != -3) bids.push_back(b);
+  std::vector<float> halo(bids.size() * (size_t)hs * hs * hs);
+  MSBG::HaloBlockSet hb(msbg, h, 1);
+  const double t0 = nowSec();
+  for (size_t k = 0; k < bids.size(); k++) {
+    float **p = hb.fillHaloBlock_<T>(chan, bids[k], 0, 0, (unsigned)job.constr01);
+    memcpy(halo.data() + k * (size_t)hs * hs * hs, p[0], sizeof(float) * hs * hs * hs);
+  }
+  out.tPdeSec = nowSec() - t0;
+  out.nBlocks = nBlocks;
+  out.nActive = (int)bids.size();
+  out.elemBytes = (int)sizeof(T);
+  out.nThreadsUsed = 1;
+  fwrite(&out, sizeof(out), 1, fout);
+  fwrite(bids.data(), 4, bids.size(), fout);
+  fwrite(halo.data(), 4, halo.size(), fout);
+  MultiresSparseGrid::destroy(msbg);
+  return 0;
+}
+
+// The demo's ray-march renderer (src/render.h:52-160, src/render.cpp:20-101) on a uint16
+// payload loaded into the value blocks of a single-level grid, as the interp job does.
+int runRenderJob(const OracleJobHeader &job, const float *cam, const int32_t *bids,
+                 const uint16_t *payload, FILE *fout) {
+  OracleOutHeader out;
+  memset(&out, 0, sizeof(out));
+  memcpy(out.magic, ORACLE_OUT_MAGIC, 8);
+  MultiresSparseGrid *msbg = MultiresSparseGrid::create(
+      "TEST", job.sx, job.sy, job.sz, job.bsx, -1, 0, -1,
+      MSBG::OPT_SINGLE_LEVEL | MSBG::OPT_SINGLE_CHANNEL_FLOAT);
+  if (!msbg) return 2;
+  SparseGrid<uint16_t> *sg0 = MSBG::getChannel<uint16_t>(msbg, MSBG::CH_UINT16_1, 0);
+  if (!sg0) return 3;
+  const int nBlocks = msbg->nBlocks();
+  std::vector<int> levels(nBlocks, msbg->getNumLevels() - 1);
+  for (int64_t t = 0; t < job.nBlocksIn; t++) {
+    if (bids[t] < 0 || bids[t] >= nBlocks) return 4;
+    levels[bids[t]] = 0;
+  }
+  msbg->regularizeRefinementMap(levels.data());
+  msbg->setRefinementMap(levels.data(), NULL, -1, NULL, false);
+  sg0->reset();
+  sg0->prepareDataAccess();
+  sg0->setEmptyValue(0);
+  sg0->setFullValue(65535);
+  for (int bid = 0; bid < nBlocks; bid++) sg0->setEmptyBlock(bid);
+  const size_t nv = (size_t)sg0->nVoxelsInBlock();
+  for (int64_t t = 0; t < job.nBlocksIn; t++) {
+    uint16_t *data = sg0->getBlockDataPtr(bids[t], 1, 0);
+    memcpy(data, payload + (size_t)t * nv, nv * sizeof(uint16_t));
+  }
+  const int w = job.nIter, h = job.laplTyp;
+  RDR::RaymarchRenderer renderer(w, h, sg0);
+  // the demo passes float camera values (src/msbg_demo.cpp:123-127, 143-147)
+  renderer.setCamera({cam[0], cam[1], cam[2]}, {cam[3], cam[4], cam[5]}, cam[12]);
+  renderer.setSunLight({cam[6], cam[7], cam[8]});
+  renderer.setSurfaceColor({cam[9], cam[10], cam[11]});
+  const double t0 = nowSec();
+  BmpBitmap *B = renderer.render();
+  out.tPdeSec = nowSec() - t0;
+  if (!B) return 6;
+  out.nBlocks = nBlocks;
+  out.nActive = w * h;
+  out.elemBytes = 2;
+  out.nThreadsUsed = omp_get_max_threads();
+  fwrite(&out, sizeof(out), 1, fout);
+  fwrite(B->data, 4, (size_t)w * h, fout);
+  MultiresSparseGrid::destroy(msbg);
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -386,7 +508,23 @@ int main(int argc, char **argv) {
   if (job.nPoints && fread(pts.data(), 4, pts.size(), fin) != pts.size()) return 1;
   if (job.nBlocksIn && fread(lv.data(), 4, lv.size(), fin) != lv.size()) return 1;
   std::vector<uint8_t> payload;
-  if (job.jobType == ORACLE_JOB_INTERP) {
+  std::vector<int32_t> state;
+  std::vector<std::vector<uint8_t>> levelPay;
+  if (job.jobType == ORACLE_JOB_HALO) {
+    const size_t elem = job.chanType == ORACLE_CHAN_U16 ? 2 : 4;
+    state.resize((size_t)job.nLevels * job.nBlocksIn);
+    if (fread(state.data(), 4, state.size(), fin) != state.size()) return 1;
+    levelPay.resize(job.nLevels);
+    for (int l = 0; l < job.nLevels; l++) {
+      int32_t mx = -1;
+      for (int64_t b = 0; b < job.nBlocksIn; b++) mx = std::max(mx, state[(size_t)l * job.nBlocksIn + b]);
+      const size_t bs = (size_t)(job.bsx >> l);
+      levelPay[l].resize((size_t)(mx + 1) * bs * bs * bs * elem);
+      if (!levelPay[l].empty() && fread(levelPay[l].data(), 1, levelPay[l].size(), fin) != levelPay[l].size())
+        return 1;
+    }
+  }
+  if (job.jobType == ORACLE_JOB_INTERP || job.jobType == ORACLE_JOB_RENDER) {
     const size_t elem = job.chanType == ORACLE_CHAN_U16 ? 2 : 4;
     payload.resize((size_t)job.nBlocksIn * job.bsx * job.bsx * job.bsx * elem);
     if (!payload.empty() && fread(payload.data(), 1, payload.size(), fin) != payload.size())
@@ -405,6 +543,14 @@ int main(int argc, char **argv) {
   int rc;
   if (job.jobType == ORACLE_JOB_LEVELS)
     rc = runLevelsJob(job, lv.data(), fout);
+  else if (job.jobType == ORACLE_JOB_RENDER)
+    rc = job.chanType == ORACLE_CHAN_U16 && job.nPoints == 5
+             ? runRenderJob(job, pts.data(), lv.data(), reinterpret_cast<const uint16_t *>(payload.data()), fout)
+             : 7;
+  else if (job.jobType == ORACLE_JOB_HALO && job.chanType == ORACLE_CHAN_U16)
+    rc = runHaloJob<uint16_t>(job, lv.data(), state.data(), levelPay, fout);
+  else if (job.jobType == ORACLE_JOB_HALO)
+    rc = runHaloJob<float>(job, lv.data(), state.data(), levelPay, fout);
   else if (job.jobType == ORACLE_JOB_INTERP && job.chanType == ORACLE_CHAN_U16)
     rc = runInterpJob<uint16_t>(job, pts.data(), lv.data(),
                                 reinterpret_cast<const uint16_t *>(payload.data()), fout);

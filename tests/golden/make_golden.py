@@ -9,8 +9,8 @@ never on the GPU host; the .npz files it writes are committed.
 
     python tests/golden/make_golden.py
 
-It writes reference_small.npz (splat, levels, sweeps) and reference_interp.npz
-(trilinear interpolation).
+It writes reference_small.npz (splat, levels, sweeps), reference_interp.npz
+(trilinear interpolation) and reference_halo.npz (cross-resolution halo fill).
 """
 from __future__ import annotations
 
@@ -23,6 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 import oracle_io as O  # noqa: E402
 
@@ -105,6 +106,7 @@ def main() -> None:
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
     make_interp(out)
+    make_halo()
 
 
 IP_OPTS = (0, O.IP_CORNER, O.IP_BC_DIRICHLET, O.IP_BC_DIRICHLET_OLD, O.IP_CORNER | O.IP_BC_DIRICHLET,
@@ -149,6 +151,38 @@ def make_interp(small: dict) -> None:
             v, _, _ = O.run_reference_interp(res, res, res, bs, chan, rbids, pay, pts, opt)
             out[f"rand_{name}_{opt}"] = v
     path = os.path.join(HERE, "reference_interp.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
+
+
+HALO_NB, HALO_BSX, HALO_LEVELS = (5, 4, 6), 8, 3
+HALO_OPTS = (0, O.BC_NEUMANN, O.BC_COARSE_LEVEL)
+
+
+def make_halo() -> None:
+    """HaloBlockSet::fillHaloBlock_ of every block of each level of a 3-level channel
+    (oracle/ref_driver.cpp, halo job): FP32 and uint16, options none / OPT_BC_NEUMANN /
+    OPT_BC_COARSE_LEVEL, halo sizes 1 and 2."""
+    import halo_cases as H
+    import port as P
+    out = {"nb": np.array(HALO_NB, np.int32), "bsx": np.int32(HALO_BSX), "n_levels": np.int32(HALO_LEVELS),
+           "empty_value": np.float32(0.25), "full_value": np.float32(0.75)}
+    res = [x * HALO_BSX for x in HALO_NB]
+    for kind, chan in (("f32", O.CHAN_F32), ("u16", O.CHAN_U16)):
+        lv, st, pay = H.halo_case(HALO_NB, HALO_BSX, HALO_LEVELS, 20261203 + 930 + chan, kind,
+                                  lambda *a: P.regularize(*a)[0])
+        out[f"{kind}_levels"] = lv
+        for l in range(HALO_LEVELS):
+            out[f"{kind}_state{l}"] = st[l]
+            out[f"{kind}_pay{l}"] = pay[l]
+        for L in range(HALO_LEVELS):
+            for opt in HALO_OPTS:
+                for h in (1, 2):
+                    bids, vals = O.run_reference_halo(*res, HALO_BSX, HALO_LEVELS, chan, lv, st, pay, L, h, opt,
+                                                      0.25, 0.75)
+                    assert np.array_equal(bids, H.blocks_at(lv, st, L))
+                    out[f"{kind}_L{L}_o{opt}_h{h}"] = vals
+    path = os.path.join(HERE, "reference_halo.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
 

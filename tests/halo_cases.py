@@ -1,0 +1,61 @@
+"""Seeded multi-level channel layouts for the cross-resolution halo fill tests.
+
+A case is a regular level map (levels grow with the distance from one corner of the block
+grid, with seeded jitter, then regularizeRefinementMap) and, for every resolution level
+l, per-block states and a payload of (bsx>>l)^3 values per payload block:
+  - blocks at level l: a payload block, now and then the constant empty or full block;
+  - other blocks: a payload block (ghost data), the constant empty block or no block;
+  - the coarsest level has a block everywhere, and a block without a block at level l
+    has one at level l+1, so every coarse-level read of the halo fill finds data, as the
+    reference requires (src/halo.h:310-322).
+Payload values: uint16 uniform; FP32 the uint16 values / 65536; FP16 the FP32 values
+rounded to half.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+LBLK_EMPTY, LBLK_FULL, LBLK_NONE = -1, -2, -3
+
+
+def halo_case(nb, bsx: int, n_levels: int, seed: int, kind: str, regularize):
+    """kind: 'f32' | 'u16' | 'f16'; regularize(levels, nbx, nby, nbz, n_levels) -> levels."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = int(np.prod(nb))
+    bz, by, bx = np.meshgrid(np.arange(nb[2]), np.arange(nb[1]), np.arange(nb[0]), indexing="ij")
+    d = (bx + by + bz).ravel() + rng.integers(-1, 2, n)
+    lv = np.clip(d // 3, 0, n_levels - 1).astype(np.int32)
+    lv = np.asarray(regularize(lv, nb[0], nb[1], nb[2], n_levels), np.int32)
+    states, pays = [], []
+    for l in range(n_levels):
+        st = np.full(n, LBLK_NONE, np.int32)
+        r = rng.random(n)
+        own = lv == l
+        st[~own & (r < 0.3)] = 0
+        st[~own & (r >= 0.3) & (r < 0.4)] = LBLK_EMPTY
+        st[own] = 0
+        st[own & (r < 0.05)] = LBLK_EMPTY
+        st[own & (r >= 0.05) & (r < 0.08)] = LBLK_FULL
+        if l == n_levels - 1:
+            st[st == LBLK_NONE] = 0
+        states.append(st)
+    for l in range(n_levels - 2, -1, -1):
+        miss = (states[l] == LBLK_NONE) & (states[l + 1] == LBLK_NONE)
+        states[l + 1][miss] = LBLK_EMPTY
+    for l in range(n_levels):
+        st = states[l]
+        k = st == 0
+        st[k] = np.arange(int(k.sum()), dtype=np.int32)
+        bs = bsx >> l
+        u16 = rng.integers(0, 65536, (int(k.sum()), bs ** 3)).astype(np.uint16)
+        if kind == "u16":
+            pays.append(u16)
+        else:
+            f32 = (u16.astype(np.float32) * np.float32(1.0 / 65536.0)).astype(np.float32)
+            pays.append(f32 if kind == "f32" else f32.astype(np.float16))
+    return lv, states, pays
+
+
+def blocks_at(lv, states, level):
+    """Blocks whose level is `level` and that have a block at that level, ascending."""
+    return np.nonzero((np.asarray(lv) == level) & (states[level] != LBLK_NONE))[0].astype(np.int32)
