@@ -392,6 +392,11 @@ def run_gpu(args, spec, dist: Dist):
     if not args.no_jacobi:
         halo = halo_measure(g, info, storage, elem, bsx, args.steps, dist, peaks)
 
+    # ray-march render of the iso-0.5 surface (RaymarchRenderer::render) of the swept field
+    render = None
+    if not args.no_jacobi:
+        render = render_measure(g, args.steps, dist, cpu=dist.rank == 0 and not args.no_cpu_baseline)
+
     # e2e through the host-buffer entry point
     e2e = None
     if not args.no_e2e:
@@ -429,6 +434,11 @@ def run_gpu(args, spec, dist: Dist):
         cpu = {"value": v, "unit": "voxel-updates/s", "cores": threads, "kind": "port",
                "sample": desc}
 
+    # the workload's field error against an FP64 GPU run of the same algorithm
+    field_error = None
+    if args.fp64_check:
+        field_error = fp64_field_error(g, d, n, spec, bands, variant)
+
     d.free()
     g.close()
     poisson = None
@@ -455,7 +465,9 @@ def run_gpu(args, spec, dist: Dist):
         "jacobi_sweeps": jacobi,
         "restriction": restriction,
         "g2p": g2p,
+        "field_error_vs_fp64": field_error,
         "halo_fill": halo,
+        "render": render,
         "poisson": poisson,
     }
     print(json.dumps(line), flush=True)
@@ -507,6 +519,104 @@ def halo_measure(g, info, storage, elem, bsx, steps, dist, peaks, batch=16384) -
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": gbs / peaks["hbm_gbs"],
                          "algorithmic_bytes_per_block": hs ** 3 * (elem + 4)}}
+
+
+def fp64_field_error(g, d_pts, n, spec, bands, variant, chunk=4096) -> dict:
+    """The workload's pipeline (splat, finalize, spec['n_iter'] MCF sweeps) once more on g in
+    its storage, and on a second grid with FP64 storage and FP64 arithmetic (the sweep's
+    exact form, reference operation order): relative L2 and max error of the first against
+    the second over every level-0 voxel, compared chunk by chunk on the host."""
+    res, bsx, n_iter = spec["res"], spec["bsx"], spec["n_iter"]
+    t0 = time.perf_counter()
+    g.setRefinementMap(1.0)
+    g.splat(d_pts, n, 2.0, 2.0)
+    g.splat_finalize(2.0, 2.0)
+    g.applyChannelPdeFast(0, MCF8, 1, n_iter, spec["dt"], 0.0, variant)
+    g.synchronize()
+    g64 = G.MultiresSparseGrid(res, res, res, bsx, spec["n_levels"], G.F64)
+    try:
+        if bands:
+            g64.levels_from_bands(d_pts, n, bands)
+        else:
+            g64.mark_points(d_pts, n, 4.0)
+            g64.levels_from_marks()
+        g64.regularizeRefinementMap()
+        g64.setRefinementMap(1.0)
+        g64.splat(d_pts, n, 2.0, 2.0)
+        g64.splat_finalize(2.0, 2.0)
+        t1 = time.perf_counter()
+        g64.applyChannelPdeFast(0, MCF8, 1, n_iter, spec["dt"], 0.0, G.SWEEP_EXACT)
+        g64.synchronize()
+        t64 = time.perf_counter() - t1
+        same_layout = bool(np.array_equal(g.active_blocks(), g64.active_blocks()))
+        n_act = g.info().nActive
+        vpb = bsx ** 3
+        dt_lo = G.NP_STORAGE[g.storage[0]]
+        p_lo, p_hi = g.payload_ptr(0), g64.payload_ptr(0)
+        esz = np.dtype(dt_lo).itemsize
+        se = sr = 0.0
+        mx = 0.0
+        for k0 in range(0, n_act, chunk):
+            m = min(chunk, n_act - k0)
+            lo = np.empty(m * vpb, dt_lo)
+            hi = np.empty(m * vpb, np.float64)
+            g._check(g.L.msbg_gpu_copy_d2h(g.h, G._ptr(lo), C.c_void_p(p_lo + k0 * vpb * esz), lo.nbytes))
+            g64._check(g64.L.msbg_gpu_copy_d2h(g64.h, G._ptr(hi), C.c_void_p(p_hi + k0 * vpb * 8), hi.nbytes))
+            g.synchronize()
+            g64.synchronize()
+            e = lo.astype(np.float64) - hi
+            se += float(np.dot(e, e))
+            sr += float(np.dot(hi, hi))
+            mx = max(mx, float(np.abs(e).max()))
+        return {"reference": "same pipeline on the GPU with FP64 storage and FP64 arithmetic (exact form)",
+                "tested": f"{spec['storage']} storage, FP32 arithmetic, {'fast' if variant == G.SWEEP_FAST else 'exact'} form",
+                "same_active_blocks": same_layout, "voxels": int(n_act * vpb),
+                "rel_l2": (se / sr) ** 0.5 if sr > 0 else None, "max_abs": mx,
+                "fp64_sweep_seconds": t64, "seconds": time.perf_counter() - t0}
+    finally:
+        g64.close()
+
+
+def render_measure(g, steps, dist, cpu: bool, width=1920, height=1080) -> dict:
+    """RaymarchRenderer::render of channel 0 from the demo's camera at width x height;
+    with cpu, the CPU restatement renders 1/64 of the pixels (the same view at width/8 x
+    height/8) on all host cores."""
+    d_rgb = G.DeviceBuffer.alloc(width * height * 3)
+    g.render_device(0, width, height, G.DEMO_CAMERA, d_rgb)
+    g.synchronize()
+    l0 = g.launch_count()
+    g.event_record(10)
+    n = max(1, min(steps, 3))
+    for _ in range(n):
+        g.render_device(0, width, height, G.DEMO_CAMERA, d_rgb)
+    g.event_record(11)
+    g.synchronize()
+    ms = dist.max(g.event_elapsed_ms(10, 11)) / n
+    img = np.empty((height, width, 3), np.uint8)
+    g._check(g.L.msbg_gpu_copy_d2h(g.h, G._ptr(img), C.c_void_p(d_rgb.ptr), img.nbytes))
+    g.synchronize()
+    d_rgb.free()
+    out = {"kernel": "kRender (FP64 ray march, cubic B-spline normal)", "width": width, "height": height,
+           "camera": "demo (src/msbg_demo.cpp:123-127)", "ms_per_frame": ms,
+           "pixels_per_s": width * height * dist.world / (ms / 1e3), "hit_pixels": int(img.any(-1).sum()),
+           "launches_per_frame": (g.launch_count() - l0) // n,
+           "bound": "FP64 pipe (3 adds + 3 conversions per ray step) and gathers near the surface"}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import port as P  # the oracle, as the CPU baseline
+        info = g.info()
+        og = P.grid(g.sx, g.sy, g.sz, g.bsx, {G.F32: P.F32, G.F16: P.F16, G.U16: P.U16}[g.storage[0]])
+        pay = g.payload(0)
+        host = pay.view(np.uint16) if pay.dtype == np.float16 else pay
+        w8, h8 = width // 8, height // 8
+        t0 = time.perf_counter()
+        P.render(og, g.slots(), host, w8, h8, G.DEMO_CAMERA)
+        sec = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": w8 * h8 / sec, "unit": "pixels/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": f"{w8}x{h8} pixels of the same view, all host threads",
+                               "value_blocks": int(info.nActive)}
+        del pay, host
+    return out
 
 
 WARMNET = os.path.join(ROOT, "msbg_gb300", "data", "warmnet_c3.npz")
@@ -592,6 +702,8 @@ def main():
                     help="skip the sparse Poisson time-to-1e-6 measurement of the default run")
     ap.add_argument("--variant", default="fast", choices=["fast", "exact"])
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--fp64-check", action=argparse.BooleanOptionalAction, default=True,
+                    help="field error of the workload against an FP64 GPU run of the same algorithm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--traffic-per-launch", type=float, default=None,

@@ -267,9 +267,9 @@ enum { MSBG_GPU_LBLK_EMPTY = -1, MSBG_GPU_LBLK_FULL = -2, MSBG_GPU_LBLK_NONE = -
 int msbg_gpu_level_grid_set(msbg_gpu_ctx *ctx, int lchan, int level, int storage, const int32_t *hState,
                             const void *hPayload, int64_t nData, float emptyValue, float fullValue);
 /* The same for data already on the device: binds the caller's device arrays (dState:
- * nBlocks states; dPayload: the payload blocks) without copying.  They must stay valid,
- * and unchanged while a fill reads them, until the level is set or bound again or the
- * context is destroyed.  A level-0 value-block channel binds as its slab
+ * nBlocks states; dPayload: the payload blocks, 16-byte aligned) without copying.  They
+ * must stay valid, and unchanged while a fill reads them, until the level is set or
+ * bound again or the context is destroyed.  A level-0 value-block channel binds as its slab
  * (msbg_gpu_payload_ptr) with states = its slots, -3 for blocks that are not at level 0. */
 int msbg_gpu_level_grid_bind(msbg_gpu_ctx *ctx, int lchan, int level, int storage, const int32_t *dState,
                              const void *dPayload, float emptyValue, float fullValue);
@@ -277,7 +277,7 @@ int msbg_gpu_level_grid_bind(msbg_gpu_ctx *ctx, int lchan, int level, int storag
  * (src/halo.h:385-391, body src/halo.cpp:266-479, out-of-block rule
  * getOutOfBlockValue src/halo.h:270-330) for n blocks in one call.
  * dBids (device, n entries): blocks whose level in the current layout is `level` and
- * that have a block at that level of lchan.  dOut (device): per listed block k,
+ * that have a block at that level of lchan.  dOut (device, 16-byte aligned): per listed block k,
  * (bs+2h)^3 floats at dOut + k*(bs+2h)^3, [z][y][x] over the positions origin-h ..
  * origin+bs+h-1 of level `level` (bs = bsx>>level, h = haloSize, 1..4).  A position
  * inside the domain whose block exists at that level reads it; otherwise
@@ -295,6 +295,21 @@ int msbg_gpu_level_grid_bind(msbg_gpu_ctx *ctx, int lchan, int level, int storag
 enum { MSBG_GPU_BC_NEUMANN = 1 << 10, MSBG_GPU_BC_COARSE_LEVEL = 1 << 26 };
 int msbg_gpu_fill_halo_blocks(msbg_gpu_ctx *ctx, int lchan, int level, const int32_t *dBids, int64_t n,
                               int haloSize, int opt, float *dOut, int64_t *hSkipped);
+/* ---- ray-march render of the iso-0.5 surface -----------------------------------------
+ * RDR::RaymarchRenderer (src/render.h:52-160): setCamera(pos, lookAt, zoom),
+ * setSunLight(sun), setSurfaceColor(color), then render() (src/render.cpp:20-101), which the
+ * demo calls after the splat and after the sweeps (src/msbg_demo.cpp:129-175).  Renders
+ * channel chan (uint16 as the reference; FP32 and FP16 read as values, no reference
+ * counterpart) into dRGB (device, width*height*3 bytes, RGB, row-major, top row first;
+ * the reference's BMP_MKRGB pixel (r, g, b) is bytes r, g, b here; a miss is black).
+ * Camera coordinates are in units of the largest grid side (the domain is [0,1]^3 for a
+ * cubic grid).  Asynchronous on the context's stream. */
+typedef struct {
+  double pos[3], lookAt[3], sun[3], color[3];
+  double zoom;
+} msbg_gpu_camera;
+int msbg_gpu_render(msbg_gpu_ctx *ctx, int chan, int width, int height, const msbg_gpu_camera *cam,
+                    uint8_t *dRGB);
 /* One multigrid V-cycle X = M^{-1} B from X = 0 (the CG preconditioner). */
 int msbg_gpu_vcycle(msbg_gpu_ctx *ctx, int chanX, int chanB);
 /* dotProdChannel (src/msbg.h:3331-3341): FP64-accumulated sum; MSBG_GPU_ERR_NONFINITE

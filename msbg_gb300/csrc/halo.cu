@@ -74,7 +74,7 @@ struct HaloArgs {
   const int32_t *bids;
   const int32_t *levels;  // layout level of every block
   HaloLevel lv, lo;       // level l and level l+1
-  int level, bs, h, hs;
+  int level, bs, log2bs, h, hs;
   uint32_t hsMagic;       // ceil(2^32 / hs): i / hs = umulhi(i, hsMagic) for i < hs^3
   int sx, sy, sz;         // level-l domain
   int nbx, nby, nbz;
@@ -104,10 +104,29 @@ __device__ __forceinline__ Src<T> blockSrc(const HaloLevel &L, int32_t st, int b
   return {nullptr, st == MSBG_GPU_LBLK_EMPTY ? L.emptyF : L.fullF};
 }
 
+// Four consecutive voxels of a row (16- or 8-byte aligned: x is a multiple of 4).
+template <typename T> __device__ __forceinline__ void load4(const T *p, float v[4]);
+template <> __device__ __forceinline__ void load4<float>(const float *p, float v[4]) {
+  const float4 q = __ldg(reinterpret_cast<const float4 *>(p));
+  v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+}
+template <> __device__ __forceinline__ void load4<__half>(const __half *p, float v[4]) {
+  const uint2 q = __ldg(reinterpret_cast<const uint2 *>(p));
+  const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&q.x));
+  const float2 hi = __half22float2(*reinterpret_cast<const __half2 *>(&q.y));
+  v[0] = lo.x; v[1] = lo.y; v[2] = hi.x; v[3] = hi.y;
+}
+template <> __device__ __forceinline__ void load4<uint16_t>(const uint16_t *p, float v[4]) {
+  const uint2 q = __ldg(reinterpret_cast<const uint2 *>(p));
+  v[0] = __fmul_rn((float)(q.x & 0xffffu), kU16ToF);
+  v[1] = __fmul_rn((float)(q.x >> 16), kU16ToF);
+  v[2] = __fmul_rn((float)(q.y & 0xffffu), kU16ToF);
+  v[3] = __fmul_rn((float)(q.y >> 16), kU16ToF);
+}
+
 __device__ __forceinline__ int nbIndex(int p, int o, int bs) { return p < o ? 0 : (p >= o + bs ? 2 : 1); }
 
 constexpr int kHaloThreads = 256;
-constexpr int kHaloUnroll = 8;  // box positions resolved per thread before their loads issue
 
 template <typename T>
 __global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
@@ -141,9 +160,7 @@ __global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
   const bool neumann = (a.opt & MSBG_GPU_BC_NEUMANN) != 0;
   const bool coarse = (a.opt & MSBG_GPU_BC_COARSE_LEVEL) != 0;
   const int bsC = bs >> 1;
-  auto resolve = [&](int i) -> Src<T> {
-    const int q = (int)__umulhi((uint32_t)i, a.hsMagic), hz = (int)__umulhi((uint32_t)q, a.hsMagic);
-    const int hx = i - q * hs, hy = q - hz * hs;
+  auto resolve = [&](int hx, int hy, int hz) -> Src<T> {
     int px = ox + hx - h, py = oy + hy - h, pz = oz + hz - h;
     const bool inRange = px >= 0 && py >= 0 && pz >= 0 && px < a.sx && py < a.sy && pz < a.sz;
     int n = nbIndex(px, ox, bs) + 3 * nbIndex(py, oy, bs) + 9 * nbIndex(pz, oz, bs);
@@ -167,23 +184,64 @@ __global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
     if (sc == MSBG_GPU_LBLK_NONE) return {nullptr, a.lv.emptyF};
     return blockSrc<T>(a.lo, sc, bsC, (px >> 1) & (bsC - 1), (py >> 1) & (bsC - 1), (pz >> 1) & (bsC - 1));
   };
-  // kHaloUnroll positions per thread and round: all sources first, then all loads, so
-  // that each thread has that many independent reads in flight
-  for (int i0 = threadIdx.x; i0 < per; i0 += kHaloThreads * kHaloUnroll) {
-    Src<T> src[kHaloUnroll];
-#pragma unroll
-    for (int u = 0; u < kHaloUnroll; u++) {
-      const int i = i0 + u * kHaloThreads;
-      src[u] = i < per ? resolve(i) : Src<T>{nullptr, 0.0f};
+  auto value = [&](int hx, int hy, int hz) -> float {
+    const Src<T> src = resolve(hx, hy, hz);
+    return src.p ? ldRaw<T>(src.p) : src.c;
+  };
+  const int L = a.log2bs;
+  if (bs < 4) {  // every position the general way
+    for (int i = threadIdx.x; i < per; i += kHaloThreads) {
+      const int q = (int)__umulhi((uint32_t)i, a.hsMagic), hz = (int)__umulhi((uint32_t)q, a.hsMagic);
+      dst[i] = value(i - q * hs, q - hz * hs, hz);
     }
-    float v[kHaloUnroll];
-#pragma unroll
-    for (int u = 0; u < kHaloUnroll; u++) v[u] = src[u].p ? ldRaw<T>(src[u].p) : src[u].c;
-#pragma unroll
-    for (int u = 0; u < kHaloUnroll; u++) {
-      const int i = i0 + u * kHaloThreads;
-      if (i < per) dst[i] = v[u];
+    return;
+  }
+  // Plane by plane through a shared double buffer, so that every output plane (hs^2
+  // floats, a multiple of 16 bytes at a 16-byte aligned offset) leaves in whole 16-byte
+  // stores and no DRAM sector is written in parts.  Interior rows of an interior plane
+  // come from the own block, 4 voxels per thread; the rest of the plane resolves per
+  // position.
+  extern __shared__ __align__(16) float plane[];
+  const int hs2 = hs * hs;
+  const int32_t own = stL[13];
+  const T *blk = own >= 0 ? (const T *)a.lv.pay + (int64_t)own * bs * bs * bs : nullptr;
+  const float cOwn = own == MSBG_GPU_LBLK_EMPTY ? a.lv.emptyF : a.lv.fullF;
+  const int nShell = 2 * h * hs + 2 * h * bs;  // halo rows, then halo columns of the block rows
+  for (int hz = 0; hz < hs; hz++) {
+    float *buf = plane + (hz & 1) * hs2;
+    const int z = hz - h;
+    if (z < 0 || z >= bs) {
+      for (int i = threadIdx.x; i < hs2; i += kHaloThreads) {
+        const int hy = (int)__umulhi((uint32_t)i, a.hsMagic);
+        buf[i] = value(i - hy * hs, hy, hz);
+      }
+    } else {
+      for (int k = threadIdx.x; k < bs * bs / 4; k += kHaloThreads) {
+        const int xq = k & ((bs >> 2) - 1), y = k >> (L - 2);
+        float v[4];
+        if (blk) load4<T>(blk + (z * bs + y) * bs + 4 * xq, v);
+        else v[0] = v[1] = v[2] = v[3] = cOwn;
+        float *o = buf + (y + h) * hs + h + 4 * xq;
+        o[0] = v[0]; o[1] = v[1]; o[2] = v[2]; o[3] = v[3];
+      }
+      for (int j = threadIdx.x; j < nShell; j += kHaloThreads) {
+        int hx, hy;
+        if (j < 2 * h * hs) {
+          const int r = (int)__umulhi((uint32_t)j, a.hsMagic);
+          hx = j - r * hs;
+          hy = r < h ? r : r + bs;
+        } else {  // 2h halo columns on each of the bs block rows
+          const int jj = j - 2 * h * hs, yb = jj / (2 * h), xx = jj - yb * 2 * h;
+          hy = h + yb;
+          hx = xx < h ? xx : xx + bs;
+        }
+        buf[hy * hs + hx] = value(hx, hy, hz);
+      }
     }
+    __syncthreads();
+    float4 *o4 = reinterpret_cast<float4 *>(dst + hz * hs2);
+    const float4 *b4 = reinterpret_cast<const float4 *>(buf);
+    for (int i = threadIdx.x; i < hs2 / 4; i += kHaloThreads) o4[i] = b4[i];
   }
 }
 
@@ -295,6 +353,7 @@ extern "C" int msbg_gpu_fill_halo_blocks(msbg_gpu_ctx *ctx, int lchan, int level
                 opt & ~(MSBG_GPU_BC_NEUMANN | MSBG_GPU_BC_COARSE_LEVEL));
   if (n < 0 || n > 0x7fffffff || (n > 0 && (!dBids || !dOut)))
     return fail(ctx, MSBG_GPU_ERR_ARG, "fill_halo: bad block list");
+  if ((uintptr_t)dOut & 15) return fail(ctx, MSBG_GPU_ERR_ARG, "fill_halo: dOut must be 16-byte aligned");
   if (!ctx->layoutValid) return fail(ctx, MSBG_GPU_ERR_STATE, "no block layout: call set_refinement_map");
   LevelChannels *lc = levelChannels(ctx);
   LevelChannel &c = lc->ch[lchan];
@@ -316,6 +375,7 @@ extern "C" int msbg_gpu_fill_halo_blocks(msbg_gpu_ctx *ctx, int lchan, int level
   }
   a.level = level;
   a.bs = bs;
+  a.log2bs = ctx->log2bs - level;
   a.h = haloSize;
   a.hs = bs + 2 * haloSize;
   a.hsMagic = (uint32_t)(((1ull << 32) + a.hs - 1) / a.hs);  // exact for every i < hs^3 <= 40^3
@@ -324,11 +384,12 @@ extern "C" int msbg_gpu_fill_halo_blocks(msbg_gpu_ctx *ctx, int lchan, int level
   a.opt = opt;
   a.out = dOut;
   a.skipped = lc->dSkip;
+  const size_t smem = 2 * sizeof(float) * (size_t)a.hs * a.hs;  // the plane double buffer (<= 12.8 KB)
   if (n > 0) {
     switch (c.storage) {
-      case MSBG_GPU_F32: MSBG_LAUNCH(ctx, kFillHalo<float>, (unsigned)n, kHaloThreads, 0, a); break;
-      case MSBG_GPU_F16: MSBG_LAUNCH(ctx, kFillHalo<__half>, (unsigned)n, kHaloThreads, 0, a); break;
-      default: MSBG_LAUNCH(ctx, kFillHalo<uint16_t>, (unsigned)n, kHaloThreads, 0, a); break;
+      case MSBG_GPU_F32: MSBG_LAUNCH(ctx, kFillHalo<float>, (unsigned)n, kHaloThreads, smem, a); break;
+      case MSBG_GPU_F16: MSBG_LAUNCH(ctx, kFillHalo<__half>, (unsigned)n, kHaloThreads, smem, a); break;
+      default: MSBG_LAUNCH(ctx, kFillHalo<uint16_t>, (unsigned)n, kHaloThreads, smem, a); break;
     }
   }
   if (hSkipped) {

@@ -96,6 +96,7 @@ SIGNATURES = {
     "msbg_gpu_interpolate": (I, [P, I, P, I64, P, I]),
     "msbg_gpu_level_grid_set": (I, [P, I, I, I, P, P, I64, C.c_float, C.c_float]),
     "msbg_gpu_level_grid_bind": (I, [P, I, I, I, P, P, C.c_float, C.c_float]),
+    "msbg_gpu_render": (I, [P, I, I, I, P, P]),
     "msbg_gpu_fill_halo_blocks": (I, [P, I, I, P, I64, I, I, P, C.POINTER(I64)]),
     "msbg_gpu_diag_wait_timeout": (I, [P, I]),
     "msbg_gpu_vcycle": (I, [P, I, I]),
@@ -173,6 +174,22 @@ class DeviceBuffer:
             self.free()
         except Exception:
             pass
+
+
+# the demo's camera (src/msbg_demo.cpp:123-127) and surface colour (src/msbg_demo.cpp:150)
+DEMO_CAMERA = {"pos": (0.5, 0.8, 0.7), "look_at": (0.5, 0.5, 0.5), "sun": (0.5, 5.0, 5.0),
+               "color": (0.8, 0.6, 0.4), "zoom": 1.0}
+
+
+class Camera(C.Structure):
+    """msbg_gpu_camera; the demo passes float values, so they are rounded to float first."""
+    _fields_ = [("pos", C.c_double * 3), ("lookAt", C.c_double * 3), ("sun", C.c_double * 3),
+                ("color", C.c_double * 3), ("zoom", C.c_double)]
+
+    @classmethod
+    def of(cls, cam: dict) -> "Camera":
+        f = lambda v: (C.c_double * 3)(*[float(np.float32(x)) for x in v])  # noqa: E731
+        return cls(f(cam["pos"]), f(cam["look_at"]), f(cam["sun"]), f(cam["color"]), float(np.float32(cam["zoom"])))
 
 
 class MultiresSparseGrid:
@@ -454,6 +471,24 @@ class MultiresSparseGrid:
             db.free()
             do.free()
         return out, sk
+
+    # ---- RDR::RaymarchRenderer (src/render.h:52-160, src/render.cpp:20-101) -------------
+    def render_device(self, chan: int, width: int, height: int, cam: dict, d_rgb: DeviceBuffer):
+        c = Camera.of(cam)
+        self._check(self.L.msbg_gpu_render(self.h, chan, width, height, C.byref(c), C.c_void_p(d_rgb.ptr)))
+
+    def render(self, chan: int, width: int, height: int, cam: dict | None = None) -> np.ndarray:
+        """The iso-0.5 surface of channel chan seen from cam (default: the demo's camera):
+        uint8 [height][width][3] RGB."""
+        out = np.empty((height, width, 3), np.uint8)
+        d = DeviceBuffer.alloc(out.nbytes)
+        try:
+            self.render_device(chan, width, height, DEMO_CAMERA if cam is None else cam, d)
+            self._check(self.L.msbg_gpu_copy_d2h(self.h, _ptr(out), C.c_void_p(d.ptr), out.nbytes))
+            self.synchronize()
+        finally:
+            d.free()
+        return out
 
     def dotProdChannel(self, a: int, b: int) -> float:
         out = C.c_double()

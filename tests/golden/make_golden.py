@@ -10,7 +10,8 @@ never on the GPU host; the .npz files it writes are committed.
     python tests/golden/make_golden.py
 
 It writes reference_small.npz (splat, levels, sweeps), reference_interp.npz
-(trilinear interpolation) and reference_halo.npz (cross-resolution halo fill).
+(trilinear interpolation), reference_halo.npz (cross-resolution halo fill) and
+reference_render.npz (ray-march render).
 """
 from __future__ import annotations
 
@@ -107,6 +108,7 @@ def main() -> None:
     print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
     make_interp(out)
     make_halo()
+    make_render(out)
 
 
 IP_OPTS = (0, O.IP_CORNER, O.IP_BC_DIRICHLET, O.IP_BC_DIRICHLET_OLD, O.IP_CORNER | O.IP_BC_DIRICHLET,
@@ -183,6 +185,28 @@ def make_halo() -> None:
                     assert np.array_equal(bids, H.blocks_at(lv, st, L))
                     out[f"{kind}_L{L}_o{opt}_h{h}"] = vals
     path = os.path.join(HERE, "reference_halo.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
+
+
+RENDER_CAMERAS = {
+    "demo": dict(O.DEMO_CAMERA),
+    "close": {"pos": (0.2, 0.55, 0.15), "look_at": (0.45, 0.45, 0.5), "sun": (-2.0, 3.0, -1.0),
+              "color": (1.0, 1.0, 1.0), "zoom": 1.7},
+}
+RENDER_SIZES = ((160, 90), (320, 180))
+
+
+def make_render(small: dict) -> None:
+    """RDR::RaymarchRenderer::render (oracle/ref_driver.cpp, render job) of the golden uint16
+    MCF field for two cameras and two image sizes: BMP_MKRGB pixels."""
+    out = {}
+    bids, pay = small["active_bids"], small["pde_mcf8_u16_odd"]
+    for name, cam in RENDER_CAMERAS.items():
+        for w, h in RENDER_SIZES:
+            px, _, _ = O.run_reference_render(RES, RES, RES, BSX, bids, pay, w, h, cam)
+            out[f"{name}_{w}x{h}"] = px
+    path = os.path.join(HERE, "reference_render.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
 
