@@ -310,6 +310,17 @@ typedef struct {
 } msbg_gpu_camera;
 int msbg_gpu_render(msbg_gpu_ctx *ctx, int chan, int width, int height, const msbg_gpu_camera *cam,
                     uint8_t *dRGB);
+/* ---- Morton order of block lists ---------------------------------------------------
+ * MultiresSparseGrid::sortBlockListMorton (src/msbg2.cpp:46-58, declared src/msbg.h:3423):
+ * sorts the n block ids of the device list dBids in place by the Morton code of their
+ * block coordinates (FMA::morton64_encode, src/fastmath.h:290-316: x, y, z bits
+ * interleaved, x lowest).  Each block may appear once (the reference's block lists hold
+ * each block once); a repeated or out-of-range id returns MSBG_GPU_ERR_ARG and leaves the
+ * list unchanged.  The work is one pass over all 8^K codes (2^K = the next power of two
+ * at or above the longest block-grid side); grids so elongated that this exceeds both
+ * 2^27 and 8x the block count return MSBG_GPU_ERR_UNSUPPORTED.  Allocates scratch and
+ * synchronizes. */
+int msbg_gpu_sort_block_list_morton(msbg_gpu_ctx *ctx, int32_t *dBids, int64_t n);
 /* One multigrid V-cycle X = M^{-1} B from X = 0 (the CG preconditioner). */
 int msbg_gpu_vcycle(msbg_gpu_ctx *ctx, int chanX, int chanB);
 /* dotProdChannel (src/msbg.h:3331-3341): FP64-accumulated sum; MSBG_GPU_ERR_NONFINITE

@@ -123,13 +123,20 @@ __global__ void kScanApply(const int32_t *__restrict__ in, int64_t n, const int6
   }
 }
 
+int exclusiveScanFlagsWith(msbg_gpu_ctx *ctx, const int32_t *dIn, int64_t n, int64_t *dOut,
+                           int64_t *dTotal, int64_t *dPartial) {
+  const int64_t nPart = (n + kScanTile - 1) / kScanTile;
+  MSBG_LAUNCH(ctx, kScanReduce, (unsigned)nPart, kScanThreads, 0, dIn, n, dPartial);
+  MSBG_LAUNCH(ctx, kScanPartials, 1, kScanThreads, 0, dPartial, nPart, dTotal);
+  MSBG_LAUNCH(ctx, kScanApply, (unsigned)nPart, kScanThreads, 0, dIn, n, dPartial, dOut);
+  return MSBG_GPU_OK;
+}
+
+int64_t scanPartialCount(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
+
 int exclusiveScanFlags(msbg_gpu_ctx *ctx, const int32_t *dIn, int64_t n, int64_t *dOut,
                        int64_t *dTotal) {
-  const int64_t nPart = (n + kScanTile - 1) / kScanTile;
-  MSBG_LAUNCH(ctx, kScanReduce, (unsigned)nPart, kScanThreads, 0, dIn, n, ctx->dScanPartial);
-  MSBG_LAUNCH(ctx, kScanPartials, 1, kScanThreads, 0, ctx->dScanPartial, nPart, dTotal);
-  MSBG_LAUNCH(ctx, kScanApply, (unsigned)nPart, kScanThreads, 0, dIn, n, ctx->dScanPartial, dOut);
-  return MSBG_GPU_OK;
+  return exclusiveScanFlagsWith(ctx, dIn, n, dOut, dTotal, ctx->dScanPartial);
 }
 
 int ensureTmpSlab(msbg_gpu_ctx *ctx, size_t bytes) {

@@ -117,6 +117,11 @@ inline unsigned gridFor(int64_t n, int threads) {
 // Exclusive scan of int32 flags -> int64 offsets with total in *dTotal (device).
 int exclusiveScanFlags(msbg_gpu_ctx *ctx, const int32_t *dIn, int64_t n, int64_t *dOut,
                        int64_t *dTotal);
+// The same with caller scratch for the per-tile partial sums (scanPartialCount(n) int64s),
+// for inputs longer than the block count.
+int exclusiveScanFlagsWith(msbg_gpu_ctx *ctx, const int32_t *dIn, int64_t n, int64_t *dOut,
+                           int64_t *dTotal, int64_t *dPartial);
+int64_t scanPartialCount(int64_t n);
 
 // Ensure the temp slab can hold `bytes`.
 int ensureTmpSlab(msbg_gpu_ctx *ctx, size_t bytes);

@@ -97,6 +97,7 @@ SIGNATURES = {
     "msbg_gpu_level_grid_set": (I, [P, I, I, I, P, P, I64, C.c_float, C.c_float]),
     "msbg_gpu_level_grid_bind": (I, [P, I, I, I, P, P, C.c_float, C.c_float]),
     "msbg_gpu_render": (I, [P, I, I, I, P, P]),
+    "msbg_gpu_sort_block_list_morton": (I, [P, P, I64]),
     "msbg_gpu_fill_halo_blocks": (I, [P, I, I, P, I64, I, I, P, C.POINTER(I64)]),
     "msbg_gpu_diag_wait_timeout": (I, [P, I]),
     "msbg_gpu_vcycle": (I, [P, I, I]),
@@ -471,6 +472,21 @@ class MultiresSparseGrid:
             db.free()
             do.free()
         return out, sk
+
+    # reference: sortBlockListMorton (src/msbg2.cpp:46-58)
+    def sortBlockListMorton(self, bids: np.ndarray) -> np.ndarray:
+        """The block list in Morton order of the block coordinates (host in, host out)."""
+        bids = np.ascontiguousarray(bids, np.int32)
+        d = self.to_device(bids)
+        try:
+            self._check(self.L.msbg_gpu_sort_block_list_morton(self.h, C.c_void_p(d.ptr), len(bids)))
+            out = np.empty_like(bids)
+            if len(bids):
+                self._check(self.L.msbg_gpu_copy_d2h(self.h, _ptr(out), C.c_void_p(d.ptr), out.nbytes))
+            self.synchronize()
+        finally:
+            d.free()
+        return out
 
     # ---- RDR::RaymarchRenderer (src/render.h:52-160, src/render.cpp:20-101) -------------
     def render_device(self, chan: int, width: int, height: int, cam: dict, d_rgb: DeviceBuffer):

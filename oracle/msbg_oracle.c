@@ -1423,3 +1423,39 @@ int64_t orc_fill_halo(const orc_grid *g, int nLevels, const int32_t *levels,
   }
   return skipped;
 }
+
+/* ---- Morton order (src/msbg2.cpp:46-58, src/fastmath.h:290-316) ---- */
+
+static uint64_t split3(uint64_t x) {
+  x &= 0x1fffff;
+  x = (x | x << 32) & 0x1f00000000ffffull;
+  x = (x | x << 16) & 0x1f0000ff0000ffull;
+  x = (x | x << 8) & 0x100f00f00f00f00full;
+  x = (x | x << 4) & 0x10c30c30c30c30c3ull;
+  x = (x | x << 2) & 0x1249249249249249ull;
+  return x;
+}
+
+uint64_t orc_morton64(uint32_t x, uint32_t y, uint32_t z) {
+  return split3(x) | (split3(y) << 1) | (split3(z) << 2);
+}
+
+typedef struct { uint64_t key; int32_t bid; } mkey;
+
+static int mkey_cmp(const void *a, const void *b) {
+  const uint64_t ka = ((const mkey *)a)->key, kb = ((const mkey *)b)->key;
+  return ka < kb ? -1 : ka > kb ? 1 : 0;
+}
+
+void orc_sort_blocks_morton(int nbx, int nby, int nbz, int32_t *bids, int64_t n) {
+  (void)nbz;
+  mkey *k = (mkey *)malloc(sizeof(mkey) * (size_t)(n > 0 ? n : 1));
+  for (int64_t i = 0; i < n; i++) {
+    const int32_t b = bids[i];
+    k[i].key = orc_morton64((uint32_t)(b % nbx), (uint32_t)((b / nbx) % nby), (uint32_t)(b / (nbx * nby)));
+    k[i].bid = b;
+  }
+  qsort(k, (size_t)n, sizeof(mkey), mkey_cmp);
+  for (int64_t i = 0; i < n; i++) bids[i] = k[i].bid;
+  free(k);
+}

@@ -195,6 +195,13 @@ enum { ORC_RENDER_RECIP = 1 };
 void orc_render(const orc_grid *g, const int32_t *slot, const void *payload, int width, int height,
                 const orc_camera *cam, int opt, int32_t *pixels);
 
+/* ---- Morton order of block lists ---------------------------------------------------
+ * MultiresSparseGrid::sortBlockListMorton (src/msbg2.cpp:46-58): ascending
+ * FMA::morton64_encode of the block coordinates (src/fastmath.h:290-316: the bits of x,
+ * y, z interleaved, x lowest).  Sorts bids[n] in place. */
+uint64_t orc_morton64(uint32_t x, uint32_t y, uint32_t z);
+void orc_sort_blocks_morton(int nbx, int nby, int nbz, int32_t *bids, int64_t n);
+
 /* ---- conversions (exposed for tests) ---- */
 uint16_t orc_f32_to_f16(float f);
 float orc_f16_to_f32(uint16_t h);

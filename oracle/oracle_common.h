@@ -24,6 +24,8 @@
  * RDR::RaymarchRenderer (src/render.h:52-160, src/render.cpp:20-101): the points are
  * camera position, look-at point, sun position, surface colour and (zoom, 0, 0);
  * nIter x laplTyp is the image size.
+ * A "morton job" sorts a list of block ids with MultiresSparseGrid::sortBlockListMorton
+ * (src/msbg2.cpp:46-58): int32 bids[nBlocksIn] in, the sorted list out.
  */
 #ifndef MSBG_ORACLE_COMMON_H
 #define MSBG_ORACLE_COMMON_H
@@ -35,7 +37,7 @@
 
 enum { ORACLE_CHAN_F32 = 0, ORACLE_CHAN_U16 = 1 };
 enum { ORACLE_JOB_SURFACE = 1, ORACLE_JOB_LEVELS = 2, ORACLE_JOB_INTERP = 3, ORACLE_JOB_HALO = 4,
-       ORACLE_JOB_RENDER = 5 };
+       ORACLE_JOB_RENDER = 5, ORACLE_JOB_MORTON = 6 };
 
 /* Interp job option bits: the reference's own interpolation options (src/sbg.h:140-170)
  * plus one bit that the reference's enum leaves unused, for the render-density scale. */
@@ -88,7 +90,8 @@ typedef struct {
    * interp job: tPdeSec = interpolation time; then float32 values[nPoints]
    * halo job: nActive = filled blocks, tPdeSec = fill time; then int32 bids[nActive],
    *           float32 halo[nActive][(bs_l+2h)^3]
-   * render job: tPdeSec = render time; then int32 pixels[height][width] (BMP_MKRGB) */
+   * render job: tPdeSec = render time; then int32 pixels[height][width] (BMP_MKRGB)
+   * morton job: nActive = list length; then int32 sorted bids[nActive] */
 } OracleOutHeader;
 
 #endif

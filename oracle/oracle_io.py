@@ -26,7 +26,7 @@ REF_DRIVER = os.path.join(HERE, "_ref", "msbg_ref_driver")
 JOB_MAGIC = b"MSBGJOB2"
 OUT_MAGIC = b"MSBGOUT2"
 CHAN_F32, CHAN_U16 = 0, 1
-JOB_SURFACE, JOB_LEVELS, JOB_INTERP, JOB_HALO, JOB_RENDER = 1, 2, 3, 4, 5
+JOB_SURFACE, JOB_LEVELS, JOB_INTERP, JOB_HALO, JOB_RENDER, JOB_MORTON = 1, 2, 3, 4, 5, 6
 
 # interpolation options: the reference's bits (src/sbg.h:140-170) and the render-density
 # scale of the uint16 channel (a bit the reference's enum leaves unused)
@@ -237,6 +237,26 @@ def run_reference_render(sx, sy, sz, bsx, active_bids, payload_u16, width, heigh
         raise ValueError("bad oracle output")
     px = np.frombuffer(buf, np.int32, width * height, hsz).copy().reshape(height, width)
     return px, float(h[17]), int(h[19])
+
+
+def run_reference_morton(sx, sy, sz, bsx, bids, timeout: float = 600) -> np.ndarray:
+    """MultiresSparseGrid::sortBlockListMorton (src/msbg2.cpp:46-58) of a block-id list."""
+    bids = np.ascontiguousarray(bids, dtype=np.int32).ravel()
+    with tempfile.TemporaryDirectory() as td:
+        jp, op = os.path.join(td, "job.bin"), os.path.join(td, "out.bin")
+        hdr = struct.pack(_JOB_FMT, JOB_MAGIC, JOB_MORTON, sx, sy, sz, bsx, 3, 0, 0, 0, 0, 0,
+                          0.0, 0.0, 0.0, 0.0, 0, 0, bids.size)
+        with open(jp, "wb") as f:
+            f.write(hdr)
+            f.write(bids.tobytes())
+        r = subprocess.run([REF_DRIVER, jp, op], cwd=td, timeout=timeout,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference morton job failed with status {r.returncode}")
+        with open(op, "rb") as f:
+            buf = f.read()
+    hsz = struct.calcsize(_OUT_FMT)
+    return np.frombuffer(buf, np.int32, bids.size, hsz).copy()
 
 
 def read_result(path: str, bsx: int, surface: bool = True) -> OracleResult:

@@ -75,6 +75,9 @@ def lib():
                                     C.c_int, C.c_uint, P]
         L.orc_fill_halo.restype = C.c_int64
         L.orc_render.argtypes = [C.POINTER(Grid), P, P, C.c_int, C.c_int, C.c_void_p, C.c_int, P]
+        L.orc_sort_blocks_morton.argtypes = [C.c_int, C.c_int, C.c_int, P, C.c_int64]
+        L.orc_morton64.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32]
+        L.orc_morton64.restype = C.c_uint64
         L.orc_f32_to_f16.argtypes = [C.c_float]
         L.orc_f32_to_f16.restype = C.c_uint16
         L.orc_f16_to_f32.argtypes = [C.c_uint16]
@@ -199,6 +202,13 @@ def fill_halo(g: Grid, levels, states: list, payloads: list, level: int, bids, h
                                   _p(bids), len(bids),
                                   halo, opt, _p(out))
     return out, int(skipped)
+
+
+def sort_blocks_morton(nbx: int, nby: int, nbz: int, bids) -> np.ndarray:
+    """sortBlockListMorton restated (src/msbg2.cpp:46-58): the list in Morton order."""
+    out = np.ascontiguousarray(bids, np.int32).copy()
+    lib().orc_sort_blocks_morton(nbx, nby, nbz, _p(out), out.size)
+    return out
 
 
 class Camera(C.Structure):

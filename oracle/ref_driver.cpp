@@ -12,7 +12,8 @@
  * library itself: MultiresSparseGrid::create, regularizeRefinementMap,
  * setRefinementMap, SparseGrid block management, applyChannelPdeFast<T>, the
  * trilinear interpolation functions (interp job), HaloBlockSet::fillHaloBlock_<T>
- * (halo job) and the ray-march renderer RDR::RaymarchRenderer (render job).
+ * (halo job), the ray-march renderer RDR::RaymarchRenderer (render job) and
+ * sortBlockListMorton (morton job).
  *
  * Differences from the demo, both forced by the workload definition:
  *  - points come from the job file (already in voxel coordinates) instead of
@@ -489,6 +490,29 @@ int runRenderJob(const OracleJobHeader &job, const float *cam, const int32_t *bi
   return 0;
 }
 
+// MultiresSparseGrid::sortBlockListMorton (src/msbg2.cpp:46-58) of a list of block ids.
+int runMortonJob(const OracleJobHeader &job, const int32_t *bids, FILE *fout) {
+  OracleOutHeader out;
+  memset(&out, 0, sizeof(out));
+  memcpy(out.magic, ORACLE_OUT_MAGIC, 8);
+  MultiresSparseGrid *msbg = MultiresSparseGrid::create(
+      "TEST", job.sx, job.sy, job.sz, job.bsx, -1, 0, -1,
+      MSBG::OPT_SINGLE_LEVEL | MSBG::OPT_SINGLE_CHANNEL_FLOAT);
+  if (!msbg) return 2;
+  std::vector<int> list(bids, bids + job.nBlocksIn);
+  for (int b : list)
+    if (b < 0 || b >= msbg->nBlocks()) return 4;
+  const double t0 = nowSec();
+  msbg->sortBlockListMorton(list);
+  out.tPdeSec = nowSec() - t0;
+  out.nBlocks = msbg->nBlocks();
+  out.nActive = (int)list.size();
+  fwrite(&out, sizeof(out), 1, fout);
+  fwrite(list.data(), 4, list.size(), fout);
+  MultiresSparseGrid::destroy(msbg);
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -543,6 +567,8 @@ int main(int argc, char **argv) {
   int rc;
   if (job.jobType == ORACLE_JOB_LEVELS)
     rc = runLevelsJob(job, lv.data(), fout);
+  else if (job.jobType == ORACLE_JOB_MORTON)
+    rc = runMortonJob(job, lv.data(), fout);
   else if (job.jobType == ORACLE_JOB_RENDER)
     rc = job.chanType == ORACLE_CHAN_U16 && job.nPoints == 5
              ? runRenderJob(job, pts.data(), lv.data(), reinterpret_cast<const uint16_t *>(payload.data()), fout)

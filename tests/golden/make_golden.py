@@ -10,8 +10,9 @@ never on the GPU host; the .npz files it writes are committed.
     python tests/golden/make_golden.py
 
 It writes reference_small.npz (splat, levels, sweeps), reference_interp.npz
-(trilinear interpolation), reference_halo.npz (cross-resolution halo fill) and
-reference_render.npz (ray-march render).
+(trilinear interpolation), reference_halo.npz (cross-resolution halo fill),
+reference_render.npz (ray-march render) and reference_morton.npz (Morton-ordered block
+lists).
 """
 from __future__ import annotations
 
@@ -109,6 +110,7 @@ def main() -> None:
     make_interp(out)
     make_halo()
     make_render(out)
+    make_morton()
 
 
 IP_OPTS = (0, O.IP_CORNER, O.IP_BC_DIRICHLET, O.IP_BC_DIRICHLET_OLD, O.IP_CORNER | O.IP_BC_DIRICHLET,
@@ -207,6 +209,25 @@ def make_render(small: dict) -> None:
             px, _, _ = O.run_reference_render(RES, RES, RES, BSX, bids, pay, w, h, cam)
             out[f"{name}_{w}x{h}"] = px
     path = os.path.join(HERE, "reference_render.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
+
+
+MORTON_GRIDS = ((8, 8, 8), (13, 6, 10), (32, 32, 32), (40, 3, 17))
+
+
+def make_morton() -> None:
+    """MultiresSparseGrid::sortBlockListMorton (oracle/ref_driver.cpp, morton job) of seeded
+    random lists (a third of each block grid, in random order) on 16^3 blocks."""
+    out = {}
+    rng = np.random.Generator(np.random.PCG64(20261203 + 940))
+    for nb in MORTON_GRIDS:
+        n = int(np.prod(nb))
+        bids = rng.permutation(n)[: max(2, n // 3)].astype(np.int32)
+        key = "x".join(map(str, nb))
+        out[f"in_{key}"] = bids
+        out[f"out_{key}"] = O.run_reference_morton(nb[0] * 16, nb[1] * 16, nb[2] * 16, 16, bids)
+    path = os.path.join(HERE, "reference_morton.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
 
