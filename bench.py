@@ -383,20 +383,6 @@ def run_gpu(args, spec, dist: Dist):
                             "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
                             "algorithmic_bytes_per_point": 16}}
 
-    # cross-resolution halo fill (HaloBlockSet::fillHaloBlock_, OPT_BC_COARSE_LEVEL, halo 1)
-    # of every level-0 block of the swept field: level 0 of a level channel bound to the
-    # value-block slab (states: slots, "no block" off level 0), level 1 the level-1
-    # blocks.  Algorithmic bytes per block: the (bs+2)^3 box read once at S bytes per
-    # value and written once as FP32.
-    halo = None
-    if not args.no_jacobi:
-        halo = halo_measure(g, info, storage, elem, bsx, args.steps, dist, peaks)
-
-    # ray-march render of the iso-0.5 surface (RaymarchRenderer::render) of the swept field
-    render = None
-    if not args.no_jacobi:
-        render = render_measure(g, args.steps, dist, cpu=dist.rank == 0 and not args.no_cpu_baseline)
-
     # e2e through the host-buffer entry point
     e2e = None
     if not args.no_e2e:
@@ -427,6 +413,20 @@ def run_gpu(args, spec, dist: Dist):
                "seconds_per_step": t_e2e}
         G.load_library().msbg_gpu_host_free(hp)
         G.load_library().msbg_gpu_host_free(ho)
+
+    # cross-resolution halo fill (HaloBlockSet::fillHaloBlock_, OPT_BC_COARSE_LEVEL, halo 1)
+    # of every level-0 block of the swept field: level 0 of a level channel bound to the
+    # value-block slab (states: slots, "no block" off level 0), level 1 the level-1
+    # blocks.  Algorithmic bytes per block: the (bs+2)^3 box read once at S bytes per
+    # value and written once as FP32.
+    halo = None
+    if not args.no_jacobi:
+        halo = halo_measure(g, info, storage, elem, bsx, args.steps, dist, peaks)
+
+    # ray-march render of the iso-0.5 surface (RaymarchRenderer::render) of the swept field
+    render = None
+    if not args.no_jacobi:
+        render = render_measure(g, args.steps, dist, cpu=dist.rank == 0 and not args.no_cpu_baseline)
 
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:

@@ -45,7 +45,9 @@ enum {
   MSBG_GPU_ERR_NONFINITE = -6,   /* a reduction met NaN/Inf (src/msbg.cpp:4635) */
   MSBG_GPU_ERR_DIVERGED = -7,    /* solver residual non-finite or increasing    */
   MSBG_GPU_ERR_UNSUPPORTED = -8, /* option the GPU path does not implement      */
-  MSBG_GPU_ERR_TIMEOUT = -9      /* a bounded device-side wait gave up          */
+  MSBG_GPU_ERR_TIMEOUT = -9,     /* a bounded device-side wait gave up          */
+  MSBG_GPU_ERR_IO = -10          /* a checkpoint file could not be written or read, or
+                                    its contents fail their checks              */
 };
 
 /* ---- storage types of a channel ------------------------------------------ */
@@ -321,6 +323,23 @@ int msbg_gpu_render(msbg_gpu_ctx *ctx, int chan, int width, int height, const ms
  * 2^27 and 8x the block count return MSBG_GPU_ERR_UNSUPPORTED.  Allocates scratch and
  * synchronizes. */
 int msbg_gpu_sort_block_list_morton(msbg_gpu_ctx *ctx, int32_t *dBids, int64_t n);
+/* ---- checkpoint files ------------------------------------------------------------
+ * The reference has no on-disk format for a MultiresSparseGrid (its VDB writers are
+ * declarations only, src/sbg.h:599-605); this is a raw dump for checkpoint and restart.
+ * msbg_gpu_save writes the grid geometry, the level map (int8 per block) and the
+ * payload of nChans channels (chans[]; all value blocks in slot order, that is ascending
+ * block id), each with an FNV-1a 64-bit checksum, little-endian:
+ *   "MSBGCKP1", uint32 version 1, uint32 header bytes (64), int32 sx sy sz bsx nLevels
+ *   nChans, int64 nBlocks nActive, uint64 checksum of the level map;
+ *   int8 levels[nBlocks];
+ *   per channel: int32 chan, int32 storage, int64 bytes, uint64 checksum, payload bytes.
+ * msbg_gpu_load creates a context from such a file (*ctx), rebuilds the layout with
+ * msbg_gpu_set_levels + msbg_gpu_set_refinement_map and restores the channels.  Both
+ * stream through a pinned staging buffer and synchronize.  Errors: MSBG_GPU_ERR_IO for
+ * a file that cannot be opened, written or read, is truncated, has another magic or
+ * version, or fails a checksum (a failed load leaves *ctx NULL). */
+int msbg_gpu_save(msbg_gpu_ctx *ctx, const char *path, const int *chans, int nChans);
+int msbg_gpu_load(msbg_gpu_ctx **ctx, const char *path);
 /* One multigrid V-cycle X = M^{-1} B from X = 0 (the CG preconditioner). */
 int msbg_gpu_vcycle(msbg_gpu_ctx *ctx, int chanX, int chanB);
 /* dotProdChannel (src/msbg.h:3331-3341): FP64-accumulated sum; MSBG_GPU_ERR_NONFINITE

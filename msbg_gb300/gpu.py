@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import struct
 from dataclasses import dataclass
 
 import numpy as np
@@ -21,6 +22,7 @@ LIB_PATH = os.path.join(PKG, "lib", "libmsbg_gpu.so")
 OK = 0
 ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_CAPACITY, ERR_NONFINITE, ERR_DIVERGED, ERR_UNSUPPORTED, ERR_TIMEOUT = \
     -1, -2, -3, -4, -5, -6, -7, -8, -9
+ERR_IO = -10
 
 F32, U16, F16, F64 = 0, 1, 2, 3
 NP_STORAGE = {F32: np.float32, U16: np.uint16, F16: np.float16, F64: np.float64}
@@ -98,6 +100,8 @@ SIGNATURES = {
     "msbg_gpu_level_grid_bind": (I, [P, I, I, I, P, P, C.c_float, C.c_float]),
     "msbg_gpu_render": (I, [P, I, I, I, P, P]),
     "msbg_gpu_sort_block_list_morton": (I, [P, P, I64]),
+    "msbg_gpu_save": (I, [P, C.c_char_p, P, I]),
+    "msbg_gpu_load": (I, [C.POINTER(P), C.c_char_p]),
     "msbg_gpu_fill_halo_blocks": (I, [P, I, I, P, I64, I, I, P, C.POINTER(I64)]),
     "msbg_gpu_diag_wait_timeout": (I, [P, I]),
     "msbg_gpu_vcycle": (I, [P, I, I]),
@@ -193,6 +197,28 @@ class Camera(C.Structure):
         return cls(f(cam["pos"]), f(cam["look_at"]), f(cam["sun"]), f(cam["color"]), float(np.float32(cam["zoom"])))
 
 
+CKPT_HEADER = struct.Struct("<8sII6i2qQ")  # magic, version, header bytes, sx sy sz bsx nLevels nChans,
+CKPT_CHANNEL = struct.Struct("<iiqQ")      # nBlocks nActive, levels checksum; chan storage bytes checksum
+
+
+def read_checkpoint_index(path: str) -> dict:
+    """The header and channel records of a checkpoint file (msbg_gpu_save), without payloads."""
+    with open(path, "rb") as f:
+        magic, version, hbytes, sx, sy, sz, bsx, n_levels, n_chans, n_blocks, n_active, lhash = \
+            CKPT_HEADER.unpack(f.read(CKPT_HEADER.size))
+        if magic != b"MSBGCKP1" or version != 1 or hbytes != CKPT_HEADER.size:
+            raise ValueError(f"{path}: not a version-1 checkpoint")
+        f.seek(n_blocks, 1)
+        chans = []
+        for _ in range(n_chans):
+            chan, storage, nbytes, chash = CKPT_CHANNEL.unpack(f.read(CKPT_CHANNEL.size))
+            chans.append({"chan": chan, "storage": storage, "bytes": nbytes, "checksum": chash,
+                          "offset": f.tell()})
+            f.seek(nbytes, 1)
+    return {"sx": sx, "sy": sy, "sz": sz, "bsx": bsx, "n_levels": n_levels, "n_blocks": n_blocks,
+            "n_active": n_active, "levels_checksum": lhash, "channels": chans}
+
+
 class MultiresSparseGrid:
     """GPU MultiresSparseGrid over one context of the C ABI."""
 
@@ -214,6 +240,32 @@ class MultiresSparseGrid:
     def create(cls, name: str, sx: int, sy: int, sz: int, blockSize0: int, nLevels: int = 3,
                storage: int = F32, capacity_blocks: int = 0) -> "MultiresSparseGrid":
         return cls(sx, sy, sz, blockSize0, nLevels, storage, capacity_blocks)
+
+    # checkpoint files (no reference counterpart: the reference has no grid file format)
+    def save(self, path: str, chans=(0,)):
+        """Geometry, level map and the payload of channels chans to a checkpoint file."""
+        ch = np.ascontiguousarray(list(chans), np.int32)
+        self._check(self.L.msbg_gpu_save(self.h, os.fsencode(path), _ptr(ch), len(ch)))
+
+    @classmethod
+    def load(cls, path: str) -> "MultiresSparseGrid":
+        """A grid restored from a checkpoint file (layout rebuilt from its level map)."""
+        L = load_library()
+        h = C.c_void_p()
+        rc = L.msbg_gpu_load(C.byref(h), os.fsencode(path))
+        if rc != OK:
+            raise MsbgGpuError(rc, f"msbg_gpu_load failed for {path}")
+        g = cls.__new__(cls)
+        g.L, g.h = L, h
+        info = Info()
+        g._check(L.msbg_gpu_get_info(h, C.byref(info)))
+        g.sx, g.sy, g.sz, g.bsx, g.n_levels = info.sx, info.sy, info.sz, info.bsx, info.nLevels
+        g.nbx, g.nby, g.nbz = info.nbx, info.nby, info.nbz
+        g.n_blocks = g.nbx * g.nby * g.nbz
+        g.storage = {0: F32}
+        for rec in read_checkpoint_index(path)["channels"]:
+            g.storage[rec["chan"]] = rec["storage"]
+        return g
 
     def _check(self, rc: int):
         if rc != OK:
