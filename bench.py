@@ -277,6 +277,13 @@ def run_gpu(args, spec, dist: Dist):
     g.splat(d, n, 2.0, 2.0)
     g.splat_finalize(2.0, 2.0)
     g.synchronize()
+    # the splat alone (it restarts from its fill each call; the finalized field stays as is)
+    g.event_record(12)
+    for _ in range(3):
+        g.splat(d, n, 2.0, 2.0)
+    g.event_record(13)
+    g.synchronize()
+    splat_ms = dist.max(g.event_elapsed_ms(12, 13)) / 3
     info = g.info()
     n_act = info.nActive
     vox = n_act * bsx ** 3
@@ -466,6 +473,8 @@ def run_gpu(args, spec, dist: Dist):
         "restriction": restriction,
         "g2p": g2p,
         "field_error_vs_fp64": field_error,
+        "splat": {"kernel": "kSplat (FP32 staging fill + atomic min)", "ms_per_call": splat_ms,
+                  "particles_per_s": n * dist.world / (splat_ms / 1e3)},
         "halo_fill": halo,
         "render": render,
         "poisson": poisson,

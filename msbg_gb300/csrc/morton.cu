@@ -113,7 +113,7 @@ extern "C" int msbg_gpu_sort_block_list_morton(msbg_gpu_ctx *ctx, int32_t *dBids
     }
     if (hBad & 1) { rc = fail(ctx, MSBG_GPU_ERR_ARG, "sort_block_list_morton: block id out of range"); break; }
     if (hBad & 2) { rc = fail(ctx, MSBG_GPU_ERR_ARG, "sort_block_list_morton: a block is listed twice"); break; }
-    if (cudaMemcpyAsync(dBids, out, bOut, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess ||
+    if (cudaMemcpyAsync(dBids, out, (size_t)n * 4, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess ||
         cudaStreamSynchronize(ctx->stream) != cudaSuccess)
       rc = fail(ctx, MSBG_GPU_ERR_CUDA, "sort_block_list_morton: copy failed");
   } while (0);
