@@ -127,16 +127,10 @@ template <> __device__ __forceinline__ void load4<uint16_t>(const uint16_t *p, f
 __device__ __forceinline__ int nbIndex(int p, int o, int bs) { return p < o ? 0 : (p >= o + bs ? 2 : 1); }
 
 constexpr int kHaloThreads = 256;
-// how the positions of one neighbour block read
-enum { kNbConst = 0, kNbLevel = 1, kNbCoarse = 2, kNbOwnClamped = 3, kNbGeneral = 4 };
 
 template <typename T>
 __global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
   __shared__ int32_t stL[27], stC[27];
-  // per neighbour: how its positions read (kNb*), from which block, or which constant
-  __shared__ const T *nbBase[27];
-  __shared__ float nbConst[27];
-  __shared__ int nbKind[27];
   const int bid = a.bids[blockIdx.x];
   const int64_t nxy = (int64_t)a.nbx * a.nby;
   const int64_t nBlocks = nxy * a.nbz;
@@ -157,31 +151,6 @@ __global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
     }
     stL[t] = l;
     stC[t] = c;
-    const bool inside = x >= 0 && y >= 0 && z >= 0 && x < a.nbx && y < a.nby && z < a.nbz;
-    const int bsL = a.bs, bsC = a.bs >> 1;
-    int kind = kNbConst;
-    const T *base = nullptr;
-    float cv = a.lv.emptyF;
-    if (l >= 0) {
-      kind = kNbLevel;
-      base = (const T *)a.lv.pay + (int64_t)l * bsL * bsL * bsL;
-    } else if (l != MSBG_GPU_LBLK_NONE) {
-      cv = l == MSBG_GPU_LBLK_EMPTY ? a.lv.emptyF : a.lv.fullF;
-    } else if (a.opt & MSBG_GPU_BC_NEUMANN) {
-      kind = kNbOwnClamped;
-    } else if (a.opt & MSBG_GPU_BC_COARSE_LEVEL) {
-      if (!inside) {
-        kind = kNbGeneral;  // clamped into the domain: position by position
-      } else if (c >= 0) {
-        kind = kNbCoarse;
-        base = (const T *)a.lo.pay + (int64_t)c * bsC * bsC * bsC;
-      } else if (c != MSBG_GPU_LBLK_NONE) {
-        cv = c == MSBG_GPU_LBLK_EMPTY ? a.lo.emptyF : a.lo.fullF;
-      }
-    }
-    nbKind[t] = kind;
-    nbBase[t] = base;
-    nbConst[t] = cv;
   }
   __syncthreads();
   const int bs = a.bs, h = a.h, hs = a.hs;
@@ -219,24 +188,6 @@ __global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
     const Src<T> src = resolve(hx, hy, hz);
     return src.p ? ldRaw<T>(src.p) : src.c;
   };
-  // the same value through the neighbour's descriptor: one table read, then a load
-  const int msk = bs - 1, mskC = (bs >> 1) - 1, bsC2 = bs >> 1;
-  auto shellValue = [&](int hx, int hy, int hz) -> float {
-    const int px = ox + hx - h, py = oy + hy - h, pz = oz + hz - h;
-    const int n = nbIndex(px, ox, bs) + 3 * nbIndex(py, oy, bs) + 9 * nbIndex(pz, oz, bs);
-    switch (nbKind[n]) {
-      case kNbLevel: return ldRaw<T>(nbBase[n] + (((pz & msk) * bs + (py & msk)) * bs + (px & msk)));
-      case kNbCoarse:
-        return ldRaw<T>(nbBase[n] + ((((pz >> 1) & mskC) * bsC2 + ((py >> 1) & mskC)) * bsC2 + ((px >> 1) & mskC)));
-      case kNbOwnClamped: {
-        const int cx = min(max(px, ox), ox + msk) - ox, cy = min(max(py, oy), oy + msk) - oy,
-                  cz = min(max(pz, oz), oz + msk) - oz;
-        return nbKind[13] == kNbLevel ? ldRaw<T>(nbBase[13] + ((cz * bs + cy) * bs + cx)) : nbConst[13];
-      }
-      case kNbGeneral: return value(hx, hy, hz);
-      default: return nbConst[n];
-    }
-  };
   const int L = a.log2bs;
   if (bs < 4) {  // every position the general way
     for (int i = threadIdx.x; i < per; i += kHaloThreads) {
@@ -262,7 +213,7 @@ __global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
     if (z < 0 || z >= bs) {
       for (int i = threadIdx.x; i < hs2; i += kHaloThreads) {
         const int hy = (int)__umulhi((uint32_t)i, a.hsMagic);
-        buf[i] = shellValue(i - hy * hs, hy, hz);
+        buf[i] = value(i - hy * hs, hy, hz);
       }
     } else {
       for (int k = threadIdx.x; k < bs * bs / 4; k += kHaloThreads) {
@@ -284,7 +235,7 @@ __global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
           hy = h + yb;
           hx = xx < h ? xx : xx + bs;
         }
-        buf[hy * hs + hx] = shellValue(hx, hy, hz);
+        buf[hy * hs + hx] = value(hx, hy, hz);
       }
     }
     __syncthreads();
