@@ -52,17 +52,6 @@ int fillChannel(msbg_gpu_ctx *ctx, int chan, double v) {
   return MSBG_GPU_OK;
 }
 
-// dst[0] = min(dst[0], q) for a non-negative q, as an integer min on the float's bits.
-// Most candidates do not lower the value (a voxel sees many particles, and only a new
-// minimum changes it), so a plain load decides first and only a lower q issues the
-// atomic.  The load may return an older value than the atomics of other SMs have left in
-// L2, but values only fall, so an older value is never lower than the current one: a
-// skipped atomic could not have changed anything.
-__device__ __forceinline__ void splatMin(float *dst, float q) {
-  const int qi = __float_as_int(q);
-  if (qi < *reinterpret_cast<const int *>(dst)) atomicMin(reinterpret_cast<int *>(dst), qi);
-}
-
 struct SplatGeom {
   int sx, sy, sz, nbx, nby, log2bs;
   float domMin[3], domMax[3];
@@ -159,7 +148,7 @@ __global__ void __launch_bounds__(256) kSplat(const float *__restrict__ pts, int
         const float d2 = __fadd_rn(dzy, __fmul_rn(dx, dx));
         if (d2 > g.distSqMax) continue;
         const int64_t base = (ix >> s) == bxa ? sa : sb;
-        splatMin(dst + base + rowVid + (ix & mask), __fmul_rn(d2, g.distSqMaxInv));
+        atomicMin((int *)(dst + base + rowVid + (ix & mask)), __float_as_int(__fmul_rn(d2, g.distSqMaxInv)));
       }
     }
     return;
@@ -176,7 +165,7 @@ __global__ void __launch_bounds__(256) kSplat(const float *__restrict__ pts, int
     if (sl < 0) continue;  // unreachable: an earlier in-sphere voxel would have set abortAt
     const int vid = ((iz & mask) << (2 * s)) + ((iy & mask) << s) + (ix & mask);
     const float q = __fmul_rn(d2, g.distSqMaxInv);
-    splatMin(dst + (int64_t)sl * vpb + vid, q);
+    atomicMin((int *)(dst + (int64_t)sl * vpb + vid), __float_as_int(q));
   }
 }
 
