@@ -127,9 +127,8 @@ template <> __device__ __forceinline__ void load4<uint16_t>(const uint16_t *p, f
 __device__ __forceinline__ int nbIndex(int p, int o, int bs) { return p < o ? 0 : (p >= o + bs ? 2 : 1); }
 
 constexpr int kHaloThreads = 256;
-constexpr int kShellPerThread = 3;  // shell positions of a plane per thread: 2h(hs + bs) <= 576 for bs <= 32, h <= 4
 
-template <typename T>
+template <typename T, int NSH>
 __global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
   __shared__ int32_t stL[27], stC[27];
   const int bid = a.bids[blockIdx.x];
@@ -219,14 +218,14 @@ __global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
     if (own >= 0) quadSrc = (const T *)a.lv.pay + (int64_t)own * bs * bs * bs + y * bs + 4 * xq;
     quadDst = (y + h) * hs + h + 4 * xq;
   }
-  // shell positions of the interior planes: up to kShellPerThread per thread
+  // shell positions of the interior planes: up to NSH per thread
   const int nShell = 2 * h * hs + 2 * h * bs;  // halo rows, then halo columns of the block rows
-  const T *shSrc[kShellPerThread];
-  float shConst[kShellPerThread];
-  int shStep[kShellPerThread], shDst[kShellPerThread];
-  bool shHalf[kShellPerThread];
+  const T *shSrc[NSH];
+  float shConst[NSH];
+  int shStep[NSH], shDst[NSH];
+  bool shHalf[NSH];
 #pragma unroll
-  for (int u = 0; u < kShellPerThread; u++) {
+  for (int u = 0; u < NSH; u++) {
     const int j = threadIdx.x + u * kHaloThreads;
     shSrc[u] = nullptr;
     shConst[u] = 0.0f;
@@ -290,6 +289,20 @@ __global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
       shConst[u] = st == MSBG_GPU_LBLK_EMPTY ? lvp->emptyF : lvp->fullF;
     }
   }
+  // this thread's values of one interior plane, loaded one plane ahead of their use so
+  // that the loads of plane z+1 are in flight across plane z's barrier and stores
+  float qv[4], sv[NSH];
+  auto loadPlane = [&](int z) {
+    if (hasQuad) {
+      if (quadSrc) load4<T>(quadSrc + z * bs * bs, qv);
+      else qv[0] = qv[1] = qv[2] = qv[3] = quadConst;
+    }
+#pragma unroll
+    for (int u = 0; u < NSH; u++)
+      if (shDst[u] >= 0)
+        sv[u] = shSrc[u] ? ldRaw<T>(shSrc[u] + (shHalf[u] ? (z >> 1) : z) * shStep[u]) : shConst[u];
+  };
+  loadPlane(0);
   for (int hz = 0; hz < hs; hz++) {
     float *buf = plane + (hz & 1) * hs2;
     const int z = hz - h;
@@ -300,17 +313,13 @@ __global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
       }
     } else {
       if (hasQuad) {
-        float v[4];
-        if (quadSrc) load4<T>(quadSrc + z * bs * bs, v);
-        else v[0] = v[1] = v[2] = v[3] = quadConst;
         float *o = buf + quadDst;
-        o[0] = v[0]; o[1] = v[1]; o[2] = v[2]; o[3] = v[3];
+        o[0] = qv[0]; o[1] = qv[1]; o[2] = qv[2]; o[3] = qv[3];
       }
 #pragma unroll
-      for (int u = 0; u < kShellPerThread; u++) {
-        if (shDst[u] < 0) continue;
-        buf[shDst[u]] = shSrc[u] ? ldRaw<T>(shSrc[u] + (shHalf[u] ? (z >> 1) : z) * shStep[u]) : shConst[u];
-      }
+      for (int u = 0; u < NSH; u++)
+        if (shDst[u] >= 0) buf[shDst[u]] = sv[u];
+      if (z + 1 < bs) loadPlane(z + 1);
     }
     __syncthreads();
     float4 *o4 = reinterpret_cast<float4 *>(dst + hz * hs2);
@@ -328,6 +337,16 @@ float quantConst(int storage, float v) {
     case MSBG_GPU_F16: return __half2float(__float2half_rn(v));
     default: return v;
   }
+}
+
+template <int NSH>
+int launchFill(msbg_gpu_ctx *ctx, int storage, unsigned n, size_t smem, const HaloArgs &a) {
+  switch (storage) {
+    case MSBG_GPU_F32: MSBG_LAUNCH(ctx, (kFillHalo<float, NSH>), n, kHaloThreads, smem, a); break;
+    case MSBG_GPU_F16: MSBG_LAUNCH(ctx, (kFillHalo<__half, NSH>), n, kHaloThreads, smem, a); break;
+    default: MSBG_LAUNCH(ctx, (kFillHalo<uint16_t, NSH>), n, kHaloThreads, smem, a); break;
+  }
+  return MSBG_GPU_OK;
 }
 
 LevelChannels *levelChannels(msbg_gpu_ctx *ctx) {
@@ -460,11 +479,13 @@ extern "C" int msbg_gpu_fill_halo_blocks(msbg_gpu_ctx *ctx, int lchan, int level
   a.skipped = lc->dSkip;
   const size_t smem = 2 * sizeof(float) * (size_t)a.hs * a.hs;  // the plane double buffer (<= 12.8 KB)
   if (n > 0) {
-    switch (c.storage) {
-      case MSBG_GPU_F32: MSBG_LAUNCH(ctx, kFillHalo<float>, (unsigned)n, kHaloThreads, smem, a); break;
-      case MSBG_GPU_F16: MSBG_LAUNCH(ctx, kFillHalo<__half>, (unsigned)n, kHaloThreads, smem, a); break;
-      default: MSBG_LAUNCH(ctx, kFillHalo<uint16_t>, (unsigned)n, kHaloThreads, smem, a); break;
-    }
+    // shell positions of an interior plane per thread: 2h (hs + bs) <= 576 for bs <= 32, h <= 4
+    const int nsh = (2 * haloSize * (a.hs + bs) + kHaloThreads - 1) / kHaloThreads;
+    int rc = MSBG_GPU_OK;
+    if (nsh <= 1) rc = launchFill<1>(ctx, c.storage, (unsigned)n, smem, a);
+    else if (nsh == 2) rc = launchFill<2>(ctx, c.storage, (unsigned)n, smem, a);
+    else rc = launchFill<3>(ctx, c.storage, (unsigned)n, smem, a);
+    if (rc) return rc;
   }
   if (hSkipped) {
     unsigned long long s = 0;
