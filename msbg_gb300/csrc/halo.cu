@@ -128,7 +128,7 @@ __device__ __forceinline__ int nbIndex(int p, int o, int bs) { return p < o ? 0 
 
 constexpr int kHaloThreads = 256;
 
-template <typename T, int NSH>
+template <typename T>
 __global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
   __shared__ int32_t stL[27], stC[27];
   const int bid = a.bids[blockIdx.x];
@@ -198,111 +198,15 @@ __global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
   }
   // Plane by plane through a shared double buffer, so that every output plane (hs^2
   // floats, a multiple of 16 bytes at a 16-byte aligned offset) leaves in whole 16-byte
-  // stores and no DRAM sector is written in parts.  On the bs interior planes a
-  // position's source moves by a fixed step from plane to plane (one block plane at its
-  // level, or one coarse plane every second plane), so each thread resolves its interior
-  // quad and its shell positions once and then only adds that step; the 2h halo planes
-  // resolve position by position.
+  // stores and no DRAM sector is written in parts.  Interior rows of an interior plane
+  // come from the own block, 4 voxels per thread; the rest of the plane resolves per
+  // position.
   extern __shared__ __align__(16) float plane[];
   const int hs2 = hs * hs;
-  const int msk = bs - 1, mskC = bsC - 1;
-  // interior quad of this thread (bs^2/4 <= 256 quads: at most one per thread)
-  const int nQuad = bs * bs / 4;
-  const bool hasQuad = (int)threadIdx.x < nQuad;
   const int32_t own = stL[13];
-  const T *quadSrc = nullptr;
-  float quadConst = own == MSBG_GPU_LBLK_EMPTY ? a.lv.emptyF : a.lv.fullF;
-  int quadDst = 0;
-  if (hasQuad) {
-    const int xq = threadIdx.x & ((bs >> 2) - 1), y = threadIdx.x >> (L - 2);
-    if (own >= 0) quadSrc = (const T *)a.lv.pay + (int64_t)own * bs * bs * bs + y * bs + 4 * xq;
-    quadDst = (y + h) * hs + h + 4 * xq;
-  }
-  // shell positions of the interior planes: up to NSH per thread
+  const T *blk = own >= 0 ? (const T *)a.lv.pay + (int64_t)own * bs * bs * bs : nullptr;
+  const float cOwn = own == MSBG_GPU_LBLK_EMPTY ? a.lv.emptyF : a.lv.fullF;
   const int nShell = 2 * h * hs + 2 * h * bs;  // halo rows, then halo columns of the block rows
-  const T *shSrc[NSH];
-  float shConst[NSH];
-  int shStep[NSH], shDst[NSH];
-  bool shHalf[NSH];
-#pragma unroll
-  for (int u = 0; u < NSH; u++) {
-    const int j = threadIdx.x + u * kHaloThreads;
-    shSrc[u] = nullptr;
-    shConst[u] = 0.0f;
-    shStep[u] = 0;
-    shHalf[u] = false;
-    shDst[u] = -1;
-    if (j >= nShell) continue;
-    int hx, hy;
-    if (j < 2 * h * hs) {
-      const int r = (int)__umulhi((uint32_t)j, a.hsMagic);
-      hx = j - r * hs;
-      hy = r < h ? r : r + bs;
-    } else {  // 2h halo columns on each of the bs block rows
-      const int jj = j - 2 * h * hs, yb = jj / (2 * h), xx = jj - yb * 2 * h;
-      hy = h + yb;
-      hx = xx < h ? xx : xx + bs;
-    }
-    shDst[u] = hy * hs + hx;
-    // the source at interior plane z = 0 (resolve's rule with pz inside the domain)
-    int px = ox + hx - h, py = oy + hy - h;
-    const bool inRange = px >= 0 && py >= 0 && px < a.sx && py < a.sy;
-    int n = nbIndex(px, ox, bs) + 3 * nbIndex(py, oy, bs) + 9;
-    int32_t st = inRange ? stL[n] : MSBG_GPU_LBLK_NONE;
-    const HaloLevel *lvp = &a.lv;
-    bool coarseRead = false;
-    if (st == MSBG_GPU_LBLK_NONE) {
-      if (neumann) {
-        px = min(max(px, ox), ox + msk);
-        py = min(max(py, oy), oy + msk);
-        st = own;
-      } else if (coarse) {
-        if (!inRange) {
-          px = min(max(px, 0), a.sx - 1);
-          py = min(max(py, 0), a.sy - 1);
-          n = nbIndex(px, ox, bs) + 3 * nbIndex(py, oy, bs) + 9;
-          st = stL[n];
-        }
-        if (st == MSBG_GPU_LBLK_NONE) {
-          st = stC[n];
-          lvp = &a.lo;
-          coarseRead = true;
-          if (st == MSBG_GPU_LBLK_NONE) {
-            st = MSBG_GPU_LBLK_EMPTY;  // no block at level+1 either: the level's empty value
-            lvp = &a.lv;
-          }
-        }
-      } else {
-        st = MSBG_GPU_LBLK_EMPTY;
-      }
-    }
-    if (st >= 0) {
-      if (coarseRead) {
-        shSrc[u] = (const T *)lvp->pay + (int64_t)st * bsC * bsC * bsC + ((py >> 1) & mskC) * bsC + ((px >> 1) & mskC);
-        shStep[u] = bsC * bsC;
-        shHalf[u] = true;
-      } else {
-        shSrc[u] = (const T *)lvp->pay + (int64_t)st * bs * bs * bs + (py & msk) * bs + (px & msk);
-        shStep[u] = bs * bs;
-      }
-    } else {
-      shConst[u] = st == MSBG_GPU_LBLK_EMPTY ? lvp->emptyF : lvp->fullF;
-    }
-  }
-  // this thread's values of one interior plane, loaded one plane ahead of their use so
-  // that the loads of plane z+1 are in flight across plane z's barrier and stores
-  float qv[4], sv[NSH];
-  auto loadPlane = [&](int z) {
-    if (hasQuad) {
-      if (quadSrc) load4<T>(quadSrc + z * bs * bs, qv);
-      else qv[0] = qv[1] = qv[2] = qv[3] = quadConst;
-    }
-#pragma unroll
-    for (int u = 0; u < NSH; u++)
-      if (shDst[u] >= 0)
-        sv[u] = shSrc[u] ? ldRaw<T>(shSrc[u] + (shHalf[u] ? (z >> 1) : z) * shStep[u]) : shConst[u];
-  };
-  loadPlane(0);
   for (int hz = 0; hz < hs; hz++) {
     float *buf = plane + (hz & 1) * hs2;
     const int z = hz - h;
@@ -312,14 +216,27 @@ __global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
         buf[i] = value(i - hy * hs, hy, hz);
       }
     } else {
-      if (hasQuad) {
-        float *o = buf + quadDst;
-        o[0] = qv[0]; o[1] = qv[1]; o[2] = qv[2]; o[3] = qv[3];
+      for (int k = threadIdx.x; k < bs * bs / 4; k += kHaloThreads) {
+        const int xq = k & ((bs >> 2) - 1), y = k >> (L - 2);
+        float v[4];
+        if (blk) load4<T>(blk + (z * bs + y) * bs + 4 * xq, v);
+        else v[0] = v[1] = v[2] = v[3] = cOwn;
+        float *o = buf + (y + h) * hs + h + 4 * xq;
+        o[0] = v[0]; o[1] = v[1]; o[2] = v[2]; o[3] = v[3];
       }
-#pragma unroll
-      for (int u = 0; u < NSH; u++)
-        if (shDst[u] >= 0) buf[shDst[u]] = sv[u];
-      if (z + 1 < bs) loadPlane(z + 1);
+      for (int j = threadIdx.x; j < nShell; j += kHaloThreads) {
+        int hx, hy;
+        if (j < 2 * h * hs) {
+          const int r = (int)__umulhi((uint32_t)j, a.hsMagic);
+          hx = j - r * hs;
+          hy = r < h ? r : r + bs;
+        } else {  // 2h halo columns on each of the bs block rows
+          const int jj = j - 2 * h * hs, yb = jj / (2 * h), xx = jj - yb * 2 * h;
+          hy = h + yb;
+          hx = xx < h ? xx : xx + bs;
+        }
+        buf[hy * hs + hx] = value(hx, hy, hz);
+      }
     }
     __syncthreads();
     float4 *o4 = reinterpret_cast<float4 *>(dst + hz * hs2);
@@ -337,16 +254,6 @@ float quantConst(int storage, float v) {
     case MSBG_GPU_F16: return __half2float(__float2half_rn(v));
     default: return v;
   }
-}
-
-template <int NSH>
-int launchFill(msbg_gpu_ctx *ctx, int storage, unsigned n, size_t smem, const HaloArgs &a) {
-  switch (storage) {
-    case MSBG_GPU_F32: MSBG_LAUNCH(ctx, (kFillHalo<float, NSH>), n, kHaloThreads, smem, a); break;
-    case MSBG_GPU_F16: MSBG_LAUNCH(ctx, (kFillHalo<__half, NSH>), n, kHaloThreads, smem, a); break;
-    default: MSBG_LAUNCH(ctx, (kFillHalo<uint16_t, NSH>), n, kHaloThreads, smem, a); break;
-  }
-  return MSBG_GPU_OK;
 }
 
 LevelChannels *levelChannels(msbg_gpu_ctx *ctx) {
@@ -479,13 +386,11 @@ extern "C" int msbg_gpu_fill_halo_blocks(msbg_gpu_ctx *ctx, int lchan, int level
   a.skipped = lc->dSkip;
   const size_t smem = 2 * sizeof(float) * (size_t)a.hs * a.hs;  // the plane double buffer (<= 12.8 KB)
   if (n > 0) {
-    // shell positions of an interior plane per thread: 2h (hs + bs) <= 576 for bs <= 32, h <= 4
-    const int nsh = (2 * haloSize * (a.hs + bs) + kHaloThreads - 1) / kHaloThreads;
-    int rc = MSBG_GPU_OK;
-    if (nsh <= 1) rc = launchFill<1>(ctx, c.storage, (unsigned)n, smem, a);
-    else if (nsh == 2) rc = launchFill<2>(ctx, c.storage, (unsigned)n, smem, a);
-    else rc = launchFill<3>(ctx, c.storage, (unsigned)n, smem, a);
-    if (rc) return rc;
+    switch (c.storage) {
+      case MSBG_GPU_F32: MSBG_LAUNCH(ctx, kFillHalo<float>, (unsigned)n, kHaloThreads, smem, a); break;
+      case MSBG_GPU_F16: MSBG_LAUNCH(ctx, kFillHalo<__half>, (unsigned)n, kHaloThreads, smem, a); break;
+      default: MSBG_LAUNCH(ctx, kFillHalo<uint16_t>, (unsigned)n, kHaloThreads, smem, a); break;
+    }
   }
   if (hSkipped) {
     unsigned long long s = 0;
