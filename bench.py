@@ -431,9 +431,9 @@ def run_gpu(args, spec, dist: Dist):
     # value-block slab (states: slots, "no block" off level 0), level 1 the level-1
     # blocks.  Algorithmic bytes per block: the (bs+2)^3 box read once at S bytes per
     # value and written once as FP32.
-    halo = None
+    halo, bound = None, []
     if not args.no_jacobi:
-        halo = halo_measure(g, info, storage, elem, bsx, args.steps, dist, peaks)
+        halo = halo_measure(g, info, storage, elem, bsx, args.steps, dist, peaks, bound)
 
     # ray-march render of the iso-0.5 surface (RaymarchRenderer::render) of the swept field
     render = None
@@ -453,6 +453,8 @@ def run_gpu(args, spec, dist: Dist):
 
     d.free()
     g.close()
+    for b in bound:  # device arrays a level channel of g was bound to: free after g
+        b.free()
     poisson = None
     if not args.no_poisson and spec is W.SURFACE_4096:
         poisson = poisson_measure(96, max(1, min(args.steps, 3)), 1)
@@ -487,7 +489,7 @@ def run_gpu(args, spec, dist: Dist):
     print(json.dumps(line), flush=True)
 
 
-def halo_measure(g, info, storage, elem, bsx, steps, dist, peaks, batch=16384) -> dict:
+def halo_measure(g, info, storage, elem, bsx, steps, dist, peaks, bound: list, batch=16384) -> dict:
     lv = g.levels()
     slot = g.slots()
     st0 = np.where(lv == 0, slot, G.LBLK_NONE).astype(np.int32)
@@ -495,6 +497,7 @@ def halo_measure(g, info, storage, elem, bsx, steps, dist, peaks, batch=16384) -
     st1 = np.full(lv.size, G.LBLK_NONE, np.int32)
     st1[lv == 1] = np.arange(n1, dtype=np.int32)
     d_st0 = g.to_device(st0)
+    bound.append(d_st0)  # the context keeps this binding until it is destroyed
     g.level_grid_bind(0, 0, storage, d_st0.ptr, g.payload_ptr(0), 0.0, 1.0)
     g.level_grid_set(0, 1, storage, st1, np.zeros((max(n1, 1), (bsx // 2) ** 3), G.NP_STORAGE[storage]),
                      0.0, 1.0)
@@ -524,7 +527,6 @@ def halo_measure(g, info, storage, elem, bsx, steps, dist, peaks, batch=16384) -
     sk = g.fill_halo_blocks_device(0, 0, d_bids, nb, 1, G.BC_COARSE_LEVEL, d_out, count_skipped=True)
     d_out.free()
     d_bids.free()
-    d_st0.free()
     nbytes = len(bids) * hs ** 3 * (elem + 4)
     gbs = nbytes / (ms / 1e3) / 1e9
     return {"kernel": "kFillHalo (OPT_BC_COARSE_LEVEL, halo 1)", "blocks": int(len(bids)),
