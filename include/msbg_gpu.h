@@ -297,6 +297,17 @@ int msbg_gpu_level_grid_bind(msbg_gpu_ctx *ctx, int lchan, int level, int storag
 enum { MSBG_GPU_BC_NEUMANN = 1 << 10, MSBG_GPU_BC_COARSE_LEVEL = 1 << 26 };
 int msbg_gpu_fill_halo_blocks(msbg_gpu_ctx *ctx, int lchan, int level, const int32_t *dBids, int64_t n,
                               int haloSize, int opt, float *dOut, int64_t *hSkipped);
+/* downsampleFloatChannelNew (src/msbg4.cpp:1035-1379) for blocks of a multi-level channel,
+ * the step that restricts a block's data to the next coarser level (its ghost block,
+ * src/msbg.cpp:3110-3150): for each listed block (as for msbg_gpu_fill_halo_blocks, any
+ * level whose block edge is >= 2) dOut receives (bs/2)^3 floats [z][y][x], the 4^3
+ * Gauss-like weights (1,3,3,1)^3/512 (src/grid.c:30-70) over the fine cells 2v-1 .. 2v+2
+ * with the fine halo of fillHaloBlock_ with OPT_BC_COARSE_LEVEL, or with simpleAverage
+ * (OPT_SIMPLE_AVERAGE) the mean of the 8 children; summed in the reference's order as
+ * msbg_gpu_downsample_channel, which it equals on single-level layouts.  Skipped blocks
+ * leave their output as is.  Allocates scratch for the halo boxes and synchronizes. */
+int msbg_gpu_restrict_level_blocks(msbg_gpu_ctx *ctx, int lchan, int level, const int32_t *dBids, int64_t n,
+                                   int simpleAverage, float *dOut, int64_t *hSkipped);
 /* ---- ray-march render of the iso-0.5 surface -----------------------------------------
  * RDR::RaymarchRenderer (src/render.h:52-160): setCamera(pos, lookAt, zoom),
  * setSunLight(sun), setSurfaceColor(color), then render() (src/render.cpp:20-101), which the

@@ -245,6 +245,54 @@ __global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
   }
 }
 
+// Restriction of halo boxes ((bs+2)^3, halo 1) to (bs/2)^3 coarse values: the 4^3
+// Gauss-like weights (1,3,3,1)^3/512 (src/grid.c:30-70) in the reference's summation
+// order (per x offset i and row j, S[j][i] = fma(w, f, S[j][i]) over the 4 planes; then
+// T[i] = ((S0+S1)+S2)+S3 and (T0+T1)+(T2+T3)), or the 8-child mean.  One CTA per box,
+// one thread per coarse cell (strided); blocks the fill skipped are skipped here too.
+template <bool SIMPLE>
+__global__ void __launch_bounds__(256) kRestrictBoxes(const float *__restrict__ boxes, const int32_t *__restrict__ bids,
+                                                      const int32_t *__restrict__ levels,
+                                                      const int32_t *__restrict__ state, int level, int bs,
+                                                      float *__restrict__ out) {
+  const int bid = bids[blockIdx.x];
+  if (levels[bid] != level || state[bid] == MSBG_GPU_LBLK_NONE) return;
+  const int hs = bs + 2, cb = bs >> 1;
+  const float *b = boxes + (int64_t)blockIdx.x * hs * hs * hs;
+  float *o = out + (int64_t)blockIdx.x * cb * cb * cb;
+  auto at = [&](int x, int y, int z) { return b[((z + 1) * hs + (y + 1)) * hs + (x + 1)]; };
+  for (int c = threadIdx.x; c < cb * cb * cb; c += blockDim.x) {
+    const int vx = c % cb, vy = (c / cb) % cb, vz = c / (cb * cb);
+    const int x0 = 2 * vx, y0 = 2 * vy, z0 = 2 * vz;
+    float val;
+    if constexpr (SIMPLE) {
+      float sum = at(x0, y0, z0);
+#pragma unroll
+      for (int k = 1; k < 8; k++) sum = __fadd_rn(sum, at(x0 + (k & 1), y0 + ((k >> 1) & 1), z0 + (k >> 2)));
+      val = __fmul_rn(sum, 1.0f / 8.0f);
+    } else {
+      const float k1[4] = {1.f, 3.f, 3.f, 1.f};
+      float S[4][4];
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+#pragma unroll
+        for (int i = 0; i < 4; i++) S[j][i] = 0.0f;
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+#pragma unroll
+          for (int i = 0; i < 4; i++)
+            S[j][i] = __fmaf_rn(k1[k] * k1[j] * k1[i] / 512.f, at(x0 - 1 + i, y0 - 1 + j, z0 - 1 + k), S[j][i]);
+      float T[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) T[i] = __fadd_rn(__fadd_rn(__fadd_rn(S[0][i], S[1][i]), S[2][i]), S[3][i]);
+      val = __fadd_rn(__fadd_rn(T[0], T[1]), __fadd_rn(T[2], T[3]));
+    }
+    o[(vz * cb + vy) * cb + vx] = val;
+  }
+}
+
 float quantConst(int storage, float v) {
   switch (storage) {
     case MSBG_GPU_U16: {
@@ -399,4 +447,48 @@ extern "C" int msbg_gpu_fill_halo_blocks(msbg_gpu_ctx *ctx, int lchan, int level
     *hSkipped = (int64_t)s;
   }
   return MSBG_GPU_OK;
+}
+
+extern "C" int msbg_gpu_restrict_level_blocks(msbg_gpu_ctx *ctx, int lchan, int level, const int32_t *dBids,
+                                              int64_t n, int simpleAverage, float *dOut, int64_t *hSkipped) {
+  if (!ctx) return MSBG_GPU_ERR_ARG;
+  if (level < 0 || level >= ctx->nLevels || level >= kMaxGridLevels || (ctx->bsx >> level) < 2)
+    return fail(ctx, MSBG_GPU_ERR_ARG, "restrict_level: level %d out of range (block edge must be >= 2)", level);
+  if (n < 0 || n > 0x7fffffff || (n > 0 && (!dBids || !dOut)))
+    return fail(ctx, MSBG_GPU_ERR_ARG, "restrict_level: bad block list");
+  if (n == 0) {
+    if (hSkipped) *hSkipped = 0;
+    return MSBG_GPU_OK;
+  }
+  if (!ctx->levelCh || lchan < 0 || lchan >= kMaxLevelChannels || !ctx->levelCh->ch[lchan].lv[level].set)
+    return fail(ctx, MSBG_GPU_ERR_STATE, "restrict_level: level %d of level channel %d is not set", level, lchan);
+  const int bs = ctx->bsx >> level, hs = bs + 2, cb = bs / 2;
+  const int64_t box = (int64_t)hs * hs * hs, per = (int64_t)cb * cb * cb;
+  const int64_t batch = n < 4096 ? n : 4096;
+  float *boxes = nullptr;
+  MSBG_CUDA(ctx, cudaMalloc(&boxes, (size_t)(batch * box) * sizeof(float)));
+  int rc = MSBG_GPU_OK;
+  int64_t skipped = 0;
+  const int32_t *state = ctx->levelCh->ch[lchan].lv[level].state;
+  for (int64_t k0 = 0; k0 < n && !rc; k0 += batch) {
+    const int64_t m = n - k0 < batch ? n - k0 : batch;
+    int64_t sk = 0;
+    rc = msbg_gpu_fill_halo_blocks(ctx, lchan, level, dBids + k0, m, 1, MSBG_GPU_BC_COARSE_LEVEL, boxes,
+                                   hSkipped ? &sk : nullptr);
+    if (rc) break;
+    skipped += sk;
+    if (simpleAverage)
+      kRestrictBoxes<true><<<(unsigned)m, 256, 0, ctx->stream>>>(boxes, dBids + k0, ctx->dLevels, state, level, bs,
+                                                                  dOut + k0 * per);
+    else
+      kRestrictBoxes<false><<<(unsigned)m, 256, 0, ctx->stream>>>(boxes, dBids + k0, ctx->dLevels, state, level, bs,
+                                                                   dOut + k0 * per);
+    ctx->launches++;
+    if (cudaGetLastError() != cudaSuccess) rc = fail(ctx, MSBG_GPU_ERR_CUDA, "restrict_level: launch failed");
+  }
+  // the boxes are read by the kernels above: free only after them
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess && !rc) rc = fail(ctx, MSBG_GPU_ERR_CUDA, "restrict_level: sync");
+  cudaFree(boxes);
+  if (!rc && hSkipped) *hSkipped = skipped;
+  return rc;
 }

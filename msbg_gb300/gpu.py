@@ -103,6 +103,7 @@ SIGNATURES = {
     "msbg_gpu_save": (I, [P, C.c_char_p, P, I]),
     "msbg_gpu_load": (I, [C.POINTER(P), C.c_char_p]),
     "msbg_gpu_fill_halo_blocks": (I, [P, I, I, P, I64, I, I, P, C.POINTER(I64)]),
+    "msbg_gpu_restrict_level_blocks": (I, [P, I, I, P, I64, I, P, C.POINTER(I64)]),
     "msbg_gpu_diag_wait_timeout": (I, [P, I]),
     "msbg_gpu_vcycle": (I, [P, I, I]),
     "msbg_gpu_dot": (I, [P, I, I, C.POINTER(D)]),
@@ -557,6 +558,26 @@ class MultiresSparseGrid:
         finally:
             d.free()
         return out
+
+    def restrict_level_blocks(self, lchan: int, level: int, bids: np.ndarray, simple_average: bool = False):
+        """downsampleFloatChannelNew for blocks of a level channel (cross-resolution halo):
+        (float32 [n][(bs/2)^3], skipped count)."""
+        bids = np.ascontiguousarray(bids, np.int32)
+        cb = (self.bsx >> max(level, 0)) // 2
+        out = np.empty((len(bids), max(cb, 1) ** 3), np.float32)
+        db = self.to_device(bids)
+        do = DeviceBuffer.alloc(max(out.nbytes, 4))
+        sk = C.c_int64(-1)
+        try:
+            self._check(self.L.msbg_gpu_restrict_level_blocks(self.h, lchan, level, C.c_void_p(db.ptr), len(bids),
+                                                              int(simple_average), C.c_void_p(do.ptr), C.byref(sk)))
+            if len(bids):
+                self._check(self.L.msbg_gpu_copy_d2h(self.h, _ptr(out), C.c_void_p(do.ptr), out.nbytes))
+            self.synchronize()
+        finally:
+            db.free()
+            do.free()
+        return out, int(sk.value)
 
     def dotProdChannel(self, a: int, b: int) -> float:
         out = C.c_double()

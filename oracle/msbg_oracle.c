@@ -1459,3 +1459,53 @@ void orc_sort_blocks_morton(int nbx, int nby, int nbz, int32_t *bids, int64_t n)
   for (int64_t i = 0; i < n; i++) bids[i] = k[i].bid;
   free(k);
 }
+
+/* ---- restriction of multi-level blocks (src/msbg4.cpp:1035-1379) ---- */
+
+int64_t orc_restrict_level(const orc_grid *g, int nLevels, const int32_t *levels,
+                           const orc_level_grid *lg, int level, const int32_t *bids, int64_t nBids,
+                           int simpleAverage, float *out) {
+  const int bs = g->bsx >> level, cb = bs / 2, hs = bs + 2;
+  const int64_t box = (int64_t)hs * hs * hs, per = (int64_t)cb * cb * cb;
+  float *boxes = (float *)malloc(sizeof(float) * (size_t)(nBids > 0 ? nBids : 1) * (size_t)box);
+  const int64_t skipped = orc_fill_halo(g, nLevels, levels, lg, level, bids, nBids, 1, ORC_BC_COARSE_LEVEL, boxes);
+  const float k1[4] = {1.f, 3.f, 3.f, 1.f};
+  float w[4][4][4];
+  for (int k = 0; k < 4; k++)
+    for (int j = 0; j < 4; j++)
+      for (int i = 0; i < 4; i++) w[k][j][i] = k1[k] * k1[j] * k1[i] / 512.f;
+#pragma omp parallel for schedule(static)
+  for (int64_t t = 0; t < nBids; t++) {
+    const int32_t bid = bids[t];
+    if (levels[bid] != level || lg[level].state[bid] == ORC_LBLK_NONE) continue;
+    const float *b = boxes + t * box;
+    /* fine cell (x, y, z) of the block, -1 .. bs */
+#define BOX(x, y, z) b[((int64_t)((z) + 1) * hs + ((y) + 1)) * hs + ((x) + 1)]
+    for (int vz = 0; vz < cb; vz++)
+      for (int vy = 0; vy < cb; vy++)
+        for (int vx = 0; vx < cb; vx++) {
+          const int x0 = 2 * vx, y0 = 2 * vy, z0 = 2 * vz;
+          float val;
+          if (simpleAverage) {
+            float sum = 0.f;
+            for (int c = 0; c < 8; c++) {
+              const float f = BOX(x0 + (c & 1), y0 + ((c >> 1) & 1), z0 + (c >> 2));
+              sum = c == 0 ? f : sum + f;
+            }
+            val = sum * (1.f / 8.f);
+          } else {
+            float S[4][4] = {{0.f}};
+            for (int k = 0; k < 4; k++)
+              for (int j = 0; j < 4; j++)
+                for (int i = 0; i < 4; i++) S[j][i] = fmaf(w[k][j][i], BOX(x0 - 1 + i, y0 - 1 + j, z0 - 1 + k), S[j][i]);
+            float T[4];
+            for (int i = 0; i < 4; i++) T[i] = ((S[0][i] + S[1][i]) + S[2][i]) + S[3][i];
+            val = (T[0] + T[1]) + (T[2] + T[3]);
+          }
+          out[t * per + ((int64_t)vz * cb + vy) * cb + vx] = val;
+        }
+#undef BOX
+  }
+  free(boxes);
+  return skipped;
+}

@@ -202,6 +202,16 @@ void orc_render(const orc_grid *g, const int32_t *slot, const void *payload, int
 uint64_t orc_morton64(uint32_t x, uint32_t y, uint32_t z);
 void orc_sort_blocks_morton(int nbx, int nby, int nbz, int32_t *bids, int64_t n);
 
+/* Restriction of blocks of a multi-level channel: downsampleFloatChannelNew
+ * (src/msbg4.cpp:1035-1379) for each listed block at `level`: the (bs/2)^3 coarse values
+ * of the block, from its fine halo box of orc_fill_halo with halo 1 and
+ * ORC_BC_COARSE_LEVEL (the cross-resolution rule), with orc_downsample's weights and
+ * summation order (or the 8-child mean).  out: [nBids][(bs/2)^3].  Returns the number of
+ * skipped blocks (their output is left as is). */
+int64_t orc_restrict_level(const orc_grid *g, int nLevels, const int32_t *levels,
+                           const orc_level_grid *lg, int level, const int32_t *bids, int64_t nBids,
+                           int simpleAverage, float *out);
+
 /* ---- conversions (exposed for tests) ---- */
 uint16_t orc_f32_to_f16(float f);
 float orc_f16_to_f32(uint16_t h);

@@ -75,6 +75,9 @@ def lib():
                                     C.c_int, C.c_uint, P]
         L.orc_fill_halo.restype = C.c_int64
         L.orc_render.argtypes = [C.POINTER(Grid), P, P, C.c_int, C.c_int, C.c_void_p, C.c_int, P]
+        L.orc_restrict_level.argtypes = [C.POINTER(Grid), C.c_int, P, C.c_void_p, C.c_int, P, C.c_int64,
+                                         C.c_int, P]
+        L.orc_restrict_level.restype = C.c_int64
         L.orc_sort_blocks_morton.argtypes = [C.c_int, C.c_int, C.c_int, P, C.c_int64]
         L.orc_morton64.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32]
         L.orc_morton64.restype = C.c_uint64
@@ -201,6 +204,27 @@ def fill_halo(g: Grid, levels, states: list, payloads: list, level: int, bids, h
     skipped = lib().orc_fill_halo(C.byref(g), n_levels, _p(levels), C.cast(lgs, C.c_void_p), level,
                                   _p(bids), len(bids),
                                   halo, opt, _p(out))
+    return out, int(skipped)
+
+
+def restrict_level(g: Grid, levels, states: list, payloads: list, level: int, bids,
+                   simple_average: bool = False, empty_value: float = 0.0, full_value: float = 1.0):
+    """downsampleFloatChannelNew restated for blocks of a multi-level channel (cross-resolution
+    halo): float32 [len(bids)][(bs/2)^3] and the number of skipped blocks."""
+    n_levels = len(states)
+    levels = np.ascontiguousarray(levels, np.int32)
+    keep = []
+    lgs = (LevelGrid * n_levels)()
+    for l in range(n_levels):
+        st = np.ascontiguousarray(states[l], np.int32)
+        pay = np.ascontiguousarray(payloads[l]) if payloads[l] is not None else np.zeros(1, np.float32)
+        keep += [st, pay]
+        lgs[l] = LevelGrid(st.ctypes.data, pay.ctypes.data, empty_value, full_value)
+    bids = np.ascontiguousarray(bids, np.int32)
+    cb = (g.bsx >> level) // 2
+    out = np.zeros((len(bids), cb ** 3), np.float32)
+    skipped = lib().orc_restrict_level(C.byref(g), n_levels, _p(levels), C.cast(lgs, C.c_void_p), level,
+                                       _p(bids), len(bids), int(simple_average), _p(out))
     return out, int(skipped)
 
 

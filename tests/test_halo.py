@@ -220,3 +220,79 @@ def test_gpu_fill_halo_skips_and_errors(gpulib, port):
         assert g.L.msbg_gpu_fill_halo_blocks(g.h, 0, 0, None, 0, 1, 0, None, None) == G.OK
     finally:
         g.close()
+
+
+# ---------------------------------------------------------------- restriction with the halo
+
+def test_restrict_level_restatement_equals_value_block_restriction(port):
+    """On a single-level layout (value blocks at level 0, every other block the constant empty
+    block) the multi-level restriction is downsampleFloatChannelNew's value-block case."""
+    rng = np.random.default_rng(3)
+    res, bs = 96, 16
+    nb3 = (res // bs) ** 3
+    bids = np.nonzero(rng.random(nb3) < 0.5)[0].astype(np.int32)
+    pay = rng.standard_normal((len(bids), bs ** 3)).astype(np.float32)
+    slot = np.full(nb3, H.LBLK_EMPTY, np.int32)
+    slot[bids] = np.arange(len(bids), dtype=np.int32)
+    lv = np.full(nb3, 1, np.int32)
+    lv[bids] = 0
+    g = port.grid(res, res, res, bs, port.F32)
+    for simple in (False, True):
+        out, sk = port.restrict_level(g, lv, [slot, np.full(nb3, H.LBLK_NONE, np.int32)], [pay, None], 0, bids,
+                                      simple)
+        assert sk == 0
+        assert _same(out, port.downsample(g, slot, bids, pay, simple)), simple
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["f32", "f16", "u16"])
+def test_gpu_restrict_level_matches_restatement(gpulib, port, kind):
+    G = gpulib
+    storage = {"f32": G.F32, "f16": G.F16, "u16": G.U16}[kind]
+    for bsx in (16, 32):
+        nb, nl = (7, 6, 8), 3
+        lv, st, pay = H.halo_case(nb, bsx, nl, 7300 + bsx + len(kind), kind, _reg(port))
+        g = _gpu_grid(G, nb, bsx, nl, lv, st, pay, storage, 0.125, 0.875)
+        try:
+            og = port.grid(nb[0] * bsx, nb[1] * bsx, nb[2] * bsx, bsx, _port_storage(port, kind))
+            hp = _host(pay)
+            for L in range(nl):
+                bids = H.blocks_at(lv, st, L)
+                for simple in (False, True):
+                    out, sk = g.restrict_level_blocks(0, L, bids, simple)
+                    ref, _ = port.restrict_level(og, lv, st, hp, L, bids, simple, 0.125, 0.875)
+                    assert sk == 0
+                    assert _same(out, ref), (kind, bsx, L, simple, int((out != ref).sum()))
+        finally:
+            g.close()
+
+
+@pytest.mark.gpu
+def test_gpu_restrict_level_equals_downsample_channel(gpulib):
+    """Level 0 of a level channel bound to the value-block slab: the multi-level restriction
+    equals msbg_gpu_downsample_channel bit for bit."""
+    G = gpulib
+    rng = np.random.default_rng(11)
+    res, bs = 128, 16
+    nb3 = (res // bs) ** 3
+    bids = np.nonzero(rng.random(nb3) < 0.4)[0].astype(np.int32)
+    pay = rng.standard_normal((len(bids), bs ** 3)).astype(np.float16)
+    g = G.MultiresSparseGrid(res, res, res, bs, 2, G.F16)
+    try:
+        levels = np.full(nb3, 1, np.int32)
+        levels[bids] = 0
+        g.set_levels(levels)
+        g.setRefinementMap(0.0)
+        g.upload_payload(pay, 0)
+        d_st = g.to_device(g.slots())  # -1 = the constant empty block, as in the value-block layout
+        try:
+            g.level_grid_bind(0, 0, G.F16, d_st.ptr, g.payload_ptr(0), 0.0, 1.0)
+            g.level_grid_set(0, 1, G.F16, np.full(nb3, H.LBLK_NONE, np.int32), None)
+            for simple in (False, True):
+                out, _ = g.restrict_level_blocks(0, 0, g.active_blocks(), simple)
+                assert _same(out, g.downsampleFloatChannelNew(0, simple)), simple
+        finally:
+            g.close()
+            d_st.free()
+    finally:
+        g.close()
