@@ -28,6 +28,27 @@
 
 namespace msbg {
 
+// Four consecutive values of a block row as floats (one 8- or 16-byte load; x is a
+// multiple of 4), converted as Store<T>::load does.
+template <typename T> __device__ __forceinline__ void ldQuad(const T *p, float v[4]);
+template <> __device__ __forceinline__ void ldQuad<float>(const float *p, float v[4]) {
+  const float4 q = *reinterpret_cast<const float4 *>(p);
+  v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+}
+template <> __device__ __forceinline__ void ldQuad<__half>(const __half *p, float v[4]) {
+  const uint2 q = *reinterpret_cast<const uint2 *>(p);
+  const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&q.x));
+  const float2 hi = __half22float2(*reinterpret_cast<const __half2 *>(&q.y));
+  v[0] = lo.x; v[1] = lo.y; v[2] = hi.x; v[3] = hi.y;
+}
+template <> __device__ __forceinline__ void ldQuad<uint16_t>(const uint16_t *p, float v[4]) {
+  const uint2 q = *reinterpret_cast<const uint2 *>(p);
+  v[0] = __fmul_rn((float)(q.x & 0xffffu), kU16ToF);
+  v[1] = __fmul_rn((float)(q.x >> 16), kU16ToF);
+  v[2] = __fmul_rn((float)(q.y & 0xffffu), kU16ToF);
+  v[3] = __fmul_rn((float)(q.y >> 16), kU16ToF);
+}
+
 template <int BS>
 constexpr int dsThreads() {
   return (BS / 2) * (BS / 2) < 32 ? 32 : (BS / 2) * (BS / 2);
@@ -71,11 +92,7 @@ __global__ void __launch_bounds__(dsThreads<BS>(), 4) kDownsample(const T *__res
     if (tid < NI) {
       const int sc = nbs[nz + 3];  // the block above / below (or the own block)
       v.in[0] = v.in[1] = v.in[2] = v.in[3] = 0.0f;
-      if (sc >= 0) {
-        const T *q = pay + ((int64_t)sc << (3 * L)) + zoff + 4 * tid;
-#pragma unroll
-        for (int k = 0; k < 4; k++) v.in[k] = Store<T>::load(q + k);
-      }
+      if (sc >= 0) ldQuad<T>(pay + ((int64_t)sc << (3 * L)) + zoff + 4 * tid, v.in);
     }
 #pragma unroll
     for (int k = 0; k < PR; k++) {
@@ -130,7 +147,9 @@ __global__ void __launch_bounds__(dsThreads<BS>(), 4) kDownsample(const T *__res
   // (2vz+1, 2vz+2) completes them (k = 2, 3) and starts those of plane vz+1.  The
   // next pair's loads are in flight while a pair is used.
   float acc[4][4], part = 0.0f;  // acc[j][i] over k = 0, 1; part: the children sum in plane 2vz
-  Plane va, vb;
+  // Fine-plane pairs go through two register sets (A: pairs of even coarse planes, B:
+  // odd), so the loads of the next two pairs are in flight while a pair is used.
+  Plane va, vb, vc, vd;
   fetch(-1, va);
   fetch(0, vb);
   put(-1, va);
@@ -138,6 +157,8 @@ __global__ void __launch_bounds__(dsThreads<BS>(), 4) kDownsample(const T *__res
   __syncthreads();
   fetch(1, va);
   fetch(2, vb);
+  fetch(3, vc);
+  fetch(4, vd);
   if (own) {
 #pragma unroll
     for (int j = 0; j < 4; j++) {
@@ -151,18 +172,18 @@ __global__ void __launch_bounds__(dsThreads<BS>(), 4) kDownsample(const T *__res
       if (SIMPLE && j == 2) part = __fadd_rn(__fadd_rn(part, r1[1]), r1[2]);
     }
   }
-#pragma unroll 1
-  for (int vz = 0; vz < CB; vz++) {
+  // one coarse plane from the pair (p, q) of fine planes 2vz+1, 2vz+2
+  auto step = [&](int vz, Plane &p, Plane &q) {
     // the pair's ring slots are not the previous pair's, whose last reads were
     // before the previous barrier
-    put(2 * vz + 1, va);
-    put(2 * vz + 2, vb);
+    put(2 * vz + 1, p);
+    put(2 * vz + 2, q);
     __syncthreads();
-    if (vz + 1 < CB) {
-      fetch(2 * vz + 3, va);
-      fetch(2 * vz + 4, vb);
+    if (vz + 2 < CB) {  // the pair after next into the registers just emptied
+      fetch(2 * vz + 5, p);
+      fetch(2 * vz + 6, q);
     }
-    if (!own) continue;
+    if (!own) return;
     float T4[4], sum = part, npart = 0.0f;
 #pragma unroll
     for (int j = 0; j < 4; j++) {
@@ -185,6 +206,12 @@ __global__ void __launch_bounds__(dsThreads<BS>(), 4) kDownsample(const T *__res
     const float val = SIMPLE ? __fmul_rn(sum, 0.125f)
                              : __fadd_rn(__fadd_rn(T4[0], T4[1]), __fadd_rn(T4[2], T4[3]));
     out[(int64_t)t * CB * CB * CB + ((int64_t)vz * CB + vy) * CB + vx] = val;
+  };
+  static_assert(CB % 2 == 0, "coarse planes in pairs");
+#pragma unroll 1
+  for (int vz = 0; vz < CB; vz += 2) {
+    step(vz, va, vb);
+    step(vz + 1, vc, vd);
   }
 }
 
