@@ -213,7 +213,8 @@ using namespace msbg;
 extern "C" int msbg_gpu_render(msbg_gpu_ctx *ctx, int chan, int width, int height, const msbg_gpu_camera *cam,
                                uint8_t *dRGB) {
   if (!ctx) return MSBG_GPU_ERR_ARG;
-  if (width <= 0 || height <= 0 || (int64_t)width * height > ((int64_t)1 << 31) || !cam || !dRGB)
+  if (width <= 0 || height <= 0 || height > 65535 * 8 || (int64_t)width * height > ((int64_t)1 << 31) || !cam ||
+      !dRGB)
     return fail(ctx, MSBG_GPU_ERR_ARG, "render: bad image size or null argument");
   if (chan < 0 || chan >= kMaxChannels || !ctx->ch[chan].exists)
     return fail(ctx, MSBG_GPU_ERR_ARG, "channel %d does not exist", chan);
