@@ -261,6 +261,20 @@ def test_full_size_surface512_matches_restatement(gpulib, port):
     assert len(r["bids"]) > 1000
 
 
+def test_full_size_surface512_fp64_matches_restatement(gpulib, port):
+    """The FP64 GPU path that the bench's field-error figure is measured against, at the
+    512^3 workload's full size (FP64 storage and arithmetic, 4 MCF iterations, EXACT
+    variant): bit for bit against the CPU FP64 restatement."""
+    spec = W.SURFACE_512
+    pts = W.make_points(spec, 1)
+    r = _gpu_pipeline(gpulib, pts, spec["res"], spec["bsx"], gpulib.F64, 4, MCF8, spec["dt"],
+                      variant=gpulib.SWEEP_EXACT)
+    p = port.surface_pipeline(pts, spec["res"], spec["bsx"], storage=port.F64, n_iter=4, dt=spec["dt"])
+    assert np.array_equal(r["bids"], p.active_bids)
+    assert np.array_equal(_as_bits(r["final"]), _as_bits(p.after_finalize))
+    assert np.array_equal(_as_bits(r["pde"]), _as_bits(p.after_pde))
+
+
 def test_full_size_surface4096_layout_and_splat_match_restatement(gpulib, port):
     """The 4096^3 three-level FP16 workload at full size (1,024 clusters x 32,000
     points, bands 8 / 16 voxels): levels, flags, active set, particle counters and the
