@@ -129,7 +129,7 @@ __device__ __forceinline__ int nbIndex(int p, int o, int bs) { return p < o ? 0 
 constexpr int kHaloThreads = 256;
 
 template <typename T>
-__global__ void __launch_bounds__(kHaloThreads) kFillHalo(HaloArgs a) {
+__global__ void __launch_bounds__(kHaloThreads, 8) kFillHalo(HaloArgs a) {
   __shared__ int32_t stL[27], stC[27];
   const int bid = a.bids[blockIdx.x];
   const int64_t nxy = (int64_t)a.nbx * a.nby;
