@@ -48,8 +48,8 @@ from msbg_gb300 import workloads as W  # noqa: E402
 OPT8 = 1 << 29
 MCF8 = -(4 + OPT8)
 JAC8 = -(17 + OPT8)  # Jacobi diffusion (phi + dt sum f_i) / (1 + 6 dt), 8-colour in place
-# DRAM bytes (read + write) of one sweep launch of the 4096^3 workload, from the ncu
-# capture summarised in profiles/sweep_mcf_surface4096.md (mean of 8 launches)
+# DRAM bytes (read + write) of one sweep launch of the 4096^3 workload, from an ncu
+# capture of the sweep kernel on this workload (mean of 8 launches)
 SWEEP_TRAFFIC_4096 = 2.63e9
 
 
@@ -232,17 +232,19 @@ def run_reference(args, spec, dist: Dist):
         vals = vals[args.warmup:]
         desc = (f"reference applyChannelPdeFast<uint16> MCF, 4 iterations over the level-0 blocks of "
                 f"the workload's points inside a {res}^3 crop")
+        dtype = "u16 storage / f32 math"
     else:
         for i in range(args.warmup + args.steps):
             v, desc, threads = cpu_sample(spec, pts, target_sec=8.0)
             vals.append(v)
         vals = vals[args.warmup:]
         desc = "reference CPU path unavailable on this host (x86 SIMD); " + desc
+        dtype = "f16 storage / f32 math" if spec["storage"] == "f16" else "f32"
     value = float(np.median(vals))
     line = {
         "impl": "reference", "metric": "voxel-updates/s (MCF sweeps)", "value": value,
         "unit": "voxel-updates/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+        "higher_is_better": True, "dtype": dtype, "data": "synthetic",
         "config": {"workload": spec["name"]},
         "cpu_baseline": {"value": value, "unit": "voxel-updates/s", "cores": threads, "kind": kind,
                          "sample": desc},

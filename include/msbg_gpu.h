@@ -444,7 +444,11 @@ int msbg_gpu_warmnet_train_step(msbg_gpu_ctx *ctx, const float *dB, const float 
  * MSBG_GPU_NOALLOC_MAX_BLOCKS; larger maps return MSBG_GPU_ERR_CAPACITY.
  * The first call on a device looks the array's address up: make that call
  * before any stream capture.  All calls share the array, so calls whose kernels
- * may overlap on the GPU (unordered streams) race; order them on one stream. */
+ * may overlap on the GPU (unordered streams) race; order them on one stream.
+ * The call does not synchronize: its status covers the arguments and the launches
+ * only (MSBG_GPU_ERR_CUDA also when the runtime already holds an error from earlier
+ * work, which it then leaves unread); a fault while the kernels run shows up on the
+ * caller's stream, so check that stream (cudaStreamSynchronize) before using dSlot. */
 #define MSBG_GPU_NOALLOC_MAX_BLOCKS ((int64_t)1 << 24)
 int msbg_gpu_assign_slots_noalloc(const int32_t *dLevels, int64_t nBlocks, int32_t *dSlot,
                                   int32_t *dActiveBids, int64_t *dCount, void *cudaStream);

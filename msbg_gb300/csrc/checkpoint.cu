@@ -64,9 +64,12 @@ extern "C" int msbg_gpu_save(msbg_gpu_ctx *ctx, const char *path, const int *cha
   if (!ctx) return MSBG_GPU_ERR_ARG;
   if (!path || nChans < 0 || (nChans > 0 && !chans)) return fail(ctx, MSBG_GPU_ERR_ARG, "save: bad arguments");
   if (!ctx->layoutValid) return fail(ctx, MSBG_GPU_ERR_STATE, "save: no block layout");
-  for (int i = 0; i < nChans; i++)
+  for (int i = 0; i < nChans; i++) {
     if (chans[i] < 0 || chans[i] >= kMaxChannels || !ctx->ch[chans[i]].exists || !ctx->ch[chans[i]].d)
       return fail(ctx, MSBG_GPU_ERR_ARG, "save: channel %d does not exist", chans[i]);
+    for (int j = 0; j < i; j++)
+      if (chans[j] == chans[i]) return fail(ctx, MSBG_GPU_ERR_ARG, "save: channel %d listed twice", chans[i]);
+  }
   std::vector<int8_t> levels((size_t)ctx->nBlocks);
   int rc = msbg_gpu_get_levels(ctx, levels.data());
   if (rc) return rc;
@@ -140,14 +143,19 @@ extern "C" int msbg_gpu_load(msbg_gpu_ctx **out, const char *path) {
     // channels first, so that the layout sizes their slabs
     std::vector<ChanRecord> recs;
     const long dataPos = ftell(f.f);
+    bool seen[kMaxChannels] = {};
     for (int i = 0; i < h.nChans && !rc; i++) {
       ChanRecord r;
-      if (fread(&r, sizeof(r), 1, f.f) != 1 || r.chan < 0 || r.chan >= kMaxChannels || r.storage < 0 ||
-          r.storage > 3 || r.bytes != h.nActive * ctx->voxPerBlock * (int64_t)storageBytes(r.storage) ||
+      // a channel may appear once: a second record would size the slab by its own
+      // storage type while the first record's bytes were also copied into it
+      if (fread(&r, sizeof(r), 1, f.f) != 1 || r.chan < 0 || r.chan >= kMaxChannels || seen[r.chan] ||
+          r.storage < 0 || r.storage > 3 ||
+          r.bytes != h.nActive * ctx->voxPerBlock * (int64_t)storageBytes(r.storage) ||
           fseek(f.f, (long)r.bytes, SEEK_CUR)) {
         rc = MSBG_GPU_ERR_IO;
         break;
       }
+      seen[r.chan] = true;
       recs.push_back(r);
       rc = msbg_gpu_channel_create(ctx, r.chan, r.storage);
     }
@@ -160,8 +168,15 @@ extern "C" int msbg_gpu_load(msbg_gpu_ctx **out, const char *path) {
     for (const ChanRecord &r0 : recs) {
       ChanRecord r;
       if (fread(&r, sizeof(r), 1, f.f) != 1 || r.chan != r0.chan) { rc = MSBG_GPU_ERR_IO; break; }
+      const Channel &dc = ctx->ch[r.chan];
+      // the slab must hold exactly this record's bytes in the channel's current type
+      if (!dc.exists || !dc.d || dc.storage != r.storage || dc.capBlocks < (size_t)h.nActive ||
+          r.bytes != (int64_t)h.nActive * ctx->voxPerBlock * (int64_t)storageBytes(dc.storage)) {
+        rc = MSBG_GPU_ERR_IO;
+        break;
+      }
       uint64_t hash = kFnvBasis;
-      char *dst = (char *)ctx->ch[r.chan].d;
+      char *dst = (char *)dc.d;
       for (int64_t off = 0; off < r.bytes && !rc; off += (int64_t)kStage) {
         const size_t n = (size_t)((r.bytes - off) < (int64_t)kStage ? (r.bytes - off) : (int64_t)kStage);
         if (fread(st.p, 1, n, f.f) != n) { rc = MSBG_GPU_ERR_IO; break; }

@@ -317,11 +317,16 @@ __global__ void kColorFlags(const int32_t *__restrict__ active, int64_t nAct, in
   out[i] = blockColor8(bx, by, bz) == color;
 }
 
+// The colour's list starts after the lists of the lower colours, whose lengths the
+// earlier scans left in colTot[0..color-1] on the device.
 __global__ void kColorScatter(const int32_t *__restrict__ active, const int32_t *__restrict__ flag,
-                              const int64_t *__restrict__ off, int64_t nAct, int32_t base,
-                              int32_t *__restrict__ colorBids) {
+                              const int64_t *__restrict__ off, int64_t nAct, const int64_t *__restrict__ colTot,
+                              int color, int32_t *__restrict__ colorBids) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < nAct && flag[i]) colorBids[base + off[i]] = active[i];
+  if (i >= nAct || !flag[i]) return;
+  int64_t base = 0;
+  for (int c = 0; c < color; c++) base += colTot[c];
+  colorBids[base + off[i]] = active[i];
 }
 
 }  // namespace msbg
@@ -380,13 +385,13 @@ extern "C" int msbg_gpu_create(msbg_gpu_ctx **out, int sx, int sy, int sz, int b
   ALLOC(ctx->dActive, nB * 4);
   ALLOC(ctx->dColorBids, nB * 4);
   ALLOC(ctx->dScanPartial, (size_t)nPart * 8);
-  ALLOC(ctx->dCounters, 16 * 8);
+  ALLOC(ctx->dCounters, kNumCounters * 8);
   ALLOC(ctx->dStatus, 16);
 #undef ALLOC
-  if (e == cudaSuccess) e = cudaMallocHost((void **)&ctx->hCounters, 16 * 8);
+  if (e == cudaSuccess) e = cudaMallocHost((void **)&ctx->hCounters, kNumCounters * 8);
   for (int i = 0; i < kMaxEvents && e == cudaSuccess; i++) e = cudaEventCreate(&ctx->ev[i]);
   if (e == cudaSuccess) e = cudaMemset(ctx->dMark, 0, nB * 4);
-  if (e == cudaSuccess) e = cudaMemset(ctx->dCounters, 0, 16 * 8);
+  if (e == cudaSuccess) e = cudaMemset(ctx->dCounters, 0, kNumCounters * 8);
   if (e == cudaSuccess) e = cudaMemset(ctx->dStatus, 0, 16);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e != cudaSuccess) {
@@ -547,7 +552,7 @@ extern "C" int msbg_gpu_set_refinement_map(msbg_gpu_ctx *ctx, double fillValue) 
   if (rc) return rc;
   MSBG_LAUNCH(ctx, kAssignSlots, gridFor(nB, 256), 256, 0, ctx->dLevels, dOff, nB, ctx->dSlot,
               ctx->dActive);
-  MSBG_CUDA(ctx, cudaMemcpyAsync(ctx->hCounters, dCnt, 16 * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  MSBG_CUDA(ctx, cudaMemcpyAsync(ctx->hCounters, dCnt, 16 * 8, cudaMemcpyDeviceToHost, ctx->stream));  // 0..15
   MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   const int64_t nAct = ctx->hCounters[2];
   for (int l = 0; l < 8; l++) ctx->blocksPerLevel[l] = ctx->hCounters[4 + l];
@@ -555,21 +560,28 @@ extern "C" int msbg_gpu_set_refinement_map(msbg_gpu_ctx *ctx, double fillValue) 
   if (nAct > ctx->capacityLimit)
     return fail(ctx, MSBG_GPU_ERR_CAPACITY, "%lld value blocks exceed the pool capacity %lld",
                 (long long)nAct, (long long)ctx->capacityLimit);
-  // 8-color lists: stable compaction of the active list per color
+  // 8-color lists: stable compaction of the active list per color; each colour's
+  // length stays on the device (counters kColorTot..+7), where the next colours'
+  // scatters read their start, and all eight are read back once.
   int32_t *dFlag = ctx->dLevelsTmp;
+  int64_t *dColTot = dCnt + kColorTot;
+  if (nAct > 0) {
+    for (int c = 0; c < 8; c++) {
+      MSBG_LAUNCH(ctx, kColorFlags, gridFor(nAct, 256), 256, 0, ctx->dActive, nAct, ctx->nbx, ctx->nby,
+                  c, dFlag);
+      rc = exclusiveScanFlags(ctx, dFlag, nAct, dOff, dColTot + c);
+      if (rc) return rc;
+      MSBG_LAUNCH(ctx, kColorScatter, gridFor(nAct, 256), 256, 0, ctx->dActive, dFlag, dOff, nAct, dColTot,
+                  c, ctx->dColorBids);
+    }
+    MSBG_CUDA(ctx, cudaMemcpyAsync(ctx->hCounters + kColorTot, dColTot, 8 * 8, cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+    MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
   int32_t base = 0;
   for (int c = 0; c < 8; c++) {
     ctx->colorStart[c] = base;
-    if (nAct == 0) continue;
-    MSBG_LAUNCH(ctx, kColorFlags, gridFor(nAct, 256), 256, 0, ctx->dActive, nAct, ctx->nbx, ctx->nby,
-                c, dFlag);
-    rc = exclusiveScanFlags(ctx, dFlag, nAct, dOff, dCnt + 3);
-    if (rc) return rc;
-    MSBG_LAUNCH(ctx, kColorScatter, gridFor(nAct, 256), 256, 0, ctx->dActive, dFlag, dOff, nAct, base,
-                ctx->dColorBids);
-    MSBG_CUDA(ctx, cudaMemcpyAsync(ctx->hCounters + 3, dCnt + 3, 8, cudaMemcpyDeviceToHost, ctx->stream));
-    MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    base += (int32_t)ctx->hCounters[3];
+    if (nAct > 0) base += (int32_t)ctx->hCounters[kColorTot + c];
   }
   ctx->colorStart[8] = base;
   ctx->nActive = nAct;

@@ -21,6 +21,11 @@ void levelChannelsFree(LevelChannels *lc);
 void warmNetFree(WarmNetState *w);
 void batchFree(BatchState *b);
 constexpr int kMaxChannels = 64;
+// device counters of a context (int64): 0 nActParticles, 1 nAborted, 2 nActive,
+// 3 scratch, 4..11 blocks per level (5, 6 reused as scan totals by the solver),
+// 16..23 value blocks per 8-colour class
+constexpr int kColorTot = 16;
+constexpr int kNumCounters = 32;
 constexpr int kMaxEvents = 16;
 
 struct Channel {
@@ -54,7 +59,7 @@ struct msbg_gpu_ctx {
   int32_t *dActive = nullptr;    // [nBlocks] ascending bids of value blocks
   int32_t *dColorBids = nullptr; // [nBlocks] value blocks grouped by 8-color class
   int64_t *dScanPartial = nullptr; // scan scratch
-  int64_t *dCounters = nullptr;  // [8]: 0 nActParticles, 1 nAborted, 2 nActive, 3.. color counts
+  int64_t *dCounters = nullptr;  // [kNumCounters], see kColorTot
   int64_t *hCounters = nullptr;  // pinned mirror
   int *dStatus = nullptr;        // device-side error bits (bounded waits that gave up)
   bool layoutValid = false;

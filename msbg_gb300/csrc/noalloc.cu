@@ -148,6 +148,9 @@ extern "C" int msbg_gpu_assign_slots_noalloc(const int32_t *dLevels, int64_t nBl
   int64_t *part = nullptr;
   const int rc = scratchFor(dev, &part);
   if (rc != MSBG_GPU_OK) return rc;
+  // An error that earlier, unrelated work left in the runtime is not this call's:
+  // report it without launching and leave it for its owner to read.
+  if (cudaPeekAtLastError() != cudaSuccess) return MSBG_GPU_ERR_CUDA;
   cudaStream_t st = (cudaStream_t)cudaStream;
   const int64_t nTiles = (nBlocks + kTile - 1) / kTile;
   if (nTiles > 0) kTileCounts<<<(unsigned)nTiles, kThreads, 0, st>>>(dLevels, nBlocks, part);

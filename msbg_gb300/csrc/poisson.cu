@@ -968,6 +968,9 @@ extern "C" int msbg_gpu_mgpcg_solve(msbg_gpu_ctx *ctx, int chanX, int chanB, dou
   if ((rc = applyT<float>(ctx, ps, ps->f32, 0, x, b, r, 1))) return rc;
   double rr0, bb;
   if ((rc = trueResidual(ctx, ps, x, b, &rr0, &bb))) return rc;
+  // a NaN or Inf in B or in the start X makes the first residual non-finite
+  if (!isfinite(rr0) || !isfinite(bb))
+    return fail(ctx, MSBG_GPU_ERR_DIVERGED, "initial residual is not finite (B or X holds NaN/Inf)");
   const double bnorm = sqrt(bb);
   double rel = bnorm > 0 ? sqrt(rr0) / bnorm : 0.0;
   int it = 0;

@@ -126,3 +126,42 @@ def test_gpu_checkpoint_errors(gpulib, tmp_path):
         assert e.value.code == G.ERR_IO
     finally:
         g.close()
+
+
+def _two_record_file(G, recs) -> bytes:
+    """A 32^3 grid of 16^3 blocks with two value blocks, and the given (chan, storage, payload)
+    records, each with a correct checksum."""
+    levels = np.array([0, 1, 2, 0, 1, 2, 2, 2], np.int8)
+    blob = struct.pack("<8sII6i2qQ", b"MSBGCKP1", 1, 64, 32, 32, 32, 16, 3, len(recs), 8, 2,
+                       _fnv(levels.tobytes()))
+    blob += levels.tobytes()
+    for chan, storage, pay in recs:
+        blob += struct.pack("<iiqQ", chan, storage, len(pay), _fnv(pay)) + pay
+    return blob
+
+
+@pytest.mark.gpu
+def test_gpu_checkpoint_rejects_a_repeated_channel(gpulib, tmp_path):
+    """A file that holds two records for one channel (here FP32 and then FP16 for channel 0,
+    each consistent with its own storage type) is refused with MSBG_GPU_ERR_IO; copying both
+    would write the FP32 record's bytes into a slab sized for FP16.  The same file with the
+    records on two channels loads, and save refuses a channel listed twice."""
+    G = gpulib
+    p32 = np.arange(2 * 16 ** 3, dtype=np.float32).tobytes()
+    p16 = np.arange(2 * 16 ** 3, dtype=np.float16).tobytes()
+    bad = tmp_path / "dup.msbg"
+    bad.write_bytes(_two_record_file(G, [(0, G.F32, p32), (0, G.F16, p16)]))
+    with pytest.raises(G.MsbgGpuError) as e:
+        G.MultiresSparseGrid.load(str(bad))
+    assert e.value.code == G.ERR_IO
+    good = tmp_path / "two.msbg"
+    good.write_bytes(_two_record_file(G, [(0, G.F32, p32), (1, G.F16, p16)]))
+    h = G.MultiresSparseGrid.load(str(good))
+    try:
+        assert h.info().nActive == 2
+        assert h.payload(0).tobytes() == p32 and h.payload(1).tobytes() == p16
+        with pytest.raises(G.MsbgGpuError) as e:
+            h.save(str(tmp_path / "again.msbg"), (0, 1, 0))
+        assert e.value.code == G.ERR_ARG
+    finally:
+        h.close()

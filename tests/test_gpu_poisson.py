@@ -185,3 +185,59 @@ def test_mixed_precision_warm_start_and_zero_rhs(setup):
     g.mgpcg_solve(CH_X, CH_B, tol=5e-7, max_iter=100)
     outer, inner, rel = g.mgpcg_solve_mixed(CH_X, CH_B, tol=1e-6)
     assert outer == 0 and inner == 0 and rel <= 1e-6
+
+
+def test_nonfinite_rhs_is_reported_not_solved(setup):
+    """A NaN entering from the host (here in B, and then in the start X) ends both solves with
+    MSBG_GPU_ERR_DIVERGED instead of a result; the context keeps working afterwards."""
+    G, P, g, prob = setup
+    rng = np.random.default_rng(9)
+    b = _rand(prob, rng).astype(np.float32)
+    pb = prob.payload(b)
+    bad = pb.copy()
+    bad[len(bad) // 2, 17] = np.nan
+    g.upload_payload(bad, CH_B)
+    g.fill(0.0, CH_X)
+    for solve in (lambda: g.mgpcg_solve(CH_X, CH_B, tol=1e-6, max_iter=50),
+                  lambda: g.mgpcg_solve_mixed(CH_X, CH_B, tol=1e-6)):
+        with pytest.raises(G.MsbgGpuError) as e:
+            solve()
+        assert e.value.code == G.ERR_DIVERGED
+    g.upload_payload(pb, CH_B)
+    x0 = np.zeros_like(pb)
+    x0[0, 3] = np.inf
+    g.upload_payload(x0, CH_X)
+    with pytest.raises(G.MsbgGpuError) as e:
+        g.mgpcg_solve(CH_X, CH_B, tol=1e-6, max_iter=50)
+    assert e.value.code == G.ERR_DIVERGED
+    g.fill(0.0, CH_X)
+    it, rel = g.mgpcg_solve(CH_X, CH_B, tol=1e-6, max_iter=100)
+    assert rel <= 1e-6 and it > 0
+
+
+def test_non_spd_coefficients_diverge(gpulib, port):
+    """A host-built coefficient set whose diagonal is the negated sum of the face
+    coefficients (a negative definite operator) is refused with MSBG_GPU_ERR_DIVERGED, at the
+    latest by the solve; nothing faults."""
+    G, P = gpulib, port
+    g, prob = _layout(G, P, res=64, bs=8)
+    try:
+        d = g.payload(CH_D)
+        g.upload_payload(-d, CH_D)
+        with pytest.raises(G.MsbgGpuError) as e:
+            g.poisson_set_coefficients(CH_CX, CH_CY, CH_CZ, CH_D)
+            rng = np.random.default_rng(10)
+            g.upload_payload(prob.payload(_rand(prob, rng).astype(np.float32)), CH_B)
+            g.fill(0.0, CH_X)
+            g.mgpcg_solve(CH_X, CH_B, tol=1e-6, max_iter=200)
+        assert e.value.code == G.ERR_DIVERGED
+        # a valid set on the same context solves again
+        g.upload_payload(d, CH_D)
+        g.poisson_set_coefficients(CH_CX, CH_CY, CH_CZ, CH_D)
+        rng = np.random.default_rng(11)
+        g.upload_payload(prob.payload(_rand(prob, rng).astype(np.float32)), CH_B)
+        g.fill(0.0, CH_X)
+        it, rel = g.mgpcg_solve(CH_X, CH_B, tol=1e-6, max_iter=100)
+        assert rel <= 1e-6
+    finally:
+        g.close()

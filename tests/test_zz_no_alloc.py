@@ -60,10 +60,53 @@ def test_noalloc_slots_match_set_refinement_map(gpulib):
             assert int(cnt[0]) == len(want_act) == int((lv == 0).sum())
             assert np.array_equal(slot, want_slot)
             assert np.array_equal(act[: int(cnt[0])], want_act)
+        # an empty map launches only the offsets kernel, which writes a count of 0
+        junk = np.array([12345], np.int64)
+        assert L.msbg_gpu_copy_h2d(h, d_cnt, junk.ctypes.data_as(C.c_void_p), 8) == 0
+        assert L.msbg_gpu_synchronize(h) == 0
+        assert L.msbg_gpu_assign_slots_noalloc(d_lv, 0, d_slot, d_act, d_cnt, None) == 0
+        cnt = np.ones(1, np.int64)
+        assert L.msbg_gpu_copy_d2h(h, cnt.ctypes.data_as(C.c_void_p), d_cnt, 8) == 0
+        assert int(cnt[0]) == 0
         # oversized maps are refused before any launch
         too_big = G.load_library().msbg_gpu_assign_slots_noalloc(
             d_lv, (1 << 24) + 1, d_slot, d_act, d_cnt, None)
         assert too_big == G.ERR_CAPACITY
+    finally:
+        for p in (d_lv, d_slot, d_act, d_cnt):
+            L.msbg_gpu_device_free(p)
+        L.msbg_gpu_destroy(h)
+
+
+def test_noalloc_slots_beyond_one_offset_chunk(gpulib):
+    """About 2.2 M blocks: more than 512 scan tiles of 4,096 blocks, so the single-CTA
+    offsets kernel carries its running total from one 512-tile chunk to the next.  The
+    expectation comes from numpy: slots from the cumulative count of level-0 blocks and
+    the active list from their indices."""
+    G = gpulib
+    L = G.load_library()
+    n = 2_200_000
+    rng = np.random.Generator(np.random.PCG64(20261203 + 78))
+    lv = np.where(rng.random(n) < 0.2, 0, 1).astype(np.int32)
+    want_act = np.flatnonzero(lv == 0).astype(np.int32)
+    want_slot = np.where(lv == 0, np.cumsum(lv == 0) - 1, -1).astype(np.int32)
+    h = C.c_void_p()
+    assert L.msbg_gpu_create(C.byref(h), 64, 64, 64, 16, 3, G.F32, 0) == 0
+    d_lv, d_slot, d_act, d_cnt = (_dev(L, n * 4), _dev(L, n * 4), _dev(L, n * 4), _dev(L, 8))
+    try:
+        assert L.msbg_gpu_copy_h2d(h, d_lv, lv.ctypes.data_as(C.c_void_p), lv.nbytes) == 0
+        assert L.msbg_gpu_synchronize(h) == 0
+        for _ in range(2):
+            assert L.msbg_gpu_assign_slots_noalloc(d_lv, n, d_slot, d_act, d_cnt, None) == 0
+            cnt = np.zeros(1, np.int64)
+            slot = np.empty(n, np.int32)
+            assert L.msbg_gpu_copy_d2h(h, cnt.ctypes.data_as(C.c_void_p), d_cnt, 8) == 0
+            assert L.msbg_gpu_copy_d2h(h, slot.ctypes.data_as(C.c_void_p), d_slot, n * 4) == 0
+            act = np.empty(len(want_act), np.int32)
+            assert L.msbg_gpu_copy_d2h(h, act.ctypes.data_as(C.c_void_p), d_act, act.nbytes) == 0
+            assert int(cnt[0]) == len(want_act)
+            assert np.array_equal(slot, want_slot)
+            assert np.array_equal(act, want_act)
     finally:
         for p in (d_lv, d_slot, d_act, d_cnt):
             L.msbg_gpu_device_free(p)
