@@ -292,7 +292,7 @@ def run_gpu(args, spec, dist: Dist):
     updates_per_step = vox * (n_iter + (n_iter & 1))
 
     for _ in range(args.warmup):
-        g.applyChannelPdeFast(0, MCF8, 1, n_iter, spec["dt"], 0.0, variant)
+        g.applyChannelPdeFast(0, laplTyp=MCF8, doConstrZeroOne=1, numIter=n_iter, timeStep=spec["dt"], variant=variant)
     g.synchronize()
     dist.barrier()
     clocks = ClockSampler(dist.local)
@@ -300,7 +300,7 @@ def run_gpu(args, spec, dist: Dist):
     l0 = g.launch_count()
     g.event_record(0)
     for _ in range(args.steps):
-        g.applyChannelPdeFast(0, MCF8, 1, n_iter, spec["dt"], 0.0, variant)
+        g.applyChannelPdeFast(0, laplTyp=MCF8, doConstrZeroOne=1, numIter=n_iter, timeStep=spec["dt"], variant=variant)
     g.event_record(1)
     g.synchronize()
     ms = g.event_elapsed_ms(0, 1)
@@ -326,12 +326,12 @@ def run_gpu(args, spec, dist: Dist):
     jacobi = None
     if not args.no_jacobi:
         for _ in range(max(1, args.warmup)):
-            g.applyChannelPdeFast(0, JAC8, 1, n_iter, spec["dt"], 0.0, variant)
+            g.applyChannelPdeFast(0, laplTyp=JAC8, doConstrZeroOne=1, numIter=n_iter, timeStep=spec["dt"], variant=variant)
         g.synchronize()
         lj = g.launch_count()
         g.event_record(2)
         for _ in range(args.steps):
-            g.applyChannelPdeFast(0, JAC8, 1, n_iter, spec["dt"], 0.0, variant)
+            g.applyChannelPdeFast(0, laplTyp=JAC8, doConstrZeroOne=1, numIter=n_iter, timeStep=spec["dt"], variant=variant)
         g.event_record(3)
         g.synchronize()
         msj = dist.max(g.event_elapsed_ms(2, 3))
@@ -549,7 +549,7 @@ def fp64_field_error(g, d_pts, n, spec, bands, variant, chunk=4096) -> dict:
     g.setRefinementMap(1.0)
     g.splat(d_pts, n, 2.0, 2.0)
     g.splat_finalize(2.0, 2.0)
-    g.applyChannelPdeFast(0, MCF8, 1, n_iter, spec["dt"], 0.0, variant)
+    g.applyChannelPdeFast(0, laplTyp=MCF8, doConstrZeroOne=1, numIter=n_iter, timeStep=spec["dt"], variant=variant)
     g.synchronize()
     g64 = G.MultiresSparseGrid(res, res, res, bsx, spec["n_levels"], G.F64)
     try:
@@ -563,7 +563,7 @@ def fp64_field_error(g, d_pts, n, spec, bands, variant, chunk=4096) -> dict:
         g64.splat(d_pts, n, 2.0, 2.0)
         g64.splat_finalize(2.0, 2.0)
         t1 = time.perf_counter()
-        g64.applyChannelPdeFast(0, MCF8, 1, n_iter, spec["dt"], 0.0, G.SWEEP_EXACT)
+        g64.applyChannelPdeFast(0, laplTyp=MCF8, doConstrZeroOne=1, numIter=n_iter, timeStep=spec["dt"], variant=G.SWEEP_EXACT)
         g64.synchronize()
         t64 = time.perf_counter() - t1
         same_layout = bool(np.array_equal(g.active_blocks(), g64.active_blocks()))

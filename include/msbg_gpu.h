@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define MSBG_GPU_ABI_VERSION 1
+#define MSBG_GPU_ABI_VERSION 2
 
 /* ---- status codes ---------------------------------------------------------- */
 enum {
@@ -158,16 +158,36 @@ int msbg_gpu_splat(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rParti
                    float nbDist);
 int msbg_gpu_splat_finalize(msbg_gpu_ctx *ctx, float rParticle, float nbDist);
 
+/* ---- block lists ------------------------------------------------------------------
+ * The reference's solver and sweep calls take `std::vector<int> *blockList` (NULL = all
+ * blocks).  Here a block list is dBlockList (device, nBlockList block ids; NULL = all
+ * value blocks).  Listed blocks without payload are skipped, as the reference skips
+ * BLK_NO_FLUID blocks; an id outside the block grid returns MSBG_GPU_ERR_ARG.  A call
+ * with a list synchronizes once to size its launches. */
+
 /* ---- stencil sweeps -------------------------------------------------------------
- * applyChannelPdeFast<T> (src/msbg.h:2150-2172, src/msbg4.cpp:60-957) over all
- * value blocks of channel `chan`: laplTyp < 0 updates in place with 8 colors
- * (with MSBG_GPU_OPT_8_COLOR_SCHEME) or red-black, laplTyp > 0 ping-pongs with a
- * temporary slab.  Kernels 4 (mean curvature), 17 (Jacobi diffusion),
- * 15/14 (Perona-Malik, anisAlpha > 0), 3 (simple diffusion), 1 (Laplacian).
- * numIter is rounded up to even, as the reference does.  Halo: OPT_BC_NEUMANN. */
-int msbg_gpu_apply_channel_pde_fast(msbg_gpu_ctx *ctx, int chan, int laplTyp, int doConstrZeroOne,
-                                    int numIter, float timeStep, float anisDiffAlpha,
-                                    int variant);
+ * applyChannelPdeFast<T>(chPhi, chTmp, chTmp2, blockList, laplTyp, doConstrZeroOne,
+ * densThr, densThrTol1, densThrTol2, numIter, gridSpacing, timeStep, velMagThr, msbgVel,
+ * lambda, lambdaSDF, taubinStrength, redist, anisDiffAlpha, veldep_on, veldep_fit, visOpt)
+ * (src/msbg.h:2150-2172, src/msbg4.cpp:60-957), argument for argument, plus the kernel
+ * variant.  Updates channel chPhi on the listed value blocks (all with a NULL list):
+ * laplTyp < 0 in place with 8 colors (with MSBG_GPU_OPT_8_COLOR_SCHEME) or red-black,
+ * laplTyp > 0 ping-pong through the library's own scratch (chTmp, chTmp2 are accepted and
+ * not used; unlisted blocks keep their values).  Kernels 4 (mean curvature), 17 (Jacobi
+ * diffusion), 15/14 (Perona-Malik, anisDiffAlpha > 0), 3 (simple diffusion), 1
+ * (Laplacian).  numIter is rounded up to even, as the reference does.  Halo:
+ * OPT_BC_NEUMANN.  gridSpacing must be 1 (the reference asserts it); lambda and lambdaSDF
+ * have no effect (the reference sets lambda to 0 itself); visOpt and veldepFit are
+ * ignored.  MSBG_GPU_ERR_UNSUPPORTED: negative numIter (the compressed-range mode), densThr
+ * or its tolerances > 0, velMagThr != 0, msbgVel != NULL, veldepOn, taubinStrength != 0,
+ * redist > 0. */
+int msbg_gpu_apply_channel_pde_fast(msbg_gpu_ctx *ctx, int chPhi, int chTmp, int chTmp2,
+                                    const int32_t *dBlockList, int64_t nBlockList, int laplTyp,
+                                    int doConstrZeroOne, float densThr, float densThrTol1,
+                                    float densThrTol2, int numIter, float gridSpacing, float timeStep,
+                                    float velMagThr, const void *msbgVel, float lambda, float lambdaSDF,
+                                    float taubinStrength, float redist, float anisDiffAlpha, int veldepOn,
+                                    const float *veldepFit, int visOpt, int variant);
 
 /* ---- whole surface job with host buffers (end-to-end entry point) --------------
  * Upload n points (host, float xyz), build the layout (marks with rScan =
@@ -194,14 +214,39 @@ int msbg_gpu_poisson_set_coefficients(msbg_gpu_ctx *ctx, int chanCx, int chanCy,
  * seed); copies them into the given FP32 channels when they are >= 0. */
 int msbg_gpu_poisson_procedural_coefficients(msbg_gpu_ctx *ctx, uint32_t seed, int chanCx,
                                              int chanCy, int chanCz, int chanDiag);
-/* multiplyLaplacianMatrixOpt (src/msbg.h:3167-3176): Y = A X, or Y = B - A X. */
-int msbg_gpu_multiply_laplacian(msbg_gpu_ctx *ctx, int chanX, int chanB, int chanDstY,
-                                int calcResidual);
-/* relax (src/msbg.h:3269-3277): nIter smoothing passes of A X = B on the finest
- * level, red-black over tiles with in-tile red-black Gauss-Seidel (the multigrid
- * smoother below); reverseOrder runs the adjoint order (tile colour 1 first, black
- * cells first). */
-int msbg_gpu_relax(msbg_gpu_ctx *ctx, int chanX, int chanB, int nIter, int reverseOrder);
+/* multiplyLaplacianMatrixOpt(options, levelMg, chanX, chanB, kap, chanDstY, pDotprod,
+ * blockList) (src/msbg.h:3167-3176, src/msbg3.cpp:1756-1912): Y = A X on the listed value
+ * blocks, or with MSBG_GPU_OPT_CALC_RESIDUAL Y = B - A X.  pDotprod (host, may be NULL;
+ * not with the residual, as the reference asserts) receives sum(Y X) in FP64 and makes the
+ * call synchronize.  levelMg must be 0 (the value blocks); kap is unused, as in the
+ * reference's sparse-level path.  The reference's operator is h ((1/D) X - sum W X_nb) with
+ * D = 1/diagonal stored in CH_DIAGONAL, the face areas W and h = 1 at level 0; here the
+ * diagonal itself is stored, which differs from 1/(1/d) by rounding only. */
+#define MSBG_GPU_OPT_CALC_RESIDUAL (1u << 12) /* OPT_CALC_RESIDUAL (src/msbg.h:115) */
+int msbg_gpu_multiply_laplacian(msbg_gpu_ctx *ctx, unsigned options, int levelMg, int chanX, int chanB,
+                                float kap, int chanDstY, double *pDotprod, const int32_t *dBlockList,
+                                int64_t nBlockList);
+/* relax(boundaryZoneOnly, reverseOrder, levelMg, chanX, chanB, chanTmp, nIter, options)
+ * (src/msbg.h:3269-3277, src/msbg3.cpp:2244-2369): nIter passes of the reference's block
+ * smoother on A X = B, in place: each pass relaxes the blocks of parity (bx+by+bz)&1 = 1,
+ * then 0 (0 then 1 with reverseOrder), each block with its face-neighbour halo taken at its
+ * start and _mgSmBlockIter block-local weighted Gauss-Seidel iterations
+ *   X = omega (B + sum W X_nb) / d + (1 - omega) X
+ * over groups of 8 x-consecutive cells (the reference's SIMD width), alternating sweep
+ * direction, the last iteration a Jacobi step (src/msbg3.cpp:1108-1332).  omega = 6/7 and
+ * 5 block iterations (src/msbg.cpp:814-843) unless msbg_gpu_set_relax_params changes them.
+ * The reference relaxes its member list _blocksRelax[levelMg], which nothing in the
+ * release fills; dBlockList stands in for it.  With options MSBG_GPU_RELAX_TILES the call
+ * runs the multigrid's own smoother instead (red-black over tiles with in-tile red-black
+ * Gauss-Seidel, all value blocks, no list; reverseOrder = the adjoint order).  levelMg must
+ * be 0; boundaryZoneOnly != 0 is MSBG_GPU_ERR_UNSUPPORTED; chanTmp is unused, as in the
+ * reference's in-place block order. */
+#define MSBG_GPU_RELAX_TILES (1u << 31) /* a bit the reference's option enum leaves unused */
+int msbg_gpu_relax(msbg_gpu_ctx *ctx, int boundaryZoneOnly, int reverseOrder, int levelMg, int chanX, int chanB,
+                   int chanTmp, int nIter, unsigned options, const int32_t *dBlockList, int64_t nBlockList);
+/* The block smoother's weight and block-local iterations (_mgSmOmega, _mgSmBlockIter,
+ * src/msbg.cpp:814-843; the reference reads the latter from psConf->ps_mg_sm_block_iter). */
+int msbg_gpu_set_relax_params(msbg_gpu_ctx *ctx, float omega, int blockIter);
 /* Diagnostics of the failure path: one CTA waits on an mbarrier that nothing completes,
  * with the same bounded try-wait loop as the library's kernels but a limit of `polls`
  * (1..1<<20).  The kernel records the expired wait in the device status word and returns;
@@ -353,14 +398,21 @@ int msbg_gpu_save(msbg_gpu_ctx *ctx, const char *path, const int *chans, int nCh
 int msbg_gpu_load(msbg_gpu_ctx **ctx, const char *path);
 /* One multigrid V-cycle X = M^{-1} B from X = 0 (the CG preconditioner). */
 int msbg_gpu_vcycle(msbg_gpu_ctx *ctx, int chanX, int chanB);
-/* dotProdChannel (src/msbg.h:3331-3341): FP64-accumulated sum; MSBG_GPU_ERR_NONFINITE
- * when the sum is not finite (src/msbg.cpp:4635-4642).  Synchronizes. */
-int msbg_gpu_dot(msbg_gpu_ctx *ctx, int chanA, int chanB, double *out);
-/* AXPBYChannel (src/msbg.h:3356-3362): Y = a X + b Y. */
-int msbg_gpu_axpby(msbg_gpu_ctx *ctx, double a, int chanX, double b, int chanY);
-/* AXPBYChannelCombined (src/msbg.h:3364-3368): X += a P; P = Q + b P. */
-int msbg_gpu_axpby_combined(msbg_gpu_ctx *ctx, double a, double b, int chanQ, int chanX,
-                            int chanP);
+/* dotProdChannel(ch1, ch2, levelMg, blockList, pErrCode) (src/msbg.h:3331-3341): the
+ * FP64-accumulated sum over the listed value blocks into *out; the reference's pErrCode is
+ * the return code, MSBG_GPU_ERR_NONFINITE when the sum is not finite
+ * (src/msbg.cpp:4635-4642).  levelMg must be 0.  Synchronizes. */
+int msbg_gpu_dot(msbg_gpu_ctx *ctx, int chanA, int chanB, int levelMg, const int32_t *dBlockList,
+                 int64_t nBlockList, double *out);
+/* AXPBYChannel(a, iChanX, b, iChanDstY, levelMax, levelMg, blockList) (src/msbg.h:3356-3362):
+ * Y = a X + b Y on the listed value blocks (all of them are level 0, so levelMax < 0 selects
+ * none); levelMg must be 0. */
+int msbg_gpu_axpby(msbg_gpu_ctx *ctx, double a, int chanX, double b, int chanY, int levelMax, int levelMg,
+                   const int32_t *dBlockList, int64_t nBlockList);
+/* AXPBYChannelCombined(a, b, iChanQ, iChanX, iChanP, blockList) (src/msbg.h:3364-3368):
+ * X += a P; P = Q + b P on the listed value blocks. */
+int msbg_gpu_axpby_combined(msbg_gpu_ctx *ctx, double a, double b, int chanQ, int chanX, int chanP,
+                            const int32_t *dBlockList, int64_t nBlockList);
 /* Multigrid-preconditioned CG: solves A X = B from the given X until the FP64-checked
  * relative residual ||B - A X|| / ||B|| <= tol or maxIter iterations.  Returns
  * MSBG_GPU_ERR_DIVERGED when the residual becomes non-finite or keeps growing. */
@@ -384,6 +436,10 @@ int msbg_gpu_mgpcg_solve_mixed(msbg_gpu_ctx *ctx, int chanX, int chanB, double t
  * symmetric preconditioner. */
 int msbg_gpu_poisson_set_params(msbg_gpu_ctx *ctx, int preSweeps, int postSweeps, int tileIters,
                                 int coarsestIter);
+/* Frees the solver's level-0 work vectors (FP32: r, p, z, s, 16 B per cell; FP16: 12 B per
+ * cell) and the FP16 coefficient copies of the mixed solve; the next solve allocates what it
+ * needs again.  Lets a caller run the FP32 and the mixed solve on one large layout in turn. */
+int msbg_gpu_poisson_release_work(msbg_gpu_ctx *ctx);
 /* Multigrid levels of the current hierarchy and their cell counts. */
 int msbg_gpu_mg_info(msbg_gpu_ctx *ctx, int *nLevels, int64_t *cellsPerLevel, int cap);
 

@@ -323,6 +323,7 @@ extern "C" int msbg_gpu_batch_mgpcg_solve(msbg_gpu_ctx *ctx, int chanX, int chan
   if (rc) return rc;
   PoissonState *ps = ctx->poisson;
   if (!ps->coeffsValid) return fail(ctx, MSBG_GPU_ERR_STATE, "no Poisson coefficients set");
+  if ((rc = ensureF32Work(ctx, ps))) return rc;
   float *x, *b;
   if ((rc = chanF32b(ctx, chanX, &x)) || (rc = chanF32b(ctx, chanB, &b))) return rc;
   const int nV = bs->nVol;

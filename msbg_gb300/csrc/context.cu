@@ -409,6 +409,8 @@ extern "C" int msbg_gpu_destroy(msbg_gpu_ctx *ctx) {
   cudaStreamSynchronize(ctx->stream);
   cudaFree(ctx->dMark); cudaFree(ctx->dLevels); cudaFree(ctx->dLevelsTmp); cudaFree(ctx->dFlags);
   cudaFree(ctx->dSlot); cudaFree(ctx->dActive); cudaFree(ctx->dColorBids);
+  if (ctx->dListMark) cudaFree(ctx->dListMark);
+  if (ctx->dListBids) cudaFree(ctx->dListBids);
   cudaFree(ctx->dScanPartial); cudaFree(ctx->dCounters); cudaFree(ctx->dStatus);
   if (ctx->hCounters) cudaFreeHost(ctx->hCounters);
   for (auto &c : ctx->ch) {
@@ -738,13 +740,30 @@ extern "C" int msbg_gpu_splat_finalize(msbg_gpu_ctx *ctx, float rParticle, float
   return splatFinalizeRun(ctx, rParticle, nbDist);
 }
 
-extern "C" int msbg_gpu_apply_channel_pde_fast(msbg_gpu_ctx *ctx, int chan, int laplTyp,
-                                               int doConstrZeroOne, int numIter, float timeStep,
-                                               float anisDiffAlpha, int variant) {
-  if (!ctx || numIter < 0) return MSBG_GPU_ERR_ARG;
-  int rc = checkChan(ctx, chan);
+extern "C" int msbg_gpu_apply_channel_pde_fast(msbg_gpu_ctx *ctx, int chPhi, int chTmp, int chTmp2,
+                                               const int32_t *dBlockList, int64_t nBlockList, int laplTyp,
+                                               int doConstrZeroOne, float densThr, float densThrTol1,
+                                               float densThrTol2, int numIter, float gridSpacing, float timeStep,
+                                               float velMagThr, const void *msbgVel, float lambda,
+                                               float lambdaSDF, float taubinStrength, float redist,
+                                               float anisDiffAlpha, int veldepOn, const float *veldepFit,
+                                               int visOpt, int variant) {
+  (void)chTmp; (void)chTmp2; (void)veldepFit; (void)visOpt;  // scratch is the library's own; no display
+  if (!ctx || nBlockList < 0 || (nBlockList > 0 && !dBlockList)) return MSBG_GPU_ERR_ARG;
+  if (numIter < 0)  // the reference's compressed-range mode (src/msbg4.cpp:136-141)
+    return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "negative numIter (compressed value range)");
+  if (gridSpacing != 1.0f)  // the reference asserts a unit spacing (src/msbg4.cpp:326)
+    return fail(ctx, MSBG_GPU_ERR_ARG, "gridSpacing must be 1");
+  // lambda is forced to 0 by the reference itself (src/msbg4.cpp:164); lambdaSDF serves it
+  (void)lambda; (void)lambdaSDF;
+  if (densThr > 0.0f || densThrTol1 > 0.0f || densThrTol2 > 0.0f || velMagThr != 0.0f || msbgVel || veldepOn ||
+      taubinStrength != 0.0f || redist > 0.0f)
+    return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED,
+                "density constraints, velocity terms, Taubin smoothing and redistancing are not on this path");
+  int rc = checkChan(ctx, chPhi);
   if (rc) return rc;
-  return pdeRun(ctx, chan, laplTyp, doConstrZeroOne, numIter, timeStep, anisDiffAlpha, variant);
+  return pdeRun(ctx, chPhi, laplTyp, doConstrZeroOne, numIter, timeStep, anisDiffAlpha, variant, dBlockList,
+                nBlockList);
 }
 
 extern "C" int msbg_gpu_surface_job(msbg_gpu_ctx *ctx, const float *hPts, int64_t n, float rParticle,
@@ -772,7 +791,7 @@ extern "C" int msbg_gpu_surface_job(msbg_gpu_ctx *ctx, const float *hPts, int64_
   if (!rc) rc = msbg_gpu_splat(ctx, ctx->dPts, n, rParticle, nbDist);
   if (!rc) rc = msbg_gpu_splat_finalize(ctx, rParticle, nbDist);
   if (!rc && numIter > 0)
-    rc = msbg_gpu_apply_channel_pde_fast(ctx, 0, laplTyp, 1, numIter, timeStep, 0.0f, variant);
+    rc = pdeRun(ctx, 0, laplTyp, 1, numIter, timeStep, 0.0f, variant);
   if (rc) return rc;
   if (nActiveOut) *nActiveOut = ctx->nActive;
   if (hOut) {

@@ -58,6 +58,8 @@ struct msbg_gpu_ctx {
   int32_t *dSlot = nullptr;      // [nBlocks]
   int32_t *dActive = nullptr;    // [nBlocks] ascending bids of value blocks
   int32_t *dColorBids = nullptr; // [nBlocks] value blocks grouped by 8-color class
+  int32_t *dListMark = nullptr;  // [nBlocks] sweeps with a block list: listed blocks
+  int32_t *dListBids = nullptr;  // [nBlocks] sweeps with a block list: listed value blocks by colour
   int64_t *dScanPartial = nullptr; // scan scratch
   int64_t *dCounters = nullptr;  // [kNumCounters], see kColorTot
   int64_t *hCounters = nullptr;  // pinned mirror
@@ -84,6 +86,8 @@ struct msbg_gpu_ctx {
   msbg::BatchState *batch = nullptr;       // batched solves: volumes of the layout, graph
   msbg::LevelChannels *levelCh = nullptr;  // multi-level channels of the halo fill
   int mgPre = 2, mgPost = 2, mgTileIters = 3, mgCoarsestIter = 0;  // multigrid parameters
+  float relaxOmega = 6.0f / 7.0f;  // block smoother of msbg_gpu_relax (src/msbg.cpp:814-843)
+  int relaxBlockIter = 5;
   std::string err;
 };
 
@@ -135,8 +139,9 @@ int ensureTmpSlab(msbg_gpu_ctx *ctx, size_t bytes);
 int splatRun(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rParticle, float nbDist);
 int splatFinalizeRun(msbg_gpu_ctx *ctx, float rParticle, float nbDist);
 int fillChannel(msbg_gpu_ctx *ctx, int chan, double v);
+// Sweeps over all value blocks (dList NULL) or the listed blocks (device block ids).
 int pdeRun(msbg_gpu_ctx *ctx, int chan, int laplTyp, int constr01, int numIter, float dt,
-           float anisAlpha, int variant);
+           float anisAlpha, int variant, const int32_t *dList = nullptr, int64_t nList = 0);
 
 // ---- storage conversions (device) ---------------------------------------------
 // uint16 density: load v*(1/65535) (src/sbg.h:225-247); the sweep store rounds half

@@ -441,6 +441,8 @@ void poissonFree(PoissonState *ps) {
   if (ps->dBpar) cudaFree(ps->dBpar);
   if (ps->dParList) cudaFree(ps->dParList);
   if (ps->dPartial) cudaFree(ps->dPartial);
+  if (ps->dListBuf) cudaFree(ps->dListBuf);
+  if (ps->dListPart) cudaFree(ps->dListPart);
   if (ps->dScal) cudaFree(ps->dScal);
   if (ps->hScal) cudaFreeHost(ps->hScal);
   delete ps;
@@ -505,8 +507,8 @@ static int buildHierarchy(msbg_gpu_ctx *ctx, PoissonState *ps) {
     for (auto *v : {&P.cx, &P.cy, &P.cz, &P.d}) if ((rc = allocT(ctx, (float **)&(*v)[l], n))) return rc;
     if (l > 0) for (auto *v : {&P.x, &P.b, &P.r}) if ((rc = allocT(ctx, (float **)&(*v)[l], n))) return rc;
   }
-  const int64_t n0 = ps->levels[0].nCell;
-  for (void **q : {&P.vr, &P.vp, &P.vz, &P.vs}) if ((rc = allocT(ctx, (float **)q, n0))) return rc;
+  // the FP32 CG work vectors are allocated by their first user (ensureF32Work): the
+  // mixed-precision solve never needs them
   ps->nPartial = 152 * 16;
   MSBG_CUDA(ctx, cudaMalloc(&ps->dPartial, (size_t)ps->nPartial * 2 * sizeof(double)));
   MSBG_CUDA(ctx, cudaMalloc(&ps->dScal, 32 * sizeof(double)));
@@ -806,12 +808,44 @@ static int checkStatus(msbg_gpu_ctx *ctx) {
   return MSBG_GPU_OK;
 }
 
+// The level-0 FP32 work vectors r, p, z, s of the FP32 solves (4 x 4 B per cell).
+int ensureF32Work(msbg_gpu_ctx *ctx, PoissonState *ps) {
+  PrecSet &P = ps->f32;
+  if (P.vr) return MSBG_GPU_OK;
+  const int64_t n0 = ps->levels[0].nCell;
+  int rc;
+  for (void **q : {&P.vr, &P.vp, &P.vz, &P.vs}) if ((rc = allocT(ctx, (float **)q, n0))) return rc;
+  return MSBG_GPU_OK;
+}
+
+extern "C" int msbg_gpu_poisson_release_work(msbg_gpu_ctx *ctx) {
+  if (!ctx) return MSBG_GPU_ERR_ARG;
+  if (!ctx->poisson) return MSBG_GPU_OK;
+  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  for (PrecSet *P : {&ctx->poisson->f32, &ctx->poisson->f16}) {
+    for (void **q : {&P->vr, &P->vp, &P->vz, &P->vs, &P->ve, &P->vb}) {
+      if (*q) cudaFree(*q);
+      *q = nullptr;
+    }
+  }
+  // the FP16 set (coefficient copies, coarse-level vectors) is rebuilt on demand
+  PrecSet &H = ctx->poisson->f16;
+  for (auto *v : {&H.x, &H.b, &H.r, &H.cx, &H.cy, &H.cz, &H.d}) {
+    for (void *q : *v) if (q) cudaFree(q);
+    v->clear();
+  }
+  ctx->poisson->f16Valid = false;
+  return MSBG_GPU_OK;
+}
+
 // level-0 operator and V-cycle for the batched solver (FP32)
 int batchApply(msbg_gpu_ctx *ctx, const float *x, const float *b, float *y, int mode) {
   return applyT<float>(ctx, ctx->poisson, ctx->poisson->f32, 0, x, b, y, mode);
 }
 int batchVcycle(msbg_gpu_ctx *ctx, float *x, const float *b) {
   PoissonState *ps = ctx->poisson;
+  int rc = ensureF32Work(ctx, ps);
+  if (rc) return rc;
   return vcycleT<float>(ctx, ps, ps->f32, 0, x, b, (float *)ps->f32.vs);
 }
 
@@ -823,6 +857,7 @@ int poissonEnsure(msbg_gpu_ctx *ctx) {
   ps->layoutStamp = ctx->layoutStamp;
   ps->preSweeps = ctx->mgPre; ps->postSweeps = ctx->mgPost;
   ps->tileIters = ctx->mgTileIters; ps->coarsestIter = ctx->mgCoarsestIter;
+  ps->relaxOmega = ctx->relaxOmega; ps->relaxBlockIter = ctx->relaxBlockIter;
   return buildHierarchy(ctx, ps);
 }
 
@@ -887,26 +922,82 @@ static int needCoeffs(msbg_gpu_ctx *ctx) {
   return MSBG_GPU_OK;
 }
 
-extern "C" int msbg_gpu_multiply_laplacian(msbg_gpu_ctx *ctx, int chanX, int chanB, int chanDstY, int calcResidual) {
-  if (!ctx) return MSBG_GPU_ERR_ARG;
-  int rc = needCoeffs(ctx);
-  if (rc) return rc;
-  float *x, *b = nullptr, *y;
-  if ((rc = chanF32(ctx, chanX, &x)) || (rc = chanF32(ctx, chanDstY, &y))) return rc;
-  if (calcResidual && (rc = chanF32(ctx, chanB, &b))) return rc;
-  return applyT<float>(ctx, ctx->poisson, ctx->poisson->f32, 0, x, b, y, calcResidual ? 1 : 0);
+// Levels other than the value blocks' (levelMg 0) have no channel payload here.
+static int needLevel0(msbg_gpu_ctx *ctx, int levelMg) {
+  if (levelMg != 0)
+    return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "levelMg %d: channels hold the value blocks (levelMg 0) only",
+                levelMg);
+  return MSBG_GPU_OK;
 }
 
-extern "C" int msbg_gpu_relax(msbg_gpu_ctx *ctx, int chanX, int chanB, int nIter, int reverseOrder) {
-  if (!ctx || nIter < 0) return MSBG_GPU_ERR_ARG;
-  int rc = needCoeffs(ctx);
+extern "C" int msbg_gpu_multiply_laplacian(msbg_gpu_ctx *ctx, unsigned options, int levelMg, int chanX, int chanB,
+                                           float kap, int chanDstY, double *pDotprod, const int32_t *dBlockList,
+                                           int64_t nBlockList) {
+  (void)kap;  // the reference's sparse-level path does not use it either (src/msbg3.cpp:1826-1911)
+  if (!ctx || nBlockList < 0 || (nBlockList > 0 && !dBlockList)) return MSBG_GPU_ERR_ARG;
+  const bool residual = (options & MSBG_GPU_OPT_CALC_RESIDUAL) != 0;
+  if (options & ~(unsigned)MSBG_GPU_OPT_CALC_RESIDUAL)
+    return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "multiply options 0x%x", options);
+  if (residual && pDotprod)  // as the reference asserts (src/msbg3.cpp:1884)
+    return fail(ctx, MSBG_GPU_ERR_ARG, "no dot product with OPT_CALC_RESIDUAL");
+  int rc = needLevel0(ctx, levelMg);
   if (rc) return rc;
+  if ((rc = needCoeffs(ctx))) return rc;
+  float *x, *b = nullptr, *y;
+  if ((rc = chanF32(ctx, chanX, &x)) || (rc = chanF32(ctx, chanDstY, &y))) return rc;
+  if (residual && (rc = chanF32(ctx, chanB, &b))) return rc;
+  PoissonState *ps = ctx->poisson;
+  if (dBlockList) {
+    SlotLists L;
+    if ((rc = listSlots(ctx, ps, dBlockList, nBlockList, &L))) return rc;
+    if ((rc = applyList(ctx, ps, L, x, b, y, residual ? 1 : 0, pDotprod ? ps->dScal + 13 : nullptr))) return rc;
+  } else if (pDotprod) {
+    if ((rc = applyT<float>(ctx, ps, ps->f32, 0, x, nullptr, y, 0, ps->dScal + 13))) return rc;
+  } else {
+    if ((rc = applyT<float>(ctx, ps, ps->f32, 0, x, b, y, residual ? 1 : 0))) return rc;
+  }
+  if (pDotprod) {
+    if ((rc = fetchScal(ctx, ps, 13, 1))) return rc;
+    *pDotprod = ps->hScal[13];
+  }
+  return MSBG_GPU_OK;
+}
+
+extern "C" int msbg_gpu_set_relax_params(msbg_gpu_ctx *ctx, float omega, int blockIter) {
+  if (!ctx || !(omega > 0.0f && omega < 2.0f) || blockIter < 0 || blockIter > 64) return MSBG_GPU_ERR_ARG;
+  ctx->relaxOmega = omega;
+  ctx->relaxBlockIter = blockIter;
+  if (ctx->poisson) {
+    ctx->poisson->relaxOmega = omega;
+    ctx->poisson->relaxBlockIter = blockIter;
+  }
+  return MSBG_GPU_OK;
+}
+
+extern "C" int msbg_gpu_relax(msbg_gpu_ctx *ctx, int boundaryZoneOnly, int reverseOrder, int levelMg, int chanX,
+                              int chanB, int chanTmp, int nIter, unsigned options, const int32_t *dBlockList,
+                              int64_t nBlockList) {
+  (void)chanTmp;  // in place, as the reference's red-black block order runs it (src/msbg3.cpp:2322-2336)
+  if (!ctx || nIter < 0 || nBlockList < 0 || (nBlockList > 0 && !dBlockList)) return MSBG_GPU_ERR_ARG;
+  if (boundaryZoneOnly)
+    return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "boundary-zone relaxation (no boundary zones on this path)");
+  if (options & ~(unsigned)MSBG_GPU_RELAX_TILES) return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "relax options 0x%x", options);
+  int rc = needLevel0(ctx, levelMg);
+  if (rc) return rc;
+  if ((rc = needCoeffs(ctx))) return rc;
   float *x, *b;
   if ((rc = chanF32(ctx, chanX, &x)) || (rc = chanF32(ctx, chanB, &b))) return rc;
-  if ((rc = smoothLevel<float>(ctx, ctx->poisson, ctx->poisson->f32, 0, x, b, nIter, reverseOrder != 0, kFirstNone,
-                                nullptr)))
-    return rc;
-  return checkStatus(ctx);
+  PoissonState *ps = ctx->poisson;
+  if (options & MSBG_GPU_RELAX_TILES) {
+    if (dBlockList) return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "the tile smoother relaxes all value blocks");
+    if ((rc = smoothLevel<float>(ctx, ps, ps->f32, 0, x, b, nIter, reverseOrder != 0, kFirstNone, nullptr)))
+      return rc;
+    return checkStatus(ctx);
+  }
+  SlotLists L;
+  if (dBlockList && (rc = listSlots(ctx, ps, dBlockList, nBlockList, &L))) return rc;
+  return relaxReference(ctx, ps, dBlockList ? &L : nullptr, x, b, nIter, reverseOrder ? 1 : 0, ps->relaxBlockIter,
+                        ps->relaxOmega);
 }
 
 extern "C" int msbg_gpu_vcycle(msbg_gpu_ctx *ctx, int chanX, int chanB) {
@@ -916,41 +1007,64 @@ extern "C" int msbg_gpu_vcycle(msbg_gpu_ctx *ctx, int chanX, int chanB) {
   float *x, *b;
   if ((rc = chanF32(ctx, chanX, &x)) || (rc = chanF32(ctx, chanB, &b))) return rc;
   PoissonState *ps = ctx->poisson;
+  if ((rc = ensureF32Work(ctx, ps))) return rc;
   if ((rc = vcycleT<float>(ctx, ps, ps->f32, 0, x, b, (float *)ps->f32.vs))) return rc;
   return checkStatus(ctx);
 }
 
-extern "C" int msbg_gpu_dot(msbg_gpu_ctx *ctx, int chanA, int chanB, double *out) {
-  if (!ctx || !out) return MSBG_GPU_ERR_ARG;
-  int rc = needLayoutP(ctx);
+extern "C" int msbg_gpu_dot(msbg_gpu_ctx *ctx, int chanA, int chanB, int levelMg, const int32_t *dBlockList,
+                            int64_t nBlockList, double *out) {
+  if (!ctx || !out || nBlockList < 0 || (nBlockList > 0 && !dBlockList)) return MSBG_GPU_ERR_ARG;
+  int rc = needLevel0(ctx, levelMg);
   if (rc) return rc;
+  if ((rc = needLayoutP(ctx))) return rc;
   float *a, *b;
   if ((rc = chanF32(ctx, chanA, &a)) || (rc = chanF32(ctx, chanB, &b))) return rc;
   PoissonState *ps = ctx->poisson;
-  if ((rc = dotDev<float>(ctx, ps, a, b, ps->levels[0].nCell, ps->dScal + 12))) return rc;
+  if (dBlockList) {
+    SlotLists L;
+    if ((rc = listSlots(ctx, ps, dBlockList, nBlockList, &L))) return rc;
+    if ((rc = dotList(ctx, ps, L, a, b, ps->dScal + 12))) return rc;
+  } else if ((rc = dotDev<float>(ctx, ps, a, b, ps->levels[0].nCell, ps->dScal + 12))) {
+    return rc;
+  }
   if ((rc = fetchScal(ctx, ps, 12, 1))) return rc;
   *out = ps->hScal[12];
   if (!isfinite(*out)) return fail(ctx, MSBG_GPU_ERR_NONFINITE, "dot product is not finite");  // src/msbg.cpp:4635
   return MSBG_GPU_OK;
 }
 
-extern "C" int msbg_gpu_axpby(msbg_gpu_ctx *ctx, double a, int chanX, double b, int chanY) {
-  if (!ctx) return MSBG_GPU_ERR_ARG;
-  int rc = needLayoutP(ctx);
+extern "C" int msbg_gpu_axpby(msbg_gpu_ctx *ctx, double a, int chanX, double b, int chanY, int levelMax, int levelMg,
+                              const int32_t *dBlockList, int64_t nBlockList) {
+  if (!ctx || nBlockList < 0 || (nBlockList > 0 && !dBlockList)) return MSBG_GPU_ERR_ARG;
+  int rc = needLevel0(ctx, levelMg);
   if (rc) return rc;
+  if ((rc = needLayoutP(ctx))) return rc;
   float *x, *y;
   if ((rc = chanF32(ctx, chanX, &x)) || (rc = chanF32(ctx, chanY, &y))) return rc;
+  if (levelMax < 0) return MSBG_GPU_OK;  // value blocks are level 0: none is at or below levelMax
+  if (dBlockList) {
+    SlotLists L;
+    if ((rc = listSlots(ctx, ctx->poisson, dBlockList, nBlockList, &L))) return rc;
+    return axpbyList(ctx, L, a, x, b, y);
+  }
   const int64_t n = ctx->poisson->levels[0].nCell;
   MSBG_LAUNCH(ctx, kAxpby, gridCells(n), 256, 0, a, x, b, y, n);
   return MSBG_GPU_OK;
 }
 
-extern "C" int msbg_gpu_axpby_combined(msbg_gpu_ctx *ctx, double a, double b, int chanQ, int chanX, int chanP) {
-  if (!ctx) return MSBG_GPU_ERR_ARG;
+extern "C" int msbg_gpu_axpby_combined(msbg_gpu_ctx *ctx, double a, double b, int chanQ, int chanX, int chanP,
+                                       const int32_t *dBlockList, int64_t nBlockList) {
+  if (!ctx || nBlockList < 0 || (nBlockList > 0 && !dBlockList)) return MSBG_GPU_ERR_ARG;
   int rc = needLayoutP(ctx);
   if (rc) return rc;
   float *q, *x, *p;
   if ((rc = chanF32(ctx, chanQ, &q)) || (rc = chanF32(ctx, chanX, &x)) || (rc = chanF32(ctx, chanP, &p))) return rc;
+  if (dBlockList) {
+    SlotLists L;
+    if ((rc = listSlots(ctx, ctx->poisson, dBlockList, nBlockList, &L))) return rc;
+    return axpbyCombinedList(ctx, L, a, b, q, x, p);
+  }
   const int64_t n = ctx->poisson->levels[0].nCell;
   MSBG_LAUNCH(ctx, kAxpbyCombined, gridCells(n), 256, 0, a, b, q, x, p, n);
   return MSBG_GPU_OK;
@@ -964,6 +1078,7 @@ extern "C" int msbg_gpu_mgpcg_solve(msbg_gpu_ctx *ctx, int chanX, int chanB, dou
   float *x, *b;
   if ((rc = chanF32(ctx, chanX, &x)) || (rc = chanF32(ctx, chanB, &b))) return rc;
   PoissonState *ps = ctx->poisson;
+  if ((rc = ensureF32Work(ctx, ps))) return rc;
   float *r = (float *)ps->f32.vr;
   if ((rc = applyT<float>(ctx, ps, ps->f32, 0, x, b, r, 1))) return rc;
   double rr0, bb;

@@ -158,9 +158,36 @@ struct PoissonState {
   uint8_t *dBpar = nullptr;
   std::map<std::tuple<const void *, int, int>, CUtensorMap> tmaMaps;  // smoother tensor maps
   int64_t nEven = 0;
+  int32_t *dListBuf = nullptr;   // block-list calls: slots, parity lists, counters
+  double *dListPart = nullptr;   // per-listed-block partial sums
+  int64_t listCap = 0;
+  float relaxOmega = 6.0f / 7.0f;  // the reference's smoother constants (src/msbg.cpp:814-843)
+  int relaxBlockIter = 5;
 };
 
 void poissonFree(PoissonState *ps);
+// Allocates the level-0 FP32 CG work vectors on first use.
+int ensureF32Work(msbg_gpu_ctx *ctx, PoissonState *ps);
+
+// A caller's block list (device block ids) as value-block slots (-1 for blocks without
+// payload), and its value blocks split by block parity (bx+by+bz)&1 (poisson_ref.cu).
+struct SlotLists {
+  const int32_t *all = nullptr;
+  int64_t nAll = 0;
+  const int32_t *par[2] = {nullptr, nullptr};
+  int64_t nPar[2] = {0, 0};
+};
+int listSlots(msbg_gpu_ctx *ctx, PoissonState *ps, const int32_t *dBids, int64_t n, SlotLists *out);
+// y = A x (residual: b - A x) on the listed blocks; dDot (device) = sum of y x over them
+int applyList(msbg_gpu_ctx *ctx, PoissonState *ps, const SlotLists &L, const float *x, const float *b, float *y,
+              int residual, double *dDot);
+int dotList(msbg_gpu_ctx *ctx, PoissonState *ps, const SlotLists &L, const float *a, const float *b, double *dOut);
+int axpbyList(msbg_gpu_ctx *ctx, const SlotLists &L, double a, const float *x, double b, float *y);
+int axpbyCombinedList(msbg_gpu_ctx *ctx, const SlotLists &L, double a, double b, const float *q, float *x, float *p);
+// The reference's block smoother (relax / relaxBlockList), `passes` times, on the listed
+// blocks (L) or all value blocks (L == nullptr).
+int relaxReference(msbg_gpu_ctx *ctx, PoissonState *ps, const SlotLists *L, float *x, const float *b, int passes,
+                   int reverse, int blockIter, float omega);
 int poissonEnsure(msbg_gpu_ctx *ctx);
 LvGeom geomOf(const MgLevel &L);
 BlkGeom blkOf(const PoissonState *ps, const MgLevel &L);

@@ -139,8 +139,66 @@ static int launchTyped(msbg_gpu_ctx *ctx, int storage, bool exact, const int32_t
   }
 }
 
+// Listed blocks of the colour lists: flag[i] = the block at dColorBids[i] is listed.
+__global__ void kMarkList(const int32_t *__restrict__ list, int64_t n, int64_t nBlocks, int32_t *__restrict__ mark,
+                          int32_t *__restrict__ bad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int b = list[i];
+  if (b < 0 || b >= nBlocks) atomicAdd(bad, 1);
+  else mark[b] = 1;
+}
+__global__ void kListedFlags(const int32_t *__restrict__ bids, int64_t n, const int32_t *__restrict__ mark,
+                             int32_t *__restrict__ flag) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) flag[i] = mark[bids[i]];
+}
+__global__ void kListedScatter(const int32_t *__restrict__ bids, const int32_t *__restrict__ flag,
+                               const int64_t *__restrict__ off, int64_t n, int32_t *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && flag[i]) out[off[i]] = bids[i];
+}
+// new colour starts: the scan offset at each old colour start, and the total
+__global__ void kListedStarts(const int64_t *__restrict__ off, const int64_t *__restrict__ total, int64_t n,
+                              const int *__restrict__ starts, int64_t *__restrict__ out) {
+  const int c = threadIdx.x;
+  if (c < 8) out[c] = starts[c] < n ? off[starts[c]] : *total;
+  if (c == 8) out[8] = *total;
+}
+
+// The colour lists restricted to the listed blocks (stable, so each colour keeps its
+// ascending order): into ctx->dListBids with starts cs[0..8].
+static int listedColourLists(msbg_gpu_ctx *ctx, const int32_t *dList, int64_t nList, int cs[9]) {
+  const int64_t nB = ctx->nBlocks, nAct = ctx->nActive;
+  if (!ctx->dListMark) MSBG_CUDA(ctx, cudaMalloc(&ctx->dListMark, (size_t)nB * 4));
+  if (!ctx->dListBids) MSBG_CUDA(ctx, cudaMalloc(&ctx->dListBids, (size_t)nB * 4));
+  int rc = ensureTmpSlab(ctx, (size_t)(nAct + 1) * 12 + 256);
+  if (rc) return rc;
+  int32_t *flag = (int32_t *)ctx->dTmpSlab;
+  int64_t *off = (int64_t *)((char *)ctx->dTmpSlab + (((size_t)(nAct + 1) * 4 + 15) & ~size_t(15)));
+  int64_t *aux = off + nAct + 1;  // [0]: total, [1..9]: starts, [10]: bad ids (as int32)
+  int *dStarts = (int *)(aux + 12);
+  MSBG_CUDA(ctx, cudaMemsetAsync(ctx->dListMark, 0, (size_t)nB * 4, ctx->stream));
+  MSBG_CUDA(ctx, cudaMemsetAsync(aux, 0, 12 * 8, ctx->stream));
+  if (nList > 0)
+    MSBG_LAUNCH(ctx, kMarkList, gridFor(nList, 256), 256, 0, dList, nList, nB, ctx->dListMark, (int32_t *)(aux + 10));
+  MSBG_CUDA(ctx, cudaMemcpyAsync(dStarts, ctx->colorStart, 9 * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  if (nAct > 0) {
+    MSBG_LAUNCH(ctx, kListedFlags, gridFor(nAct, 256), 256, 0, ctx->dColorBids, nAct, ctx->dListMark, flag);
+    if ((rc = exclusiveScanFlags(ctx, flag, nAct, off, aux))) return rc;
+    MSBG_LAUNCH(ctx, kListedScatter, gridFor(nAct, 256), 256, 0, ctx->dColorBids, flag, off, nAct, ctx->dListBids);
+    MSBG_LAUNCH(ctx, kListedStarts, 1, 32, 0, off, aux, nAct, dStarts, aux + 1);
+  }
+  int64_t h[11] = {};
+  MSBG_CUDA(ctx, cudaMemcpyAsync(h, aux, 11 * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if ((int32_t)h[10]) return fail(ctx, MSBG_GPU_ERR_ARG, "block list holds ids outside the block grid");
+  for (int c = 0; c <= 8; c++) cs[c] = nAct > 0 ? (int)h[1 + c] : 0;
+  return MSBG_GPU_OK;
+}
+
 int pdeRun(msbg_gpu_ctx *ctx, int chan, int laplTyp, int constr01, int numIter, float dt, float anisAlpha,
-           int variant) {
+           int variant, const int32_t *dList, int64_t nList) {
   bool color8 = false, redBlack = false;
   int kind = laplTyp;
   if (kind < 0) {  // src/msbg4.cpp:100-114
@@ -173,9 +231,16 @@ int pdeRun(msbg_gpu_ctx *ctx, int chan, int laplTyp, int constr01, int numIter, 
   if (nIter % 2 == 1) nIter++;  // src/msbg4.cpp:150-152
   const int32_t *cb = ctx->dColorBids;
   const int *cs = ctx->colorStart;
+  int listStarts[9];
+  if (dList) {
+    const int rc = listedColourLists(ctx, dList, nList, listStarts);
+    if (rc) return rc;
+    cb = ctx->dListBids;
+    cs = listStarts;
+  }
   if ((color8 || redBlack) && c.storage != MSBG_GPU_F64) {
     // streaming kernel with the x-face cache (sweep_color.cu)
-    const int rc = colorSweepRun(ctx, c, exact, color8, nIter, g.p);
+    const int rc = colorSweepRun(ctx, c, exact, color8, nIter, g.p, cb, cs);
     if (rc < 0) return rc;
     if (rc == 0) {
       // the streaming kernel's bounded shared-memory waits report through dStatus
@@ -210,23 +275,34 @@ int pdeRun(msbg_gpu_ctx *ctx, int chan, int laplTyp, int constr01, int numIter, 
     }
     return MSBG_GPU_OK;
   }
-  // ping-pong through the temp slab; the active list is the whole block set
+  // ping-pong through the temp slab over the whole block set, or over the listed value
+  // blocks with both buffers holding the unlisted blocks' values
   const size_t bytes = (size_t)ctx->nActive * ctx->voxPerBlock * storageBytes(c.storage);
-  int rc = ensureTmpSlab(ctx, bytes ? bytes : 1);
-  if (rc) return rc;
-  void *bufs[2] = {c.d, ctx->dTmpSlab};
-  int cur = 0;
-  for (int it = 0; it < nIter; it++) {
+  const int32_t *pbids = dList ? cb : ctx->dActive;
+  const int pn = dList ? cs[8] : (int)ctx->nActive;
+  void *tmp = nullptr;
+  if (dList) {  // the colour-list scratch above lives in the temp slab: a slab of its own
+    if (bytes) MSBG_CUDA(ctx, cudaMallocAsync(&tmp, bytes, ctx->stream));
+    if (bytes) MSBG_CUDA(ctx, cudaMemcpyAsync(tmp, c.d, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  } else {
+    int rc = ensureTmpSlab(ctx, bytes ? bytes : 1);
+    if (rc) return rc;
+    tmp = ctx->dTmpSlab;
+  }
+  void *bufs[2] = {c.d, tmp};
+  int cur = 0, rc = MSBG_GPU_OK;
+  for (int it = 0; it < nIter && !rc; it++) {
     const bool copyOnly = it == nIter - 1 && (nIter0 % 2) == 1;
     if (copyOnly) {
-      if (bytes) MSBG_CUDA(ctx, cudaMemcpyAsync(bufs[cur ^ 1], bufs[cur], bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+      if (bytes && cudaMemcpyAsync(bufs[cur ^ 1], bufs[cur], bytes, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess)
+        rc = fail(ctx, MSBG_GPU_ERR_CUDA, "ping-pong copy failed");
     } else {
-      rc = launchTyped(ctx, c.storage, exact, ctx->dActive, (int)ctx->nActive, bufs[cur], bufs[cur ^ 1], g);
-      if (rc) return rc;
+      rc = launchTyped(ctx, c.storage, exact, pbids, pn, bufs[cur], bufs[cur ^ 1], g);
     }
     cur ^= 1;
   }
-  return MSBG_GPU_OK;
+  if (dList && tmp) cudaFreeAsync(tmp, ctx->stream);
+  return rc;
 }
 
 }  // namespace msbg

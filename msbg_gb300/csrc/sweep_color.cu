@@ -541,7 +541,7 @@ __global__ void kExtractFaces(const T *__restrict__ pay, int64_t nAct, T *__rest
 
 template <typename T, int BS>
 static int runColorT(msbg_gpu_ctx *ctx, Channel &c, bool exact, bool color8, int nIter,
-                     const SweepParams &p) {
+                     const SweepParams &p, const int32_t *bids, const int *cs) {
   const int64_t nAct = ctx->nActive;
   if (nAct == 0) return MSBG_GPU_OK;
   const size_t faceBytes = (size_t)nAct * (2 * BS * BS + 4 * BS) * sizeof(T);
@@ -579,32 +579,32 @@ static int runColorT(msbg_gpu_ctx *ctx, Channel &c, bool exact, bool color8, int
     attrSet[ki] = true;
   }
   static const int rbOrder[2][4] = {{1, 2, 4, 7}, {0, 3, 5, 6}};
-  const int *cs = ctx->colorStart;
   constexpr int NT = ColorSweep<T, BS>::NT;
   for (int it = 0; it < nIter; it++) {
     for (int pass = 0; pass < 8; pass++) {
       const int col = color8 ? pass : rbOrder[pass / 4][pass % 4];
       const int cnt = cs[col + 1] - cs[col];
       if (cnt <= 0) continue;
-      a.bids = ctx->dColorBids + cs[col];
+      a.bids = bids + cs[col];
       MSBG_LAUNCH(ctx, kern, (unsigned)cnt, NT, smem, a);
     }
   }
   return MSBG_GPU_OK;
 }
 
-int colorSweepRun(msbg_gpu_ctx *ctx, Channel &c, bool exact, bool color8, int nIter, const SweepParams &p) {
+int colorSweepRun(msbg_gpu_ctx *ctx, Channel &c, bool exact, bool color8, int nIter, const SweepParams &p,
+                  const int32_t *bids, const int *cs) {
   if (ctx->bsx == 32) {
     switch (c.storage) {
-      case MSBG_GPU_F32: return runColorT<float, 32>(ctx, c, exact, color8, nIter, p);
-      case MSBG_GPU_F16: return runColorT<__half, 32>(ctx, c, exact, color8, nIter, p);
-      case MSBG_GPU_U16: return runColorT<uint16_t, 32>(ctx, c, exact, color8, nIter, p);
+      case MSBG_GPU_F32: return runColorT<float, 32>(ctx, c, exact, color8, nIter, p, bids, cs);
+      case MSBG_GPU_F16: return runColorT<__half, 32>(ctx, c, exact, color8, nIter, p, bids, cs);
+      case MSBG_GPU_U16: return runColorT<uint16_t, 32>(ctx, c, exact, color8, nIter, p, bids, cs);
     }
   } else if (ctx->bsx == 16) {
     switch (c.storage) {
-      case MSBG_GPU_F32: return runColorT<float, 16>(ctx, c, exact, color8, nIter, p);
-      case MSBG_GPU_F16: return runColorT<__half, 16>(ctx, c, exact, color8, nIter, p);
-      case MSBG_GPU_U16: return runColorT<uint16_t, 16>(ctx, c, exact, color8, nIter, p);
+      case MSBG_GPU_F32: return runColorT<float, 16>(ctx, c, exact, color8, nIter, p, bids, cs);
+      case MSBG_GPU_F16: return runColorT<__half, 16>(ctx, c, exact, color8, nIter, p, bids, cs);
+      case MSBG_GPU_U16: return runColorT<uint16_t, 16>(ctx, c, exact, color8, nIter, p, bids, cs);
     }
   }
   return 1;  // not handled: caller uses the gather kernel

@@ -279,6 +279,9 @@ __device__ __forceinline__ void computeStrip(const float Pm[3][6], const float P
   }
 }
 
-int colorSweepRun(msbg_gpu_ctx *ctx, Channel &c, bool exact, bool color8, int nIter, const SweepParams &p);
+// bids / colorStart: the blocks of each colour (colour c: bids[colorStart[c] ..
+// colorStart[c+1]-1]); the context's full colour lists, or a caller's subset.
+int colorSweepRun(msbg_gpu_ctx *ctx, Channel &c, bool exact, bool color8, int nIter, const SweepParams &p,
+                  const int32_t *bids, const int *colorStart);
 
 }  // namespace msbg

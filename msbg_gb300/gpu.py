@@ -39,6 +39,10 @@ IP_NO_BORDER_CHECK, IP_RENDER_DENS = 1 << 15, 1 << 18
 BC_NEUMANN, BC_COARSE_LEVEL = 1 << 10, 1 << 26
 LBLK_EMPTY, LBLK_FULL, LBLK_NONE = -1, -2, -3
 
+# solver options: OPT_CALC_RESIDUAL (src/msbg.h:115); the tile smoother of msbg_gpu_relax
+OPT_CALC_RESIDUAL, RELAX_TILES = 1 << 12, 1 << 31
+CH_NULL = 0  # no channel (the reference's CH_NULL)
+
 BLK_DOM_BORDER, BLK_COARSE_FINE, BLK_FINE_COARSE = 1 << 1, 1 << 2, 1 << 3
 BLK_EXISTS, BLK_UNIFORM_EMPTY = 1 << 12, 1 << 13
 
@@ -68,7 +72,8 @@ SIGNATURES = {
     "msbg_gpu_fill": (I, [P, I, D]),
     "msbg_gpu_splat": (I, [P, P, I64, F, F]),
     "msbg_gpu_splat_finalize": (I, [P, F, F]),
-    "msbg_gpu_apply_channel_pde_fast": (I, [P, I, I, I, I, F, F, I]),
+    "msbg_gpu_apply_channel_pde_fast": (I, [P, I, I, I, P, I64, I, I, F, F, F, I, F, F, F, P, F, F, F, F, F, I, P,
+                                            I, I]),
     "msbg_gpu_surface_job": (I, [P, P, I64, F, F, P, I, I, I, F, I, P, SZ, C.POINTER(I64)]),
     "msbg_gpu_event_record": (I, [P, I]),
     "msbg_gpu_event_elapsed": (I, [P, I, I, C.POINTER(F)]),
@@ -92,8 +97,9 @@ SIGNATURES = {
     "msbg_gpu_assign_slots_noalloc": (I, [P, I64, P, P, P, P]),
     "msbg_gpu_poisson_set_coefficients": (I, [P, I, I, I, I]),
     "msbg_gpu_poisson_procedural_coefficients": (I, [P, C.c_uint32, I, I, I, I]),
-    "msbg_gpu_multiply_laplacian": (I, [P, I, I, I, I]),
-    "msbg_gpu_relax": (I, [P, I, I, I, I]),
+    "msbg_gpu_multiply_laplacian": (I, [P, C.c_uint, I, I, I, F, I, C.POINTER(D), P, I64]),
+    "msbg_gpu_relax": (I, [P, I, I, I, I, I, I, I, C.c_uint, P, I64]),
+    "msbg_gpu_set_relax_params": (I, [P, F, I]),
     "msbg_gpu_downsample_channel": (I, [P, I, P, I]),
     "msbg_gpu_interpolate": (I, [P, I, P, I64, P, I]),
     "msbg_gpu_level_grid_set": (I, [P, I, I, I, P, P, I64, C.c_float, C.c_float]),
@@ -106,11 +112,12 @@ SIGNATURES = {
     "msbg_gpu_restrict_level_blocks": (I, [P, I, I, P, I64, I, P, C.POINTER(I64)]),
     "msbg_gpu_diag_wait_timeout": (I, [P, I]),
     "msbg_gpu_vcycle": (I, [P, I, I]),
-    "msbg_gpu_dot": (I, [P, I, I, C.POINTER(D)]),
-    "msbg_gpu_axpby": (I, [P, D, I, D, I]),
-    "msbg_gpu_axpby_combined": (I, [P, D, D, I, I, I]),
+    "msbg_gpu_dot": (I, [P, I, I, I, P, I64, C.POINTER(D)]),
+    "msbg_gpu_axpby": (I, [P, D, I, D, I, I, I, P, I64]),
+    "msbg_gpu_axpby_combined": (I, [P, D, D, I, I, I, P, I64]),
     "msbg_gpu_mgpcg_solve": (I, [P, I, I, D, I, C.POINTER(I), C.POINTER(D)]),
     "msbg_gpu_mg_info": (I, [P, C.POINTER(I), P, I]),
+    "msbg_gpu_poisson_release_work": (I, [P]),
     "msbg_gpu_poisson_set_params": (I, [P, I, I, I, I]),
     "msbg_gpu_mgpcg_solve_mixed": (I, [P, I, I, D, I, D, I, C.POINTER(I), C.POINTER(I), C.POINTER(D)]),
 }
@@ -398,10 +405,33 @@ class MultiresSparseGrid:
 
     # reference: applyChannelPdeFast<T> (src/msbg.h:2150-2172); the reference's
     # (chPhi, laplTyp, doConstrZeroOne, numIter, timeStep, anisDiffAlpha) subset
-    def applyChannelPdeFast(self, chPhi: int, laplTyp: int, doConstrZeroOne: int, numIter: int,
-                            timeStep: float, anisDiffAlpha: float = 0.0, variant: int = SWEEP_EXACT):
-        self._check(self.L.msbg_gpu_apply_channel_pde_fast(self.h, chPhi, laplTyp, doConstrZeroOne,
-                                                           numIter, timeStep, anisDiffAlpha, variant))
+    def _block_list(self, blockList):
+        """(device pointer, count, buffer to keep alive) of a block list: None (all value
+        blocks), a DeviceBuffer of int32 ids, or host ids (copied to the device)."""
+        if blockList is None:
+            return None, 0, None
+        if isinstance(blockList, DeviceBuffer):
+            return C.c_void_p(blockList.ptr), blockList.nbytes // 4, blockList
+        a = np.ascontiguousarray(blockList, np.int32).ravel()
+        buf = self.to_device(a if a.size else np.zeros(1, np.int32))
+        return C.c_void_p(buf.ptr), a.size, buf
+
+    # reference: applyChannelPdeFast<T> (src/msbg.h:2150-2172), the same arguments in the same
+    # order (msbgVel / veldep_fit must stay None), plus the kernel variant
+    def applyChannelPdeFast(self, chPhi: int, chTmp: int = CH_NULL, chTmp2: int = CH_NULL, blockList=None,
+                            laplTyp: int = LAPL_MCF_8COLOR, doConstrZeroOne: int = 1, densThr: float = 0.0,
+                            densThrTol1: float = 0.0, densThrTol2: float = 0.0, numIter: int = 1,
+                            gridSpacing: float = 1.0, timeStep: float = 0.025, velMagThr: float = 0.0,
+                            msbgVel=None, lambda_: float = 0.0, lambdaSDF: float = 0.0, taubinStrength: float = 0.0,
+                            redist: float = 0.0, anisDiffAlpha: float = 0.0, veldep_on: int = 0, veldep_fit=None,
+                            visOpt: int = 0, variant: int = SWEEP_EXACT):
+        lp, ln, keep = self._block_list(blockList)
+        self._check(self.L.msbg_gpu_apply_channel_pde_fast(
+            self.h, chPhi, chTmp, chTmp2, lp, ln, laplTyp, int(doConstrZeroOne), densThr, densThrTol1, densThrTol2,
+            numIter, gridSpacing, timeStep, velMagThr, msbgVel, lambda_, lambdaSDF, taubinStrength, redist,
+            anisDiffAlpha, veldep_on, veldep_fit, visOpt, variant))
+        if keep is not None and keep is not blockList:
+            self.synchronize()
 
     def surface_job(self, pts: np.ndarray, r_particle=2.0, nb_dist=2.0, bands=None,
                     laplTyp=LAPL_MCF_8COLOR, numIter=20, timeStep=0.1, variant=SWEEP_EXACT,
@@ -423,11 +453,38 @@ class MultiresSparseGrid:
     def poisson_procedural_coefficients(self, seed: int, cx=-1, cy=-1, cz=-1, diag=-1):
         self._check(self.L.msbg_gpu_poisson_procedural_coefficients(self.h, seed, cx, cy, cz, diag))
 
-    def multiplyLaplacianMatrix(self, chanX: int, chanB: int, chanDstY: int, calcResidual: bool = False):
-        self._check(self.L.msbg_gpu_multiply_laplacian(self.h, chanX, chanB, chanDstY, int(calcResidual)))
+    # reference: multiplyLaplacianMatrixOpt(options, levelMg, chanX, chanB, kap, chanDstY,
+    # pDotprod, blockList) (src/msbg.h:3167-3176); returns sum(Y X) when withDotprod
+    def multiplyLaplacianMatrixOpt(self, options: int, levelMg: int, chanX: int, chanB: int, kap: float,
+                                   chanDstY: int, withDotprod: bool = False, blockList=None):
+        lp, ln, keep = self._block_list(blockList)
+        dot = C.c_double()
+        self._check(self.L.msbg_gpu_multiply_laplacian(self.h, options, levelMg, chanX, chanB, kap, chanDstY,
+                                                       C.byref(dot) if withDotprod else None, lp, ln))
+        if keep is not None and keep is not blockList:
+            self.synchronize()
+        return dot.value if withDotprod else None
 
-    def relax(self, chanX: int, chanB: int, nIter: int, reverseOrder: bool = False):
-        self._check(self.L.msbg_gpu_relax(self.h, chanX, chanB, nIter, int(reverseOrder)))
+    def multiplyLaplacianMatrix(self, chanX: int, chanB: int, chanDstY: int, calcResidual: bool = False):
+        """Y = A X (or B - A X) over all value blocks."""
+        self.multiplyLaplacianMatrixOpt(OPT_CALC_RESIDUAL if calcResidual else 0, 0, chanX, chanB, 0.0, chanDstY)
+
+    # reference: relax(boundaryZoneOnly, reverseOrder, levelMg, chanX, chanB, chanTmp, nIter,
+    # options) (src/msbg.h:3269-3277); blockList stands in for the member list _blocksRelax
+    def relax(self, boundaryZoneOnly: int, reverseOrder: int, levelMg: int, chanX: int, chanB: int,
+              chanTmp: int, nIter: int, options: int = 0, blockList=None):
+        lp, ln, keep = self._block_list(blockList)
+        self._check(self.L.msbg_gpu_relax(self.h, int(boundaryZoneOnly), int(reverseOrder), levelMg, chanX, chanB,
+                                          chanTmp, nIter, options, lp, ln))
+        if keep is not None and keep is not blockList:
+            self.synchronize()
+
+    def relax_tiles(self, chanX: int, chanB: int, nIter: int, reverseOrder: bool = False):
+        """nIter passes of the multigrid's tile smoother (relax with RELAX_TILES)."""
+        self.relax(0, int(reverseOrder), 0, chanX, chanB, CH_NULL, nIter, RELAX_TILES)
+
+    def set_relax_params(self, omega: float = 6.0 / 7.0, block_iter: int = 5):
+        self._check(self.L.msbg_gpu_set_relax_params(self.h, omega, block_iter))
 
     def vcycle(self, chanX: int, chanB: int):
         self._check(self.L.msbg_gpu_vcycle(self.h, chanX, chanB))
@@ -579,16 +636,33 @@ class MultiresSparseGrid:
             do.free()
         return out, int(sk.value)
 
-    def dotProdChannel(self, a: int, b: int) -> float:
+    # reference: dotProdChannel(ch1, ch2, levelMg, blockList, pErrCode) (src/msbg.h:3331-3341);
+    # a non-finite sum raises MsbgGpuError with ERR_NONFINITE (the reference's pErrCode)
+    def dotProdChannel(self, a: int, b: int, levelMg: int = 0, blockList=None) -> float:
+        lp, ln, keep = self._block_list(blockList)
         out = C.c_double()
-        self._check(self.L.msbg_gpu_dot(self.h, a, b, C.byref(out)))
+        self._check(self.L.msbg_gpu_dot(self.h, a, b, levelMg, lp, ln, C.byref(out)))
         return out.value
 
-    def AXPBYChannel(self, a: float, chanX: int, b: float, chanY: int):
-        self._check(self.L.msbg_gpu_axpby(self.h, a, chanX, b, chanY))
+    # reference: AXPBYChannel(a, iChanX, b, iChanDstY, levelMax, levelMg, blockList)
+    # (src/msbg.h:3356-3362)
+    def AXPBYChannel(self, a: float, chanX: int, b: float, chanY: int, levelMax: int = 9999, levelMg: int = 0,
+                     blockList=None):
+        lp, ln, keep = self._block_list(blockList)
+        self._check(self.L.msbg_gpu_axpby(self.h, a, chanX, b, chanY, levelMax, levelMg, lp, ln))
+        if keep is not None and keep is not blockList:
+            self.synchronize()
 
-    def AXPBYChannelCombined(self, a: float, b: float, chanQ: int, chanX: int, chanP: int):
-        self._check(self.L.msbg_gpu_axpby_combined(self.h, a, b, chanQ, chanX, chanP))
+    # reference: AXPBYChannelCombined(a, b, iChanQ, iChanX, iChanP, blockList) (src/msbg.h:3364-3368)
+    def AXPBYChannelCombined(self, a: float, b: float, chanQ: int, chanX: int, chanP: int, blockList=None):
+        lp, ln, keep = self._block_list(blockList)
+        self._check(self.L.msbg_gpu_axpby_combined(self.h, a, b, chanQ, chanX, chanP, lp, ln))
+        if keep is not None and keep is not blockList:
+            self.synchronize()
+
+    def poisson_release_work(self):
+        """Frees the solver's level-0 work vectors and FP16 copies (reallocated on demand)."""
+        self._check(self.L.msbg_gpu_poisson_release_work(self.h))
 
     def mgpcg_solve(self, chanX: int, chanB: int, tol: float = 1e-6, max_iter: int = 200):
         it, rel = C.c_int(), C.c_double()
@@ -712,7 +786,8 @@ def surface_pipeline(pts: np.ndarray, res, bsx: int, storage: int = F32, n_iter:
         g.splat_finalize(r_particle, nb_dist)
         after_final = g.payload(0) if keep_after_finalize else None
         if n_iter > 0:
-            g.applyChannelPdeFast(0, lapl_typ, 1, n_iter, dt, 0.0, variant)
+            g.applyChannelPdeFast(0, laplTyp=lapl_typ, doConstrZeroOne=1, numIter=n_iter, timeStep=dt,
+                                  variant=variant)
         out = dict(levels=g.levels(), flags=g.flags(), active_bids=g.active_blocks(),
                    after_finalize=after_final, after_pde=g.payload(0), info=g.info(),
                    launches=g.launch_count())

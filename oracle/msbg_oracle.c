@@ -1509,3 +1509,93 @@ int64_t orc_restrict_level(const orc_grid *g, int nLevels, const int32_t *levels
   free(boxes);
   return skipped;
 }
+
+/* ---- the reference's block smoother (src/msbg3.cpp:1108-1332, 2170-2369) ---------- */
+
+/* One block: halo buffer hb [(bs+2)^3], x-fastest, position (i+1, j+1, k+1) for cell
+ * (i, j, k) of the block; then blockIter in-place iterations; the last one into x. */
+static void relax_ref_block(int nx, int ny, int nz, int bs, float *x, const float *b, const float *cx,
+                            const float *cy, const float *cz, const float *dinv, int bx, int by, int bz,
+                            int reverse, int blockIter, float omega, float *hb) {
+  const int hs = bs + 2, hs2 = hs * hs;
+  const int64_t sxy = (int64_t)nx * ny;
+  const int ox = bx * bs, oy = by * bs, oz = bz * bs;
+  for (int k = -1; k <= bs; k++)
+    for (int j = -1; j <= bs; j++)
+      for (int i = -1; i <= bs; i++) {
+        const int gx = ox + i, gy = oy + j, gz = oz + k;
+        const int out = (i < 0) + (i >= bs) + (j < 0) + (j >= bs) + (k < 0) + (k >= bs);
+        float v = 0.0f;
+        /* own cells and the face-neighbour layers; edges and corners are never read */
+        if (out <= 1 && gx >= 0 && gy >= 0 && gz >= 0 && gx < nx && gy < ny && gz < nz)
+          v = x[gz * sxy + (int64_t)gy * nx + gx];
+        hb[(k + 1) * hs2 + (j + 1) * hs + (i + 1)] = v;
+      }
+  /* upper-face coefficient of a cell: the lower face of the next cell (0 past the
+     domain, as the reference's zero block there) */
+  const float oneMinusOmega = 1.0f - omega;
+  /* the reference's SIMD width for the block edge (src/msbg3.cpp:1688-1745): 8 for edges
+     16 and 8, the edge itself below; edge 32 (which the reference does not handle)
+     takes 8 */
+  const int gw = bs >= 8 ? 8 : bs;
+  const int G = bs / gw;
+  float y[8];
+  for (int it = 0; it < blockIter; it++) {
+    const int backward = (it & 1) == (reverse ? 1 : 0);
+    const int last = it == blockIter - 1;
+    for (int s = 0; s < bs * bs * G; s++) {
+      const int q = backward ? bs * bs * G - 1 - s : s;
+      const int g = q % G, j = (q / G) % bs, k = q / (G * bs);
+      for (int l = 0; l < gw; l++) {
+        const int i = gw * g + l;
+        const int gx = ox + i, gy = oy + j, gz = oz + k;
+        const int64_t c = gz * sxy + (int64_t)gy * nx + gx;
+        const float *p = hb + (k + 1) * hs2 + (j + 1) * hs + (i + 1);
+        const float F0 = p[0], F1 = p[-1], F2 = p[1], F3 = p[-hs], F4 = p[hs], F5 = p[-hs2], F6 = p[hs2];
+        const float W1 = cx[c], W2 = gx + 1 < nx ? cx[c + 1] : 0.0f;
+        const float W3 = cy[c], W4 = gy + 1 < ny ? cy[c + nx] : 0.0f;
+        const float W5 = cz[c], W6 = gz + 1 < nz ? cz[c + sxy] : 0.0f;
+        float S = 0.0f;
+        S = fmaf(F1, W1, S);
+        S = fmaf(F2, W2, S);
+        S = fmaf(F3, W3, S);
+        S = fmaf(F4, W4, S);
+        S = fmaf(F5, W5, S);
+        S = fmaf(F6, W6, S);
+        const float t = omega * (b[c] + S);
+        y[l] = t * dinv[c] + oneMinusOmega * F0;
+      }
+      for (int l = 0; l < gw; l++) {
+        const int i = gw * g + l;
+        if (last)
+          x[(oz + k) * sxy + (int64_t)(oy + j) * nx + ox + i] = y[l];
+        else
+          hb[(k + 1) * hs2 + (j + 1) * hs + (i + 1)] = y[l];
+      }
+    }
+  }
+}
+
+void orc_relax_ref(int nx, int ny, int nz, int bs, float *x, const float *b, const float *cx,
+                   const float *cy, const float *cz, const float *dinv, const int32_t *bids, int64_t n,
+                   int passes, int reverse, int blockIter, float omega) {
+  const int nbx = nx / bs, nby = ny / bs;
+  const int hs = bs + 2;
+  for (int pass = 0; pass < passes; pass++)
+    for (int rb = 0; rb < 2; rb++) {
+#pragma omp parallel
+      {
+        float *hb = (float *)malloc(sizeof(float) * hs * hs * hs);
+#pragma omp for schedule(dynamic, 4)
+        for (int64_t t = 0; t < n; t++) {
+          const int bid = bids[t];
+          const int bx = bid % nbx, by = (bid / nbx) % nby, bz = bid / (nbx * nby);
+          int skip = ((bx + by + bz) & 1) == rb;
+          if (reverse) skip = !skip;
+          if (skip) continue;
+          relax_ref_block(nx, ny, nz, bs, x, b, cx, cy, cz, dinv, bx, by, bz, reverse, blockIter, omega, hb);
+        }
+        free(hb);
+      }
+    }
+}

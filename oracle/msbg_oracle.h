@@ -250,6 +250,24 @@ int orc_poisson_vcycle(const orc_level0 *L, int log2bs0, const double *b, double
 int orc_poisson_mgpcg(const orc_level0 *L, int log2bs0, const double *b, double *x, double tol,
                       int maxIter, int preSweeps, int postSweeps, int tileIters, int coarsestIter,
                       int64_t coarsestCells, int *iters, double *relres);
+/* The reference's block smoother, FP32 on dense [nz][ny][nx] arrays (cells outside the
+ * value blocks hold 0 in x): relax() (src/msbg3.cpp:2244-2369) calling relaxBlockList
+ * (src/msbg3.cpp:2170-2239) `passes` times.  Each pass runs two half-passes over the
+ * listed blocks (bids on the nx/bs x ny/bs x nz/bs block grid): blocks whose
+ * (bx+by+bz)&1 differs from the half-pass index (the other parity first with reverse),
+ * each with its face-neighbour halo taken at its start and blockIter block-local
+ * iterations in place (IprocessBlockLaplacian, src/msbg3.cpp:1108-1332): groups of gw
+ * x-consecutive cells updated together (gw = the reference's SIMD width, 8 for block
+ * edges 8 and 16, the edge itself for 4 and 2, src/msbg3.cpp:1688-1745; 8 for edge 32,
+ * which the reference does not handle),
+ *   S = fma(F6,W6, ... fma(F1,W1, 0)),  Y = omega (B + S) D + (1 - omega) F0,
+ * D = 1/diagonal (dinv), W the face coefficients (lower faces cx/cy/cz, upper faces the
+ * next cell's); iteration i sweeps the groups backward when (i&1) == reverse, forward
+ * otherwise; the last iteration writes to x instead of the block buffer, so it is a
+ * Jacobi step. */
+void orc_relax_ref(int nx, int ny, int nz, int bs, float *x, const float *b, const float *cx,
+                   const float *cy, const float *cz, const float *dinv, const int32_t *bids, int64_t n,
+                   int passes, int reverse, int blockIter, float omega);
 /* The GPU's seeded coefficients (float values) on a dense grid: lower faces + diagonal. */
 void orc_poisson_coeffs_dense(uint32_t seed, int nx, int ny, int nz, const uint8_t *act, double *cx,
                               double *cy, double *cz, double *d);

@@ -26,6 +26,15 @@
  * nIter x laplTyp is the image size.
  * A "morton job" sorts a list of block ids with MultiresSparseGrid::sortBlockListMorton
  * (src/msbg2.cpp:46-58): int32 bids[nBlocksIn] in, the sorted list out.
+ * A "solver job" runs the solver building blocks (multiplyLaplacianMatrixOpt,
+ * dotProdChannel, AXPBYChannelCombined, relaxBlockList) on the value blocks of a
+ * single-resolution layout: int32 bids[nBlocksIn], then float32 [nBlocksIn][bsx^3]
+ * arrays X, B, Q, P, CX, CY, CZ, DINV in; dt / rParticle = AXPBY a / b, nIter = relax
+ * passes, constr01 = reverse order.  Out: double dot(AX, X), dot(X, B), then A X,
+ * B - A X, X + aP, Q + bP and the relaxed X, each [nBlocksIn][bsx^3].
+ * A "downsample job" takes the halo job's input (FP32 only) and dumps
+ * downsampleFloatChannelNew to multigrid level 1 for every level-0 block (constr01 = 1:
+ * OPT_SIMPLE_AVERAGE): int32 bids[nActive], float32 [nActive][(bsx/2)^3].
  */
 #ifndef MSBG_ORACLE_COMMON_H
 #define MSBG_ORACLE_COMMON_H
@@ -37,7 +46,7 @@
 
 enum { ORACLE_CHAN_F32 = 0, ORACLE_CHAN_U16 = 1 };
 enum { ORACLE_JOB_SURFACE = 1, ORACLE_JOB_LEVELS = 2, ORACLE_JOB_INTERP = 3, ORACLE_JOB_HALO = 4,
-       ORACLE_JOB_RENDER = 5, ORACLE_JOB_MORTON = 6 };
+       ORACLE_JOB_RENDER = 5, ORACLE_JOB_MORTON = 6, ORACLE_JOB_SOLVER = 7, ORACLE_JOB_DOWNSAMPLE = 8 };
 
 /* Interp job option bits: the reference's own interpolation options (src/sbg.h:140-170)
  * plus one bit that the reference's enum leaves unused, for the render-density scale. */

@@ -309,3 +309,76 @@ def run_reference_levels(sx, sy, sz, bsx, n_levels, levels, timeout: float = 600
         subprocess.run([REF_DRIVER, jp, op], check=True, cwd=td, timeout=timeout,
                        stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
         return read_result(op, bsx, surface=False)
+
+
+JOB_SOLVER, JOB_DOWNSAMPLE = 7, 8
+
+
+def run_reference_solver(sx, sy, sz, bsx, bids, x, b, q, p, cx, cy, cz, d, a: float = 0.5,
+                         bcoef: float = -2.0, relax_passes: int = 1, reverse: bool = False,
+                         n_threads: int = 0, timeout: float = 600) -> dict:
+    """The reference's solver building blocks on the value blocks `bids` of a single-resolution
+    layout (src/msbg3.cpp:1756-1912, 2170-2369; src/msbg.cpp:4524-4768).  Every array is a
+    payload [n][bsx^3]; cx, cy, cz are the lower-face coefficients and d the diagonal (the job
+    stores 1/d in CH_DIAGONAL, as the reference's operator expects).  Returns the dots and
+    the arrays described in oracle_common.h."""
+    bids = np.ascontiguousarray(bids, np.int32).ravel()
+    n, nv = bids.size, bsx ** 3
+    dinv = (1.0 / np.asarray(d, np.float32)).astype(np.float32)
+    arrs = [np.ascontiguousarray(v, np.float32).reshape(n, nv) for v in (x, b, q, p, cx, cy, cz, dinv)]
+    with tempfile.TemporaryDirectory() as td:
+        jp, op = os.path.join(td, "job.bin"), os.path.join(td, "out.bin")
+        hdr = struct.pack(_JOB_FMT, JOB_MAGIC, JOB_SOLVER, sx, sy, sz, bsx, 3, CHAN_F32, relax_passes, 0,
+                          int(reverse), n_threads, a, bcoef, 0.0, 0.0, 0, 0, n)
+        with open(jp, "wb") as f:
+            f.write(hdr)
+            f.write(bids.tobytes())
+            for v in arrs:
+                f.write(v.tobytes())
+        r = subprocess.run([REF_DRIVER, jp, op], cwd=td, timeout=timeout,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference solver job failed with status {r.returncode}")
+        with open(op, "rb") as f:
+            buf = f.read()
+    hsz = struct.calcsize(_OUT_FMT)
+    h = struct.unpack(_OUT_FMT, buf[:hsz])
+    if h[0] != OUT_MAGIC:
+        raise ValueError("bad oracle output")
+    dots = np.frombuffer(buf, np.float64, 2, hsz)
+    off = hsz + 16
+    out = {"dot_ax_x": float(dots[0]), "dot_x_b": float(dots[1]), "dot_error": int(h[3])}
+    for name in ("ax", "residual", "axpby_x", "axpby_p", "relaxed"):
+        out[name] = np.frombuffer(buf, np.float32, n * nv, off).copy().reshape(n, nv)
+        off += 4 * n * nv
+    return out
+
+
+def run_reference_downsample(sx, sy, sz, bsx, n_levels, levels, states, payloads, simple_average=False,
+                             empty_value=0.0, full_value=1.0, timeout: float = 600):
+    """downsampleFloatChannelNew (src/msbg4.cpp:1035-1379) to multigrid level 1 of an FP32
+    multi-level channel given as the halo job's level states and payloads.
+
+    Returns (bids int32 [m] of the level-0 blocks, coarse float32 [m][(bsx/2)^3])."""
+    with tempfile.TemporaryDirectory() as td:
+        jp, op = os.path.join(td, "job.bin"), os.path.join(td, "out.bin")
+        write_halo_job(jp, sx, sy, sz, bsx, n_levels, CHAN_F32, levels, states, payloads, 0, 1,
+                       int(simple_average), empty_value, full_value)
+        with open(jp, "r+b") as f:  # the same layout under the downsample job type
+            f.seek(8)
+            f.write(struct.pack("<i", JOB_DOWNSAMPLE))
+        r = subprocess.run([REF_DRIVER, jp, op], cwd=td, timeout=timeout,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference downsample job failed with status {r.returncode}")
+        with open(op, "rb") as f:
+            buf = f.read()
+    hsz = struct.calcsize(_OUT_FMT)
+    h = struct.unpack(_OUT_FMT, buf[:hsz])
+    if h[0] != OUT_MAGIC:
+        raise ValueError("bad oracle output")
+    m = int(h[2])
+    nvc = (bsx // 2) ** 3
+    bids = np.frombuffer(buf, np.int32, m, hsz).copy()
+    vals = np.frombuffer(buf, np.float32, m * nvc, hsz + 4 * m).copy().reshape(m, nvc)
+    return bids, vals

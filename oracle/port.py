@@ -83,6 +83,8 @@ def lib():
         L.orc_morton64.restype = C.c_uint64
         L.orc_f32_to_f16.argtypes = [C.c_float]
         L.orc_f32_to_f16.restype = C.c_uint16
+        L.orc_relax_ref.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, P, P, P, P, C.c_int64,
+                                    C.c_int, C.c_int, C.c_int, C.c_float]
         L.orc_f16_to_f32.argtypes = [C.c_uint16]
         L.orc_f16_to_f32.restype = C.c_float
         _lib = L
@@ -374,6 +376,9 @@ def active_mask(bids: np.ndarray, nb, bs: int) -> np.ndarray:
 # coarsest level's red-black sweeps (0 = exact Cholesky solve), and the cell
 # count at which coarsening stops.
 MG_PRE, MG_POST, MG_TILE_ITERS, MG_COARSEST_ITER, MG_COARSEST_CELLS = 2, 2, 3, 0, 512
+# The reference's smoother constants (src/msbg.cpp:814-843): omega = 6/7 (as a float),
+# 5 block-local iterations.
+REF_SM_OMEGA, REF_SM_BLOCK_ITER = float(np.float32(6.0) / np.float32(7.0)), 5
 
 
 class PoissonProblem:
@@ -434,6 +439,19 @@ class PoissonProblem:
                                 _p(x), tol, max_iter, self.pre, self.post, self.k, self.coarsest_iter,
                                 self.coarsest_cells, C.byref(it), C.byref(rel))
         return x, it.value, rel.value
+
+    def relax_reference(self, x, b, passes=1, reverse=False, block_iter=REF_SM_BLOCK_ITER,
+                        omega=REF_SM_OMEGA, block_list=None):
+        """The reference's block smoother (orc_relax_ref) in FP32 on this problem's
+        coefficients: dense x, b in, relaxed dense x (float32) out."""
+        nz, ny, nx = self.act.shape
+        f = lambda a: np.ascontiguousarray(a, np.float32)
+        xx = f(np.where(self.act > 0, x, 0.0)).copy()
+        dinv = f(np.where(self.act > 0, 1.0 / np.where(self.act > 0, self.d.astype(np.float32), 1.0), 0.0))
+        bl = np.ascontiguousarray(self.bids if block_list is None else block_list, np.int32)
+        lib().orc_relax_ref(nx, ny, nz, self.bs, _p(xx), _p(f(b)), _p(f(self.cx)), _p(f(self.cy)),
+                            _p(f(self.cz)), _p(dinv), _p(bl), len(bl), passes, int(reverse), block_iter, omega)
+        return xx
 
     def rel_residual(self, x, b):
         r = self.apply(x, b)

@@ -12,8 +12,10 @@
  * library itself: MultiresSparseGrid::create, regularizeRefinementMap,
  * setRefinementMap, SparseGrid block management, applyChannelPdeFast<T>, the
  * trilinear interpolation functions (interp job), HaloBlockSet::fillHaloBlock_<T>
- * (halo job), the ray-march renderer RDR::RaymarchRenderer (render job) and
- * sortBlockListMorton (morton job).
+ * (halo job), the ray-march renderer RDR::RaymarchRenderer (render job),
+ * sortBlockListMorton (morton job), the solver building blocks
+ * multiplyLaplacianMatrixOpt / dotProdChannel / AXPBYChannelCombined / relaxBlockList
+ * (solver job) and downsampleFloatChannelNew (downsample job).
  *
  * Differences from the demo, both forced by the workload definition:
  *  - points come from the job file (already in voxel coordinates) instead of
@@ -513,6 +515,221 @@ int runMortonJob(const OracleJobHeader &job, const int32_t *bids, FILE *fout) {
   return 0;
 }
 
+
+// Loads one channel of a single-level grid: value blocks (bids) get their payload from
+// src ([n][bs^3]), every other block is the channel's constant empty block (value 0).
+template <typename T>
+void loadValueBlocks(SparseGrid<T> *sg, const std::vector<int32_t> &bids, const T *src, int nBlocks,
+                     T emptyValue) {
+  sg->reset();
+  sg->prepareDataAccess();
+  sg->setEmptyValue(emptyValue);
+  for (int b = 0; b < nBlocks; b++) sg->setEmptyBlock(b);
+  const size_t nv = (size_t)sg->nVoxelsInBlock();
+  for (size_t t = 0; t < bids.size(); t++) {
+    T *d = sg->getBlockDataPtr(bids[t], 1, 0);
+    if (src)
+      memcpy(d, src + t * nv, nv * sizeof(T));
+    else
+      for (size_t i = 0; i < nv; i++) d[i] = emptyValue;
+  }
+}
+
+template <typename T>
+void dumpValueBlocks(SparseGrid<T> *sg, const std::vector<int32_t> &bids, FILE *fout) {
+  const size_t nv = (size_t)sg->nVoxelsInBlock();
+  for (int32_t b : bids) fwrite(sg->getBlockDataPtr(b, 0, 0), sizeof(T), nv, fout);
+}
+
+// The solver building blocks of the reference on the value blocks of a single-resolution
+// layout (every block at level 0; blocks without payload are constant empty blocks, so
+// the operator sees Dirichlet 0 outside the value blocks):
+//   multiplyLaplacianMatrixOpt (src/msbg3.cpp:1756-1912): Y = A X with its dot product
+//     sum(Y X), and with OPT_CALC_RESIDUAL R = B - A X;
+//   dotProdChannel_ (src/msbg.cpp:4524-4646): sum(X B);
+//   AXPBYChannelCombined (src/msbg.cpp:4651-4768): X += a P; P = Q + b P;
+//   relaxBlockList (src/msbg3.cpp:2170-2239) run job.nIter times as relax() runs it
+//     (src/msbg3.cpp:2244-2369): red-black over blocks, _mgSmBlockIter block-local
+//     Gauss-Seidel iterations with omega = _mgSmOmega (src/msbg.cpp:814-843).
+// The release fills none of the solver's coefficient channels, so this job writes them:
+// the face-area channels hold the lower-face coefficients cx, cy, cz of every cell (read
+// because each value block is flagged BLK_CUTS_SOLID and each cell CELL_PARTIAL_SOLID),
+// CH_DIAGONAL the reciprocal of the diagonal (the operator multiplies by 1/D,
+// src/msbg3.cpp:1300-1302).  Inputs after the header: int32 bids[n], then float32
+// [n][bs^3] arrays X, B, Q, P, CX, CY, CZ, DINV.  Header: dt = a, rParticle = b,
+// nIter = relax passes, constr01 = 1 for the reverse order.
+int runSolverJob(const OracleJobHeader &job, const int32_t *bidsIn, const float *arrays, FILE *fout) {
+  OracleOutHeader out;
+  memset(&out, 0, sizeof(out));
+  memcpy(out.magic, ORACLE_OUT_MAGIC, 8);
+  MultiresSparseGrid *msbg =
+      MultiresSparseGrid::create("TEST", job.sx, job.sy, job.sz, job.bsx, -1, 0, -1, 0, NULL, NULL, 3);
+  if (!msbg) return 2;
+  const int nBlocks = msbg->nBlocks();
+  std::vector<int32_t> bids(bidsIn, bidsIn + job.nBlocksIn);
+  std::vector<char> isValue(nBlocks, 0);
+  for (int32_t b : bids) {
+    if (b < 0 || b >= nBlocks) return 4;
+    isValue[b] = 1;
+  }
+  std::vector<int> levels(nBlocks, 0);
+  msbg->setRefinementMap(levels.data(), NULL, 0, NULL, false, false);
+  const size_t nv = (size_t)job.bsx * job.bsx * job.bsx, na = bids.size() * nv;
+  const float *X = arrays, *B = X + na, *Q = B + na, *P = Q + na, *CX = P + na, *CY = CX + na,
+              *CZ = CY + na, *DI = CZ + na;
+  using MSBG::CH_PRESSURE;
+  using MSBG::CH_DIVERGENCE;
+  using MSBG::CH_CG_P;
+  using MSBG::CH_CG_Q;
+  using MSBG::CH_DIAGONAL;
+  SparseGrid<PSFloat> *sgX = msbg->getPSFloatChannel(CH_PRESSURE, 0, 0),
+                      *sgB = msbg->getPSFloatChannel(CH_DIVERGENCE, 0, 0),
+                      *sgP = msbg->getPSFloatChannel(CH_CG_P, 0, 0),
+                      *sgQ = msbg->getPSFloatChannel(CH_CG_Q, 0, 0),
+                      *sgD = msbg->getPSFloatChannel(CH_DIAGONAL, 0, 0);
+  if (!sgX || !sgB || !sgP || !sgQ || !sgD) return 3;
+  loadValueBlocks<float>(sgD, bids, DI, nBlocks, 0.f);
+  for (int k = 0; k < 3; k++) {
+    SparseGrid<float> *fa = msbg->getFaceAreaChannel(k, 0, 0);
+    if (!fa) return 3;
+    loadValueBlocks<float>(fa, bids, k == 0 ? CX : k == 1 ? CY : CZ, nBlocks, 0.f);
+  }
+  {
+    SparseGrid<MSBG::CellFlags> *sgF = msbg->getFlagsChannel(MSBG::CH_CELL_FLAGS, 0, 0);
+    if (!sgF) return 3;
+    sgF->reset();
+    sgF->prepareDataAccess();
+    sgF->setEmptyValue(MSBG::CELL_EMPTY_VAL);
+    for (int b = 0; b < nBlocks; b++) sgF->setEmptyBlock(b);
+    for (int32_t b : bids) {
+      MSBG::CellFlags *f = sgF->getBlockDataPtr(b, 1, 0);
+      for (size_t i = 0; i < nv; i++) f[i] = MSBG::CELL_PARTIAL_SOLID;
+    }
+  }
+  for (int b = 0; b < nBlocks; b++) {
+    MSBG::BlockInfo *bi = msbg->getBlockInfo(b, 0);
+    if (isValue[b]) {
+      bi->flags &= ~(MSBG::BLK_NO_FLUID | MSBG::BLK_FIXED | MSBG::BLK_ONLY_FLUID);
+      bi->flags |= MSBG::BLK_CUTS_SOLID;
+    } else {
+      bi->flags |= MSBG::BLK_NO_FLUID;
+    }
+  }
+  std::vector<int> list(bids.begin(), bids.end());
+  auto loadXB = [&]() {
+    loadValueBlocks<float>(sgX, bids, X, nBlocks, 0.f);
+    loadValueBlocks<float>(sgB, bids, B, nBlocks, 0.f);
+  };
+  const double t0 = nowSec();
+  // Y = A X (into CG_Q) with sum(Y X)
+  loadXB();
+  loadValueBlocks<float>(sgQ, bids, nullptr, nBlocks, 0.f);
+  long double dotYX = 0;
+  msbg->multiplyLaplacianMatrixOpt(0, 0, CH_PRESSURE, CH_DIVERGENCE, 0.f, CH_CG_Q, &dotYX, &list);
+  std::vector<float> Y(na), R(na);
+  for (size_t t = 0; t < bids.size(); t++) memcpy(&Y[t * nv], sgQ->getBlockDataPtr(bids[t], 0, 0), nv * 4);
+  // R = B - A X (into CG_Q)
+  msbg->multiplyLaplacianMatrixOpt(MSBG::OPT_CALC_RESIDUAL, 0, CH_PRESSURE, CH_DIVERGENCE, 0.f, CH_CG_Q, NULL,
+                                   &list);
+  for (size_t t = 0; t < bids.size(); t++) memcpy(&R[t * nv], sgQ->getBlockDataPtr(bids[t], 0, 0), nv * 4);
+  int err = 0;
+  const long double dotXB = msbg->dotProdChannel(CH_PRESSURE, CH_DIVERGENCE, 0, &list, &err);
+  // X += a P; P = Q + b P
+  loadValueBlocks<float>(sgQ, bids, Q, nBlocks, 0.f);
+  loadValueBlocks<float>(sgP, bids, P, nBlocks, 0.f);
+  msbg->AXPBYChannelCombined(job.dt, job.rParticle, CH_CG_Q, CH_PRESSURE, CH_CG_P, &list);
+  std::vector<float> Xa(na), Pa(na);
+  for (size_t t = 0; t < bids.size(); t++) {
+    memcpy(&Xa[t * nv], sgX->getBlockDataPtr(bids[t], 0, 0), nv * 4);
+    memcpy(&Pa[t * nv], sgP->getBlockDataPtr(bids[t], 0, 0), nv * 4);
+  }
+  // relax: nIter passes of relaxBlockList in place, as relax() does
+  loadXB();
+  const unsigned ropt = MSBG::OPT_JACOBI | (job.constr01 ? MSBG::OPT_REVERSE_ORDER : 0);
+  for (int it = 0; it < job.nIter; it++) msbg->relaxBlockList(&list, 0, it, CH_PRESSURE, CH_DIVERGENCE, ropt, CH_PRESSURE);
+  out.tPdeSec = nowSec() - t0;
+  out.nBlocks = nBlocks;
+  out.nActive = (int)bids.size();
+  out.elemBytes = 4;
+  out.nThreadsUsed = omp_get_max_threads();
+  out.nActParticles = err;
+  fwrite(&out, sizeof(out), 1, fout);
+  const double dots[2] = {(double)dotYX, (double)dotXB};
+  fwrite(dots, 8, 2, fout);
+  fwrite(Y.data(), 4, na, fout);
+  fwrite(R.data(), 4, na, fout);
+  fwrite(Xa.data(), 4, na, fout);
+  fwrite(Pa.data(), 4, na, fout);
+  dumpValueBlocks<float>(sgX, bids, fout);
+  MultiresSparseGrid::destroy(msbg);
+  return 0;
+}
+
+// downsampleFloatChannelNew (src/msbg4.cpp:1035-1379) to multigrid level 1 on a
+// multi-level grid loaded like the halo job (channel CH_FLOAT_1, every resolution level
+// with the job's block states and payloads; job.laplTyp = 0).  constr01 = 1 adds
+// OPT_SIMPLE_AVERAGE.  For every block of the level map at level 0 (the blocks the
+// function restricts from finer data) the output holds its level-1 block of the
+// destination channel CH_FLOAT_2, (bsx/2)^3 floats.
+int runDownsampleJob(const OracleJobHeader &job, const int32_t *levelsIn, const int32_t *state,
+                     const std::vector<std::vector<uint8_t>> &pay, FILE *fout) {
+  OracleOutHeader out;
+  memset(&out, 0, sizeof(out));
+  memcpy(out.magic, ORACLE_OUT_MAGIC, 8);
+  const int chan = MSBG::CH_FLOAT_1, chDst = MSBG::CH_FLOAT_2;
+  MultiresSparseGrid *msbg = MultiresSparseGrid::create(
+      "TEST", job.sx, job.sy, job.sz, job.bsx, -1, 0, -1, 0, NULL, NULL, job.nLevels);
+  if (!msbg) return 2;
+  const int nBlocks = msbg->nBlocks();
+  if ((int64_t)nBlocks != job.nBlocksIn) return 4;
+  std::vector<int> levels(levelsIn, levelsIn + nBlocks);
+  msbg->regularizeRefinementMap(levels.data());
+  for (int b = 0; b < nBlocks; b++)
+    if (levels[b] != levelsIn[b]) return 5;
+  msbg->setRefinementMap(levels.data(), NULL, -1, NULL, false, false);
+  for (int l = 0; l < job.nLevels; l++) {
+    SparseGrid<float> *sg = MSBG::getChannel<float>(msbg, chan, l);
+    if (!sg) return 3;
+    sg->reset();
+    sg->prepareDataAccess();
+    sg->setEmptyValue(job.dt);
+    sg->setFullValue(job.rParticle);
+    const size_t nv = (size_t)sg->nVoxelsInBlock();
+    const int32_t *st = state + (size_t)l * nBlocks;
+    const float *src = reinterpret_cast<const float *>(pay[l].data());
+    for (int b = 0; b < nBlocks; b++) {
+      if (st[b] >= 0)
+        memcpy(sg->getBlockDataPtr(b, 1, 0), src + (size_t)st[b] * nv, nv * sizeof(float));
+      else if (st[b] == -1)
+        sg->setEmptyBlock(b);
+      else if (st[b] == -2)
+        sg->setFullBlock(b);
+    }
+  }
+  const unsigned opt = MSBG::OPT_ALL_CELLS | (job.constr01 ? MSBG::OPT_SIMPLE_AVERAGE : 0);
+  const double t0 = nowSec();
+  msbg->downsampleFloatChannelNew(1, chan, chDst, opt);
+  out.tPdeSec = nowSec() - t0;
+  std::vector<int32_t> bids;
+  for (int b = 0; b < nBlocks; b++)
+    if (levels[b] == 0) bids.push_back(b);
+  SparseGrid<float> *dst = MSBG::getChannel<float>(msbg, chDst, 1, 1);
+  if (!dst) return 3;
+  const size_t nvc = (size_t)dst->nVoxelsInBlock();
+  out.nBlocks = nBlocks;
+  out.nActive = (int)bids.size();
+  out.elemBytes = 4;
+  out.nThreadsUsed = omp_get_max_threads();
+  fwrite(&out, sizeof(out), 1, fout);
+  fwrite(bids.data(), 4, bids.size(), fout);
+  for (int32_t b : bids) {
+    if (!dst->isValueBlock(b)) return 6;
+    fwrite(dst->getBlockDataPtr(b, 0, 0), 4, nvc, fout);
+  }
+  MultiresSparseGrid::destroy(msbg);
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -534,7 +751,13 @@ int main(int argc, char **argv) {
   std::vector<uint8_t> payload;
   std::vector<int32_t> state;
   std::vector<std::vector<uint8_t>> levelPay;
-  if (job.jobType == ORACLE_JOB_HALO) {
+  std::vector<float> solverArrays;
+  if (job.jobType == ORACLE_JOB_SOLVER) {
+    solverArrays.resize((size_t)8 * job.nBlocksIn * job.bsx * job.bsx * job.bsx);
+    if (!solverArrays.empty() && fread(solverArrays.data(), 4, solverArrays.size(), fin) != solverArrays.size())
+      return 1;
+  }
+  if (job.jobType == ORACLE_JOB_HALO || job.jobType == ORACLE_JOB_DOWNSAMPLE) {
     const size_t elem = job.chanType == ORACLE_CHAN_U16 ? 2 : 4;
     state.resize((size_t)job.nLevels * job.nBlocksIn);
     if (fread(state.data(), 4, state.size(), fin) != state.size()) return 1;
@@ -567,6 +790,10 @@ int main(int argc, char **argv) {
   int rc;
   if (job.jobType == ORACLE_JOB_LEVELS)
     rc = runLevelsJob(job, lv.data(), fout);
+  else if (job.jobType == ORACLE_JOB_SOLVER)
+    rc = runSolverJob(job, lv.data(), solverArrays.data(), fout);
+  else if (job.jobType == ORACLE_JOB_DOWNSAMPLE)
+    rc = job.chanType == ORACLE_CHAN_F32 ? runDownsampleJob(job, lv.data(), state.data(), levelPay, fout) : 7;
   else if (job.jobType == ORACLE_JOB_MORTON)
     rc = runMortonJob(job, lv.data(), fout);
   else if (job.jobType == ORACLE_JOB_RENDER)

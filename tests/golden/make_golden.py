@@ -11,8 +11,12 @@ never on the GPU host; the .npz files it writes are committed.
 
 It writes reference_small.npz (splat, levels, sweeps), reference_interp.npz
 (trilinear interpolation), reference_halo.npz (cross-resolution halo fill),
-reference_render.npz (ray-march render) and reference_morton.npz (Morton-ordered block
-lists).
+reference_render.npz (ray-march render), reference_morton.npz (Morton-ordered block
+lists), reference_solver.npz (the solver building blocks and the block smoother),
+reference_downsample.npz (downsampleFloatChannelNew on multi-level channels) and
+reference_surface512.npz (the 512^3 surface workload at full size: layout, counters,
+per-block sums and a voxel sample of the fields).  Arguments name a subset
+(small interp halo render morton solver downsample surface512).
 """
 from __future__ import annotations
 
@@ -56,9 +60,29 @@ SWEEP_CASES = [
 ]
 
 
-def main() -> None:
+def main(which: list[str]) -> None:
     if not O.ref_available():
         raise SystemExit("oracle/_ref/msbg_ref_driver missing: run `make -C oracle ref` first")
+    parts = set(which) or {"small", "interp", "halo", "render", "morton", "solver", "downsample", "surface512"}
+    if parts & {"small", "interp", "render"}:
+        out = make_small()
+        if "interp" in parts:
+            make_interp(out)
+        if "render" in parts:
+            make_render(out)
+    if "halo" in parts:
+        make_halo()
+    if "morton" in parts:
+        make_morton()
+    if "solver" in parts:
+        make_solver()
+    if "downsample" in parts:
+        make_downsample()
+    if "surface512" in parts:
+        make_surface512()
+
+
+def make_small() -> dict:
     pts = golden_points()
     out = {"points": pts, "res": np.int32(RES), "bsx": np.int32(BSX)}
     for name, chan, lt, it, dt, al in SWEEP_CASES:
@@ -107,10 +131,7 @@ def main() -> None:
     path = os.path.join(HERE, "reference_small.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
-    make_interp(out)
-    make_halo()
-    make_render(out)
-    make_morton()
+    return out
 
 
 IP_OPTS = (0, O.IP_CORNER, O.IP_BC_DIRICHLET, O.IP_BC_DIRICHLET_OLD, O.IP_CORNER | O.IP_BC_DIRICHLET,
@@ -232,5 +253,79 @@ def make_morton() -> None:
     print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
 
 
+def make_solver() -> None:
+    """The reference's multiplyLaplacianMatrixOpt (Y = A X with sum(Y X), and B - A X),
+    dotProdChannel, AXPBYChannelCombined and relax (relaxBlockList passes) on the seeded cases
+    of tests/solver_cases.py (oracle/ref_driver.cpp, solver job)."""
+    import port as P
+    import solver_cases as S
+    out = {}
+    for name, res, bs, nblk, seed in S.SOLVER_CASES:
+        bids, nb, prob, (x, b, q, p) = S.solver_case(P, res, bs, nblk, seed)
+        coef = [prob.payload(v).astype(np.float32) for v in (prob.cx, prob.cy, prob.cz, prob.d)]
+        for k, (passes, rev) in enumerate(S.RELAX_RUNS):
+            r = O.run_reference_solver(res, res, res, bs, bids, x, b, q, p, *coef, a=S.AXPBY_A, bcoef=S.AXPBY_B,
+                                       relax_passes=passes, reverse=rev)
+            if k == 0:
+                for key in ("ax", "residual", "axpby_x", "axpby_p"):
+                    out[f"{name}_{key}"] = r[key]
+                out[f"{name}_dots"] = np.array([r["dot_ax_x"], r["dot_x_b"]])
+            out[f"{name}_relaxed_{passes}_{int(rev)}"] = r["relaxed"]
+    path = os.path.join(HERE, "reference_solver.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
+
+
+def make_downsample() -> None:
+    """downsampleFloatChannelNew to multigrid level 1 (oracle/ref_driver.cpp, downsample job)
+    of seeded 3-level FP32 channels, 4^3 Gauss-like weights and OPT_SIMPLE_AVERAGE."""
+    import halo_cases as H
+    import port as P
+    out = {}
+    for nb, bsx, seed in H.DOWNSAMPLE_CASES:
+        lv, st, pay = H.halo_case(nb, bsx, 3, seed, "f32", lambda *a: P.regularize(*a)[0])
+        key = "x".join(map(str, nb)) + f"_bs{bsx}"
+        for simple in (False, True):
+            bids, vals = O.run_reference_downsample(*(n * bsx for n in nb), bsx, 3, lv, st, pay, simple,
+                                                    H.DOWNSAMPLE_EMPTY, H.DOWNSAMPLE_FULL)
+            out[f"{key}_bids"] = bids
+            out[f"{key}_{'mean' if simple else 'gauss'}"] = vals
+    path = os.path.join(HERE, "reference_downsample.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
+
+
+SURFACE512_SAMPLE = 60000
+
+
+def make_surface512() -> None:
+    """The 512^3 surface workload at full size (64 spheres x 32,000 points, bs 16, 20 MCF
+    iterations, dt 0.1) through the reference, FP32 and uint16: active blocks, levels, flags,
+    particle counts, per-block sums of the finalized and swept fields, and a seeded sample of
+    their voxels (the full fields are 50 MB each)."""
+    from msbg_gb300 import workloads as W
+    spec = W.SURFACE_512
+    pts = W.make_points(spec, 1)
+    res, bsx = spec["res"], spec["bsx"]
+    out = {}
+    for name, chan in (("f32", O.CHAN_F32), ("u16", O.CHAN_U16)):
+        r = O.run_reference_surface(O.SurfaceJob(res, res, res, bsx, pts, chan=chan, n_iter=spec["n_iter"],
+                                                 dt=spec["dt"]), timeout=3600)
+        if "active_bids" not in out:
+            out.update(active_bids=r.active_bids, levels=r.levels, flags=r.flags,
+                       n_act_particles=np.int64(r.n_act_particles))
+            rng = np.random.Generator(np.random.PCG64(20261203 + 970))
+            out["sample_index"] = np.sort(rng.choice(r.after_pde.size, SURFACE512_SAMPLE, replace=False))
+        else:
+            assert np.array_equal(out["active_bids"], r.active_bids)
+        idx = out["sample_index"]
+        for stage, field in (("final", r.after_finalize), ("pde", r.after_pde)):
+            out[f"{name}_{stage}_block_sums"] = field.astype(np.float64).sum(axis=1)
+            out[f"{name}_{stage}_sample"] = field.reshape(-1)[idx]
+    path = os.path.join(HERE, "reference_surface512.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
+
+
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -17,6 +17,12 @@ import numpy as np
 
 LBLK_EMPTY, LBLK_FULL, LBLK_NONE = -1, -2, -3
 
+# restriction fixtures (downsampleFloatChannelNew): (block grid, block edge, seed), and the
+# constant blocks' values
+DOWNSAMPLE_CASES = (((4, 4, 4), 16, 20261203 + 960), ((5, 3, 4), 8, 20261203 + 961),
+                    ((3, 3, 2), 32, 20261203 + 962))
+DOWNSAMPLE_EMPTY, DOWNSAMPLE_FULL = 0.25, 0.75
+
 
 def halo_case(nb, bsx: int, n_levels: int, seed: int, kind: str, regularize):
     """kind: 'f32' | 'u16' | 'f16'; regularize(levels, nbx, nby, nbz, n_levels) -> levels."""

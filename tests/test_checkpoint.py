@@ -55,7 +55,7 @@ def _grid(G):
     g.setRefinementMap(1.0)
     g.splat(d, len(pts), 2.0, 2.0)
     g.splat_finalize(2.0, 2.0)
-    g.applyChannelPdeFast(0, G.LAPL_MCF_8COLOR, 1, 4, 0.1, 0.0, G.SWEEP_FAST)
+    g.applyChannelPdeFast(0, laplTyp=G.LAPL_MCF_8COLOR, doConstrZeroOne=1, numIter=4, timeStep=0.1, variant=G.SWEEP_FAST)
     d.free()
     g.channel_create(3, G.F32)
     g.upload_payload(np.random.default_rng(3).standard_normal(
@@ -88,7 +88,7 @@ def test_gpu_save_load_round_trip(gpulib, tmp_path):
                 assert np.array_equal(raw.view(np.uint8), a.view(np.uint8))
             # the restored grid continues exactly as the original
             for x in (g, h):
-                x.applyChannelPdeFast(0, G.LAPL_MCF_8COLOR, 1, 2, 0.1, 0.0, G.SWEEP_FAST)
+                x.applyChannelPdeFast(0, laplTyp=G.LAPL_MCF_8COLOR, doConstrZeroOne=1, numIter=2, timeStep=0.1, variant=G.SWEEP_FAST)
             assert np.array_equal(g.payload(0).view(np.uint16), h.payload(0).view(np.uint16))
         finally:
             h.close()

@@ -75,7 +75,7 @@ def test_relax_tiles(setup, reverse):
     x, b = _rand(prob, rng).astype(np.float32), _rand(prob, rng).astype(np.float32)
     g.upload_payload(prob.payload(x), CH_X)
     g.upload_payload(prob.payload(b), CH_B)
-    g.relax(CH_X, CH_B, 2, reverseOrder=reverse)
+    g.relax_tiles(CH_X, CH_B, 2, reverseOrder=reverse)
     want = prob.smooth(x, b, 2, reverse=reverse)
     assert rel_l2(prob.dense(g.payload(CH_X)), want) < 1e-5
 

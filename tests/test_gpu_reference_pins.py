@@ -1,0 +1,207 @@
+"""The GPU against fixtures made by the reference itself, and the block-list forms of the
+reference's calls.
+
+* Solver building blocks (reference_solver.npz): msbg_gpu_multiply_laplacian (Y = A X and its
+  dot sum(Y X), B - A X), msbg_gpu_dot, msbg_gpu_axpby_combined and msbg_gpu_relax (the
+  reference's block smoother) against multiplyLaplacianMatrixOpt, dotProdChannel,
+  AXPBYChannelCombined and relax() run by the reference: rel-L2 1e-6 (the reference keeps
+  1/diagonal and builds with -ffast-math), dots within 1e-6 relative.  The smoother is also bit
+  for bit against the CPU restatement, whose operation order it follows.
+* Block lists: a listed call touches only the listed value blocks, and equals the whole-layout
+  call there; sweeps with a list equal the restatement's sweeps of that list bit for bit.
+* downsampleFloatChannelNew on multi-level channels (reference_downsample.npz): bit for bit.
+* The 512^3 surface workload at full size (reference_surface512.npz): active set, levels,
+  flags and particle counts bit for bit; FP32 field sums and voxel sample within rel-L2 1e-5
+  for the EXACT and FAST sweep variants; the uint16 sample within 8 quanta.
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, rel_l2
+from msbg_gb300 import workloads as W
+
+import halo_cases as H
+import solver_cases as S
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(ROOT, "tests", "golden")
+CH_X, CH_B, CH_Q, CH_P, CH_Y, CH_CX, CH_CY, CH_CZ, CH_D = range(1, 10)
+
+
+@pytest.fixture(scope="module")
+def solver_gold():
+    return dict(np.load(os.path.join(GOLD, "reference_solver.npz")))
+
+
+def _solver_grid(G, res, bs, bids):
+    nb3 = (res // bs) ** 3
+    g = G.MultiresSparseGrid(res, res, res, bs, 3, G.F32)
+    lv = np.full(nb3, 2, np.int32)
+    lv[bids] = 0
+    g.set_levels(lv)
+    g.setRefinementMap(0.0)
+    for c in range(CH_X, CH_D + 1):
+        g.channel_create(c, G.F32)
+    g.poisson_procedural_coefficients(S.COEFF_SEED, CH_CX, CH_CY, CH_CZ, CH_D)
+    assert np.array_equal(g.active_blocks(), bids)
+    return g
+
+
+@pytest.mark.parametrize("case", S.SOLVER_CASES, ids=[c[0] for c in S.SOLVER_CASES])
+def test_solver_blocks_match_reference(gpulib, port, solver_gold, case):
+    G = gpulib
+    name, res, bs, nblk, seed = case
+    bids, nb, prob, (x, b, q, p) = S.solver_case(port, res, bs, nblk, seed)
+    g = _solver_grid(G, res, bs, bids)
+    try:
+        g.upload_payload(x, CH_X)
+        g.upload_payload(b, CH_B)
+        dyx = g.multiplyLaplacianMatrixOpt(0, 0, CH_X, CH_B, 0.0, CH_Y, withDotprod=True)
+        assert rel_l2(g.payload(CH_Y), solver_gold[f"{name}_ax"]) < 1e-6
+        dots = solver_gold[f"{name}_dots"]
+        assert abs(dyx - dots[0]) <= 1e-6 * abs(dots[0])
+        g.multiplyLaplacianMatrixOpt(G.OPT_CALC_RESIDUAL, 0, CH_X, CH_B, 0.0, CH_Y)
+        assert rel_l2(g.payload(CH_Y), solver_gold[f"{name}_residual"]) < 1e-6
+        assert abs(g.dotProdChannel(CH_X, CH_B) - dots[1]) <= 1e-9 * abs(dots[1])
+        g.upload_payload(q, CH_Q)
+        g.upload_payload(p, CH_P)
+        g.AXPBYChannelCombined(S.AXPBY_A, S.AXPBY_B, CH_Q, CH_X, CH_P)
+        assert rel_l2(g.payload(CH_X), solver_gold[f"{name}_axpby_x"]) < 1e-7
+        assert rel_l2(g.payload(CH_P), solver_gold[f"{name}_axpby_p"]) < 1e-7
+        for passes, rev in S.RELAX_RUNS:
+            g.upload_payload(x, CH_X)
+            g.relax(0, int(rev), 0, CH_X, CH_B, G.CH_NULL, passes)
+            got = g.payload(CH_X)
+            assert rel_l2(got, solver_gold[f"{name}_relaxed_{passes}_{int(rev)}"]) < 1e-6
+            want = prob.payload(prob.relax_reference(prob.dense(x), prob.dense(b), passes=passes, reverse=rev))
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (passes, rev)
+    finally:
+        g.close()
+
+
+def test_block_lists_touch_only_listed_blocks(gpulib, port):
+    G = gpulib
+    name, res, bs, nblk, seed = S.SOLVER_CASES[0]
+    bids, nb, prob, (x, b, q, p) = S.solver_case(port, res, bs, nblk, seed)
+    g = _solver_grid(G, res, bs, bids)
+    try:
+        pick = np.array([0, 3, 5], np.int64)
+        sub = bids[pick]
+        listed = np.isin(bids, sub)
+        g.upload_payload(x, CH_X)
+        g.upload_payload(b, CH_B)
+        g.multiplyLaplacianMatrix(CH_X, CH_B, CH_Y)
+        full = g.payload(CH_Y)
+        sentinel = np.full_like(x, 7.0)
+        g.upload_payload(sentinel, CH_Y)
+        dyx = g.multiplyLaplacianMatrixOpt(0, 0, CH_X, CH_B, 0.0, CH_Y, withDotprod=True, blockList=sub)
+        y = g.payload(CH_Y)
+        assert np.array_equal(y[~listed], sentinel[~listed])
+        assert rel_l2(y[listed], full[listed]) < 1e-6
+        assert abs(dyx - float((y[listed].astype(np.float64) * x[listed]).sum())) <= 1e-9 * abs(dyx) + 1e-12
+        # a listed block without payload is skipped; an id outside the grid is an error
+        nb3 = (res // bs) ** 3
+        empty_bid = int(np.setdiff1d(np.arange(nb3), bids)[0])
+        d_xb = g.dotProdChannel(CH_X, CH_B, 0, np.append(sub, empty_bid))
+        assert abs(d_xb - float((x[listed].astype(np.float64) * b[listed]).sum())) <= 1e-9 * abs(d_xb)
+        with pytest.raises(G.MsbgGpuError) as e:
+            g.dotProdChannel(CH_X, CH_B, 0, np.array([nb3 + 5], np.int32))
+        assert e.value.code == G.ERR_ARG
+        g.upload_payload(q, CH_Q)
+        g.upload_payload(p, CH_P)
+        g.AXPBYChannel(0.5, CH_Q, 2.0, CH_P, 9999, 0, sub)
+        pp = g.payload(CH_P)
+        assert np.array_equal(pp[~listed], p[~listed])
+        assert rel_l2(pp[listed], 0.5 * q[listed].astype(np.float64) + 2.0 * p[listed]) < 1e-7
+        # the block smoother on a sub-list equals the restatement's on that list
+        g.relax(0, 0, 0, CH_X, CH_B, G.CH_NULL, 1, blockList=sub)
+        want = prob.payload(prob.relax_reference(prob.dense(x), prob.dense(b), passes=1, block_list=sub))
+        assert np.array_equal(g.payload(CH_X).view(np.uint32), want.view(np.uint32))
+    finally:
+        g.close()
+
+
+@pytest.mark.parametrize("storage", ["f32", "u16"])
+@pytest.mark.parametrize("lapl", ["mcf8", "jacobi_rb", "jacobi_pp"])
+def test_sweeps_with_a_block_list_match_restatement(gpulib, port, golden, storage, lapl):
+    """applyChannelPdeFast with a block list (the demo passes &activeBlocks): here every third
+    value block of the golden layout; the EXACT variant equals the restatement sweeping the
+    same list bit for bit, and unlisted blocks keep their values."""
+    G, P = gpulib, port
+    lt = {"mcf8": -(4 + G.OPT_8_COLOR_SCHEME), "jacobi_rb": -17, "jacobi_pp": 17}[lapl]
+    st = {"f32": (G.F32, P.F32), "u16": (G.U16, P.U16)}[storage]
+    pts, res, bsx = golden["points"], int(golden["res"]), int(golden["bsx"])
+    r = G.surface_pipeline(pts, res, bsx, storage=st[0], n_iter=0)
+    bids = r["active_bids"]
+    sub = bids[::3]
+    init = r["after_finalize"]
+    g = G.MultiresSparseGrid(res, res, res, bsx, 3, st[0])
+    try:
+        nb3 = (res // bsx) ** 3
+        lv = np.full(nb3, 2, np.int32)
+        lv[bids] = 0
+        g.set_levels(lv)
+        g.setRefinementMap(0.0)
+        g.upload_payload(init, 0)
+        g.applyChannelPdeFast(0, blockList=sub, laplTyp=lt, doConstrZeroOne=1, numIter=3, timeStep=0.1)
+        got = g.payload(0)
+    finally:
+        g.close()
+    og = P.grid(res, res, res, bsx, st[1])
+    slot = np.full(nb3, -1, np.int32)
+    slot[bids] = np.arange(len(bids), dtype=np.int32)
+    want = np.ascontiguousarray(init).copy()
+    # ping-pong: the second buffer starts as a copy, so unlisted blocks read their values there
+    P.pde(og, slot, np.ascontiguousarray(sub, np.int32), want, lt, 1, 3, 0.1, tmp=want.copy() if lt > 0 else None)
+    assert np.array_equal(got.view(np.uint16 if storage == "u16" else np.uint32),
+                          want.view(np.uint16 if storage == "u16" else np.uint32))
+    unlisted = ~np.isin(bids, sub)
+    assert np.array_equal(got[unlisted], init[unlisted])
+
+
+def test_restriction_matches_reference_fixture(gpulib, port):
+    G = gpulib
+    gold = dict(np.load(os.path.join(GOLD, "reference_downsample.npz")))
+    for nb, bsx, seed in H.DOWNSAMPLE_CASES:
+        lv, st, pay = H.halo_case(nb, bsx, 3, seed, "f32", lambda *a: port.regularize(*a)[0])
+        key = "x".join(map(str, nb)) + f"_bs{bsx}"
+        g = G.MultiresSparseGrid(nb[0] * bsx, nb[1] * bsx, nb[2] * bsx, bsx, 3, G.F32)
+        try:
+            g.set_levels(lv)
+            g.setRefinementMap(0.0)
+            for l in range(3):
+                g.level_grid_set(0, l, G.F32, st[l], pay[l] if len(pay[l]) else None, H.DOWNSAMPLE_EMPTY,
+                                 H.DOWNSAMPLE_FULL)
+            bids = gold[f"{key}_bids"]
+            for mode, simple in (("gauss", False), ("mean", True)):
+                out, sk = g.restrict_level_blocks(0, 0, bids, simple)
+                assert sk == 0
+                assert np.array_equal(out.view(np.uint32), gold[f"{key}_{mode}"].view(np.uint32)), (key, mode)
+        finally:
+            g.close()
+
+
+@pytest.mark.parametrize("storage,variant", [("f32", "exact"), ("f32", "fast"), ("u16", "exact")])
+def test_surface512_full_size_matches_reference(gpulib, storage, variant):
+    G = gpulib
+    gold = dict(np.load(os.path.join(GOLD, "reference_surface512.npz")))
+    spec = W.SURFACE_512
+    pts = W.make_points(spec, 1)
+    r = G.surface_pipeline(pts, spec["res"], spec["bsx"], storage={"f32": G.F32, "u16": G.U16}[storage],
+                           n_iter=spec["n_iter"], dt=spec["dt"],
+                           variant={"exact": G.SWEEP_EXACT, "fast": G.SWEEP_FAST}[variant])
+    assert np.array_equal(r["active_bids"], gold["active_bids"])
+    assert np.array_equal(r["levels"], gold["levels"]) and np.array_equal(r["flags"], gold["flags"])
+    assert r["info"].nActParticles == int(gold["n_act_particles"])
+    idx = gold["sample_index"]
+    for stage, field in (("final", r["after_finalize"]), ("pde", r["after_pde"])):
+        if storage == "f32":
+            assert rel_l2(field.astype(np.float64).sum(1), gold[f"f32_{stage}_block_sums"]) < 1e-5
+            assert rel_l2(field.reshape(-1)[idx], gold[f"f32_{stage}_sample"]) < 1e-5
+        else:
+            d = np.abs(field.reshape(-1)[idx].astype(np.int64) - gold[f"u16_{stage}_sample"].astype(np.int64))
+            assert d.max() <= 8

@@ -45,7 +45,8 @@ def _gpu_pipeline(gpulib, pts, res, bsx, storage, n_iter, lapl_typ, dt, alpha=0.
         g.splat_finalize(2.0, 2.0)
         fin = g.payload(0)
         if n_iter:
-            g.applyChannelPdeFast(0, lapl_typ, constr01, n_iter, dt, alpha, variant)
+            g.applyChannelPdeFast(0, laplTyp=lapl_typ, doConstrZeroOne=constr01, numIter=n_iter, timeStep=dt,
+                                  anisDiffAlpha=alpha, variant=variant)
         out = dict(levels=g.levels(), flags=g.flags(), bids=g.active_blocks(), final=fin,
                    pde=g.payload(0), info=g.info(), launches=g.launch_count())
         d.free()
@@ -216,7 +217,7 @@ def test_gpu_error_codes(gpulib):
     g = G.MultiresSparseGrid(64, 64, 64, 16, 3, G.F32, capacity_blocks=2)
     try:
         with pytest.raises(G.MsbgGpuError) as e:
-            g.applyChannelPdeFast(0, MCF8, 1, 2, 0.1)
+            g.applyChannelPdeFast(0, laplTyp=MCF8, doConstrZeroOne=1, numIter=2, timeStep=0.1)
         assert e.value.code == G.ERR_STATE
         pts = W.sphere_cloud(64, 2, 2000, seed=5, radius_range=(0.15, 0.2))
         d = g.to_device(pts)
@@ -233,7 +234,7 @@ def test_gpu_error_codes(gpulib):
         g.set_levels(np.zeros(64, np.int32))
         g.setRefinementMap(0.5)
         with pytest.raises(G.MsbgGpuError) as e:
-            g.applyChannelPdeFast(0, -(2 + OPT8), 1, 2, 0.1)
+            g.applyChannelPdeFast(0, laplTyp=-(2 + OPT8), doConstrZeroOne=1, numIter=2, timeStep=0.1)
         assert e.value.code == G.ERR_UNSUPPORTED
         with pytest.raises(G.MsbgGpuError) as e:
             g.set_levels(np.full(64, 7, np.int32))
