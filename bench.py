@@ -406,7 +406,7 @@ def run_gpu(args, spec, dist: Dist):
         e2e_steps = max(1, min(args.steps, 3))
         b = np.asarray(bands, np.float32) if bands else None
         n_act_out = C.c_int64()
-        gpu_times = []
+        gpu_times, stage_runs = [], []
         for i in range(1 + e2e_steps):
             dist.barrier()
             g.event_record(14)
@@ -420,11 +420,16 @@ def run_gpu(args, spec, dist: Dist):
             if i > 0:
                 times.append(dt_s)
                 gpu_times.append(g.event_elapsed_ms(14, 15) / 1e3)
+            if i > 0:
+                stage_runs.append(g.surface_job_stages())
         t_e2e = dist.max(float(np.median(times)))
+        stages = {k: float(np.median([r[k] for r in stage_runs])) for k in stage_runs[0]}
         e2e = {"value": updates_per_step * dist.world / t_e2e, "unit": "voxel-updates/s",
                "h2d_bytes_per_step": int(pts.nbytes), "d2h_bytes_per_step": int(out_bytes),
                "seconds_per_step": t_e2e,
-               "stream_seconds_per_step": float(np.median(gpu_times))}
+               "stream_seconds_per_step": float(np.median(gpu_times)),
+               "stage_ms": stages, "stage_ms_sum": float(sum(stages.values())),
+               "d2h_gb_per_s": out_bytes / (stages["download"] / 1e3) / 1e9 if stages.get("download") else None}
         G.load_library().msbg_gpu_host_free(hp)
         G.load_library().msbg_gpu_host_free(ho)
 
@@ -457,9 +462,15 @@ def run_gpu(args, spec, dist: Dist):
     g.close()
     for b in bound:  # device arrays a level channel of g was bound to: free after g
         b.free()
-    poisson = None
+    poisson = poisson_crop = poisson_batch = None
     if not args.no_poisson and spec is W.SURFACE_4096:
-        poisson = poisson_measure(96, max(1, min(args.steps, 3)), 1)
+        # the stated Poisson workload: every level-0 block of the layout; then the learned
+        # warm start, which does not fit beside the solver at that size, on a crop of it;
+        # then the 256-volume batch
+        poisson = poisson_full_measure(1, 1)
+        poisson_crop = poisson_measure(96, max(1, min(args.steps, 3)), 1)
+        from msbg_gb300 import batch_workload as BW
+        poisson_batch = BW.run_batch(max(1, min(args.steps, 3)), 1, WARMNET)
     if dist.rank != 0:
         return
     line = {
@@ -487,6 +498,8 @@ def run_gpu(args, spec, dist: Dist):
         "halo_fill": halo,
         "render": render,
         "poisson": poisson,
+        "poisson_crop96": poisson_crop,
+        "poisson_batch": poisson_batch,
     }
     print(json.dumps(line), flush=True)
 
@@ -668,6 +681,39 @@ def poisson_measure(n_objects: int, steps: int, warmup: int,
         for m in modes:
             if m != "plain" and "plain" in out:
                 out[f"{m}_speedup_vs_plain"] = out["plain"]["ms"] / out[m]["ms"]
+        return out
+    finally:
+        g.close()
+
+
+def poisson_full_measure(steps: int, warmup: int) -> dict:
+    """Time-to-1e-6 on the stated Poisson workload: every level-0 block of the 4096^3
+    three-level layout (144,191 blocks, 4.72 G cells), plain FP32 MG-PCG and FP16-storage /
+    FP32 iterative refinement from X = 0.  The two run in turn on one context, whose work
+    vectors are released in between (both together need more than the GPU's memory)."""
+    g, spec = PW.surface_layout_grid(None)
+    try:
+        bs = spec["bsx"]
+        t0 = time.perf_counter()
+        PW.setup_problem(g, bs)
+        setup_s = time.perf_counter() - t0
+        cells = int(g.info().nActive) * bs ** 3
+        out = {"workload": "poisson-4096^3-bs32-full", "cells": cells,
+               "mg_levels": [int(v) for v in g.mg_info()], "tolerance": 1e-6,
+               "rhs": "N(0,1) per cell, zero mean per 6-connected component",
+               "coefficients": "face coefficients U[0.5,2], Dirichlet 0 outside",
+               "host_setup_s": setup_s}
+        for kind in ("plain", "mixed"):
+            for _ in range(warmup):
+                PW.timed_solve(g, kind)
+            runs = [PW.timed_solve(g, kind) for _ in range(steps)]
+            out[kind] = sorted(runs, key=lambda r: r["ms"])[len(runs) // 2]
+            g.poisson_release_work()
+        out["mixed_speedup_vs_plain"] = out["plain"]["ms"] / out["mixed"]["ms"]
+        n1 = cells // 8
+        out["learned"] = (f"not run at this size: the network's level-1 buffers ({n1 * (52 + 32 + 2) * 4 / 1e9:.0f} GB "
+                          f"of activations and gradients, {cells * 8 / 1e9:.0f} GB of level-0 staging) do not fit "
+                          f"beside the solver's arrays; see poisson_crop96")
         return out
     finally:
         g.close()

@@ -132,6 +132,23 @@ int msbg_gpu_regularize_refinement_map(msbg_gpu_ctx *ctx);
  * value blocks for level 0 in ascending bid order, 8-color lists, every
  * channel's payload filled with fillValue. */
 int msbg_gpu_set_refinement_map(msbg_gpu_ctx *ctx, double fillValue);
+/* setRefinementMap's block lists (src/msbg.cpp:1682-1727): MSBG_GPU_LIST_EXISTING = the
+ * reference's _blocksExisting (blocks flagged BLK_EXISTS), MSBG_GPU_LIST_FINE_COARSE =
+ * _blocksFineCoarsePerLevel[level] (blocks of that level flagged BLK_FINE_COARSE), in
+ * ascending block id (the release fills them in no fixed order).  dBids: device, nBlocks
+ * entries; *hCount: the list's length.  Synchronizes. */
+enum { MSBG_GPU_LIST_EXISTING = 0, MSBG_GPU_LIST_FINE_COARSE = 1 };
+int msbg_gpu_get_block_list(msbg_gpu_ctx *ctx, int which, int level, int32_t *dBids, int64_t *hCount);
+/* setRefinementMap's fine-coarse distance channel CH_DIST_FINECOARSE at resolution level
+ * `level` (src/msbg.cpp:1887-1960, 1994-2033), as a level grid: dState (device, nBlocks):
+ * the data index of every block of that level flagged BLK_FINE_COARSE (ascending id), whose
+ * cells (level coordinates, x fastest) hold uint16(1024 * min(6, distance from the cell
+ * centre to the nearest coarser 26-neighbour block)) in dData (device, capBlocks blocks of
+ * (bsx>>level)^3); MSBG_GPU_LBLK_FULL (value 6 * 1024) for blocks of level-1 or level that
+ * touch such a block; MSBG_GPU_LBLK_EMPTY otherwise.  *hCount: the data blocks;
+ * MSBG_GPU_ERR_CAPACITY when they exceed capBlocks.  Synchronizes. */
+int msbg_gpu_dist_fine_coarse(msbg_gpu_ctx *ctx, int level, int32_t *dState, uint16_t *dData, int64_t capBlocks,
+                              int64_t *hCount);
 /* Read back the layout (synchronize): levels int8[nBlocks], flags uint16[nBlocks],
  * active block ids int32[nActive], slots int32[nBlocks]. */
 int msbg_gpu_get_levels(msbg_gpu_ctx *ctx, int8_t *hLevels);
@@ -198,6 +215,12 @@ int msbg_gpu_surface_job(msbg_gpu_ctx *ctx, const float *hPts, int64_t n, float 
                          float nbDist, const float *hBands, int nBands, int laplTyp, int numIter,
                          float timeStep, int variant, void *hOut, size_t hOutCap,
                          int64_t *nActiveOut);
+/* Stream time (ms) of the stages of the last msbg_gpu_surface_job, from CUDA events at their
+ * boundaries: points uploaded, layout built (levels, regularisation, refinement map, slab
+ * fill), splat, finalize, sweeps, payload downloaded.  msOut receives min(cap, *nOut)
+ * values; host time spent inside a stage (the layout's read-back of the block counts)
+ * counts towards it. */
+int msbg_gpu_surface_job_stages(msbg_gpu_ctx *ctx, float *msOut, int cap, int *nOut);
 
 /* ---- sparse Poisson solve -------------------------------------------------------------
  * Operator on the value-block cells (src/msbg3.cpp:1281-1296):
@@ -342,6 +365,25 @@ int msbg_gpu_level_grid_bind(msbg_gpu_ctx *ctx, int lchan, int level, int storag
 enum { MSBG_GPU_BC_NEUMANN = 1 << 10, MSBG_GPU_BC_COARSE_LEVEL = 1 << 26 };
 int msbg_gpu_fill_halo_blocks(msbg_gpu_ctx *ctx, int lchan, int level, const int32_t *dBids, int64_t n,
                               int haloSize, int opt, float *dOut, int64_t *hSkipped);
+/* The solver's halo: HaloBlockSet::fillHaloBlock3(iChan, bid, bx, by, bz, levelMg, tid)
+ * (src/halo.h:396-401, body src/halo.cpp:536-738) for n listed blocks at levelMg 0, halo 1.
+ * The cell flags (the reference's CH_CELL_FLAGS grids) come from flags channel fchan, set
+ * per level with msbg_gpu_level_flags_set (states as for level grids, raw uint16 flags, the
+ * constant blocks' flags).  Per position p of the (bs+2)^3 box (floats [z][y][x] at
+ * dOut + k*(bs+2)^3): p inside the domain in a block of layout level 0 -> CELL_VOID:
+ * +1e20 (SPEC_FLOAT_DIRICHLET), CELL_SOLID: -1e20 (SPEC_FLOAT_NEUMANN), else the value of
+ * level 0 of lchan; in a coarser block -> the same from level 1 at p/2; outside the domain
+ * -> +1e20 if the face it leaves through is open (hDomainBc[face] == 0, DBC_OPEN), else
+ * -1e20, the x face deciding before y before z.  hDomainBc (host, 6): the boundary types of
+ * faces -x, +x, -y, +y, -z, +z (src/msbg.h:910-915).  Listed blocks not at layout level 0,
+ * or without a level-0 block of lchan, are skipped (counted in *hSkipped, which makes the
+ * call synchronize). */
+#define MSBG_GPU_CELL_SOLID (1u << 0)  /* CELL_SOLID (src/msbg.h:602) */
+#define MSBG_GPU_CELL_VOID (1u << 12)  /* CELL_VOID (src/msbg.h:614) */
+int msbg_gpu_level_flags_set(msbg_gpu_ctx *ctx, int fchan, int level, const int32_t *hState,
+                             const uint16_t *hFlags, int64_t nData, uint16_t emptyFlags, uint16_t fullFlags);
+int msbg_gpu_fill_halo_blocks3(msbg_gpu_ctx *ctx, int lchan, int fchan, int levelMg, const int32_t *dBids,
+                               int64_t n, const int32_t *hDomainBc, float *dOut, int64_t *hSkipped);
 /* downsampleFloatChannelNew (src/msbg4.cpp:1035-1379) for blocks of a multi-level channel,
  * the step that restricts a block's data to the next coarser level (its ghost block,
  * src/msbg.cpp:3110-3150): for each listed block (as for msbg_gpu_fill_halo_blocks, any

@@ -390,6 +390,7 @@ extern "C" int msbg_gpu_create(msbg_gpu_ctx **out, int sx, int sy, int sz, int b
 #undef ALLOC
   if (e == cudaSuccess) e = cudaMallocHost((void **)&ctx->hCounters, kNumCounters * 8);
   for (int i = 0; i < kMaxEvents && e == cudaSuccess; i++) e = cudaEventCreate(&ctx->ev[i]);
+  for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&ctx->stageEv[i]);
   if (e == cudaSuccess) e = cudaMemset(ctx->dMark, 0, nB * 4);
   if (e == cudaSuccess) e = cudaMemset(ctx->dCounters, 0, kNumCounters * 8);
   if (e == cudaSuccess) e = cudaMemset(ctx->dStatus, 0, 16);
@@ -424,6 +425,7 @@ extern "C" int msbg_gpu_destroy(msbg_gpu_ctx *ctx) {
   msbg::warmNetFree(ctx->warmnet);
   msbg::poissonFree(ctx->poisson);
   for (auto &ev : ctx->ev) if (ev) cudaEventDestroy(ev);
+  for (auto &ev : ctx->stageEv) if (ev) cudaEventDestroy(ev);
   delete ctx;
   return MSBG_GPU_OK;
 }
@@ -771,6 +773,15 @@ extern "C" int msbg_gpu_surface_job(msbg_gpu_ctx *ctx, const float *hPts, int64_
                                     int numIter, float timeStep, int variant, void *hOut,
                                     size_t hOutCap, int64_t *nActiveOut) {
   if (!ctx || n < 0 || (n && !hPts)) return MSBG_GPU_ERR_ARG;
+  // stage boundaries on the stream: start, points uploaded, layout built, splat,
+  // finalize, sweeps, payload downloaded
+  ctx->stageCount = 0;
+  auto stage = [&]() -> int {
+    MSBG_CUDA(ctx, cudaEventRecord(ctx->stageEv[ctx->stageCount], ctx->stream));
+    ctx->stageCount++;
+    return MSBG_GPU_OK;
+  };
+  if (stage()) return MSBG_GPU_ERR_CUDA;
   if (ctx->ptsCap < n) {
     if (ctx->dPts) MSBG_CUDA(ctx, cudaFree(ctx->dPts));
     ctx->dPts = nullptr;
@@ -779,27 +790,43 @@ extern "C" int msbg_gpu_surface_job(msbg_gpu_ctx *ctx, const float *hPts, int64_
     ctx->ptsCap = n;
   }
   if (n) MSBG_CUDA(ctx, cudaMemcpyAsync(ctx->dPts, hPts, (size_t)n * 12, cudaMemcpyHostToDevice, ctx->stream));
-  int rc;
-  if (nBands > 0) {
-    rc = msbg_gpu_levels_from_bands(ctx, ctx->dPts, n, hBands, nBands);
-  } else {
-    rc = msbg_gpu_mark_points(ctx, ctx->dPts, n, rParticle + nbDist);
-    if (!rc) rc = msbg_gpu_levels_from_marks(ctx);
+  int rc = stage();
+  if (!rc) {
+    if (nBands > 0) {
+      rc = msbg_gpu_levels_from_bands(ctx, ctx->dPts, n, hBands, nBands);
+    } else {
+      rc = msbg_gpu_mark_points(ctx, ctx->dPts, n, rParticle + nbDist);
+      if (!rc) rc = msbg_gpu_levels_from_marks(ctx);
+    }
   }
   if (!rc) rc = msbg_gpu_regularize_refinement_map(ctx);
   if (!rc) rc = msbg_gpu_set_refinement_map(ctx, 1.0);
+  if (!rc) rc = stage();
   if (!rc) rc = msbg_gpu_splat(ctx, ctx->dPts, n, rParticle, nbDist);
+  if (!rc) rc = stage();
   if (!rc) rc = msbg_gpu_splat_finalize(ctx, rParticle, nbDist);
+  if (!rc) rc = stage();
   if (!rc && numIter > 0)
     rc = pdeRun(ctx, 0, laplTyp, 1, numIter, timeStep, 0.0f, variant);
+  if (!rc) rc = stage();
   if (rc) return rc;
   if (nActiveOut) *nActiveOut = ctx->nActive;
   if (hOut) {
     const size_t bytes = (size_t)ctx->nActive * ctx->voxPerBlock * storageBytes(ctx->ch[0].storage);
     if (bytes > hOutCap) return fail(ctx, MSBG_GPU_ERR_ARG, "output buffer too small (%zu < %zu)", hOutCap, bytes);
-    return msbg_gpu_download_payload(ctx, 0, hOut);
+    MSBG_CUDA(ctx, cudaMemcpyAsync(hOut, ctx->ch[0].d, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   }
+  if ((rc = stage())) return rc;
   MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return MSBG_GPU_OK;
+}
+
+extern "C" int msbg_gpu_surface_job_stages(msbg_gpu_ctx *ctx, float *msOut, int cap, int *nOut) {
+  if (!ctx || !msOut || cap < 0) return MSBG_GPU_ERR_ARG;
+  const int n = ctx->stageCount > 1 ? ctx->stageCount - 1 : 0;
+  for (int i = 0; i < n && i < cap; i++)
+    MSBG_CUDA(ctx, cudaEventElapsedTime(&msOut[i], ctx->stageEv[i], ctx->stageEv[i + 1]));
+  if (nOut) *nOut = n;
   return MSBG_GPU_OK;
 }
 

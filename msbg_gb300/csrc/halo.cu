@@ -48,16 +48,18 @@ struct LevelChannel {
 
 struct LevelChannels {
   LevelChannel ch[kMaxLevelChannels];
+  LevelChannel fl[kMaxLevelChannels];  // cell flags (raw uint16) of the solver's halo
   unsigned long long *dSkip = nullptr;
 };
 
 void levelChannelsFree(LevelChannels *lc) {
   if (!lc) return;
-  for (auto &c : lc->ch)
-    for (auto &g : c.lv) {
-      if (g.ownState) cudaFree(g.ownState);
-      if (g.ownPay) cudaFree(g.ownPay);
-    }
+  for (LevelChannel *set : {lc->ch, lc->fl})
+    for (int i = 0; i < kMaxLevelChannels; i++)
+      for (auto &g : set[i].lv) {
+        if (g.ownState) cudaFree(g.ownState);
+        if (g.ownPay) cudaFree(g.ownPay);
+      }
   if (lc->dSkip) cudaFree(lc->dSkip);
   delete lc;
 }
@@ -491,4 +493,179 @@ extern "C" int msbg_gpu_restrict_level_blocks(msbg_gpu_ctx *ctx, int lchan, int 
   cudaFree(boxes);
   if (!rc && hSkipped) *hSkipped = skipped;
   return rc;
+}
+
+// =====================================================================================
+// HaloBlockSet::fillHaloBlock3 (src/halo.cpp:536-738): the solver's halo, at multigrid
+// level 0 with halo 1, for blocks of layout level 0.  Per position p of the (bs+2)^3
+// box (level-0 coordinates):
+//   p in the domain, its block at layout level 0: flags(0, p) & CELL_VOID -> +1e20
+//     (SPEC_FLOAT_DIRICHLET, src/msbgcell.h:199-200), & CELL_SOLID -> -1e20
+//     (SPEC_FLOAT_NEUMANN), else value(0, p);
+//   p in the domain, its block coarser: the same from level 1 at p/2 (getOutOfBlockValue3,
+//     src/halo.cpp:536-562); p/2 lies in the block with p's block coordinates;
+//   p outside the domain: +1e20 when the face it leaves through is open, else -1e20, the
+//     x face deciding before y before z (the 3x3x3 table, src/msbg.cpp:2527-2548).
+// Not a hot kernel (the release calls it nowhere): one CTA per block, one position per
+// thread and step.
+// =====================================================================================
+namespace msbg {
+namespace {
+
+constexpr uint16_t kCellSolid = 1u << 0, kCellVoid = 1u << 12;  // src/msbg.h:602-614
+
+struct Halo3Level {
+  const int32_t *vState, *fState;
+  const void *vPay;
+  const uint16_t *fPay;
+  float vEmpty, vFull;
+  uint16_t fEmpty, fFull;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) kFillHalo3(const int32_t *__restrict__ bids, const int32_t *__restrict__ levels,
+                                                  Halo3Level L0, Halo3Level L1, int bs, int sx, int sy, int sz,
+                                                  int nbx, int nby, int64_t nBlocks, int4 dbcLo, int4 dbcHi,
+                                                  float *__restrict__ out, unsigned long long *__restrict__ skipped) {
+  const int hs = bs + 2;
+  const int64_t per = (int64_t)hs * hs * hs;
+  const int b = bids[blockIdx.x];
+  if (b < 0 || b >= nBlocks || levels[b] != 0 || L0.vState[b] == MSBG_GPU_LBLK_NONE) {
+    if (threadIdx.x == 0) atomicAdd(skipped, 1ull);
+    return;
+  }
+  const int ox = (b % nbx) * bs, oy = ((b / nbx) % nby) * bs, oz = (int)(b / ((int64_t)nbx * nby)) * bs;
+  float *dst = out + (int64_t)blockIdx.x * per;
+  for (int64_t i = threadIdx.x; i < per; i += blockDim.x) {
+    const int hx = (int)(i % hs), hy = (int)((i / hs) % hs), hz = (int)(i / ((int64_t)hs * hs));
+    const int px = ox + hx - 1, py = oy + hy - 1, pz = oz + hz - 1;
+    int side = -1;
+    if (pz < 0) side = 4; else if (pz >= sz) side = 5;
+    if (py < 0) side = 2; else if (py >= sy) side = 3;
+    if (px < 0) side = 0; else if (px >= sx) side = 1;
+    float v;
+    if (side >= 0) {
+      const int d = side == 0 ? dbcLo.x : side == 1 ? dbcHi.x : side == 2 ? dbcLo.y : side == 3 ? dbcHi.y
+                  : side == 4 ? dbcLo.z : dbcHi.z;
+      v = d == 0 ? 1e20f : -1e20f;
+    } else {
+      const int64_t b2 = (int64_t)(px / bs) + (int64_t)(py / bs) * nbx + (int64_t)(pz / bs) * nbx * nby;
+      const int l = levels[b2] == 0 ? 0 : 1;
+      const Halo3Level &L = l ? L1 : L0;
+      const int bl = bs >> l;
+      const int64_t vid = ((int64_t)((pz >> l) & (bl - 1)) * bl + ((py >> l) & (bl - 1))) * bl + ((px >> l) & (bl - 1));
+      const int32_t fs = L.fState ? L.fState[b2] : MSBG_GPU_LBLK_NONE;
+      const uint16_t f = fs >= 0 ? L.fPay[(int64_t)fs * bl * bl * bl + vid]
+                       : fs == MSBG_GPU_LBLK_EMPTY ? L.fEmpty : fs == MSBG_GPU_LBLK_FULL ? L.fFull : (uint16_t)0;
+      if (f & kCellVoid) {
+        v = 1e20f;
+      } else if (f & kCellSolid) {
+        v = -1e20f;
+      } else {
+        const int32_t vs = L.vState ? L.vState[b2] : MSBG_GPU_LBLK_NONE;
+        v = vs >= 0 ? ldRaw<T>((const T *)L.vPay + (int64_t)vs * bl * bl * bl + vid)
+          : vs == MSBG_GPU_LBLK_EMPTY ? L.vEmpty : vs == MSBG_GPU_LBLK_FULL ? L.vFull : 0.0f;
+      }
+    }
+    dst[i] = v;
+  }
+}
+
+}  // namespace
+}  // namespace msbg
+
+extern "C" int msbg_gpu_level_flags_set(msbg_gpu_ctx *ctx, int fchan, int level, const int32_t *hState,
+                                        const uint16_t *hFlags, int64_t nData, uint16_t emptyFlags,
+                                        uint16_t fullFlags) {
+  if (!ctx) return MSBG_GPU_ERR_ARG;
+  if (fchan < 0 || fchan >= kMaxLevelChannels)
+    return fail(ctx, MSBG_GPU_ERR_ARG, "level_flags_set: flags channel %d out of range", fchan);
+  if (level < 0 || level >= ctx->nLevels || level >= kMaxGridLevels || (ctx->bsx >> level) < 1)
+    return fail(ctx, MSBG_GPU_ERR_ARG, "level_flags_set: level %d out of range", level);
+  if (!hState || nData < 0 || (nData > 0 && !hFlags))
+    return fail(ctx, MSBG_GPU_ERR_ARG, "level_flags_set: null or negative argument");
+  for (int64_t b = 0; b < ctx->nBlocks; b++)
+    if (hState[b] < MSBG_GPU_LBLK_NONE || hState[b] >= nData)
+      return fail(ctx, MSBG_GPU_ERR_ARG, "level_flags_set: block %lld has state %d outside [-3, %lld)",
+                  (long long)b, hState[b], (long long)nData);
+  LevelGrid &g = levelChannels(ctx)->fl[fchan].lv[level];
+  g.set = false;
+  if (!g.ownState) MSBG_CUDA(ctx, cudaMalloc(&g.ownState, ctx->nBlocks * sizeof(int32_t)));
+  const int64_t bs = ctx->bsx >> level;
+  const size_t bytes = (size_t)nData * bs * bs * bs * sizeof(uint16_t);
+  if (g.payCap < bytes) {
+    MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (g.ownPay) MSBG_CUDA(ctx, cudaFree(g.ownPay));
+    g.ownPay = nullptr;
+    g.payCap = 0;
+    MSBG_CUDA(ctx, cudaMalloc(&g.ownPay, bytes));
+    g.payCap = bytes;
+  }
+  MSBG_CUDA(ctx, cudaMemcpyAsync(g.ownState, hState, ctx->nBlocks * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+  if (bytes) MSBG_CUDA(ctx, cudaMemcpyAsync(g.ownPay, hFlags, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  g.state = g.ownState;
+  g.pay = g.ownPay;
+  g.emptyF = emptyFlags;  // flag values, exact as floats
+  g.fullF = fullFlags;
+  g.set = true;
+  return MSBG_GPU_OK;
+}
+
+extern "C" int msbg_gpu_fill_halo_blocks3(msbg_gpu_ctx *ctx, int lchan, int fchan, int levelMg, const int32_t *dBids,
+                                          int64_t n, const int32_t *hDomainBc, float *dOut, int64_t *hSkipped) {
+  if (!ctx) return MSBG_GPU_ERR_ARG;
+  if (levelMg != 0) return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "fill_halo_blocks3: levelMg 0 only");
+  if (!hDomainBc || n < 0 || n > 0x7fffffff || (n > 0 && (!dBids || !dOut)))
+    return fail(ctx, MSBG_GPU_ERR_ARG, "fill_halo_blocks3: bad arguments");
+  if (!ctx->layoutValid) return fail(ctx, MSBG_GPU_ERR_STATE, "fill_halo_blocks3: no block layout");
+  if (ctx->nLevels < 2) return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "fill_halo_blocks3: needs a level 1");
+  if (lchan < 0 || lchan >= kMaxLevelChannels || fchan < 0 || fchan >= kMaxLevelChannels || !ctx->levelCh)
+    return fail(ctx, MSBG_GPU_ERR_STATE, "fill_halo_blocks3: channels not set");
+  const LevelChannel &vc = ctx->levelCh->ch[lchan];
+  const LevelChannel &fc = ctx->levelCh->fl[fchan];
+  for (int l = 0; l < 2; l++)
+    if (!vc.lv[l].set || !fc.lv[l].set)
+      return fail(ctx, MSBG_GPU_ERR_STATE, "fill_halo_blocks3: level %d of the values or the flags is not set", l);
+  if (n == 0) {
+    if (hSkipped) *hSkipped = 0;
+    return MSBG_GPU_OK;
+  }
+  Halo3Level L[2];
+  for (int l = 0; l < 2; l++) {
+    L[l].vState = vc.lv[l].state;
+    L[l].vPay = vc.lv[l].pay;
+    L[l].vEmpty = vc.lv[l].emptyF;
+    L[l].vFull = vc.lv[l].fullF;
+    L[l].fState = fc.lv[l].state;
+    L[l].fPay = (const uint16_t *)fc.lv[l].pay;
+    L[l].fEmpty = (uint16_t)fc.lv[l].emptyF;
+    L[l].fFull = (uint16_t)fc.lv[l].fullF;
+  }
+  LevelChannels *lc = levelChannels(ctx);
+  if (!lc->dSkip) MSBG_CUDA(ctx, cudaMalloc(&lc->dSkip, sizeof(unsigned long long)));
+  MSBG_CUDA(ctx, cudaMemsetAsync(lc->dSkip, 0, sizeof(unsigned long long), ctx->stream));
+  const int4 lo = make_int4(hDomainBc[0], hDomainBc[2], hDomainBc[4], 0);
+  const int4 hi = make_int4(hDomainBc[1], hDomainBc[3], hDomainBc[5], 0);
+  switch (vc.storage) {
+    case MSBG_GPU_F32:
+      MSBG_LAUNCH(ctx, kFillHalo3<float>, (unsigned)n, 256, 0, dBids, ctx->dLevels, L[0], L[1], ctx->bsx, ctx->sx,
+                  ctx->sy, ctx->sz, ctx->nbx, ctx->nby, ctx->nBlocks, lo, hi, dOut, lc->dSkip);
+      break;
+    case MSBG_GPU_F16:
+      MSBG_LAUNCH(ctx, kFillHalo3<__half>, (unsigned)n, 256, 0, dBids, ctx->dLevels, L[0], L[1], ctx->bsx, ctx->sx,
+                  ctx->sy, ctx->sz, ctx->nbx, ctx->nby, ctx->nBlocks, lo, hi, dOut, lc->dSkip);
+      break;
+    default:
+      MSBG_LAUNCH(ctx, kFillHalo3<uint16_t>, (unsigned)n, 256, 0, dBids, ctx->dLevels, L[0], L[1], ctx->bsx, ctx->sx,
+                  ctx->sy, ctx->sz, ctx->nbx, ctx->nby, ctx->nBlocks, lo, hi, dOut, lc->dSkip);
+  }
+  if (hSkipped) {
+    unsigned long long sk = 0;
+    MSBG_CUDA(ctx, cudaMemcpyAsync(&sk, lc->dSkip, sizeof(sk), cudaMemcpyDeviceToHost, ctx->stream));
+    MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *hSkipped = (int64_t)sk;
+  }
+  return MSBG_GPU_OK;
 }

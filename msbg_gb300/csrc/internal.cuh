@@ -49,6 +49,8 @@ struct msbg_gpu_ctx {
 
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[msbg::kMaxEvents] = {};
+  cudaEvent_t stageEv[8] = {};   // msbg_gpu_surface_job: events at its stage boundaries
+  int stageCount = 0;            // events recorded by the last surface job
 
   // layout (device)
   int32_t *dMark = nullptr;      // [nBlocks] 0/1 (demo's blockActive as a flag)

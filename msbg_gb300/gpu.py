@@ -66,6 +66,8 @@ SIGNATURES = {
     "msbg_gpu_get_flags": (I, [P, P]),
     "msbg_gpu_get_active_blocks": (I, [P, P, I64, C.POINTER(I64)]),
     "msbg_gpu_get_slots": (I, [P, P]),
+    "msbg_gpu_get_block_list": (I, [P, I, I, P, C.POINTER(I64)]),
+    "msbg_gpu_dist_fine_coarse": (I, [P, I, P, P, I64, C.POINTER(I64)]),
     "msbg_gpu_upload_payload": (I, [P, I, P]),
     "msbg_gpu_download_payload": (I, [P, I, P]),
     "msbg_gpu_payload_ptr": (I, [P, I, C.POINTER(P)]),
@@ -75,6 +77,7 @@ SIGNATURES = {
     "msbg_gpu_apply_channel_pde_fast": (I, [P, I, I, I, P, I64, I, I, F, F, F, I, F, F, F, P, F, F, F, F, F, I, P,
                                             I, I]),
     "msbg_gpu_surface_job": (I, [P, P, I64, F, F, P, I, I, I, F, I, P, SZ, C.POINTER(I64)]),
+    "msbg_gpu_surface_job_stages": (I, [P, P, I, C.POINTER(I)]),
     "msbg_gpu_event_record": (I, [P, I]),
     "msbg_gpu_event_elapsed": (I, [P, I, I, C.POINTER(F)]),
     "msbg_gpu_launch_count": (I64, [P]),
@@ -110,6 +113,8 @@ SIGNATURES = {
     "msbg_gpu_load": (I, [C.POINTER(P), C.c_char_p]),
     "msbg_gpu_fill_halo_blocks": (I, [P, I, I, P, I64, I, I, P, C.POINTER(I64)]),
     "msbg_gpu_restrict_level_blocks": (I, [P, I, I, P, I64, I, P, C.POINTER(I64)]),
+    "msbg_gpu_level_flags_set": (I, [P, I, I, P, P, I64, C.c_uint16, C.c_uint16]),
+    "msbg_gpu_fill_halo_blocks3": (I, [P, I, I, I, P, I64, P, P, C.POINTER(I64)]),
     "msbg_gpu_diag_wait_timeout": (I, [P, I]),
     "msbg_gpu_vcycle": (I, [P, I, I]),
     "msbg_gpu_dot": (I, [P, I, I, I, P, I64, C.POINTER(D)]),
@@ -455,6 +460,15 @@ class MultiresSparseGrid:
 
     # reference: multiplyLaplacianMatrixOpt(options, levelMg, chanX, chanB, kap, chanDstY,
     # pDotprod, blockList) (src/msbg.h:3167-3176); returns sum(Y X) when withDotprod
+    SURFACE_JOB_STAGES = ("upload", "layout", "splat", "finalize", "sweeps", "download")
+
+    def surface_job_stages(self) -> dict:
+        """Stream milliseconds of the stages of the last surface_job."""
+        ms = (C.c_float * 8)()
+        n = C.c_int()
+        self._check(self.L.msbg_gpu_surface_job_stages(self.h, ms, 8, C.byref(n)))
+        return {k: float(ms[i]) for i, k in enumerate(self.SURFACE_JOB_STAGES[: n.value])}
+
     def multiplyLaplacianMatrixOpt(self, options: int, levelMg: int, chanX: int, chanB: int, kap: float,
                                    chanDstY: int, withDotprod: bool = False, blockList=None):
         lp, ln, keep = self._block_list(blockList)
@@ -615,6 +629,74 @@ class MultiresSparseGrid:
         finally:
             d.free()
         return out
+
+    LIST_EXISTING, LIST_FINE_COARSE = 0, 1
+
+    def block_list(self, which: int, level: int = 0) -> np.ndarray:
+        """setRefinementMap's _blocksExisting (LIST_EXISTING) or _blocksFineCoarsePerLevel[level]
+        (LIST_FINE_COARSE), ascending."""
+        d = DeviceBuffer.alloc(self.n_blocks * 4)
+        n = C.c_int64()
+        try:
+            self._check(self.L.msbg_gpu_get_block_list(self.h, which, level, C.c_void_p(d.ptr), C.byref(n)))
+            out = np.empty(n.value, np.int32)
+            if n.value:
+                self._check(self.L.msbg_gpu_copy_d2h(self.h, _ptr(out), C.c_void_p(d.ptr), out.nbytes))
+            self.synchronize()
+        finally:
+            d.free()
+        return out
+
+    def dist_fine_coarse(self, level: int):
+        """CH_DIST_FINECOARSE of one level: (state int32 [nBlocks], uint16 [n][(bsx>>level)^3])."""
+        nv = (self.bsx >> level) ** 3
+        ds = DeviceBuffer.alloc(self.n_blocks * 4)
+        dd = DeviceBuffer.alloc(self.n_blocks * nv * 2)
+        n = C.c_int64()
+        try:
+            self._check(self.L.msbg_gpu_dist_fine_coarse(self.h, level, C.c_void_p(ds.ptr), C.c_void_p(dd.ptr),
+                                                         self.n_blocks, C.byref(n)))
+            st = np.empty(self.n_blocks, np.int32)
+            data = np.empty((n.value, nv), np.uint16)
+            self._check(self.L.msbg_gpu_copy_d2h(self.h, _ptr(st), C.c_void_p(ds.ptr), st.nbytes))
+            if n.value:
+                self._check(self.L.msbg_gpu_copy_d2h(self.h, _ptr(data), C.c_void_p(dd.ptr), data.nbytes))
+            self.synchronize()
+        finally:
+            ds.free()
+            dd.free()
+        return st, data
+
+    def level_flags_set(self, fchan: int, level: int, state: np.ndarray, flags: np.ndarray | None,
+                        empty_flags: int = 0, full_flags: int = 0):
+        """Cell flags of resolution level `level` of flags channel fchan: per-block states and
+        the uint16 flags [n][(bsx>>level)^3] (the reference's CH_CELL_FLAGS grid)."""
+        st = np.ascontiguousarray(state, np.int32)
+        f = None if flags is None else np.ascontiguousarray(flags, np.uint16)
+        n_data = 0 if f is None else int(f.size // ((self.bsx >> level) ** 3))
+        self._check(self.L.msbg_gpu_level_flags_set(self.h, fchan, level, _ptr(st), None if f is None else _ptr(f),
+                                                    n_data, empty_flags, full_flags))
+
+    # reference: HaloBlockSet::fillHaloBlock3 (src/halo.h:396-401), one call for a list
+    def fillHaloBlock3(self, lchan: int, fchan: int, bids: np.ndarray, domain_bc, levelMg: int = 0):
+        """The solver's halo of the listed blocks: (float32 [n][(bsx+2)^3], skipped count)."""
+        bids = np.ascontiguousarray(bids, np.int32)
+        hs = self.bsx + 2
+        out = np.empty((len(bids), hs ** 3), np.float32)
+        db = self.to_device(bids if len(bids) else np.zeros(1, np.int32))
+        do = DeviceBuffer.alloc(max(out.nbytes, 4))
+        dbc = np.ascontiguousarray(domain_bc, np.int32)
+        sk = C.c_int64(-1)
+        try:
+            self._check(self.L.msbg_gpu_fill_halo_blocks3(self.h, lchan, fchan, levelMg, C.c_void_p(db.ptr), len(bids),
+                                                          _ptr(dbc), C.c_void_p(do.ptr), C.byref(sk)))
+            if len(bids):
+                self._check(self.L.msbg_gpu_copy_d2h(self.h, _ptr(out), C.c_void_p(do.ptr), out.nbytes))
+            self.synchronize()
+        finally:
+            db.free()
+            do.free()
+        return out, int(sk.value)
 
     def restrict_level_blocks(self, lchan: int, level: int, bids: np.ndarray, simple_average: bool = False):
         """downsampleFloatChannelNew for blocks of a level channel (cross-resolution halo):

@@ -1599,3 +1599,120 @@ void orc_relax_ref(int nx, int ny, int nz, int bs, float *x, const float *b, con
       }
     }
 }
+
+/* ---- the solver's halo (src/halo.cpp:536-738) ------------------------------------- */
+
+static uint16_t lf_value(const orc_grid *g, const orc_flag_grid *lf, int l, int x, int y, int z) {
+  const int bs = g->bsx >> l;
+  const int64_t bid = (int64_t)(x / bs) + (int64_t)(y / bs) * g->nbx + (int64_t)(z / bs) * g->nbx * g->nby;
+  const int32_t st = lf[l].state[bid];
+  if (st == ORC_LBLK_EMPTY) return lf[l].emptyFlags;
+  if (st == ORC_LBLK_FULL) return lf[l].fullFlags;
+  if (st < 0) return 0;
+  return lf[l].payload[(int64_t)st * bs * bs * bs + ((int64_t)(z % bs) * bs + (y % bs)) * bs + (x % bs)];
+}
+
+int64_t orc_fill_halo3(const orc_grid *g, int nLevels, const int32_t *levels, const orc_level_grid *lg,
+                       const orc_flag_grid *lf, const int32_t *bids, int64_t nBids, const int32_t *dbc,
+                       float *out) {
+  const float kDirichlet = 1e20f, kNeumann = -1e20f; /* SPEC_FLOAT_*, src/msbgcell.h:199-200 */
+  const int bs = g->bsx, hs = bs + 2;
+  const int s[3] = {g->sx, g->sy, g->sz};
+  const int64_t per = (int64_t)hs * hs * hs;
+  int64_t skipped = 0;
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : skipped)
+  for (int64_t k = 0; k < nBids; k++) {
+    const int32_t bid = bids[k];
+    float *dst = out + k * per;
+    if (levels[bid] != 0 || nLevels < 2) {
+      skipped++;
+      continue;
+    }
+    const int o[3] = {(bid % g->nbx) * bs, ((bid / g->nbx) % g->nby) * bs, (bid / (g->nbx * g->nby)) * bs};
+    for (int hz = 0; hz < hs; hz++)
+      for (int hy = 0; hy < hs; hy++)
+        for (int hx = 0; hx < hs; hx++) {
+          const int p[3] = {o[0] + hx - 1, o[1] + hy - 1, o[2] + hz - 1};
+          float v;
+          int side = -1; /* the face p leaves through: x decides before y before z */
+          for (int a = 2; a >= 0; a--)
+            if (p[a] < 0 || p[a] >= s[a]) side = 2 * a + (p[a] >= s[a]);
+          if (side < 0) {
+            const int64_t b2 = (int64_t)(p[0] / bs) + (int64_t)(p[1] / bs) * g->nbx +
+                               (int64_t)(p[2] / bs) * g->nbx * g->nby;
+            const int l = levels[b2] == 0 ? 0 : 1;
+            const int q[3] = {p[0] >> l, p[1] >> l, p[2] >> l};
+            const uint16_t f = lf_value(g, lf, l, q[0], q[1], q[2]);
+            int found;
+            v = (f & ORC_CELL_VOID) ? kDirichlet
+                : (f & ORC_CELL_SOLID) ? kNeumann
+                                        : lg_value(g, lg, l, q[0], q[1], q[2], &found);
+          } else {
+            v = dbc[side] == 0 ? kDirichlet : kNeumann;
+          }
+          dst[((int64_t)hz * hs + hy) * hs + hx] = v;
+        }
+  }
+  return skipped;
+}
+
+/* ---- setRefinementMap: the fine-coarse distance channel (src/msbg.cpp:1887-2033) ---- */
+
+int64_t orc_dist_fine_coarse(const int32_t *levels, const uint16_t *flags, int nbx, int nby, int nbz, int bsx,
+                             int level, int dTransRes, int32_t *state, uint16_t *data) {
+  const int64_t nB = (int64_t)nbx * nby * nbz;
+  const int bs = bsx >> level;
+  const uint16_t kFineCoarse = 1u << 3; /* BLK_FINE_COARSE, src/msbg.h:561-573 */
+  int64_t n = 0;
+  for (int64_t b = 0; b < nB; b++) {
+    state[b] = ORC_LBLK_EMPTY;
+    if (levels[b] == level && (flags[b] & kFineCoarse)) state[b] = (int32_t)n++;
+  }
+  for (int64_t b = 0; b < nB; b++) {
+    const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((int64_t)nbx * nby));
+    if (state[b] >= 0) {
+      float box[26][3];
+      int nbox = 0;
+      for (int dz = -1; dz <= 1; dz++)
+        for (int dy = -1; dy <= 1; dy++)
+          for (int dx = -1; dx <= 1; dx++) {
+            const int x = bx + dx, y = by + dy, z = bz + dz;
+            if ((!dx && !dy && !dz) || x < 0 || y < 0 || z < 0 || x >= nbx || y >= nby || z >= nbz) continue;
+            if (levels[((int64_t)z * nby + y) * nbx + x] <= level) continue;
+            box[nbox][0] = (float)x; box[nbox][1] = (float)y; box[nbox][2] = (float)z;
+            nbox++;
+          }
+      uint16_t *d = data + state[b] * (int64_t)bs * bs * bs;
+      int vid = 0;
+      for (int z1 = bz * bs; z1 < (bz + 1) * bs; z1++)
+        for (int y1 = by * bs; y1 < (by + 1) * bs; y1++)
+          for (int x1 = bx * bs; x1 < (bx + 1) * bs; x1++, vid++) {
+            const float p[3] = {x1 + 0.5f, y1 + 0.5f, z1 + 0.5f};
+            float d2 = 1e20f;
+            for (int i = 0; i < nbox; i++) { /* distToBoxSq, src/msbg.h:3874-3886 */
+              float s2 = 0.0f;
+              for (int a = 0; a < 3; a++) {
+                const float lo = box[i][a] * (float)bs - p[a], hi = p[a] - (box[i][a] + 1.0f) * (float)bs;
+                float m = lo > 0.0f ? lo : 0.0f;
+                m = m > hi ? m : hi;
+                s2 += m * m;
+              }
+              d2 = d2 < s2 ? d2 : s2;
+            }
+            float dist = sqrtf(d2);
+            if (dist < 0.0f || dist > (float)dTransRes) dist = (float)dTransRes;
+            d[vid] = (uint16_t)(dist * 1024.0f);
+          }
+    } else if (levels[b] <= level && levels[b] >= level - 1) {
+      for (int dz = -1; dz <= 1 && state[b] == ORC_LBLK_EMPTY; dz++)
+        for (int dy = -1; dy <= 1; dy++)
+          for (int dx = -1; dx <= 1; dx++) {
+            const int x = bx + dx, y = by + dy, z = bz + dz;
+            if ((!dx && !dy && !dz) || x < 0 || y < 0 || z < 0 || x >= nbx || y >= nby || z >= nbz) continue;
+            const int64_t b2 = ((int64_t)z * nby + y) * nbx + x;
+            if (levels[b2] == level && (flags[b2] & kFineCoarse)) state[b] = ORC_LBLK_FULL;
+          }
+    }
+  }
+  return n;
+}

@@ -172,6 +172,29 @@ int64_t orc_fill_halo(const orc_grid *g, int nLevels, const int32_t *levels,
                       const orc_level_grid *lg, int level, const int32_t *bids, int64_t nBids,
                       int haloSize, unsigned opt, float *out);
 
+/* Cell flags of one resolution level (the reference's CH_CELL_FLAGS grids): per-block
+ * states as orc_level_grid, uint16 payload, and the constant blocks' flags. */
+typedef struct {
+  const int32_t *state;
+  const uint16_t *payload; /* [n][(bsx>>l)^3] */
+  uint16_t emptyFlags, fullFlags;
+} orc_flag_grid;
+enum { ORC_CELL_SOLID = 1 << 0, ORC_CELL_VOID = 1 << 12 }; /* src/msbg.h:602-614 */
+/* HaloBlockSet::fillHaloBlock3 (src/halo.cpp:536-738) at multigrid level 0, halo 1, for the
+ * listed blocks of layout level 0 (others skipped and counted): per position p of the
+ * (bs+2)^3 box, in level-0 coordinates,
+ *   p in the domain, its block at layout level 0: flags(0, p) & CELL_VOID -> +1e20
+ *     (SPEC_FLOAT_DIRICHLET), & CELL_SOLID -> -1e20 (SPEC_FLOAT_NEUMANN), else value(0, p);
+ *   p in the domain, its block coarser: the same with flags and value of level 1 at p/2
+ *     (getOutOfBlockValue3, src/halo.cpp:536-562);
+ *   p outside the domain: +1e20 when the face it leaves through is open (DBC_OPEN = 0),
+ *     else -1e20; the x face decides before y before z (the 3x3x3 table,
+ *     src/msbg.cpp:2527-2548).
+ * dbc[6]: the domain boundary types of faces -x, +x, -y, +y, -z, +z. */
+int64_t orc_fill_halo3(const orc_grid *g, int nLevels, const int32_t *levels, const orc_level_grid *lg,
+                       const orc_flag_grid *lf, const int32_t *bids, int64_t nBids, const int32_t *dbc,
+                       float *out);
+
 /* ---- ray-march render of the iso-0.5 surface ----------------------------------
  * RDR::RaymarchRenderer (src/render.h:52-160, src/render.cpp:20-101): per pixel a
  * primary ray from the camera (FP64), stepped by 1/res (res = max(sx,sy,sz)) for at
@@ -268,6 +291,16 @@ int orc_poisson_mgpcg(const orc_level0 *L, int log2bs0, const double *b, double 
 void orc_relax_ref(int nx, int ny, int nz, int bs, float *x, const float *b, const float *cx,
                    const float *cy, const float *cz, const float *dinv, const int32_t *bids, int64_t n,
                    int passes, int reverse, int blockIter, float omega);
+/* setRefinementMap's fine-coarse distance channel CH_DIST_FINECOARSE at resolution level l
+ * (src/msbg.cpp:1887-1960, 1994-2033) from the regularised level map and the BlockInfo
+ * flags: every block of level l flagged BLK_FINE_COARSE is a value block (ascending id,
+ * state[b] = its index) whose cell (x,y,z) (level-l coordinates) holds
+ * uint16(1024 * min(dTransRes, sqrt(min over its 26-neighbours of level > l of
+ * distToBoxSq(box, cell centre)))); a block of level l-1 or l that is no value block but has
+ * a BLK_FINE_COARSE 26-neighbour of level l is full (state -2, value dTransRes*1024); other
+ * blocks are empty (-1).  data: [n][(bsx>>l)^3]; returns n. */
+int64_t orc_dist_fine_coarse(const int32_t *levels, const uint16_t *flags, int nbx, int nby, int nbz, int bsx,
+                             int level, int dTransRes, int32_t *state, uint16_t *data);
 /* The GPU's seeded coefficients (float values) on a dense grid: lower faces + diagonal. */
 void orc_poisson_coeffs_dense(uint32_t seed, int nx, int ny, int nz, const uint8_t *act, double *cx,
                               double *cy, double *cz, double *d);

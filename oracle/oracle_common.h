@@ -35,6 +35,15 @@
  * A "downsample job" takes the halo job's input (FP32 only) and dumps
  * downsampleFloatChannelNew to multigrid level 1 for every level-0 block (constr01 = 1:
  * OPT_SIMPLE_AVERAGE): int32 bids[nActive], float32 [nActive][(bsx/2)^3].
+ * A "halo3 job" takes the halo job's FP32 input plus the cell flags of every level (int32
+ * states [nLevels][nBlocks], then per level uint16 [max+1][(bsx>>l)^3]) and int32 domain
+ * boundary types [6] (-x,+x,-y,+y,-z,+z), the constant blocks' flags in `reserved`
+ * (empty | full << 16), and dumps HaloBlockSet::fillHaloBlock3 at multigrid level 0 of
+ * every level-0 block: int32 bids[nActive], float32 [nActive][(bsx+2)^3].
+ * A "layout job" takes the levels job's input and dumps, after the header, lists (int32
+ * count, then the sorted ids): _blocksExisting, _blocksFineCoarsePerLevel[l] for every
+ * level, then per level the CH_DIST_FINECOARSE grid: its value blocks (list, then uint16
+ * [n][(bsx>>l)^3]), its full blocks (list) and the full value (uint16).
  */
 #ifndef MSBG_ORACLE_COMMON_H
 #define MSBG_ORACLE_COMMON_H
@@ -46,7 +55,8 @@
 
 enum { ORACLE_CHAN_F32 = 0, ORACLE_CHAN_U16 = 1 };
 enum { ORACLE_JOB_SURFACE = 1, ORACLE_JOB_LEVELS = 2, ORACLE_JOB_INTERP = 3, ORACLE_JOB_HALO = 4,
-       ORACLE_JOB_RENDER = 5, ORACLE_JOB_MORTON = 6, ORACLE_JOB_SOLVER = 7, ORACLE_JOB_DOWNSAMPLE = 8 };
+       ORACLE_JOB_RENDER = 5, ORACLE_JOB_MORTON = 6, ORACLE_JOB_SOLVER = 7, ORACLE_JOB_DOWNSAMPLE = 8,
+       ORACLE_JOB_HALO3 = 9, ORACLE_JOB_LAYOUT = 10 };
 
 /* Interp job option bits: the reference's own interpolation options (src/sbg.h:140-170)
  * plus one bit that the reference's enum leaves unused, for the render-density scale. */

@@ -311,7 +311,7 @@ def run_reference_levels(sx, sy, sz, bsx, n_levels, levels, timeout: float = 600
         return read_result(op, bsx, surface=False)
 
 
-JOB_SOLVER, JOB_DOWNSAMPLE = 7, 8
+JOB_SOLVER, JOB_DOWNSAMPLE, JOB_HALO3, JOB_LAYOUT = 7, 8, 9, 10
 
 
 def run_reference_solver(sx, sy, sz, bsx, bids, x, b, q, p, cx, cy, cz, d, a: float = 0.5,
@@ -382,3 +382,85 @@ def run_reference_downsample(sx, sy, sz, bsx, n_levels, levels, states, payloads
     bids = np.frombuffer(buf, np.int32, m, hsz).copy()
     vals = np.frombuffer(buf, np.float32, m * nvc, hsz + 4 * m).copy().reshape(m, nvc)
     return bids, vals
+
+
+def run_reference_halo3(sx, sy, sz, bsx, n_levels, levels, states, payloads, flag_states, flag_payloads,
+                        domain_bc, empty_value=0.0, full_value=1.0, empty_flags=0, full_flags=0,
+                        timeout: float = 600):
+    """HaloBlockSet::fillHaloBlock3 (src/halo.cpp:536-738) of every level-0 block by the
+    reference itself: FP32 level grids, uint16 cell flags per level, domain boundary types
+    (-x,+x,-y,+y,-z,+z; 0 = DBC_OPEN, 1 = DBC_SOLID).  Returns (bids, float32 [m][(bsx+2)^3])."""
+    with tempfile.TemporaryDirectory() as td:
+        jp, op = os.path.join(td, "job.bin"), os.path.join(td, "out.bin")
+        write_halo_job(jp, sx, sy, sz, bsx, n_levels, CHAN_F32, levels, states, payloads, 0, 1, 0,
+                       empty_value, full_value)
+        with open(jp, "r+b") as f:
+            f.seek(8)
+            f.write(struct.pack("<i", JOB_HALO3))
+            f.seek(struct.calcsize("<8s11i4f"))
+            f.write(struct.pack("<i", (int(empty_flags) & 0xffff) | ((int(full_flags) & 0xffff) << 16)))
+        with open(jp, "ab") as f:
+            for l in range(n_levels):
+                f.write(np.ascontiguousarray(flag_states[l], dtype=np.int32).tobytes())
+            for l in range(n_levels):
+                n = int(np.max(flag_states[l])) + 1 if len(flag_states[l]) else 0
+                bs = bsx >> l
+                f.write(np.ascontiguousarray(flag_payloads[l], dtype=np.uint16).reshape(-1)[: n * bs ** 3].tobytes())
+            f.write(np.asarray(domain_bc, np.int32).tobytes())
+        r = subprocess.run([REF_DRIVER, jp, op], cwd=td, timeout=timeout,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference halo3 job failed with status {r.returncode}")
+        with open(op, "rb") as f:
+            buf = f.read()
+    hsz = struct.calcsize(_OUT_FMT)
+    h = struct.unpack(_OUT_FMT, buf[:hsz])
+    if h[0] != OUT_MAGIC:
+        raise ValueError("bad oracle output")
+    m = int(h[2])
+    hs = bsx + 2
+    bids = np.frombuffer(buf, np.int32, m, hsz).copy()
+    vals = np.frombuffer(buf, np.float32, m * hs ** 3, hsz + 4 * m).copy().reshape(m, hs ** 3)
+    return bids, vals
+
+
+def run_reference_layout(sx, sy, sz, bsx, n_levels, levels, timeout: float = 600) -> dict:
+    """setRefinementMap's block lists and fine-coarse distance channel (src/msbg.cpp:1428-2165)
+    by the reference itself: {"existing": ids, "fine_coarse": [ids per level], "dist": [per
+    level {"value_bids", "value" uint16 [n][(bsx>>l)^3], "full_bids", "full_value"}]}."""
+    lv = np.ascontiguousarray(levels, dtype=np.int32).ravel()
+    with tempfile.TemporaryDirectory() as td:
+        jp, op = os.path.join(td, "job.bin"), os.path.join(td, "out.bin")
+        hdr = struct.pack(_JOB_FMT, JOB_MAGIC, JOB_LAYOUT, sx, sy, sz, bsx, n_levels, 0, 0, 0, 0, 1,
+                          0.0, 0.0, 0.0, 0.0, 0, 0, lv.size)
+        with open(jp, "wb") as f:
+            f.write(hdr)
+            f.write(lv.tobytes())
+        r = subprocess.run([REF_DRIVER, jp, op], cwd=td, timeout=timeout,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference layout job failed with status {r.returncode}")
+        with open(op, "rb") as f:
+            buf = f.read()
+    off = struct.calcsize(_OUT_FMT)
+    if buf[:8] != OUT_MAGIC:
+        raise ValueError("bad oracle output")
+
+    def lst():
+        nonlocal off
+        n = int(np.frombuffer(buf, np.int32, 1, off)[0])
+        v = np.frombuffer(buf, np.int32, n, off + 4).copy()
+        off += 4 + 4 * n
+        return v
+
+    out = {"existing": lst(), "fine_coarse": [lst() for _ in range(n_levels)], "dist": []}
+    for l in range(n_levels):
+        vb = lst()
+        nv = (bsx >> l) ** 3
+        val = np.frombuffer(buf, np.uint16, len(vb) * nv, off).copy().reshape(len(vb), nv)
+        off += 2 * len(vb) * nv
+        fb = lst()
+        fv = int(np.frombuffer(buf, np.uint16, 1, off)[0])
+        off += 2
+        out["dist"].append({"value_bids": vb, "value": val, "full_bids": fb, "full_value": fv})
+    return out

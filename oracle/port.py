@@ -85,6 +85,10 @@ def lib():
         L.orc_f32_to_f16.restype = C.c_uint16
         L.orc_relax_ref.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, P, P, P, P, C.c_int64,
                                     C.c_int, C.c_int, C.c_int, C.c_float]
+        L.orc_fill_halo3.argtypes = [C.POINTER(Grid), C.c_int, P, P, P, P, C.c_int64, P, P]
+        L.orc_fill_halo3.restype = C.c_int64
+        L.orc_dist_fine_coarse.argtypes = [P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P, P]
+        L.orc_dist_fine_coarse.restype = C.c_int64
         L.orc_f16_to_f32.argtypes = [C.c_uint16]
         L.orc_f16_to_f32.restype = C.c_float
         _lib = L
@@ -206,6 +210,49 @@ def fill_halo(g: Grid, levels, states: list, payloads: list, level: int, bids, h
     skipped = lib().orc_fill_halo(C.byref(g), n_levels, _p(levels), C.cast(lgs, C.c_void_p), level,
                                   _p(bids), len(bids),
                                   halo, opt, _p(out))
+    return out, int(skipped)
+
+
+def dist_fine_coarse(levels, flags, nb, bsx: int, level: int, d_trans_res: int = 6):
+    """CH_DIST_FINECOARSE of level `level` restated: (state int32 [nBlocks], uint16 [n][(bsx>>l)^3])."""
+    lv = np.ascontiguousarray(levels, np.int32)
+    fl = np.ascontiguousarray(flags, np.uint16)
+    bs = bsx >> level
+    state = np.empty(lv.size, np.int32)
+    data = np.zeros((lv.size, bs ** 3), np.uint16)
+    n = lib().orc_dist_fine_coarse(_p(lv), _p(fl), nb[0], nb[1], nb[2], bsx, level, d_trans_res, _p(state), _p(data))
+    return state, data[:n].copy()
+
+
+class FlagGrid(C.Structure):
+    _fields_ = [("state", C.c_void_p), ("payload", C.c_void_p), ("emptyFlags", C.c_uint16),
+                ("fullFlags", C.c_uint16)]
+
+
+def fill_halo3(g: Grid, levels, states: list, payloads: list, flag_states: list, flag_payloads: list, bids,
+               domain_bc, empty_value: float = 0.0, full_value: float = 1.0, empty_flags: int = 0,
+               full_flags: int = 0) -> tuple[np.ndarray, int]:
+    """fillHaloBlock3 restated (src/halo.cpp:536-738) at multigrid level 0: float32
+    [len(bids)][(bsx+2)^3] and the number of skipped blocks."""
+    n_levels = len(states)
+    levels = np.ascontiguousarray(levels, np.int32)
+    keep = []
+    lgs = (LevelGrid * n_levels)()
+    lfs = (FlagGrid * n_levels)()
+    for l in range(n_levels):
+        st = np.ascontiguousarray(states[l], np.int32)
+        pay = np.ascontiguousarray(payloads[l]) if payloads[l] is not None else np.zeros(1, np.float32)
+        fs = np.ascontiguousarray(flag_states[l], np.int32)
+        fp = np.ascontiguousarray(flag_payloads[l], np.uint16) if flag_payloads[l] is not None else np.zeros(1, np.uint16)
+        keep += [st, pay, fs, fp]
+        lgs[l] = LevelGrid(st.ctypes.data, pay.ctypes.data, empty_value, full_value)
+        lfs[l] = FlagGrid(fs.ctypes.data, fp.ctypes.data, empty_flags, full_flags)
+    bids = np.ascontiguousarray(bids, np.int32)
+    hs = g.bsx + 2
+    out = np.zeros((len(bids), hs ** 3), np.float32)
+    dbc = np.ascontiguousarray(domain_bc, np.int32)
+    skipped = lib().orc_fill_halo3(C.byref(g), n_levels, _p(levels), C.cast(lgs, C.c_void_p), C.cast(lfs, C.c_void_p),
+                                   _p(bids), len(bids), _p(dbc), _p(out))
     return out, int(skipped)
 
 

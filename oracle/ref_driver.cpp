@@ -730,6 +730,123 @@ int runDownsampleJob(const OracleJobHeader &job, const int32_t *levelsIn, const 
   return 0;
 }
 
+// HaloBlockSet::fillHaloBlock3 (src/halo.cpp:536-738), the solver's halo, at multigrid
+// level 0: the halo job's multi-level FP32 channel plus the cell flags (CH_CELL_FLAGS) of
+// every resolution level and the domain's boundary types; every level-0 block that has a
+// block at level 0 is filled (halo 1).  Flags of constant blocks: reserved = empty | full<<16.
+int runHalo3Job(const OracleJobHeader &job, const int32_t *levelsIn, const int32_t *state,
+                const std::vector<std::vector<uint8_t>> &pay, const int32_t *fstate,
+                const std::vector<std::vector<uint16_t>> &fpay, const int32_t *dbc, FILE *fout) {
+  OracleOutHeader out;
+  memset(&out, 0, sizeof(out));
+  memcpy(out.magic, ORACLE_OUT_MAGIC, 8);
+  const int chan = MSBG::CH_FLOAT_1;
+  MultiresSparseGrid *msbg = MultiresSparseGrid::create(
+      "TEST", job.sx, job.sy, job.sz, job.bsx, -1, 0, -1, 0, NULL, NULL, job.nLevels);
+  if (!msbg) return 2;
+  const int nBlocks = msbg->nBlocks();
+  if ((int64_t)nBlocks != job.nBlocksIn) return 4;
+  if (msbg->setDomainBoundarySpec_(dbc[0], dbc[1], dbc[2], dbc[3], dbc[4], dbc[5])) return 8;
+  std::vector<int> levels(levelsIn, levelsIn + nBlocks);
+  msbg->regularizeRefinementMap(levels.data());
+  for (int b = 0; b < nBlocks; b++)
+    if (levels[b] != levelsIn[b]) return 5;
+  msbg->setRefinementMap(levels.data(), NULL, 0, NULL, false, false);
+  const uint16_t emptyFlags = (uint16_t)(job.reserved & 0xffff), fullFlags = (uint16_t)((uint32_t)job.reserved >> 16);
+  for (int l = 0; l < job.nLevels; l++) {
+    SparseGrid<float> *sg = MSBG::getChannel<float>(msbg, chan, l);
+    SparseGrid<MSBG::CellFlags> *sf = msbg->getFlagsChannel(MSBG::CH_CELL_FLAGS, l, 0);
+    if (!sg || !sf) return 3;
+    sg->reset();
+    sg->prepareDataAccess();
+    sg->setEmptyValue(job.dt);
+    sg->setFullValue(job.rParticle);
+    sf->reset();
+    sf->prepareDataAccess();
+    sf->setEmptyValue(emptyFlags);
+    sf->setFullValue(fullFlags);
+    const size_t nv = (size_t)sg->nVoxelsInBlock();
+    const int32_t *st = state + (size_t)l * nBlocks, *ft = fstate + (size_t)l * nBlocks;
+    const float *src = reinterpret_cast<const float *>(pay[l].data());
+    for (int b = 0; b < nBlocks; b++) {
+      if (st[b] >= 0) memcpy(sg->getBlockDataPtr(b, 1, 0), src + (size_t)st[b] * nv, nv * sizeof(float));
+      else if (st[b] == -1) sg->setEmptyBlock(b);
+      else if (st[b] == -2) sg->setFullBlock(b);
+      if (ft[b] >= 0) memcpy(sf->getBlockDataPtr(b, 1, 0), fpay[l].data() + (size_t)ft[b] * nv, nv * 2);
+      else if (ft[b] == -1) sf->setEmptyBlock(b);
+      else if (ft[b] == -2) sf->setFullBlock(b);
+    }
+  }
+  const int bs = job.bsx, hs = bs + 2;
+  std::vector<int32_t> bids;
+  for (int b = 0; b < nBlocks; b++)
+    if (levels[b] == 0 && state[b] != -3) bids.push_back(b);
+  std::vector<float> halo(bids.size() * (size_t)hs * hs * hs);
+  MSBG::HaloBlockSet hb(msbg, 1, 1);
+  const int nbx = job.sx / bs, nby = job.sy / bs;
+  const double t0 = nowSec();
+  for (size_t k = 0; k < bids.size(); k++) {
+    const int b = bids[k];
+    float *p = hb.fillHaloBlock3(chan, b, b % nbx, (b / nbx) % nby, b / (nbx * nby), 0, 0);
+    memcpy(halo.data() + k * (size_t)hs * hs * hs, p, sizeof(float) * hs * hs * hs);
+  }
+  out.tPdeSec = nowSec() - t0;
+  out.nBlocks = nBlocks;
+  out.nActive = (int)bids.size();
+  out.elemBytes = 4;
+  out.nThreadsUsed = 1;
+  fwrite(&out, sizeof(out), 1, fout);
+  fwrite(bids.data(), 4, bids.size(), fout);
+  fwrite(halo.data(), 4, halo.size(), fout);
+  MultiresSparseGrid::destroy(msbg);
+  return 0;
+}
+
+// setRefinementMap's outputs beyond the per-block levels and flags (src/msbg.cpp:1428-2165):
+// the block lists _blocksExisting and _blocksFineCoarsePerLevel[l] (each sorted: the
+// release fills them from per-thread parts in no fixed order), and the fine-coarse distance
+// channel CH_DIST_FINECOARSE of every level (value blocks with their uint16 data, then the
+// full blocks).  Same grid and calls as the levels job.
+int runLayoutJob(const OracleJobHeader &job, const int32_t *levelsIn, FILE *fout) {
+  OracleOutHeader out;
+  memset(&out, 0, sizeof(out));
+  memcpy(out.magic, ORACLE_OUT_MAGIC, 8);
+  MultiresSparseGrid *msbg = MultiresSparseGrid::create(
+      "TEST", job.sx, job.sy, job.sz, job.bsx, -1, 0, -1, 0, NULL, NULL, job.nLevels);
+  if (!msbg) return 2;
+  const int nBlocks = msbg->nBlocks();
+  if ((int64_t)nBlocks != job.nBlocksIn) return 4;
+  std::vector<int> levels(levelsIn, levelsIn + nBlocks);
+  msbg->regularizeRefinementMap(levels.data());
+  msbg->setRefinementMap(levels.data(), NULL, 0, NULL, false, false);
+  out.nBlocks = nBlocks;
+  fwrite(&out, sizeof(out), 1, fout);
+  auto dumpList = [&](std::vector<int> v) {
+    std::sort(v.begin(), v.end());
+    const int32_t n = (int32_t)v.size();
+    fwrite(&n, 4, 1, fout);
+    fwrite(v.data(), 4, v.size(), fout);
+  };
+  dumpList(msbg->_blocksExisting);
+  for (int l = 0; l < job.nLevels; l++) dumpList(msbg->_blocksFineCoarsePerLevel[l]);
+  for (int l = 0; l < job.nLevels; l++) {
+    SparseGrid<uint16_t> *sg = msbg->getDistFineCoarseChannel(l);
+    if (!sg) return 3;
+    std::vector<int> val, full;
+    for (int b = 0; b < nBlocks; b++) {
+      if (sg->isValueBlock(b)) val.push_back(b);
+      else if (sg->isFullBlock(b)) full.push_back(b);
+    }
+    dumpList(val);
+    for (int b : val) fwrite(sg->getBlockDataPtr(b, 0, 0), 2, (size_t)sg->nVoxelsInBlock(), fout);
+    dumpList(full);
+    const uint16_t fv = sg->getFullValue();
+    fwrite(&fv, 2, 1, fout);
+  }
+  MultiresSparseGrid::destroy(msbg);
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -757,7 +874,9 @@ int main(int argc, char **argv) {
     if (!solverArrays.empty() && fread(solverArrays.data(), 4, solverArrays.size(), fin) != solverArrays.size())
       return 1;
   }
-  if (job.jobType == ORACLE_JOB_HALO || job.jobType == ORACLE_JOB_DOWNSAMPLE) {
+  std::vector<int32_t> fstate, dbc(6, 0);
+  std::vector<std::vector<uint16_t>> flagPay;
+  if (job.jobType == ORACLE_JOB_HALO || job.jobType == ORACLE_JOB_DOWNSAMPLE || job.jobType == ORACLE_JOB_HALO3) {
     const size_t elem = job.chanType == ORACLE_CHAN_U16 ? 2 : 4;
     state.resize((size_t)job.nLevels * job.nBlocksIn);
     if (fread(state.data(), 4, state.size(), fin) != state.size()) return 1;
@@ -769,6 +888,20 @@ int main(int argc, char **argv) {
       levelPay[l].resize((size_t)(mx + 1) * bs * bs * bs * elem);
       if (!levelPay[l].empty() && fread(levelPay[l].data(), 1, levelPay[l].size(), fin) != levelPay[l].size())
         return 1;
+    }
+    if (job.jobType == ORACLE_JOB_HALO3) {  // then the flags' states and payloads, and the domain's boundaries
+      fstate.resize((size_t)job.nLevels * job.nBlocksIn);
+      if (fread(fstate.data(), 4, fstate.size(), fin) != fstate.size()) return 1;
+      flagPay.resize(job.nLevels);
+      for (int l = 0; l < job.nLevels; l++) {
+        int32_t mx = -1;
+        for (int64_t b = 0; b < job.nBlocksIn; b++) mx = std::max(mx, fstate[(size_t)l * job.nBlocksIn + b]);
+        const size_t bs = (size_t)(job.bsx >> l);
+        flagPay[l].resize((size_t)(mx + 1) * bs * bs * bs);
+        if (!flagPay[l].empty() && fread(flagPay[l].data(), 2, flagPay[l].size(), fin) != flagPay[l].size())
+          return 1;
+      }
+      if (fread(dbc.data(), 4, 6, fin) != 6) return 1;
     }
   }
   if (job.jobType == ORACLE_JOB_INTERP || job.jobType == ORACLE_JOB_RENDER) {
@@ -790,8 +923,14 @@ int main(int argc, char **argv) {
   int rc;
   if (job.jobType == ORACLE_JOB_LEVELS)
     rc = runLevelsJob(job, lv.data(), fout);
+  else if (job.jobType == ORACLE_JOB_LAYOUT)
+    rc = runLayoutJob(job, lv.data(), fout);
   else if (job.jobType == ORACLE_JOB_SOLVER)
     rc = runSolverJob(job, lv.data(), solverArrays.data(), fout);
+  else if (job.jobType == ORACLE_JOB_HALO3)
+    rc = job.chanType == ORACLE_CHAN_F32
+             ? runHalo3Job(job, lv.data(), state.data(), levelPay, fstate.data(), flagPay, dbc.data(), fout)
+             : 7;
   else if (job.jobType == ORACLE_JOB_DOWNSAMPLE)
     rc = job.chanType == ORACLE_CHAN_F32 ? runDownsampleJob(job, lv.data(), state.data(), levelPay, fout) : 7;
   else if (job.jobType == ORACLE_JOB_MORTON)

@@ -15,8 +15,10 @@ reference_render.npz (ray-march render), reference_morton.npz (Morton-ordered bl
 lists), reference_solver.npz (the solver building blocks and the block smoother),
 reference_downsample.npz (downsampleFloatChannelNew on multi-level channels) and
 reference_surface512.npz (the 512^3 surface workload at full size: layout, counters,
-per-block sums and a voxel sample of the fields).  Arguments name a subset
-(small interp halo render morton solver downsample surface512).
+per-block sums and a voxel sample of the fields), reference_halo3.npz (the solver's halo,
+fillHaloBlock3) and reference_layout.npz (setRefinementMap's block lists and fine-coarse
+distance channel).  Arguments name a subset
+(small interp halo render morton solver downsample surface512 halo3 layout).
 """
 from __future__ import annotations
 
@@ -63,7 +65,8 @@ SWEEP_CASES = [
 def main(which: list[str]) -> None:
     if not O.ref_available():
         raise SystemExit("oracle/_ref/msbg_ref_driver missing: run `make -C oracle ref` first")
-    parts = set(which) or {"small", "interp", "halo", "render", "morton", "solver", "downsample", "surface512"}
+    parts = set(which) or {"small", "interp", "halo", "render", "morton", "solver", "downsample", "surface512",
+                           "halo3", "layout"}
     if parts & {"small", "interp", "render"}:
         out = make_small()
         if "interp" in parts:
@@ -80,6 +83,10 @@ def main(which: list[str]) -> None:
         make_downsample()
     if "surface512" in parts:
         make_surface512()
+    if "halo3" in parts:
+        make_halo3()
+    if "layout" in parts:
+        make_layout()
 
 
 def make_small() -> dict:
@@ -296,6 +303,46 @@ def make_downsample() -> None:
 
 
 SURFACE512_SAMPLE = 60000
+
+
+def make_layout() -> None:
+    """setRefinementMap's block lists and CH_DIST_FINECOARSE (oracle/ref_driver.cpp, layout
+    job) on the 3- and 4-level maps of reference_small.npz."""
+    small = dict(np.load(os.path.join(HERE, "reference_small.npz")))
+    out = {}
+    for nl in (3, 4):
+        r = O.run_reference_layout(8 * BSX, 8 * BSX, 8 * BSX, BSX, nl, small[f"lvl{nl}_in"])
+        out[f"lvl{nl}_existing"] = r["existing"]
+        for l in range(nl):
+            out[f"lvl{nl}_fine_coarse{l}"] = r["fine_coarse"][l]
+            d = r["dist"][l]
+            out[f"lvl{nl}_dist{l}_value_bids"] = d["value_bids"]
+            out[f"lvl{nl}_dist{l}_value"] = d["value"]
+            out[f"lvl{nl}_dist{l}_full_bids"] = d["full_bids"]
+            out[f"lvl{nl}_dist{l}_full_value"] = np.uint16(d["full_value"])
+    path = os.path.join(HERE, "reference_layout.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
+
+
+def make_halo3() -> None:
+    """HaloBlockSet::fillHaloBlock3 at multigrid level 0 (oracle/ref_driver.cpp, halo3 job) of
+    every level-0 block of seeded 3-level FP32 channels with seeded cell flags, for the domain
+    boundary types of tests/halo_cases.py."""
+    import halo_cases as H
+    import port as P
+    out = {}
+    for nb, bsx, seed, dbc in H.HALO3_CASES:
+        lv, st, pay = H.halo_case(nb, bsx, 3, seed, "f32", lambda *a: P.regularize(*a)[0])
+        fst, fpay, ef, ff = H.flags_case(st, bsx, seed + 100)
+        key = "x".join(map(str, nb)) + f"_bs{bsx}"
+        bids, vals = O.run_reference_halo3(*(n * bsx for n in nb), bsx, 3, lv, st, pay, fst, fpay, dbc,
+                                           H.DOWNSAMPLE_EMPTY, H.DOWNSAMPLE_FULL, ef, ff)
+        out[f"{key}_bids"] = bids
+        out[f"{key}_halo"] = vals
+    path = os.path.join(HERE, "reference_halo3.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
 
 
 def make_surface512() -> None:

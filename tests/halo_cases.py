@@ -22,6 +22,10 @@ LBLK_EMPTY, LBLK_FULL, LBLK_NONE = -1, -2, -3
 DOWNSAMPLE_CASES = (((4, 4, 4), 16, 20261203 + 960), ((5, 3, 4), 8, 20261203 + 961),
                     ((3, 3, 2), 32, 20261203 + 962))
 DOWNSAMPLE_EMPTY, DOWNSAMPLE_FULL = 0.25, 0.75
+# the solver's halo (fillHaloBlock3): (block grid, block edge, seed, domain boundary types of
+# faces -x,+x,-y,+y,-z,+z; 0 open, 1 solid)
+HALO3_CASES = (((4, 4, 4), 16, 20261203 + 980, (0, 1, 0, 1, 1, 0)),
+               ((5, 3, 4), 8, 20261203 + 981, (1, 1, 0, 0, 1, 0)))
 
 
 def halo_case(nb, bsx: int, n_levels: int, seed: int, kind: str, regularize):
@@ -65,3 +69,21 @@ def halo_case(nb, bsx: int, n_levels: int, seed: int, kind: str, regularize):
 def blocks_at(lv, states, level):
     """Blocks whose level is `level` and that have a block at that level, ascending."""
     return np.nonzero((np.asarray(lv) == level) & (states[level] != LBLK_NONE))[0].astype(np.int32)
+
+
+# cell flags (src/msbg.h:602-614): the two the solver's halo reads, and others it ignores
+CELL_SOLID, CELL_PARTIAL_SOLID, CELL_VOID, CELL_AIR = 1 << 0, 1 << 6, 1 << 12, 1 << 2
+
+
+def flags_case(states, bsx: int, seed: int):
+    """Cell flags for the levels of a halo case: the same block states as the values, each
+    payload cell CELL_VOID (8 %), CELL_SOLID (8 %) or other bits; constant blocks' flags."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    fpay = []
+    for l, st in enumerate(states):
+        n = int(st.max()) + 1 if len(st) and st.max() >= 0 else 0
+        u = rng.random((n, (bsx >> l) ** 3))
+        f = np.where(u < 0.08, CELL_VOID, np.where(u < 0.16, CELL_SOLID, np.where(u < 0.5, CELL_PARTIAL_SOLID,
+                                                                                     CELL_AIR)))
+        fpay.append(f.astype(np.uint16))
+    return [s.copy() for s in states], fpay, CELL_VOID | CELL_AIR, CELL_AIR

@@ -296,3 +296,70 @@ def test_gpu_restrict_level_equals_downsample_channel(gpulib):
             d_st.free()
     finally:
         g.close()
+
+
+# ---------------------------------------------------------------- the solver's halo (fillHaloBlock3)
+
+H3_GOLDEN = os.path.join(ROOT, "tests", "golden", "reference_halo3.npz")
+
+
+def _halo3_case(port, nb, bsx, seed):
+    lv, st, pay = H.halo_case(nb, bsx, 3, seed, "f32", _reg(port))
+    fst, fpay, ef, ff = H.flags_case(st, bsx, seed + 100)
+    return lv, st, pay, fst, fpay, ef, ff
+
+
+def test_halo3_restatement_matches_reference_fixture(port):
+    """fillHaloBlock3 (src/halo.cpp:536-738): the restatement equals the reference bit for bit,
+    markers (+1e20 void / open faces, -1e20 solid / closed faces) included."""
+    gold = dict(np.load(H3_GOLDEN))
+    for nb, bsx, seed, dbc in H.HALO3_CASES:
+        lv, st, pay, fst, fpay, ef, ff = _halo3_case(port, nb, bsx, seed)
+        key = "x".join(map(str, nb)) + f"_bs{bsx}"
+        bids = gold[f"{key}_bids"]
+        assert np.array_equal(bids, np.nonzero(lv == 0)[0])
+        g = port.grid(nb[0] * bsx, nb[1] * bsx, nb[2] * bsx, bsx, port.F32)
+        out, sk = port.fill_halo3(g, lv, st, pay, fst, fpay, bids, dbc, H.DOWNSAMPLE_EMPTY, H.DOWNSAMPLE_FULL, ef, ff)
+        assert sk == 0
+        assert _same(out, gold[f"{key}_halo"]), key
+        assert (np.abs(out) == 1e20).mean() > 0.05  # the markers are exercised
+
+
+def test_halo3_restatement_matches_fresh_reference(port):
+    import oracle_io as O
+    if not O.ref_available():
+        pytest.skip("the reference is not built on this host")
+    nb, bsx, dbc = (3, 3, 2), 32, (0, 0, 1, 0, 0, 1)
+    lv, st, pay, fst, fpay, ef, ff = _halo3_case(port, nb, bsx, 20261203 + 985)
+    sx, sy, sz = (n * bsx for n in nb)
+    bids, ref = O.run_reference_halo3(sx, sy, sz, bsx, 3, lv, st, pay, fst, fpay, dbc, 0.1, 0.9, ef, ff)
+    g = port.grid(sx, sy, sz, bsx, port.F32)
+    out, _ = port.fill_halo3(g, lv, st, pay, fst, fpay, bids, dbc, 0.1, 0.9, ef, ff)
+    assert _same(out, ref)
+
+
+@pytest.mark.gpu
+def test_gpu_halo3_matches_reference_fixture_and_restatement(gpulib, port):
+    G = gpulib
+    gold = dict(np.load(H3_GOLDEN))
+    cases = list(H.HALO3_CASES) + [((3, 3, 2), 32, 20261203 + 985, (0, 0, 1, 0, 0, 1))]
+    for nb, bsx, seed, dbc in cases:
+        lv, st, pay, fst, fpay, ef, ff = _halo3_case(port, nb, bsx, seed)
+        g = _gpu_grid(G, nb, bsx, 3, lv, st, pay, G.F32, H.DOWNSAMPLE_EMPTY, H.DOWNSAMPLE_FULL, lchan=2)
+        try:
+            for l in range(3):
+                g.level_flags_set(5, l, fst[l], fpay[l] if len(fpay[l]) else None, ef, ff)
+            bids = np.nonzero(lv == 0)[0].astype(np.int32)
+            # a block of another level in the list is skipped
+            extra = np.nonzero(lv != 0)[0][:1].astype(np.int32)
+            out, sk = g.fillHaloBlock3(2, 5, np.concatenate([bids, extra]), dbc)
+            assert sk == len(extra)
+            og = port.grid(nb[0] * bsx, nb[1] * bsx, nb[2] * bsx, bsx, port.F32)
+            want, _ = port.fill_halo3(og, lv, st, pay, fst, fpay, bids, dbc, H.DOWNSAMPLE_EMPTY, H.DOWNSAMPLE_FULL,
+                                      ef, ff)
+            assert _same(out[: len(bids)], want), (nb, bsx)
+            key = "x".join(map(str, nb)) + f"_bs{bsx}"
+            if f"{key}_halo" in gold:
+                assert _same(out[: len(bids)], gold[f"{key}_halo"]), key
+        finally:
+            g.close()
