@@ -73,11 +73,36 @@ def test_gpu_matches_reference_fixture(gpulib, golden, lg):
             g.set_levels(golden[f"lvl{nl}_in"])
             g.regularizeRefinementMap()
             g.setRefinementMap(0.0)
-            assert np.array_equal(g.flags(), golden[f"lvl{nl}_flags"])
-            assert np.array_equal(g.block_list(g.LIST_EXISTING), lg[f"lvl{nl}_existing"])
+            # The levels-only reference job allocates no channel data, so no block of it carries
+            # BLK_EXISTS; this library gives every level-0 block its value block (and the bit).
+            keep = np.uint16(0xFFFF & ~BLK_EXISTS)
+            assert np.array_equal(g.flags() & keep, golden[f"lvl{nl}_flags"])
+            assert len(lg[f"lvl{nl}_existing"]) == 0
+            lv = golden[f"lvl{nl}_out"]
+            assert np.array_equal(g.block_list(g.LIST_EXISTING), np.nonzero(lv == 0)[0])
             for l in range(nl):
                 assert np.array_equal(g.block_list(g.LIST_FINE_COARSE, l), lg[f"lvl{nl}_fine_coarse{l}"])
                 state, data = g.dist_fine_coarse(l)
                 _check_dist(state, data, lg, nl, l)
         finally:
             g.close()
+
+
+@pytest.mark.gpu
+def test_gpu_existing_blocks_of_the_demo_pipeline(gpulib, golden):
+    """_blocksExisting of the reference's demo pipeline (reference_small.npz: levels, flags and
+    active blocks after setRefinementMap with value blocks) equals this library's list."""
+    G = gpulib
+    res, bsx = int(golden["res"]), int(golden["bsx"])
+    want = np.nonzero(golden["flags"] & BLK_EXISTS)[0]
+    assert np.array_equal(want, golden["active_bids"])
+    g = G.MultiresSparseGrid(res, res, res, bsx, 3, G.F32)
+    try:
+        g.set_levels(golden["levels"].astype(np.int32))
+        g.regularizeRefinementMap()
+        g.setRefinementMap(0.0)
+        assert np.array_equal(g.levels(), golden["levels"])
+        assert np.array_equal(g.flags(), golden["flags"])
+        assert np.array_equal(g.block_list(g.LIST_EXISTING), want)
+    finally:
+        g.close()
