@@ -168,11 +168,22 @@ int msbg_gpu_fill(msbg_gpu_ctx *ctx, int chan, double value);
 /* ---- splat --------------------------------------------------------------------
  * Splat of min(distSq/distSqMax) into channel 0 (src/msbg_demo.cpp:527-636):
  * a particle is abandoned at its first (z,y,x scan order) in-sphere voxel that
- * lies in a non-value block, as the demo does.  Min is order-independent, so
- * one launch replaces the demo's 8 color passes.  Then the distance-to-density
+ * lies in a non-value block, as the demo does.  The particles are sorted into
+ * lists of the value blocks their boxes touch, and each value block takes the
+ * minimum over its list; min is order-independent, so this replaces the demo's
+ * 8 color passes over its per-block lists.  Then the distance-to-density
  * finalize (src/msbg_demo.cpp:655-680). */
 int msbg_gpu_splat(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rParticle,
                    float nbDist);
+/* The demo's per-block particle lists particlesPerBlock (src/msbg_demo.cpp:349-390):
+ * every point that passes the marking loop's domain tests, in the list of the
+ * block that contains it.  CSR form in caller device arrays: dOffsets[nBlocks+1]
+ * (int64; block b's list is dIndex[dOffsets[b] .. dOffsets[b+1]-1]) and dIndex
+ * (int32 point indices, capacity n).  *hCount = the listed points (the demo's
+ * nActParticles).  The order inside a list is unspecified, as in the reference,
+ * whose lists are lock-free stacks filled by a parallel loop. */
+int msbg_gpu_particles_per_block(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, int64_t *dOffsets,
+                                 int32_t *dIndex, int64_t *hCount);
 int msbg_gpu_splat_finalize(msbg_gpu_ctx *ctx, float rParticle, float nbDist);
 
 /* ---- block lists ------------------------------------------------------------------

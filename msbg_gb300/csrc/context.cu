@@ -75,13 +75,21 @@ __device__ int64_t blockExclusive(int64_t v, int64_t *total) {
   return warpOff + inc - v;
 }
 
+// FLAGS: scan the 0/1 flags of the inputs (in[i] != 0); otherwise the values
+// themselves (non-negative counts).
+template <bool FLAGS>
+__device__ __forceinline__ int64_t scanItem(int32_t v) {
+  if constexpr (FLAGS) return v != 0; else return (int64_t)v;
+}
+
+template <bool FLAGS>
 __global__ void kScanReduce(const int32_t *__restrict__ in, int64_t n, int64_t *__restrict__ part) {
   const int64_t base = (int64_t)blockIdx.x * kScanTile;
   int64_t s = 0;
 #pragma unroll
   for (int k = 0; k < kScanItems; k++) {
     const int64_t i = base + (int64_t)k * kScanThreads + threadIdx.x;
-    if (i < n) s += in[i] != 0;
+    if (i < n) s += scanItem<FLAGS>(in[i]);
   }
   int64_t tot;
   blockExclusive(s, &tot);
@@ -102,6 +110,7 @@ __global__ void kScanPartials(int64_t *part, int64_t nPart, int64_t *total) {
   if (threadIdx.x == 0) *total = carry;
 }
 
+template <bool FLAGS>
 __global__ void kScanApply(const int32_t *__restrict__ in, int64_t n, const int64_t *__restrict__ part,
                            int64_t *__restrict__ out) {
   const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
@@ -110,7 +119,7 @@ __global__ void kScanApply(const int32_t *__restrict__ in, int64_t n, const int6
 #pragma unroll
   for (int k = 0; k < kScanItems; k++) {
     const int64_t i = base + k;
-    v[k] = (i < n && in[i] != 0) ? 1 : 0;
+    v[k] = i < n ? scanItem<FLAGS>(in[i]) : 0;
     s += v[k];
   }
   int64_t tot;
@@ -123,13 +132,23 @@ __global__ void kScanApply(const int32_t *__restrict__ in, int64_t n, const int6
   }
 }
 
+template <bool FLAGS>
+static int exclusiveScanT(msbg_gpu_ctx *ctx, const int32_t *dIn, int64_t n, int64_t *dOut, int64_t *dTotal,
+                          int64_t *dPartial) {
+  const int64_t nPart = (n + kScanTile - 1) / kScanTile;
+  MSBG_LAUNCH(ctx, kScanReduce<FLAGS>, (unsigned)nPart, kScanThreads, 0, dIn, n, dPartial);
+  MSBG_LAUNCH(ctx, kScanPartials, 1, kScanThreads, 0, dPartial, nPart, dTotal);
+  MSBG_LAUNCH(ctx, kScanApply<FLAGS>, (unsigned)nPart, kScanThreads, 0, dIn, n, dPartial, dOut);
+  return MSBG_GPU_OK;
+}
+
 int exclusiveScanFlagsWith(msbg_gpu_ctx *ctx, const int32_t *dIn, int64_t n, int64_t *dOut,
                            int64_t *dTotal, int64_t *dPartial) {
-  const int64_t nPart = (n + kScanTile - 1) / kScanTile;
-  MSBG_LAUNCH(ctx, kScanReduce, (unsigned)nPart, kScanThreads, 0, dIn, n, dPartial);
-  MSBG_LAUNCH(ctx, kScanPartials, 1, kScanThreads, 0, dPartial, nPart, dTotal);
-  MSBG_LAUNCH(ctx, kScanApply, (unsigned)nPart, kScanThreads, 0, dIn, n, dPartial, dOut);
-  return MSBG_GPU_OK;
+  return exclusiveScanT<true>(ctx, dIn, n, dOut, dTotal, dPartial);
+}
+
+int exclusiveScanCounts(msbg_gpu_ctx *ctx, const int32_t *dIn, int64_t n, int64_t *dOut, int64_t *dTotal) {
+  return exclusiveScanT<false>(ctx, dIn, n, dOut, dTotal, ctx->dScanPartial);
 }
 
 int64_t scanPartialCount(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
@@ -137,6 +156,26 @@ int64_t scanPartialCount(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
 int exclusiveScanFlags(msbg_gpu_ctx *ctx, const int32_t *dIn, int64_t n, int64_t *dOut,
                        int64_t *dTotal) {
   return exclusiveScanFlagsWith(ctx, dIn, n, dOut, dTotal, ctx->dScanPartial);
+}
+
+int copyAsyncSplit(msbg_gpu_ctx *ctx, void *dst, const void *src, size_t bytes, cudaMemcpyKind kind) {
+  constexpr size_t kSplitBytes = size_t(64) << 20;
+  if (bytes < kSplitBytes) {
+    MSBG_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, kind, ctx->stream));
+    return MSBG_GPU_OK;
+  }
+  if (!ctx->copyStream) {
+    MSBG_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copyStream, cudaStreamNonBlocking));
+    for (auto &e : ctx->copyEv) MSBG_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  const size_t half = (bytes / 2 + 4095) & ~size_t(4095);
+  MSBG_CUDA(ctx, cudaEventRecord(ctx->copyEv[0], ctx->stream));
+  MSBG_CUDA(ctx, cudaStreamWaitEvent(ctx->copyStream, ctx->copyEv[0], 0));
+  MSBG_CUDA(ctx, cudaMemcpyAsync((char *)dst + half, (const char *)src + half, bytes - half, kind, ctx->copyStream));
+  MSBG_CUDA(ctx, cudaMemcpyAsync(dst, src, half, kind, ctx->stream));
+  MSBG_CUDA(ctx, cudaEventRecord(ctx->copyEv[1], ctx->copyStream));
+  MSBG_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->copyEv[1], 0));
+  return MSBG_GPU_OK;
 }
 
 int ensureTmpSlab(msbg_gpu_ctx *ctx, size_t bytes) {
@@ -389,6 +428,17 @@ extern "C" int msbg_gpu_create(msbg_gpu_ctx **out, int sx, int sy, int sz, int b
   ALLOC(ctx->dStatus, 16);
 #undef ALLOC
   if (e == cudaSuccess) e = cudaMallocHost((void **)&ctx->hCounters, kNumCounters * 8);
+  if (e == cudaSuccess) {
+    // per-call scratch (splat lists, list copies) comes from the device's
+    // stream-ordered pool: keep what it has allocated for the next call instead of
+    // returning it at every synchronization (a property of this process's pool)
+    int dev = 0;
+    cudaMemPool_t pool;
+    uint64_t keep = ~0ull;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetDefaultMemPool(&pool, dev);
+    if (e == cudaSuccess) e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
   for (int i = 0; i < kMaxEvents && e == cudaSuccess; i++) e = cudaEventCreate(&ctx->ev[i]);
   for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&ctx->stageEv[i]);
   if (e == cudaSuccess) e = cudaMemset(ctx->dMark, 0, nB * 4);
@@ -426,6 +476,11 @@ extern "C" int msbg_gpu_destroy(msbg_gpu_ctx *ctx) {
   msbg::poissonFree(ctx->poisson);
   for (auto &ev : ctx->ev) if (ev) cudaEventDestroy(ev);
   for (auto &ev : ctx->stageEv) if (ev) cudaEventDestroy(ev);
+  for (auto &ev : ctx->copyEv) if (ev) cudaEventDestroy(ev);
+  if (ctx->copyStream) {
+    cudaStreamSynchronize(ctx->copyStream);
+    cudaStreamDestroy(ctx->copyStream);
+  }
   delete ctx;
   return MSBG_GPU_OK;
 }
@@ -694,8 +749,7 @@ extern "C" int msbg_gpu_upload_payload(msbg_gpu_ctx *ctx, int chan, const void *
   int rc = checkChan(ctx, chan);
   if (rc) return rc;
   const size_t bytes = (size_t)ctx->nActive * ctx->voxPerBlock * storageBytes(ctx->ch[chan].storage);
-  if (bytes)
-    MSBG_CUDA(ctx, cudaMemcpyAsync(ctx->ch[chan].d, hData, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  if (bytes) return copyAsyncSplit(ctx, ctx->ch[chan].d, hData, bytes, cudaMemcpyHostToDevice);
   return MSBG_GPU_OK;
 }
 
@@ -704,8 +758,7 @@ extern "C" int msbg_gpu_download_payload(msbg_gpu_ctx *ctx, int chan, void *hDat
   int rc = checkChan(ctx, chan);
   if (rc) return rc;
   const size_t bytes = (size_t)ctx->nActive * ctx->voxPerBlock * storageBytes(ctx->ch[chan].storage);
-  if (bytes)
-    MSBG_CUDA(ctx, cudaMemcpyAsync(hData, ctx->ch[chan].d, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  if (bytes && (rc = copyAsyncSplit(ctx, hData, ctx->ch[chan].d, bytes, cudaMemcpyDeviceToHost))) return rc;
   MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return MSBG_GPU_OK;
 }
@@ -733,6 +786,13 @@ extern "C" int msbg_gpu_splat(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, f
   if ((double)(rParticle + nbDist) * 2.0 + 1.0 > (double)ctx->bsx)
     return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "splat box wider than a block");
   return splatRun(ctx, dPts, n, rParticle, nbDist);
+}
+
+extern "C" int msbg_gpu_particles_per_block(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, int64_t *dOffsets,
+                                            int32_t *dIndex, int64_t *hCount) {
+  if (!ctx || n < 0 || (n > 0 && (!dPts || !dIndex)) || !dOffsets || !hCount) return MSBG_GPU_ERR_ARG;
+  if (n > (int64_t)0x7fffffff) return fail(ctx, MSBG_GPU_ERR_ARG, "particles_per_block: %lld points", (long long)n);
+  return particlesPerBlockRun(ctx, dPts, n, dOffsets, dIndex, hCount);
 }
 
 extern "C" int msbg_gpu_splat_finalize(msbg_gpu_ctx *ctx, float rParticle, float nbDist) {
@@ -789,7 +849,10 @@ extern "C" int msbg_gpu_surface_job(msbg_gpu_ctx *ctx, const float *hPts, int64_
     MSBG_CUDA(ctx, cudaMalloc(&ctx->dPts, (size_t)n * 12));
     ctx->ptsCap = n;
   }
-  if (n) MSBG_CUDA(ctx, cudaMemcpyAsync(ctx->dPts, hPts, (size_t)n * 12, cudaMemcpyHostToDevice, ctx->stream));
+  if (n) {
+    int r = copyAsyncSplit(ctx, ctx->dPts, hPts, (size_t)n * 12, cudaMemcpyHostToDevice);
+    if (r) return r;
+  }
   int rc = stage();
   if (!rc) {
     if (nBands > 0) {
@@ -814,7 +877,7 @@ extern "C" int msbg_gpu_surface_job(msbg_gpu_ctx *ctx, const float *hPts, int64_
   if (hOut) {
     const size_t bytes = (size_t)ctx->nActive * ctx->voxPerBlock * storageBytes(ctx->ch[0].storage);
     if (bytes > hOutCap) return fail(ctx, MSBG_GPU_ERR_ARG, "output buffer too small (%zu < %zu)", hOutCap, bytes);
-    MSBG_CUDA(ctx, cudaMemcpyAsync(hOut, ctx->ch[0].d, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if ((rc = copyAsyncSplit(ctx, hOut, ctx->ch[0].d, bytes, cudaMemcpyDeviceToHost))) return rc;
   }
   if ((rc = stage())) return rc;
   MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

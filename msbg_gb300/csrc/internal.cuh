@@ -50,6 +50,8 @@ struct msbg_gpu_ctx {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[msbg::kMaxEvents] = {};
   cudaEvent_t stageEv[8] = {};   // msbg_gpu_surface_job: events at its stage boundaries
+  cudaStream_t copyStream = nullptr;        // second copy engine for large host transfers
+  cudaEvent_t copyEv[2] = {};               // fork / join of a split copy
   int stageCount = 0;            // events recorded by the last surface job
 
   // layout (device)
@@ -133,6 +135,13 @@ int exclusiveScanFlags(msbg_gpu_ctx *ctx, const int32_t *dIn, int64_t n, int64_t
 int exclusiveScanFlagsWith(msbg_gpu_ctx *ctx, const int32_t *dIn, int64_t n, int64_t *dOut,
                            int64_t *dTotal, int64_t *dPartial);
 int64_t scanPartialCount(int64_t n);
+// Exclusive scan of non-negative int32 counts (n <= nBlocks) -> int64 offsets, total in *dTotal.
+int exclusiveScanCounts(msbg_gpu_ctx *ctx, const int32_t *dIn, int64_t n, int64_t *dOut, int64_t *dTotal);
+
+// Host <-> device copy on the context's stream; above 64 MiB the second half goes
+// through a second stream, so two copy engines move it (ordered like one copy on
+// the context's stream).
+int copyAsyncSplit(msbg_gpu_ctx *ctx, void *dst, const void *src, size_t bytes, cudaMemcpyKind kind);
 
 // Ensure the temp slab can hold `bytes`.
 int ensureTmpSlab(msbg_gpu_ctx *ctx, size_t bytes);
@@ -140,6 +149,8 @@ int ensureTmpSlab(msbg_gpu_ctx *ctx, size_t bytes);
 // Per-file entry points used by the ABI layer.
 int splatRun(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rParticle, float nbDist);
 int splatFinalizeRun(msbg_gpu_ctx *ctx, float rParticle, float nbDist);
+int particlesPerBlockRun(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, int64_t *dOff, int32_t *dIndex,
+                         int64_t *count);
 int fillChannel(msbg_gpu_ctx *ctx, int chan, double v);
 // Sweeps over all value blocks (dList NULL) or the listed blocks (device block ids).
 int pdeRun(msbg_gpu_ctx *ctx, int chan, int laplTyp, int constr01, int numIter, float dt,

@@ -1,11 +1,14 @@
 // Particle splat and distance-to-density finalize (channel 0).
 //
 // Reference: the demo's 8-color lockless splat (src/msbg_demo.cpp:527-636) and
-// finalize (src/msbg_demo.cpp:655-680).  The CPU code needs the 8 colors so that
-// threads never write the same block concurrently; on the GPU every write is an
-// atomicMin on the float's bit pattern (distances are non-negative, so their bit
-// patterns order like the floats), which is order-independent: one launch over
-// all particles gives the same field as the colored passes.
+// finalize (src/msbg_demo.cpp:655-680).  The CPU code walks per-block particle
+// lists in 8 colors so that threads never write the same block concurrently.
+// Here the particles are sorted by the value blocks their splat boxes touch (a
+// counting sort: count, scan, scatter), and one CTA per value block takes the
+// minimum of its particles' values in shared memory (atomicMin on the float's bit
+// pattern: distances are non-negative, so their bit patterns order like the
+// floats) and writes the block once.  The minimum is order-independent, so this
+// gives the same field as the colored passes.
 //
 // The minimum is taken in FP32.  For uint16 / FP16 storage the splat runs into an
 // FP32 staging slab and the finalize quantizes the minimum to the storage type
@@ -58,115 +61,196 @@ struct SplatGeom {
   float rScan, distSqMax, distSqMaxInv;
 };
 
-// One warp per particle.  The lanes walk the particle's clipped voxel box in the
-// demo's z,y,x scan order (flattened).  Abort rule (src/msbg_demo.cpp:613-618):
-// the particle stops at the first in-sphere voxel whose block is not a value
-// block; voxels before it in scan order keep their writes.  The box spans at most
-// two blocks per axis, so the warp first checks those blocks: if all are value
-// blocks nothing can abort (the common case); otherwise it finds the earliest
-// aborting scan index with a warp min-reduction and writes only voxels before it.
-__global__ void __launch_bounds__(256) kSplat(const float *__restrict__ pts, int64_t n, SplatGeom g,
-                                              const int32_t *__restrict__ slot,
-                                              float *__restrict__ dst,
-                                              unsigned long long *__restrict__ nAborted) {
-  const int64_t warpId = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warpId >= n) return;
-  const float px = pts[3 * warpId], py = pts[3 * warpId + 1], pz = pts[3 * warpId + 2];
-  // domain tests of the marking loop (src/msbg_demo.cpp:358-360)
+// A particle's splat box (src/msbg_demo.cpp:571-592): voxels [i1, i2] per axis,
+// the voxel centres within rScan of the particle, clamped to the grid.
+struct SplatBox {
+  int ix1, iy1, iz1, ix2, iy2, iz2;
+  float x0, y0, z0;  // particle position - 0.5 (voxel centre offsets)
+};
+
+__device__ __forceinline__ bool splatBox(const SplatGeom &g, float px, float py, float pz, SplatBox &b) {
+  const float r = g.rScan;
+  b.ix1 = max((int)ceilf(__fsub_rn(__fsub_rn(px, r), 0.5f)), 0);
+  b.iy1 = max((int)ceilf(__fsub_rn(__fsub_rn(py, r), 0.5f)), 0);
+  b.iz1 = max((int)ceilf(__fsub_rn(__fsub_rn(pz, r), 0.5f)), 0);
+  b.ix2 = min((int)floorf(__fsub_rn(__fadd_rn(px, r), 0.5f)), g.sx - 1);
+  b.iy2 = min((int)floorf(__fsub_rn(__fadd_rn(py, r), 0.5f)), g.sy - 1);
+  b.iz2 = min((int)floorf(__fsub_rn(__fadd_rn(pz, r), 0.5f)), g.sz - 1);
+  b.x0 = __fsub_rn(px, 0.5f); b.y0 = __fsub_rn(py, 0.5f); b.z0 = __fsub_rn(pz, 0.5f);
+  return b.ix2 >= b.ix1 && b.iy2 >= b.iy1 && b.iz2 >= b.iz1;
+}
+
+// Pass 1, one thread per particle.  Valid particles (the marking loop's domain
+// tests, src/msbg_demo.cpp:358-360, and an owning value block: the demo walks the
+// particle lists of value blocks only, src/msbg_demo.cpp:541-566) get their abort
+// index: the scan position (z, y, x order over the box) of the first in-sphere
+// voxel whose block is not a value block (src/msbg_demo.cpp:613-618), or the box
+// size.  Voxels from that position on are not written.  Every value block the box
+// touches (at most two per axis) counts the particle once.  abortAt = 0 marks a
+// particle that writes nothing.
+__global__ void __launch_bounds__(256) kSplatCount(const float *__restrict__ pts, int64_t n, SplatGeom g,
+                                                   const int32_t *__restrict__ slot, int32_t *__restrict__ abortAt,
+                                                   int32_t *__restrict__ cnt,
+                                                   unsigned long long *__restrict__ nAborted) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float px = pts[3 * i], py = pts[3 * i + 1], pz = pts[3 * i + 2];
+  abortAt[i] = 0;
   if (px < g.domMin[0] || px > g.domMax[0] || py < g.domMin[1] || py > g.domMax[1] ||
       pz < g.domMin[2] || pz > g.domMax[2])
     return;
-  const int s = g.log2bs, mask = (1 << s) - 1;
+  const int s = g.log2bs;
   const int64_t nxy = (int64_t)g.nbx * g.nby;
   {
     const int ix = (int)px, iy = (int)py, iz = (int)pz;
     if (ix < 0 || ix >= g.sx || iy < 0 || iy >= g.sy || iz < 0 || iz >= g.sz) return;
-    // the demo walks the particle lists of value blocks only
-    // (src/msbg_demo.cpp:541-566): a particle owned by a non-value block is never splatted
     if (slot[(int64_t)(iz >> s) * nxy + (int64_t)(iy >> s) * g.nbx + (ix >> s)] < 0) return;
   }
-  const float r = g.rScan;
-  const int ix1 = max((int)ceilf(__fsub_rn(__fsub_rn(px, r), 0.5f)), 0);
-  const int iy1 = max((int)ceilf(__fsub_rn(__fsub_rn(py, r), 0.5f)), 0);
-  const int iz1 = max((int)ceilf(__fsub_rn(__fsub_rn(pz, r), 0.5f)), 0);
-  const int ix2 = min((int)floorf(__fsub_rn(__fadd_rn(px, r), 0.5f)), g.sx - 1);
-  const int iy2 = min((int)floorf(__fsub_rn(__fadd_rn(py, r), 0.5f)), g.sy - 1);
-  const int iz2 = min((int)floorf(__fsub_rn(__fadd_rn(pz, r), 0.5f)), g.sz - 1);
-  const int nx = ix2 - ix1 + 1, ny = iy2 - iy1 + 1, nz = iz2 - iz1 + 1;
-  if (nx <= 0 || ny <= 0 || nz <= 0) return;
-  const float x0 = __fsub_rn(px, 0.5f), y0 = __fsub_rn(py, 0.5f), z0 = __fsub_rn(pz, 0.5f);
-  const int64_t vpb = (int64_t)1 << (3 * s);
-
-  // blocks touched by the box (<= 2 per axis)
-  bool allValue = true;
-  {
-    const int bxa = ix1 >> s, bxb = ix2 >> s, bya = iy1 >> s, byb = iy2 >> s, bza = iz1 >> s, bzb = iz2 >> s;
-    if (lane < 8) {
-      const int bx = (lane & 1) ? bxb : bxa, by = (lane & 2) ? byb : bya, bz = (lane & 4) ? bzb : bza;
-      allValue = slot[bz * nxy + (int64_t)by * g.nbx + bx] >= 0;
-    }
-    allValue = __all_sync(0xffffffffu, allValue);
-  }
+  SplatBox b;
+  if (!splatBox(g, px, py, pz, b)) return;
+  const int nx = b.ix2 - b.ix1 + 1, ny = b.iy2 - b.iy1 + 1, nz = b.iz2 - b.iz1 + 1;
   const int total = nx * ny * nz;
-  int abortAt = total;
+  const int bx[2] = {b.ix1 >> s, b.ix2 >> s}, by[2] = {b.iy1 >> s, b.iy2 >> s}, bz[2] = {b.iz1 >> s, b.iz2 >> s};
+  int32_t sl[8];
+  bool allValue = true;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    sl[k] = slot[(int64_t)bz[k >> 2] * nxy + (int64_t)by[(k >> 1) & 1] * g.nbx + bx[k & 1]];
+    allValue = allValue && sl[k] >= 0;
+  }
+  int abortIdx = total;
   if (!allValue) {
-    int first = total;
-    for (int t = lane; t < total; t += 32) {
+    for (int t = 0; t < total; t++) {
       const int lx = t % nx, rest = t / nx, ly = rest % ny, lz = rest / ny;
-      const int ix = ix1 + lx, iy = iy1 + ly, iz = iz1 + lz;
-      const float dz = __fsub_rn((float)iz, z0), dy = __fsub_rn((float)iy, y0), dx = __fsub_rn((float)ix, x0);
+      const int ix = b.ix1 + lx, iy = b.iy1 + ly, iz = b.iz1 + lz;
+      const float dz = __fsub_rn((float)iz, b.z0), dy = __fsub_rn((float)iy, b.y0), dx = __fsub_rn((float)ix, b.x0);
       const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dz, dz), __fmul_rn(dy, dy)), __fmul_rn(dx, dx));
       if (d2 > g.distSqMax) continue;
-      const int64_t b = (int64_t)(iz >> s) * nxy + (int64_t)(iy >> s) * g.nbx + (ix >> s);
-      if (slot[b] < 0) { first = t; break; }  // lane-local scan order is increasing
-    }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
-    abortAt = first;
-    if (lane == 0 && abortAt < total) atomicAdd(nAborted, 1ull);
-  }
-  if (abortAt == total) {
-    // Nothing aborts (every touched block holds data): lanes take whole (y, z) rows of
-    // the box, skip the rows outside the sphere (dz*dz + dy*dy already exceeds it, and
-    // adding dx*dx >= 0 cannot lower a float sum), and find the row's two possible
-    // blocks once.
-    const int nRows = ny * nz;
-    for (int row = lane; row < nRows; row += 32) {
-      const int ly = row % ny, lz = row / ny;
-      const int iy = iy1 + ly, iz = iz1 + lz;
-      const float dz = __fsub_rn((float)iz, z0), dy = __fsub_rn((float)iy, y0);
-      const float dzy = __fadd_rn(__fmul_rn(dz, dz), __fmul_rn(dy, dy));
-      if (dzy > g.distSqMax) continue;
-      const int64_t rowBlk = (int64_t)(iz >> s) * nxy + (int64_t)(iy >> s) * g.nbx;
-      const int bxa = ix1 >> s;
-      const int64_t sa = (int64_t)slot[rowBlk + bxa] * vpb, sb = (int64_t)slot[rowBlk + (ix2 >> s)] * vpb;
-      const int rowVid = ((iz & mask) << (2 * s)) + ((iy & mask) << s);
-      for (int ix = ix1; ix <= ix2; ix++) {
-        // distSq exactly as the demo forms it: (dz*dz + dy*dy) + dx*dx
-        const float dx = __fsub_rn((float)ix, x0);
-        const float d2 = __fadd_rn(dzy, __fmul_rn(dx, dx));
-        if (d2 > g.distSqMax) continue;
-        const int64_t base = (ix >> s) == bxa ? sa : sb;
-        atomicMin((int *)(dst + base + rowVid + (ix & mask)), __float_as_int(__fmul_rn(d2, g.distSqMaxInv)));
+      if (slot[(int64_t)(iz >> s) * nxy + (int64_t)(iy >> s) * g.nbx + (ix >> s)] < 0) {
+        abortIdx = t;
+        break;
       }
     }
-    return;
+    if (abortIdx < total) atomicAdd(nAborted, 1ull);
   }
-  for (int t = lane; t < abortAt; t += 32) {
-    const int lx = t % nx, rest = t / nx, ly = rest % ny, lz = rest / ny;
-    const int ix = ix1 + lx, iy = iy1 + ly, iz = iz1 + lz;
-    // distSq exactly as the demo forms it: (dz*dz + dy*dy) + dx*dx
-    const float dz = __fsub_rn((float)iz, z0), dy = __fsub_rn((float)iy, y0), dx = __fsub_rn((float)ix, x0);
-    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dz, dz), __fmul_rn(dy, dy)), __fmul_rn(dx, dx));
-    if (d2 > g.distSqMax) continue;
-    const int64_t b = (int64_t)(iz >> s) * nxy + (int64_t)(iy >> s) * g.nbx + (ix >> s);
-    const int sl = slot[b];
-    if (sl < 0) continue;  // unreachable: an earlier in-sphere voxel would have set abortAt
-    const int vid = ((iz & mask) << (2 * s)) + ((iy & mask) << s) + (ix & mask);
-    const float q = __fmul_rn(d2, g.distSqMaxInv);
-    atomicMin((int *)(dst + (int64_t)sl * vpb + vid), __float_as_int(q));
+  abortAt[i] = abortIdx;
+  if (abortIdx == 0) return;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    // each distinct touched value block once
+    const bool dup = ((k & 1) && bx[1] == bx[0]) || ((k & 2) && by[1] == by[0]) || ((k & 4) && bz[1] == bz[0]);
+    if (!dup && sl[k] >= 0) atomicAdd(&cnt[sl[k]], 1);
   }
+}
+
+// Pass 2: the particle's index into the list of every value block it touches
+// (list of slot s: entries[off[s] .. off[s+1]-1], in no particular order).
+__global__ void __launch_bounds__(256) kSplatScatter(const float *__restrict__ pts, int64_t n, SplatGeom g,
+                                                     const int32_t *__restrict__ slot,
+                                                     const int32_t *__restrict__ abortAt,
+                                                     const int64_t *__restrict__ off, int32_t *__restrict__ cursor,
+                                                     int32_t *__restrict__ entries) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || abortAt[i] == 0) return;
+  const float px = pts[3 * i], py = pts[3 * i + 1], pz = pts[3 * i + 2];
+  SplatBox b;
+  splatBox(g, px, py, pz, b);
+  const int s = g.log2bs;
+  const int64_t nxy = (int64_t)g.nbx * g.nby;
+  const int bx[2] = {b.ix1 >> s, b.ix2 >> s}, by[2] = {b.iy1 >> s, b.iy2 >> s}, bz[2] = {b.iz1 >> s, b.iz2 >> s};
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const bool dup = ((k & 1) && bx[1] == bx[0]) || ((k & 2) && by[1] == by[0]) || ((k & 4) && bz[1] == bz[0]);
+    if (dup) continue;
+    const int sl = slot[(int64_t)bz[k >> 2] * nxy + (int64_t)by[(k >> 1) & 1] * g.nbx + bx[k & 1]];
+    if (sl >= 0) entries[off[sl] + atomicAdd(&cursor[sl], 1)] = (int32_t)i;
+  }
+}
+
+// Pass 3, one CTA per value block (slot = blockIdx.x): the minimum of the splat
+// values of the block's particles in shared memory (1.0 where none reaches), then
+// one coalesced write of the block.  A warp takes one particle at a time; its
+// lanes take the (y, z) rows of the box clipped to the block, skip rows already
+// outside the sphere (dz*dz + dy*dy exceeds it, and adding dx*dx >= 0 cannot lower
+// a float sum), and keep the voxels before the particle's abort index.
+template <int BS>
+__global__ void __launch_bounds__(512) kSplatBlock(const float *__restrict__ pts, SplatGeom g,
+                                                   const int32_t *__restrict__ active,
+                                                   const int32_t *__restrict__ abortAt,
+                                                   const int64_t *__restrict__ off,
+                                                   const int32_t *__restrict__ entries, float *__restrict__ dst) {
+  constexpr int VPB = BS * BS * BS;
+  extern __shared__ __align__(16) int smin[];
+  const int sl = blockIdx.x;
+  const int bid = active[sl];
+  const int X0 = (bid % g.nbx) * BS, Y0 = ((bid / g.nbx) % g.nby) * BS, Z0 = (int)(bid / ((int64_t)g.nbx * g.nby)) * BS;
+  const int one = __float_as_int(1.0f);
+  for (int v = threadIdx.x * 4; v < VPB; v += blockDim.x * 4)
+    *reinterpret_cast<int4 *>(smin + v) = make_int4(one, one, one, one);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nWarps = blockDim.x >> 5;
+  const int64_t e0 = off[sl], e1 = off[sl + 1];
+  for (int64_t e = e0 + warp; e < e1; e += nWarps) {
+    const int i = entries[e];
+    const float px = pts[3 * (int64_t)i], py = pts[3 * (int64_t)i + 1], pz = pts[3 * (int64_t)i + 2];
+    const int ab = abortAt[i];
+    SplatBox b;
+    splatBox(g, px, py, pz, b);
+    const int nx = b.ix2 - b.ix1 + 1, ny = b.iy2 - b.iy1 + 1;
+    const int cx1 = max(b.ix1, X0), cx2 = min(b.ix2, X0 + BS - 1);
+    const int cy1 = max(b.iy1, Y0), cy2 = min(b.iy2, Y0 + BS - 1);
+    const int cz1 = max(b.iz1, Z0), cz2 = min(b.iz2, Z0 + BS - 1);
+    const int cny = cy2 - cy1 + 1, cnz = cz2 - cz1 + 1;
+    if (cx2 < cx1 || cny <= 0 || cnz <= 0) continue;
+    for (int row = lane; row < cny * cnz; row += 32) {
+      const int iy = cy1 + row % cny, iz = cz1 + row / cny;
+      const float dz = __fsub_rn((float)iz, b.z0), dy = __fsub_rn((float)iy, b.y0);
+      const float dzy = __fadd_rn(__fmul_rn(dz, dz), __fmul_rn(dy, dy));
+      if (dzy > g.distSqMax) continue;
+      const int rowScan = ((iz - b.iz1) * ny + (iy - b.iy1)) * nx - b.ix1;  // + ix: the scan index
+      int *rowMin = smin + ((iz - Z0) * BS + (iy - Y0)) * BS - X0;
+      for (int ix = cx1; ix <= cx2; ix++) {
+        // distSq exactly as the demo forms it: (dz*dz + dy*dy) + dx*dx
+        const float dx = __fsub_rn((float)ix, b.x0);
+        const float d2 = __fadd_rn(dzy, __fmul_rn(dx, dx));
+        if (d2 > g.distSqMax || rowScan + ix >= ab) continue;
+        atomicMin(rowMin + ix, __float_as_int(__fmul_rn(d2, g.distSqMaxInv)));
+      }
+    }
+  }
+  __syncthreads();
+  float *out = dst + (int64_t)sl * VPB;
+  for (int v = threadIdx.x * 4; v < VPB; v += blockDim.x * 4)
+    *reinterpret_cast<int4 *>(out + v) = *reinterpret_cast<const int4 *>(smin + v);
+}
+
+// The demo's particlesPerBlock (src/msbg_demo.cpp:349-390): the containing block
+// of every point that passes the marking loop's domain tests.
+__device__ __forceinline__ int64_t ownerBlock(const SplatGeom &g, int nbz, const float *pts, int64_t i) {
+  const float px = pts[3 * i], py = pts[3 * i + 1], pz = pts[3 * i + 2];
+  if (px < g.domMin[0] || px > g.domMax[0] || py < g.domMin[1] || py > g.domMax[1] || pz < g.domMin[2] ||
+      pz > g.domMax[2])
+    return -1;
+  const int ix = (int)px, iy = (int)py, iz = (int)pz;
+  if (ix < 0 || ix >= g.sx || iy < 0 || iy >= g.sy || iz < 0 || iz >= g.sz) return -1;
+  const int s = g.log2bs;
+  return ((int64_t)(iz >> s) * g.nby + (iy >> s)) * g.nbx + (ix >> s);
+}
+
+__global__ void kOwnerCount(const float *__restrict__ pts, int64_t n, SplatGeom g, int nbz, int32_t *__restrict__ cnt) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t b = ownerBlock(g, nbz, pts, i);
+  if (b >= 0) atomicAdd(&cnt[b], 1);
+}
+
+__global__ void kOwnerScatter(const float *__restrict__ pts, int64_t n, SplatGeom g, int nbz,
+                              const int64_t *__restrict__ off, int32_t *__restrict__ cursor,
+                              int32_t *__restrict__ index) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t b = ownerBlock(g, nbz, pts, i);
+  if (b >= 0) index[off[b] + atomicAdd(&cursor[b], 1)] = (int32_t)i;
 }
 
 // distance -> density of one voxel (q: the quantized minimum splat value)
@@ -217,31 +301,22 @@ __global__ void kFinalize<double>(const float *__restrict__ splat, double *__res
   out[i] = (double)finalizeValue(splat[i], rParticle, nbDist, distSqMax);
 }
 
-__global__ void kFillF32(float *p, int64_t n, float v) {  // 8 per thread and step
-  const int64_t n8 = n / 8;
-  const float4 q = make_float4(v, v, v, v);
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n8; i += (int64_t)gridDim.x * blockDim.x) {
-    reinterpret_cast<float4 *>(p)[2 * i] = q;
-    reinterpret_cast<float4 *>(p)[2 * i + 1] = q;
-  }
-  for (int64_t i = 8 * n8 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = v;
-}
-
 int splatRun(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rParticle, float nbDist) {
   Channel &c = ctx->ch[0];
-  const int64_t nVox = ctx->nActive * ctx->voxPerBlock;
+  const int64_t nAct = ctx->nActive;
+  const int64_t nVox = nAct * ctx->voxPerBlock;
   float *dst;
   if (c.storage == MSBG_GPU_F32) {
-    dst = (float *)c.d;  // channel was filled with 1.0 by set_refinement_map
+    dst = (float *)c.d;
   } else {
     int rc = ensureTmpSlab(ctx, (size_t)(nVox > 0 ? nVox : 1) * 4);
     if (rc) return rc;
     dst = (float *)ctx->dTmpSlab;
-    if (nVox) MSBG_LAUNCH(ctx, kFillF32, gridVec(nVox), 256, 0, dst, nVox, 1.0f);
   }
   MSBG_CUDA(ctx, cudaMemsetAsync(ctx->dCounters + 1, 0, 8, ctx->stream));
-  if (n == 0 || nVox == 0) return MSBG_GPU_OK;
+  if (nVox == 0) return MSBG_GPU_OK;
+  if (ctx->bsx != 16 && ctx->bsx != 32)
+    return fail(ctx, MSBG_GPU_ERR_ARG, "splat: block size %d (16 or 32)", ctx->bsx);
   SplatGeom g;
   g.sx = ctx->sx; g.sy = ctx->sy; g.sz = ctx->sz; g.nbx = ctx->nbx; g.nby = ctx->nby;
   g.log2bs = ctx->log2bs;
@@ -249,10 +324,48 @@ int splatRun(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rParticle, f
   g.rScan = rParticle + nbDist;
   g.distSqMax = g.rScan * g.rScan;
   g.distSqMaxInv = 1.0f / g.distSqMax;
-  const int64_t threads = n * 32;
-  MSBG_LAUNCH(ctx, kSplat, gridFor(threads, 256), 256, 0, dPts, n, g, ctx->dSlot, dst,
-              (unsigned long long *)(ctx->dCounters + 1));
-  return MSBG_GPU_OK;
+  // scratch (stream-ordered): abort indices [n], counts / cursors [nAct], offsets
+  // [nAct + 1], list entries [8 n] (a box touches at most 8 blocks)
+  const int64_t nn = n > 0 ? n : 1;
+  const size_t bAbort = (size_t)nn * 4, bCnt = ((size_t)nAct * 4 + 15) & ~size_t(15),
+               bOff = (size_t)(nAct + 1) * 8, bEnt = (size_t)nn * 8 * 4;
+  char *scratch = nullptr;
+  MSBG_CUDA(ctx, cudaMallocAsync((void **)&scratch, bAbort + 2 * bCnt + bOff + bEnt + 64, ctx->stream));
+  int32_t *abortAt = (int32_t *)scratch;
+  int32_t *cnt = (int32_t *)(scratch + ((bAbort + 15) & ~size_t(15)));
+  int32_t *cursor = (int32_t *)((char *)cnt + bCnt);
+  int64_t *off = (int64_t *)((char *)cursor + bCnt);
+  int32_t *entries = (int32_t *)((char *)off + ((bOff + 15) & ~size_t(15)));
+  int rc = MSBG_GPU_OK;
+  auto run = [&]() -> int {
+    MSBG_CUDA(ctx, cudaMemsetAsync(cnt, 0, 2 * bCnt, ctx->stream));
+    if (n > 0) {
+      MSBG_LAUNCH(ctx, kSplatCount, gridFor(n, 256), 256, 0, dPts, n, g, ctx->dSlot, abortAt, cnt,
+                  (unsigned long long *)(ctx->dCounters + 1));
+    }
+    int r = exclusiveScanCounts(ctx, cnt, nAct, off, off + nAct);
+    if (r) return r;
+    if (n > 0) {
+      MSBG_LAUNCH(ctx, kSplatScatter, gridFor(n, 256), 256, 0, dPts, n, g, ctx->dSlot, abortAt, off, cursor,
+                  entries);
+    }
+    if (ctx->bsx == 32) {
+      constexpr int smem = 32 * 32 * 32 * 4;
+      static bool attr = false;
+      if (!attr) {
+        MSBG_CUDA(ctx, cudaFuncSetAttribute(kSplatBlock<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        attr = true;
+      }
+      MSBG_LAUNCH(ctx, kSplatBlock<32>, (unsigned)nAct, 512, smem, dPts, g, ctx->dActive, abortAt, off, entries, dst);
+    } else {
+      MSBG_LAUNCH(ctx, kSplatBlock<16>, (unsigned)nAct, 256, 16 * 16 * 16 * 4, dPts, g, ctx->dActive, abortAt, off,
+                  entries, dst);
+    }
+    return MSBG_GPU_OK;
+  };
+  rc = run();
+  cudaFreeAsync(scratch, ctx->stream);
+  return rc;
 }
 
 int splatFinalizeRun(msbg_gpu_ctx *ctx, float rParticle, float nbDist) {
@@ -270,6 +383,32 @@ int splatFinalizeRun(msbg_gpu_ctx *ctx, float rParticle, float nbDist) {
     default: MSBG_LAUNCH(ctx, kFinalize<double>, gridFor(n, 256), 256, 0, src, (double *)c.d, n, rParticle, nbDist, distSqMax); break;
   }
   return MSBG_GPU_OK;
+}
+
+int particlesPerBlockRun(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, int64_t *dOff, int32_t *dIndex,
+                         int64_t *count) {
+  const int64_t nB = ctx->nBlocks;
+  SplatGeom g;
+  g.sx = ctx->sx; g.sy = ctx->sy; g.sz = ctx->sz; g.nbx = ctx->nbx; g.nby = ctx->nby;
+  g.log2bs = ctx->log2bs;
+  for (int k = 0; k < 3; k++) { g.domMin[k] = ctx->domMin[k]; g.domMax[k] = ctx->domMax[k]; }
+  const size_t bCnt = ((size_t)nB * 4 + 15) & ~size_t(15);
+  int32_t *cnt = nullptr;
+  MSBG_CUDA(ctx, cudaMallocAsync((void **)&cnt, 2 * bCnt, ctx->stream));
+  int32_t *cursor = (int32_t *)((char *)cnt + bCnt);
+  auto run = [&]() -> int {
+    MSBG_CUDA(ctx, cudaMemsetAsync(cnt, 0, 2 * bCnt, ctx->stream));
+    if (n > 0) MSBG_LAUNCH(ctx, kOwnerCount, gridFor(n, 256), 256, 0, dPts, n, g, ctx->nbz, cnt);
+    int r = exclusiveScanCounts(ctx, cnt, nB, dOff, dOff + nB);
+    if (r) return r;
+    if (n > 0) MSBG_LAUNCH(ctx, kOwnerScatter, gridFor(n, 256), 256, 0, dPts, n, g, ctx->nbz, dOff, cursor, dIndex);
+    MSBG_CUDA(ctx, cudaMemcpyAsync(count, dOff + nB, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    return MSBG_GPU_OK;
+  };
+  int rc = run();
+  cudaFreeAsync(cnt, ctx->stream);
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess && !rc) rc = fail(ctx, MSBG_GPU_ERR_CUDA, "particles_per_block");
+  return rc;
 }
 
 }  // namespace msbg

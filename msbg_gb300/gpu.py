@@ -74,6 +74,7 @@ SIGNATURES = {
     "msbg_gpu_fill": (I, [P, I, D]),
     "msbg_gpu_splat": (I, [P, P, I64, F, F]),
     "msbg_gpu_splat_finalize": (I, [P, F, F]),
+    "msbg_gpu_particles_per_block": (I, [P, P, I64, P, P, C.POINTER(I64)]),
     "msbg_gpu_apply_channel_pde_fast": (I, [P, I, I, I, P, I64, I, I, F, F, F, I, F, F, F, P, F, F, F, F, F, I, P,
                                             I, I]),
     "msbg_gpu_surface_job": (I, [P, P, I64, F, F, P, I, I, I, F, I, P, SZ, C.POINTER(I64)]),
@@ -407,6 +408,26 @@ class MultiresSparseGrid:
 
     def splat_finalize(self, r_particle: float = 2.0, nb_dist: float = 2.0):
         self._check(self.L.msbg_gpu_splat_finalize(self.h, r_particle, nb_dist))
+
+    def particles_per_block(self, d_pts: DeviceBuffer, n: int):
+        """The demo's particlesPerBlock as CSR: (offsets int64 [nBlocks+1], point indices
+        int32 [count]); the order inside a list is unspecified."""
+        off_d = DeviceBuffer.alloc((self.n_blocks + 1) * 8)
+        idx_d = DeviceBuffer.alloc(max(n, 1) * 4)
+        cnt = C.c_int64()
+        try:
+            self._check(self.L.msbg_gpu_particles_per_block(self.h, C.c_void_p(d_pts.ptr), n, C.c_void_p(off_d.ptr),
+                                                            C.c_void_p(idx_d.ptr), C.byref(cnt)))
+            off = np.empty(self.n_blocks + 1, np.int64)
+            idx = np.empty(cnt.value, np.int32)
+            self._check(self.L.msbg_gpu_copy_d2h(self.h, _ptr(off), C.c_void_p(off_d.ptr), off.nbytes))
+            if cnt.value:
+                self._check(self.L.msbg_gpu_copy_d2h(self.h, _ptr(idx), C.c_void_p(idx_d.ptr), idx.nbytes))
+            self.synchronize()
+        finally:
+            off_d.free()
+            idx_d.free()
+        return off, idx
 
     # reference: applyChannelPdeFast<T> (src/msbg.h:2150-2172); the reference's
     # (chPhi, laplTyp, doConstrZeroOne, numIter, timeStep, anisDiffAlpha) subset

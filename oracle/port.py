@@ -129,6 +129,23 @@ def mark_blocks(g: Grid, pts: np.ndarray, r_scan: float):
     return cnt, valid, n_valid
 
 
+def particles_per_block(g: Grid, pts: np.ndarray):
+    """The demo's per-block particle lists particlesPerBlock restated
+    (src/msbg_demo.cpp:349-390): each point that passes the marking loop's domain tests
+    (orc_mark_blocks) goes to the list of the block containing it.  CSR form: offsets
+    [nBlocks+1] and point indices, each list in ascending index."""
+    _, valid, _ = mark_blocks(g, pts, 0.0)
+    idx = np.nonzero(valid)[0]
+    ip = pts[idx].astype(np.float32).astype(np.int64)  # (int)p, as the demo's getBlockCoords
+    s = int(g.bsx).bit_length() - 1
+    bid = ((ip[:, 2] >> s) * g.nby + (ip[:, 1] >> s)) * g.nbx + (ip[:, 0] >> s)
+    order = np.argsort(bid, kind="stable")
+    cnt = np.bincount(bid, minlength=g.nbx * g.nby * g.nbz)
+    off = np.zeros(len(cnt) + 1, np.int64)
+    np.cumsum(cnt, out=off[1:])
+    return off, idx[order].astype(np.int32)
+
+
 def regularize(levels: np.ndarray, nbx, nby, nbz, n_levels):
     lv = np.ascontiguousarray(levels, np.int32).copy()
     per = np.zeros(8, np.int64)

@@ -134,7 +134,7 @@ def test_gpu_vs_port_seeded(gpulib, port, storage, bsx):
 # relative for FP16, 1/65535 for uint16), so the bound is 1e-3 there.
 FAST_CASES = [("mcf", 16, "F32", 1, 1e-5), ("jacobi", 16, "F32", 1, 1e-5), ("mcf", 16, "F32", 0, 1e-5),
               ("mcf", 32, "F16", 1, 1e-3), ("jacobi", 32, "F16", 0, 1e-3), ("jacobi", 32, "U16", 1, 1e-3),
-              ("mcf", 32, "F32", 1, 1e-5)]
+              ("mcf", 32, "F32", 1, 1e-5), ("jacobi", 32, "F32", 1, 1e-5), ("jacobi", 16, "F16", 1, 1e-3)]
 
 
 @pytest.mark.parametrize("lapl,bsx,storage,constr01,tol", FAST_CASES)
@@ -312,3 +312,44 @@ def test_gpu_bounded_wait_times_out_and_context_stays_usable(gpulib):
         assert e.value.code == G.ERR_TIMEOUT
     finally:
         g.close()
+
+
+@pytest.mark.gpu
+def test_gpu_large_payload_copies_split_over_two_streams(gpulib):
+    """Host transfers above 64 MiB go out in two halves on two streams (two copy engines);
+    a 512 MiB FP32 channel makes the round trip unchanged."""
+    G = gpulib
+    g = G.MultiresSparseGrid(512, 512, 512, 16, 1, G.F32)
+    try:
+        g.set_levels(np.zeros(32 ** 3, np.int32))
+        g.setRefinementMap(0.0)
+        rng = np.random.Generator(np.random.PCG64(7))
+        data = rng.random((32 ** 3, 16 ** 3), dtype=np.float32)
+        assert data.nbytes > 64 << 20
+        g.upload_payload(data, 0)
+        assert np.array_equal(g.payload(0), data)
+        g.fill(0.25, 0)
+        assert np.all(g.payload(0) == 0.25)
+    finally:
+        g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bsx", [16, 32])
+def test_gpu_particles_per_block_match_restatement(gpulib, port, bsx):
+    """msbg_gpu_particles_per_block against the restatement: the same offsets, and the same
+    points in every list (the order inside a list is unspecified, as in the reference)."""
+    res = 256
+    pts = W.sphere_cloud(res, 12, 6000, seed=W.workload_seed(1, 91))
+    pts = np.concatenate([pts, np.array([[-1.0, 5.0, 5.0], [300.0, 1.0, 1.0]], np.float32)])
+    g = gpulib.MultiresSparseGrid(res, res, res, bsx, 3, gpulib.F32)
+    try:
+        d = g.to_device(pts)
+        off, idx = g.particles_per_block(d, len(pts))
+    finally:
+        g.close()
+    want_off, want_idx = port.particles_per_block(port.grid(res, res, res, bsx, port.F32), pts)
+    assert np.array_equal(off, want_off)
+    assert len(idx) == len(pts) - 2
+    got = np.concatenate([np.sort(idx[off[b]:off[b + 1]]) for b in range(len(off) - 1)])
+    assert np.array_equal(got, want_idx)

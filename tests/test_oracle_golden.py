@@ -61,3 +61,18 @@ def test_port_refinement_map_golden(port, golden, nl):
     assert np.array_equal(lv, golden[f"lvl{nl}_out"])
     assert np.array_equal(per, golden[f"lvl{nl}_per_level"])
     assert np.array_equal(port.block_flags(lv, 8, 8, 8), golden[f"lvl{nl}_flags"])
+
+
+def test_port_particles_per_block_golden(port, golden):
+    """particlesPerBlock restated: the listed points are the demo's nActParticles (the
+    reference's own count of the points its marking loop keeps), each in the list of the
+    block that contains it."""
+    res, bsx = int(golden["res"]), int(golden["bsx"])
+    pts = golden["points"]
+    g = port.grid(res, res, res, bsx, port.F32)
+    off, idx = port.particles_per_block(g, pts)
+    assert off[-1] == len(idx) == int(golden["n_act_particles"])
+    nb = res // bsx
+    ip = pts[idx].astype(np.int64)
+    owner = ((ip[:, 2] // bsx) * nb + ip[:, 1] // bsx) * nb + ip[:, 0] // bsx
+    assert np.array_equal(owner, np.repeat(np.arange(nb ** 3), np.diff(off)))
