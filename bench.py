@@ -713,6 +713,9 @@ def poisson_full_measure(steps: int, warmup: int) -> dict:
             out[kind] = sorted(runs, key=lambda r: r["ms"])[len(runs) // 2]
             g.poisson_release_work()
         out["mixed_speedup_vs_plain"] = out["plain"]["ms"] / out["mixed"]["ms"]
+        # the operator launch shapes the autotuner picked (level, bytes per value, mode,
+        # cells per thread, grid), during the warm-up solves
+        out["operator_shapes"] = [list(t) for t in g.poisson_tuning()]
         n1 = cells // 8
         out["learned"] = (f"not run at this size: the network's level-1 buffers ({n1 * (52 + 32 + 2) * 4 / 1e9:.0f} GB "
                           f"of activations and gradients, {cells * 8 / 1e9:.0f} GB of level-0 staging) do not fit "

@@ -495,6 +495,13 @@ int msbg_gpu_poisson_set_params(msbg_gpu_ctx *ctx, int preSweeps, int postSweeps
 int msbg_gpu_poisson_release_work(msbg_gpu_ctx *ctx);
 /* Multigrid levels of the current hierarchy and their cell counts. */
 int msbg_gpu_mg_info(msbg_gpu_ctx *ctx, int *nLevels, int64_t *cellsPerLevel, int cap);
+/* The launch-shape autotuner of the operator kernel: on the first operator call of a
+ * (level, precision, mode) on a level of at least 2^21 cells, the candidate shapes (cells
+ * per thread 4 or 8, grids of 608 / 1216 / 2432 CTAs) are timed on that call's data and
+ * the fastest is kept for the layout.  enable: 1 on (the default), 0 off (static shapes),
+ * -1 unchanged.  hOut (may be NULL): up to cap entries of 5 int32 each (level, bytes per
+ * value, mode, cells per thread, grid) for the shapes picked so far; *nOut their count. */
+int msbg_gpu_poisson_tuning(msbg_gpu_ctx *ctx, int enable, int32_t *hOut, int cap, int *nOut);
 
 /* ---- batched solves ------------------------------------------------------------------
  * Many independent volumes on one layout: every value block belongs to one volume

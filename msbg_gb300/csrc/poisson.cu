@@ -1169,6 +1169,28 @@ extern "C" int msbg_gpu_poisson_set_params(msbg_gpu_ctx *ctx, int preSweeps, int
   return MSBG_GPU_OK;
 }
 
+extern "C" int msbg_gpu_poisson_tuning(msbg_gpu_ctx *ctx, int enable, int32_t *hOut, int cap, int *nOut) {
+  if (!ctx || enable < -1 || enable > 1 || cap < 0) return MSBG_GPU_ERR_ARG;
+  int rc = needLayoutP(ctx);
+  if (rc) return rc;
+  PoissonState *ps = ctx->poisson;
+  if (enable >= 0) ps->autotune = enable != 0;
+  int n = 0;
+  for (const auto &kv : ps->applyShape) {
+    if (hOut && n < cap) {
+      int32_t *e = hOut + 5 * n;
+      e[0] = std::get<0>(kv.first);
+      e[1] = std::get<1>(kv.first);
+      e[2] = std::get<2>(kv.first);
+      e[3] = kv.second >> 16;
+      e[4] = kv.second & 0xffff;
+    }
+    n++;
+  }
+  if (nOut) *nOut = n;
+  return MSBG_GPU_OK;
+}
+
 extern "C" int msbg_gpu_mg_info(msbg_gpu_ctx *ctx, int *nLevels, int64_t *cellsPerLevel, int cap) {
   if (!ctx || !nLevels) return MSBG_GPU_ERR_ARG;
   int rc = needLayoutP(ctx);

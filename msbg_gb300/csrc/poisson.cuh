@@ -163,6 +163,11 @@ struct PoissonState {
   int64_t listCap = 0;
   float relaxOmega = 6.0f / 7.0f;  // the reference's smoother constants (src/msbg.cpp:814-843)
   int relaxBlockIter = 5;
+  // Launch shapes of the operator kernel picked by the autotuner: key (level, bytes per
+  // value, mode), value cells-per-thread * 65536 + grid cap (CTAs).  Filled on the first
+  // call of each key on a large enough level, by timing the candidates on that call's data.
+  std::map<std::tuple<int, int, int>, int> applyShape;
+  bool autotune = true;
 };
 
 void poissonFree(PoissonState *ps);

@@ -756,10 +756,10 @@ BlkGeom blkOf(const PoissonState *ps, const MgLevel &L) {
 template <typename V, int CPT>
 static int applyLaunch(msbg_gpu_ctx *ctx, PoissonState *ps, const MgLevel &Lv, const PrecSet &P, size_t l,
                        const V *x, const V *b, V *y, int mode, double *dotOut, V *bc, V *xc, __half *rhOut,
-                       float rhScale) {
+                       float rhScale, int gridCap) {
   const int64_t nSeg = Lv.nCell / CPT;
   int64_t grid = (nSeg + 255) / 256;
-  if (grid > ps->nPartial) grid = ps->nPartial;
+  if (grid > gridCap) grid = gridCap;
   if (grid < 1) grid = 1;
   const BlkGeom gg = blkOf(ps, Lv);
   const V *cx = (const V *)P.cx[l], *cy = (const V *)P.cy[l], *cz = (const V *)P.cz[l], *d = (const V *)P.d[l];
@@ -780,15 +780,63 @@ static int applyLaunch(msbg_gpu_ctx *ctx, PoissonState *ps, const MgLevel &Lv, c
   return MSBG_GPU_OK;
 }
 
+// Launch-shape autotuner of the operator kernel.  The shape is the block-to-thread
+// mapping (cells per thread: 4, or 8 with 16-byte (FP16) / 32-byte (FP32) row loads
+// on levels with bs >= 8) and the grid (CTAs of the grid-stride loop).  On the
+// first call of a (level, precision, mode) on a level of at least 2^21 cells, each
+// candidate runs on the call's own data (every candidate computes the same cells,
+// so the repeated launches leave the same outputs) and the fastest is kept for the
+// layout; smaller levels, calls during a stream capture, and a context with tuning
+// switched off use the static rule (8 cells for FP16 on bs >= 8, else 4; the
+// largest grid).  The FP64 dot products of different shapes sum in different
+// orders, so they can differ in their last bits, as the reference's thread-local
+// reductions do between runs.
 template <typename V>
 int blkApply(msbg_gpu_ctx *ctx, PoissonState *ps, size_t l, const PrecSet &P, const V *x, const V *b, V *y,
              int mode, double *dotOut, V *bc, V *xc, __half *rhOut, float rhScale) {
   const MgLevel &Lv = ps->levels[l];
-  if constexpr (sizeof(V) == 2) {
-    if (Lv.bs >= 8 && mode != 2)  // FP16: 8 cells (16 bytes) per row load
-      return applyLaunch<V, 8>(ctx, ps, Lv, P, l, x, b, y, mode, dotOut, bc, xc, rhOut, rhScale);
+  auto launch = [&](int cpt, int cap) -> int {
+    if (cpt == 8) return applyLaunch<V, 8>(ctx, ps, Lv, P, l, x, b, y, mode, dotOut, bc, xc, rhOut, rhScale, cap);
+    return applyLaunch<V, 4>(ctx, ps, Lv, P, l, x, b, y, mode, dotOut, bc, xc, rhOut, rhScale, cap);
+  };
+  const bool can8 = Lv.bs >= 8 && mode != 2;
+  int cpt = (sizeof(V) == 2 && can8) ? 8 : 4, cap = ps->nPartial;
+  const auto key = std::make_tuple((int)l, (int)sizeof(V), mode);
+  auto it = ps->applyShape.find(key);
+  if (it != ps->applyShape.end()) {
+    cpt = it->second >> 16;
+    cap = it->second & 0xffff;
+  } else if (ps->autotune && Lv.nCell >= (int64_t(1) << 21)) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    MSBG_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &cs));
+    if (cs == cudaStreamCaptureStatusNone) {
+      cudaEvent_t e[2];
+      MSBG_CUDA(ctx, cudaEventCreate(&e[0]));
+      MSBG_CUDA(ctx, cudaEventCreate(&e[1]));
+      float best = 1e30f;
+      int rc = MSBG_GPU_OK;
+      for (int c : {4, 8}) {
+        if (c == 8 && !can8) continue;
+        for (int g : {152 * 4, 152 * 8, ps->nPartial}) {
+          if ((rc = launch(c, g))) break;  // warm
+          cudaEventRecord(e[0], ctx->stream);
+          for (int k = 0; k < 2 && !rc; k++) rc = launch(c, g);
+          cudaEventRecord(e[1], ctx->stream);
+          if (rc) break;
+          cudaEventSynchronize(e[1]);
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, e[0], e[1]);
+          if (ms < best) { best = ms; cpt = c; cap = g; }
+        }
+        if (rc) break;
+      }
+      cudaEventDestroy(e[0]);
+      cudaEventDestroy(e[1]);
+      if (rc) return rc;
+      ps->applyShape[key] = (cpt << 16) | cap;
+    }
   }
-  return applyLaunch<V, 4>(ctx, ps, Lv, P, l, x, b, y, mode, dotOut, bc, xc, rhOut, rhScale);
+  return launch(cpt, cap);
 }
 
 static unsigned quadGrid(const PoissonState *ps, int64_t nq) {

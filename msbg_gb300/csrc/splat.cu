@@ -173,20 +173,24 @@ __global__ void __launch_bounds__(256) kSplatScatter(const float *__restrict__ p
 // lanes take the (y, z) rows of the box clipped to the block, skip rows already
 // outside the sphere (dz*dz + dy*dy exceeds it, and adding dx*dx >= 0 cannot lower
 // a float sum), and keep the voxels before the particle's abort index.
+// The block's minima in shared memory use a row stride of BS + 1 words: the lanes
+// of a warp take different rows, which then fall into different banks.
+template <int BS>
+constexpr int splatSmemWords() { return BS * BS * (BS + 1); }
+
 template <int BS>
 __global__ void __launch_bounds__(512) kSplatBlock(const float *__restrict__ pts, SplatGeom g,
                                                    const int32_t *__restrict__ active,
                                                    const int32_t *__restrict__ abortAt,
                                                    const int64_t *__restrict__ off,
                                                    const int32_t *__restrict__ entries, float *__restrict__ dst) {
-  constexpr int VPB = BS * BS * BS;
+  constexpr int VPB = BS * BS * BS, RS = BS + 1, NW = splatSmemWords<BS>();
   extern __shared__ __align__(16) int smin[];
   const int sl = blockIdx.x;
   const int bid = active[sl];
   const int X0 = (bid % g.nbx) * BS, Y0 = ((bid / g.nbx) % g.nby) * BS, Z0 = (int)(bid / ((int64_t)g.nbx * g.nby)) * BS;
   const int one = __float_as_int(1.0f);
-  for (int v = threadIdx.x * 4; v < VPB; v += blockDim.x * 4)
-    *reinterpret_cast<int4 *>(smin + v) = make_int4(one, one, one, one);
+  for (int v = threadIdx.x; v < NW; v += blockDim.x) smin[v] = one;
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nWarps = blockDim.x >> 5;
   const int64_t e0 = off[sl], e1 = off[sl + 1];
@@ -208,7 +212,7 @@ __global__ void __launch_bounds__(512) kSplatBlock(const float *__restrict__ pts
       const float dzy = __fadd_rn(__fmul_rn(dz, dz), __fmul_rn(dy, dy));
       if (dzy > g.distSqMax) continue;
       const int rowScan = ((iz - b.iz1) * ny + (iy - b.iy1)) * nx - b.ix1;  // + ix: the scan index
-      int *rowMin = smin + ((iz - Z0) * BS + (iy - Y0)) * BS - X0;
+      int *rowMin = smin + ((iz - Z0) * BS + (iy - Y0)) * RS - X0;
       for (int ix = cx1; ix <= cx2; ix++) {
         // distSq exactly as the demo forms it: (dz*dz + dy*dy) + dx*dx
         const float dx = __fsub_rn((float)ix, b.x0);
@@ -220,8 +224,10 @@ __global__ void __launch_bounds__(512) kSplatBlock(const float *__restrict__ pts
   }
   __syncthreads();
   float *out = dst + (int64_t)sl * VPB;
-  for (int v = threadIdx.x * 4; v < VPB; v += blockDim.x * 4)
-    *reinterpret_cast<int4 *>(out + v) = *reinterpret_cast<const int4 *>(smin + v);
+  for (int v = threadIdx.x * 4; v < VPB; v += blockDim.x * 4) {
+    const int *row = smin + (v / BS) * RS + v % BS;
+    *reinterpret_cast<int4 *>(out + v) = make_int4(row[0], row[1], row[2], row[3]);
+  }
 }
 
 // The demo's particlesPerBlock (src/msbg_demo.cpp:349-390): the containing block
@@ -350,7 +356,7 @@ int splatRun(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rParticle, f
                   entries);
     }
     if (ctx->bsx == 32) {
-      constexpr int smem = 32 * 32 * 32 * 4;
+      constexpr int smem = splatSmemWords<32>() * 4;
       static bool attr = false;
       if (!attr) {
         MSBG_CUDA(ctx, cudaFuncSetAttribute(kSplatBlock<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
@@ -358,8 +364,8 @@ int splatRun(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rParticle, f
       }
       MSBG_LAUNCH(ctx, kSplatBlock<32>, (unsigned)nAct, 512, smem, dPts, g, ctx->dActive, abortAt, off, entries, dst);
     } else {
-      MSBG_LAUNCH(ctx, kSplatBlock<16>, (unsigned)nAct, 256, 16 * 16 * 16 * 4, dPts, g, ctx->dActive, abortAt, off,
-                  entries, dst);
+      MSBG_LAUNCH(ctx, kSplatBlock<16>, (unsigned)nAct, 256, splatSmemWords<16>() * 4, dPts, g, ctx->dActive, abortAt,
+                  off, entries, dst);
     }
     return MSBG_GPU_OK;
   };

@@ -55,6 +55,12 @@ __device__ __forceinline__ typename Vec4T<T>::V pack4(const float o[4]) {
   typename Vec4T<T>::V v;
   if constexpr (sizeof(T) == 4) {
     v.x = o[0]; v.y = o[1]; v.z = o[2]; v.w = o[3];
+  } else if constexpr (std::is_same<T, __half>::value) {
+    // two round-to-nearest-even conversions of a pair each (the same rounding as
+    // __float2half_rn per value)
+    const __half2 lo = __floats2half2_rn(o[0], o[1]), hi = __floats2half2_rn(o[2], o[3]);
+    v.x = *reinterpret_cast<const uint32_t *>(&lo);
+    v.y = *reinterpret_cast<const uint32_t *>(&hi);
   } else {
     T *e = reinterpret_cast<T *>(&v);
 #pragma unroll

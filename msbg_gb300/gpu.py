@@ -123,6 +123,7 @@ SIGNATURES = {
     "msbg_gpu_axpby_combined": (I, [P, D, D, I, I, I, P, I64]),
     "msbg_gpu_mgpcg_solve": (I, [P, I, I, D, I, C.POINTER(I), C.POINTER(D)]),
     "msbg_gpu_mg_info": (I, [P, C.POINTER(I), P, I]),
+    "msbg_gpu_poisson_tuning": (I, [P, I, P, I, C.POINTER(I)]),
     "msbg_gpu_poisson_release_work": (I, [P]),
     "msbg_gpu_poisson_set_params": (I, [P, I, I, I, I]),
     "msbg_gpu_mgpcg_solve_mixed": (I, [P, I, I, D, I, D, I, C.POINTER(I), C.POINTER(I), C.POINTER(D)]),
@@ -857,6 +858,14 @@ class MultiresSparseGrid:
         cells = np.zeros(32, np.int64)
         self._check(self.L.msbg_gpu_mg_info(self.h, C.byref(n), _ptr(cells), 32))
         return cells[: n.value].copy()
+
+    def poisson_tuning(self, enable: int = -1) -> list:
+        """The operator launch shapes the autotuner picked: (level, bytes per value, mode,
+        cells per thread, grid) each; enable 1 / 0 switches tuning on / off (-1: as is)."""
+        n = C.c_int()
+        out = np.zeros((64, 5), np.int32)
+        self._check(self.L.msbg_gpu_poisson_tuning(self.h, enable, _ptr(out), 64, C.byref(n)))
+        return [tuple(int(v) for v in r) for r in out[: min(n.value, 64)]]
 
     # ---- timing -------------------------------------------------------------------------
     def event_record(self, slot: int):

@@ -241,3 +241,42 @@ def test_non_spd_coefficients_diverge(gpulib, port):
         assert rel <= 1e-6
     finally:
         g.close()
+
+
+def test_launch_shape_autotuner(gpulib):
+    """The operator's launch-shape autotuner on a layout large enough to tune (a 256^3
+    block of bs 32, 16.7 M cells): it picks one valid shape per (level, precision, mode)
+    it met, and the solve reaches the tolerance in the same iterations and to the same
+    solution (FP32) as with the static shapes."""
+    G = gpulib
+    g = G.MultiresSparseGrid(256, 256, 256, 32, 2, G.F32)
+    try:
+        g.set_levels(np.zeros(8 ** 3, np.int32))
+        g.setRefinementMap(0.0)
+        for ch in (CH_X, CH_B, CH_CX, CH_CY, CH_CZ, CH_D):
+            g.channel_create(ch, G.F32)
+        g.poisson_procedural_coefficients(4242, CH_CX, CH_CY, CH_CZ, CH_D)
+        rng = np.random.default_rng(11)
+        b = rng.standard_normal((8 ** 3, 32 ** 3)).astype(np.float32)
+        b -= b.mean()
+        g.upload_payload(b, CH_B)
+        g.poisson_tuning(0)
+        g.fill(0.0, CH_X)
+        it0, rel0 = g.mgpcg_solve(CH_X, CH_B, tol=1e-6, max_iter=100)
+        x0 = g.payload(CH_X)
+        assert g.poisson_tuning() == []
+        g.poisson_tuning(1)
+        g.fill(0.0, CH_X)
+        it1, rel1 = g.mgpcg_solve(CH_X, CH_B, tol=1e-6, max_iter=100)
+        x1 = g.payload(CH_X)
+        shapes = g.poisson_tuning()
+        assert shapes, "a 16.7 M-cell level is tuned"
+        keys = [s[:3] for s in shapes]
+        assert len(keys) == len(set(keys))
+        for level, nbytes, mode, cpt, grid in shapes:
+            assert nbytes == 4 and cpt in (4, 8) and grid in (608, 1216, 2432)
+            assert mode in (0, 1, 2) and (mode != 2 or cpt == 4)
+        assert rel0 <= 1e-6 and rel1 <= 1e-6 and it0 == it1
+        assert rel_l2(x1, x0) < 1e-5
+    finally:
+        g.close()
