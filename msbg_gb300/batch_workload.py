@@ -135,6 +135,9 @@ def run_batch(steps: int = 3, warmup: int = 1, learned_weights: str | None = Non
                          "iterations_mean": float(its[ok].mean()) if ok.any() else None,
                          "iterations_max": int(its.max()), "converged": int(ok.sum()),
                          "max_rel_residual_fp64": float(rel.max())}
+        # the operator launch shapes the autotuner picked for the batch's levels (level,
+        # bytes per value, mode, cells per thread, grid)
+        out["operator_shapes"] = [list(t) for t in g.poisson_tuning()]
         return out
     finally:
         g.close()

@@ -467,6 +467,8 @@ extern "C" int msbg_gpu_destroy(msbg_gpu_ctx *ctx) {
   for (auto &c : ctx->ch) {
     if (c.d) cudaFree(c.d);
     if (c.cache) cudaFree(c.cache);
+    for (auto &gr : c.sweepGraphs) cudaGraphExecDestroy(gr.exec);
+    c.sweepGraphs.clear();
   }
   if (ctx->dTmpSlab) cudaFree(ctx->dTmpSlab);
   if (ctx->dPts) cudaFree(ctx->dPts);
@@ -481,6 +483,7 @@ extern "C" int msbg_gpu_destroy(msbg_gpu_ctx *ctx) {
     cudaStreamSynchronize(ctx->copyStream);
     cudaStreamDestroy(ctx->copyStream);
   }
+  if (ctx->captureStream) cudaStreamDestroy(ctx->captureStream);
   delete ctx;
   return MSBG_GPU_OK;
 }

@@ -7,6 +7,7 @@
 #include <stdio.h>
 
 #include <string>
+#include <vector>
 
 #include "msbg_gpu.h"
 
@@ -28,6 +29,13 @@ constexpr int kColorTot = 16;
 constexpr int kNumCounters = 32;
 constexpr int kMaxEvents = 16;
 
+// A captured sequence of launches and the bytes it was captured from (kernel,
+// arguments, grid): replayed while a call presents the same bytes.
+struct CachedGraph {
+  std::vector<unsigned char> key;
+  cudaGraphExec_t exec = nullptr;
+};
+
 struct Channel {
   bool exists = false;
   int storage = MSBG_GPU_F32;
@@ -35,6 +43,7 @@ struct Channel {
   size_t capBlocks = 0;   // blocks the slab can hold
   void *cache = nullptr;  // x-face + corner-column cache of the colored sweeps
   size_t cacheBytes = 0;
+  std::vector<CachedGraph> sweepGraphs;  // the colour passes of recent sweep calls (most recent last)
 };
 
 }  // namespace msbg
@@ -51,6 +60,7 @@ struct msbg_gpu_ctx {
   cudaEvent_t ev[msbg::kMaxEvents] = {};
   cudaEvent_t stageEv[8] = {};   // msbg_gpu_surface_job: events at its stage boundaries
   cudaStream_t copyStream = nullptr;        // second copy engine for large host transfers
+  cudaStream_t captureStream = nullptr;     // stream the sweeps' launch graphs are captured on
   cudaEvent_t copyEv[2] = {};               // fork / join of a split copy
   int stageCount = 0;            // events recorded by the last surface job
 

@@ -168,8 +168,11 @@ __global__ void __launch_bounds__(256) kSplatScatter(const float *__restrict__ p
 }
 
 // Pass 3, one CTA per value block (slot = blockIdx.x): the minimum of the splat
-// values of the block's particles in shared memory (1.0 where none reaches), then
-// one coalesced write of the block.  A warp takes one particle at a time; its
+// values of the block's particles in shared memory, starting from the block's
+// current values (init: FP32 channels, where the demo's splat takes the minimum
+// with what the channel holds) or from 1.0 (the FP32 staging of other storage
+// types, which the demo fills with 1.0 first), then one coalesced write of the
+// block.  A warp takes one particle at a time; its
 // lanes take the (y, z) rows of the box clipped to the block, skip rows already
 // outside the sphere (dz*dz + dy*dy exceeds it, and adding dx*dx >= 0 cannot lower
 // a float sum), and keep the voxels before the particle's abort index.
@@ -183,14 +186,17 @@ __global__ void __launch_bounds__(512) kSplatBlock(const float *__restrict__ pts
                                                    const int32_t *__restrict__ active,
                                                    const int32_t *__restrict__ abortAt,
                                                    const int64_t *__restrict__ off,
-                                                   const int32_t *__restrict__ entries, float *__restrict__ dst) {
-  constexpr int VPB = BS * BS * BS, RS = BS + 1, NW = splatSmemWords<BS>();
+                                                   const int32_t *__restrict__ entries, const float *init,
+                                                   float *dst) {
+  constexpr int VPB = BS * BS * BS, RS = BS + 1;
   extern __shared__ __align__(16) int smin[];
   const int sl = blockIdx.x;
   const int bid = active[sl];
   const int X0 = (bid % g.nbx) * BS, Y0 = ((bid / g.nbx) % g.nby) * BS, Z0 = (int)(bid / ((int64_t)g.nbx * g.nby)) * BS;
   const int one = __float_as_int(1.0f);
-  for (int v = threadIdx.x; v < NW; v += blockDim.x) smin[v] = one;
+  const float *in = init ? init + (int64_t)sl * VPB : nullptr;
+  for (int v = threadIdx.x; v < VPB; v += blockDim.x)
+    smin[(v / BS) * RS + v % BS] = in ? __float_as_int(in[v]) : one;
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nWarps = blockDim.x >> 5;
   const int64_t e0 = off[sl], e1 = off[sl + 1];
@@ -321,8 +327,6 @@ int splatRun(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rParticle, f
   }
   MSBG_CUDA(ctx, cudaMemsetAsync(ctx->dCounters + 1, 0, 8, ctx->stream));
   if (nVox == 0) return MSBG_GPU_OK;
-  if (ctx->bsx != 16 && ctx->bsx != 32)
-    return fail(ctx, MSBG_GPU_ERR_ARG, "splat: block size %d (16 or 32)", ctx->bsx);
   SplatGeom g;
   g.sx = ctx->sx; g.sy = ctx->sy; g.sz = ctx->sz; g.nbx = ctx->nbx; g.nby = ctx->nby;
   g.log2bs = ctx->log2bs;
@@ -355,6 +359,7 @@ int splatRun(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rParticle, f
       MSBG_LAUNCH(ctx, kSplatScatter, gridFor(n, 256), 256, 0, dPts, n, g, ctx->dSlot, abortAt, off, cursor,
                   entries);
     }
+    const float *init = c.storage == MSBG_GPU_F32 ? dst : nullptr;
     if (ctx->bsx == 32) {
       constexpr int smem = splatSmemWords<32>() * 4;
       static bool attr = false;
@@ -362,10 +367,14 @@ int splatRun(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rParticle, f
         MSBG_CUDA(ctx, cudaFuncSetAttribute(kSplatBlock<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         attr = true;
       }
-      MSBG_LAUNCH(ctx, kSplatBlock<32>, (unsigned)nAct, 512, smem, dPts, g, ctx->dActive, abortAt, off, entries, dst);
-    } else {
+      MSBG_LAUNCH(ctx, kSplatBlock<32>, (unsigned)nAct, 512, smem, dPts, g, ctx->dActive, abortAt, off, entries, init,
+                  dst);
+    } else if (ctx->bsx == 16) {
       MSBG_LAUNCH(ctx, kSplatBlock<16>, (unsigned)nAct, 256, splatSmemWords<16>() * 4, dPts, g, ctx->dActive, abortAt,
-                  off, entries, dst);
+                  off, entries, init, dst);
+    } else {
+      MSBG_LAUNCH(ctx, kSplatBlock<8>, (unsigned)nAct, 128, splatSmemWords<8>() * 4, dPts, g, ctx->dActive, abortAt,
+                  off, entries, init, dst);
     }
     return MSBG_GPU_OK;
   };

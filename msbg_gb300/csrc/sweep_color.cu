@@ -586,15 +586,74 @@ static int runColorT(msbg_gpu_ctx *ctx, Channel &c, bool exact, bool color8, int
   }
   static const int rbOrder[2][4] = {{1, 2, 4, 7}, {0, 3, 5, 6}};
   constexpr int NT = ColorSweep<T, BS>::NT;
-  for (int it = 0; it < nIter; it++) {
-    for (int pass = 0; pass < 8; pass++) {
-      const int col = color8 ? pass : rbOrder[pass / 4][pass % 4];
-      const int cnt = cs[col + 1] - cs[col];
-      if (cnt <= 0) continue;
-      a.bids = bids + cs[col];
-      MSBG_LAUNCH(ctx, kern, (unsigned)cnt, NT, smem, a);
+  int nLaunch = 0;
+  for (int pass = 0; pass < 8; pass++) nLaunch += cs[pass + 1] > cs[pass];
+  nLaunch *= nIter;
+  if (nLaunch == 0) return MSBG_GPU_OK;
+  auto launchAll = [&](cudaStream_t st) -> int {
+    for (int it = 0; it < nIter; it++) {
+      for (int pass = 0; pass < 8; pass++) {
+        const int col = color8 ? pass : rbOrder[pass / 4][pass % 4];
+        const int cnt = cs[col + 1] - cs[col];
+        if (cnt <= 0) continue;
+        a.bids = bids + cs[col];
+        kern<<<(unsigned)cnt, NT, smem, st>>>(a);
+        if (cudaGetLastError() != cudaSuccess) return MSBG_GPU_ERR_CUDA;
+      }
     }
+    return MSBG_GPU_OK;
+  };
+  // The colour passes go out as one CUDA graph, captured the first time a call
+  // presents these launches (kernel, arguments, grids) and replayed after that: a
+  // small layout's passes (a few hundred blocks each) are otherwise bound by the
+  // launches themselves.  A context whose stream is being captured by its caller
+  // launches them directly.
+  cudaStreamCaptureStatus outer = cudaStreamCaptureStatusNone;
+  MSBG_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &outer));
+  if (outer != cudaStreamCaptureStatusNone) {
+    if (launchAll(ctx->stream)) return fail(ctx, MSBG_GPU_ERR_CUDA, "sweep: launch failed");
+    ctx->launches += nLaunch;
+    return MSBG_GPU_OK;
   }
+  std::vector<unsigned char> key;
+  auto put = [&key](const auto &v) {
+    const unsigned char *b = reinterpret_cast<const unsigned char *>(&v);
+    key.insert(key.end(), b, b + sizeof(v));
+  };
+  put(reinterpret_cast<const void *>(kern)); put(bids); put(a.slot); put(a.payload); put(a.faces); put(a.corners);
+  put(a.nbx); put(a.nby); put(a.nbz); put(a.emptyValue); put(a.status);
+  put(p.kind); put(p.constr01); put(p.dt); put(p.anisAlpha); put(nIter); put(color8);
+  for (int i = 0; i < 9; i++) put(cs[i]);
+  cudaGraphExec_t exec = nullptr;
+  for (size_t i = 0; i < c.sweepGraphs.size(); i++)
+    if (c.sweepGraphs[i].key == key) {
+      CachedGraph hit = std::move(c.sweepGraphs[i]);
+      c.sweepGraphs.erase(c.sweepGraphs.begin() + i);
+      c.sweepGraphs.push_back(std::move(hit));
+      exec = c.sweepGraphs.back().exec;
+      break;
+    }
+  if (!exec) {
+    if (!ctx->captureStream) MSBG_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->captureStream, cudaStreamNonBlocking));
+    MSBG_CUDA(ctx, cudaStreamBeginCapture(ctx->captureStream, cudaStreamCaptureModeThreadLocal));
+    const int lrc = launchAll(ctx->captureStream);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(ctx->captureStream, &graph);
+    if (lrc || ee != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return fail(ctx, MSBG_GPU_ERR_CUDA, "sweep: capturing the colour passes failed");
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) return cudaFail(ctx, ie, "cudaGraphInstantiate");
+    if (c.sweepGraphs.size() >= 4) {  // keep the four most recent
+      cudaGraphExecDestroy(c.sweepGraphs.front().exec);
+      c.sweepGraphs.erase(c.sweepGraphs.begin());
+    }
+    c.sweepGraphs.push_back(CachedGraph{std::move(key), exec});
+  }
+  MSBG_CUDA(ctx, cudaGraphLaunch(exec, ctx->stream));
+  ctx->launches += nLaunch;
   return MSBG_GPU_OK;
 }
 

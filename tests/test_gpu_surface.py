@@ -353,3 +353,28 @@ def test_gpu_particles_per_block_match_restatement(gpulib, port, bsx):
     assert len(idx) == len(pts) - 2
     got = np.concatenate([np.sort(idx[off[b]:off[b + 1]]) for b in range(len(off) - 1)])
     assert np.array_equal(got, want_idx)
+
+
+@pytest.mark.gpu
+def test_gpu_splat_takes_the_minimum_with_the_fp32_channel(gpulib):
+    """On an FP32 channel the splat takes the minimum with what the channel holds, as the
+    demo's splat does (src/msbg_demo.cpp:624-628): filled with 0.5 instead of 1.0, the result
+    is min(0.5, the splat over 1.0) voxel by voxel."""
+    G = gpulib
+    res = 128
+    pts = W.sphere_cloud(res, 6, 3000, seed=W.workload_seed(1, 93))
+    out = {}
+    for fill in (1.0, 0.5):
+        g = G.MultiresSparseGrid(res, res, res, 16, 3, G.F32)
+        try:
+            d = g.to_device(pts)
+            g.mark_points(d, len(pts), 4.0)
+            g.levels_from_marks()
+            g.regularizeRefinementMap()
+            g.setRefinementMap(fill)
+            g.splat(d, len(pts), 2.0, 2.0)
+            out[fill] = g.payload(0)
+        finally:
+            g.close()
+    assert out[1.0].min() < 0.5 < out[1.0].max()
+    assert np.array_equal(out[0.5], np.minimum(out[1.0], np.float32(0.5)))
