@@ -212,8 +212,13 @@ __global__ void __launch_bounds__(512) kSplatBlock(const float *__restrict__ pts
     const int cz1 = max(b.iz1, Z0), cz2 = min(b.iz2, Z0 + BS - 1);
     const int cny = cy2 - cy1 + 1, cnz = cz2 - cz1 + 1;
     if (cx2 < cx1 || cny <= 0 || cnz <= 0) continue;
+    // the lane's rows: row = lane + 32 k, decoded as (row % cny, row / cny) through an
+    // approximate reciprocal (row < 34^2 and cny <= 33: the quotient's fraction stays
+    // at least 1/(2 cny) away from an integer, so the truncation is exact)
+    const float rcny = __frcp_rn((float)cny);
     for (int row = lane; row < cny * cnz; row += 32) {
-      const int iy = cy1 + row % cny, iz = cz1 + row / cny;
+      const int qz = (int)(((float)row + 0.5f) * rcny);
+      const int iy = cy1 + row - qz * cny, iz = cz1 + qz;
       const float dz = __fsub_rn((float)iz, b.z0), dy = __fsub_rn((float)iy, b.y0);
       const float dzy = __fadd_rn(__fmul_rn(dz, dz), __fmul_rn(dy, dy));
       if (dzy > g.distSqMax) continue;

@@ -125,11 +125,13 @@ def test_training_lowers_loss_and_initial_residual(setup):
     g.warmnet_predict(CH_B, CH_X)
     x0 = prob.dense(g.payload(CH_X))
     assert np.all(np.isfinite(x0))
-    assert rel_l2(x0, xstar) < 1.0  # ||x0 - x*|| < ||0 - x*||
     it_warm, rel_warm = g.mgpcg_solve(CH_X, CH_B, tol=1e-6, max_iter=100)
     g.fill(0.0, CH_X)
     it_zero, rel_zero = g.mgpcg_solve(CH_X, CH_B, tol=1e-6, max_iter=100)
     assert rel_warm <= 1e-6 and rel_zero <= 1e-6
+    # the measured gain on the held-out pair: the start's error is below 0.98 of the zero
+    # start's (0.944 measured on GB300), and the solve takes no more iterations
+    assert rel_l2(x0, xstar) < 0.98
     assert it_warm <= it_zero
     for pb, px, _ in pairs:
         pb.free()
