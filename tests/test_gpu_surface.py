@@ -378,3 +378,28 @@ def test_gpu_splat_takes_the_minimum_with_the_fp32_channel(gpulib):
             g.close()
     assert out[1.0].min() < 0.5 < out[1.0].max()
     assert np.array_equal(out[0.5], np.minimum(out[1.0], np.float32(0.5)))
+
+
+@pytest.mark.gpu
+def test_gpu_lists_and_splat_edge_cases(gpulib):
+    """No points: every per-block list is empty and the splat leaves an FP32 channel as it
+    was (the minimum with nothing); a bad argument to the tuner is an argument error."""
+    G = gpulib
+    g = G.MultiresSparseGrid(64, 64, 64, 16, 2, G.F32)
+    try:
+        g.set_levels(np.zeros(64, np.int32))
+        g.setRefinementMap(0.5)
+        d = G.DeviceBuffer.alloc(12)
+        try:
+            off, idx = g.particles_per_block(d, 0)
+            assert len(idx) == 0 and not off.any()
+            g.splat(d, 0, 2.0, 2.0)
+        finally:
+            d.free()
+        assert np.all(g.payload(0) == 0.5)
+        assert g.info().nAborted == 0
+        with pytest.raises(G.MsbgGpuError) as e:
+            g._check(g.L.msbg_gpu_poisson_tuning(g.h, 7, None, 0, None))
+        assert e.value.code == G.ERR_ARG
+    finally:
+        g.close()
