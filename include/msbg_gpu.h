@@ -406,6 +406,23 @@ int msbg_gpu_fill_halo_blocks3(msbg_gpu_ctx *ctx, int lchan, int fchan, int leve
  * leave their output as is.  Allocates scratch for the halo boxes and synchronizes. */
 int msbg_gpu_restrict_level_blocks(msbg_gpu_ctx *ctx, int lchan, int level, const int32_t *dBids, int64_t n,
                                    int simpleAverage, float *dOut, int64_t *hSkipped);
+/* multiplyLaplacianMatrixOpt (src/msbg3.cpp:1756-1912) on a multi-resolution layout, for
+ * the listed blocks of layout level `level` (the reference's call covers every level; one
+ * call per level here): Y = A X, or with MSBG_GPU_OPT_CALC_RESIDUAL Y = B - A X.  Operands
+ * are FP32 level channels: X (lchanX) at levels level-1, level, level+1 as the neighbours
+ * need them, the diagonal channel (lchanD, what the reference's CH_DIAGONAL holds: the
+ * operator multiplies by its reciprocal) and B (lchanB, residual only) at `level`.  Every
+ * block is a fluid block at its level with unit face areas (no block cuts a solid); cells
+ * of neighbouring levels meet through procNeighMixedRes2 (src/msbg3.cpp:46-161): a fine cell
+ * takes 2/3 of the coarse cell across the face, a coarse cell 1/3 of each of the four fine
+ * cells, scaled by h = 2^level; zero outside the domain.  dOut (device): n * (bsx>>level)^3
+ * floats, block k's at dOut + k*(bsx>>level)^3.  pDotprod (host, may be NULL; not with the
+ * residual) receives sum(Y X) in FP64.  A listed block is skipped (counted in *hSkipped)
+ * when it is not at `level`, has no X payload or diagonal there, or a face neighbour has no
+ * block at its level in X.  Synchronizes when pDotprod or hSkipped is given. */
+int msbg_gpu_multiply_laplacian_levels(msbg_gpu_ctx *ctx, unsigned options, int level, int lchanX, int lchanB,
+                                       int lchanD, const int32_t *dBids, int64_t n, float *dOut,
+                                       double *pDotprod, int64_t *hSkipped);
 /* ---- ray-march render of the iso-0.5 surface -----------------------------------------
  * RDR::RaymarchRenderer (src/render.h:52-160): setCamera(pos, lookAt, zoom),
  * setSunLight(sun), setSurfaceColor(color), then render() (src/render.cpp:20-101), which the

@@ -669,3 +669,276 @@ extern "C" int msbg_gpu_fill_halo_blocks3(msbg_gpu_ctx *ctx, int lchan, int fcha
   }
   return MSBG_GPU_OK;
 }
+
+// ---- the solver operator on a multi-resolution layout --------------------------------
+//
+// multiplyLaplacianMatrixOpt (src/msbg3.cpp:1756-1912) with IprocessBlockLaplacian's
+// MULTIPLY mode (src/msbg3.cpp:418-1335) for the blocks of one layout level l, every block
+// a fluid block at its own level of the X level channel, unit face areas, fluid cells.
+// Per cell (h = 2^l): F0 = h X; F1..F6 (x-1, x+1, y-1, y+1, z-1, z+1) = h X of the
+// neighbour cell in the block or in a face neighbour at level l (zero outside the domain);
+// across a face to a coarser block (level l+1) h times the FP32 product 2/3 X of the one
+// coarse cell there, to a finer block (level l-1) h times the FP64 sum of the FP32
+// products 1/3 X of the four fine cells there (procNeighMixedRes2, src/msbg3.cpp:46-161,
+// in its order of the four).  Y = (1/D) F0 - S where D != 0, else 0; S and Y in the order
+// the reference's compiled code evaluates them: in its 4- and 8-wide SIMD paths (block edge
+// >= 4) S = (F1+F2) + (F3+F4) + (F5+F6) and Y one fused multiply-add, in its 2-wide path
+// (edge 2) S left to right and Y a multiply then a subtraction.  One CTA per listed block;
+// not a hot kernel (the multigrid works on the level-0 value blocks).
+namespace msbg {
+namespace {
+
+constexpr float kCoeffCF = (float)(1.0 / (4 * 0.75));            // DPMR_GRAD_COEFF_CF (src/msbg.h:85)
+constexpr float kCoeffFC = (float)(1.0 * 2 * (1.0 / (4 * 0.75)));  // h * 2 * DPMR_GRAD_COEFF_CF, h = 1
+constexpr int kMrThreads = 256;
+
+struct MrGrid {
+  const int32_t *state;  // null: the level is not set
+  const float *pay;
+  float emptyF, fullF;
+};
+
+struct MrArgs {
+  const int32_t *bids;
+  const int32_t *levels;  // layout level of every block
+  MrGrid x[3];            // X at levels l-1 (finer), l, l+1 (coarser)
+  MrGrid d, b;            // the diagonal channel and B at level l (b: residual only)
+  int level, bs, log2bs;
+  int nbx, nby, nbz, nBlocks;
+  float h, hr;
+  int residual;
+  float *out;
+  double *dotPart;        // one FP64 partial per listed block, or null
+  unsigned long long *skipped;
+};
+
+struct MrSrc {
+  const float *pay;  // the block's payload, or null: every cell is cval
+  float cval;
+  int kind;          // 0 same level, 1 coarser, 2 finer, 3 outside the domain (zeros)
+};
+
+__device__ __forceinline__ bool mrResolve(const MrGrid &g, int bid, int bsOfLevel, MrSrc &s) {
+  if (!g.state) return false;
+  const int st = g.state[bid];
+  s.pay = nullptr;
+  s.cval = 0.0f;
+  if (st >= 0) s.pay = g.pay + (int64_t)st * bsOfLevel * bsOfLevel * bsOfLevel;
+  else if (st == MSBG_GPU_LBLK_EMPTY) s.cval = g.emptyF;
+  else if (st == MSBG_GPU_LBLK_FULL) s.cval = g.fullF;
+  else return false;  // no block at that level: the reference has no data to read there
+  return true;
+}
+
+__global__ void __launch_bounds__(kMrThreads) kApplyMultires(MrArgs a) {
+  __shared__ MrSrc face[6], own, dg, bb;
+  __shared__ int bad;
+  const int bid = a.bids[blockIdx.x];
+  const int bs = a.bs, lb = a.log2bs;
+  if (threadIdx.x == 0) {
+    bad = bid < 0 || bid >= a.nBlocks || a.levels[bid] != a.level || !mrResolve(a.x[1], bid, bs, own) || !own.pay ||
+          !mrResolve(a.d, bid, bs, dg) || (a.residual && !mrResolve(a.b, bid, bs, bb));
+  }
+  __syncthreads();
+  if (threadIdx.x < 6 && !bad) {
+    const int f = threadIdx.x, axis = f >> 1, side = f & 1;
+    int c[3] = {bid % a.nbx, (bid / a.nbx) % a.nby, bid / (a.nbx * a.nby)};
+    c[axis] += side ? 1 : -1;
+    const int nbd[3] = {a.nbx, a.nby, a.nbz};
+    MrSrc s;
+    s.kind = 3;
+    s.pay = nullptr;
+    s.cval = 0.0f;
+    if (c[axis] >= 0 && c[axis] < nbd[axis]) {
+      const int bid2 = c[0] + c[1] * a.nbx + c[2] * a.nbx * a.nby;
+      const int l2 = a.levels[bid2];
+      bool ok = true;
+      if (l2 == a.level) { s.kind = 0; ok = mrResolve(a.x[1], bid2, bs, s); }
+      else if (l2 == a.level + 1) { s.kind = 1; ok = mrResolve(a.x[2], bid2, bs >> 1, s); }
+      else if (l2 == a.level - 1) { s.kind = 2; ok = mrResolve(a.x[0], bid2, bs << 1, s); }
+      else ok = false;  // the level map is not regular
+      if (!ok) atomicOr(&bad, 1);
+    }
+    face[f] = s;
+  }
+  __syncthreads();
+  if (bad) {
+    if (threadIdx.x == 0) atomicAdd(a.skipped, 1ull);
+    return;
+  }
+  const float h = a.h;
+  // halo value of face f at in-plane coordinates (u, v): x faces (y, z), y faces (x, z),
+  // z faces (x, y)
+  auto halo = [&](int f, int u, int v) -> float {
+    const MrSrc &s = face[f];
+    const int axis = f >> 1, side = f & 1;
+    if (s.kind == 3) return 0.0f;
+    if (s.kind == 0) {
+      const int k = side ? 0 : bs - 1;
+      const int idx = axis == 0 ? k + (u << lb) + (v << 2 * lb)
+                    : axis == 1 ? u + (k << lb) + (v << 2 * lb) : u + (v << lb) + (k << 2 * lb);
+      return __fmul_rn(s.pay ? s.pay[idx] : s.cval, h);
+    }
+    if (s.kind == 1) {
+      const int b2 = bs >> 1, l2 = lb - 1, k = side ? 0 : b2 - 1, cu = u >> 1, cv = v >> 1;
+      const int idx = axis == 0 ? k + (cu << l2) + (cv << 2 * l2)
+                    : axis == 1 ? cu + (k << l2) + (cv << 2 * l2) : cu + (cv << l2) + (k << 2 * l2);
+      return __fmul_rn(__fmul_rn(kCoeffFC, s.pay ? s.pay[idx] : s.cval), h);
+    }
+    const int b2 = bs << 1, l2 = lb + 1, k = side ? 0 : b2 - 1;
+    double sum = 0.0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {  // (du, dv) = (0,0), (1,0), (0,1), (1,1)
+      const int fu = 2 * u + (q & 1), fv = 2 * v + (q >> 1);
+      const int idx = axis == 0 ? k + (fu << l2) + (fv << 2 * l2)
+                    : axis == 1 ? fu + (k << l2) + (fv << 2 * l2) : fu + (fv << l2) + (k << 2 * l2);
+      sum += (double)__fmul_rn(kCoeffCF, s.pay ? s.pay[idx] : s.cval);
+    }
+    return __double2float_rn(sum * (double)h);
+  };
+  const float *X = own.pay;
+  const int n = 1 << 3 * lb, m = bs - 1;
+  float *out = a.out + (int64_t)blockIdx.x * n;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += kMrThreads) {
+    const int vx = i & m, vy = (i >> lb) & m, vz = i >> 2 * lb;
+    const float F0 = __fmul_rn(X[i], h);
+    const float F1 = vx > 0 ? __fmul_rn(X[i - 1], h) : halo(0, vy, vz);
+    const float F2 = vx < m ? __fmul_rn(X[i + 1], h) : halo(1, vy, vz);
+    const float F3 = vy > 0 ? __fmul_rn(X[i - bs], h) : halo(2, vx, vz);
+    const float F4 = vy < m ? __fmul_rn(X[i + bs], h) : halo(3, vx, vz);
+    const float F5 = vz > 0 ? __fmul_rn(X[i - bs * bs], h) : halo(4, vx, vy);
+    const float F6 = vz < m ? __fmul_rn(X[i + bs * bs], h) : halo(5, vx, vy);
+    const float D = dg.pay ? dg.pay[i] : dg.cval;
+    float Y = 0.0f;
+    if (bs >= 4) {
+      const float S = __fadd_rn(__fadd_rn(__fadd_rn(F1, F2), __fadd_rn(F3, F4)), __fadd_rn(F5, F6));
+      if (D != 0.0f) Y = __fmaf_rn(__fdiv_rn(1.0f, D), F0, -S);
+    } else {
+      const float S = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(F1, F2), F3), F4), F5), F6);
+      if (D != 0.0f) Y = __fsub_rn(__fmul_rn(__fdiv_rn(1.0f, D), F0), S);
+    }
+    if (a.residual) Y = __fsub_rn(bb.pay ? bb.pay[i] : bb.cval, Y);
+    out[i] = Y;
+    acc += (double)Y * (double)__fmul_rn(F0, a.hr);
+  }
+  if (a.dotPart) {
+    __shared__ double warpSum[kMrThreads / 32];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) warpSum[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < kMrThreads / 32; w++) t += warpSum[w];
+      a.dotPart[blockIdx.x] = t;
+    }
+  }
+}
+
+// Sum of n FP64 partials in a fixed order (one CTA): the same bits on every run.
+__global__ void __launch_bounds__(kMrThreads) kSumPartials(const double *__restrict__ part, int64_t n,
+                                                          double *__restrict__ total) {
+  __shared__ double s[kMrThreads];
+  double t = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += kMrThreads) t += part[i];
+  s[threadIdx.x] = t;
+  __syncthreads();
+  for (int w = kMrThreads / 2; w; w >>= 1) {
+    if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = s[0];
+}
+
+MrGrid mrGrid(LevelChannels *lc, int lchan, int level, int nLevels) {
+  MrGrid g{nullptr, nullptr, 0.0f, 0.0f};
+  if (lchan < 0 || level < 0 || level >= nLevels || level >= kMaxGridLevels) return g;
+  const LevelChannel &c = lc->ch[lchan];
+  const LevelGrid &lg = c.lv[level];
+  if (c.storage != MSBG_GPU_F32 || !lg.set) return g;
+  g.state = lg.state;
+  g.pay = static_cast<const float *>(lg.pay);
+  g.emptyF = lg.emptyF;
+  g.fullF = lg.fullF;
+  return g;
+}
+
+}  // namespace
+}  // namespace msbg
+
+extern "C" int msbg_gpu_multiply_laplacian_levels(msbg_gpu_ctx *ctx, unsigned options, int level, int lchanX,
+                                                  int lchanB, int lchanD, const int32_t *dBids, int64_t n,
+                                                  float *dOut, double *pDotprod, int64_t *hSkipped) {
+  if (!ctx) return MSBG_GPU_ERR_ARG;
+  const bool residual = (options & MSBG_GPU_OPT_CALC_RESIDUAL) != 0;
+  if (options & ~MSBG_GPU_OPT_CALC_RESIDUAL)
+    return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "multiply_levels: unsupported option bits 0x%x",
+                options & ~MSBG_GPU_OPT_CALC_RESIDUAL);
+  if (residual && pDotprod)
+    return fail(ctx, MSBG_GPU_ERR_ARG, "multiply_levels: no dot product with the residual (as the reference)");
+  if (level < 0 || level >= ctx->nLevels || level >= kMaxGridLevels || (ctx->bsx >> level) < 2)
+    return fail(ctx, MSBG_GPU_ERR_ARG, "multiply_levels: level %d out of range (block edge must be >= 2)", level);
+  for (int lc : {lchanX, lchanD})
+    if (lc < 0 || lc >= kMaxLevelChannels)
+      return fail(ctx, MSBG_GPU_ERR_ARG, "multiply_levels: level channel %d out of range", lc);
+  if (residual && (lchanB < 0 || lchanB >= kMaxLevelChannels))
+    return fail(ctx, MSBG_GPU_ERR_ARG, "multiply_levels: level channel %d out of range", lchanB);
+  if (n < 0 || n > 0x7fffffff || (n > 0 && (!dBids || !dOut)))
+    return fail(ctx, MSBG_GPU_ERR_ARG, "multiply_levels: bad block list");
+  if (!ctx->layoutValid) return fail(ctx, MSBG_GPU_ERR_STATE, "no block layout: call set_refinement_map");
+  LevelChannels *lc = levelChannels(ctx);
+  MrArgs a;
+  a.x[0] = mrGrid(lc, lchanX, level - 1, ctx->nLevels);
+  a.x[1] = mrGrid(lc, lchanX, level, ctx->nLevels);
+  a.x[2] = mrGrid(lc, lchanX, level + 1, ctx->nLevels);
+  a.d = mrGrid(lc, lchanD, level, ctx->nLevels);
+  a.b = residual ? mrGrid(lc, lchanB, level, ctx->nLevels) : MrGrid{nullptr, nullptr, 0.0f, 0.0f};
+  if (!a.x[1].state || !a.d.state || (residual && !a.b.state))
+    return fail(ctx, MSBG_GPU_ERR_STATE,
+                "multiply_levels: level %d of an operand's level channel is not set as FP32", level);
+  if (n == 0) {
+    if (pDotprod) *pDotprod = 0.0;
+    if (hSkipped) *hSkipped = 0;
+    return MSBG_GPU_OK;
+  }
+  if (!lc->dSkip) MSBG_CUDA(ctx, cudaMalloc(&lc->dSkip, sizeof(unsigned long long)));
+  MSBG_CUDA(ctx, cudaMemsetAsync(lc->dSkip, 0, sizeof(unsigned long long), ctx->stream));
+  double *scratch = nullptr;  // partials [n], then the total
+  if (pDotprod) MSBG_CUDA(ctx, cudaMallocAsync((void **)&scratch, (size_t)(n + 1) * sizeof(double), ctx->stream));
+  a.bids = dBids;
+  a.levels = ctx->dLevels;
+  a.level = level;
+  a.bs = ctx->bsx >> level;
+  a.log2bs = ctx->log2bs - level;
+  a.nbx = ctx->nbx; a.nby = ctx->nby; a.nbz = ctx->nbz;
+  a.nBlocks = (int)ctx->nBlocks;
+  a.h = (float)(1 << level);
+  a.hr = 1.0f / a.h;
+  a.residual = residual;
+  a.out = dOut;
+  a.dotPart = scratch;
+  a.skipped = lc->dSkip;
+  int rc = MSBG_GPU_OK;
+  kApplyMultires<<<(unsigned)n, kMrThreads, 0, ctx->stream>>>(a);
+  ctx->launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && scratch) {
+    kSumPartials<<<1, kMrThreads, 0, ctx->stream>>>(scratch, n, scratch + n);
+    ctx->launches++;
+    e = cudaGetLastError();
+  }
+  double dot = 0.0;
+  unsigned long long sk = 0;
+  if (e == cudaSuccess && scratch) e = cudaMemcpyAsync(&dot, scratch + n, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess && hSkipped)
+    e = cudaMemcpyAsync(&sk, lc->dSkip, sizeof(sk), cudaMemcpyDeviceToHost, ctx->stream);
+  if (scratch) cudaFreeAsync(scratch, ctx->stream);
+  if (e == cudaSuccess && (pDotprod || hSkipped)) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) rc = cudaFail(ctx, e, "multiply_levels");
+  if (rc == MSBG_GPU_OK) {
+    if (pDotprod) *pDotprod = dot;
+    if (hSkipped) *hSkipped = (int64_t)sk;
+  }
+  return rc;
+}

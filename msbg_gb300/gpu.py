@@ -114,6 +114,7 @@ SIGNATURES = {
     "msbg_gpu_load": (I, [C.POINTER(P), C.c_char_p]),
     "msbg_gpu_fill_halo_blocks": (I, [P, I, I, P, I64, I, I, P, C.POINTER(I64)]),
     "msbg_gpu_restrict_level_blocks": (I, [P, I, I, P, I64, I, P, C.POINTER(I64)]),
+    "msbg_gpu_multiply_laplacian_levels": (I, [P, C.c_uint, I, I, I, I, P, I64, P, C.POINTER(D), C.POINTER(I64)]),
     "msbg_gpu_level_flags_set": (I, [P, I, I, P, P, I64, C.c_uint16, C.c_uint16]),
     "msbg_gpu_fill_halo_blocks3": (I, [P, I, I, I, P, I64, P, P, C.POINTER(I64)]),
     "msbg_gpu_diag_wait_timeout": (I, [P, I]),
@@ -739,6 +740,31 @@ class MultiresSparseGrid:
             db.free()
             do.free()
         return out, int(sk.value)
+
+    # reference: multiplyLaplacianMatrixOpt (src/msbg3.cpp:1756-1912) on a multi-resolution
+    # layout, one layout level per call
+    def multiply_laplacian_levels(self, level: int, lchan_x: int, lchan_d: int, bids: np.ndarray,
+                                  lchan_b: int = -1, residual: bool = False):
+        """Y = A X (or B - A X) for the listed blocks of layout level `level`, operands in FP32
+        level channels: (float32 [n][(bs)^3], sum(Y X) or None, skipped count)."""
+        bids = np.ascontiguousarray(bids, np.int32)
+        bs = self.bsx >> max(level, 0)
+        out = np.empty((len(bids), max(bs, 1) ** 3), np.float32)
+        db = self.to_device(bids)
+        do = DeviceBuffer.alloc(max(out.nbytes, 4))
+        dot, sk = C.c_double(), C.c_int64(-1)
+        opt = OPT_CALC_RESIDUAL if residual else 0
+        try:
+            self._check(self.L.msbg_gpu_multiply_laplacian_levels(
+                self.h, opt, level, lchan_x, lchan_b, lchan_d, C.c_void_p(db.ptr), len(bids), C.c_void_p(do.ptr),
+                None if residual else C.byref(dot), C.byref(sk)))
+            if len(bids):
+                self._check(self.L.msbg_gpu_copy_d2h(self.h, _ptr(out), C.c_void_p(do.ptr), out.nbytes))
+            self.synchronize()
+        finally:
+            db.free()
+            do.free()
+        return out, (None if residual else dot.value), int(sk.value)
 
     # reference: dotProdChannel(ch1, ch2, levelMg, blockList, pErrCode) (src/msbg.h:3331-3341);
     # a non-finite sum raises MsbgGpuError with ERR_NONFINITE (the reference's pErrCode)

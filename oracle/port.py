@@ -520,3 +520,105 @@ class PoissonProblem:
     def rel_residual(self, x, b):
         r = self.apply(x, b)
         return float(np.linalg.norm(r) / np.linalg.norm(b))
+
+
+# procNeighMixedRes2's face weights (src/msbg.h:82-87, src/msbg3.cpp:46-161), as the FP32
+# values the reference forms: a coarse cell next to finer blocks takes 1/3 of each of the
+# four fine cells across the face (DPMR_GRAD_COEFF_CF), a fine cell next to a coarser block
+# 2/3 of the one coarse cell (h * 2 * DPMR_GRAD_COEFF_CF with h = 1).
+MR_COEFF_CF = np.float32(1.0 / (4 * 0.75))
+MR_COEFF_FC = np.float32(1.0 * 2 * (1.0 / (4 * 0.75)))
+
+
+def multiply_laplacian_levels(sx, sy, sz, bsx, n_levels, levels, x, b, dinv):
+    """multiplyLaplacianMatrixOpt (src/msbg3.cpp:1756-1912, IprocessBlockLaplacian
+    src/msbg3.cpp:418-1335) on a multi-resolution layout, every block a fluid block at its
+    level (levels: regular, one entry per block), unit face areas, fluid cells.  x, b, dinv:
+    float32 over the blocks of level 0, then level 1, ..., ascending bid, (bsx>>l)^3 values
+    [z][y][x] per block of level l; dinv is what CH_DIAGONAL holds.
+
+    Per cell of a block at level l (h = 2^l): F0 = h X; the six neighbours F1..F6 (x-1, x+1,
+    y-1, y+1, z-1, z+1) are h X of the neighbour cell, in the block or in a face neighbour at
+    the same level (zero outside the domain); across a face to a coarser block h times the
+    FP32 product 2/3 X_coarse (src/msbg3.cpp:109-141); across a face to a finer block h times
+    the FP64 sum, in the reference's order, of the four FP32 products 1/3 X_fine
+    (src/msbg3.cpp:77-107).  S = F1 + ... + F6 and Y = (1/dinv) F0 - S where dinv != 0,
+    else 0 (src/msbg3.cpp:1266-1285), all FP32; R = B - Y; the dot product sum(Y * F0/h)
+    in FP64.  The reference as compiled here (-O3 -ffast-math -march=native) adds S as
+    (F1+F2) + (F3+F4) + (F5+F6) and forms Y with one fused multiply-add in its 4- and 8-wide
+    SIMD paths (blocks of edge >= 4), and keeps the source order (S left to right, Y a
+    multiply then a subtraction) in its 2-wide path (blocks of edge 2); this restatement does
+    the same (the product of two FP32 values is exact in FP64) and matches it bit for bit.
+    Returns (dot, y, r) in x's order."""
+    f32, f64 = np.float32, np.float64
+    lv = np.asarray(levels).ravel()
+    nbx, nby, nbz = sx // bsx, sy // bsx, sz // bsx
+    x, b, dinv = (np.asarray(a, f32).ravel() for a in (x, b, dinv))
+    blocks, order, off = {}, [], 0
+    for l in range(n_levels):
+        bs = bsx >> l
+        for bid in np.flatnonzero(lv == l):
+            n = bs ** 3
+            blocks[int(bid)] = (l, off, x[off:off + n].reshape(bs, bs, bs))
+            order.append(int(bid))
+            off += n
+    if off != x.size:
+        raise ValueError("array sizes do not match the level map")
+    y, r = np.empty_like(x), np.empty_like(x)
+    dot = 0.0
+
+    def face(bid, l, axis, side):
+        """Halo plane of block bid (level l) on face (axis 0 x / 1 y / 2 z, side 0 low /
+        1 high), as [z][y] (x faces), [z][x] (y faces) or [y][x] (z faces), scaled by h."""
+        bs, h = bsx >> l, f32(2 ** l)
+        bxyz = [bid % nbx, (bid // nbx) % nby, bid // (nbx * nby)]
+        bxyz[axis] += 1 if side else -1
+        if not (0 <= bxyz[0] < nbx and 0 <= bxyz[1] < nby and 0 <= bxyz[2] < nbz):
+            return np.zeros((bs, bs), f32)
+        bid2 = bxyz[0] + bxyz[1] * nbx + bxyz[2] * nbx * nby
+        l2, _, X2 = blocks[bid2]
+        bs2 = bsx >> l2
+        k = bs2 - 1 if side == 0 else 0  # the neighbour's plane that touches the face
+        plane = (X2[:, :, k], X2[:, k, :], X2[k, :, :])[axis]
+        if l2 == l:
+            return plane * h
+        if l2 == l + 1:  # coarser neighbour: each coarse cell serves 2x2 fine cells
+            v = (MR_COEFF_FC * plane) * h
+            return np.repeat(np.repeat(v, 2, axis=0), 2, axis=1)
+        if l2 == l - 1:  # finer neighbour: four fine cells per coarse cell, FP64 sum
+            p = (MR_COEFF_CF * plane).astype(f64)
+            # plane axes (outer, inner): x faces (z, y), y faces (z, x), z faces (y, x);
+            # the reference adds (inner, outer) offsets (0,0), (1,0), (0,1), (1,1)
+            s = p[0::2, 0::2] + p[0::2, 1::2]
+            s = s + p[1::2, 0::2]
+            s = s + p[1::2, 1::2]
+            return (s * f64(h)).astype(f32)
+        raise ValueError("level map is not regular")
+
+    for bid in order:
+        l, o, X = blocks[bid]
+        bs, h = bsx >> l, f32(2 ** l)
+        n = bs ** 3
+        P = np.zeros((bs + 2,) * 3, f32)
+        F0 = X * h
+        P[1:-1, 1:-1, 1:-1] = F0
+        P[1:-1, 1:-1, 0], P[1:-1, 1:-1, -1] = face(bid, l, 0, 0), face(bid, l, 0, 1)
+        P[1:-1, 0, 1:-1], P[1:-1, -1, 1:-1] = face(bid, l, 1, 0), face(bid, l, 1, 1)
+        P[0, 1:-1, 1:-1], P[-1, 1:-1, 1:-1] = face(bid, l, 2, 0), face(bid, l, 2, 1)
+        F = (P[1:-1, 1:-1, :-2], P[1:-1, 1:-1, 2:], P[1:-1, :-2, 1:-1], P[1:-1, 2:, 1:-1],
+             P[:-2, 1:-1, 1:-1], P[2:, 1:-1, 1:-1])
+        if bs >= 4:
+            S = ((F[0] + F[1]) + (F[2] + F[3])) + (F[4] + F[5])
+        else:
+            S = ((((F[0] + F[1]) + F[2]) + F[3]) + F[4]) + F[5]
+        D = dinv[o:o + n].reshape(bs, bs, bs)
+        with np.errstate(divide="ignore"):
+            rD = f32(1.0) / D
+        if bs >= 4:
+            Y = np.where(D != 0, (rD.astype(f64) * F0.astype(f64) - S.astype(f64)).astype(f32), f32(0.0))
+        else:
+            Y = np.where(D != 0, rD * F0 - S, f32(0.0)).astype(f32)
+        y[o:o + n] = Y.ravel()
+        r[o:o + n] = (b[o:o + n] - Y.ravel()).astype(f32)
+        dot += float((Y.astype(f64) * (F0 * f32(1.0 / h)).astype(f64)).sum())
+    return dot, y, r

@@ -15,7 +15,8 @@
  * (halo job), the ray-march renderer RDR::RaymarchRenderer (render job),
  * sortBlockListMorton (morton job), the solver building blocks
  * multiplyLaplacianMatrixOpt / dotProdChannel / AXPBYChannelCombined / relaxBlockList
- * (solver job) and downsampleFloatChannelNew (downsample job).
+ * (solver job), the same operator on a multi-resolution layout (multires job) and
+ * downsampleFloatChannelNew (downsample job).
  *
  * Differences from the demo, both forced by the workload definition:
  *  - points come from the job file (already in voxel coordinates) instead of
@@ -665,6 +666,106 @@ int runSolverJob(const OracleJobHeader &job, const int32_t *bidsIn, const float 
   return 0;
 }
 
+// multiplyLaplacianMatrixOpt (src/msbg3.cpp:1756-1912) on a multi-resolution layout: every
+// block of the job's level map (already regular) is a fluid block at its own level, so
+// blocks of neighbouring levels meet through the mixed-resolution faces of
+// procNeighMixedRes2 (src/msbg3.cpp:46-161) and the halo code around it
+// (src/msbg3.cpp:664-1042).  No block cuts a solid (no face-area channels are read) and
+// every cell is fluid (cell flags 0).  Inputs after the levels: float32 X, B and DINV (what
+// CH_DIAGONAL holds; the operator multiplies by 1/DINV), each over the blocks of level 0,
+// then level 1, ..., in ascending bid order, (bsx>>l)^3 values per block of level l.
+// Output: sum(Y X) (FP64), then Y = A X and R = B - A X in the same order.
+int runMultiresJob(const OracleJobHeader &job, const int32_t *levelsIn, const float *arrays, FILE *fout) {
+  OracleOutHeader out;
+  memset(&out, 0, sizeof(out));
+  memcpy(out.magic, ORACLE_OUT_MAGIC, 8);
+  MultiresSparseGrid *msbg = MultiresSparseGrid::create(
+      "TEST", job.sx, job.sy, job.sz, job.bsx, -1, 0, -1, 0, NULL, NULL, job.nLevels);
+  if (!msbg) return 2;
+  const int nBlocks = msbg->nBlocks();
+  if ((int64_t)nBlocks != job.nBlocksIn) return 4;
+  std::vector<int> levels(levelsIn, levelsIn + nBlocks);
+  msbg->regularizeRefinementMap(levels.data());
+  for (int b = 0; b < nBlocks; b++)
+    if (levels[b] != levelsIn[b]) return 5;
+  msbg->setRefinementMap(levels.data(), NULL, 0, NULL, false, false);
+  using MSBG::CH_PRESSURE;
+  using MSBG::CH_DIVERGENCE;
+  using MSBG::CH_CG_Q;
+  using MSBG::CH_DIAGONAL;
+  std::vector<std::vector<int32_t>> bidsL(job.nLevels);
+  for (int b = 0; b < nBlocks; b++) {
+    if (levels[b] < 0 || levels[b] >= job.nLevels) return 4;
+    bidsL[levels[b]].push_back(b);
+  }
+  size_t total = 0;
+  for (int l = 0; l < job.nLevels; l++) {
+    const size_t bs = (size_t)(job.bsx >> l);
+    total += bidsL[l].size() * bs * bs * bs;
+  }
+  const float *X = arrays, *B = X + total, *DI = B + total;
+  size_t off = 0;
+  for (int l = 0; l < job.nLevels; l++) {
+    SparseGrid<PSFloat> *sgX = msbg->getPSFloatChannel(CH_PRESSURE, l, 0),
+                        *sgB = msbg->getPSFloatChannel(CH_DIVERGENCE, l, 0),
+                        *sgQ = msbg->getPSFloatChannel(CH_CG_Q, l, 0),
+                        *sgD = msbg->getPSFloatChannel(CH_DIAGONAL, l, 0);
+    SparseGrid<MSBG::CellFlags> *sgF = msbg->getFlagsChannel(MSBG::CH_CELL_FLAGS, l, 0);
+    if (!sgX || !sgB || !sgQ || !sgD || !sgF) return 3;
+    loadValueBlocks<float>(sgX, bidsL[l], X + off, nBlocks, 0.f);
+    loadValueBlocks<float>(sgB, bidsL[l], B + off, nBlocks, 0.f);
+    loadValueBlocks<float>(sgD, bidsL[l], DI + off, nBlocks, 0.f);
+    loadValueBlocks<float>(sgQ, bidsL[l], nullptr, nBlocks, 0.f);
+    loadValueBlocks<MSBG::CellFlags>(sgF, bidsL[l], nullptr, nBlocks, 0);
+    for (int k = 0; k < 3; k++) {  // allocated, read by no block (none cuts a solid)
+      SparseGrid<float> *fa = msbg->getFaceAreaChannel(k, l, 0);
+      if (!fa) return 3;
+      loadValueBlocks<float>(fa, bidsL[l], nullptr, nBlocks, 1.f);
+    }
+    const size_t bs = (size_t)(job.bsx >> l);
+    off += bidsL[l].size() * bs * bs * bs;
+  }
+  for (int b = 0; b < nBlocks; b++) {
+    MSBG::BlockInfo *bi = msbg->getBlockInfo(b, 0);
+    bi->flags &= ~(MSBG::BLK_NO_FLUID | MSBG::BLK_FIXED | MSBG::BLK_ONLY_FLUID | MSBG::BLK_CUTS_SOLID);
+  }
+  auto dumpQ = [&](std::vector<float> &dst) {
+    dst.resize(total);
+    size_t o = 0;
+    for (int l = 0; l < job.nLevels; l++) {
+      SparseGrid<PSFloat> *sgQ = msbg->getPSFloatChannel(CH_CG_Q, l, 0);
+      const size_t nv = (size_t)sgQ->nVoxelsInBlock();
+      for (int32_t b : bidsL[l]) {
+        memcpy(&dst[o], sgQ->getBlockDataPtr(b, 0, 0), nv * 4);
+        o += nv;
+      }
+    }
+  };
+  std::vector<int> list;
+  for (int l = 0; l < job.nLevels; l++) list.insert(list.end(), bidsL[l].begin(), bidsL[l].end());
+  const double t0 = nowSec();
+  long double dotYX = 0;
+  msbg->multiplyLaplacianMatrixOpt(0, 0, CH_PRESSURE, CH_DIVERGENCE, 0.f, CH_CG_Q, &dotYX, &list);
+  std::vector<float> Y, R;
+  dumpQ(Y);
+  msbg->multiplyLaplacianMatrixOpt(MSBG::OPT_CALC_RESIDUAL, 0, CH_PRESSURE, CH_DIVERGENCE, 0.f, CH_CG_Q, NULL,
+                                   &list);
+  dumpQ(R);
+  out.tPdeSec = nowSec() - t0;
+  out.nBlocks = nBlocks;
+  out.nActive = nBlocks;
+  for (int l = 0; l < job.nLevels && l < 8; l++) out.nBlocksPerLevel[l] = (int64_t)bidsL[l].size();
+  out.elemBytes = 4;
+  out.nThreadsUsed = omp_get_max_threads();
+  fwrite(&out, sizeof(out), 1, fout);
+  const double dot = (double)dotYX;
+  fwrite(&dot, 8, 1, fout);
+  fwrite(Y.data(), 4, total, fout);
+  fwrite(R.data(), 4, total, fout);
+  MultiresSparseGrid::destroy(msbg);
+  return 0;
+}
+
 // downsampleFloatChannelNew (src/msbg4.cpp:1035-1379) to multigrid level 1 on a
 // multi-level grid loaded like the halo job (channel CH_FLOAT_1, every resolution level
 // with the job's block states and payloads; job.laplTyp = 0).  constr01 = 1 adds
@@ -874,6 +975,19 @@ int main(int argc, char **argv) {
     if (!solverArrays.empty() && fread(solverArrays.data(), 4, solverArrays.size(), fin) != solverArrays.size())
       return 1;
   }
+  if (job.jobType == ORACLE_JOB_MULTIRES) {
+    size_t total = 0;
+    std::vector<size_t> perLevel(job.nLevels > 0 ? job.nLevels : 0, 0);
+    for (int64_t b = 0; b < job.nBlocksIn; b++)
+      if (lv[b] >= 0 && lv[b] < job.nLevels) perLevel[lv[b]]++;
+    for (int l = 0; l < job.nLevels; l++) {
+      const size_t bs = (size_t)(job.bsx >> l);
+      total += perLevel[l] * bs * bs * bs;
+    }
+    solverArrays.resize(3 * total);
+    if (!solverArrays.empty() && fread(solverArrays.data(), 4, solverArrays.size(), fin) != solverArrays.size())
+      return 1;
+  }
   std::vector<int32_t> fstate, dbc(6, 0);
   std::vector<std::vector<uint16_t>> flagPay;
   if (job.jobType == ORACLE_JOB_HALO || job.jobType == ORACLE_JOB_DOWNSAMPLE || job.jobType == ORACLE_JOB_HALO3) {
@@ -927,6 +1041,8 @@ int main(int argc, char **argv) {
     rc = runLayoutJob(job, lv.data(), fout);
   else if (job.jobType == ORACLE_JOB_SOLVER)
     rc = runSolverJob(job, lv.data(), solverArrays.data(), fout);
+  else if (job.jobType == ORACLE_JOB_MULTIRES)
+    rc = runMultiresJob(job, lv.data(), solverArrays.data(), fout);
   else if (job.jobType == ORACLE_JOB_HALO3)
     rc = job.chanType == ORACLE_CHAN_F32
              ? runHalo3Job(job, lv.data(), state.data(), levelPay, fstate.data(), flagPay, dbc.data(), fout)

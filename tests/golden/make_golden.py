@@ -16,9 +16,10 @@ lists), reference_solver.npz (the solver building blocks and the block smoother)
 reference_downsample.npz (downsampleFloatChannelNew on multi-level channels) and
 reference_surface512.npz (the 512^3 surface workload at full size: layout, counters,
 per-block sums and a voxel sample of the fields), reference_halo3.npz (the solver's halo,
-fillHaloBlock3) and reference_layout.npz (setRefinementMap's block lists and fine-coarse
-distance channel).  Arguments name a subset
-(small interp halo render morton solver downsample surface512 halo3 layout).
+fillHaloBlock3), reference_layout.npz (setRefinementMap's block lists and fine-coarse
+distance channel) and reference_multires.npz (the solver operator on multi-resolution
+layouts).  Arguments name a subset
+(small interp halo render morton solver downsample surface512 halo3 layout multires).
 """
 from __future__ import annotations
 
@@ -66,7 +67,7 @@ def main(which: list[str]) -> None:
     if not O.ref_available():
         raise SystemExit("oracle/_ref/msbg_ref_driver missing: run `make -C oracle ref` first")
     parts = set(which) or {"small", "interp", "halo", "render", "morton", "solver", "downsample", "surface512",
-                           "halo3", "layout"}
+                           "halo3", "layout", "multires"}
     if parts & {"small", "interp", "render"}:
         out = make_small()
         if "interp" in parts:
@@ -87,6 +88,8 @@ def main(which: list[str]) -> None:
         make_halo3()
     if "layout" in parts:
         make_layout()
+    if "multires" in parts:
+        make_multires()
 
 
 def make_small() -> dict:
@@ -303,6 +306,26 @@ def make_downsample() -> None:
 
 
 SURFACE512_SAMPLE = 60000
+
+
+def make_multires() -> None:
+    """multiplyLaplacianMatrixOpt on multi-resolution layouts (oracle/ref_driver.cpp, multires
+    job): Y = A X with sum(Y X) and B - A X for the seeded cases of tests/halo_cases.py, whose
+    neighbouring levels meet through procNeighMixedRes2."""
+    import halo_cases as H
+    import port as P
+    out = {}
+    for nb, bsx, seed in H.MULTIRES_CASES:
+        lv, x, b, dinv = H.multires_case(nb, bsx, 3, seed, lambda *a: P.regularize(*a)[0])
+        key = "x".join(map(str, nb)) + f"_bs{bsx}"
+        r = O.run_reference_multires(*(n * bsx for n in nb), bsx, 3, lv, x, b, dinv)
+        out[f"{key}_levels"] = lv
+        out[f"{key}_y"] = r["y"]
+        out[f"{key}_r"] = r["r"]
+        out[f"{key}_dot"] = np.float64(r["dot"])
+    path = os.path.join(HERE, "reference_multires.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
 
 
 def make_layout() -> None:

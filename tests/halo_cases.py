@@ -87,3 +87,29 @@ def flags_case(states, bsx: int, seed: int):
                                                                                      CELL_AIR)))
         fpay.append(f.astype(np.uint16))
     return [s.copy() for s in states], fpay, CELL_VOID | CELL_AIR, CELL_AIR
+
+
+# the solver operator on multi-resolution layouts (multiplyLaplacianMatrixOpt with
+# procNeighMixedRes2): (block grid, block edge, seed).  The reference's operator takes block
+# edges 16, 8, 4 and 2 (an edge-32 layout stops it with an assertion).
+MULTIRES_CASES = (((4, 4, 4), 16, 20261203 + 990), ((5, 3, 4), 8, 20261203 + 991),
+                  ((6, 5, 4), 16, 20261203 + 992))
+
+
+def multires_case(nb, bsx: int, n_levels: int, seed: int, regularize):
+    """A regular level map (as halo_case) with every block a fluid block at its level, and
+    float32 X, B and the diagonal channel's values over the blocks of level 0, then level 1,
+    ..., ascending bid: X, B standard normal, the diagonal uniform in [0.1, 0.2] with about
+    1% zeros (cells the operator sets to 0).  Returns (levels, x, b, dinv)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = int(np.prod(nb))
+    bz, by, bx = np.meshgrid(np.arange(nb[2]), np.arange(nb[1]), np.arange(nb[0]), indexing="ij")
+    d = (bx + by + bz).ravel() + rng.integers(-1, 2, n)
+    lv = np.clip(d // 2, 0, n_levels - 1).astype(np.int32)
+    lv = np.asarray(regularize(lv, nb[0], nb[1], nb[2], n_levels), np.int32)
+    total = sum(int((lv == l).sum()) * (bsx >> l) ** 3 for l in range(n_levels))
+    x = rng.standard_normal(total).astype(np.float32)
+    b = rng.standard_normal(total).astype(np.float32)
+    dinv = rng.uniform(0.1, 0.2, total).astype(np.float32)
+    dinv[rng.random(total) < 0.01] = 0.0
+    return lv, x, b, dinv

@@ -10,6 +10,9 @@ reference's calls.
 * Block lists: a listed call touches only the listed value blocks, and equals the whole-layout
   call there; sweeps with a list equal the restatement's sweeps of that list bit for bit.
 * downsampleFloatChannelNew on multi-level channels (reference_downsample.npz): bit for bit.
+* multiplyLaplacianMatrixOpt on 3-level layouts with mixed-resolution faces
+  (reference_multires.npz, msbg_gpu_multiply_laplacian_levels): Y = A X and B - A X bit for
+  bit, the dot product to FP64 rounding.
 * The 512^3 surface workload at full size (reference_surface512.npz): active set, levels,
   flags and particle counts bit for bit; FP32 field sums and voxel sample within rel-L2 1e-5
   for the EXACT and FAST sweep variants; the uint16 sample within 8 quanta.
@@ -205,3 +208,58 @@ def test_surface512_full_size_matches_reference(gpulib, storage, variant):
         else:
             d = np.abs(field.reshape(-1)[idx].astype(np.int64) - gold[f"u16_{stage}_sample"].astype(np.int64))
             assert d.max() <= 8
+
+
+def _multires_grid(G, nb, bsx, lv, x, b, dinv):
+    """A context on the level map with level channels 0 = X, 1 = the diagonal channel, 2 = B:
+    level l holds the blocks of level l (payload in ascending bid order), no block elsewhere."""
+    g = G.MultiresSparseGrid(nb[0] * bsx, nb[1] * bsx, nb[2] * bsx, bsx, 3, G.F32)
+    g.set_levels(lv)
+    g.setRefinementMap(0.0)
+    off, spans = 0, []
+    for l in range(3):
+        at = lv == l
+        st = np.full(lv.size, H.LBLK_NONE, np.int32)
+        st[at] = np.arange(int(at.sum()), dtype=np.int32)
+        n = int(at.sum()) * (bsx >> l) ** 3
+        for lchan, arr in ((0, x), (1, dinv), (2, b)):
+            g.level_grid_set(lchan, l, G.F32, st, arr[off:off + n] if n else None)
+        spans.append((off, n))
+        off += n
+    return g, spans
+
+
+@pytest.mark.parametrize("case", H.MULTIRES_CASES, ids=["x".join(map(str, c[0])) + f"_bs{c[1]}" for c in H.MULTIRES_CASES])
+def test_multires_operator_matches_reference(gpulib, port, case):
+    G = gpulib
+    gold = dict(np.load(os.path.join(GOLD, "reference_multires.npz")))
+    nb, bsx, seed = case
+    key = "x".join(map(str, nb)) + f"_bs{bsx}"
+    lv, x, b, dinv = H.multires_case(nb, bsx, 3, seed, lambda *a: port.regularize(*a)[0])
+    assert np.array_equal(lv, gold[f"{key}_levels"])
+    g, spans = _multires_grid(G, nb, bsx, lv, x, b, dinv)
+    try:
+        dot = 0.0
+        for l, (off, n) in enumerate(spans):
+            bids = np.flatnonzero(lv == l).astype(np.int32)
+            y, d, sk = g.multiply_laplacian_levels(l, 0, 1, bids)
+            assert sk == 0
+            assert np.array_equal(y.reshape(-1).view(np.uint32), gold[f"{key}_y"][off:off + n].view(np.uint32)), (key, l)
+            r, _, sk = g.multiply_laplacian_levels(l, 0, 1, bids, lchan_b=2, residual=True)
+            assert sk == 0
+            assert np.array_equal(r.reshape(-1).view(np.uint32), gold[f"{key}_r"][off:off + n].view(np.uint32)), (key, l)
+            dot += d
+        assert abs(dot - float(gold[f"{key}_dot"])) <= 1e-12 * abs(dot)
+        # a block of another level, and one out of range, are skipped; the rest is unchanged
+        bids0 = np.flatnonzero(lv == 0).astype(np.int32)
+        other = np.flatnonzero(lv == 1)[:1].astype(np.int32)
+        y, _, sk = g.multiply_laplacian_levels(0, 0, 1, np.concatenate([bids0, other, [lv.size]]).astype(np.int32))
+        assert sk == 2
+        off, n = spans[0]
+        assert np.array_equal(y[: len(bids0)].reshape(-1).view(np.uint32), gold[f"{key}_y"][off:off + n].view(np.uint32))
+        # an operand level channel that is not set
+        with pytest.raises(G.MsbgGpuError) as e:
+            g.multiply_laplacian_levels(0, 7, 1, bids0)
+        assert e.value.code == G.ERR_STATE
+    finally:
+        g.close()

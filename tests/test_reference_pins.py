@@ -129,3 +129,58 @@ def test_fresh_reference_downsample(port):
     got, _ = port.restrict_level(g, lv, st, pay, 0, bids, False, 0.1, 0.9)
     ulp = np.abs(got.view(np.int32).astype(np.int64) - vals.view(np.int32).astype(np.int64))
     assert ulp.max() <= 1 and (ulp > 0).mean() < 0.005
+
+
+# ------------------------------------------- the solver operator on multi-resolution layouts
+
+def _multires_key(nb, bsx):
+    return "x".join(map(str, nb)) + f"_bs{bsx}"
+
+
+@pytest.mark.parametrize("case", H.MULTIRES_CASES, ids=[_multires_key(c[0], c[1]) for c in H.MULTIRES_CASES])
+def test_multires_operator_matches_reference(port, case):
+    """multiplyLaplacianMatrixOpt on a 3-level layout, blocks of neighbouring levels meeting
+    through procNeighMixedRes2 (src/msbg3.cpp:46-161): the restatement equals the reference
+    bit for bit (Y = A X and B - A X), the FP64 dot product to rounding."""
+    gold = dict(np.load(os.path.join(GOLD, "reference_multires.npz")))
+    nb, bsx, seed = case
+    key = _multires_key(nb, bsx)
+    lv, x, b, dinv = H.multires_case(nb, bsx, 3, seed, lambda *a: port.regularize(*a)[0])
+    assert np.array_equal(lv, gold[f"{key}_levels"])
+    assert len(np.unique(lv)) == 3  # every level present, so both kinds of mixed faces occur
+    dot, y, r = port.multiply_laplacian_levels(*(n * bsx for n in nb), bsx, 3, lv, x, b, dinv)
+    assert np.array_equal(y.view(np.uint32), gold[f"{key}_y"].view(np.uint32))
+    assert np.array_equal(r.view(np.uint32), gold[f"{key}_r"].view(np.uint32))
+    assert abs(dot - float(gold[f"{key}_dot"])) <= 1e-12 * abs(dot)
+
+
+def test_multires_faces_weigh_the_other_level(port):
+    """Known answers of the mixed-resolution faces: X = 1 everywhere and the diagonal channel
+    1/6 make Y = 6 h - S vanish inside a level and leave, on a fine cell next to a coarser
+    block, h (1 - 2/3) from the one face (the coarse side weighs 2/3), and on a coarse cell
+    next to a finer block h (1 - 4/3) (four fine cells of 1/3)."""
+    nb, bsx = (2, 1, 1), 8
+    lv = np.array([0, 1], np.int32)
+    n0, n1 = bsx ** 3, (bsx // 2) ** 3
+    x = np.ones(n0 + n1, np.float32)
+    dinv = np.full(n0 + n1, np.float32(1) / np.float32(6), np.float32)
+    dot, y, r = port.multiply_laplacian_levels(2 * bsx, bsx, bsx, bsx, 2, lv, x, x, dinv)
+    y0 = y[:n0].reshape(bsx, bsx, bsx)
+    y1 = y[n0:].reshape(bsx // 2, bsx // 2, bsx // 2)
+    # interior cells of either block: 6 h X / 6 ... minus the six neighbours h X
+    assert abs(float(y0[3, 3, 3])) < 1e-6 and abs(float(y1[1, 1, 1])) < 1e-6
+    # level-0 cell at x = bsx-1 (face to the coarser block): 1 - 2/3
+    assert abs(float(y0[3, 3, bsx - 1]) - (1 - 2 / 3)) < 1e-6
+    # level-1 cell at x = 0 (face to the finer block), h = 2: 2 (1 - 4/3)
+    assert abs(float(y1[1, 1, 0]) - 2 * (1 - 4 / 3)) < 1e-5
+
+
+def test_multires_restatement_matches_fresh_reference(port):
+    O = _ref()
+    nb, bsx = (4, 3, 5), 8
+    lv, x, b, dinv = H.multires_case(nb, bsx, 3, 20261203 + 995, lambda *a: port.regularize(*a)[0])
+    ref = O.run_reference_multires(*(n * bsx for n in nb), bsx, 3, lv, x, b, dinv)
+    dot, y, r = port.multiply_laplacian_levels(*(n * bsx for n in nb), bsx, 3, lv, x, b, dinv)
+    assert np.array_equal(y.view(np.uint32), ref["y"].view(np.uint32))
+    assert np.array_equal(r.view(np.uint32), ref["r"].view(np.uint32))
+    assert abs(dot - ref["dot"]) <= 1e-12 * abs(dot)
