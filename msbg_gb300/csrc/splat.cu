@@ -177,25 +177,29 @@ __global__ void __launch_bounds__(256) kSplatScatter(const float *__restrict__ p
 // outside the sphere (dz*dz + dy*dy exceeds it, and adding dx*dx >= 0 cannot lower
 // a float sum), and keep the voxels before the particle's abort index.
 // The block's minima in shared memory use a row stride of BS + 1 words: the lanes
-// of a warp take different rows, which then fall into different banks.
-template <int BS>
-constexpr int splatSmemWords() { return BS * BS * (BS + 1); }
+// of a warp take different rows, which then fall into different banks.  NZ CTAs
+// share a block, each taking BS/NZ of its z-planes (and clipping the boxes to
+// them): for BS = 32 two halves of 68 KB let three CTAs share an SM where a whole
+// block's 135 KB allowed one.
+template <int BS, int NZ>
+constexpr int splatSmemWords() { return BS * (BS / NZ) * (BS + 1); }
 
-template <int BS>
-__global__ void __launch_bounds__(512) kSplatBlock(const float *__restrict__ pts, SplatGeom g,
+template <int BS, int NZ>
+__global__ void __launch_bounds__(512, NZ == 1 ? 1 : 3) kSplatBlock(const float *__restrict__ pts, SplatGeom g,
                                                    const int32_t *__restrict__ active,
                                                    const int32_t *__restrict__ abortAt,
                                                    const int64_t *__restrict__ off,
                                                    const int32_t *__restrict__ entries, const float *init,
                                                    float *dst) {
-  constexpr int VPB = BS * BS * BS, RS = BS + 1;
+  constexpr int VPB = BS * BS * BS, RS = BS + 1, PZ = BS / NZ, VPP = BS * BS * PZ;
   extern __shared__ __align__(16) int smin[];
-  const int sl = blockIdx.x;
+  const int sl = blockIdx.x / NZ, zp = blockIdx.x % NZ;
   const int bid = active[sl];
-  const int X0 = (bid % g.nbx) * BS, Y0 = ((bid / g.nbx) % g.nby) * BS, Z0 = (int)(bid / ((int64_t)g.nbx * g.nby)) * BS;
+  const int X0 = (bid % g.nbx) * BS, Y0 = ((bid / g.nbx) % g.nby) * BS,
+            Z0 = (int)(bid / ((int64_t)g.nbx * g.nby)) * BS + zp * PZ;  // this CTA's first plane
   const int one = __float_as_int(1.0f);
-  const float *in = init ? init + (int64_t)sl * VPB : nullptr;
-  for (int v = threadIdx.x; v < VPB; v += blockDim.x)
+  const float *in = init ? init + (int64_t)sl * VPB + zp * VPP : nullptr;
+  for (int v = threadIdx.x; v < VPP; v += blockDim.x)
     smin[(v / BS) * RS + v % BS] = in ? __float_as_int(in[v]) : one;
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nWarps = blockDim.x >> 5;
@@ -209,7 +213,7 @@ __global__ void __launch_bounds__(512) kSplatBlock(const float *__restrict__ pts
     const int nx = b.ix2 - b.ix1 + 1, ny = b.iy2 - b.iy1 + 1;
     const int cx1 = max(b.ix1, X0), cx2 = min(b.ix2, X0 + BS - 1);
     const int cy1 = max(b.iy1, Y0), cy2 = min(b.iy2, Y0 + BS - 1);
-    const int cz1 = max(b.iz1, Z0), cz2 = min(b.iz2, Z0 + BS - 1);
+    const int cz1 = max(b.iz1, Z0), cz2 = min(b.iz2, Z0 + PZ - 1);
     const int cny = cy2 - cy1 + 1, cnz = cz2 - cz1 + 1;
     if (cx2 < cx1 || cny <= 0 || cnz <= 0) continue;
     // the lane's rows: row = lane + 32 k, decoded as (row % cny, row / cny) through an
@@ -234,8 +238,8 @@ __global__ void __launch_bounds__(512) kSplatBlock(const float *__restrict__ pts
     }
   }
   __syncthreads();
-  float *out = dst + (int64_t)sl * VPB;
-  for (int v = threadIdx.x * 4; v < VPB; v += blockDim.x * 4) {
+  float *out = dst + (int64_t)sl * VPB + zp * VPP;
+  for (int v = threadIdx.x * 4; v < VPP; v += blockDim.x * 4) {
     const int *row = smin + (v / BS) * RS + v % BS;
     *reinterpret_cast<int4 *>(out + v) = make_int4(row[0], row[1], row[2], row[3]);
   }
@@ -366,20 +370,20 @@ int splatRun(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rParticle, f
     }
     const float *init = c.storage == MSBG_GPU_F32 ? dst : nullptr;
     if (ctx->bsx == 32) {
-      constexpr int smem = splatSmemWords<32>() * 4;
+      constexpr int smem = splatSmemWords<32, 2>() * 4;
       static bool attr = false;
       if (!attr) {
-        MSBG_CUDA(ctx, cudaFuncSetAttribute(kSplatBlock<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        MSBG_CUDA(ctx, cudaFuncSetAttribute(kSplatBlock<32, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         attr = true;
       }
-      MSBG_LAUNCH(ctx, kSplatBlock<32>, (unsigned)nAct, 512, smem, dPts, g, ctx->dActive, abortAt, off, entries, init,
-                  dst);
+      MSBG_LAUNCH(ctx, (kSplatBlock<32, 2>), (unsigned)(2 * nAct), 512, smem, dPts, g, ctx->dActive, abortAt, off,
+                  entries, init, dst);
     } else if (ctx->bsx == 16) {
-      MSBG_LAUNCH(ctx, kSplatBlock<16>, (unsigned)nAct, 256, splatSmemWords<16>() * 4, dPts, g, ctx->dActive, abortAt,
-                  off, entries, init, dst);
+      MSBG_LAUNCH(ctx, (kSplatBlock<16, 1>), (unsigned)nAct, 256, (splatSmemWords<16, 1>() * 4), dPts, g, ctx->dActive,
+                  abortAt, off, entries, init, dst);
     } else {
-      MSBG_LAUNCH(ctx, kSplatBlock<8>, (unsigned)nAct, 128, splatSmemWords<8>() * 4, dPts, g, ctx->dActive, abortAt,
-                  off, entries, init, dst);
+      MSBG_LAUNCH(ctx, (kSplatBlock<8, 1>), (unsigned)nAct, 128, (splatSmemWords<8, 1>() * 4), dPts, g, ctx->dActive,
+                  abortAt, off, entries, init, dst);
     }
     return MSBG_GPU_OK;
   };
