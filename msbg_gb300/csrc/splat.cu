@@ -183,9 +183,14 @@ __global__ void __launch_bounds__(256) kSplatScatter(const float *__restrict__ p
 // block's 135 KB allowed one.
 template <int BS, int NZ>
 constexpr int splatSmemWords() { return BS * (BS / NZ) * (BS + 1); }
+// threads per CTA (BS^2 / 2), and CTAs per SM to keep the registers for: 1536 threads
+template <int BS>
+constexpr int splatThreads() { return BS * BS / 2; }
+template <int BS>
+constexpr int splatMinCtas() { return 1536 / splatThreads<BS>(); }
 
 template <int BS, int NZ>
-__global__ void __launch_bounds__(512, NZ == 1 ? 1 : 3) kSplatBlock(const float *__restrict__ pts, SplatGeom g,
+__global__ void __launch_bounds__(splatThreads<BS>(), splatMinCtas<BS>()) kSplatBlock(const float *__restrict__ pts, SplatGeom g,
                                                    const int32_t *__restrict__ active,
                                                    const int32_t *__restrict__ abortAt,
                                                    const int64_t *__restrict__ off,
@@ -228,11 +233,15 @@ __global__ void __launch_bounds__(512, NZ == 1 ? 1 : 3) kSplatBlock(const float 
       if (dzy > g.distSqMax) continue;
       const int rowScan = ((iz - b.iz1) * ny + (iy - b.iy1)) * nx - b.ix1;  // + ix: the scan index
       int *rowMin = smin + ((iz - Z0) * BS + (iy - Y0)) * RS - X0;
-      for (int ix = cx1; ix <= cx2; ix++) {
+      // the scan index grows with ix along the row, so the abort rule cuts the row at
+      // ab - rowScan; x runs as a float (exact for these integers)
+      const int xEnd = min(cx2, ab - 1 - rowScan);
+      float fx = (float)cx1;
+      for (int ix = cx1; ix <= xEnd; ix++, fx += 1.0f) {
         // distSq exactly as the demo forms it: (dz*dz + dy*dy) + dx*dx
-        const float dx = __fsub_rn((float)ix, b.x0);
+        const float dx = __fsub_rn(fx, b.x0);
         const float d2 = __fadd_rn(dzy, __fmul_rn(dx, dx));
-        if (d2 > g.distSqMax || rowScan + ix >= ab) continue;
+        if (d2 > g.distSqMax) continue;
         atomicMin(rowMin + ix, __float_as_int(__fmul_rn(d2, g.distSqMaxInv)));
       }
     }
@@ -376,13 +385,13 @@ int splatRun(msbg_gpu_ctx *ctx, const float *dPts, int64_t n, float rParticle, f
         MSBG_CUDA(ctx, cudaFuncSetAttribute(kSplatBlock<32, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         attr = true;
       }
-      MSBG_LAUNCH(ctx, (kSplatBlock<32, 2>), (unsigned)(2 * nAct), 512, smem, dPts, g, ctx->dActive, abortAt, off,
+      MSBG_LAUNCH(ctx, (kSplatBlock<32, 2>), (unsigned)(2 * nAct), splatThreads<32>(), smem, dPts, g, ctx->dActive, abortAt, off,
                   entries, init, dst);
     } else if (ctx->bsx == 16) {
-      MSBG_LAUNCH(ctx, (kSplatBlock<16, 1>), (unsigned)nAct, 256, (splatSmemWords<16, 1>() * 4), dPts, g, ctx->dActive,
+      MSBG_LAUNCH(ctx, (kSplatBlock<16, 1>), (unsigned)nAct, splatThreads<16>(), (splatSmemWords<16, 1>() * 4), dPts, g, ctx->dActive,
                   abortAt, off, entries, init, dst);
     } else {
-      MSBG_LAUNCH(ctx, (kSplatBlock<8, 1>), (unsigned)nAct, 128, (splatSmemWords<8, 1>() * 4), dPts, g, ctx->dActive,
+      MSBG_LAUNCH(ctx, (kSplatBlock<8, 1>), (unsigned)nAct, splatThreads<8>(), (splatSmemWords<8, 1>() * 4), dPts, g, ctx->dActive,
                   abortAt, off, entries, init, dst);
     }
     return MSBG_GPU_OK;
