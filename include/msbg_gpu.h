@@ -423,6 +423,18 @@ int msbg_gpu_restrict_level_blocks(msbg_gpu_ctx *ctx, int lchan, int level, cons
 int msbg_gpu_multiply_laplacian_levels(msbg_gpu_ctx *ctx, unsigned options, int level, int lchanX, int lchanB,
                                        int lchanD, const int32_t *dBids, int64_t n, float *dOut,
                                        double *pDotprod, int64_t *hSkipped);
+/* relaxBlockList(blocks, levelMg = 0, iIter, chanX, chanB, options, chanX) (src/msbg.h:3279-3285,
+ * src/msbg3.cpp:2170-2239) on a multi-resolution layout: one pass of the reference's block
+ * smoother over the listed blocks of any level, red-black over blocks ((bx+by+bz)&1 = 1
+ * first, 0 first with reverseOrder), each block relaxed in place in level `its level` of the
+ * X level channel from the operator's halo of msbg_gpu_multiply_laplacian_levels
+ * (mixed-resolution faces included) by _mgSmBlockIter block-local weighted Gauss-Seidel
+ * iterations with omega = _mgSmOmega (msbg_gpu_set_relax_params; 5 and 6/7 by default),
+ * as msbg_gpu_relax describes.  X (written: a bound payload receives the result), B and the
+ * diagonal channel are FP32 level channels.  Listed blocks without data at their level, or
+ * out of range, are skipped (counted in *hSkipped, which makes the call synchronize). */
+int msbg_gpu_relax_levels(msbg_gpu_ctx *ctx, int reverseOrder, int lchanX, int lchanB, int lchanD,
+                          const int32_t *dBids, int64_t n, int64_t *hSkipped);
 /* ---- ray-march render of the iso-0.5 surface -----------------------------------------
  * RDR::RaymarchRenderer (src/render.h:52-160): setCamera(pos, lookAt, zoom),
  * setSunLight(sun), setSurfaceColor(color), then render() (src/render.cpp:20-101), which the

@@ -730,6 +730,55 @@ __device__ __forceinline__ bool mrResolve(const MrGrid &g, int bid, int bsOfLeve
   return true;
 }
 
+// Face f (axis f/2, side f%2) of block bid at level a.level: where its neighbour's cells
+// come from.  Returns false when the neighbour has no data where it must be read (a level
+// not set, no block there, or a level map that is not regular).
+__device__ __forceinline__ bool mrFace(const MrArgs &a, int bid, int f, MrSrc &s) {
+  const int axis = f >> 1, side = f & 1;
+  int c[3] = {bid % a.nbx, (bid / a.nbx) % a.nby, bid / (a.nbx * a.nby)};
+  c[axis] += side ? 1 : -1;
+  const int nbd[3] = {a.nbx, a.nby, a.nbz};
+  s.kind = 3;
+  s.pay = nullptr;
+  s.cval = 0.0f;
+  if (c[axis] < 0 || c[axis] >= nbd[axis]) return true;
+  const int bid2 = c[0] + c[1] * a.nbx + c[2] * a.nbx * a.nby;
+  const int l2 = a.levels[bid2];
+  if (l2 == a.level) { s.kind = 0; return mrResolve(a.x[1], bid2, a.bs, s); }
+  if (l2 == a.level + 1) { s.kind = 1; return mrResolve(a.x[2], bid2, a.bs >> 1, s); }
+  if (l2 == a.level - 1) { s.kind = 2; return mrResolve(a.x[0], bid2, a.bs << 1, s); }
+  return false;
+}
+
+// Halo value of face f at in-plane coordinates (u, v) (x faces (y, z), y faces (x, z),
+// z faces (x, y)) of a block of edge bs = 2^lb at spacing h.
+__device__ __forceinline__ float mrHalo(const MrSrc &s, int f, int u, int v, int bs, int lb, float h) {
+  const int axis = f >> 1, side = f & 1;
+  if (s.kind == 3) return 0.0f;
+  if (s.kind == 0) {
+    const int k = side ? 0 : bs - 1;
+    const int idx = axis == 0 ? k + (u << lb) + (v << 2 * lb)
+                  : axis == 1 ? u + (k << lb) + (v << 2 * lb) : u + (v << lb) + (k << 2 * lb);
+    return __fmul_rn(s.pay ? s.pay[idx] : s.cval, h);
+  }
+  if (s.kind == 1) {
+    const int b2 = bs >> 1, l2 = lb - 1, k = side ? 0 : b2 - 1, cu = u >> 1, cv = v >> 1;
+    const int idx = axis == 0 ? k + (cu << l2) + (cv << 2 * l2)
+                  : axis == 1 ? cu + (k << l2) + (cv << 2 * l2) : cu + (cv << l2) + (k << 2 * l2);
+    return __fmul_rn(__fmul_rn(kCoeffFC, s.pay ? s.pay[idx] : s.cval), h);
+  }
+  const int b2 = bs << 1, l2 = lb + 1, k = side ? 0 : b2 - 1;
+  double sum = 0.0;
+#pragma unroll
+  for (int q = 0; q < 4; q++) {  // (du, dv) = (0,0), (1,0), (0,1), (1,1)
+    const int fu = 2 * u + (q & 1), fv = 2 * v + (q >> 1);
+    const int idx = axis == 0 ? k + (fu << l2) + (fv << 2 * l2)
+                  : axis == 1 ? fu + (k << l2) + (fv << 2 * l2) : fu + (fv << l2) + (k << 2 * l2);
+    sum += (double)__fmul_rn(kCoeffCF, s.pay ? s.pay[idx] : s.cval);
+  }
+  return __double2float_rn(sum * (double)h);
+}
+
 __global__ void __launch_bounds__(kMrThreads) kApplyMultires(MrArgs a) {
   __shared__ MrSrc face[6], own, dg, bb;
   __shared__ int bad;
@@ -741,25 +790,9 @@ __global__ void __launch_bounds__(kMrThreads) kApplyMultires(MrArgs a) {
   }
   __syncthreads();
   if (threadIdx.x < 6 && !bad) {
-    const int f = threadIdx.x, axis = f >> 1, side = f & 1;
-    int c[3] = {bid % a.nbx, (bid / a.nbx) % a.nby, bid / (a.nbx * a.nby)};
-    c[axis] += side ? 1 : -1;
-    const int nbd[3] = {a.nbx, a.nby, a.nbz};
     MrSrc s;
-    s.kind = 3;
-    s.pay = nullptr;
-    s.cval = 0.0f;
-    if (c[axis] >= 0 && c[axis] < nbd[axis]) {
-      const int bid2 = c[0] + c[1] * a.nbx + c[2] * a.nbx * a.nby;
-      const int l2 = a.levels[bid2];
-      bool ok = true;
-      if (l2 == a.level) { s.kind = 0; ok = mrResolve(a.x[1], bid2, bs, s); }
-      else if (l2 == a.level + 1) { s.kind = 1; ok = mrResolve(a.x[2], bid2, bs >> 1, s); }
-      else if (l2 == a.level - 1) { s.kind = 2; ok = mrResolve(a.x[0], bid2, bs << 1, s); }
-      else ok = false;  // the level map is not regular
-      if (!ok) atomicOr(&bad, 1);
-    }
-    face[f] = s;
+    if (!mrFace(a, bid, threadIdx.x, s)) atomicOr(&bad, 1);
+    face[threadIdx.x] = s;
   }
   __syncthreads();
   if (bad) {
@@ -767,35 +800,7 @@ __global__ void __launch_bounds__(kMrThreads) kApplyMultires(MrArgs a) {
     return;
   }
   const float h = a.h;
-  // halo value of face f at in-plane coordinates (u, v): x faces (y, z), y faces (x, z),
-  // z faces (x, y)
-  auto halo = [&](int f, int u, int v) -> float {
-    const MrSrc &s = face[f];
-    const int axis = f >> 1, side = f & 1;
-    if (s.kind == 3) return 0.0f;
-    if (s.kind == 0) {
-      const int k = side ? 0 : bs - 1;
-      const int idx = axis == 0 ? k + (u << lb) + (v << 2 * lb)
-                    : axis == 1 ? u + (k << lb) + (v << 2 * lb) : u + (v << lb) + (k << 2 * lb);
-      return __fmul_rn(s.pay ? s.pay[idx] : s.cval, h);
-    }
-    if (s.kind == 1) {
-      const int b2 = bs >> 1, l2 = lb - 1, k = side ? 0 : b2 - 1, cu = u >> 1, cv = v >> 1;
-      const int idx = axis == 0 ? k + (cu << l2) + (cv << 2 * l2)
-                    : axis == 1 ? cu + (k << l2) + (cv << 2 * l2) : cu + (cv << l2) + (k << 2 * l2);
-      return __fmul_rn(__fmul_rn(kCoeffFC, s.pay ? s.pay[idx] : s.cval), h);
-    }
-    const int b2 = bs << 1, l2 = lb + 1, k = side ? 0 : b2 - 1;
-    double sum = 0.0;
-#pragma unroll
-    for (int q = 0; q < 4; q++) {  // (du, dv) = (0,0), (1,0), (0,1), (1,1)
-      const int fu = 2 * u + (q & 1), fv = 2 * v + (q >> 1);
-      const int idx = axis == 0 ? k + (fu << l2) + (fv << 2 * l2)
-                    : axis == 1 ? fu + (k << l2) + (fv << 2 * l2) : fu + (fv << l2) + (k << 2 * l2);
-      sum += (double)__fmul_rn(kCoeffCF, s.pay ? s.pay[idx] : s.cval);
-    }
-    return __double2float_rn(sum * (double)h);
-  };
+  auto halo = [&](int f, int u, int v) -> float { return mrHalo(face[f], f, u, v, bs, lb, h); };
   const float *X = own.pay;
   const int n = 1 << 3 * lb, m = bs - 1;
   float *out = a.out + (int64_t)blockIdx.x * n;
@@ -941,4 +946,190 @@ extern "C" int msbg_gpu_multiply_laplacian_levels(msbg_gpu_ctx *ctx, unsigned op
     if (hSkipped) *hSkipped = (int64_t)sk;
   }
   return rc;
+}
+
+// ---- the reference's block smoother on a multi-resolution layout ---------------------
+//
+// relaxBlockList (src/msbg3.cpp:2170-2239) with IprocessBlockLaplacian's RELAX mode
+// (src/msbg3.cpp:1108-1398): one launch per layout level and block parity; a CTA takes a
+// listed block of that level and parity, stages it and its halo (the operator's, above) in
+// shared memory as h X, and runs blockIter block-local iterations in place: groups of the
+// reference's SIMD width (8 cells along x, or the block edge below 8) in z, y, x order,
+// backward on alternate iterations, as wavefronts of groups that share no face; the last
+// iteration, from the buffer, writes X = Y / h.  Per cell Y = omega (B + S) D +
+// (1 - omega) F0 in the order the reference's compiled code evaluates it (its 4- and 8-wide
+// paths: S = (F1+F2) + (F3+F4) + (F5+F6), Y = fma(1 - omega, F0, (omega D)(S + B); its
+// 2-wide path: source order).
+namespace msbg {
+namespace {
+
+template <int BS> constexpr int log2Edge() { return BS == 32 ? 5 : BS == 16 ? 4 : BS == 8 ? 3 : BS == 4 ? 2 : 1; }
+
+template <int BS>
+__global__ void __launch_bounds__(kMrThreads) kRelaxMultires(MrArgs a, int parity, float omega, int blockIter,
+                                                             int reverse, int countOutOfRange) {
+  constexpr int HS = BS + 2, HS2 = HS * HS, VPB = BS * BS * BS, LB = log2Edge<BS>();
+  constexpr int GW = BS >= 8 ? 8 : BS, G = BS / GW, T = G + 2 * BS - 2;
+  extern __shared__ float hb[];
+  __shared__ MrSrc face[6], own, dg, bb;
+  __shared__ int state;  // 0 relax, 1 another launch's block, 2 skipped
+  const int bid = a.bids[blockIdx.x];
+  if (threadIdx.x == 0) {
+    int st = 0;
+    if (bid < 0 || bid >= a.nBlocks) {
+      st = countOutOfRange ? 2 : 1;
+    } else {
+      const int par = (bid % a.nbx + (bid / a.nbx) % a.nby + bid / (a.nbx * a.nby)) & 1;
+      if (par != parity || a.levels[bid] != a.level) st = 1;
+      else if (!mrResolve(a.x[1], bid, BS, own) || !own.pay || !mrResolve(a.d, bid, BS, dg) ||
+               !mrResolve(a.b, bid, BS, bb))
+        st = 2;
+    }
+    state = st;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6 && state == 0) {
+    MrSrc s;
+    if (!mrFace(a, bid, threadIdx.x, s)) atomicMax(&state, 2);
+    face[threadIdx.x] = s;
+  }
+  __syncthreads();
+  if (state) {
+    if (state == 2 && threadIdx.x == 0) atomicAdd(a.skipped, 1ull);
+    return;
+  }
+  const float h = a.h;
+  float *X = const_cast<float *>(own.pay);  // relaxed in place: no other CTA of this launch reads it
+  for (int v = threadIdx.x; v < VPB; v += kMrThreads) {
+    const int i = v & (BS - 1), j = (v >> LB) & (BS - 1), k = v >> 2 * LB;
+    hb[(k + 1) * HS2 + (j + 1) * HS + i + 1] = __fmul_rn(X[v], h);
+  }
+  for (int v = threadIdx.x; v < 6 * BS * BS; v += kMrThreads) {
+    const int f = v / (BS * BS), p = v % (BS * BS), u = p & (BS - 1), w = p >> LB;
+    const int axis = f >> 1, side = f & 1, e = side ? BS + 1 : 0;
+    const int idx = axis == 0 ? (w + 1) * HS2 + (u + 1) * HS + e
+                  : axis == 1 ? (w + 1) * HS2 + e * HS + u + 1 : e * HS2 + (w + 1) * HS + u + 1;
+    hb[idx] = mrHalo(face[f], f, u, w, BS, LB, h);
+  }
+  __syncthreads();
+  const float om1 = __fsub_rn(1.0f, omega);
+  auto group = [&](int gi, int j, int k, float *y) {
+#pragma unroll
+    for (int l = 0; l < GW; l++) {
+      const int i = gi * GW + l, c = (k * BS + j) * BS + i;
+      const float *p = hb + (k + 1) * HS2 + (j + 1) * HS + i + 1;
+      const float F0 = p[0], F1 = p[-1], F2 = p[1], F3 = p[-HS], F4 = p[HS], F5 = p[-HS2], F6 = p[HS2];
+      const float B = bb.pay ? bb.pay[c] : bb.cval, D = dg.pay ? dg.pay[c] : dg.cval;
+      if constexpr (BS >= 4) {
+        const float t = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(F1, F2), __fadd_rn(F3, F4)), __fadd_rn(F5, F6)), B);
+        y[l] = __fmaf_rn(om1, F0, __fmul_rn(__fmul_rn(omega, D), t));
+      } else {
+        const float t = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(F1, F2), F3), F4), F5), F6), B);
+        y[l] = __fadd_rn(__fmul_rn(__fmul_rn(omega, t), D), __fmul_rn(om1, F0));
+      }
+    }
+  };
+  for (int it = 0; it < blockIter - 1; it++) {
+    const bool backward = (it & 1) == reverse;
+    for (int t = 0; t < T; t++) {
+      for (int q = threadIdx.x; q < BS * BS; q += kMrThreads) {
+        const int j0 = q % BS, k0 = q / BS, g0 = t - j0 - k0;
+        if (g0 < 0 || g0 >= G) continue;
+        const int gi = backward ? G - 1 - g0 : g0, j = backward ? BS - 1 - j0 : j0, k = backward ? BS - 1 - k0 : k0;
+        float y[GW];
+        group(gi, j, k, y);
+        float *o = hb + (k + 1) * HS2 + (j + 1) * HS + gi * GW + 1;
+#pragma unroll
+        for (int l = 0; l < GW; l++) o[l] = y[l];
+      }
+      __syncthreads();
+    }
+  }
+  if (blockIter >= 1) {  // the last iteration: every group from the buffer, into X
+    const float hr = a.hr;
+    for (int q = threadIdx.x; q < G * BS * BS; q += kMrThreads) {
+      const int gi = q % G, j = (q / G) % BS, k = q / (G * BS);
+      float y[GW];
+      group(gi, j, k, y);
+      float *o = X + (k * BS + j) * BS + gi * GW;
+#pragma unroll
+      for (int l = 0; l < GW; l++) o[l] = __fmul_rn(y[l], hr);
+    }
+  }
+}
+
+template <int BS>
+int launchRelaxMultires(msbg_gpu_ctx *ctx, const MrArgs &a, unsigned n, int parity, float omega, int blockIter,
+                        int reverse, int countOutOfRange) {
+  constexpr int smem = (BS + 2) * (BS + 2) * (BS + 2) * (int)sizeof(float);
+  static bool attr = false;
+  if (!attr) {
+    MSBG_CUDA(ctx, cudaFuncSetAttribute(kRelaxMultires<BS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    attr = true;
+  }
+  MSBG_LAUNCH(ctx, kRelaxMultires<BS>, n, kMrThreads, smem, a, parity, omega, blockIter, reverse, countOutOfRange);
+  return MSBG_GPU_OK;
+}
+
+}  // namespace
+}  // namespace msbg
+
+extern "C" int msbg_gpu_relax_levels(msbg_gpu_ctx *ctx, int reverseOrder, int lchanX, int lchanB, int lchanD,
+                                     const int32_t *dBids, int64_t n, int64_t *hSkipped) {
+  if (!ctx) return MSBG_GPU_ERR_ARG;
+  for (int lc : {lchanX, lchanB, lchanD})
+    if (lc < 0 || lc >= kMaxLevelChannels)
+      return fail(ctx, MSBG_GPU_ERR_ARG, "relax_levels: level channel %d out of range", lc);
+  if (n < 0 || n > 0x7fffffff || (n > 0 && !dBids)) return fail(ctx, MSBG_GPU_ERR_ARG, "relax_levels: bad block list");
+  if (!ctx->layoutValid) return fail(ctx, MSBG_GPU_ERR_STATE, "no block layout: call set_refinement_map");
+  if (ctx->bsx > 32) return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "relax_levels: block edge above 32");
+  LevelChannels *lc = levelChannels(ctx);
+  if (!lc->dSkip) MSBG_CUDA(ctx, cudaMalloc(&lc->dSkip, sizeof(unsigned long long)));
+  MSBG_CUDA(ctx, cudaMemsetAsync(lc->dSkip, 0, sizeof(unsigned long long), ctx->stream));
+  bool first = true;
+  for (int pass = 0; pass < 2 && n > 0; pass++) {
+    // blocks of parity (bx+by+bz)&1 = 1 first, 0 first in the reverse order
+    const int parity = (pass == 0) == !reverseOrder ? 1 : 0;
+    for (int level = 0; level < ctx->nLevels && level < kMaxGridLevels; level++) {
+      const int bs = ctx->bsx >> level;
+      if (bs < 2) break;
+      MrArgs a;
+      a.x[0] = mrGrid(lc, lchanX, level - 1, ctx->nLevels);
+      a.x[1] = mrGrid(lc, lchanX, level, ctx->nLevels);
+      a.x[2] = mrGrid(lc, lchanX, level + 1, ctx->nLevels);
+      a.d = mrGrid(lc, lchanD, level, ctx->nLevels);
+      a.b = mrGrid(lc, lchanB, level, ctx->nLevels);
+      a.bids = dBids;
+      a.levels = ctx->dLevels;
+      a.level = level;
+      a.bs = bs;
+      a.log2bs = ctx->log2bs - level;
+      a.nbx = ctx->nbx; a.nby = ctx->nby; a.nbz = ctx->nbz;
+      a.nBlocks = (int)ctx->nBlocks;
+      a.h = (float)(1 << level);
+      a.hr = 1.0f / a.h;
+      a.residual = 0;
+      a.out = nullptr;
+      a.dotPart = nullptr;
+      a.skipped = lc->dSkip;
+      const int cnt = first ? 1 : 0;
+      first = false;
+      int rc;
+      switch (bs) {
+        case 32: rc = launchRelaxMultires<32>(ctx, a, (unsigned)n, parity, ctx->relaxOmega, ctx->relaxBlockIter, reverseOrder ? 1 : 0, cnt); break;
+        case 16: rc = launchRelaxMultires<16>(ctx, a, (unsigned)n, parity, ctx->relaxOmega, ctx->relaxBlockIter, reverseOrder ? 1 : 0, cnt); break;
+        case 8: rc = launchRelaxMultires<8>(ctx, a, (unsigned)n, parity, ctx->relaxOmega, ctx->relaxBlockIter, reverseOrder ? 1 : 0, cnt); break;
+        case 4: rc = launchRelaxMultires<4>(ctx, a, (unsigned)n, parity, ctx->relaxOmega, ctx->relaxBlockIter, reverseOrder ? 1 : 0, cnt); break;
+        default: rc = launchRelaxMultires<2>(ctx, a, (unsigned)n, parity, ctx->relaxOmega, ctx->relaxBlockIter, reverseOrder ? 1 : 0, cnt); break;
+      }
+      if (rc) return rc;
+    }
+  }
+  if (hSkipped) {
+    unsigned long long sk = 0;
+    MSBG_CUDA(ctx, cudaMemcpyAsync(&sk, lc->dSkip, sizeof(sk), cudaMemcpyDeviceToHost, ctx->stream));
+    MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *hSkipped = (int64_t)sk;
+  }
+  return MSBG_GPU_OK;
 }

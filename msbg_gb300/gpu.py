@@ -115,6 +115,7 @@ SIGNATURES = {
     "msbg_gpu_fill_halo_blocks": (I, [P, I, I, P, I64, I, I, P, C.POINTER(I64)]),
     "msbg_gpu_restrict_level_blocks": (I, [P, I, I, P, I64, I, P, C.POINTER(I64)]),
     "msbg_gpu_multiply_laplacian_levels": (I, [P, C.c_uint, I, I, I, I, P, I64, P, C.POINTER(D), C.POINTER(I64)]),
+    "msbg_gpu_relax_levels": (I, [P, I, I, I, I, P, I64, C.POINTER(I64)]),
     "msbg_gpu_level_flags_set": (I, [P, I, I, P, P, I64, C.c_uint16, C.c_uint16]),
     "msbg_gpu_fill_halo_blocks3": (I, [P, I, I, I, P, I64, P, P, C.POINTER(I64)]),
     "msbg_gpu_diag_wait_timeout": (I, [P, I]),
@@ -765,6 +766,21 @@ class MultiresSparseGrid:
             db.free()
             do.free()
         return out, (None if residual else dot.value), int(sk.value)
+
+    # reference: relaxBlockList (src/msbg3.cpp:2170-2239) on a multi-resolution layout
+    def relax_levels(self, lchan_x: int, lchan_b: int, lchan_d: int, bids: np.ndarray, reverse: bool = False) -> int:
+        """One pass of the block smoother over the listed blocks (any level), X relaxed in place
+        in its level channel; returns the number of skipped blocks."""
+        bids = np.ascontiguousarray(bids, np.int32)
+        db = self.to_device(bids)
+        sk = C.c_int64(-1)
+        try:
+            self._check(self.L.msbg_gpu_relax_levels(self.h, int(reverse), lchan_x, lchan_b, lchan_d,
+                                                     C.c_void_p(db.ptr), len(bids), C.byref(sk)))
+            self.synchronize()
+        finally:
+            db.free()
+        return int(sk.value)
 
     # reference: dotProdChannel(ch1, ch2, levelMg, blockList, pErrCode) (src/msbg.h:3331-3341);
     # a non-finite sum raises MsbgGpuError with ERR_NONFINITE (the reference's pErrCode)

@@ -469,14 +469,16 @@ def run_reference_layout(sx, sy, sz, bsx, n_levels, levels, timeout: float = 600
 JOB_MULTIRES = 11
 
 
-def run_reference_multires(sx, sy, sz, bsx, n_levels, levels, x, b, dinv, timeout: float = 600) -> dict:
+def run_reference_multires(sx, sy, sz, bsx, n_levels, levels, x, b, dinv, relax_passes: int = 0,
+                           reverse: bool = False, timeout: float = 600) -> dict:
     """multiplyLaplacianMatrixOpt (src/msbg3.cpp:1756-1912) by the reference itself on a
     multi-resolution layout: every block of the (regular) level map `levels` is a fluid block
     at its level, with unit face areas and fluid cells, so neighbouring levels meet through
     procNeighMixedRes2 (src/msbg3.cpp:46-161).  x, b, dinv: float32 over the blocks of level 0,
     then level 1, ..., ascending bid, (bsx>>l)^3 values per block of level l; dinv is what
     CH_DIAGONAL holds (the operator multiplies by 1/dinv).  Returns {"dot": sum(Y X),
-    "y": A X, "r": B - A X} in the same order."""
+    "y": A X, "r": B - A X} in the same order, and with relax_passes > 0 "relaxed": X after
+    that many passes of relaxBlockList (src/msbg3.cpp:2170-2239) from x."""
     lv = np.ascontiguousarray(levels, np.int32).ravel()
     arrs = [np.ascontiguousarray(v, np.float32).ravel() for v in (x, b, dinv)]
     total = sum(int((lv == l).sum()) * (bsx >> l) ** 3 for l in range(n_levels))
@@ -484,8 +486,8 @@ def run_reference_multires(sx, sy, sz, bsx, n_levels, levels, x, b, dinv, timeou
         raise ValueError("array sizes do not match the level map")
     with tempfile.TemporaryDirectory() as td:
         jp, op = os.path.join(td, "job.bin"), os.path.join(td, "out.bin")
-        hdr = struct.pack(_JOB_FMT, JOB_MAGIC, JOB_MULTIRES, sx, sy, sz, bsx, n_levels, CHAN_F32, 0, 0, 0, 1,
-                          0.0, 0.0, 0.0, 0.0, 0, 0, lv.size)
+        hdr = struct.pack(_JOB_FMT, JOB_MAGIC, JOB_MULTIRES, sx, sy, sz, bsx, n_levels, CHAN_F32, relax_passes, 0,
+                          int(reverse), 1, 0.0, 0.0, 0.0, 0.0, 0, 0, lv.size)
         with open(jp, "wb") as f:
             f.write(hdr)
             f.write(lv.tobytes())
@@ -503,4 +505,7 @@ def run_reference_multires(sx, sy, sz, bsx, n_levels, levels, x, b, dinv, timeou
     dot = float(np.frombuffer(buf, np.float64, 1, hsz)[0])
     y = np.frombuffer(buf, np.float32, total, hsz + 8).copy()
     res = np.frombuffer(buf, np.float32, total, hsz + 8 + 4 * total).copy()
-    return {"dot": dot, "y": y, "r": res}
+    out = {"dot": dot, "y": y, "r": res}
+    if relax_passes > 0:
+        out["relaxed"] = np.frombuffer(buf, np.float32, total, hsz + 8 + 8 * total).copy()
+    return out

@@ -530,6 +530,73 @@ MR_COEFF_CF = np.float32(1.0 / (4 * 0.75))
 MR_COEFF_FC = np.float32(1.0 * 2 * (1.0 / (4 * 0.75)))
 
 
+class _MultiresLayout:
+    """Blocks of a multi-resolution layout over flat float32 arrays ordered by level, then
+    ascending bid ((bsx>>l)^3 values [z][y][x] per block of level l), and the halo of a block
+    as the reference's operator and smoother read it (IprocessBlockLaplacian,
+    src/msbg3.cpp:563-1042): h X inside, h X of a same-level face neighbour, procNeighMixedRes2's
+    weighted values across a face to another level (src/msbg3.cpp:46-161), zero outside."""
+
+    def __init__(self, sx, sy, sz, bsx, n_levels, levels, x):
+        self.bsx, self.lv = bsx, np.asarray(levels).ravel()
+        self.nbx, self.nby, self.nbz = sx // bsx, sy // bsx, sz // bsx
+        self.blocks, self.order, off = {}, [], 0
+        for l in range(n_levels):
+            bs = bsx >> l
+            for bid in np.flatnonzero(self.lv == l):
+                n = bs ** 3
+                self.blocks[int(bid)] = (l, off, x[off:off + n].reshape(bs, bs, bs))
+                self.order.append(int(bid))
+                off += n
+        if off != x.size:
+            raise ValueError("array sizes do not match the level map")
+
+    def face(self, bid, l, axis, side):
+        """Halo plane of block bid (level l) on face (axis 0 x / 1 y / 2 z, side 0 low /
+        1 high), as [z][y] (x faces), [z][x] (y faces) or [y][x] (z faces), scaled by h."""
+        f32, f64 = np.float32, np.float64
+        bs, h = self.bsx >> l, f32(2 ** l)
+        nbx, nby, nbz = self.nbx, self.nby, self.nbz
+        bxyz = [bid % nbx, (bid // nbx) % nby, bid // (nbx * nby)]
+        bxyz[axis] += 1 if side else -1
+        if not (0 <= bxyz[0] < nbx and 0 <= bxyz[1] < nby and 0 <= bxyz[2] < nbz):
+            return np.zeros((bs, bs), f32)
+        l2, _, X2 = self.blocks[bxyz[0] + bxyz[1] * nbx + bxyz[2] * nbx * nby]
+        k = (self.bsx >> l2) - 1 if side == 0 else 0  # the neighbour's plane that touches the face
+        plane = (X2[:, :, k], X2[:, k, :], X2[k, :, :])[axis]
+        if l2 == l:
+            return plane * h
+        if l2 == l + 1:  # coarser neighbour: each coarse cell serves 2x2 fine cells
+            v = (MR_COEFF_FC * plane) * h
+            return np.repeat(np.repeat(v, 2, axis=0), 2, axis=1)
+        if l2 == l - 1:  # finer neighbour: four fine cells per coarse cell, FP64 sum
+            p = (MR_COEFF_CF * plane).astype(f64)
+            # plane axes (outer, inner): x faces (z, y), y faces (z, x), z faces (y, x);
+            # the reference adds (inner, outer) offsets (0,0), (1,0), (0,1), (1,1)
+            s = p[0::2, 0::2] + p[0::2, 1::2]
+            s = s + p[1::2, 0::2]
+            s = s + p[1::2, 1::2]
+            return (s * f64(h)).astype(f32)
+        raise ValueError("level map is not regular")
+
+    def halo(self, bid):
+        """(level, offset, h X of the block with its six face layers, (bs+2)^3 float32)."""
+        l, o, X = self.blocks[bid]
+        bs = self.bsx >> l
+        P = np.zeros((bs + 2,) * 3, np.float32)
+        P[1:-1, 1:-1, 1:-1] = X * np.float32(2 ** l)
+        P[1:-1, 1:-1, 0], P[1:-1, 1:-1, -1] = self.face(bid, l, 0, 0), self.face(bid, l, 0, 1)
+        P[1:-1, 0, 1:-1], P[1:-1, -1, 1:-1] = self.face(bid, l, 1, 0), self.face(bid, l, 1, 1)
+        P[0, 1:-1, 1:-1], P[-1, 1:-1, 1:-1] = self.face(bid, l, 2, 0), self.face(bid, l, 2, 1)
+        return l, o, P
+
+
+def _six(P):
+    """The six neighbours F1..F6 (x-1, x+1, y-1, y+1, z-1, z+1) of every interior cell of P."""
+    return (P[1:-1, 1:-1, :-2], P[1:-1, 1:-1, 2:], P[1:-1, :-2, 1:-1], P[1:-1, 2:, 1:-1],
+            P[:-2, 1:-1, 1:-1], P[2:, 1:-1, 1:-1])
+
+
 def multiply_laplacian_levels(sx, sy, sz, bsx, n_levels, levels, x, b, dinv):
     """multiplyLaplacianMatrixOpt (src/msbg3.cpp:1756-1912, IprocessBlockLaplacian
     src/msbg3.cpp:418-1335) on a multi-resolution layout, every block a fluid block at its
@@ -551,62 +618,16 @@ def multiply_laplacian_levels(sx, sy, sz, bsx, n_levels, levels, x, b, dinv):
     the same (the product of two FP32 values is exact in FP64) and matches it bit for bit.
     Returns (dot, y, r) in x's order."""
     f32, f64 = np.float32, np.float64
-    lv = np.asarray(levels).ravel()
-    nbx, nby, nbz = sx // bsx, sy // bsx, sz // bsx
     x, b, dinv = (np.asarray(a, f32).ravel() for a in (x, b, dinv))
-    blocks, order, off = {}, [], 0
-    for l in range(n_levels):
-        bs = bsx >> l
-        for bid in np.flatnonzero(lv == l):
-            n = bs ** 3
-            blocks[int(bid)] = (l, off, x[off:off + n].reshape(bs, bs, bs))
-            order.append(int(bid))
-            off += n
-    if off != x.size:
-        raise ValueError("array sizes do not match the level map")
+    L = _MultiresLayout(sx, sy, sz, bsx, n_levels, levels, x)
     y, r = np.empty_like(x), np.empty_like(x)
     dot = 0.0
-
-    def face(bid, l, axis, side):
-        """Halo plane of block bid (level l) on face (axis 0 x / 1 y / 2 z, side 0 low /
-        1 high), as [z][y] (x faces), [z][x] (y faces) or [y][x] (z faces), scaled by h."""
-        bs, h = bsx >> l, f32(2 ** l)
-        bxyz = [bid % nbx, (bid // nbx) % nby, bid // (nbx * nby)]
-        bxyz[axis] += 1 if side else -1
-        if not (0 <= bxyz[0] < nbx and 0 <= bxyz[1] < nby and 0 <= bxyz[2] < nbz):
-            return np.zeros((bs, bs), f32)
-        bid2 = bxyz[0] + bxyz[1] * nbx + bxyz[2] * nbx * nby
-        l2, _, X2 = blocks[bid2]
-        bs2 = bsx >> l2
-        k = bs2 - 1 if side == 0 else 0  # the neighbour's plane that touches the face
-        plane = (X2[:, :, k], X2[:, k, :], X2[k, :, :])[axis]
-        if l2 == l:
-            return plane * h
-        if l2 == l + 1:  # coarser neighbour: each coarse cell serves 2x2 fine cells
-            v = (MR_COEFF_FC * plane) * h
-            return np.repeat(np.repeat(v, 2, axis=0), 2, axis=1)
-        if l2 == l - 1:  # finer neighbour: four fine cells per coarse cell, FP64 sum
-            p = (MR_COEFF_CF * plane).astype(f64)
-            # plane axes (outer, inner): x faces (z, y), y faces (z, x), z faces (y, x);
-            # the reference adds (inner, outer) offsets (0,0), (1,0), (0,1), (1,1)
-            s = p[0::2, 0::2] + p[0::2, 1::2]
-            s = s + p[1::2, 0::2]
-            s = s + p[1::2, 1::2]
-            return (s * f64(h)).astype(f32)
-        raise ValueError("level map is not regular")
-
-    for bid in order:
-        l, o, X = blocks[bid]
+    for bid in L.order:
+        l, o, P = L.halo(bid)
         bs, h = bsx >> l, f32(2 ** l)
         n = bs ** 3
-        P = np.zeros((bs + 2,) * 3, f32)
-        F0 = X * h
-        P[1:-1, 1:-1, 1:-1] = F0
-        P[1:-1, 1:-1, 0], P[1:-1, 1:-1, -1] = face(bid, l, 0, 0), face(bid, l, 0, 1)
-        P[1:-1, 0, 1:-1], P[1:-1, -1, 1:-1] = face(bid, l, 1, 0), face(bid, l, 1, 1)
-        P[0, 1:-1, 1:-1], P[-1, 1:-1, 1:-1] = face(bid, l, 2, 0), face(bid, l, 2, 1)
-        F = (P[1:-1, 1:-1, :-2], P[1:-1, 1:-1, 2:], P[1:-1, :-2, 1:-1], P[1:-1, 2:, 1:-1],
-             P[:-2, 1:-1, 1:-1], P[2:, 1:-1, 1:-1])
+        F0 = P[1:-1, 1:-1, 1:-1]
+        F = _six(P)
         if bs >= 4:
             S = ((F[0] + F[1]) + (F[2] + F[3])) + (F[4] + F[5])
         else:
@@ -622,3 +643,69 @@ def multiply_laplacian_levels(sx, sy, sz, bsx, n_levels, levels, x, b, dinv):
         r[o:o + n] = (b[o:o + n] - Y.ravel()).astype(f32)
         dot += float((Y.astype(f64) * (F0 * f32(1.0 / h)).astype(f64)).sum())
     return dot, y, r
+
+
+def relax_levels(sx, sy, sz, bsx, n_levels, levels, x, b, dinv, passes=1, reverse=False,
+                 block_iter=REF_SM_BLOCK_ITER, omega=REF_SM_OMEGA):
+    """relaxBlockList (src/msbg3.cpp:2170-2239), `passes` times, on a multi-resolution layout
+    laid out as for multiply_laplacian_levels: red-black over the blocks of every level (parity
+    (bx+by+bz)&1 = 1 first, 0 first with reverse), each block relaxed in place from its halo
+    (the operator's, read once at its start) by block_iter block-local iterations
+    (IprocessBlockLaplacian's RELAX mode, src/msbg3.cpp:1108-1398): groups of the reference's
+    SIMD width (8 cells along x, or the block edge below 8) in z, y, x order, backward on
+    alternate iterations (the other way with reverse), each group computed from the buffer
+    before it is stored; the last iteration, computed from the buffer without storing
+    into it, gives X = Y / h.  Per cell Y = omega (B + S) D + (1 - omega) F0 with S = F1 + ...
+    + F6 and D what CH_DIAGONAL holds.  The reference's build evaluates it in its 4- and 8-wide
+    paths (block edge >= 4) as S = (F1+F2) + (F3+F4) + (F5+F6), t = S + B,
+    Y = fma(1 - omega, F0, (omega D) t), and in its 2-wide path in source order; this
+    restatement does the same and matches it bit for bit.  Returns the relaxed x."""
+    f32, f64 = np.float32, np.float64
+    x = np.asarray(x, f32).ravel().copy()
+    b, dinv = (np.asarray(a, f32).ravel() for a in (b, dinv))
+    L = _MultiresLayout(sx, sy, sz, bsx, n_levels, levels, x)
+    om = f32(omega)
+    om1 = f32(1.0) - om
+    parities = (0, 1) if reverse else (1, 0)
+    for _ in range(passes):
+        for par in parities:
+            for bid in L.order:
+                if (bid % L.nbx + (bid // L.nbx) % L.nby + bid // (L.nbx * L.nby)) & 1 != par:
+                    continue
+                l, o, Pb = L.halo(bid)
+                bs, h = bsx >> l, f32(2 ** l)
+                n = bs ** 3
+                B = b[o:o + n].reshape(bs, bs, bs)
+                D = dinv[o:o + n].reshape(bs, bs, bs)
+                gw = 8 if bs >= 8 else bs
+                ng = bs // gw
+
+                def update(k, j, i):
+                    F0 = Pb[k + 1, j + 1, i + 1]
+                    F = (Pb[k + 1, j + 1, i], Pb[k + 1, j + 1, i + 2], Pb[k + 1, j, i + 1], Pb[k + 1, j + 2, i + 1],
+                         Pb[k, j + 1, i + 1], Pb[k + 2, j + 1, i + 1])
+                    Bc, Dc = B[k, j, i], D[k, j, i]
+                    if bs >= 4:
+                        t = (((F[0] + F[1]) + (F[2] + F[3])) + (F[4] + F[5])) + Bc
+                        return (om1.astype(f64) * F0.astype(f64) + ((om * Dc) * t).astype(f64)).astype(f32)
+                    t = (((((F[0] + F[1]) + F[2]) + F[3]) + F[4]) + F[5]) + Bc
+                    return ((om * t) * Dc + om1 * F0).astype(f32)
+
+                gi, jj, kk = np.meshgrid(np.arange(ng), np.arange(bs), np.arange(bs), indexing="ij")
+                wave = gi + jj + kk  # groups on one wavefront share no face: updated together
+                for it in range(block_iter):
+                    if it < block_iter - 1:
+                        backward = bool(reverse) == bool(it & 1)
+                        for t in range(ng + 2 * bs - 2):
+                            m = wave == t
+                            g0, j0, k0 = gi[m], jj[m], kk[m]
+                            if backward:
+                                g0, j0, k0 = ng - 1 - g0, bs - 1 - j0, bs - 1 - k0
+                            ci = (g0[:, None] * gw + np.arange(gw)[None, :]).ravel()
+                            cj, ck = np.repeat(j0, gw), np.repeat(k0, gw)
+                            Pb[ck + 1, cj + 1, ci + 1] = update(ck, cj, ci)
+                    else:
+                        ck, cj, ci = (a.ravel() for a in np.meshgrid(np.arange(bs), np.arange(bs), np.arange(bs),
+                                                                     indexing="ij"))
+                        L.blocks[bid][2][...] = (update(ck, cj, ci) * f32(1.0 / h)).reshape(bs, bs, bs)
+    return x

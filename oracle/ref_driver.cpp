@@ -674,7 +674,10 @@ int runSolverJob(const OracleJobHeader &job, const int32_t *bidsIn, const float 
 // every cell is fluid (cell flags 0).  Inputs after the levels: float32 X, B and DINV (what
 // CH_DIAGONAL holds; the operator multiplies by 1/DINV), each over the blocks of level 0,
 // then level 1, ..., in ascending bid order, (bsx>>l)^3 values per block of level l.
-// Output: sum(Y X) (FP64), then Y = A X and R = B - A X in the same order.
+// Output: sum(Y X) (FP64), then Y = A X and R = B - A X in the same order.  With
+// job.nIter > 0, X is loaded again and relaxed by job.nIter passes of relaxBlockList
+// (src/msbg3.cpp:2170-2239, red-black over the blocks of every level, constr01 = 1 for the
+// reverse order), and the relaxed X follows in the same order.
 int runMultiresJob(const OracleJobHeader &job, const int32_t *levelsIn, const float *arrays, FILE *fout) {
   OracleOutHeader out;
   memset(&out, 0, sizeof(out));
@@ -751,6 +754,31 @@ int runMultiresJob(const OracleJobHeader &job, const int32_t *levelsIn, const fl
   msbg->multiplyLaplacianMatrixOpt(MSBG::OPT_CALC_RESIDUAL, 0, CH_PRESSURE, CH_DIVERGENCE, 0.f, CH_CG_Q, NULL,
                                    &list);
   dumpQ(R);
+  std::vector<float> Xr;
+  if (job.nIter > 0) {
+    size_t o = 0;
+    for (int l = 0; l < job.nLevels; l++) {
+      SparseGrid<PSFloat> *sgX = msbg->getPSFloatChannel(CH_PRESSURE, l, 0);
+      const size_t nv = (size_t)sgX->nVoxelsInBlock();
+      for (int32_t b : bidsL[l]) {
+        memcpy(sgX->getBlockDataPtr(b, 0, 0), X + o, nv * 4);
+        o += nv;
+      }
+    }
+    const unsigned ropt = MSBG::OPT_JACOBI | (job.constr01 ? MSBG::OPT_REVERSE_ORDER : 0);
+    for (int it = 0; it < job.nIter; it++)
+      msbg->relaxBlockList(&list, 0, it, CH_PRESSURE, CH_DIVERGENCE, ropt, CH_PRESSURE);
+    Xr.resize(total);
+    o = 0;
+    for (int l = 0; l < job.nLevels; l++) {
+      SparseGrid<PSFloat> *sgX = msbg->getPSFloatChannel(CH_PRESSURE, l, 0);
+      const size_t nv = (size_t)sgX->nVoxelsInBlock();
+      for (int32_t b : bidsL[l]) {
+        memcpy(&Xr[o], sgX->getBlockDataPtr(b, 0, 0), nv * 4);
+        o += nv;
+      }
+    }
+  }
   out.tPdeSec = nowSec() - t0;
   out.nBlocks = nBlocks;
   out.nActive = nBlocks;
@@ -762,6 +790,7 @@ int runMultiresJob(const OracleJobHeader &job, const int32_t *levelsIn, const fl
   fwrite(&dot, 8, 1, fout);
   fwrite(Y.data(), 4, total, fout);
   fwrite(R.data(), 4, total, fout);
+  if (!Xr.empty()) fwrite(Xr.data(), 4, total, fout);
   MultiresSparseGrid::destroy(msbg);
   return 0;
 }

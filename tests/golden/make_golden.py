@@ -309,9 +309,10 @@ SURFACE512_SAMPLE = 60000
 
 
 def make_multires() -> None:
-    """multiplyLaplacianMatrixOpt on multi-resolution layouts (oracle/ref_driver.cpp, multires
-    job): Y = A X with sum(Y X) and B - A X for the seeded cases of tests/halo_cases.py, whose
-    neighbouring levels meet through procNeighMixedRes2."""
+    """multiplyLaplacianMatrixOpt and relaxBlockList on multi-resolution layouts
+    (oracle/ref_driver.cpp, multires job): Y = A X with sum(Y X), B - A X and the relaxed X
+    for the seeded cases of tests/halo_cases.py, whose neighbouring levels meet through
+    procNeighMixedRes2."""
     import halo_cases as H
     import port as P
     out = {}
@@ -323,6 +324,10 @@ def make_multires() -> None:
         out[f"{key}_y"] = r["y"]
         out[f"{key}_r"] = r["r"]
         out[f"{key}_dot"] = np.float64(r["dot"])
+        for passes, rev in H.MULTIRES_RELAX_RUNS:
+            rr = O.run_reference_multires(*(n * bsx for n in nb), bsx, 3, lv, x, b, dinv, relax_passes=passes,
+                                          reverse=rev)
+            out[f"{key}_relaxed_{passes}_{int(rev)}"] = rr["relaxed"]
     path = os.path.join(HERE, "reference_multires.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")

@@ -94,6 +94,8 @@ def flags_case(states, bsx: int, seed: int):
 # edges 16, 8, 4 and 2 (an edge-32 layout stops it with an assertion).
 MULTIRES_CASES = (((4, 4, 4), 16, 20261203 + 990), ((5, 3, 4), 8, 20261203 + 991),
                   ((6, 5, 4), 16, 20261203 + 992))
+# relaxBlockList runs on them: (passes, reverse order)
+MULTIRES_RELAX_RUNS = ((1, False), (2, True))
 
 
 def multires_case(nb, bsx: int, n_levels: int, seed: int, regularize):

@@ -263,3 +263,46 @@ def test_multires_operator_matches_reference(gpulib, port, case):
         assert e.value.code == G.ERR_STATE
     finally:
         g.close()
+
+
+@pytest.mark.parametrize("case", H.MULTIRES_CASES, ids=["x".join(map(str, c[0])) + f"_bs{c[1]}" for c in H.MULTIRES_CASES])
+def test_multires_block_smoother_matches_reference(gpulib, port, case):
+    """msbg_gpu_relax_levels against relaxBlockList run by the reference: bit for bit, X relaxed
+    in place in device arrays bound as level channel 3."""
+    G = gpulib
+    L = G.load_library()
+    gold = dict(np.load(os.path.join(GOLD, "reference_multires.npz")))
+    nb, bsx, seed = case
+    key = "x".join(map(str, nb)) + f"_bs{bsx}"
+    lv, x, b, dinv = H.multires_case(nb, bsx, 3, seed, lambda *a: port.regularize(*a)[0])
+    g, spans = _multires_grid(G, nb, bsx, lv, x, b, dinv)
+    bufs = []
+    try:
+        for l, (off, n) in enumerate(spans):
+            at = lv == l
+            st = np.full(lv.size, H.LBLK_NONE, np.int32)
+            st[at] = np.arange(int(at.sum()), dtype=np.int32)
+            ds, dp = g.to_device(st), g.to_device(x[off:off + n].copy() if n else np.zeros(4, np.float32))
+            bufs += [ds, dp]
+            g.level_grid_bind(3, l, G.F32, ds.ptr, dp.ptr)
+        bids = np.arange(lv.size, dtype=np.int32)
+        for passes, rev in H.MULTIRES_RELAX_RUNS:
+            for l, (off, n) in enumerate(spans):  # X from the start
+                if n:
+                    src = np.ascontiguousarray(x[off:off + n])
+                    assert L.msbg_gpu_copy_h2d(g.h, bufs[2 * l + 1].ptr, src.ctypes.data, src.nbytes) == 0
+            for _ in range(passes):
+                assert g.relax_levels(3, 2, 1, bids, reverse=rev) == 0
+            got = np.empty_like(x)
+            for l, (off, n) in enumerate(spans):
+                if n:
+                    assert L.msbg_gpu_copy_d2h(g.h, got[off:off + n].ctypes.data, bufs[2 * l + 1].ptr, 4 * n) == 0
+            g.synchronize()
+            want = gold[f"{key}_relaxed_{passes}_{int(rev)}"]
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (key, passes, rev)
+        # out-of-range ids are skipped, once per call
+        assert g.relax_levels(3, 2, 1, np.array([lv.size, -1], np.int32)) == 2
+    finally:
+        for d in bufs:
+            d.free()
+        g.close()

@@ -154,6 +154,22 @@ def test_multires_operator_matches_reference(port, case):
     assert abs(dot - float(gold[f"{key}_dot"])) <= 1e-12 * abs(dot)
 
 
+@pytest.mark.parametrize("case", H.MULTIRES_CASES, ids=[_multires_key(c[0], c[1]) for c in H.MULTIRES_CASES])
+def test_multires_block_smoother_matches_reference(port, case):
+    """relaxBlockList on a 3-level layout (the operator's halo with mixed-resolution faces,
+    5 block-local iterations, omega 6/7): the restatement equals the reference bit for bit,
+    one forward pass and two passes in the reverse order."""
+    gold = dict(np.load(os.path.join(GOLD, "reference_multires.npz")))
+    nb, bsx, seed = case
+    key = _multires_key(nb, bsx)
+    lv, x, b, dinv = H.multires_case(nb, bsx, 3, seed, lambda *a: port.regularize(*a)[0])
+    for passes, rev in H.MULTIRES_RELAX_RUNS:
+        got = port.relax_levels(*(n * bsx for n in nb), bsx, 3, lv, x, b, dinv, passes=passes, reverse=rev)
+        want = gold[f"{key}_relaxed_{passes}_{int(rev)}"]
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (passes, rev)
+        assert rel_l2(want, x) > 0.1  # the smoother did move the field
+
+
 def test_multires_faces_weigh_the_other_level(port):
     """Known answers of the mixed-resolution faces: X = 1 everywhere and the diagonal channel
     1/6 make Y = 6 h - S vanish inside a level and leave, on a fine cell next to a coarser
