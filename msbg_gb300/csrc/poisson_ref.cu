@@ -229,9 +229,10 @@ __global__ void __launch_bounds__(kListThreads) kRelaxRef(const int32_t *__restr
       S = __fmaf_rn(F4, W4, S);
       S = __fmaf_rn(F5, W5, S);
       S = __fmaf_rn(F6, W6, S);
+      // omega (B + S) D + (1 - omega) F0 as the reference's compiled 8-wide path forms it
       const float dinv = __frcp_rn(d[c]);
-      const float t = __fmul_rn(omega, __fadd_rn(b[c], S));
-      y[l] = __fadd_rn(__fmul_rn(t, dinv), __fmul_rn(oneMinusOmega, F0));
+      const float t = __fadd_rn(S, b[c]);
+      y[l] = __fmaf_rn(oneMinusOmega, F0, __fmul_rn(__fmul_rn(omega, dinv), t));
     }
   };
   for (int it = 0; it < blockIter - 1; it++) {

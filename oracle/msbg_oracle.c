@@ -1562,8 +1562,11 @@ static void relax_ref_block(int nx, int ny, int nz, int bs, float *x, const floa
         S = fmaf(F4, W4, S);
         S = fmaf(F5, W5, S);
         S = fmaf(F6, W6, S);
-        const float t = omega * (b[c] + S);
-        y[l] = t * dinv[c] + oneMinusOmega * F0;
+        /* omega (B + S) D + (1 - omega) F0 as the reference's build (-O3 -ffast-math
+           -march=native) evaluates it in its 8-wide path: t = S + B, then one fused
+           multiply-add with (omega D) t; this matches its output bit for bit */
+        const float t = S + b[c];
+        y[l] = fmaf(oneMinusOmega, F0, (omega * dinv[c]) * t);
       }
       for (int l = 0; l < gw; l++) {
         const int i = gw * g + l;
