@@ -255,7 +255,9 @@ int msbg_gpu_poisson_procedural_coefficients(msbg_gpu_ctx *ctx, uint32_t seed, i
  * call synchronize.  levelMg must be 0 (the value blocks); kap is unused, as in the
  * reference's sparse-level path.  The reference's operator is h ((1/D) X - sum W X_nb) with
  * D = 1/diagonal stored in CH_DIAGONAL, the face areas W and h = 1 at level 0; here the
- * diagonal itself is stored, which differs from 1/(1/d) by rounding only. */
+ * diagonal itself is stored, and the call forms 1/(1/d) in FP32 from it and evaluates the
+ * rest in the reference's compiled order, so Y equals the reference's bit for bit.  Without a
+ * list the call covers every value block. */
 #define MSBG_GPU_OPT_CALC_RESIDUAL (1u << 12) /* OPT_CALC_RESIDUAL (src/msbg.h:115) */
 int msbg_gpu_multiply_laplacian(msbg_gpu_ctx *ctx, unsigned options, int levelMg, int chanX, int chanB,
                                 float kap, int chanDstY, double *pDotprod, const int32_t *dBlockList,

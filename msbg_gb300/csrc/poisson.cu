@@ -947,15 +947,15 @@ extern "C" int msbg_gpu_multiply_laplacian(msbg_gpu_ctx *ctx, unsigned options, 
   if ((rc = chanF32(ctx, chanX, &x)) || (rc = chanF32(ctx, chanDstY, &y))) return rc;
   if (residual && (rc = chanF32(ctx, chanB, &b))) return rc;
   PoissonState *ps = ctx->poisson;
-  if (dBlockList) {
-    SlotLists L;
-    if ((rc = listSlots(ctx, ps, dBlockList, nBlockList, &L))) return rc;
-    if ((rc = applyList(ctx, ps, L, x, b, y, residual ? 1 : 0, pDotprod ? ps->dScal + 13 : nullptr))) return rc;
-  } else if (pDotprod) {
-    if ((rc = applyT<float>(ctx, ps, ps->f32, 0, x, nullptr, y, 0, ps->dScal + 13))) return rc;
-  } else {
-    if ((rc = applyT<float>(ctx, ps, ps->f32, 0, x, b, y, residual ? 1 : 0))) return rc;
+  // the reference's operator form (kApplyList) over the list, or over every value block;
+  // the multigrid keeps its own operator kernels
+  if (!dBlockList) {
+    dBlockList = ctx->dActive;
+    nBlockList = ctx->nActive;
   }
+  SlotLists L;
+  if ((rc = listSlots(ctx, ps, dBlockList, nBlockList, &L))) return rc;
+  if ((rc = applyList(ctx, ps, L, x, b, y, residual ? 1 : 0, pDotprod ? ps->dScal + 13 : nullptr))) return rc;
   if (pDotprod) {
     if ((rc = fetchScal(ctx, ps, 13, 1))) return rc;
     *pDotprod = ps->hScal[13];

@@ -71,6 +71,9 @@ __device__ __forceinline__ double ctaSumD(double v) {
 
 // (A x)_c = d x_c - sum_f c_f x_nb(f) for the cells of the listed blocks (x = 0 outside
 // the value blocks); residual: y = b - A x; part[k] = sum over block k of y*x (FP64).
+// The reference keeps 1/d in CH_DIAGONAL and multiplies x by the reciprocal of that, in one
+// fused multiply-add with the face sum (its compiled form); so does this kernel, from d:
+// 1/(1/d) in FP32, which makes it equal the reference's operator bit for bit.
 __global__ void __launch_bounds__(kListThreads) kApplyList(const int32_t *__restrict__ slots, BlkGeom g,
                                                            const float *__restrict__ x, const float *__restrict__ b,
                                                            const float *__restrict__ cx, const float *__restrict__ cy,
@@ -117,7 +120,7 @@ __global__ void __launch_bounds__(kListThreads) kApplyList(const int32_t *__rest
     s6 = fmaf(cz[c], zm, s6);
     s6 = fmaf(czp, zp, s6);
     const float xc = x[c];
-    float r = fmaf(d[c], xc, -s6);
+    float r = fmaf(__fdiv_rn(1.0f, __frcp_rn(d[c])), xc, -s6);
     if (residual) r = b[c] - r;
     y[c] = r;
     acc += (double)r * (double)xc;
