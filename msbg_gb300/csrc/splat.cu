@@ -183,9 +183,10 @@ __global__ void __launch_bounds__(256) kSplatScatter(const float *__restrict__ p
 // block's 135 KB allowed one.
 template <int BS, int NZ>
 constexpr int splatSmemWords() { return BS * (BS / NZ) * (BS + 1); }
-// threads per CTA (BS^2 / 2), and CTAs per SM to keep the registers for: 1536 threads
+// threads per CTA (512, 256, 128 for BS 32, 16, 8), and CTAs per SM to keep the registers
+// for: 1536 threads
 template <int BS>
-constexpr int splatThreads() { return BS * BS / 2; }
+constexpr int splatThreads() { return 16 * BS; }
 template <int BS>
 constexpr int splatMinCtas() { return 1536 / splatThreads<BS>(); }
 
