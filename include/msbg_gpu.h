@@ -262,6 +262,21 @@ int msbg_gpu_poisson_procedural_coefficients(msbg_gpu_ctx *ctx, uint32_t seed, i
 int msbg_gpu_multiply_laplacian(msbg_gpu_ctx *ctx, unsigned options, int levelMg, int chanX, int chanB,
                                 float kap, int chanDstY, double *pDotprod, const int32_t *dBlockList,
                                 int64_t nBlockList);
+/* multiplyLaplacianMatrixOpt(options, levelMg, chanX, chanB, kap, chanDstY) at a dense
+ * multigrid level (levelMg >= the number of resolution levels; src/msbg3.cpp:1756-1812, the
+ * operator ImultiplyLaplacianMatrixProcessSliceDenseLevel, src/msbg3.cpp:166-403) on device
+ * arrays of one such level: sx*sy*sz cells, x fastest, with the cell flags (uint16, the
+ * reference's CellFlags bits), X, B (residual only), the diagonal channel as the reference
+ * holds it (1/diagonal) and the lower-face areas.  Outside the box X and the face areas are 0
+ * and the cells are void, as the reference's zero border with void flags gives.  Each row goes
+ * in groups of 4 cells from x = 0: a group without a fluid cell is skipped and its outputs are
+ * not written; a group with a solid or partially solid cell weighs every neighbour by its face
+ * area.  Fluid cells get Y = h ((1/D) X - sum F), h = 2^levelMg, other cells of a processed
+ * group 0; with MSBG_GPU_OPT_CALC_RESIDUAL Y = B - A X.  Bit for bit with the reference's
+ * compiled operator.  Asynchronous on the context's stream. */
+int msbg_gpu_multiply_laplacian_dense(msbg_gpu_ctx *ctx, unsigned options, int levelMg, int sx, int sy, int sz,
+                                      const uint16_t *dFlags, const float *dX, const float *dB, const float *dDiag,
+                                      const float *dAreaX, const float *dAreaY, const float *dAreaZ, float *dY);
 /* relax(boundaryZoneOnly, reverseOrder, levelMg, chanX, chanB, chanTmp, nIter, options)
  * (src/msbg.h:3269-3277, src/msbg3.cpp:2244-2369): nIter passes of the reference's block
  * smoother on A X = B, in place: each pass relaxes the blocks of parity (bx+by+bz)&1 = 1,

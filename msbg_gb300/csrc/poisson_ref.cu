@@ -386,3 +386,77 @@ int relaxReference(msbg_gpu_ctx *ctx, PoissonState *ps, const SlotLists *L, floa
 }
 
 }  // namespace msbg
+
+// ---- the operator at a dense multigrid level --------------------------------------------
+//
+// ImultiplyLaplacianMatrixProcessSliceDenseLevel (src/msbg3.cpp:166-403), the operator of
+// multiplyLaplacianMatrixOpt at levelMg >= nLevels, on one dense level's arrays (x fastest;
+// X and the face areas are 0 outside the box, and its cells are void there).  The reference
+// walks each row in groups of 4 cells from x = 0: a group without a fluid cell is skipped,
+// a group with a solid or partially solid cell weighs every cell's neighbours by the face
+// areas.  Per fluid cell Y = h (X / D - S), S = (F1+F2) + ((F3+F4) + (F5+F6)) (the
+// reference's compiled form of h (1/D) X - h sum F), 0 for other cells of a processed
+// group; the residual B - Y.  One thread per cell.
+namespace msbg {
+namespace {
+
+constexpr unsigned kCellSolid = 1u << 0, kCellPartialSolid = 1u << 6, kCellVoid = 1u << 12;
+
+__global__ void __launch_bounds__(256) kApplyDense(int sx, int sy, int sz, float h, int residual,
+                                                   const uint16_t *__restrict__ fl, const float *__restrict__ x,
+                                                   const float *__restrict__ b, const float *__restrict__ d,
+                                                   const float *__restrict__ ax, const float *__restrict__ ay,
+                                                   const float *__restrict__ az, float *__restrict__ y) {
+  const int64_t sxy = (int64_t)sx * sy, n = sxy * sz;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t row = i / sx;
+  const int xx = (int)(i - row * sx), yy = (int)(row % sy), zz = (int)(row / sy);
+  bool active = false, weighted = false;
+  for (int k = 0, g0 = xx & ~3; k < 4 && g0 + k < sx; k++) {
+    const unsigned f = fl[row * sx + g0 + k];
+    active |= (f & (kCellSolid | kCellVoid)) == 0;
+    weighted |= (f & (kCellSolid | kCellPartialSolid)) != 0;
+  }
+  if (!active) return;  // the reference skips the group and leaves its outputs as they are
+  float Y = 0.0f;
+  if ((fl[i] & (kCellSolid | kCellVoid)) == 0) {
+    float F1 = xx > 0 ? x[i - 1] : 0.0f, F2 = xx < sx - 1 ? x[i + 1] : 0.0f;
+    float F3 = yy > 0 ? x[i - sx] : 0.0f, F4 = yy < sy - 1 ? x[i + sx] : 0.0f;
+    float F5 = zz > 0 ? x[i - sxy] : 0.0f, F6 = zz < sz - 1 ? x[i + sxy] : 0.0f;
+    if (weighted) {
+      F1 = __fmul_rn(F1, ax[i]);
+      F2 = __fmul_rn(F2, xx < sx - 1 ? ax[i + 1] : 0.0f);
+      F3 = __fmul_rn(F3, ay[i]);
+      F4 = __fmul_rn(F4, yy < sy - 1 ? ay[i + sx] : 0.0f);
+      F5 = __fmul_rn(F5, az[i]);
+      F6 = __fmul_rn(F6, zz < sz - 1 ? az[i + sxy] : 0.0f);
+    }
+    const float S = __fadd_rn(__fadd_rn(F1, F2), __fadd_rn(__fadd_rn(F3, F4), __fadd_rn(F5, F6)));
+    Y = __fmul_rn(__fsub_rn(__fdiv_rn(x[i], d[i]), S), h);
+  }
+  if (residual) Y = __fsub_rn(b[i], Y);
+  y[i] = Y;
+}
+
+}  // namespace
+}  // namespace msbg
+
+extern "C" int msbg_gpu_multiply_laplacian_dense(msbg_gpu_ctx *ctx, unsigned options, int levelMg, int sx, int sy,
+                                                 int sz, const uint16_t *dFlags, const float *dX, const float *dB,
+                                                 const float *dDiag, const float *dAreaX, const float *dAreaY,
+                                                 const float *dAreaZ, float *dY) {
+  using namespace msbg;
+  if (!ctx) return MSBG_GPU_ERR_ARG;
+  const bool residual = (options & MSBG_GPU_OPT_CALC_RESIDUAL) != 0;
+  if (options & ~(unsigned)MSBG_GPU_OPT_CALC_RESIDUAL)
+    return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "multiply_dense: options 0x%x", options);
+  if (levelMg < 0 || levelMg > 30) return fail(ctx, MSBG_GPU_ERR_ARG, "multiply_dense: levelMg %d out of range", levelMg);
+  if (sx <= 0 || sy <= 0 || sz <= 0) return fail(ctx, MSBG_GPU_ERR_ARG, "multiply_dense: empty box");
+  if (!dFlags || !dX || !dDiag || !dAreaX || !dAreaY || !dAreaZ || !dY || (residual && !dB))
+    return fail(ctx, MSBG_GPU_ERR_ARG, "multiply_dense: null array");
+  const int64_t n = (int64_t)sx * sy * sz;
+  MSBG_LAUNCH(ctx, kApplyDense, (unsigned)((n + 255) / 256), 256, 0, sx, sy, sz, (float)(1 << levelMg),
+              residual ? 1 : 0, dFlags, dX, dB, dDiag, dAreaX, dAreaY, dAreaZ, dY);
+  return MSBG_GPU_OK;
+}

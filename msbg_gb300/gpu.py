@@ -116,6 +116,7 @@ SIGNATURES = {
     "msbg_gpu_restrict_level_blocks": (I, [P, I, I, P, I64, I, P, C.POINTER(I64)]),
     "msbg_gpu_multiply_laplacian_levels": (I, [P, C.c_uint, I, I, I, I, P, I64, P, C.POINTER(D), C.POINTER(I64)]),
     "msbg_gpu_relax_levels": (I, [P, I, I, I, I, P, I64, C.POINTER(I64)]),
+    "msbg_gpu_multiply_laplacian_dense": (I, [P, C.c_uint, I, I, I, I, P, P, P, P, P, P, P, P]),
     "msbg_gpu_level_flags_set": (I, [P, I, I, P, P, I64, C.c_uint16, C.c_uint16]),
     "msbg_gpu_fill_halo_blocks3": (I, [P, I, I, I, P, I64, P, P, C.POINTER(I64)]),
     "msbg_gpu_diag_wait_timeout": (I, [P, I]),
@@ -766,6 +767,28 @@ class MultiresSparseGrid:
             db.free()
             do.free()
         return out, (None if residual else dot.value), int(sk.value)
+
+    # reference: multiplyLaplacianMatrixOpt at a dense multigrid level (src/msbg3.cpp:166-403)
+    def multiply_laplacian_dense(self, level_mg: int, flags, x, dinv, area_x, area_y, area_z, b=None,
+                                 residual: bool = False, y_init=None) -> np.ndarray:
+        """Host arrays [sz][sy][sx] in, Y (or B - A X) out; cells of skipped groups keep y_init
+        (0 by default)."""
+        fl = np.ascontiguousarray(flags, np.uint16)
+        sz, sy, sx = fl.shape
+        arrs = [np.ascontiguousarray(a, np.float32).reshape(fl.shape) for a in (x, dinv, area_x, area_y, area_z)]
+        bb = np.ascontiguousarray(b if b is not None else np.zeros(fl.shape), np.float32).reshape(fl.shape)
+        y = np.ascontiguousarray(np.zeros(fl.shape, np.float32) if y_init is None else y_init, np.float32).copy()
+        bufs = [self.to_device(a) for a in [fl, *arrs, bb, y]]
+        try:
+            df, dx, dd, da, db_, dc, dbb, dy = (C.c_void_p(u.ptr) for u in bufs)
+            self._check(self.L.msbg_gpu_multiply_laplacian_dense(
+                self.h, OPT_CALC_RESIDUAL if residual else 0, level_mg, sx, sy, sz, df, dx, dbb, dd, da, db_, dc, dy))
+            self._check(self.L.msbg_gpu_copy_d2h(self.h, _ptr(y), dy, y.nbytes))
+            self.synchronize()
+        finally:
+            for u in bufs:
+                u.free()
+        return y
 
     # reference: relaxBlockList (src/msbg3.cpp:2170-2239) on a multi-resolution layout
     def relax_levels(self, lchan_x: int, lchan_b: int, lchan_d: int, bids: np.ndarray, reverse: bool = False) -> int:

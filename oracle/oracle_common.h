@@ -56,7 +56,7 @@
 enum { ORACLE_CHAN_F32 = 0, ORACLE_CHAN_U16 = 1 };
 enum { ORACLE_JOB_SURFACE = 1, ORACLE_JOB_LEVELS = 2, ORACLE_JOB_INTERP = 3, ORACLE_JOB_HALO = 4,
        ORACLE_JOB_RENDER = 5, ORACLE_JOB_MORTON = 6, ORACLE_JOB_SOLVER = 7, ORACLE_JOB_DOWNSAMPLE = 8,
-       ORACLE_JOB_HALO3 = 9, ORACLE_JOB_LAYOUT = 10, ORACLE_JOB_MULTIRES = 11 };
+       ORACLE_JOB_HALO3 = 9, ORACLE_JOB_LAYOUT = 10, ORACLE_JOB_MULTIRES = 11, ORACLE_JOB_DENSE = 12 };
 
 /* Interp job option bits: the reference's own interpolation options (src/sbg.h:140-170)
  * plus one bit that the reference's enum leaves unused, for the render-density scale. */

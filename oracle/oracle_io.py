@@ -509,3 +509,42 @@ def run_reference_multires(sx, sy, sz, bsx, n_levels, levels, x, b, dinv, relax_
     if relax_passes > 0:
         out["relaxed"] = np.frombuffer(buf, np.float32, total, hsz + 8 + 8 * total).copy()
     return out
+
+
+JOB_DENSE = 12
+
+
+def run_reference_dense(sx0, sy0, sz0, bsx, n_levels, flags, x, b, dinv, area_x, area_y, area_z,
+                        timeout: float = 600) -> dict:
+    """multiplyLaplacianMatrixOpt by the reference itself at the first dense multigrid level
+    (levelMg = n_levels) of a grid sx0 x sy0 x sz0 with block edge bsx: the masked 7-point
+    operator of ImultiplyLaplacianMatrixProcessSliceDenseLevel (src/msbg3.cpp:166-403).
+    flags (cell flags, uint16) and the float32 arrays are [sz][sy][sx] of that level (x
+    fastest); dinv is what CH_DIAGONAL holds, area_* the lower-face areas.  Returns
+    {"y": A X, "r": B - A X} in the same layout."""
+    fl = np.ascontiguousarray(flags, np.uint16)
+    shape = fl.shape
+    arrs = [np.ascontiguousarray(v, np.float32).reshape(shape) for v in (x, b, dinv, area_x, area_y, area_z)]
+    n = fl.size
+    with tempfile.TemporaryDirectory() as td:
+        jp, op = os.path.join(td, "job.bin"), os.path.join(td, "out.bin")
+        hdr = struct.pack(_JOB_FMT, JOB_MAGIC, JOB_DENSE, sx0, sy0, sz0, bsx, n_levels, CHAN_F32, 0, 0, 0, 1,
+                          0.0, 0.0, 0.0, 0.0, 0, 0, n)
+        with open(jp, "wb") as f:
+            f.write(hdr)
+            f.write(fl.astype(np.int32).tobytes())
+            for a in arrs:
+                f.write(a.tobytes())
+        r = subprocess.run([REF_DRIVER, jp, op], cwd=td, timeout=timeout,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference dense job failed with status {r.returncode}")
+        with open(op, "rb") as f:
+            buf = f.read()
+    hsz = struct.calcsize(_OUT_FMT)
+    h = struct.unpack(_OUT_FMT, buf[:hsz])
+    if h[0] != OUT_MAGIC or (int(h[3]), int(h[2]), int(h[1])) != (shape[0], shape[1], shape[2]):
+        raise ValueError("bad oracle output or level size")
+    y = np.frombuffer(buf, np.float32, n, hsz).copy().reshape(shape)
+    res = np.frombuffer(buf, np.float32, n, hsz + 4 * n).copy().reshape(shape)
+    return {"y": y, "r": res}

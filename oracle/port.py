@@ -709,3 +709,47 @@ def relax_levels(sx, sy, sz, bsx, n_levels, levels, x, b, dinv, passes=1, revers
                                                                      indexing="ij"))
                         L.blocks[bid][2][...] = (update(ck, cj, ci) * f32(1.0 / h)).reshape(bs, bs, bs)
     return x
+
+
+CELL_SOLID, CELL_PARTIAL_SOLID, CELL_VOID = 1 << 0, 1 << 6, 1 << 12
+
+
+def multiply_laplacian_dense(flags, x, b, dinv, area_x, area_y, area_z, h):
+    """multiplyLaplacianMatrixOpt at a dense multigrid level: the masked 7-point operator of
+    ImultiplyLaplacianMatrixProcessSliceDenseLevel (src/msbg3.cpp:166-403) on [sz][sy][sx]
+    arrays (x fastest), X and the face areas 0 outside the box.  The reference walks each row
+    in groups of 4 cells from x = 0: a group without a fluid cell (not CELL_SOLID or
+    CELL_VOID) is skipped (its outputs are not written: 0 here); a group in which some cell is
+    CELL_SOLID or CELL_PARTIAL_SOLID weighs every cell's neighbours F1..F6 by the face areas
+    (lower faces of the cell, upper faces = lower faces of the next cell).  Per cell
+    Y = h (1/dinv) X - h S with S = F1 + ... + F6, zero for non-fluid cells; the residual
+    B - Y for every cell of a processed group.  The reference as compiled here folds the
+    reciprocal into a division and adds S as (F1+F2) + ((F3+F4) + (F5+F6)):
+    Y = h (X / dinv - S), which this restatement follows bit for bit.  Returns (y, r)."""
+    f32 = np.float32
+    fl = np.asarray(flags).astype(np.int64)
+    sz, sy, sx = fl.shape
+    x, b, dinv, ax, ay, az = (np.asarray(a, f32).reshape(fl.shape) for a in (x, b, dinv, area_x, area_y, area_z))
+    X = np.pad(x, 1)
+    AX, AY, AZ = np.pad(ax, 1), np.pad(ay, 1), np.pad(az, 1)
+    F = [X[1:-1, 1:-1, :-2], X[1:-1, 1:-1, 2:], X[1:-1, :-2, 1:-1], X[1:-1, 2:, 1:-1], X[:-2, 1:-1, 1:-1],
+         X[2:, 1:-1, 1:-1]]
+    W = [ax, AX[1:-1, 1:-1, 2:], ay, AY[1:-1, 2:, 1:-1], az, AZ[2:, 1:-1, 1:-1]]
+    fluid = (fl & (CELL_SOLID | CELL_VOID)) == 0
+    part = (fl & (CELL_SOLID | CELL_PARTIAL_SOLID)) != 0
+    g = -(-sx // 4) * 4
+
+    def group_any(m):
+        mm = np.zeros((sz, sy, g), bool)
+        mm[:, :, :sx] = m
+        return np.repeat(mm.reshape(sz, sy, g // 4, 4).any(-1), 4, axis=-1)[:, :, :sx]
+
+    weighted, active = group_any(part), group_any(fluid)
+    Fw = [np.where(weighted, Fi * Wi, Fi).astype(f32) for Fi, Wi in zip(F, W)]
+    S = (Fw[0] + Fw[1]) + ((Fw[2] + Fw[3]) + (Fw[4] + Fw[5]))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        Y = ((x / dinv).astype(f32) - S) * f32(h)
+    Y = np.where(fluid, Y, f32(0.0)).astype(f32)
+    y = np.where(active, Y, f32(0.0)).astype(f32)
+    r = np.where(active, b - Y, f32(0.0)).astype(f32)
+    return y, r

@@ -15,7 +15,8 @@
  * (halo job), the ray-march renderer RDR::RaymarchRenderer (render job),
  * sortBlockListMorton (morton job), the solver building blocks
  * multiplyLaplacianMatrixOpt / dotProdChannel / AXPBYChannelCombined / relaxBlockList
- * (solver job), the same operator on a multi-resolution layout (multires job) and
+ * (solver job), the same operator on a multi-resolution layout (multires job) and at a
+ * dense multigrid level (dense job), and
  * downsampleFloatChannelNew (downsample job).
  *
  * Differences from the demo, both forced by the workload definition:
@@ -32,6 +33,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "msbg.h"
@@ -795,6 +797,85 @@ int runMultiresJob(const OracleJobHeader &job, const int32_t *levelsIn, const fl
   return 0;
 }
 
+// multiplyLaplacianMatrixOpt (src/msbg3.cpp:1756-1812) at the first dense multigrid level
+// (levelMg = nLevels: the dense grids MultiresSparseGrid::create adds below the sparse
+// levels, src/msbg.cpp:847-1000), i.e. the masked 7-point operator
+// ImultiplyLaplacianMatrixProcessSliceDenseLevel (src/msbg3.cpp:166-403).  Inputs after the
+// header (job.nBlocksIn = the level's cells sx*sy*sz, x fastest): the cell flags (int32), then
+// float32 X, B, DINV (what CH_DIAGONAL holds) and the face areas AX, AY, AZ (lower faces of
+// each cell).  Every other cell of the dense arrays (the 2-cell border and the x padding)
+// is zero, so X and the face areas read 0 outside the box, except the cell flags, which hold
+// the flags grid's empty value CELL_EMPTY_VAL (void) there.  Output: Y = A X, then
+// R = B - A X, over the box.
+int runDenseJob(const OracleJobHeader &job, const uint16_t *flagsIn, const float *arrays, FILE *fout) {
+  OracleOutHeader out;
+  memset(&out, 0, sizeof(out));
+  memcpy(out.magic, ORACLE_OUT_MAGIC, 8);
+  MultiresSparseGrid *msbg = MultiresSparseGrid::create(
+      "TEST", job.sx, job.sy, job.sz, job.bsx, -1, 0, -1, 0, NULL, NULL, job.nLevels);
+  if (!msbg) return 2;
+  const int L = job.nLevels;
+  if (msbg->getNumMgLevels() <= L) return 6;
+  using MSBG::CH_PRESSURE;
+  using MSBG::CH_DIVERGENCE;
+  using MSBG::CH_CG_Q;
+  using MSBG::CH_DIAGONAL;
+  SparseGrid<MSBG::CellFlags> *sgF = msbg->getFlagsChannel(MSBG::CH_CELL_FLAGS, L, L);
+  SparseGrid<PSFloat> *sgX = msbg->getPSFloatChannel(CH_PRESSURE, L, L),
+                      *sgB = msbg->getPSFloatChannel(CH_DIVERGENCE, L, L),
+                      *sgQ = msbg->getPSFloatChannel(CH_CG_Q, L, L),
+                      *sgD = msbg->getPSFloatChannel(CH_DIAGONAL, L, L);
+  SparseGrid<float> *sgA[3] = {msbg->getFaceAreaChannel(0, L, L), msbg->getFaceAreaChannel(1, L, L),
+                               msbg->getFaceAreaChannel(2, L, L)};
+  if (!sgF || !sgX || !sgB || !sgQ || !sgD || !sgA[0] || !sgA[1] || !sgA[2]) return 3;
+  const int sx = sgF->sx(), sy = sgF->sy(), sz = sgF->sz();
+  const int64_t n = (int64_t)sx * sy * sz;
+  if (n != job.nBlocksIn) return 4;
+  // the dense arrays: sxAct x (sy + 4) x (sz + 4) cells with a 2-cell border (src/sbg.cpp:131-189)
+  auto fill = [&](auto *sg, const auto *src, double outside = 0.0) {
+    using T = std::remove_pointer_t<decltype(sg->getDataPtrGen_(0, 0, 0, 1))>;
+    T *p = sg->getDataPtrGen_(0, 0, 0, 1);
+    const size_t all = (size_t)sg->sxAct() * (sy + 4) * (sz + 4);
+    for (size_t i = 0; i < all; i++) p[i] = (T)outside;
+    if (!src) return;
+    for (int z = 0; z < sz; z++)
+      for (int y = 0; y < sy; y++)
+        for (int x = 0; x < sx; x++) p[sg->getGridIndex(x, y, z)] = src[((int64_t)z * sy + y) * sx + x];
+  };
+  const float *X = arrays, *B = X + n, *DI = B + n, *A = DI + n;
+  fill(sgF, flagsIn, (double)MSBG::CELL_EMPTY_VAL);
+  fill(sgX, X);
+  fill(sgB, B);
+  fill(sgD, DI);
+  for (int k = 0; k < 3; k++) fill(sgA[k], A + (int64_t)k * n);
+  auto dump = [&](std::vector<float> &dst) {
+    const PSFloat *p = sgQ->getDataPtrGen_(0, 0, 0, 1);
+    dst.resize((size_t)n);
+    for (int z = 0; z < sz; z++)
+      for (int y = 0; y < sy; y++)
+        for (int x = 0; x < sx; x++) dst[((int64_t)z * sy + y) * sx + x] = p[sgQ->getGridIndex(x, y, z)];
+  };
+  const double t0 = nowSec();
+  std::vector<float> Y, R;
+  fill(sgQ, (const float *)nullptr);
+  msbg->multiplyLaplacianMatrixOpt(0, L, CH_PRESSURE, CH_DIVERGENCE, 0.f, CH_CG_Q, NULL, NULL);
+  dump(Y);
+  fill(sgQ, (const float *)nullptr);
+  msbg->multiplyLaplacianMatrixOpt(MSBG::OPT_CALC_RESIDUAL, L, CH_PRESSURE, CH_DIVERGENCE, 0.f, CH_CG_Q, NULL, NULL);
+  dump(R);
+  out.tPdeSec = nowSec() - t0;
+  out.nBlocks = sx;
+  out.nActive = sy;
+  out.nActParticles = sz;
+  out.elemBytes = 4;
+  out.nThreadsUsed = omp_get_max_threads();
+  fwrite(&out, sizeof(out), 1, fout);
+  fwrite(Y.data(), 4, (size_t)n, fout);
+  fwrite(R.data(), 4, (size_t)n, fout);
+  MultiresSparseGrid::destroy(msbg);
+  return 0;
+}
+
 // downsampleFloatChannelNew (src/msbg4.cpp:1035-1379) to multigrid level 1 on a
 // multi-level grid loaded like the halo job (channel CH_FLOAT_1, every resolution level
 // with the job's block states and payloads; job.laplTyp = 0).  constr01 = 1 adds
@@ -1017,6 +1098,13 @@ int main(int argc, char **argv) {
     if (!solverArrays.empty() && fread(solverArrays.data(), 4, solverArrays.size(), fin) != solverArrays.size())
       return 1;
   }
+  std::vector<uint16_t> denseFlags;
+  if (job.jobType == ORACLE_JOB_DENSE) {  // the int32 array read above holds the cell flags
+    denseFlags.resize((size_t)job.nBlocksIn);
+    for (int64_t i = 0; i < job.nBlocksIn; i++) denseFlags[(size_t)i] = (uint16_t)lv[(size_t)i];
+    solverArrays.resize((size_t)6 * job.nBlocksIn);
+    if (fread(solverArrays.data(), 4, solverArrays.size(), fin) != solverArrays.size()) return 1;
+  }
   std::vector<int32_t> fstate, dbc(6, 0);
   std::vector<std::vector<uint16_t>> flagPay;
   if (job.jobType == ORACLE_JOB_HALO || job.jobType == ORACLE_JOB_DOWNSAMPLE || job.jobType == ORACLE_JOB_HALO3) {
@@ -1072,6 +1160,8 @@ int main(int argc, char **argv) {
     rc = runSolverJob(job, lv.data(), solverArrays.data(), fout);
   else if (job.jobType == ORACLE_JOB_MULTIRES)
     rc = runMultiresJob(job, lv.data(), solverArrays.data(), fout);
+  else if (job.jobType == ORACLE_JOB_DENSE)
+    rc = runDenseJob(job, denseFlags.data(), solverArrays.data(), fout);
   else if (job.jobType == ORACLE_JOB_HALO3)
     rc = job.chanType == ORACLE_CHAN_F32
              ? runHalo3Job(job, lv.data(), state.data(), levelPay, fstate.data(), flagPay, dbc.data(), fout)

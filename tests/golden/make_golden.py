@@ -17,9 +17,10 @@ reference_downsample.npz (downsampleFloatChannelNew on multi-level channels) and
 reference_surface512.npz (the 512^3 surface workload at full size: layout, counters,
 per-block sums and a voxel sample of the fields), reference_halo3.npz (the solver's halo,
 fillHaloBlock3), reference_layout.npz (setRefinementMap's block lists and fine-coarse
-distance channel) and reference_multires.npz (the solver operator on multi-resolution
-layouts).  Arguments name a subset
-(small interp halo render morton solver downsample surface512 halo3 layout multires).
+distance channel), reference_multires.npz (the solver operator and block smoother on
+multi-resolution layouts) and reference_dense.npz (the operator at a dense multigrid
+level).  Arguments name a subset
+(small interp halo render morton solver downsample surface512 halo3 layout multires dense).
 """
 from __future__ import annotations
 
@@ -67,7 +68,7 @@ def main(which: list[str]) -> None:
     if not O.ref_available():
         raise SystemExit("oracle/_ref/msbg_ref_driver missing: run `make -C oracle ref` first")
     parts = set(which) or {"small", "interp", "halo", "render", "morton", "solver", "downsample", "surface512",
-                           "halo3", "layout", "multires"}
+                           "halo3", "layout", "multires", "dense"}
     if parts & {"small", "interp", "render"}:
         out = make_small()
         if "interp" in parts:
@@ -90,6 +91,8 @@ def main(which: list[str]) -> None:
         make_layout()
     if "multires" in parts:
         make_multires()
+    if "dense" in parts:
+        make_dense()
 
 
 def make_small() -> dict:
@@ -329,6 +332,21 @@ def make_multires() -> None:
                                           reverse=rev)
             out[f"{key}_relaxed_{passes}_{int(rev)}"] = rr["relaxed"]
     path = os.path.join(HERE, "reference_multires.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
+
+
+def make_dense() -> None:
+    """multiplyLaplacianMatrixOpt at the first dense multigrid level (oracle/ref_driver.cpp,
+    dense job): Y = A X and B - A X for the seeded cases of tests/halo_cases.py."""
+    import halo_cases as H
+    out = {}
+    for sx0, sy0, sz0, bsx, nl, seed in H.DENSE_CASES:
+        key = f"{sx0}x{sy0}x{sz0}_L{nl}"
+        r = O.run_reference_dense(sx0, sy0, sz0, bsx, nl, *H.dense_case(sx0, sy0, sz0, nl, seed))
+        out[f"{key}_y"] = r["y"]
+        out[f"{key}_r"] = r["r"]
+    path = os.path.join(HERE, "reference_dense.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
 

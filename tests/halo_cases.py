@@ -115,3 +115,28 @@ def multires_case(nb, bsx: int, n_levels: int, seed: int, regularize):
     dinv = rng.uniform(0.1, 0.2, total).astype(np.float32)
     dinv[rng.random(total) < 0.01] = 0.0
     return lv, x, b, dinv
+
+
+# the solver operator at the first dense multigrid level: (domain sx, sy, sz of level 0,
+# block edge, resolution levels (the dense level is levelMg = this), seed)
+DENSE_CASES = ((80, 96, 64, 16, 2, 20261203 + 1000), (80, 96, 64, 16, 3, 20261203 + 1001),
+               (112, 48, 80, 16, 2, 20261203 + 1002))
+CELL_SOLID, CELL_PARTIAL_SOLID, CELL_VOID = 1 << 0, 1 << 6, 1 << 12
+
+
+def dense_case(sx0, sy0, sz0, n_levels, seed):
+    """Arrays [sz][sy][sx] of the dense level levelMg = n_levels (edges sx0 >> n_levels, ...):
+    cell flags (10% solid, 10% void, 15% partially solid, the rest fluid), X and B standard
+    normal, the diagonal channel uniform in [0.1, 0.2] with about 2% zeros, face areas uniform
+    in [0.3, 1]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = (sz0 >> n_levels, sy0 >> n_levels, sx0 >> n_levels)
+    r = rng.random(s)
+    flags = np.where(r < 0.1, CELL_SOLID, np.where(r < 0.2, CELL_VOID,
+                                                   np.where(r < 0.35, CELL_PARTIAL_SOLID, 0))).astype(np.uint16)
+    x = rng.standard_normal(s).astype(np.float32)
+    b = rng.standard_normal(s).astype(np.float32)
+    dinv = rng.uniform(0.1, 0.2, s).astype(np.float32)
+    dinv[rng.random(s) < 0.02] = 0.0
+    ax, ay, az = (rng.uniform(0.3, 1.0, s).astype(np.float32) for _ in range(3))
+    return flags, x, b, dinv, ax, ay, az
