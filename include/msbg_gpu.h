@@ -277,6 +277,16 @@ int msbg_gpu_multiply_laplacian(msbg_gpu_ctx *ctx, unsigned options, int levelMg
 int msbg_gpu_multiply_laplacian_dense(msbg_gpu_ctx *ctx, unsigned options, int levelMg, int sx, int sy, int sz,
                                       const uint16_t *dFlags, const float *dX, const float *dB, const float *dDiag,
                                       const float *dAreaX, const float *dAreaY, const float *dAreaZ, float *dY);
+/* relax(0, reverseOrder, levelMg, chanX, chanB, chanTmp, nIter, 0) at a dense multigrid level
+ * (src/msbg3.cpp:2244-2310 -> ImultiplyLaplacianMatrixDenseLevel, src/msbg3.cpp:1917-2165):
+ * nIter omega-Jacobi iterations (omega from msbg_gpu_set_relax_params) of the operator above,
+ * alternating between dX and dTmp (the reference's chanTmp; cells of skipped groups keep what
+ * it holds), the whole of dTmp copied to dX after an odd count.  Fluid cells get
+ * omega (B + h S) D / h + (1 - omega) X in the reference's compiled order, other cells of a
+ * processed group 0.  Bit for bit with the reference.  Asynchronous on the context's stream. */
+int msbg_gpu_relax_dense(msbg_gpu_ctx *ctx, int levelMg, int sx, int sy, int sz, int nIter, const uint16_t *dFlags,
+                         float *dX, const float *dB, const float *dDiag, const float *dAreaX, const float *dAreaY,
+                         const float *dAreaZ, float *dTmp);
 /* relax(boundaryZoneOnly, reverseOrder, levelMg, chanX, chanB, chanTmp, nIter, options)
  * (src/msbg.h:3269-3277, src/msbg3.cpp:2244-2369): nIter passes of the reference's block
  * smoother on A X = B, in place: each pass relaxes the blocks of parity (bx+by+bz)&1 = 1,

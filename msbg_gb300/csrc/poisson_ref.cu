@@ -439,8 +439,74 @@ __global__ void __launch_bounds__(256) kApplyDense(int sx, int sy, int sz, float
   y[i] = Y;
 }
 
+// One omega-Jacobi iteration of the dense-level smoother (src/msbg3.cpp:1917-2165, without
+// the block Gauss-Seidel and scheduled-omega switches, as the release builds it): src -> dst,
+// the operator's groups and weights; fluid cells Y = fma(1 - omega, F0, (B + h S)(D omega/h)),
+// the reference's compiled form, other cells of a processed group 0, skipped groups untouched.
+__global__ void __launch_bounds__(256) kRelaxDense(int sx, int sy, int sz, float h, float omega,
+                                                   const uint16_t *__restrict__ fl, const float *__restrict__ x,
+                                                   const float *__restrict__ b, const float *__restrict__ d,
+                                                   const float *__restrict__ ax, const float *__restrict__ ay,
+                                                   const float *__restrict__ az, float *__restrict__ y) {
+  const int64_t sxy = (int64_t)sx * sy, n = sxy * sz;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t row = i / sx;
+  const int xx = (int)(i - row * sx), yy = (int)(row % sy), zz = (int)(row / sy);
+  bool active = false, weighted = false;
+  for (int k = 0, g0 = xx & ~3; k < 4 && g0 + k < sx; k++) {
+    const unsigned f = fl[row * sx + g0 + k];
+    active |= (f & (kCellSolid | kCellVoid)) == 0;
+    weighted |= (f & (kCellSolid | kCellPartialSolid)) != 0;
+  }
+  if (!active) return;
+  float Y = 0.0f;
+  if ((fl[i] & (kCellSolid | kCellVoid)) == 0) {
+    float F1 = xx > 0 ? x[i - 1] : 0.0f, F2 = xx < sx - 1 ? x[i + 1] : 0.0f;
+    float F3 = yy > 0 ? x[i - sx] : 0.0f, F4 = yy < sy - 1 ? x[i + sx] : 0.0f;
+    float F5 = zz > 0 ? x[i - sxy] : 0.0f, F6 = zz < sz - 1 ? x[i + sxy] : 0.0f;
+    if (weighted) {
+      F1 = __fmul_rn(F1, ax[i]);
+      F2 = __fmul_rn(F2, xx < sx - 1 ? ax[i + 1] : 0.0f);
+      F3 = __fmul_rn(F3, ay[i]);
+      F4 = __fmul_rn(F4, yy < sy - 1 ? ay[i + sx] : 0.0f);
+      F5 = __fmul_rn(F5, az[i]);
+      F6 = __fmul_rn(F6, zz < sz - 1 ? az[i + sxy] : 0.0f);
+    }
+    const float S = __fmul_rn(__fadd_rn(__fadd_rn(F1, F2), __fadd_rn(__fadd_rn(F3, F4), __fadd_rn(F5, F6))), h);
+    const float t = __fadd_rn(b[i], S);
+    const float dho = __fmul_rn(d[i], __fdiv_rn(omega, h));
+    Y = __fmaf_rn(__fsub_rn(1.0f, omega), x[i], __fmul_rn(t, dho));
+  }
+  y[i] = Y;
+}
+
 }  // namespace
 }  // namespace msbg
+
+extern "C" int msbg_gpu_relax_dense(msbg_gpu_ctx *ctx, int levelMg, int sx, int sy, int sz, int nIter,
+                                    const uint16_t *dFlags, float *dX, const float *dB, const float *dDiag,
+                                    const float *dAreaX, const float *dAreaY, const float *dAreaZ, float *dTmp) {
+  using namespace msbg;
+  if (!ctx) return MSBG_GPU_ERR_ARG;
+  if (levelMg < 0 || levelMg > 30) return fail(ctx, MSBG_GPU_ERR_ARG, "relax_dense: levelMg %d out of range", levelMg);
+  if (sx <= 0 || sy <= 0 || sz <= 0 || nIter < 0) return fail(ctx, MSBG_GPU_ERR_ARG, "relax_dense: bad sizes");
+  if (!dFlags || !dX || !dB || !dDiag || !dAreaX || !dAreaY || !dAreaZ || !dTmp || dTmp == dX)
+    return fail(ctx, MSBG_GPU_ERR_ARG, "relax_dense: null or aliased array");
+  const int64_t n = (int64_t)sx * sy * sz;
+  const float h = (float)(1 << levelMg);
+  float *src = dX, *dst = dTmp;
+  for (int it = 0; it < nIter; it++) {
+    MSBG_LAUNCH(ctx, kRelaxDense, (unsigned)((n + 255) / 256), 256, 0, sx, sy, sz, h, ctx->relaxOmega, dFlags, src, dB,
+                dDiag, dAreaX, dAreaY, dAreaZ, dst);
+    float *t = src;
+    src = dst;
+    dst = t;
+  }
+  // after an odd count the result is in the temporary array: the whole array goes to X
+  if (src != dX) MSBG_CUDA(ctx, cudaMemcpyAsync(dX, src, (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+  return MSBG_GPU_OK;
+}
 
 extern "C" int msbg_gpu_multiply_laplacian_dense(msbg_gpu_ctx *ctx, unsigned options, int levelMg, int sx, int sy,
                                                  int sz, const uint16_t *dFlags, const float *dX, const float *dB,

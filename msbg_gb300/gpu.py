@@ -117,6 +117,7 @@ SIGNATURES = {
     "msbg_gpu_multiply_laplacian_levels": (I, [P, C.c_uint, I, I, I, I, P, I64, P, C.POINTER(D), C.POINTER(I64)]),
     "msbg_gpu_relax_levels": (I, [P, I, I, I, I, P, I64, C.POINTER(I64)]),
     "msbg_gpu_multiply_laplacian_dense": (I, [P, C.c_uint, I, I, I, I, P, P, P, P, P, P, P, P]),
+    "msbg_gpu_relax_dense": (I, [P, I, I, I, I, I, P, P, P, P, P, P, P, P]),
     "msbg_gpu_level_flags_set": (I, [P, I, I, P, P, I64, C.c_uint16, C.c_uint16]),
     "msbg_gpu_fill_halo_blocks3": (I, [P, I, I, I, P, I64, P, P, C.POINTER(I64)]),
     "msbg_gpu_diag_wait_timeout": (I, [P, I]),
@@ -789,6 +790,28 @@ class MultiresSparseGrid:
             for u in bufs:
                 u.free()
         return y
+
+    # reference: relax() at a dense multigrid level (src/msbg3.cpp:1917-2165)
+    def relax_dense(self, level_mg: int, n_iter: int, flags, x, b, dinv, area_x, area_y, area_z,
+                    tmp=None) -> np.ndarray:
+        """Host arrays [sz][sy][sx] in (tmp: the temporary channel, zero by default), X after the
+        iterations out."""
+        fl = np.ascontiguousarray(flags, np.uint16)
+        sz, sy, sx = fl.shape
+        arrs = [np.ascontiguousarray(a, np.float32).reshape(fl.shape) for a in (x, b, dinv, area_x, area_y, area_z)]
+        t = np.ascontiguousarray(np.zeros(fl.shape) if tmp is None else tmp, np.float32).reshape(fl.shape)
+        bufs = [self.to_device(a) for a in [fl, *arrs, t]]
+        out = np.empty(fl.shape, np.float32)
+        try:
+            df, dx, db_, dd, da, dby, dc, dt = (C.c_void_p(u.ptr) for u in bufs)
+            self._check(self.L.msbg_gpu_relax_dense(self.h, level_mg, sx, sy, sz, n_iter, df, dx, db_, dd, da, dby,
+                                                    dc, dt))
+            self._check(self.L.msbg_gpu_copy_d2h(self.h, _ptr(out), dx, out.nbytes))
+            self.synchronize()
+        finally:
+            for u in bufs:
+                u.free()
+        return out
 
     # reference: relaxBlockList (src/msbg3.cpp:2170-2239) on a multi-resolution layout
     def relax_levels(self, lchan_x: int, lchan_b: int, lchan_d: int, bids: np.ndarray, reverse: bool = False) -> int:

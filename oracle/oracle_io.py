@@ -515,21 +515,22 @@ JOB_DENSE = 12
 
 
 def run_reference_dense(sx0, sy0, sz0, bsx, n_levels, flags, x, b, dinv, area_x, area_y, area_z,
-                        timeout: float = 600) -> dict:
+                        relax_iter: int = 0, timeout: float = 600) -> dict:
     """multiplyLaplacianMatrixOpt by the reference itself at the first dense multigrid level
     (levelMg = n_levels) of a grid sx0 x sy0 x sz0 with block edge bsx: the masked 7-point
     operator of ImultiplyLaplacianMatrixProcessSliceDenseLevel (src/msbg3.cpp:166-403).
     flags (cell flags, uint16) and the float32 arrays are [sz][sy][sx] of that level (x
     fastest); dinv is what CH_DIAGONAL holds, area_* the lower-face areas.  Returns
-    {"y": A X, "r": B - A X} in the same layout."""
+    {"y": A X, "r": B - A X} in the same layout, and with relax_iter > 0 "relaxed": X after
+    relax() with that many iterations at the level (omega-Jacobi, src/msbg3.cpp:1917-2165)."""
     fl = np.ascontiguousarray(flags, np.uint16)
     shape = fl.shape
     arrs = [np.ascontiguousarray(v, np.float32).reshape(shape) for v in (x, b, dinv, area_x, area_y, area_z)]
     n = fl.size
     with tempfile.TemporaryDirectory() as td:
         jp, op = os.path.join(td, "job.bin"), os.path.join(td, "out.bin")
-        hdr = struct.pack(_JOB_FMT, JOB_MAGIC, JOB_DENSE, sx0, sy0, sz0, bsx, n_levels, CHAN_F32, 0, 0, 0, 1,
-                          0.0, 0.0, 0.0, 0.0, 0, 0, n)
+        hdr = struct.pack(_JOB_FMT, JOB_MAGIC, JOB_DENSE, sx0, sy0, sz0, bsx, n_levels, CHAN_F32, relax_iter, 0, 0,
+                          1, 0.0, 0.0, 0.0, 0.0, 0, 0, n)
         with open(jp, "wb") as f:
             f.write(hdr)
             f.write(fl.astype(np.int32).tobytes())
@@ -547,4 +548,7 @@ def run_reference_dense(sx0, sy0, sz0, bsx, n_levels, flags, x, b, dinv, area_x,
         raise ValueError("bad oracle output or level size")
     y = np.frombuffer(buf, np.float32, n, hsz).copy().reshape(shape)
     res = np.frombuffer(buf, np.float32, n, hsz + 4 * n).copy().reshape(shape)
-    return {"y": y, "r": res}
+    out = {"y": y, "r": res}
+    if relax_iter > 0:
+        out["relaxed"] = np.frombuffer(buf, np.float32, n, hsz + 8 * n).copy().reshape(shape)
+    return out

@@ -753,3 +753,48 @@ def multiply_laplacian_dense(flags, x, b, dinv, area_x, area_y, area_z, h):
     y = np.where(active, Y, f32(0.0)).astype(f32)
     r = np.where(active, b - Y, f32(0.0)).astype(f32)
     return y, r
+
+
+def relax_dense(flags, x, b, dinv, area_x, area_y, area_z, h, iters, omega=REF_SM_OMEGA, tmp=None):
+    """relax() at a dense multigrid level (src/msbg3.cpp:2244-2310 -> 1917-2165): `iters`
+    omega-Jacobi iterations of the operator of multiply_laplacian_dense, alternating between x
+    and a temporary array (tmp, zero by default), the result copied to x after an odd count.
+    Per iteration the 4-cell groups of multiply_laplacian_dense decide skipping (a skipped
+    group's cells keep what the destination held) and weighting; fluid cells get
+    Y = omega h^-1 D (B + h S) + (1 - omega) F0, other cells of a processed group 0.  The
+    reference's build evaluates it as fma(1 - omega, F0, (B + h S) (D omega/h)) with S as in
+    the operator; so does this restatement, which matches it bit for bit.  Returns x after
+    the iterations."""
+    f32, f64 = np.float32, np.float64
+    fl = np.asarray(flags).astype(np.int64)
+    sz, sy, sx = fl.shape
+    x, b, dinv, ax, ay, az = (np.asarray(a, f32).reshape(fl.shape) for a in (x, b, dinv, area_x, area_y, area_z))
+    fluid = (fl & (CELL_SOLID | CELL_VOID)) == 0
+    part = (fl & (CELL_SOLID | CELL_PARTIAL_SOLID)) != 0
+    g = -(-sx // 4) * 4
+
+    def group_any(m):
+        mm = np.zeros((sz, sy, g), bool)
+        mm[:, :, :sx] = m
+        return np.repeat(mm.reshape(sz, sy, g // 4, 4).any(-1), 4, axis=-1)[:, :, :sx]
+
+    weighted, active = group_any(part), group_any(fluid)
+    AX, AY, AZ = np.pad(ax, 1), np.pad(ay, 1), np.pad(az, 1)
+    W = [ax, AX[1:-1, 1:-1, 2:], ay, AY[1:-1, 2:, 1:-1], az, AZ[2:, 1:-1, 1:-1]]
+    hh, om = f32(h), f32(omega)
+    om1 = f32(1.0) - om
+    dho = dinv * (om / hh)
+    src = x.copy()
+    dst = np.zeros_like(x) if tmp is None else np.asarray(tmp, f32).reshape(fl.shape).copy()
+    for _ in range(iters):
+        X = np.pad(src, 1)
+        F = [X[1:-1, 1:-1, :-2], X[1:-1, 1:-1, 2:], X[1:-1, :-2, 1:-1], X[1:-1, 2:, 1:-1], X[:-2, 1:-1, 1:-1],
+             X[2:, 1:-1, 1:-1]]
+        Fw = [np.where(weighted, Fi * Wi, Fi).astype(f32) for Fi, Wi in zip(F, W)]
+        S = ((Fw[0] + Fw[1]) + ((Fw[2] + Fw[3]) + (Fw[4] + Fw[5]))) * hh
+        t = b + S
+        Y = (om1.astype(f64) * src.astype(f64) + (t * dho).astype(f64)).astype(f32)
+        Y = np.where(fluid, Y, f32(0.0))
+        dst = np.where(active, Y, dst).astype(f32)
+        src, dst = dst, src
+    return src

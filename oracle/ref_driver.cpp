@@ -806,7 +806,9 @@ int runMultiresJob(const OracleJobHeader &job, const int32_t *levelsIn, const fl
 // each cell).  Every other cell of the dense arrays (the 2-cell border and the x padding)
 // is zero, so X and the face areas read 0 outside the box, except the cell flags, which hold
 // the flags grid's empty value CELL_EMPTY_VAL (void) there.  Output: Y = A X, then
-// R = B - A X, over the box.
+// R = B - A X, over the box; with job.nIter > 0 also X after relax() with job.nIter iterations
+// at that level (the dense levels' omega-Jacobi, src/msbg3.cpp:1917-2165, between X and a
+// temporary channel that starts at zero).
 int runDenseJob(const OracleJobHeader &job, const uint16_t *flagsIn, const float *arrays, FILE *fout) {
   OracleOutHeader out;
   memset(&out, 0, sizeof(out));
@@ -863,6 +865,17 @@ int runDenseJob(const OracleJobHeader &job, const uint16_t *flagsIn, const float
   fill(sgQ, (const float *)nullptr);
   msbg->multiplyLaplacianMatrixOpt(MSBG::OPT_CALC_RESIDUAL, L, CH_PRESSURE, CH_DIVERGENCE, 0.f, CH_CG_Q, NULL, NULL);
   dump(R);
+  std::vector<float> Xr;
+  if (job.nIter > 0) {
+    fill(sgX, X);
+    fill(sgQ, (const float *)nullptr);  // the temporary channel of the Jacobi iterations
+    msbg->relax(0, job.constr01, L, CH_PRESSURE, CH_DIVERGENCE, CH_CG_Q, job.nIter, 0);
+    const PSFloat *p = sgX->getDataPtrGen_(0, 0, 0, 1);
+    Xr.resize((size_t)n);
+    for (int z = 0; z < sz; z++)
+      for (int y = 0; y < sy; y++)
+        for (int x = 0; x < sx; x++) Xr[((int64_t)z * sy + y) * sx + x] = p[sgX->getGridIndex(x, y, z)];
+  }
   out.tPdeSec = nowSec() - t0;
   out.nBlocks = sx;
   out.nActive = sy;
@@ -872,6 +885,7 @@ int runDenseJob(const OracleJobHeader &job, const uint16_t *flagsIn, const float
   fwrite(&out, sizeof(out), 1, fout);
   fwrite(Y.data(), 4, (size_t)n, fout);
   fwrite(R.data(), 4, (size_t)n, fout);
+  if (!Xr.empty()) fwrite(Xr.data(), 4, (size_t)n, fout);
   MultiresSparseGrid::destroy(msbg);
   return 0;
 }

@@ -337,15 +337,19 @@ def make_multires() -> None:
 
 
 def make_dense() -> None:
-    """multiplyLaplacianMatrixOpt at the first dense multigrid level (oracle/ref_driver.cpp,
-    dense job): Y = A X and B - A X for the seeded cases of tests/halo_cases.py."""
+    """multiplyLaplacianMatrixOpt and relax() at the first dense multigrid level
+    (oracle/ref_driver.cpp, dense job): Y = A X, B - A X and X after the Jacobi iterations for
+    the seeded cases of tests/halo_cases.py."""
     import halo_cases as H
     out = {}
     for sx0, sy0, sz0, bsx, nl, seed in H.DENSE_CASES:
         key = f"{sx0}x{sy0}x{sz0}_L{nl}"
-        r = O.run_reference_dense(sx0, sy0, sz0, bsx, nl, *H.dense_case(sx0, sy0, sz0, nl, seed))
+        case = H.dense_case(sx0, sy0, sz0, nl, seed)
+        r = O.run_reference_dense(sx0, sy0, sz0, bsx, nl, *case)
         out[f"{key}_y"] = r["y"]
         out[f"{key}_r"] = r["r"]
+        for it in H.DENSE_RELAX_ITERS:
+            out[f"{key}_relaxed_{it}"] = O.run_reference_dense(sx0, sy0, sz0, bsx, nl, *case, relax_iter=it)["relaxed"]
     path = os.path.join(HERE, "reference_dense.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")

@@ -122,6 +122,9 @@ def multires_case(nb, bsx: int, n_levels: int, seed: int, regularize):
 DENSE_CASES = ((80, 96, 64, 16, 2, 20261203 + 1000), (80, 96, 64, 16, 3, 20261203 + 1001),
                (112, 48, 80, 16, 2, 20261203 + 1002))
 CELL_SOLID, CELL_PARTIAL_SOLID, CELL_VOID = 1 << 0, 1 << 6, 1 << 12
+# relax() iteration counts run at that level (odd: the result is copied back from the
+# temporary channel)
+DENSE_RELAX_ITERS = (1, 4)
 
 
 def dense_case(sx0, sy0, sz0, n_levels, seed):

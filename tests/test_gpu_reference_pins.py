@@ -332,3 +332,19 @@ def test_dense_level_operator_matches_reference(gpulib, case):
         assert not fluid[kept].any() and np.array_equal(y7[~kept].view(np.uint32), y[~kept].view(np.uint32))
     finally:
         g.close()
+
+
+@pytest.mark.parametrize("case", H.DENSE_CASES, ids=[f"{c[0]}x{c[1]}x{c[2]}_L{c[4]}" for c in H.DENSE_CASES])
+def test_dense_level_smoother_matches_reference(gpulib, case):
+    G = gpulib
+    gold = dict(np.load(os.path.join(GOLD, "reference_dense.npz")))
+    sx0, sy0, sz0, bsx, nl, seed = case
+    key = f"{sx0}x{sy0}x{sz0}_L{nl}"
+    flags, x, b, dinv, ax, ay, az = H.dense_case(sx0, sy0, sz0, nl, seed)
+    g = G.MultiresSparseGrid(sx0, sy0, sz0, bsx, nl, G.F32)
+    try:
+        for it in H.DENSE_RELAX_ITERS:
+            got = g.relax_dense(nl, it, flags, x, b, dinv, ax, ay, az)
+            assert np.array_equal(got.view(np.uint32), gold[f"{key}_relaxed_{it}"].view(np.uint32)), it
+    finally:
+        g.close()

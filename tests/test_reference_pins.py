@@ -219,3 +219,16 @@ def test_dense_level_operator_matches_reference(port, case):
     assert np.array_equal(y.view(np.uint32), gold[f"{key}_y"].view(np.uint32))
     assert np.array_equal(r.view(np.uint32), gold[f"{key}_r"].view(np.uint32))
     assert np.isinf(y).any() and (y == 0).mean() > 0.1  # zero diagonals and non-fluid cells occur
+
+
+@pytest.mark.parametrize("case", H.DENSE_CASES, ids=[f"{c[0]}x{c[1]}x{c[2]}_L{c[4]}" for c in H.DENSE_CASES])
+def test_dense_level_smoother_matches_reference(port, case):
+    """relax() at the first dense multigrid level (omega-Jacobi between X and a temporary
+    channel): the restatement equals the reference bit for bit after an odd and an even count."""
+    gold = dict(np.load(os.path.join(GOLD, "reference_dense.npz")))
+    sx0, sy0, sz0, bsx, nl, seed = case
+    key = f"{sx0}x{sy0}x{sz0}_L{nl}"
+    flags, x, b, dinv, ax, ay, az = H.dense_case(sx0, sy0, sz0, nl, seed)
+    for it in H.DENSE_RELAX_ITERS:
+        got = port.relax_dense(flags, x, b, dinv, ax, ay, az, 2 ** nl, it)
+        assert np.array_equal(got.view(np.uint32), gold[f"{key}_relaxed_{it}"].view(np.uint32)), it
