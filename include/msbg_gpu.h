@@ -226,6 +226,19 @@ int msbg_gpu_surface_job(msbg_gpu_ctx *ctx, const float *hPts, int64_t n, float 
                          float nbDist, const float *hBands, int nBands, int laplTyp, int numIter,
                          float timeStep, int variant, void *hOut, size_t hOutCap,
                          int64_t *nActiveOut);
+/* The streaming form of msbg_gpu_surface_job for a sequence of jobs on one context: the same
+ * arguments and result, queued.  The call returns after the job's last host read-back (the
+ * sweeps' status check): nActiveOut is known then and the points have been uploaded, so hPts
+ * may be reused; hOut is complete only after msbg_gpu_surface_job_wait.  This job's result comes
+ * down (through a device staging copy of the payload) while the next job's points go up and it
+ * computes, so a sequence runs at the rate of its compute.  The library's small read-backs go
+ * through pinned memory written by a kernel, so they do not wait behind the download on a copy
+ * engine.  hPts and hOut should be pinned (msbg_gpu_host_alloc). */
+int msbg_gpu_surface_job_submit(msbg_gpu_ctx *ctx, const float *hPts, int64_t n, float rParticle, float nbDist,
+                                const float *hBands, int nBands, int laplTyp, int numIter, float timeStep,
+                                int variant, void *hOut, size_t hOutCap, int64_t *nActiveOut);
+/* Waits for every submitted job, uploads and downloads included. */
+int msbg_gpu_surface_job_wait(msbg_gpu_ctx *ctx);
 /* Stream time (ms) of the stages of the last msbg_gpu_surface_job, from CUDA events at their
  * boundaries: points uploaded, layout built (levels, regularisation, refinement map, slab
  * fill), splat, finalize, sweeps, payload downloaded.  msOut receives min(cap, *nOut)

@@ -158,6 +158,19 @@ int exclusiveScanFlags(msbg_gpu_ctx *ctx, const int32_t *dIn, int64_t n, int64_t
   return exclusiveScanFlagsWith(ctx, dIn, n, dOut, dTotal, ctx->dScanPartial);
 }
 
+__global__ void kReadSmall(const uint32_t *__restrict__ src, int nWords, uint32_t *__restrict__ hDst) {
+  for (int i = threadIdx.x; i < nWords; i += blockDim.x) hDst[i] = src[i];
+}
+
+int readSmall(msbg_gpu_ctx *ctx, void *hDst, const void *dSrc, size_t bytes) {
+  if (bytes > kSmallReadBytes || (bytes & 3) || ((uintptr_t)dSrc & 3))
+    return fail(ctx, MSBG_GPU_ERR_ARG, "readSmall: %zu bytes", bytes);
+  if (bytes) MSBG_LAUNCH(ctx, kReadSmall, 1, 32, 0, (const uint32_t *)dSrc, (int)(bytes / 4), (uint32_t *)ctx->hSmall);
+  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (bytes) memcpy(hDst, ctx->hSmall, bytes);
+  return MSBG_GPU_OK;
+}
+
 int copyAsyncSplit(msbg_gpu_ctx *ctx, void *dst, const void *src, size_t bytes, cudaMemcpyKind kind) {
   constexpr size_t kSplitBytes = size_t(64) << 20;
   if (bytes < kSplitBytes) {
@@ -428,6 +441,7 @@ extern "C" int msbg_gpu_create(msbg_gpu_ctx **out, int sx, int sy, int sz, int b
   ALLOC(ctx->dStatus, 16);
 #undef ALLOC
   if (e == cudaSuccess) e = cudaMallocHost((void **)&ctx->hCounters, kNumCounters * 8);
+  if (e == cudaSuccess) e = cudaMallocHost((void **)&ctx->hSmall, kSmallReadBytes);
   if (e == cudaSuccess) {
     // per-call scratch (splat lists, list copies) comes from the device's
     // stream-ordered pool: keep what it has allocated for the next call instead of
@@ -464,6 +478,7 @@ extern "C" int msbg_gpu_destroy(msbg_gpu_ctx *ctx) {
   if (ctx->dListBids) cudaFree(ctx->dListBids);
   cudaFree(ctx->dScanPartial); cudaFree(ctx->dCounters); cudaFree(ctx->dStatus);
   if (ctx->hCounters) cudaFreeHost(ctx->hCounters);
+  if (ctx->hSmall) cudaFreeHost(ctx->hSmall);
   for (auto &c : ctx->ch) {
     if (c.d) cudaFree(c.d);
     if (c.cache) cudaFree(c.cache);
@@ -484,6 +499,19 @@ extern "C" int msbg_gpu_destroy(msbg_gpu_ctx *ctx) {
     cudaStreamDestroy(ctx->copyStream);
   }
   if (ctx->captureStream) cudaStreamDestroy(ctx->captureStream);
+  for (cudaStream_t st : {ctx->h2dStream, ctx->d2hStream})
+    if (st) {
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
+    }
+  for (int i = 0; i < 2; i++) {
+    if (ctx->dPtsQ[i]) cudaFree(ctx->dPtsQ[i]);
+    if (ctx->ptsQReady[i]) cudaEventDestroy(ctx->ptsQReady[i]);
+    if (ctx->ptsQFree[i]) cudaEventDestroy(ctx->ptsQFree[i]);
+  }
+  if (ctx->dStageOut) cudaFree(ctx->dStageOut);
+  if (ctx->stageOutReady) cudaEventDestroy(ctx->stageOutReady);
+  if (ctx->stageOutFree) cudaEventDestroy(ctx->stageOutFree);
   delete ctx;
   return MSBG_GPU_OK;
 }
@@ -614,8 +642,7 @@ extern "C" int msbg_gpu_set_refinement_map(msbg_gpu_ctx *ctx, double fillValue) 
   if (rc) return rc;
   MSBG_LAUNCH(ctx, kAssignSlots, gridFor(nB, 256), 256, 0, ctx->dLevels, dOff, nB, ctx->dSlot,
               ctx->dActive);
-  MSBG_CUDA(ctx, cudaMemcpyAsync(ctx->hCounters, dCnt, 16 * 8, cudaMemcpyDeviceToHost, ctx->stream));  // 0..15
-  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if ((rc = readSmall(ctx, ctx->hCounters, dCnt, 16 * 8))) return rc;  // 0..15
   const int64_t nAct = ctx->hCounters[2];
   for (int l = 0; l < 8; l++) ctx->blocksPerLevel[l] = ctx->hCounters[4 + l];
   ctx->nActParticles = ctx->hCounters[0];
@@ -636,9 +663,7 @@ extern "C" int msbg_gpu_set_refinement_map(msbg_gpu_ctx *ctx, double fillValue) 
       MSBG_LAUNCH(ctx, kColorScatter, gridFor(nAct, 256), 256, 0, ctx->dActive, dFlag, dOff, nAct, dColTot,
                   c, ctx->dColorBids);
     }
-    MSBG_CUDA(ctx, cudaMemcpyAsync(ctx->hCounters + kColorTot, dColTot, 8 * 8, cudaMemcpyDeviceToHost,
-                                   ctx->stream));
-    MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if ((rc = readSmall(ctx, ctx->hCounters + kColorTot, dColTot, 8 * 8))) return rc;
   }
   int32_t base = 0;
   for (int c = 0; c < 8; c++) {
@@ -884,6 +909,90 @@ extern "C" int msbg_gpu_surface_job(msbg_gpu_ctx *ctx, const float *hPts, int64_
   }
   if ((rc = stage())) return rc;
   MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return MSBG_GPU_OK;
+}
+
+// The streaming form: the same job, queued.  Job k's points go up on h2dStream into one of
+// two buffers (the upload waits for the splat of job k-2, the buffer's last reader); the
+// compute stream waits for them and runs the layout, splat, finalise and sweeps (the host
+// reads back the block count and the sweeps' status, so the call returns only when the
+// compute stream has got that far), then copies the result to a device staging buffer
+// (after the previous download has left it); d2hStream downloads it while the next job
+// computes.  Those read-backs go through readSmall, not a copy engine: a copy would queue
+// behind the previous job's download there and hold the next job's compute back by it.
+extern "C" int msbg_gpu_surface_job_submit(msbg_gpu_ctx *ctx, const float *hPts, int64_t n, float rParticle,
+                                           float nbDist, const float *hBands, int nBands, int laplTyp,
+                                           int numIter, float timeStep, int variant, void *hOut,
+                                           size_t hOutCap, int64_t *nActiveOut) {
+  if (!ctx || n < 0 || (n && !hPts)) return MSBG_GPU_ERR_ARG;
+  auto event = [&](cudaEvent_t &e) -> int {
+    if (!e) MSBG_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return MSBG_GPU_OK;
+  };
+  for (cudaStream_t *st : {&ctx->h2dStream, &ctx->d2hStream})
+    if (!*st) MSBG_CUDA(ctx, cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
+  const int q = (int)(ctx->jobSeq & 1);
+  int rc;
+  if ((rc = event(ctx->ptsQReady[q])) || (rc = event(ctx->ptsQFree[q])) || (rc = event(ctx->stageOutReady)) ||
+      (rc = event(ctx->stageOutFree)))
+    return rc;
+  if (ctx->ptsQCap[q] < n) {
+    MSBG_CUDA(ctx, cudaDeviceSynchronize());  // the buffer may still be read by an earlier job
+    if (ctx->dPtsQ[q]) MSBG_CUDA(ctx, cudaFree(ctx->dPtsQ[q]));
+    ctx->dPtsQ[q] = nullptr;
+    ctx->ptsQCap[q] = 0;
+    MSBG_CUDA(ctx, cudaMalloc(&ctx->dPtsQ[q], (size_t)(n ? n : 1) * 12));
+    ctx->ptsQCap[q] = n;
+  }
+  float *dPts = ctx->dPtsQ[q];
+  if (n) {
+    MSBG_CUDA(ctx, cudaStreamWaitEvent(ctx->h2dStream, ctx->ptsQFree[q], 0));
+    MSBG_CUDA(ctx, cudaMemcpyAsync(dPts, hPts, (size_t)n * 12, cudaMemcpyHostToDevice, ctx->h2dStream));
+  }
+  MSBG_CUDA(ctx, cudaEventRecord(ctx->ptsQReady[q], ctx->h2dStream));
+  MSBG_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ptsQReady[q], 0));
+  ctx->jobSeq++;
+  if (nBands > 0) {
+    rc = msbg_gpu_levels_from_bands(ctx, dPts, n, hBands, nBands);
+  } else {
+    rc = msbg_gpu_mark_points(ctx, dPts, n, rParticle + nbDist);
+    if (!rc) rc = msbg_gpu_levels_from_marks(ctx);
+  }
+  if (!rc) rc = msbg_gpu_regularize_refinement_map(ctx);
+  if (!rc) rc = msbg_gpu_set_refinement_map(ctx, 1.0);
+  if (!rc) rc = msbg_gpu_splat(ctx, dPts, n, rParticle, nbDist);
+  if (rc) return rc;
+  MSBG_CUDA(ctx, cudaEventRecord(ctx->ptsQFree[q], ctx->stream));
+  if ((rc = msbg_gpu_splat_finalize(ctx, rParticle, nbDist))) return rc;
+  if (numIter > 0 && (rc = pdeRun(ctx, 0, laplTyp, 1, numIter, timeStep, 0.0f, variant))) return rc;
+  if (nActiveOut) *nActiveOut = ctx->nActive;
+  if (hOut) {
+    const size_t bytes = (size_t)ctx->nActive * ctx->voxPerBlock * storageBytes(ctx->ch[0].storage);
+    if (bytes > hOutCap) return fail(ctx, MSBG_GPU_ERR_ARG, "output buffer too small (%zu < %zu)", hOutCap, bytes);
+    if (ctx->stageOutCap < bytes) {
+      MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->d2hStream));  // the last download reads it
+      if (ctx->dStageOut) MSBG_CUDA(ctx, cudaFree(ctx->dStageOut));
+      ctx->dStageOut = nullptr;
+      ctx->stageOutCap = 0;
+      MSBG_CUDA(ctx, cudaMalloc(&ctx->dStageOut, bytes));
+      ctx->stageOutCap = bytes;
+    }
+    MSBG_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->stageOutFree, 0));
+    if (bytes)
+      MSBG_CUDA(ctx, cudaMemcpyAsync(ctx->dStageOut, ctx->ch[0].d, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    MSBG_CUDA(ctx, cudaEventRecord(ctx->stageOutReady, ctx->stream));
+    MSBG_CUDA(ctx, cudaStreamWaitEvent(ctx->d2hStream, ctx->stageOutReady, 0));
+    if (bytes) MSBG_CUDA(ctx, cudaMemcpyAsync(hOut, ctx->dStageOut, bytes, cudaMemcpyDeviceToHost, ctx->d2hStream));
+    MSBG_CUDA(ctx, cudaEventRecord(ctx->stageOutFree, ctx->d2hStream));
+  }
+  return MSBG_GPU_OK;
+}
+
+extern "C" int msbg_gpu_surface_job_wait(msbg_gpu_ctx *ctx) {
+  if (!ctx) return MSBG_GPU_ERR_ARG;
+  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (ctx->h2dStream) MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->h2dStream));
+  if (ctx->d2hStream) MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->d2hStream));
   return MSBG_GPU_OK;
 }
 

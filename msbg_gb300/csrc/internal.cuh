@@ -63,6 +63,16 @@ struct msbg_gpu_ctx {
   cudaStream_t captureStream = nullptr;     // stream the sweeps' launch graphs are captured on
   cudaEvent_t copyEv[2] = {};               // fork / join of a split copy
   int stageCount = 0;            // events recorded by the last surface job
+  // msbg_gpu_surface_job_submit: points double-buffered and uploaded on h2dStream, the
+  // result staged on the device and downloaded on d2hStream while the next job computes
+  cudaStream_t h2dStream = nullptr, d2hStream = nullptr;
+  float *dPtsQ[2] = {};
+  int64_t ptsQCap[2] = {};
+  cudaEvent_t ptsQReady[2] = {}, ptsQFree[2] = {};
+  void *dStageOut = nullptr;
+  size_t stageOutCap = 0;
+  cudaEvent_t stageOutReady = nullptr, stageOutFree = nullptr;
+  int64_t jobSeq = 0;
 
   // layout (device)
   int32_t *dMark = nullptr;      // [nBlocks] 0/1 (demo's blockActive as a flag)
@@ -77,6 +87,7 @@ struct msbg_gpu_ctx {
   int64_t *dScanPartial = nullptr; // scan scratch
   int64_t *dCounters = nullptr;  // [kNumCounters], see kColorTot
   int64_t *hCounters = nullptr;  // pinned mirror
+  int64_t *hSmall = nullptr;     // pinned, kSmallReadBytes: target of readSmall
   int *dStatus = nullptr;        // device-side error bits (bounded waits that gave up)
   bool layoutValid = false;
   int64_t nActive = 0;
@@ -152,6 +163,13 @@ int exclusiveScanCounts(msbg_gpu_ctx *ctx, const int32_t *dIn, int64_t n, int64_
 // through a second stream, so two copy engines move it (ordered like one copy on
 // the context's stream).
 int copyAsyncSplit(msbg_gpu_ctx *ctx, void *dst, const void *src, size_t bytes, cudaMemcpyKind kind);
+
+// Read up to kSmallReadBytes (a multiple of 4) of device memory into host memory, ordered on
+// the context's stream, and wait for it.  A one-warp kernel stores the words into pinned
+// host memory, so the read does not queue on a copy engine behind a large download that
+// another stream has in flight (the streaming surface job's payload).
+constexpr size_t kSmallReadBytes = 256;
+int readSmall(msbg_gpu_ctx *ctx, void *hDst, const void *dSrc, size_t bytes);
 
 // Ensure the temp slab can hold `bytes`.
 int ensureTmpSlab(msbg_gpu_ctx *ctx, size_t bytes);

@@ -190,8 +190,7 @@ static int listedColourLists(msbg_gpu_ctx *ctx, const int32_t *dList, int64_t nL
     MSBG_LAUNCH(ctx, kListedStarts, 1, 32, 0, off, aux, nAct, dStarts, aux + 1);
   }
   int64_t h[11] = {};
-  MSBG_CUDA(ctx, cudaMemcpyAsync(h, aux, 11 * 8, cudaMemcpyDeviceToHost, ctx->stream));
-  MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if ((rc = readSmall(ctx, h, aux, 11 * 8))) return rc;
   if ((int32_t)h[10]) return fail(ctx, MSBG_GPU_ERR_ARG, "block list holds ids outside the block grid");
   for (int c = 0; c <= 8; c++) cs[c] = nAct > 0 ? (int)h[1 + c] : 0;
   return MSBG_GPU_OK;
@@ -245,8 +244,7 @@ int pdeRun(msbg_gpu_ctx *ctx, int chan, int laplTyp, int constr01, int numIter, 
     if (rc == 0) {
       // the streaming kernel's bounded shared-memory waits report through dStatus
       int st = 0;
-      MSBG_CUDA(ctx, cudaMemcpyAsync(&st, ctx->dStatus, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-      MSBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      if (const int r = readSmall(ctx, &st, ctx->dStatus, sizeof(int))) return r;
       if (st) {
         MSBG_CUDA(ctx, cudaMemsetAsync(ctx->dStatus, 0, sizeof(int), ctx->stream));
         return fail(ctx, MSBG_GPU_ERR_TIMEOUT, "a sweep CTA gave up waiting for its tile (status %d)", st);

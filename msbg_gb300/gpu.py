@@ -79,6 +79,8 @@ SIGNATURES = {
                                             I, I]),
     "msbg_gpu_surface_job": (I, [P, P, I64, F, F, P, I, I, I, F, I, P, SZ, C.POINTER(I64)]),
     "msbg_gpu_surface_job_stages": (I, [P, P, I, C.POINTER(I)]),
+    "msbg_gpu_surface_job_submit": (I, [P, P, I64, F, F, P, I, I, I, F, I, P, SZ, C.POINTER(I64)]),
+    "msbg_gpu_surface_job_wait": (I, [P]),
     "msbg_gpu_event_record": (I, [P, I]),
     "msbg_gpu_event_elapsed": (I, [P, I, I, C.POINTER(F)]),
     "msbg_gpu_launch_count": (I64, [P]),
@@ -476,6 +478,21 @@ class MultiresSparseGrid:
             self.h, _ptr(pts), len(pts), r_particle, nb_dist, _ptr(b), 0 if b is None else len(b),
             laplTyp, numIter, timeStep, variant, _ptr(out), cap, C.byref(n_act)))
         return n_act.value
+
+    def surface_job_submit(self, pts: np.ndarray, out: np.ndarray, r_particle=2.0, nb_dist=2.0, bands=None,
+                           laplTyp=LAPL_MCF_8COLOR, numIter=20, timeStep=0.1, variant=SWEEP_EXACT) -> int:
+        """The streaming form: queues the job (out is complete after surface_job_wait); returns
+        its value-block count.  pts may be reused when the call returns."""
+        pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 3)
+        b = None if bands is None else np.ascontiguousarray(bands, np.float32)
+        n_act = C.c_int64()
+        self._check(self.L.msbg_gpu_surface_job_submit(
+            self.h, _ptr(pts), len(pts), r_particle, nb_dist, _ptr(b), 0 if b is None else len(b),
+            laplTyp, numIter, timeStep, variant, _ptr(out), out.nbytes, C.byref(n_act)))
+        return n_act.value
+
+    def surface_job_wait(self):
+        self._check(self.L.msbg_gpu_surface_job_wait(self.h))
 
     # ---- Poisson solve (src/msbg3.cpp, src/msbg.cpp:4524-4872) --------------------------
     def poisson_set_coefficients(self, cx: int, cy: int, cz: int, diag: int):

@@ -208,6 +208,36 @@ def test_gpu_surface_job_entry_point(gpulib):
         g.close()
 
 
+def test_gpu_surface_job_streaming_equals_one_at_a_time(gpulib):
+    """msbg_gpu_surface_job_submit: a sequence of different jobs queued back to back (the next
+    job's upload and this job's download overlap the compute) gives every job the result of
+    msbg_gpu_surface_job, bit for bit, with FP16 and FP32 payloads."""
+    G = gpulib
+    res = 128
+    clouds = [W.sphere_cloud(res, k, 2500, seed=W.workload_seed(1, 30 + k)) for k in (3, 6, 4, 5)]
+    for storage, dt in ((G.F32, np.float32), (G.F16, np.float16)):
+        nb3 = (res // 16) ** 3
+        want = []
+        g = G.MultiresSparseGrid(res, res, res, 16, 3, storage)
+        try:
+            for pts in clouds:
+                out = np.zeros(nb3 * 4096, dt)
+                n = g.surface_job(pts, numIter=6, timeStep=0.1, out=out)
+                want.append((n, out.copy()))
+        finally:
+            g.close()
+        g = G.MultiresSparseGrid(res, res, res, 16, 3, storage)
+        try:
+            outs = [np.full(nb3 * 4096, 7, dt) for _ in clouds]
+            ns = [g.surface_job_submit(pts, out, numIter=6, timeStep=0.1) for pts, out in zip(clouds, outs)]
+            g.surface_job_wait()
+            for (n, w), m, out in zip(want, ns, outs):
+                assert m == n
+                assert np.array_equal(out[: n * 4096].view(np.uint8), w[: n * 4096].view(np.uint8))
+        finally:
+            g.close()
+
+
 def test_gpu_error_codes(gpulib):
     G = gpulib
     with pytest.raises(G.MsbgGpuError) as e:
