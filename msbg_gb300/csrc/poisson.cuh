@@ -88,6 +88,42 @@ __device__ __forceinline__ void stRow(__half *__restrict__ p, const float *v) {
   }
 }
 
+// N consecutive values of a row held in their storage form (FP16 stays packed two
+// per register) and widened to FP32 where the arithmetic reads them; a kernel
+// that keeps many rows live then needs half the registers for FP16 rows.
+template <typename V, int N> struct RawRow;
+template <int N> struct RawRow<float, N> {
+  float v[N];
+  __device__ __forceinline__ void ld(const float *__restrict__ p) { ldRow<N>(p, v); }
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int i = 0; i < N; i++) v[i] = 0.f;
+  }
+  __device__ __forceinline__ float operator[](int i) const { return v[i]; }
+};
+template <int N> struct RawRow<__half, N> {
+  static_assert(N == 4 || N == 8, "rows of 4 or 8 FP16 values");
+  uint32_t u[N / 2];
+  __device__ __forceinline__ void ld(const __half *__restrict__ p) {
+    if constexpr (N == 4) {
+      const uint2 w = *reinterpret_cast<const uint2 *>(p);
+      u[0] = w.x; u[1] = w.y;
+    } else {
+      const uint4 w = *reinterpret_cast<const uint4 *>(p);
+      u[0] = w.x; u[1] = w.y; u[2] = w.z; u[3] = w.w;
+    }
+  }
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int i = 0; i < N / 2; i++) u[i] = 0u;
+  }
+  __device__ __forceinline__ float operator[](int i) const {
+    const uint32_t w = u[i >> 1];
+    const __half2 h = *reinterpret_cast<const __half2 *>(&w);
+    return (i & 1) ? __high2float(h) : __low2float(h);
+  }
+};
+
 constexpr int kRedThreads = 256;
 
 // CTA-wide FP64 sum (blockDim.x == kRedThreads); every thread gets the total

@@ -24,6 +24,7 @@
 #include <cuda_fp16.h>
 
 #include <mutex>
+#include <type_traits>
 
 #include "internal.cuh"
 #include "poisson.cuh"
@@ -86,7 +87,7 @@ __device__ __forceinline__ int64_t parentOf(int64_t j, int L) {
 // z parity, y pair, z pair; so the 8 children of the coarse cells over a segment
 // pair are the 4 lanes {q, q^xq, q^2xq, q^3xq}.
 template <typename V, int MODE, int CPT = 4>
-__global__ void __launch_bounds__(256, CPT == 4 ? 3 : 2)
+__global__ void __launch_bounds__(256, CPT == 4 || sizeof(V) == 2 ? 3 : 2)
     kApplyRows(BlkGeom g, const V *__restrict__ x, const V *__restrict__ b, const V *__restrict__ cx,
                const V *__restrict__ cy, const V *__restrict__ cz, const V *__restrict__ d, V *__restrict__ y,
                double *__restrict__ dotPartial, V *__restrict__ bc, V *__restrict__ xc,
@@ -113,12 +114,12 @@ __global__ void __launch_bounds__(256, CPT == 4 ? 3 : 2)
     const int64_t base = (int64_t)s << (3 * L);
     const int64_t c = base + ((int64_t)((lz << L) + ly) << L) + lx;
 
-    float xv[CPT], dv[CPT], cxv[CPT], cyv[CPT], czv[CPT], ym[CPT], yq[CPT], zm[CPT], zq[CPT], cyu[CPT], czu[CPT];
-    ldRow<CPT>(x + c, xv);
-    ldRow<CPT>(d + c, dv);
-    ldRow<CPT>(cx + c, cxv);
-    ldRow<CPT>(cy + c, cyv);
-    ldRow<CPT>(cz + c, czv);
+    RawRow<V, CPT> xv, dv, cxv, cyv, czv, ym, yq, zm, zq, cyu, czu;
+    xv.ld(x + c);
+    dv.ld(d + c);
+    cxv.ld(cx + c);
+    cyv.ld(cy + c);
+    czv.ld(cz + c);
     float xl = 0.f, xr = 0.f, cxr = 0.f;
     {
       const int64_t j = lx > 0 ? c - 1 : cellAt(g, s, lx - 1, ly, lz);
@@ -128,17 +129,17 @@ __global__ void __launch_bounds__(256, CPT == 4 ? 3 : 2)
     }
     {
       const int64_t j = ly > 0 ? c - sy : cellAt(g, s, lx, ly - 1, lz);
-      if (j >= 0) ldRow<CPT>(x + j, ym); else for (int i = 0; i < CPT; i++) ym[i] = 0.f;
+      if (j >= 0) ym.ld(x + j); else ym.zero();
       const int64_t k = ly + 1 < bs ? c + sy : cellAt(g, s, lx, ly + 1, lz);
-      if (k >= 0) { ldRow<CPT>(x + k, yq); ldRow<CPT>(cy + k, cyu); }
-      else for (int i = 0; i < CPT; i++) yq[i] = cyu[i] = 0.f;
+      if (k >= 0) { yq.ld(x + k); cyu.ld(cy + k); }
+      else { yq.zero(); cyu.zero(); }
     }
     {
       const int64_t j = lz > 0 ? c - sz : cellAt(g, s, lx, ly, lz - 1);
-      if (j >= 0) ldRow<CPT>(x + j, zm); else for (int i = 0; i < CPT; i++) zm[i] = 0.f;
+      if (j >= 0) zm.ld(x + j); else zm.zero();
       const int64_t k = lz + 1 < bs ? c + sz : cellAt(g, s, lx, ly, lz + 1);
-      if (k >= 0) { ldRow<CPT>(x + k, zq); ldRow<CPT>(cz + k, czu); }
-      else for (int i = 0; i < CPT; i++) zq[i] = czu[i] = 0.f;
+      if (k >= 0) { zq.ld(x + k); czu.ld(cz + k); }
+      else { zq.zero(); czu.zero(); }
     }
     float r[CPT];
     if constexpr (MODE == 2) {
@@ -293,7 +294,7 @@ struct TileSmem {
   using Sh = TileShape<BS>;
   static constexpr int TX = Sh::TX, TY = Sh::TY, TZ = Sh::TZ;
   static constexpr int E = (int)sizeof(V);
-  static constexpr bool H = E != 4;  // FP16 storage: FP32 working copies of cx, cy
+  static constexpr bool H = E != 4;  // FP16 storage: cx, cy read from the staged boxes
   static constexpr int C3 = TX * TY * TZ, CY2 = TX * TZ, CZ2 = TX * TY, CX2 = TY * TZ;
   static constexpr int al(int b) { return (b + 127) & ~127; }
   // FP32 x of the tile with its x and y halo: [TZ][TY + 2][TX + 2], cell (x, y, z)
@@ -311,17 +312,14 @@ struct TileSmem {
   static constexpr int XZHI = XZLO + al(CZ2 * E);
   static constexpr int CYHI = XZHI + al(CZ2 * E);   // cy at y = TY ([z][x], V)
   static constexpr int CZHI = CYHI + al(CY2 * E);   // cz at z = TZ ([y][x], V)
-  static constexpr int CXHI = CZHI + al(CZ2 * E);   // cx at x = TX ([z][y], float)
+  static constexpr int CXHI = CZHI + al(CZ2 * E);   // cx at x = TX ([z][y], float; V on FP16 storage)
   static constexpr int END0 = CXHI + al(CX2 * 4);
   // the padded x array: over the x/b/d/cz boxes once they sit in registers when
   // it fits there (FP32), else after everything
   static constexpr bool XS_OVER = XSB <= CX;
   static constexpr int XS = XS_OVER ? 0 : END0;
   static constexpr int END1 = XS_OVER ? END0 : END0 + XSB;
-  static constexpr int WCX = END1;                  // FP16 storage: FP32 cx, cy, cy face
-  static constexpr int WCY = WCX + (H ? al(C3 * 4) : 0);
-  static constexpr int WCYHI = WCY + (H ? al(C3 * 4) : 0);
-  static constexpr int BYTES = WCYHI + (H ? al(CY2 * 4) : 0);
+  static constexpr int BYTES = END1;
 };
 template <int BS>
 constexpr int tileThreads() {
@@ -348,6 +346,33 @@ __device__ __forceinline__ void colStep(float *xr, const float *bb, const float 
     acc += pcxu[z * scxu] * q[1];
     acc += cys[z * TXY] * q[-XRS];
     acc += pcyu[z * scyu] * q[XRS];
+    acc += czr[z] * xr[z];
+    acc += czr[z + 1] * xr[z + 2];
+    const float v = acc * rd[z];
+    xr[z + 1] = v;
+    q[0] = v;
+  }
+}
+
+// The same half step on FP16 storage.  The column's own lower-face coefficients
+// (cx, cy of cell z) sit in registers as one packed FP16 pair per cell; the upper
+// ones (the x+1 / y+1 neighbour's cx / cy) are read from the staged FP16 boxes
+// (pointer, stride per z).  FP16 to FP32 is exact, so the sums are those of the
+// FP32-copy form, in the same order.
+template <int TZ, int TXY, int XRS, int XPS, int P>
+__device__ __forceinline__ void colStepH(float *xr, const float *bb, const float *rd, const float *czr, float *xp,
+                                         const uint32_t *cpk, const __half *pcxu, int scxu, const __half *pcyu,
+                                         int scyu) {
+#pragma unroll
+  for (int z = P; z < TZ; z += 2) {
+    float *q = xp + z * XPS;
+    const uint32_t w = cpk[z];
+    const float2 c = __half22float2(*reinterpret_cast<const __half2 *>(&w));
+    float acc = bb[z];
+    acc += c.x * q[-1];
+    acc += __half2float(pcxu[z * scxu]) * q[1];
+    acc += c.y * q[-XRS];
+    acc += __half2float(pcyu[z * scyu]) * q[XRS];
     acc += czr[z] * xr[z];
     acc += czr[z + 1] * xr[z + 2];
     const float v = acc * rd[z];
@@ -440,7 +465,8 @@ __global__ void __launch_bounds__(tileThreads<BS>(), 2)
   // plain loads (face cell (y, z) = (q % TY, q / TY)), coarse corrections
   constexpr int NXF = (S::CX2 + TXY - 1) / TXY;
   float xlo[NXF], xhi[NXF];
-  float *cxhi = reinterpret_cast<float *>(tb + S::CXHI);
+  using CxT = std::conditional_t<S::H, V, float>;
+  CxT *cxhi = reinterpret_cast<CxT *>(tb + S::CXHI);
 #pragma unroll
   for (int i = 0; i < NXF; i++) {
     const int q = r + i * TXY;
@@ -449,10 +475,10 @@ __global__ void __launch_bounds__(tileThreads<BS>(), 2)
       const int j = q % TY, kk = q / TY;
       const int64_t lo = cellAt(g, s, ox - 1, oy + j, oz + kk);
       const int64_t hi = cellAt(g, s, ox + TX, oy + j, oz + kk);
-      float chi = 0.f;
+      CxT chi = CxT(0.f);
       if (lo >= 0 && !haloZero) xlo[i] = ldv(x + lo) + (haloCorr ? ldv(xc + parentOf(lo, L)) : 0.f);
       if (hi >= 0) {
-        chi = ldv(cxg + hi);
+        if constexpr (S::H) chi = cxg[hi]; else chi = ldv(cxg + hi);
         if (!haloZero) xhi[i] = ldv(x + hi) + (haloCorr ? ldv(xc + parentOf(hi, L)) : 0.f);
       }
       cxhi[q] = chi;
@@ -528,21 +554,13 @@ __global__ void __launch_bounds__(tileThreads<BS>(), 2)
       }
     }
   }
-  float *cxw, *cyw, *cyhw;
-  if constexpr (!S::H) {
-    cxw = reinterpret_cast<float *>(tb + S::CX); cyw = reinterpret_cast<float *>(tb + S::CY);
-    cyhw = reinterpret_cast<float *>(tb + S::CYHI);
-  } else {
-    cxw = reinterpret_cast<float *>(tb + S::WCX); cyw = reinterpret_cast<float *>(tb + S::WCY);
-    cyhw = reinterpret_cast<float *>(tb + S::WCYHI);
-    const V *scx = reinterpret_cast<const V *>(tb + S::CX), *scy = reinterpret_cast<const V *>(tb + S::CY);
-    const V *fcy = reinterpret_cast<const V *>(tb + S::CYHI);
+  // FP16 storage: the column's own (cx, cy) pairs into registers
+  uint32_t cpk[S::H ? TZ : 1];
+  if constexpr (S::H) {
+    const uint16_t *scx = reinterpret_cast<const uint16_t *>(tb + S::CX);
+    const uint16_t *scy = reinterpret_cast<const uint16_t *>(tb + S::CY);
 #pragma unroll
-    for (int z = 0; z < TZ; z++) {
-      cxw[own + z * TXY] = ldv(scx + own + z * TXY);
-      cyw[own + z * TXY] = ldv(scy + own + z * TXY);
-    }
-    for (int q = r; q < S::CY2; q += TXY) cyhw[q] = ldv(fcy + q);
+    for (int z = 0; z < TZ; z++) cpk[z] = (uint32_t)scx[own + z * TXY] | ((uint32_t)scy[own + z * TXY] << 16);
   }
   if (S::XS_OVER) __syncthreads();  // the boxes under the padded array are read
   float *xs = reinterpret_cast<float *>(tb + S::XS);
@@ -569,19 +587,28 @@ __global__ void __launch_bounds__(tileThreads<BS>(), 2)
   }
   __syncthreads();
   // upper-face coefficients inside the tile or on a face (pointer, stride per z)
-  const float *cxs = cxw + own, *cys = cyw + own;
-  const float *pcxu = tx < TX - 1 ? cxs + 1 : cxhi + ty;
+  using CT = std::conditional_t<S::H, V, float>;  // type of the staged cx, cy boxes and faces
+  const CT *cxs = reinterpret_cast<const CT *>(tb + S::CX) + own;
+  const CT *cys = reinterpret_cast<const CT *>(tb + S::CY) + own;
+  const CT *pcxu = tx < TX - 1 ? cxs + 1 : cxhi + ty;
   const int scxu = tx < TX - 1 ? TXY : TY;
-  const float *pcyu = ty < TY - 1 ? cys + TX : cyhw + tx;
+  const CT *pcyu = ty < TY - 1 ? cys + TX : reinterpret_cast<const CT *>(tb + S::CYHI) + tx;
   const int scyu = ty < TY - 1 ? TXY : TX;
   for (int it = 0; it < k; it++) {
     for (int ci = 0; ci < 2; ci++) {
       const int cc = reverse ? 1 - ci : ci;
       if (valid) {  // cells z with (tx + ty + z) & 1 == cc: z = ((cc - P) & 1) + 2m
-        if (((cc - P) & 1) == 0)
-          colStep<TZ, TXY, S::XRS, S::XPS, 0>(xr, bb, rd, czr, xp, cxs, pcxu, scxu, cys, pcyu, scyu);
-        else
-          colStep<TZ, TXY, S::XRS, S::XPS, 1>(xr, bb, rd, czr, xp, cxs, pcxu, scxu, cys, pcyu, scyu);
+        if constexpr (S::H) {
+          if (((cc - P) & 1) == 0)
+            colStepH<TZ, TXY, S::XRS, S::XPS, 0>(xr, bb, rd, czr, xp, cpk, pcxu, scxu, pcyu, scyu);
+          else
+            colStepH<TZ, TXY, S::XRS, S::XPS, 1>(xr, bb, rd, czr, xp, cpk, pcxu, scxu, pcyu, scyu);
+        } else {
+          if (((cc - P) & 1) == 0)
+            colStep<TZ, TXY, S::XRS, S::XPS, 0>(xr, bb, rd, czr, xp, cxs, pcxu, scxu, cys, pcyu, scyu);
+          else
+            colStep<TZ, TXY, S::XRS, S::XPS, 1>(xr, bb, rd, czr, xp, cxs, pcxu, scxu, cys, pcyu, scyu);
+        }
       }
       __syncthreads();
     }
