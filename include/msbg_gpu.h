@@ -312,7 +312,9 @@ int msbg_gpu_relax_dense(msbg_gpu_ctx *ctx, int levelMg, int sx, int sy, int sz,
  * The reference relaxes its member list _blocksRelax[levelMg], which nothing in the
  * release fills; dBlockList stands in for it.  With options MSBG_GPU_RELAX_TILES the call
  * runs the multigrid's own smoother instead (red-black over tiles with in-tile red-black
- * Gauss-Seidel, all value blocks, no list; reverseOrder = the adjoint order).  levelMg must
+ * Gauss-Seidel, all value blocks, no list; reverseOrder = the adjoint order); when chanX and
+ * chanB are both FP16 channels it runs the mixed solve's FP16-storage form of that smoother
+ * (FP32 arithmetic, the coefficients rounded to FP16 once).  levelMg must
  * be 0; boundaryZoneOnly != 0 is MSBG_GPU_ERR_UNSUPPORTED; chanTmp is unused, as in the
  * reference's in-place block order. */
 #define MSBG_GPU_RELAX_TILES (1u << 31) /* a bit the reference's option enum leaves unused */

@@ -985,9 +985,21 @@ extern "C" int msbg_gpu_relax(msbg_gpu_ctx *ctx, int boundaryZoneOnly, int rever
   int rc = needLevel0(ctx, levelMg);
   if (rc) return rc;
   if ((rc = needCoeffs(ctx))) return rc;
+  PoissonState *ps = ctx->poisson;
+  if ((options & MSBG_GPU_RELAX_TILES) && chanX >= 0 && chanX < kMaxChannels && chanB >= 0 &&
+      chanB < kMaxChannels && ctx->ch[chanX].exists && ctx->ch[chanB].exists &&
+      ctx->ch[chanX].storage == MSBG_GPU_F16 && ctx->ch[chanB].storage == MSBG_GPU_F16) {
+    // FP16 channels: the mixed solve's FP16-storage smoother on the FP16 copies of
+    // the coefficients
+    if (dBlockList) return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "the tile smoother relaxes all value blocks");
+    if ((rc = ensureHalf(ctx, ps))) return rc;
+    if ((rc = smoothLevel<__half>(ctx, ps, ps->f16, 0, (__half *)ctx->ch[chanX].d, (const __half *)ctx->ch[chanB].d,
+                                  nIter, reverseOrder != 0, kFirstNone, nullptr)))
+      return rc;
+    return checkStatus(ctx);
+  }
   float *x, *b;
   if ((rc = chanF32(ctx, chanX, &x)) || (rc = chanF32(ctx, chanB, &b))) return rc;
-  PoissonState *ps = ctx->poisson;
   if (options & MSBG_GPU_RELAX_TILES) {
     if (dBlockList) return fail(ctx, MSBG_GPU_ERR_UNSUPPORTED, "the tile smoother relaxes all value blocks");
     if ((rc = smoothLevel<float>(ctx, ps, ps->f32, 0, x, b, nIter, reverseOrder != 0, kFirstNone, nullptr)))

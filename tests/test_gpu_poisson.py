@@ -280,3 +280,23 @@ def test_launch_shape_autotuner(gpulib):
         assert rel_l2(x1, x0) < 1e-5
     finally:
         g.close()
+
+
+@pytest.mark.parametrize("reverse", [False, True])
+def test_relax_tiles_fp16_storage(setup, reverse):
+    """The mixed solve's FP16-storage tile smoother (FP16 x, b and coefficients, FP32
+    arithmetic) against the FP64 restatement on the same inputs: within the FP16
+    rounding of the stored values (unit roundoff 4.9e-4)."""
+    G, P, g, prob = setup
+    rng = np.random.default_rng(12)
+    x = _rand(prob, rng).astype(np.float16).astype(np.float64)
+    b = _rand(prob, rng).astype(np.float16).astype(np.float64)
+    chx, chb = 10, 11
+    g.channel_create(chx, G.F16)
+    g.channel_create(chb, G.F16)
+    g.upload_payload(prob.payload(x).astype(np.float16), chx)
+    g.upload_payload(prob.payload(b).astype(np.float16), chb)
+    g.relax_tiles(chx, chb, 2, reverseOrder=reverse)
+    got = prob.dense(g.payload(chx).astype(np.float64))
+    want = prob.smooth(x, b, 2, reverse=reverse)
+    assert rel_l2(got, want) < 2e-3
