@@ -610,7 +610,8 @@ __global__ void __launch_bounds__(tileThreads<BS>(), 2)
             colStep<TZ, TXY, S::XRS, S::XPS, 1>(xr, bb, rd, czr, xp, cxs, pcxu, scxu, cys, pcyu, scyu);
         }
       }
-      __syncthreads();
+      // the write-back reads registers only: no barrier after the last half step
+      if (ci == 0 || it + 1 < k) __syncthreads();
     }
   }
   if (valid) {

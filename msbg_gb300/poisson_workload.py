@@ -82,11 +82,15 @@ def load_warmnet(path: str):
     return [z[f"W{l}"] for l in range(4)], [z[f"c{l}"] for l in range(4)]
 
 
-def timed_solve(g, kind: str, tol: float = 1e-6, max_iter: int = 200, inner_tol: float = 3e-3,
+def timed_solve(g, kind: str, tol: float = 1e-6, max_iter: int = 200, inner_tol: float = 3e-2,
                 max_outer: int = 12, max_inner: int = 60) -> dict:
     """One solve, timed with CUDA events on the context's stream: from X = 0
     ("plain", "mixed") or from the learned warm start ("learned", "learned_mixed";
-    the network's forward pass is inside the timed region)."""
+    the network's forward pass is inside the timed region).  The mixed solves stop
+    each FP16 inner solve at a relative residual of inner_tol (3e-2: four outer
+    steps of about two inner iterations; on the 4096^3 layout 1.45 s against 1.59 s
+    with 3e-3 and 1.81 s with 1e-2); the outer loop still stops on the FP64-checked
+    residual of the FP32 system."""
     g.synchronize()
     l0 = g.launch_count()
     if kind.startswith("learned"):
